@@ -1,0 +1,756 @@
+"""CPU oracle for the Wannier-interpolation hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is a plain numpy restatement of the
+reference (wannier-berri) algorithm for the path R-space matrices -> k-space
+fields -> eigh -> U^dagger X U -> Berry-curvature / orbital-moment / dipole
+formulas -> Fermi-level scan, plus the Kubo optical-conductivity band sums and
+the MDRS (use_ws_distance) replica construction.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference arm may
+import it, and only as the checker or the timed CPU baseline.  The GPU product
+never calls into this file.
+
+Parity pin: every routine is checked in ``tests/test_oracle_golden.py`` against
+the reference's own golden files (``tests/reference/integrate_files/random-*``,
+``tests/reference/formula/*``) and against outputs of the reference itself,
+committed as fixtures under ``tests/golden/`` by ``tests/golden/make_golden.py``.
+
+Every function names the reference file:line it follows (paths are relative to
+the reference project root).  Loop structure follows the reference (per k-point,
+per band group) so that timing this module is representative of the reference
+CPU path.
+"""
+from math import ceil
+
+import numpy as np
+
+# wannierberri/utility.py:45-46 -- cyclic index pairs used for cross products
+ALPHA = np.array([1, 2, 0])
+BETA = np.array([2, 0, 1])
+
+# wannierberri/factors.py:1-26 (scipy.constants, CODATA values as shipped by scipy)
+from scipy.constants import elementary_charge, hbar, physical_constants, angstrom
+
+BOHR = physical_constants['Bohr radius'][0] / angstrom
+EV_AU = physical_constants['electron volt-hartree relationship'][0]
+FACTOR_AHC = -(elementary_charge ** 2 / hbar / angstrom)      # factors.py:25
+FACTOR_OPT = -FACTOR_AHC                                       # factors.py:36
+FACTOR_MORB = -EV_AU / BOHR ** 2                               # calculators/static.py:237
+
+
+# ---------------------------------------------------------------------------
+# System container (system/system_R.py, fourier/rvectors.py)
+# ---------------------------------------------------------------------------
+class RSystem:
+    """Real-space tight-binding data: lattice, R-vectors, Wannier centres, XX_R.
+
+    Mirrors the pieces of ``System_R`` (system/system_R.py:18-212) and
+    ``Rvectors`` (fourier/rvectors.py:11-506) that the hot path reads.
+    ``XX_R[key]`` has shape (nR, nw, nw, 3...) like ``System_R._XX_R``.
+    """
+
+    def __init__(self, real_lattice, iRvec, wannier_centers_cart, XX_R, force_internal_terms_only=False):
+        self.real_lattice = np.array(real_lattice, dtype=float)
+        self.iRvec = np.array(iRvec, dtype=int)
+        self.num_wann = XX_R['Ham'].shape[1]
+        if wannier_centers_cart is None:
+            wannier_centers_cart = np.zeros((self.num_wann, 3))
+        self.wannier_centers_cart = np.array(wannier_centers_cart, dtype=float)
+        self.XX_R = dict(XX_R)
+        self.force_internal_terms_only = force_internal_terms_only
+
+    @property
+    def cell_volume(self):  # system/system.py:174-181
+        return abs(np.linalg.det(self.real_lattice))
+
+    @property
+    def wannier_centers_red(self):  # system/system_R.py:609-610
+        return self.wannier_centers_cart.dot(np.linalg.inv(self.real_lattice))
+
+    @property
+    def nRvec(self):
+        return self.iRvec.shape[0]
+
+    def cRvec(self):  # fourier/rvectors.py:350-352
+        return self.iRvec.dot(self.real_lattice)
+
+    def shifts_diff_cart(self):
+        """t_n - t_m for every (m, n): fourier/rvectors.py:362-368 (left = right = wcc)."""
+        t = self.wannier_centers_cart
+        return -t[:, None, :] + t[None, :, :]
+
+    def cRvec_shifted(self):  # fourier/rvectors.py:354-360
+        return self.cRvec()[:, None, None, :] + self.shifts_diff_cart()[None, :, :, :]
+
+    def conj_XX_R(self, XX_R):
+        """X(R) -> X(-R)^dagger, fourier/rvectors.py:372-430 (reverseR + conj_XX_R)."""
+        index = {tuple(R): i for i, R in enumerate(self.iRvec)}
+        res = np.zeros(XX_R.shape, dtype=complex)
+        for i, R in enumerate(self.iRvec):
+            j = index.get(tuple(-R))
+            if j is not None:
+                res[i] = XX_R[j]
+        return res.swapaxes(1, 2).conj()
+
+    def set_R_mat(self, key, value, Hermitian=False):
+        """system/system_R.py:117-175 (full-matrix branch only)."""
+        if Hermitian:
+            value = 0.5 * (value + self.conj_XX_R(value))
+        self.XX_R[key] = value
+
+
+def iterate_nd(size, pm=False):
+    """utility.py:103-115: all integer points of [0,size) (or [-size,size] with pm), C order."""
+    axes = [np.arange(-s, s + 1) if pm else np.arange(s) for s in size]
+    g = np.meshgrid(*axes, indexing='ij')
+    return np.stack([x.reshape(-1) for x in g], axis=1)
+
+
+def wigner_seitz(real_lattice, mp_grid, shift_reduced, tolerance=1e-5, ws_search_size=3):
+    """fourier/rvectors.py:570-609: WS replicas of every mp-grid point for one centre shift.
+
+    Returns (iRvec, Ndegen, iRvec % mp_grid) like ``WignerSeitz.__call__``.
+    """
+    mp_grid = np.array(mp_grid)
+    iRvec0 = iterate_nd(mp_grid)
+    super_i = iterate_nd([ws_search_size] * 3, pm=True) * mp_grid[None, :]
+    iR_search = iRvec0[:, None, :] + super_i[None, :, :]          # (npt, nsuper, 3)
+    cR_search = iR_search.dot(real_lattice)
+    shift_cart = np.asarray(shift_reduced).dot(real_lattice)
+    dist = np.linalg.norm(cR_search + shift_cart, axis=2)
+    iRvec, Ndegen = [], []
+    for i in range(iR_search.shape[0]):
+        dmin = dist[i].min()
+        sel = np.where(abs(dist[i] - dmin) < tolerance)[0]
+        for j in sel:
+            iRvec.append(iR_search[i, j])
+            Ndegen.append(len(sel))
+    iRvec = np.array(iRvec)
+    return iRvec, np.array(Ndegen), iRvec % mp_grid
+
+
+def do_ws_dist(system, mp_grid, ws_dist_tol=1e-5):
+    """MDRS: system/system_R.py:572-588 with fourier/rvectors.py:57-99,126-227.
+
+    Returns a new RSystem whose (iRvec, XX_R) carry the Wigner-Seitz replicas
+    with 1/N_degen weights, all-zero R-vectors dropped (rvectors.py:111-123).
+    """
+    mp_grid = np.array(mp_grid, dtype=int)
+    wcc_red = system.wannier_centers_red
+    num_digits = int(np.ceil(-np.log10(ws_dist_tol))) + 1
+    nw = system.num_wann
+    shifts = np.round(-wcc_red[:, None] + wcc_red[None, :], num_digits).reshape(-1, 3)
+    all_shifts, shift_index = np.unique(shifts, axis=0, return_inverse=True)
+    shift_index = shift_index.reshape(nw, nw)
+    iRvec_list, Ndegen_list, iRmod_list = [], [], []
+    for s in all_shifts:
+        a, b, c = wigner_seitz(system.real_lattice, mp_grid, s, tolerance=ws_dist_tol)
+        iRvec_list.append(a)
+        Ndegen_list.append(b)
+        iRmod_list.append(c)
+    iRvec_new = np.array(sorted(set(tuple(R) for R in np.concatenate(iRvec_list))), dtype=int)
+    index = {tuple(R): i for i, R in enumerate(iRvec_new)}
+    nRnew = len(iRvec_new)
+    remap = np.zeros((nRnew, nw, nw, 3), dtype=int)
+    weights = np.zeros((nRnew, nw, nw))
+    for ia in range(nw):
+        for ib in range(nw):
+            ish = shift_index[ia, ib]
+            for R, Rm, nd in zip(iRvec_list[ish], iRmod_list[ish], Ndegen_list[ish]):
+                iR = index[tuple(R)]
+                remap[iR, ia, ib] = Rm
+                weights[iR, ia, ib] += 1.0 / nd
+    assert np.isclose(weights.sum(), np.prod(mp_grid) * nw * nw)
+    new_XX = {}
+    for key, val in system.XX_R.items():
+        grid = np.zeros(tuple(mp_grid) + val.shape[1:], dtype=complex)   # rvectors.py:126-141
+        for i, R in enumerate(system.iRvec % mp_grid):
+            grid[tuple(R)] += val[i]
+        out = np.zeros((nRnew,) + val.shape[1:], dtype=complex)
+        wshape = (nRnew,) + (1,) * (val.ndim - 3)
+        for a in range(nw):
+            for b in range(nw):
+                out[:, a, b] = grid[remap[:, a, b, 0], remap[:, a, b, 1], remap[:, a, b, 2], a, b]
+                out[:, a, b] *= weights[:, a, b].reshape(wshape)
+        new_XX[key] = out
+    # exclude_zeros: rvectors.py:111-123
+    keep = np.zeros(nRnew, dtype=bool)
+    for iR in range(nRnew):
+        keep[iR] = any(np.any(np.abs(X[iR]) > 1e-8) for X in new_XX.values())
+    new_XX = {k: v[keep] for k, v in new_XX.items()}
+    return RSystem(system.real_lattice, iRvec_new[keep], system.wannier_centers_cart, new_XX,
+                   system.force_internal_terms_only)
+
+
+# ---------------------------------------------------------------------------
+# R -> k transform (fourier/fft.py:133-192, fourier/rvectors.py:443-506)
+# ---------------------------------------------------------------------------
+def fft_R_to_k(XX_R, iRvec, NKFFT, hermitian=False):
+    """Scatter X_R onto the FFT grid at R mod N (aliases add), inverse FFT times
+    prod(N) == sum_R exp(+2 pi i j.R/N) X_R, optional 1/2(X + X^dagger), C-order k."""
+    NKFFT = tuple(int(n) for n in NKFFT)
+    AAA = np.zeros(NKFFT + XX_R.shape[1:], dtype=complex)
+    for iR, R in enumerate(np.asarray(iRvec) % NKFFT):
+        AAA[tuple(R)] += XX_R[iR]
+    AAA = np.fft.ifftn(AAA, axes=(0, 1, 2)) * np.prod(NKFFT)
+    if hermitian:
+        AAA = 0.5 * (AAA + AAA.swapaxes(3, 4).conj())
+    return AAA.reshape((np.prod(NKFFT),) + XX_R.shape[1:])
+
+
+def grid_points(NKFFT):
+    """grid/grid.py:68-75: j/N for j in C order."""
+    return iterate_nd(NKFFT) / np.array(NKFFT)[None, :]
+
+
+# ---------------------------------------------------------------------------
+# Data_K for one FFT block (data_K/data_K.py, data_K/data_K_R.py)
+# ---------------------------------------------------------------------------
+class DataK:
+    """One FFT block at shift dK (reduced, K/NKFFT): data_K/data_K.py:73-111."""
+
+    def __init__(self, system, NKFFT, dK):
+        self.system = system
+        self.NKFFT = np.array(NKFFT, dtype=int)
+        self.dK = np.array(dK, dtype=float)
+        self.nk = int(np.prod(self.NKFFT))
+        self.num_wann = system.num_wann
+        self.cell_volume = system.cell_volume
+        self.force_internal_terms_only = system.force_internal_terms_only
+        # rvectors.py:467-468
+        self.expdK = np.exp(2j * np.pi * system.iRvec.dot(self.dK))
+        self._R = {}
+        self._bar = {}
+        self._cov = {}
+        self._cache = {}
+
+    # --- R-space matrices with the block phase (data_K_R.py:28-51) ---
+    def derivative(self, XX_R):  # rvectors.py:487-494
+        cR = self.system.cRvec_shifted()
+        nR, nw = cR.shape[0], cR.shape[1]
+        return 1j * XX_R.reshape(XX_R.shape + (1,)) * cR.reshape((nR, nw, nw) + (1,) * (XX_R.ndim - 3) + (3,))
+
+    def get_R_mat(self, key):
+        if key not in self._R:
+            if key == 'rotAA':  # data_K_R.py:48-51
+                d = self.derivative(self.get_R_mat('AA'))
+                res = d[:, :, :, BETA, ALPHA] - d[:, :, :, ALPHA, BETA]
+            else:  # rvectors.py:477-485
+                X = self.system.XX_R[key]
+                res = X * self.expdK.reshape((-1,) + (1,) * (X.ndim - 1))
+            self._R[key] = res
+        return self._R[key]
+
+    def R_to_k(self, XX_R, der=0, hermitian=True):  # rvectors.py:496-506
+        for _ in range(der):
+            XX_R = self.derivative(XX_R)
+        return fft_R_to_k(XX_R, self.system.iRvec, self.NKFFT, hermitian=hermitian)
+
+    # --- k-space basics (data_K.py:211-218, data_K_R.py:24-26) ---
+    @property
+    def HH_K(self):
+        if 'HH_K' not in self._cache:
+            self._cache['HH_K'] = self.R_to_k(self.system.XX_R['Ham'] * self.expdK[:, None, None], hermitian=True)
+        return self._cache['HH_K']
+
+    def _eigh(self):
+        if 'E_K' not in self._cache:
+            E, U = np.linalg.eigh(self.HH_K)
+            self._cache['E_K'] = E
+            self._cache['UU_K'] = U
+        return self._cache['E_K'], self._cache['UU_K']
+
+    @property
+    def E_K(self):
+        return self._eigh()[0]
+
+    @property
+    def UU_K(self):
+        return self._eigh()[1]
+
+    def _rotate(self, mat):  # data_K.py:130-132
+        U = self.UU_K
+        return np.einsum('kba,kbc...,kcd->kad...', U.conj(), mat, U, optimize='greedy')
+
+    def Xbar(self, name, der=0):  # data_K_R.py:69-97
+        key = (name, der)
+        if key not in self._bar:
+            Xk = self.R_to_k(self.get_R_mat(name).copy(), der=der,
+                             hermitian=(name in ['AA', 'SS', 'OO', 'rotAA']))
+            self._bar[key] = self._rotate(Xk)
+        return self._bar[key]
+
+    @property
+    def dEig_inv(self):  # data_K.py:290-298
+        if 'dEig_inv' not in self._cache:
+            thr = 1e-7
+            d = self.E_K[:, :, None] - self.E_K[:, None, :]
+            sel = abs(d) < thr
+            d[sel] = thr
+            d = 1. / d
+            d[sel] = 0.
+            self._cache['dEig_inv'] = d
+        return self._cache['dEig_inv']
+
+    @property
+    def D_H(self):  # data_K.py:324-326
+        if 'D_H' not in self._cache:
+            self._cache['D_H'] = -self.Xbar('Ham', 1) * self.dEig_inv[:, :, :, None]
+        return self._cache['D_H']
+
+    def get_A_H(self, external_terms=True):  # data_K.py:328-334
+        A = 1j * self.D_H
+        if external_terms:
+            A = A + self.Xbar('AA')
+        return A
+
+    def delE_K(self):  # data_K.py:236-242
+        d = np.einsum("klla->kla", self.Xbar('Ham', 1))
+        if np.abs(d.imag).max() > 1e-10:
+            raise RuntimeError("The band derivatives have considerable imaginary part")
+        return d.real
+
+    # --- band groups (data_K.py:172-198, grid/tetrahedron.py:132-162) ---
+    def get_bands_in_range_groups_ik(self, ik, emin, emax, degen_thresh=-1, sea=False):
+        E = self.E_K[ik]
+        borders = [0] + list(np.where((E[1:] - E[:-1]) > degen_thresh)[0] + 1) + [len(E)]
+        groups = [(b1, b2) for b1, b2 in zip(borders, borders[1:])
+                  if E[b1:b2].max() >= emin and E[b1:b2].min() <= emax]
+        weights = {(b1, b2): E[b1:b2].mean() for b1, b2 in groups}
+        if sea:
+            below = np.where(E < emin)[0]
+            bandmax = below[-1] + 1 if len(below) > 0 else 0
+            if len(groups) > 0:
+                bandmax = min(bandmax, groups[0][0])
+            if bandmax > 0:
+                weights[(0, bandmax)] = -np.inf
+        return weights
+
+    # --- covariant matrices (data_K.py:244-288) ---
+    def covariant(self, name, commader=0, gender=0):
+        key = (name, commader, gender)
+        if key not in self._cov:
+            if gender == 0:
+                res = Matrix_ln(self.Xbar(name, commader))
+            elif name == 'Ham':
+                res = V_covariant(self.Xbar('Ham', 1))
+            else:
+                res = Matrix_GenDer_ln(self.covariant(name), self.covariant(name, commader=1), self.Dcov)
+            self._cov[key] = res
+        return self._cov[key]
+
+    @property
+    def Dcov(self):
+        if 'Dcov' not in self._cache:
+            self._cache['Dcov'] = Dcov(self)
+        return self._cache['Dcov']
+
+
+# ---------------------------------------------------------------------------
+# Formula protocol (formula/formula.py:31-118, formula/elementary.py)
+# ---------------------------------------------------------------------------
+class Formula_ln:
+    """formula/formula.py:31-78: ln/nn/nl/ll sub-blocks and the real trace."""
+    additive = True
+    ndim = 0
+
+    def nl(self, ik, inn, out):
+        return self.ln(ik, out, inn)
+
+    def ll(self, ik, inn, out):
+        return self.nn(ik, out, inn)
+
+    def trace(self, ik, inn, out):
+        return np.einsum("nn...->...", self.nn(ik, inn, out)).real
+
+
+class Matrix_ln(Formula_ln):  # formula/formula.py:81-92
+    def __init__(self, matrix):
+        self.matrix = matrix
+        self.ndim = matrix.ndim - 3
+
+    def ln(self, ik, inn, out):
+        return self.matrix[ik][out][:, inn]
+
+    def nn(self, ik, inn, out):
+        return self.matrix[ik][inn][:, inn]
+
+
+class V_covariant(Matrix_ln):  # data_K/data_K.py:273-285 (ln block is zero)
+    def ln(self, ik, inn, out):
+        return np.zeros((len(out), len(inn), 3), dtype=complex)
+
+
+class Matrix_GenDer_ln(Formula_ln):  # formula/formula.py:95-118
+    def __init__(self, matrix, matrix_comader, D):
+        self.A, self.dA, self.D = matrix, matrix_comader, D
+        self.ndim = matrix.ndim + 1
+
+    def nn(self, ik, inn, out):
+        s = self.dA.nn(ik, inn, out).copy()
+        s -= np.einsum("mld,lnb...->mnb...d", self.D.nl(ik, inn, out), self.A.ln(ik, inn, out))
+        s += np.einsum("mlb...,lnd->mnb...d", self.A.nl(ik, inn, out), self.D.ln(ik, inn, out))
+        return s
+
+    def ln(self, ik, inn, out):
+        s = self.dA.ln(ik, inn, out).copy()
+        s -= np.einsum("mld,lnb...->mnb...d", self.D.ln(ik, inn, out), self.A.nn(ik, inn, out))
+        s += np.einsum("mlb...,lnd->mnb...d", self.A.ll(ik, inn, out), self.D.ln(ik, inn, out))
+        return s
+
+
+class Dcov(Matrix_ln):  # formula/elementary.py:46-52
+    def __init__(self, data_K):
+        super().__init__(data_K.D_H)
+
+    def nn(self, ik, inn, out):
+        raise ValueError("Dln should not be called within inner states")
+
+
+class DEinv_ln(Matrix_ln):  # formula/elementary.py:18-25
+    def __init__(self, data_K):
+        super().__init__(data_K.dEig_inv)
+
+    def nn(self, ik, inn, out):
+        raise NotImplementedError()
+
+
+class Eavln(Matrix_ln):  # formula/elementary.py:8-15
+    def __init__(self, data_K):
+        super().__init__(0.5 * (data_K.E_K[:, :, None] + data_K.E_K[:, None, :]))
+        self.ndim = 0
+
+
+class DerDcov(Dcov):  # formula/elementary.py:55-70
+    def __init__(self, data_K):
+        self.W = data_K.covariant('Ham', commader=2)
+        self.V = data_K.covariant('Ham', gender=1)
+        self.D = data_K.Dcov
+        self.dEinv = DEinv_ln(data_K)
+
+    def ln(self, ik, inn, out):
+        s = self.W.ln(ik, inn, out).copy()
+        t = np.einsum("lpb,pnd->lnbd", self.V.ll(ik, inn, out), self.D.ln(ik, inn, out))
+        s += t + t.swapaxes(2, 3)
+        t = -np.einsum("lmb,mnd->lnbd", self.D.ln(ik, inn, out), self.V.nn(ik, inn, out))
+        s += t + t.swapaxes(2, 3)
+        s *= -self.dEinv.ln(ik, inn, out)[:, :, None, None]
+        return s
+
+
+class _TermsFormula(Formula_ln):
+    """formula/formula.py:12-29: internal/external term switches."""
+
+    def __init__(self, data_K, internal_terms=True, external_terms=True, **_):
+        self.internal_terms = internal_terms
+        self.external_terms = external_terms
+        if data_K.force_internal_terms_only:
+            self.external_terms = False
+
+
+class Omega(_TermsFormula):  # formula/covariant.py:161-203
+    def __init__(self, data_K, **kw):
+        super().__init__(data_K, **kw)
+        self.D = data_K.Dcov
+        if self.external_terms:
+            self.A = data_K.covariant('AA')
+            self.O = data_K.covariant('rotAA')
+        self.ndim = 1
+
+    def nn(self, ik, inn, out):
+        s = np.zeros((len(inn), len(inn), 3), dtype=complex)
+        Dnl, Dln = self.D.nl(ik, inn, out), self.D.ln(ik, inn, out)
+        if self.internal_terms:
+            s += -1j * np.einsum("mlc,lnc->mnc", Dnl[:, :, ALPHA], Dln[:, :, BETA])
+        if self.external_terms:
+            Aln, Ann = self.A.ln(ik, inn, out), self.A.nn(ik, inn, out)
+            s += 0.5 * self.O.nn(ik, inn, out)
+            s += -1 * np.einsum("mlc,lnc->mnc", Dnl[:, :, ALPHA], Aln[:, :, BETA])
+            s += +1 * np.einsum("mlc,lnc->mnc", Dnl[:, :, BETA], Aln[:, :, ALPHA])
+            s += -1j * np.einsum("mlc,lnc->mnc", Ann[:, :, ALPHA], Ann[:, :, BETA])
+        s += s.swapaxes(0, 1).conj()
+        return s
+
+
+class DerOmega(_TermsFormula):  # formula/covariant.py:212-259
+    def __init__(self, data_K, **kw):
+        super().__init__(data_K, **kw)
+        self.dD = DerDcov(data_K)
+        self.D = data_K.Dcov
+        if self.external_terms:
+            self.A = data_K.covariant('AA')
+            self.dA = data_K.covariant('AA', gender=1)
+            self.dO = data_K.covariant('rotAA', gender=1)
+        self.ndim = 2
+
+    def nn(self, ik, inn, out):
+        s = np.zeros((len(inn), len(inn), 3, 3), dtype=complex)
+        if self.external_terms:
+            s += 0.5 * self.dO.nn(ik, inn, out)
+        Dnl = self.D.nl(ik, inn, out)
+        dDln = self.dD.ln(ik, inn, out)
+        if self.external_terms:
+            dAln, dAnn = self.dA.ln(ik, inn, out), self.dA.nn(ik, inn, out)
+            dDnl = self.dD.nl(ik, inn, out)
+            Aln, Ann = self.A.ln(ik, inn, out), self.A.nn(ik, inn, out)
+        for sg, a, b in (+1, ALPHA, BETA), (-1, BETA, ALPHA):
+            if self.internal_terms:
+                s += -1j * sg * np.einsum("mlc,lncd->mncd", Dnl[:, :, a], dDln[:, :, b])
+            if self.external_terms:
+                s += -1 * sg * np.einsum("mlc,lncd->mncd", Dnl[:, :, a], dAln[:, :, b, :])
+                s += -1 * sg * np.einsum("mlcd,lnc->mncd", dDnl[:, :, a, :], Aln[:, :, b])
+                s += -1j * sg * np.einsum("mlc,lncd->mncd", Ann[:, :, a], dAnn[:, :, b, :])
+        s += s.swapaxes(0, 1).conj()
+        return s
+
+
+class Morb_H(_TermsFormula):  # formula/covariant.py:375-421
+    additive = False
+
+    def __init__(self, data_K, **kw):
+        super().__init__(data_K, **kw)
+        if self.external_terms:
+            self.A = data_K.covariant('AA')
+            self.B = data_K.covariant('BB')
+            self.C = data_K.covariant('CC')
+        self.D = data_K.Dcov
+        self.E = data_K.E_K
+        self.ndim = 1
+
+    def nn(self, ik, inn, out):
+        s = np.zeros((len(inn), len(inn), 3), dtype=complex)
+        Dnl, Dln = self.D.nl(ik, inn, out), self.D.ln(ik, inn, out)
+        if self.internal_terms:
+            s += -1j * np.einsum("mlc,lnc->mnc", Dnl[:, :, ALPHA] * self.E[ik][out][None, :, None], Dln[:, :, BETA])
+        if self.external_terms:
+            Bln, Ann = self.B.ln(ik, inn, out), self.A.nn(ik, inn, out)
+            s += 0.5 * self.C.nn(ik, inn, out)
+            s += -1 * np.einsum("mlc,lnc->mnc", Dnl[:, :, ALPHA], Bln[:, :, BETA])
+            s += +1 * np.einsum("mlc,lnc->mnc", Dnl[:, :, BETA], Bln[:, :, ALPHA])
+            s += -1j * np.einsum("mlc,lnc->mnc", Ann[:, :, ALPHA] * self.E[ik][inn][None, :, None], Ann[:, :, BETA])
+        s += s.swapaxes(0, 1).conj()
+        return s
+
+
+class Morb_Hpm(_TermsFormula):  # formula/covariant.py:424-449
+    additive = False
+
+    def __init__(self, data_K, sign=+1, **kw):
+        super().__init__(data_K, **kw)
+        self.H = Morb_H(data_K, **kw)
+        self.sign = sign
+        if sign != 0:
+            self.O = Omega(data_K, **kw)
+            self.Eav = Eavln(data_K)
+        self.ndim = 1
+
+    def nn(self, ik, inn, out):
+        r = self.H.nn(ik, inn, out)
+        if self.sign != 0:
+            r = r + self.sign * self.Eav.nn(ik, inn, out)[:, :, None] * self.O.nn(ik, inn, out)
+        return r
+
+
+# ---------------------------------------------------------------------------
+# Results (result/energyresult.py, minimal)
+# ---------------------------------------------------------------------------
+class EnergyResult:
+    def __init__(self, Energies, data):
+        self.Energies = Energies if isinstance(Energies, (list, tuple)) else [Energies]
+        self.data = data
+
+    def __add__(self, other):
+        return EnergyResult(self.Energies, self.data + other.data)
+
+    def __mul__(self, number):
+        return EnergyResult(self.Energies, self.data * number)
+
+
+# ---------------------------------------------------------------------------
+# Static calculators (calculators/static.py:24-169, 231-247, 353-364, 472-487)
+# ---------------------------------------------------------------------------
+class StaticCalculator:
+    def __init__(self, Efermi, constant_factor=1., degen_thresh=1e-4, kwargs_formula=None, use_factor=True):
+        self.Efermi = np.array(Efermi, dtype=float)
+        self.constant_factor = constant_factor
+        self.degen_thresh = degen_thresh
+        self.kwargs_formula = dict(kwargs_formula or {})
+        self.use_factor = use_factor
+        self.extraEf = 0 if self.fder == 0 else 1 if self.fder in (1, 2) else 2
+        self.dEF = self.Efermi[1] - self.Efermi[0] if len(self.Efermi) > 1 else 0.001
+        self.EFmin = self.Efermi[0] - self.extraEf * self.dEF
+        self.EFmax = self.Efermi[-1] + self.extraEf * self.dEF
+        self.nEF_extra = self.Efermi.shape[0] + 2 * self.extraEf
+
+    def values(self, data_K):
+        """Per-k group traces {(ib1,ib2): value} and group energies (static.py:64-117)."""
+        formula = self.Formula(data_K, **self.kwargs_formula)
+        NB = data_K.num_wann
+        weights = [data_K.get_bands_in_range_groups_ik(ik, self.EFmin, self.EFmax, self.degen_thresh,
+                                                       sea=(self.fder == 0)) for ik in range(data_K.nk)]
+        values = []
+        for ik, bnd in enumerate(weights):
+            v = {}
+            if formula.additive:
+                for n in bnd:
+                    inn = np.arange(n[0], n[1])
+                    out = np.concatenate((np.arange(0, n[0]), np.arange(n[1], NB)))
+                    v[n] = formula.trace(ik, inn, out)
+            else:
+                cache = {}
+                for nb in set(x for n in bnd for x in n):
+                    if nb == 0:
+                        cache[nb] = np.zeros((3,) * formula.ndim)
+                    else:
+                        cache[nb] = formula.trace(ik, np.arange(0, nb), np.arange(nb, NB))
+                for n in bnd:
+                    v[n] = cache[n[1]] - cache[n[0]]
+            values.append(v)
+        return formula, weights, values
+
+    def __call__(self, data_K):
+        formula, weights, values = self.values(data_K)
+        shape = (3,) * formula.ndim
+        restot = np.zeros((self.nEF_extra,) + shape)
+        for ik, w in enumerate(weights):
+            for n, E in sorted(w.items()):
+                if E < self.EFmin:
+                    restot += values[ik][n][None]
+                elif E <= self.EFmax:
+                    iEf = ceil((E - self.EFmin) / self.dEF)
+                    restot[iEf:] += values[ik][n]
+        if self.fder == 1:
+            restot = (restot[2:] - restot[:-2]) / (2 * self.dEF)
+        elif self.fder != 0:
+            raise NotImplementedError()
+        restot /= data_K.cell_volume
+        restot /= data_K.nk
+        restot *= self.constant_factor if self.use_factor else np.sign(self.constant_factor)
+        return EnergyResult(self.Efermi, restot)
+
+
+class AHC(StaticCalculator):  # calculators/static.py:353-364
+    Formula = Omega
+    fder = 0
+
+    def __init__(self, constant_factor=FACTOR_AHC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class BerryDipole_FermiSea(StaticCalculator):  # calculators/static.py:472-487
+    Formula = DerOmega
+    fder = 0
+
+    def __call__(self, data_K):
+        res = super().__call__(data_K)
+        res.data = res.data.swapaxes(1, 2)
+        return res
+
+
+class Morb(StaticCalculator):  # calculators/static.py:231-247
+    Formula = Morb_Hpm
+    fder = 0
+
+    def __init__(self, constant_factor=FACTOR_MORB, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+        self.AHC = AHC(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        Hplus = super().__call__(data_K)
+        Om = self.AHC(data_K)
+        Hplus.data = Hplus.data + (-2) * Om.data * self.Efermi[:, None]
+        return Hplus * data_K.cell_volume
+
+
+# ---------------------------------------------------------------------------
+# Kubo optical conductivity (calculators/dynamic.py:26-114,170-196; utility.py:147-182)
+# ---------------------------------------------------------------------------
+def lorentzian(x, width):
+    return 1.0 / (np.pi * width) * width ** 2 / (x ** 2 + width ** 2)
+
+
+def gaussian(x, width):
+    inds = abs(x) < width * np.sqrt(200.0)
+    out = np.zeros(x.shape, dtype=float)
+    out[inds] = 1.0 / (np.sqrt(np.pi) * width) * np.exp(-(x[inds] / width) ** 2)
+    return out
+
+
+def fermi_dirac(E, mu, kBT):
+    if kBT == 0:
+        return 1.0 * (E <= mu)
+    res = np.zeros(mu.shape, dtype=float)
+    res[mu > E + 30 * kBT] = 1.0
+    res[mu < E - 30 * kBT] = 0.0
+    sel = abs(mu - E) <= 30 * kBT
+    res[sel] = 1.0 / (np.exp((E - mu[sel]) / kBT) + 1)
+    return res
+
+
+class OpticalConductivity:
+    def __init__(self, Efermi, omega, kBT=0, smr_fixed_width=0.1, smr_type='Lorentzian', degen_thresh=1e-4,
+                 kwargs_formula=None):
+        self.Efermi = np.array(Efermi, dtype=float).reshape(-1)
+        self.omega = np.array(omega, dtype=float)
+        self.kBT = kBT
+        self.smr_fixed_width = smr_fixed_width
+        self.smr_type = smr_type
+        self.degen_thresh = degen_thresh
+        self.kwargs_formula = dict(kwargs_formula or {})
+        self.eocc1max = self.Efermi.min() - 30 * kBT
+        self.eocc0min = self.Efermi.max() + 30 * kBT
+
+    def nonzero(self, E1, E2):
+        return not ((E1 < self.eocc1max and E2 < self.eocc1max) or (E1 > self.eocc0min and E2 > self.eocc0min))
+
+    def factor_omega(self, E1, E2):
+        arg = E2 - E1 - self.omega
+        cfac = 1. / (arg - 1j * self.smr_fixed_width)
+        if self.smr_type != 'Lorentzian':
+            cfac.imag = np.pi * gaussian(arg, self.smr_fixed_width)
+        return (E2 - E1) * cfac
+
+    def __call__(self, data_K):
+        external = self.kwargs_formula.get('external_terms', True) and not data_K.force_internal_terms_only
+        A = data_K.get_A_H(external_terms=external)
+        AA = 1j * A[:, :, :, :, None] * A.swapaxes(1, 2)[:, :, :, None, :]   # dynamic.py:172-175
+        restot = np.zeros((len(self.omega), len(self.Efermi) * 9), dtype=complex)
+        for ik in range(data_K.nk):
+            groups = data_K.get_bands_in_range_groups_ik(ik, -np.inf, np.inf, self.degen_thresh)
+            pairs = [(gm, gn, Em, En) for gm, Em in groups.items() for gn, En in groups.items()
+                     if self.nonzero(Em, En)]
+            if not pairs:
+                continue
+            M = np.array([AA[ik, np.arange(*p[0])].sum(axis=0)[np.arange(*p[1])].sum(axis=0) for p in pairs])
+            fE = np.array([fermi_dirac(p[3], self.Efermi, self.kBT) - fermi_dirac(p[2], self.Efermi, self.kBT)
+                           for p in pairs])
+            fw = np.array([self.factor_omega(p[2], p[3]) for p in pairs]).T
+            restot += fw @ (fE[:, :, None] * M.reshape(len(pairs), -1)[:, None, :]).reshape(len(pairs), -1)
+        restot = restot.reshape((len(self.omega), len(self.Efermi), 3, 3)).swapaxes(0, 1)
+        restot *= FACTOR_OPT / (data_K.nk * data_K.cell_volume)
+        return EnergyResult([self.Efermi, self.omega], restot)
+
+
+# ---------------------------------------------------------------------------
+# Driver (run_grid.py:118-403, grid/grid.py:149-189, grid/Kpoint.py:75-77)
+# ---------------------------------------------------------------------------
+def block_shifts(NKdiv, NKFFT):
+    """K-points of the division grid (C order) and their dK = K/NKFFT."""
+    NKdiv = np.array(NKdiv)
+    K = iterate_nd(NKdiv) / NKdiv[None, :]
+    return K / np.array(NKFFT)[None, :]
+
+
+def run(system, NKdiv, NKFFT, calculators, blocks=None):
+    """Serial run() over the FFT blocks without symmetry or refinement: sum of
+    block results times factor 1/prod(NKdiv) (run_grid.py:59-66, grid/grid.py:152)."""
+    shifts = block_shifts(NKdiv, NKFFT)
+    if blocks is not None:
+        shifts = shifts[blocks]
+    factor = 1. / np.prod(NKdiv)
+    total = {}
+    for dK in shifts:
+        data = DataK(system, NKFFT, dK)
+        for key, calc in calculators.items():
+            r = calc(data) * factor
+            total[key] = r if key not in total else total[key] + r
+    return total

@@ -1,0 +1,161 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run in a container where the reference (wannier-berri) source tree is mounted:
+
+    python tests/golden/make_golden.py /root/reference
+
+It imports the reference with two tiny shims (``termcolor.cprint`` -> print,
+``numba.njit`` -> identity; neither is on the hot path) and with
+PYTHONDONTWRITEBYTECODE so nothing is written into the reference tree.
+
+Fixtures written (all small, complex128/float64):
+
+* ``random_system.npz`` + ``random_results.npz`` -- the reference's own test
+  system ``tests/data/random`` (nw=6, nR=20) and its stored golden results
+  ``tests/reference/integrate_files/random-{ahc,Morb,opt_conductivity}_iter-0000.npz``
+  (settings of ``tests/test_run.py:653-669``: NK=6, NKFFT=3, E_F=linspace(-2,2,5)).
+* ``fe_system.npz`` + ``fe_formula.npz`` -- ``tests/reference/systems/system_Fe_sym_W90_OSD``
+  (Ham, AA, BB, CC only) and the stored formula traces
+  ``tests/reference/formula/{Omega,DerOmega,Morb_H,Dcov,DerDcov,DEinv_ln}.npz``
+  (settings of ``tests/test_formula.py:18-41,171-213``).
+* ``synthetic_ref.npz`` -- outputs of the reference's ``wannierberri.run`` /
+  ``Data_K_R`` on small seeded models with the structure of the benchmark
+  configurations (cubic nw=8 / triclinic nw=6 with MDRS / spinor nw=8), made by
+  ``wbgpu.models``: per-block E_K, and AHC / Morb / BerryDipole_FermiSea /
+  OpticalConductivity results.
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def setup_reference(ref_root):
+    os.environ['PYTHONDONTWRITEBYTECODE'] = '1'
+    sys.dont_write_bytecode = True
+    shim = tempfile.mkdtemp(prefix='wbshim_')
+    os.makedirs(os.path.join(shim, 'termcolor'))
+    os.makedirs(os.path.join(shim, 'numba'))
+    with open(os.path.join(shim, 'termcolor', '__init__.py'), 'w') as f:
+        f.write("def cprint(*a, **k):\n    print(a[0] if a else '')\n"
+                "def colored(s, *a, **k):\n    return s\n")
+    with open(os.path.join(shim, 'numba', '__init__.py'), 'w') as f:
+        f.write("def njit(*a, **k):\n    if len(a) == 1 and callable(a[0]) and not k:\n        return a[0]\n"
+                "    return lambda f: f\njit = njit\n")
+    sys.path.insert(0, shim)
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, os.path.join(REPO, 'wannier-berri_gb300'))
+    import wannierberri  # noqa: F401
+    return wannierberri
+
+
+def ref_system_from_arrays(wb, d):
+    from wannierberri.system.system_R import System_R
+    from wannierberri.fourier.rvectors import Rvectors
+    s = System_R(silent=True)
+    s.set_real_lattice(real_lattice=d['real_lattice'])
+    s.num_wann = d['XX_R']['Ham'].shape[1]
+    s.set_wannier_centers(wannier_centers_cart=d['wannier_centers_cart'])
+    s.rvec = Rvectors(lattice=s.real_lattice, iRvec=d['iRvec'], shifts_left_red=s.wannier_centers_red)
+    for k, v in d['XX_R'].items():
+        s.set_R_mat(k, v.copy())
+    s.do_at_end_of_init()
+    return s
+
+
+def pack_system(prefix, s, keys):
+    out = {prefix + 'real_lattice': s.real_lattice, prefix + 'iRvec': s.rvec.iRvec,
+           prefix + 'wannier_centers_cart': s.wannier_centers_cart}
+    for k in keys:
+        out[prefix + 'XX_R_' + k] = s.get_R_mat(k)
+    return out
+
+
+def run_ref(wb, system, NKdiv, NKFFT, calculators):
+    from wannierberri.grid import Grid
+    tmp = tempfile.mkdtemp(prefix='wbrun_')
+    grid = Grid(system=system, NKdiv=NKdiv, NKFFT=NKFFT, use_symmetry=False)
+    res = wb.run(system, grid=grid, calculators=calculators, parallel=False, use_irred_kpt=False,
+                 symmetrize=False, fout_name=os.path.join(tmp, 'r'), file_Klist_path=os.path.join(tmp, 'k'),
+                 print_progress_step_time=1e9)
+    return {k: res.results[k].data for k in calculators}
+
+
+def main(ref_root):
+    wb = setup_reference(ref_root)
+    from wannierberri.system.system_R import System_R
+    from wannierberri import calculators as calc
+    from wbgpu import models
+
+    # ---- 1. the reference's own random system and stored results
+    rs = System_R.from_npz(path=os.path.join(ref_root, 'tests', 'data', 'random'), legacy=True)
+    np.savez_compressed(os.path.join(HERE, 'random_system.npz'), **pack_system('', rs, ['Ham', 'AA', 'BB', 'CC']))
+    res = {}
+    for q in ['ahc', 'Morb', 'opt_conductivity']:
+        f = np.load(os.path.join(ref_root, 'tests', 'reference', 'integrate_files', f'random-{q}_iter-0000.npz'),
+                    allow_pickle=True)
+        res[q + '_data'] = f['data']
+        res[q + '_E0'] = f['Energies_0']
+        if 'Energies_1' in f:
+            res[q + '_E1'] = f['Energies_1']
+    np.savez_compressed(os.path.join(HERE, 'random_results.npz'), **res)
+
+    # ---- 2. Fe formula system and stored formula traces
+    fe = System_R.from_npz(os.path.join(ref_root, 'tests', 'reference', 'systems', 'system_Fe_sym_W90_OSD'),
+                           matrices=['Ham', 'AA', 'BB', 'CC'])
+    np.savez_compressed(os.path.join(HERE, 'fe_system.npz'), **pack_system('', fe, ['Ham', 'AA', 'BB', 'CC']))
+    fres = {}
+    for name in ['Omega', 'DerOmega', 'Morb_H', 'Dcov', 'DerDcov', 'DEinv_ln']:
+        f = np.load(os.path.join(ref_root, 'tests', 'reference', 'formula', name + '.npz'))
+        for k in f.files:
+            fres[name + '/' + k] = f[k]
+    np.savez_compressed(os.path.join(HERE, 'fe_formula.npz'), **fres)
+
+    # ---- 3. reference outputs on seeded synthetic models
+    out = {}
+    EF = np.linspace(-2, 2, 41)
+    # config-1 structure at full nw=8, R in [-2,2]^3: one 8^3 block at a generic shift + 2^3 blocks of 4^3
+    d1 = models.config_system(1)
+    s1 = ref_system_from_arrays(wb, d1)
+    from wannierberri.data_K.data_K_R import Data_K_R
+    from wannierberri.grid import Grid
+    g = Grid(system=s1, NKdiv=1, NKFFT=8, use_symmetry=False)
+    dK = np.array([0.3, 0.1, 0.7]) / 8
+    dk = Data_K_R(s1, dK=dK, grid=g)
+    out['c1_block_dK'] = dK
+    out['c1_block_E'] = dk.E_K
+    ahc = calc.static.AHC(Efermi=np.linspace(-2, 2, 501))
+    out['c1_block_ahc'] = ahc(dk).data
+    r = run_ref(wb, s1, 2, 4, {'ahc': calc.static.AHC(Efermi=EF)})
+    out['c1_run_ahc'] = r['ahc']
+    # config-2 structure (triclinic, random centres, BB/CC, MDRS) at small size
+    d2 = models.config_system(2, small=True)
+    s2 = ref_system_from_arrays(wb, d2)
+    s2.do_ws_dist(mp_grid=3)
+    out['c2_mdrs_iRvec'] = s2.rvec.iRvec
+    for k in ['Ham', 'AA', 'BB', 'CC']:
+        out['c2_mdrs_' + k] = s2.get_R_mat(k)
+    r = run_ref(wb, s2, 2, 4, {'ahc': calc.static.AHC(Efermi=EF),
+                               'morb': calc.static.Morb(Efermi=EF),
+                               'bcd': calc.static.BerryDipole_FermiSea(Efermi=EF)})
+    for k, v in r.items():
+        out['c2_run_' + k] = v
+    # config-3 structure (spin-interlaced + SOC) at small size: optical conductivity + AHC
+    d3 = models.config_system(3, small=True)
+    s3 = ref_system_from_arrays(wb, d3)
+    EF3 = np.linspace(-1, 1, 11)
+    om = np.linspace(0, 4, 40)
+    r = run_ref(wb, s3, 2, 4, {'opt': calc.dynamic.OpticalConductivity(Efermi=EF3, omega=om, smr_fixed_width=0.05),
+                               'ahc': calc.static.AHC(Efermi=EF3)})
+    for k, v in r.items():
+        out['c3_run_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'synthetic_ref.npz'), **out)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

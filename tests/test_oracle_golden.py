@@ -1,0 +1,159 @@
+"""Pin the CPU oracle against the reference's own golden vectors (CPU only).
+
+* tests/reference/integrate_files/random-*_iter-0000.npz with the settings of
+  the reference's tests/test_run.py:653-669 (NK=6, NKFFT=3).
+* tests/reference/formula/*.npz with the settings of tests/test_formula.py:18-41,171-213.
+* reference outputs on seeded synthetic models (tests/golden/make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import wb_oracle as O
+from wbgpu import models
+
+
+def load_system(path, prefix=''):
+    f = np.load(path)
+    XX = {k[len(prefix) + 5:]: f[k] for k in f.files if k.startswith(prefix + 'XX_R_')}
+    return O.RSystem(f[prefix + 'real_lattice'], f[prefix + 'iRvec'], f[prefix + 'wannier_centers_cart'], XX)
+
+
+def maxrel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def random_sys(golden_dir):
+    return load_system(os.path.join(golden_dir, 'random_system.npz'))
+
+
+@pytest.fixture(scope="module")
+def random_res(golden_dir):
+    return np.load(os.path.join(golden_dir, 'random_results.npz'))
+
+
+@pytest.fixture(scope="module")
+def random_run(random_sys, random_res):
+    EF = np.linspace(-2, 2, 5)
+    calcs = {'ahc': O.AHC(Efermi=EF), 'Morb': O.Morb(Efermi=EF),
+             'opt_conductivity': O.OpticalConductivity(Efermi=np.array([17.0, 18.0]), omega=np.arange(0.0, 7.1, 1.0),
+                                                       smr_fixed_width=0.20, smr_type="Gaussian")}
+    return O.run(random_sys, NKdiv=(2, 2, 2), NKFFT=(3, 3, 3), calculators=calcs)
+
+
+@pytest.mark.parametrize("quant", ['ahc', 'Morb', 'opt_conductivity'])
+def test_random_golden(random_run, random_res, quant):
+    """Same acceptance rule as the reference: abs err < 1e-8 * max|ref| (tests/common_comparers.py:189-196)."""
+    ref = random_res[quant + '_data']
+    got = random_run[quant].data
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))
+
+
+FORMULAE_LN = ['Dcov', 'DerDcov', 'DEinv_ln']
+FORMULAE_NN = ['Omega', 'DerOmega', 'Morb_H']
+
+
+@pytest.fixture(scope="module")
+def fe_datak(golden_dir):
+    s = load_system(os.path.join(golden_dir, 'fe_system.npz'))
+    return O.DataK(s, NKFFT=(1, 2, 3), dK=(0, 0, 0))
+
+
+@pytest.mark.parametrize("name", FORMULAE_LN + FORMULAE_NN)
+def test_fe_formula_golden(fe_datak, golden_dir, name):
+    """tests/test_formula.py:171-220 with its tolerances."""
+    data = fe_datak
+    ref = np.load(os.path.join(golden_dir, 'fe_formula.npz'))
+    cls = {'Dcov': lambda d: d.Dcov, 'DerDcov': O.DerDcov, 'DEinv_ln': O.DEinv_ln,
+           'Omega': O.Omega, 'DerOmega': O.DerOmega, 'Morb_H': O.Morb_H}[name]
+    NB = data.num_wann
+    value = {}
+    for ik in range(data.nk):
+        groups = data.get_bands_in_range_groups_ik(ik, -10, 30, degen_thresh=1)
+        acc = {k: [] for k in ["Xnn", "Xll", "XlnXnl", "XnlXln", "XnnXnn", "XllXll"]}
+        for n in groups:
+            inn = np.arange(n[0], n[1])
+            out = np.concatenate((np.arange(0, n[0]), np.arange(n[1], NB)))
+            form = cls(data)
+            if name not in FORMULAE_NN:
+                Xnl = form.ln(ik, inn, out)
+                Xln = form.ln(ik, out, inn)
+                acc["XnlXln"].append(np.einsum("nl...,ln...->...", Xnl, Xln))
+                acc["XlnXnl"].append(np.einsum("ln...,nl...->...", Xln, Xnl))
+            if name not in FORMULAE_LN:
+                Xll = form.ll(ik, inn, inn)
+                Xnn = form.nn(ik, inn, inn)
+                acc["Xll"].append(np.einsum("ll...->...", Xll))
+                acc["Xnn"].append(np.einsum("nn...->...", Xnn))
+                acc["XllXll"].append(np.einsum("ll...,ll...->...", Xll, Xll))
+                acc["XnnXnn"].append(np.einsum("nn...,nn...->...", Xnn, Xnn))
+        for k, v in acc.items():
+            value[f"{k}_ik={ik}"] = np.array(v)
+    rel_tol, atol_zero = (1e-5, 2e-6) if "Der" in name else (1e-6, 1e-10)
+    keys = [k for k in ref.files if k.startswith(name + '/')]
+    assert keys
+    for key in keys:
+        val = ref[key]
+        out = value[key.split('/', 1)[1]]
+        assert out.shape == val.shape
+        if val.size == 0:
+            continue
+        mx = np.max(abs(val))
+        if mx < atol_zero:
+            assert np.max(abs(out)) < atol_zero
+        else:
+            assert np.max(abs(val - out)) / mx < rel_tol, key
+
+
+@pytest.fixture(scope="module")
+def synth(golden_dir):
+    return np.load(os.path.join(golden_dir, 'synthetic_ref.npz'))
+
+
+def rsys(d):
+    return O.RSystem(d['real_lattice'], d['iRvec'], d['wannier_centers_cart'], d['XX_R'])
+
+
+def test_synthetic_c1_block(synth):
+    """One full-size config-1 block (nw=8, 125 R, 8^3 k at a generic shift): energies and AHC."""
+    s = rsys(models.config_system(1))
+    data = O.DataK(s, NKFFT=(8, 8, 8), dK=synth['c1_block_dK'])
+    assert np.max(np.abs(data.E_K - synth['c1_block_E'])) < 1e-10
+    ahc = O.AHC(Efermi=np.linspace(-2, 2, 501))(data).data
+    assert maxrel(ahc, synth['c1_block_ahc']) < 1e-10
+
+
+def test_synthetic_c1_run(synth):
+    s = rsys(models.config_system(1))
+    r = O.run(s, (2, 2, 2), (4, 4, 4), {'ahc': O.AHC(Efermi=np.linspace(-2, 2, 41))})
+    assert maxrel(r['ahc'].data, synth['c1_run_ahc']) < 1e-10
+
+
+def test_synthetic_c2_mdrs_and_run(synth):
+    s = rsys(models.config_system(2, small=True))
+    s2 = O.do_ws_dist(s, mp_grid=(3, 3, 3))
+    # same replica set and matrices (order-independent comparison)
+    ref_R = synth['c2_mdrs_iRvec']
+    idx = {tuple(R): i for i, R in enumerate(s2.iRvec)}
+    assert len(idx) == len(ref_R)
+    perm = np.array([idx[tuple(R)] for R in ref_R])
+    for k in ['Ham', 'AA', 'BB', 'CC']:
+        assert np.max(np.abs(s2.XX_R[k][perm] - synth['c2_mdrs_' + k])) < 1e-12
+    EF = np.linspace(-2, 2, 41)
+    r = O.run(s2, (2, 2, 2), (4, 4, 4), {'ahc': O.AHC(Efermi=EF), 'morb': O.Morb(Efermi=EF),
+                                         'bcd': O.BerryDipole_FermiSea(Efermi=EF)})
+    for k in ['ahc', 'morb', 'bcd']:
+        assert maxrel(r[k].data, synth['c2_run_' + k]) < 1e-9, k
+
+
+def test_synthetic_c3_run(synth):
+    s = rsys(models.config_system(3, small=True))
+    EF3 = np.linspace(-1, 1, 11)
+    om = np.linspace(0, 4, 40)
+    r = O.run(s, (2, 2, 2), (4, 4, 4), {'opt': O.OpticalConductivity(Efermi=EF3, omega=om, smr_fixed_width=0.05),
+                                        'ahc': O.AHC(Efermi=EF3)})
+    assert maxrel(r['opt'].data, synth['c3_run_opt']) < 1e-10
+    assert maxrel(r['ahc'].data, synth['c3_run_ahc']) < 1e-9
