@@ -1,0 +1,111 @@
+/*
+ * wbgpu -- C ABI of the GB300 (sm_103a) Wannier-interpolation backend.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream (as void*),
+ * launches stream-ordered work and returns an int status (WBG_STATUS_*).  No entry point
+ * allocates device memory: the caller passes every output and a workspace whose size
+ * the matching *_workspace_size query reports.  Complex numbers are interleaved
+ * (re, im) pairs of double (fp64 != 0) or float (fp64 == 0); matrices are row-major
+ * [m][n] with m, n Wannier indices.
+ *
+ * Reference interfaces replaced (paths relative to the wannier-berri project root):
+ *   wbg_r2k            fourier/fft.py:133-192 FFT_R_to_k.__call__ with
+ *                      fourier/rvectors.py:477-506 apply_expdK / derivative / R_to_k and
+ *                      data_K/data_K_R.py:28-51,91-97 get_R_mat / rotAA / _R_to_k_H
+ *   wbg_eigh_batched   data_K/data_K.py:211-218 E_K / UU_K (np.linalg.eigh of HH_K)
+ *   wbg_rotate         data_K/data_K.py:130-132 _rotate and data_K/data_K_R.py:69-89 Xbar
+ *   wbg_berry_omega    formula/covariant.py:161-203 Omega traced over the band groups of
+ *                      data_K/data_K.py:172-198 and binned as in calculators/static.py:103-136
+ *   wbg_scan_finalize  calculators/static.py:131-155 (cumulative Fermi scan, /V /nk * factor)
+ */
+#ifndef WBGPU_H
+#define WBGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WBG_ABI_VERSION 1
+
+#define WBG_STATUS_OK 0
+#define WBG_STATUS_BAD_ARGUMENT 1
+#define WBG_STATUS_TOO_LARGE 2
+#define WBG_STATUS_CUDA_ERROR 3
+#define WBG_STATUS_NO_CONVERGENCE 4
+#define WBG_STATUS_WORKSPACE_TOO_SMALL 5
+
+/* Geometry of one R -> k transform launch.  R-vectors are sorted by (R0, R1, R2);
+ * a "pair" is a run of equal (R0, R1), a "slice" a run of pairs with equal R0. */
+typedef struct {
+  int nR, nw, nw2, nBase; /* R-vectors, Wannier functions, nw*nw, base fields in XR      */
+  int nP, nU;             /* number of (R0,R1) pairs and of R0 slices                    */
+  int N0, N1, N2, nk;     /* FFT block grid and nk = N0*N1*N2                            */
+  int nr0, nr1, nr2;      /* widths of the per-axis phase tables                         */
+  int rmin0, rmin1, rmin2;/* smallest R component per axis (phase table offset)          */
+  int maxPairLen, maxSliceLen;
+} wbg_r2k_geom;
+
+/* Real lattice, rows are lattice vectors (Angstrom): R_cart = iR . L */
+typedef struct {
+  double L[9];
+} wbg_lattice;
+
+/* Fermi-level scan (calculators/static.py:53-58): levels EFmin + i*dEF, i < nEF */
+typedef struct {
+  double EFmin, EFmax, dEF, degen_thresh;
+  int nEF;
+  int reserved;
+} wbg_scan;
+
+int wbg_abi_version(void);
+const char* wbg_status_string(int status);
+
+/* ---- stage 1: R -> k --------------------------------------------------------------------
+ * XR          [nBase][nR][nw][nw] complex, R in sorted order, block phase NOT applied
+ * pair_start  [nP+1] first sorted R of each pair;  r2 [nR] third R component
+ * slice_start [nU+1] first pair of each slice;     pair_r1 [nP];  slice_r0 [nU]
+ * ph0/ph1/ph2 [nblocks][N_d][nr_d] complex: exp(2 pi i R_d (j/N_d + dK_d)), R_d = rmin_d + r
+ * field_desc  [nfields][4] int: (kind, base, a, b) -- kind 0: plain transform of `base`;
+ *             1: d/dk_a; 2: d/dk_a d/dk_b; 3: curl component a of d A (A = bases base..base+2);
+ *             4: d/dk_b of that curl.  Derivatives are i (R + t_n - t_m) as in
+ *             fourier/rvectors.py:355-369,487-494, with t = wcc [nw][3] Cartesian.
+ * order       0, 1, 2: highest derivative order the fields use
+ * fields_out  [nblocks*nk][nfields][nw][nw] complex
+ */
+int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int order, int nblocks, int fp64, size_t* bytes);
+int wbg_r2k(const void* XR, const int* pair_start, const int* r2, const int* slice_start, const int* pair_r1,
+            const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, const int* field_desc,
+            int nfields, const void* wcc, int order, int nblocks, int fp64, void* workspace,
+            size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g, const wbg_lattice* lat,
+            void* stream);
+
+/* ---- stage 2: batched Hermitian eigensolver (FP64) --------------------------------------
+ * H: matrix k at H + k*strideH (complex128 elements), symmetrised as 1/2 (H + H^dagger).
+ * E [nk][nw] ascending; U: matrix k at U + k*strideU, column n = eigenvector n.
+ * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
+int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
+int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
+                     void* workspace, size_t workspace_bytes, int* errflag, void* stream);
+
+/* ---- stage 3: U^dagger X U ----------------------------------------------------------------
+ * X [nk][nFin][nw][nw] (precision fp64), U complex128 with stride strideU.
+ * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U, Hermitian part if herm[f]. */
+int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
+               int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);
+
+/* ---- stage 4: Berry curvature traces + Fermi-level histogram ----------------------------
+ * Xbar [nk][nFbar][nw][nw]: velocity dH/dk at iV..iV+2, A at iA..iA+2, rotA at iO..iO+2.
+ * hist [scan.nEF][3] (double) is accumulated (not cleared). */
+int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
+                    const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                    void* stream);
+
+/* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
+int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WBGPU_H */

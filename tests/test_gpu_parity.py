@@ -1,0 +1,128 @@
+"""GPU parity: every stage through the C ABI against the CPU oracle (tolerances in each test).
+
+FP64 path: energies to 1e-10 eV, k-space fields to 1e-12 relative, AHC to 1e-9 relative.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import wb_oracle as O  # noqa: E402
+from wbgpu import models, engine, system as wsys  # noqa: E402
+import wbgpu  # noqa: E402
+
+
+def osys(d):
+    return O.RSystem(d['real_lattice'], d['iRvec'], d['wannier_centers_cart'], d['XX_R'])
+
+
+def maxrel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def c2small():
+    d = models.config_system(2, small=True)
+    s = wsys.System_R.from_dict(d)
+    s.do_ws_dist(3)
+    o = O.RSystem(s.real_lattice, s.iRvec, s.wannier_centers_cart, s._XX_R)
+    return s, o
+
+
+@pytest.mark.parametrize("fp64,tol", [(True, 1e-12), (False, 2e-6)])
+@pytest.mark.parametrize("NKFFT", [(4, 3, 5), (2, 2, 2)])
+def test_r2k_fields(c2small, fp64, tol, NKFFT):
+    s, o = c2small
+    dev = engine.DeviceSystem(s)
+    dKs = np.array([[0.13, -0.21, 0.37], [0.0, 0.0, 0.0]]) / np.array(NKFFT)
+    q = {'V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C'}
+    fields, index, nF, _ = engine.r2k(dev, dKs, NKFFT, q, True, fp64)
+    f = fields.cpu().numpy()
+    nk = int(np.prod(NKFFT))
+    for ib, dK in enumerate(dKs):
+        data = O.DataK(o, NKFFT, dK)
+        fb = f[ib * nk:(ib + 1) * nk]
+        checks = {'H': data.R_to_k(data.get_R_mat('Ham'), 0, hermitian=False)[..., None],
+                  'V': data.R_to_k(data.get_R_mat('Ham'), 1, hermitian=False),
+                  'W': data.R_to_k(data.get_R_mat('Ham'), 2, hermitian=False).reshape(nk, s.num_wann, s.num_wann, 9),
+                  'A': data.R_to_k(data.get_R_mat('AA'), 0, hermitian=False),
+                  'dA': data.R_to_k(data.get_R_mat('AA'), 1, hermitian=False).reshape(nk, s.num_wann, s.num_wann, 9),
+                  'O': data.R_to_k(data.get_R_mat('rotAA'), 0, hermitian=False),
+                  'dO': data.R_to_k(data.get_R_mat('rotAA'), 1, hermitian=False).reshape(nk, s.num_wann, s.num_wann, 9),
+                  'B': data.R_to_k(data.get_R_mat('BB'), 0, hermitian=False),
+                  'C': data.R_to_k(data.get_R_mat('CC'), 0, hermitian=False)}
+        for name, ref in checks.items():
+            n = ref.shape[-1]
+            got = np.moveaxis(fb[:, index[name]:index[name] + n], 1, -1)
+            assert maxrel(got, ref) < tol, (name, ib, maxrel(got, ref))
+
+
+@pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
+def test_eigh_random(nw):
+    rng = np.random.default_rng(nw)
+    nk = 300
+    H = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
+    H = H + H.conj().swapaxes(1, 2)
+    # planted degeneracies / near-degeneracies in part of the batch
+    for k in range(0, nk, 7):
+        w, v = np.linalg.eigh(H[k])
+        w[: nw // 2] = np.round(w[: nw // 2], 1)
+        if nw > 2:
+            w[1] = w[0] + 1e-9
+        H[k] = (v * w) @ v.conj().T
+    Ht = torch.from_numpy(H).cuda()
+    E, U, flag = engine.eigh(Ht, nw * nw, nw, nk)
+    torch.cuda.synchronize()
+    assert int(flag.item()) == 0
+    E, U = E.cpu().numpy(), U.cpu().numpy()
+    Href = 0.5 * (H + H.conj().swapaxes(1, 2))
+    Eref = np.linalg.eigvalsh(Href)
+    scale = np.abs(Eref).max()
+    assert np.max(np.abs(E - Eref)) < 1e-12 * max(scale, 1) * nw
+    I = np.eye(nw)
+    assert np.max(np.abs(np.einsum('kmi,kmj->kij', U.conj(), U) - I)) < 1e-10
+    R = np.einsum('kmi,kmn,knj->kij', U.conj(), Href, U) - E[:, None, :] * I
+    assert np.max(np.abs(R)) < 1e-11 * max(scale, 1) * nw
+
+
+def test_ahc_golden_random(golden_dir):
+    """The reference's own golden AHC (tests/reference/integrate_files/random-ahc_iter-0000.npz)."""
+    import os
+    f = np.load(os.path.join(golden_dir, 'random_system.npz'))
+    XX = {k[5:]: f[k] for k in f.files if k.startswith('XX_R_')}
+    s = wsys.System_R.from_arrays(f['real_lattice'], f['iRvec'], f['wannier_centers_cart'], XX)
+    ref = np.load(os.path.join(golden_dir, 'random_results.npz'))
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=3), {'ahc': wbgpu.calculators.AHC(Efermi=np.linspace(-2, 2, 5))})
+    got, exp = res['ahc'].data, ref['ahc_data']
+    assert np.max(np.abs(got - exp)) < 1e-8 * np.max(np.abs(exp))
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_ahc_c1(precision, tol):
+    d = models.config_system(1)
+    EF = np.linspace(-2, 2, 501)
+    s = wsys.System_R.from_dict(d)
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=8), {'ahc': wbgpu.calculators.AHC(Efermi=EF)}, precision=precision)
+    ref = O.run(osys(d), (2, 2, 2), (8, 8, 8), {'ahc': O.AHC(Efermi=EF)})
+    assert maxrel(res['ahc'].data, ref['ahc'].data) < tol
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_ahc_c2small_mdrs(c2small, precision, tol):
+    s, o = c2small
+    EF = np.linspace(-2, 2, 201)
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(4, 5, 3)), {'ahc': wbgpu.calculators.AHC(Efermi=EF)},
+                    precision=precision)
+    ref = O.run(o, (2, 2, 2), (4, 5, 3), {'ahc': O.AHC(Efermi=EF)})
+    assert maxrel(res['ahc'].data, ref['ahc'].data) < tol
+
+
+def test_ahc_internal_only(c2small):
+    s, o = c2small
+    EF = np.linspace(-2, 2, 51)
+    kw = dict(kwargs_formula={'external_terms': False})
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=1, NKFFT=4), {'ahc': wbgpu.calculators.AHC(Efermi=EF, **kw)})
+    ref = O.run(o, (1, 1, 1), (4, 4, 4), {'ahc': O.AHC(Efermi=EF, **kw)})
+    assert maxrel(res['ahc'].data, ref['ahc'].data) < 1e-9

@@ -1,0 +1,118 @@
+"""CPU-only checks: the C-ABI library loads and exports every symbol include/wbgpu.h declares,
+and the host-side logic (R-vector structure, phase tables, grids, MDRS) matches the oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import wb_oracle as O
+from wbgpu import models, engine, system as wsys, grid as wgrid, _lib
+
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(REPO, 'include', 'wbgpu.h')).read()
+    return sorted(set(re.findall(r'^\s*(?:int|const char\*|size_t)\s+(wbg_\w+)\s*\(', src, re.M)))
+
+
+def test_header_matches_binding():
+    assert header_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_loads_and_exports():
+    lib = _lib.load()
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    assert lib.wbg_abi_version() == 1
+    assert lib.wbg_status_string(5).decode() == "workspace too small"
+
+
+def test_workspace_queries_without_gpu():
+    import ctypes
+    lib = _lib.load()
+    g = _lib.R2KGeom(nR=10, nw=4, nw2=16, nBase=4, nP=5, nU=3, N0=4, N1=4, N2=4, nk=64, nr0=3, nr1=3, nr2=3,
+                     rmin0=-1, rmin1=-1, rmin2=-1, maxPairLen=3, maxSliceLen=3)
+    b = ctypes.c_size_t(0)
+    assert lib.wbg_r2k_workspace_size(ctypes.byref(g), 1, 2, 1, ctypes.byref(b)) == 0
+    assert b.value > 0
+    assert lib.wbg_r2k_workspace_size(ctypes.byref(g), 3, 2, 1, ctypes.byref(b)) == 1
+    assert lib.wbg_eigh_workspace_size(200, 10, ctypes.byref(b)) == 1
+    with pytest.raises(ValueError):
+        _lib.check(1, "x")
+    with pytest.raises(RuntimeError):
+        _lib.check(3, "x")
+
+
+def test_rgeometry_structure():
+    rng = np.random.default_rng(3)
+    R = np.unique(rng.integers(-3, 4, size=(80, 3)), axis=0)
+    rng.shuffle(R)
+    g = engine.RGeometry(R)
+    Rs = R[g.order]
+    # pairs and slices partition the sorted list exactly
+    for p in range(g.nP):
+        blk = Rs[g.pair_start[p]:g.pair_start[p + 1]]
+        assert np.all(blk[:, :2] == blk[0, :2]) and blk[0, 1] == g.pair_r1[p]
+        assert np.all(np.diff(blk[:, 2]) > 0)
+    for u in range(g.nU):
+        for p in range(g.slice_start[u], g.slice_start[u + 1]):
+            assert Rs[g.pair_start[p], 0] == g.slice_r0[u]
+    assert g.pair_start[-1] == len(R) and g.slice_start[-1] == g.nP
+
+
+def test_separable_phases_reproduce_dft():
+    """The per-axis tables multiply to exp(2 pi i R.(j/N + dK)), the kernel of fft.py:175-180 with expdK."""
+    d = models.config_system(2, small=True)
+    g = engine.RGeometry(d['iRvec'])
+    N = (3, 4, 5)
+    dK = np.array([[0.1, -0.2, 0.3]]) / N
+    ph = g.phases(dK, N)
+    X = d['XX_R']['Ham'][g.order]
+    data = O.DataK(O.RSystem(d['real_lattice'], d['iRvec'], d['wannier_centers_cart'], d['XX_R']), N, dK[0])
+    ref = data.R_to_k(data.get_R_mat('Ham'), 0, hermitian=False)
+    Rs = g.R - g.rmin
+    out = np.zeros_like(ref)
+    for ik, (j0, j1, j2) in enumerate(np.ndindex(*N)):
+        e = ph[0][0, j0, Rs[:, 0]] * ph[1][0, j1, Rs[:, 1]] * ph[2][0, j2, Rs[:, 2]]
+        out[ik] = np.einsum('r,rmn->mn', e, X)
+    assert np.max(np.abs(out - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_grid_block_shifts_match_reference_layout():
+    g = wgrid.Grid(NKdiv=(2, 3, 1), NKFFT=(4, 4, 6))
+    assert np.allclose(g.block_shifts(), O.block_shifts((2, 3, 1), (4, 4, 6)))
+    assert g.nblocks == 6 and g.nk_per_block == 96
+
+
+def test_mdrs_matches_oracle():
+    d = models.config_system(2, small=True)
+    s = wsys.System_R.from_dict(d).do_ws_dist(3)
+    o = O.do_ws_dist(O.RSystem(d['real_lattice'], d['iRvec'], d['wannier_centers_cart'], d['XX_R']), (3, 3, 3))
+    idx = {tuple(R): i for i, R in enumerate(s.iRvec)}
+    assert len(idx) == len(o.iRvec)
+    perm = np.array([idx[tuple(R)] for R in o.iRvec])
+    for k in o.XX_R:
+        assert np.max(np.abs(s._XX_R[k][perm] - o.XX_R[k])) == 0.0
+
+
+def test_set_R_mat_hermitian_and_errors():
+    d = models.config_system(1, small=True)
+    s = wsys.System_R(real_lattice=d['real_lattice'], iRvec=d['iRvec'], wannier_centers_cart=None, num_wann=4)
+    X = np.random.default_rng(0).standard_normal((s.nRvec, 4, 4)) + 0j
+    s.set_R_mat('Ham', X, Hermitian=True)
+    H = s.get_R_mat('Ham')
+    assert np.allclose(H, s.conj_XX_R(H))
+    with pytest.raises(RuntimeError):
+        s.set_R_mat('Ham', X)
+    with pytest.raises(ValueError):
+        s.get_R_mat('AA')
+
+
+def test_field_plan_layout():
+    desc, index = engine.field_plan({'V', 'A', 'O'}, True, ['AA'])
+    assert index == {'H': 0, 'V': 1, 'A': 4, 'O': 7}
+    assert desc[0] == (0, 0, 0, 0) and desc[1] == (1, 0, 0, 0) and desc[7] == (3, 1, 0, 0)
+    assert engine.order_for({'V', 'A', 'O'}) == 1 and engine.order_for({'W'}) == 2

@@ -1,0 +1,70 @@
+// C ABI entry points (declared in include/wbgpu.h).  Thin argument checks around the
+// stage launchers; no entry point allocates memory.
+#include "wbgpu_common.cuh"
+#include "wbgpu_r2k.cuh"
+#include "wbgpu_eigh.cuh"
+#include "wbgpu_band.cuh"
+
+extern "C" {
+
+int wbg_abi_version(void) { return WBG_ABI_VERSION; }
+
+const char* wbg_status_string(int status) {
+  switch (status) {
+    case WBG_STATUS_OK: return "ok";
+    case WBG_STATUS_BAD_ARGUMENT: return "bad argument";
+    case WBG_STATUS_TOO_LARGE: return "problem size exceeds kernel limits";
+    case WBG_STATUS_CUDA_ERROR: return "CUDA error";
+    case WBG_STATUS_NO_CONVERGENCE: return "eigensolver did not converge";
+    case WBG_STATUS_WORKSPACE_TOO_SMALL: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int order, int nblocks, int fp64, size_t* bytes) {
+  if (!g || !bytes || order < 0 || order > 2 || nblocks < 1) return WBG_STATUS_BAD_ARGUMENT;
+  *bytes = wbg_r2k_workspace_bytes(g, order, nblocks, fp64);
+  return WBG_STATUS_OK;
+}
+
+int wbg_r2k(const void* XR, const int* pair_start, const int* r2, const int* slice_start, const int* pair_r1,
+            const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, const int* field_desc,
+            int nfields, const void* wcc, int order, int nblocks, int fp64, void* workspace,
+            size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g, const wbg_lattice* lat,
+            void* stream) {
+  if (!XR || !pair_start || !r2 || !slice_start || !pair_r1 || !slice_r0 || !ph0 || !ph1 || !ph2 || !field_desc ||
+      !wcc || !workspace || !fields_out || !g || !lat)
+    return WBG_STATUS_BAD_ARGUMENT;
+  return wbg_r2k_run(XR, pair_start, r2, slice_start, pair_r1, slice_r0, ph0, ph1, ph2,
+                     reinterpret_cast<const int4*>(field_desc), wcc, workspace, workspace_bytes, fields_out, g, order,
+                     nfields, lat, nblocks, fp64, (cudaStream_t)stream);
+}
+
+int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes) {
+  if (!bytes || nw < 1 || nw > WBG_EIGH_NMAX || nk < 1) return WBG_STATUS_BAD_ARGUMENT;
+  *bytes = wbg_eigh_workspace_bytes(nw, nk);
+  return WBG_STATUS_OK;
+}
+
+int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
+                     void* workspace, size_t workspace_bytes, int* errflag, void* stream) {
+  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, workspace, workspace_bytes, errflag, (cudaStream_t)stream);
+}
+
+int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
+               int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream) {
+  return wbg_rotate_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, fp64, (cudaStream_t)stream);
+}
+
+int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
+                    const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                    void* stream) {
+  return wbg_berry_omega_run(E, Xbar, nFbar, iV, iA, iO, nw, nk, scan, internal_terms, external_terms, hist, fp64,
+                             (cudaStream_t)stream);
+}
+
+int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream) {
+  return wbg_scan_finalize_run(hist, nEF, ncomp, scale, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,13 @@
+// Internal declarations of the band-basis stages (see wbgpu_band.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/wbgpu.h"
+
+typedef wbg_scan WbgScan;
+
+int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
+                   int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream);
+int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
+                        const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
+                        cudaStream_t stream);
+int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);

@@ -1,0 +1,367 @@
+// Batched Hermitian eigensolver in FP64 (stage 2 of the path): H(k) -> E_K (ascending), UU_K.
+//
+// Replaces np.linalg.eigh in data_K/data_K.py:211-218 (E_K, UU_K) applied to
+// HH_K = 1/2 (H + H^dagger) (fourier/fft.py:183-186, data_K/data_K_R.py:24-26).
+//
+// GB300 runs FP64 at ~1.9 DFMA/clk/SM and a warp instruction costs the same whether
+// one lane or 32 lanes are active, so each phase is mapped so that every lane does
+// useful FP64 work:
+//   1. eigh_tridiag : Householder reduction to real tridiagonal T = Q^dagger H Q,
+//                     one group of L lanes per matrix, lane owns rows (shared memory).
+//   2. eigh_ql      : implicit QL (Wilkinson shift) eigenvalues of T, one thread per matrix.
+//   3. eigh_vectors : inverse iteration on T (partial-pivot LU), one lane per eigenvector,
+//                     modified Gram-Schmidt inside clusters, back-transform by the
+//                     Householder reflectors (U = Q Z).
+#include <float.h>
+#include "wbgpu_common.cuh"
+#include "wbgpu_eigh.cuh"
+
+namespace {
+
+WBG_D double group_sum(double v, int L) {
+  for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// ---------------------------------------------------------------------------------------
+// 1. Householder tridiagonalisation.  grid: ceil(nk/G) blocks of G*L threads.
+// Outputs: Vh[k][c][i] (v of reflector c, v_{c+1}=1, zeros for i<=c), tau[k][c],
+//          d[k][i], e[k][i] (e[n-1] = 0).
+// ---------------------------------------------------------------------------------------
+__global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, int n, int nk, int L, int G,
+                             double2* __restrict__ Vh, double2* __restrict__ tauOut, double* __restrict__ dOut,
+                             double* __restrict__ eOut) {
+  extern __shared__ double2 sm[];
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  long long k = (long long)blockIdx.x * G + grp;
+  const bool valid = k < nk;
+  if (!valid) k = nk - 1;  // redundant work keeps every lane of the warp in the same control flow
+  double2* A = sm + (size_t)grp * (n * n + 2 * n);
+  double2* vs = A + n * n;
+  double2* ws = vs + n;
+  const double2* Hk = H + k * strideK;
+  for (int idx = lane; idx < n * n; idx += L) {
+    const int i = idx / n, j = idx % n;
+    const double2 a = Hk[i * n + j], b = Hk[j * n + i];
+    A[idx] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+  }
+  __syncwarp();
+  for (int c = 0; c < n - 1; ++c) {
+    double xn = 0.0;
+    for (int i = lane; i < n; i += L)
+      if (i >= c + 2) { const double2 x = A[i * n + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
+    xn = group_sum(xn, L);
+    const double2 alpha = A[(c + 1) * n + c];
+    double beta, tr = 0.0, ti = 0.0;
+    double2 scale = make_double2(0.0, 0.0);
+    if (xn == 0.0 && alpha.y == 0.0) {
+      beta = alpha.x;  // H = I
+    } else {
+      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
+      beta = alpha.x >= 0.0 ? -nrm : nrm;
+      tr = (beta - alpha.x) / beta;
+      ti = -alpha.y / beta;
+      // scale = 1 / (alpha - beta)
+      const double ar = alpha.x - beta, ai = alpha.y;
+      const double den = ar * ar + ai * ai;
+      scale = make_double2(ar / den, -ai / den);
+    }
+    const double2 tau = make_double2(tr, ti);
+    // executed unconditionally (tau = 0 makes it a no-op) so that every lane of the warp
+    // reaches the same __syncwarp / shuffle calls when several matrices share a warp
+    {
+      for (int i = lane; i < n; i += L) {
+        if (i == c + 1) { vs[i] = make_double2(1.0, 0.0); A[i * n + c] = vs[i]; }
+        else if (i >= c + 2) { const double2 v = cmul(A[i * n + c], scale); vs[i] = v; A[i * n + c] = v; }
+      }
+      __syncwarp();
+      // p = tau * A v ; partial dot w^dagger v
+      double dr = 0.0, di = 0.0;
+      for (int i = lane; i < n; i += L) {
+        if (i >= c + 1) {
+          double2 acc = make_double2(0.0, 0.0);
+          for (int j = c + 1; j < n; ++j) cfma(acc, A[i * n + j], vs[j]);
+          const double2 p = cmul(tau, acc);
+          ws[i] = p;
+          const double2 v = vs[i];
+          dr = fma(p.x, v.x, fma(p.y, v.y, dr));  // conj(p) v
+          di = fma(p.x, v.y, fma(-p.y, v.x, di));
+        }
+      }
+      dr = group_sum(dr, L);
+      di = group_sum(di, L);
+      // alpha2 = -1/2 tau (w^dagger v)
+      const double2 a2 = cscale(cmul(tau, make_double2(dr, di)), -0.5);
+      for (int i = lane; i < n; i += L)
+        if (i >= c + 1) cfma(ws[i], a2, vs[i]);
+      __syncwarp();
+      for (int i = lane; i < n; i += L) {
+        if (i >= c + 1) {
+          const double2 vi = vs[i], wi = ws[i];
+          for (int j = c + 1; j < n; ++j) {
+            double2 a = A[i * n + j];
+            const double2 vj = vs[j], wj = ws[j];
+            // a -= v_i conj(w_j) + w_i conj(v_j)
+            a.x -= vi.x * wj.x + vi.y * wj.y + wi.x * vj.x + wi.y * vj.y;
+            a.y -= vi.y * wj.x - vi.x * wj.y + wi.y * vj.x - wi.x * vj.y;
+            A[i * n + j] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (valid) {
+      for (int i = lane; i < n; i += L) {
+        double2 v = make_double2(0.0, 0.0);
+        if (tr != 0.0 || ti != 0.0) { if (i >= c + 1) v = A[i * n + c]; }
+        Vh[(k * n + c) * n + i] = v;
+      }
+      if (lane == 0) {
+        tauOut[k * n + c] = tau;
+        eOut[k * n + c] = beta;
+        dOut[k * n + c] = A[c * n + c].x;
+      }
+    }
+    __syncwarp();
+  }
+  if (valid && lane == 0) {
+    dOut[k * n + n - 1] = A[(n - 1) * n + n - 1].x;
+    eOut[k * n + n - 1] = 0.0;
+    tauOut[k * n + n - 1] = make_double2(0.0, 0.0);
+  }
+  if (valid)
+    for (int i = lane; i < n; i += L) Vh[(k * n + n - 1) * n + i] = make_double2(0.0, 0.0);
+}
+
+// ---------------------------------------------------------------------------------------
+// 2. Implicit QL eigenvalues of the real symmetric tridiagonal (d, e), thread per matrix.
+// ---------------------------------------------------------------------------------------
+__global__ void eigh_ql(const double* __restrict__ dIn, const double* __restrict__ eIn, int n, int nk,
+                        double* __restrict__ Eout, int* __restrict__ errflag) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  double d[WBG_EIGH_NMAX], e[WBG_EIGH_NMAX];
+  for (int i = 0; i < n; ++i) { d[i] = dIn[k * n + i]; e[i] = eIn[k * n + i]; }
+  e[n - 1] = 0.0;
+  bool ok = true;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0, m;
+    do {
+      for (m = l; m < n - 1; ++m) {
+        const double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= DBL_EPSILON * dd) break;
+      }
+      if (m != l) {
+        if (iter++ >= 60) { ok = false; break; }
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double r = hypot(g, 1.0);
+        g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i;
+        bool underflow = false;
+        for (i = m - 1; i >= l; --i) {
+          double f = s * e[i];
+          const double b = c * e[i];
+          r = hypot(f, g);
+          e[i + 1] = r;
+          if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; underflow = true; break; }
+          s = f / r;
+          c = g / r;
+          g = d[i + 1] - p;
+          r = (d[i] - g) * s + 2.0 * c * b;
+          p = s * r;
+          d[i + 1] = g + p;
+          g = c * r - b;
+        }
+        if (underflow) continue;
+        d[l] -= p;
+        e[l] = g;
+        e[m] = 0.0;
+      }
+    } while (m != l);
+    if (!ok) break;
+  }
+  if (!ok) atomicOr(errflag, WBG_FLAG_QL_NOCONV);
+  // ascending insertion sort
+  for (int i = 1; i < n; ++i) {
+    const double x = d[i];
+    int j = i - 1;
+    while (j >= 0 && d[j] > x) { d[j + 1] = d[j]; --j; }
+    d[j + 1] = x;
+  }
+  for (int i = 0; i < n; ++i) Eout[k * n + i] = d[i];
+}
+
+WBG_D double hash_uniform(unsigned int a, unsigned int b) {
+  unsigned int h = a * 2654435761u ^ (b + 0x9e3779b9u + (a << 6) + (a >> 2));
+  h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15; h *= 0x846ca68bu; h ^= h >> 16;
+  return (double)(h & 0xffffff) / (double)0x800000 - 1.0;  // [-1, 1)
+}
+
+// ---------------------------------------------------------------------------------------
+// 3. Eigenvectors: inverse iteration on T, clusters re-orthogonalised, U = Q Z.
+// grid: ceil(nk/G) blocks of G*L threads; lane j computes eigenvectors j, j+L, ...
+// Shared memory per group: U[n][n] complex; the real inverse-iteration vectors Z live in
+// the real parts of U (Z(i,j) = U[i][j].x) until the back-transform turns them complex.
+// ---------------------------------------------------------------------------------------
+__global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __restrict__ tauIn,
+                             const double* __restrict__ dIn, const double* __restrict__ eIn,
+                             const double* __restrict__ E, int n, int nk, int L, int G, double2* __restrict__ Uout,
+                             long long strideU) {
+  extern __shared__ double sme[];
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  long long k = (long long)blockIdx.x * G + grp;
+  const bool valid = k < nk;
+  if (!valid) k = nk - 1;
+  double2* Us = reinterpret_cast<double2*>(sme + (size_t)grp * (2 * n * n + 3 * n));  // [i][j]
+  double* Zs = reinterpret_cast<double*>(Us);  // Z(i, j) = Zs[2 * (i * n + j)]
+  double* ds = Zs + 2 * n * n;
+  double* es = ds + n;
+  double* lam = es + n;
+  for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = E[k * n + i]; }
+  __syncwarp();
+  // matrix scale for tiny-pivot replacement and cluster tolerance
+  double tnorm = 0.0;
+  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(ds[i]) + fabs(es[i]) + (i > 0 ? fabs(es[i - 1]) : 0.0));
+  tnorm = fmax(tnorm, DBL_MIN);
+  const double tiny = DBL_EPSILON * tnorm;
+  const double ortol = 1e-5 * tnorm;
+  const double pertol = 10.0 * DBL_EPSILON * tnorm;
+  double u0[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
+  unsigned char piv[WBG_EIGH_NMAX];
+  for (int j = lane; j < n; j += L) {
+    // shift, separated from a numerically equal lower neighbour
+    double shift = lam[j];
+    for (int jj = j - 1; jj >= 0 && shift - lam[jj] < pertol; --jj) shift = lam[jj] + pertol * (j - jj);
+    // LU with partial pivoting of T - shift I
+    double ca = ds[0] - shift, cb = n > 1 ? es[0] : 0.0;
+    for (int i = 0; i < n - 1; ++i) {
+      const double ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : 0.0;
+      if (fabs(ca) >= fabs(ci)) {
+        if (ca == 0.0) ca = tiny;
+        const double mlt = ci / ca;
+        u0[i] = ca; u1[i] = cb; u2[i] = 0.0; lm[i] = mlt; piv[i] = 0;
+        ca = ai1 - mlt * cb;
+        cb = bi1;
+      } else {
+        const double mlt = ca / ci;
+        u0[i] = ci; u1[i] = ai1; u2[i] = bi1; lm[i] = mlt; piv[i] = 1;
+        ca = cb - mlt * ai1;
+        cb = -mlt * bi1;
+      }
+    }
+    if (fabs(ca) < tiny) ca = ca >= 0.0 ? tiny : -tiny;
+    u0[n - 1] = ca;
+    for (int i = 0; i < n - 1; ++i)
+      if (fabs(u0[i]) < tiny) u0[i] = u0[i] >= 0.0 ? tiny : -tiny;
+    for (int i = 0; i < n; ++i) x[i] = hash_uniform((unsigned)j + 1u, (unsigned)i + 7u);
+    for (int it = 0; it < 3; ++it) {
+      // forward: apply the row operations to the right-hand side
+      double rp = x[0];
+      for (int i = 0; i < n - 1; ++i) {
+        const double y1 = x[i + 1];
+        if (piv[i] == 0) { x[i] = rp; rp = y1 - lm[i] * rp; }
+        else { x[i] = y1; rp = rp - lm[i] * y1; }
+      }
+      x[n - 1] = rp;
+      // back substitution
+      x[n - 1] = x[n - 1] / u0[n - 1];
+      if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) / u0[n - 2];
+      for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) / u0[i];
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
+      nrm = 1.0 / sqrt(nrm);
+      for (int i = 0; i < n; ++i) x[i] *= nrm;
+    }
+    for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] = x[i];
+  }
+  __syncwarp();
+  // modified Gram-Schmidt inside clusters (eigenvalues closer than ortol), in eigenvalue order
+  bool anyc = false;
+  for (int j = 1; j < n; ++j) anyc |= (lam[j] - lam[j - 1] < ortol);
+  anyc = __any_sync(0xffffffffu, anyc);  // warp-uniform: groups sharing a warp run the same loop
+  if (anyc) {
+    for (int jp = 0; jp < n - 1; ++jp) {
+      for (int j = lane; j < n; j += L) {
+        if (j > jp) {
+          bool same = true;
+          for (int q = jp + 1; q <= j; ++q) same &= (lam[q] - lam[q - 1] < ortol);
+          if (same) {
+            double dot = 0.0;
+            for (int i = 0; i < n; ++i) dot = fma(Zs[2 * (i * n + jp)], Zs[2 * (i * n + j)], dot);
+            for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] -= dot * Zs[2 * (i * n + jp)];
+            if (j == jp + 1) {
+              double nrm = 0.0;
+              for (int i = 0; i < n; ++i) nrm = fma(Zs[2 * (i * n + j)], Zs[2 * (i * n + j)], nrm);
+              nrm = 1.0 / sqrt(nrm);
+              for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] *= nrm;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // back-transform: u = H_0 H_1 ... H_{n-2} z
+  for (int j = lane; j < n; j += L) {
+    for (int i = 0; i < n; ++i) Us[i * n + j].y = 0.0;
+    for (int c = n - 2; c >= 0; --c) {
+      const double2 tau = tauIn[k * n + c];
+      if (tau.x == 0.0 && tau.y == 0.0) continue;
+      const double2* v = Vh + (k * n + c) * n;
+      double2 s = make_double2(0.0, 0.0);
+      for (int i = c + 1; i < n; ++i) cfmac(s, v[i], Us[i * n + j]);
+      const double2 ts = cmul(tau, s);
+      for (int i = c + 1; i < n; ++i) {
+        double2 u = Us[i * n + j];
+        const double2 vv = v[i];
+        u.x -= vv.x * ts.x - vv.y * ts.y;
+        u.y -= vv.x * ts.y + vv.y * ts.x;
+        Us[i * n + j] = u;
+      }
+    }
+  }
+  __syncwarp();
+  if (valid)
+    for (int idx = lane; idx < n * n; idx += L) Uout[k * strideU + idx] = Us[idx];
+}
+
+int lanes_for(int n) {
+  int L = 1;
+  while (L < n && L < 32) L <<= 1;
+  return L < 4 ? 4 : L;
+}
+
+}  // namespace
+
+size_t wbg_eigh_workspace_bytes(int n, int nk) {
+  // Vh (n*n complex) + tau (n complex) + d, e (n real each) per matrix
+  return (size_t)nk * ((size_t)n * n * 16 + (size_t)n * 16 + 2 * (size_t)n * 8) + 1024;
+}
+
+int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU,
+                 void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
+  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
+  if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
+  char* w = (char*)workspace;
+  double2* Vh = (double2*)w; w += (size_t)nk * n * n * 16;
+  double2* tau = (double2*)w; w += (size_t)nk * n * 16;
+  double* d = (double*)w; w += (size_t)nk * n * 8;
+  double* e = (double*)w;
+  const int L = lanes_for(n);
+  const size_t smT = ((size_t)n * n + 2 * n) * sizeof(double2);
+  int G = (4 * 32) / L;
+  while (G > 1 && G * smT > 96 * 1024) G /= 2;
+  if (G * smT > 220 * 1024) return WBG_ERR_SIZE;
+  cudaFuncSetAttribute(eigh_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  eigh_tridiag<<<(nk + G - 1) / G, G * L, G * smT, stream>>>((const double2*)H, strideH, n, nk, L, G, Vh, tau, d, e);
+  eigh_ql<<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
+  const size_t smV = (2 * (size_t)n * n + 3 * n) * sizeof(double);
+  int GV = (2 * 32) / L;
+  while (GV > 1 && GV * smV > 96 * 1024) GV /= 2;
+  if (GV * smV > 220 * 1024) return WBG_ERR_SIZE;
+  cudaFuncSetAttribute(eigh_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  eigh_vectors<<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
+                                                                 (double2*)U, strideU);
+  return wbg_cuda_status(cudaGetLastError());
+}

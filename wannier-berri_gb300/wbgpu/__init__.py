@@ -1,0 +1,13 @@
+"""wbgpu: GB300-native (sm_103a) Wannier-interpolation backend.
+
+Host-side mirror of the reference interface for the hot path -- ``System_R``,
+``Grid``, ``run`` and the calculators -- over hand-written CUDA kernels reached
+through the C ABI of libwbgpu.so (include/wbgpu.h).
+"""
+from .system import System_R
+from .grid import Grid
+from .run import run
+from . import calculators, models, engine
+from .result import EnergyResult, ResultDict
+
+__all__ = ['System_R', 'Grid', 'run', 'calculators', 'models', 'engine', 'EnergyResult', 'ResultDict']

@@ -1,0 +1,85 @@
+"""ctypes binding of libwbgpu.so (C ABI declared in include/wbgpu.h).
+
+Status codes are turned into the exception types the reference raises for the same
+kind of failure: ValueError for bad arguments / sizes, RuntimeError for CUDA errors
+and eigensolver non-convergence (the reference raises RuntimeError for numerical
+failures, e.g. data_K/data_K.py:239-241).
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_workspace_size', 'wbg_r2k',
+           'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_rotate', 'wbg_berry_omega',
+           'wbg_scan_finalize']
+
+STATUS_OK = 0
+
+
+class R2KGeom(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in
+                ['nR', 'nw', 'nw2', 'nBase', 'nP', 'nU', 'N0', 'N1', 'N2', 'nk', 'nr0', 'nr1', 'nr2',
+                 'rmin0', 'rmin1', 'rmin2', 'maxPairLen', 'maxSliceLen']]
+
+
+class Lattice(ctypes.Structure):
+    _fields_ = [('L', ctypes.c_double * 9)]
+
+
+class Scan(ctypes.Structure):
+    _fields_ = [('EFmin', ctypes.c_double), ('EFmax', ctypes.c_double), ('dEF', ctypes.c_double),
+                ('degen_thresh', ctypes.c_double), ('nEF', ctypes.c_int), ('reserved', ctypes.c_int)]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
+_SZ = ctypes.c_size_t
+
+_SIGS = {
+    'wbg_abi_version': (_I, []),
+    'wbg_status_string': (ctypes.c_char_p, [_I]),
+    'wbg_r2k_workspace_size': (_I, [ctypes.POINTER(R2KGeom), _I, _I, _I, ctypes.POINTER(_SZ)]),
+    'wbg_r2k': (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _P, _SZ, _P,
+                     ctypes.POINTER(R2KGeom), ctypes.POINTER(Lattice), _P]),
+    'wbg_eigh_workspace_size': (_I, [_I, _I, ctypes.POINTER(_SZ)]),
+    'wbg_eigh_batched': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _P, _SZ, _P, _P]),
+    'wbg_rotate': (_I, [_P, _LL, _P, _I, _P, _P, _I, _P, _I, _I, _I, _P]),
+    'wbg_berry_omega': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),
+    'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
+}
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=True):
+    """Load libwbgpu.so; build it first if it is missing (needs nvcc)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"libwbgpu.so not built at {path}")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, what):
+    if status == STATUS_OK:
+        return
+    msg = load().wbg_status_string(status).decode()
+    if status in (1, 2, 5):
+        raise ValueError(f"{what}: {msg} (status {status})")
+    raise RuntimeError(f"{what}: {msg} (status {status})")

@@ -1,0 +1,318 @@
+"""GPU engine: R-space matrices resident on the device, one pipeline launch per batch of
+FFT blocks: R->k fields (wbg_r2k) -> eigh (wbg_eigh_batched) -> U^dagger X U (wbg_rotate).
+
+The band-basis data it produces (``BandData``) is what the reference's ``Data_K``
+hands to its formulae (data_K/data_K.py:211-334): E_K, UU_K and the rotated
+matrices Xbar(name, der).  Device memory comes from PyTorch; every kernel runs in
+libwbgpu.so through the C ABI.  There is no CPU fallback: without a CUDA device or
+without the library every entry point raises.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+# quantity -> (base kind, r2k kind, components, hermitian after rotation, derivative order)
+#   V  = Xbar('Ham', 1)   W = Xbar('Ham', 2)   A = Xbar('AA')    dA = Xbar('AA', 1)
+#   O  = Xbar('rotAA')    dO = Xbar('rotAA', 1)   B = Xbar('BB')   C = Xbar('CC')
+QUANTITIES = {
+    'V': dict(order=1, herm=0, ncomp=3),
+    'W': dict(order=2, herm=0, ncomp=9),
+    'A': dict(order=0, herm=1, ncomp=3),
+    'dA': dict(order=1, herm=1, ncomp=9),
+    'O': dict(order=1, herm=1, ncomp=3),
+    'dO': dict(order=2, herm=1, ncomp=9),
+    'B': dict(order=0, herm=0, ncomp=3),
+    'C': dict(order=0, herm=0, ncomp=3),
+}
+QUANTITY_ORDER = ['V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C']
+MOM0, DER1, DER2, ROT, DROT = 0, 1, 2, 3, 4
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("wbgpu needs a CUDA device (sm_103a); no CPU fallback exists")
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class RGeometry:
+    """Sorted R-vector structure for the pruned separable R->k transform."""
+
+    def __init__(self, iRvec):
+        iRvec = np.asarray(iRvec, dtype=np.int64)
+        self.order = np.lexsort((iRvec[:, 2], iRvec[:, 1], iRvec[:, 0]))
+        R = iRvec[self.order]
+        self.R = R
+        new_pair = np.ones(len(R), dtype=bool)
+        new_pair[1:] = np.any(R[1:, :2] != R[:-1, :2], axis=1)
+        self.pair_start = np.append(np.nonzero(new_pair)[0], len(R)).astype(np.int32)
+        pairs = R[self.pair_start[:-1]]
+        new_slice = np.ones(len(pairs), dtype=bool)
+        new_slice[1:] = pairs[1:, 0] != pairs[:-1, 0]
+        self.slice_start = np.append(np.nonzero(new_slice)[0], len(pairs)).astype(np.int32)
+        self.pair_r1 = pairs[:, 1].astype(np.int32)
+        self.slice_r0 = pairs[self.slice_start[:-1], 0].astype(np.int32)
+        self.r2 = R[:, 2].astype(np.int32)
+        self.rmin = R.min(axis=0)
+        self.nr = R.max(axis=0) - self.rmin + 1
+        self.nP = len(pairs)
+        self.nU = len(self.slice_r0)
+        self.maxPairLen = int(np.diff(self.pair_start).max())
+        self.maxSliceLen = int(np.diff(self.slice_start).max())
+
+    def phases(self, dKs, NKFFT):
+        """Per-axis tables exp(2 pi i R_d (j/N_d + dK_d)) for every block: list of 3 arrays
+        (nblocks, N_d, nr_d) complex128 (rvectors.py:467-468 with the FFT kernel of fft.py:179)."""
+        dKs = np.atleast_2d(dKs)
+        out = []
+        for d in range(3):
+            Rd = self.rmin[d] + np.arange(self.nr[d])
+            k = np.arange(NKFFT[d])[None, :] / NKFFT[d] + dKs[:, d][:, None]     # (nb, N)
+            out.append(np.exp(2j * np.pi * k[:, :, None] * Rd[None, None, :]))
+        return out
+
+
+class DeviceSystem:
+    """R-space matrices of one system resident on the GPU (uploaded once)."""
+
+    def __init__(self, system, device='cuda'):
+        require_cuda()
+        _lib.load()
+        self.system = system
+        self.device = torch.device(device)
+        self.nw = system.num_wann
+        self.geom = RGeometry(system.iRvec)
+        self.lattice = np.array(system.real_lattice, dtype=float)
+        self.wcc = np.array(system.wannier_centers_cart, dtype=float)
+        self._bases = {}
+        self._cache = {}
+
+    def bases_for(self, keys):
+        """Base-field list for the R->k launch: Ham, then 3 components of each extra key."""
+        names = [('Ham', None)]
+        for key in keys:
+            if key != 'Ham':
+                names += [(key, c) for c in range(3)]
+        return names
+
+    def XR(self, names, fp64):
+        ck = (tuple(names), fp64)
+        if ck not in self._cache:
+            order = self.geom.order
+            arrs = []
+            for key, c in names:
+                X = self.system.get_R_mat(key)
+                arrs.append(X[order] if c is None else X[order][..., c])
+            a = np.stack(arrs).reshape(len(names), len(order), self.nw * self.nw)
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+            self._cache[ck] = t if fp64 else t.to(torch.complex64)
+        return self._cache[ck]
+
+    def geom_tensors(self):
+        if 'geom' not in self._cache:
+            g = self.geom
+            mk = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).to(self.device)
+            self._cache['geom'] = dict(pair_start=mk(g.pair_start), r2=mk(g.r2), slice_start=mk(g.slice_start),
+                                       pair_r1=mk(g.pair_r1), slice_r0=mk(g.slice_r0))
+        return self._cache['geom']
+
+    def wcc_tensor(self, fp64):
+        k = ('wcc', fp64)
+        if k not in self._cache:
+            self._cache[k] = torch.tensor(self.wcc, dtype=torch.float64 if fp64 else torch.float32,
+                                          device=self.device).contiguous()
+        return self._cache[k]
+
+
+def field_plan(quantities, with_H, extra_keys):
+    """Field descriptors (kind, base, a, b) for the requested quantities.
+    Bases: 0 = Ham, then AA x/y/z, then BB x/y/z, CC x/y/z as present in ``extra_keys``."""
+    base_of = {'Ham': 0}
+    nb = 1
+    for key in extra_keys:
+        base_of[key] = nb
+        nb += 3
+    desc, index = [], {}
+    if with_H:
+        index['H'] = 0
+        desc.append((MOM0, 0, 0, 0))
+    for q in QUANTITY_ORDER:
+        if q not in quantities:
+            continue
+        index[q] = len(desc)
+        if q == 'V':
+            desc += [(DER1, 0, a, 0) for a in range(3)]
+        elif q == 'W':
+            desc += [(DER2, 0, a, b) for a in range(3) for b in range(3)]
+        elif q == 'A':
+            desc += [(MOM0, base_of['AA'] + b, 0, 0) for b in range(3)]
+        elif q == 'dA':
+            desc += [(DER1, base_of['AA'] + b, d, 0) for b in range(3) for d in range(3)]
+        elif q == 'O':
+            desc += [(ROT, base_of['AA'], g, 0) for g in range(3)]
+        elif q == 'dO':
+            desc += [(DROT, base_of['AA'], g, d) for g in range(3) for d in range(3)]
+        elif q == 'B':
+            desc += [(MOM0, base_of['BB'] + a, 0, 0) for a in range(3)]
+        elif q == 'C':
+            desc += [(MOM0, base_of['CC'] + a, 0, 0) for a in range(3)]
+    return desc, index
+
+
+def extra_keys_for(quantities):
+    keys = []
+    if quantities & {'A', 'dA', 'O', 'dO'}:
+        keys.append('AA')
+    if 'B' in quantities:
+        keys.append('BB')
+    if 'C' in quantities:
+        keys.append('CC')
+    return keys
+
+
+def order_for(quantities):
+    return max([QUANTITIES[q]['order'] for q in quantities] + [0])
+
+
+class BandData:
+    """Band-basis data of a batch of FFT blocks (the reference Data_K content).
+
+    E: (nk_tot, nw) float64; U: (nk_tot, nw, nw) complex128 (view into ``Ubuf``);
+    Xbar: (nk_tot, nF, nw, nw) complex (float64 or float32 parts); index: quantity -> first field.
+    """
+
+    def __init__(self, E, U, Xbar, index, nblocks, nk, nw, fp64_fields):
+        self.E, self.U, self.Xbar, self.index = E, U, Xbar, index
+        self.nblocks, self.nk, self.nw = nblocks, nk, nw
+        self.fp64_fields = fp64_fields
+
+    @property
+    def nk_total(self):
+        return self.nblocks * self.nk
+
+
+def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
+    """Run the R->k stage for a batch of blocks; returns (fields, index, nF)."""
+    NKFFT = [int(n) for n in NKFFT]
+    keys = extra_keys_for(quantities)
+    names = dev.bases_for(keys)
+    order = order_for(quantities)
+    desc, index = field_plan(quantities, with_H, keys)
+    nF = len(desc)
+    nb = len(dKs)
+    g = dev.geom
+    nw = dev.nw
+    nk = int(np.prod(NKFFT))
+    geo = _lib.R2KGeom(nR=len(g.R), nw=nw, nw2=nw * nw, nBase=len(names), nP=g.nP, nU=g.nU,
+                       N0=NKFFT[0], N1=NKFFT[1], N2=NKFFT[2], nk=nk,
+                       nr0=int(g.nr[0]), nr1=int(g.nr[1]), nr2=int(g.nr[2]),
+                       rmin0=int(g.rmin[0]), rmin1=int(g.rmin[1]), rmin2=int(g.rmin[2]),
+                       maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
+    lat = _lib.Lattice()
+    for i, v in enumerate(dev.lattice.reshape(-1)):
+        lat.L[i] = float(v)
+    lib = _lib.load()
+    ws = ctypes.c_size_t(0)
+    _lib.check(lib.wbg_r2k_workspace_size(ctypes.byref(geo), order, nb, int(fp64), ctypes.byref(ws)), "wbg_r2k_workspace_size")
+    cdt = torch.complex128 if fp64 else torch.complex64
+    if workspace is None or workspace.numel() < ws.value:
+        workspace = torch.empty(int(ws.value), dtype=torch.uint8, device=dev.device)
+    if out is None:
+        out = torch.empty((nb * nk, nF, nw, nw), dtype=cdt, device=dev.device)
+    ph = [torch.from_numpy(p).to(dev.device).to(cdt).contiguous() for p in g.phases(dKs, NKFFT)]
+    fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
+    gt = dev.geom_tensors()
+    X = dev.XR(names, fp64)
+    st = lib.wbg_r2k(_ptr(X), _ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
+                     _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[1]), _ptr(ph[2]), _ptr(fd), nF,
+                     _ptr(dev.wcc_tensor(fp64)), order, nb, int(fp64), _ptr(workspace), ctypes.c_size_t(workspace.numel()),
+                     _ptr(out), ctypes.byref(geo), ctypes.byref(lat), _stream())
+    _lib.check(st, "wbg_r2k")
+    return out, index, nF, (ph, fd, workspace)
+
+
+def eigh(Hfields, strideH, nw, nk, E=None, U=None):
+    lib = _lib.load()
+    dev = Hfields.device
+    ws = ctypes.c_size_t(0)
+    _lib.check(lib.wbg_eigh_workspace_size(nw, nk, ctypes.byref(ws)), "wbg_eigh_workspace_size")
+    work = torch.empty(int(ws.value), dtype=torch.uint8, device=dev)
+    if E is None:
+        E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
+    if U is None:
+        U = torch.empty((nk, nw, nw), dtype=torch.complex128, device=dev)
+    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = lib.wbg_eigh_batched(_ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw, _ptr(work),
+                              ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
+    _lib.check(st, "wbg_eigh_batched")
+    return E, U, flag
+
+
+def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
+    lib = _lib.load()
+    dev = U.device
+    cdt = torch.complex128 if fp64 else torch.complex64
+    if out is None:
+        out = torch.empty((nk, len(sel), nw, nw), dtype=cdt, device=dev)
+    s = torch.tensor(sel, dtype=torch.int32, device=dev)
+    h = torch.tensor(herm, dtype=torch.int32, device=dev)
+    st = lib.wbg_rotate(_ptr(U), nw * nw, _ptr(fields), nFin, _ptr(s), _ptr(h), len(sel), _ptr(out), nw, nk,
+                        int(fp64), _stream())
+    _lib.check(st, "wbg_rotate")
+    return out, (s, h)
+
+
+def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
+    """Stages 1-3 for a batch of blocks.  precision 'fp64': everything in FP64;
+    'mixed': H(k) and eigh in FP64, the other fields and the rotation in FP32."""
+    require_cuda()
+    quantities = set(quantities)
+    nw = dev.nw
+    nk = int(np.prod(NKFFT))
+    nb = len(dKs)
+    keep = []
+    if precision == 'fp64':
+        fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, True, True)
+        keep.append(k1)
+        E, U, flag = eigh(fields, nF * nw * nw, nw, nb * nk)
+        fp64_fields = True
+    elif precision == 'mixed':
+        Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, True)
+        keep.append(k0)
+        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk)
+        del Hf
+        fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, False, False)
+        keep.append(k1)
+        fp64_fields = False
+    else:
+        raise ValueError(f"unknown precision mode {precision!r}")
+    sel, herm, bindex = [], [], {}
+    for q in QUANTITY_ORDER:
+        if q in quantities:
+            bindex[q] = len(sel)
+            n = QUANTITIES[q]['ncomp']
+            sel += list(range(index[q], index[q] + n))
+            herm += [QUANTITIES[q]['herm']] * n
+    if sel:
+        Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nb * nk, fp64_fields)
+        keep.append(k2)
+    else:
+        Xbar = None
+    bd = BandData(E, U, Xbar, bindex, nb, nk, nw, fp64_fields)
+    bd._keep = keep
+    bd._flag = flag
+    return bd
+
+
+def check_flag(bd):
+    if int(bd._flag.item()) != 0:
+        raise RuntimeError("wbg_eigh_batched: QL iteration did not converge for some k-point")
