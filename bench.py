@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""Benchmark: AHC k-points/s at num_wann=32 (the triclinic MDRS workload).
+
+Workload: seeded random TB model, triclinic lattice (3-5 A, 80-100 deg), nw=32,
+R in [-4,4]^3 with Wigner-Seitz replicas (MDRS, mp_grid 9 -> ~1275 R-vectors),
+192^3 k-points in 24^3 FFT blocks (NKdiv=8), AHC over 1001 Fermi levels in [-2,2] eV.
+One step = one batch of FFT blocks through the whole hot path (R->k fields, FP64 eigh,
+U^dagger X U, fused Berry curvature + Fermi-scan histogram).  Synthetic data (no
+dataset exists for this workload).  Every step's fields (GBs) exceed the 129 MB L2, so
+no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--precision mixed|fp64] [--impl reference]
+
+The GPU arm prints one JSON line with value (device-resident throughput), e2e
+(public-API run() with pinned host->device upload of the R-space matrices and the
+result read back every step), the roofline of the dominant kernel measured live with
+CUDA events, the CPU baseline (the oracle on the host cores) and SM clocks sampled
+during the timed region.  --impl reference times the reference algorithm's CPU
+restatement (oracle) on all host cores with the same metric.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, 'wannier-berri_gb300'))
+sys.path.insert(0, REPO)
+
+NW = 32
+NKFFT = 24
+NKDIV = 8
+NEF = 1001
+METRIC = "AHC k-points/s at nw=32 (192^3 grid in 24^3 blocks, MDRS, 1001 E_F)"
+UNIT = "k-points/s"
+CPU_SAMPLE_NKFFT = 12
+THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+def build_system():
+    from wbgpu import models, System_R
+    d = models.config_system(2)
+    s = System_R.from_dict(d)
+    s.do_ws_dist(9)
+    return s
+
+
+# ---------------------------------------------------------------------------------------
+# CPU side: the oracle on a process pool (spawned, so no CUDA state is inherited)
+# ---------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    path, dK, nkfft = args
+    sys.path.insert(0, REPO)
+    from oracle import wb_oracle as O
+    f = np.load(path)
+    XX = {'Ham': f['Ham'], 'AA': f['AA']}
+    s = O.RSystem(f['real_lattice'], f['iRvec'], f['wcc'], XX)
+    t = time.perf_counter()
+    data = O.DataK(s, (nkfft,) * 3, dK)
+    O.AHC(Efermi=np.linspace(-2, 2, NEF))(data)
+    return time.perf_counter() - t
+
+
+def save_system_npz(s):
+    fd, path = tempfile.mkstemp(suffix='.npz', prefix='wbbench_')
+    os.close(fd)
+    np.savez(path, real_lattice=s.real_lattice, iRvec=s.iRvec, wcc=s.wannier_centers_cart,
+             Ham=s.get_R_mat('Ham'), AA=s.get_R_mat('AA'))
+    return path
+
+
+def spawn_pool(procs):
+    """Spawned workers with one BLAS thread each (set in the environment they inherit, before
+    they import numpy), one process per host core -- the reference's own decomposition."""
+    for v in THREAD_VARS:
+        os.environ[v] = "1"
+    return mp.get_context('spawn').Pool(procs)
+
+
+def cpu_rate(path, nblocks, procs, pool=None):
+    """k-points/s of the oracle AHC on `nblocks` 8^3 blocks of the workload spread over `procs` processes."""
+    rng = np.random.default_rng(1)
+    jobs = [(path, rng.random(3) / CPU_SAMPLE_NKFFT, CPU_SAMPLE_NKFFT) for _ in range(nblocks)]
+    own = pool is None
+    if own:
+        pool = spawn_pool(procs)
+    t = time.perf_counter()
+    pool.map(_cpu_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t
+    if own:
+        pool.close()
+        pool.join()
+    return nblocks * CPU_SAMPLE_NKFFT ** 3 / wall, wall
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    procs = os.cpu_count() or 1
+    s = build_system()
+    path = save_system_npz(s)
+    pool = spawn_pool(procs)
+    try:
+        cpu_rate(path, procs, procs, pool)  # start-up + warm caches
+        for _ in range(max(args.warmup - 1, 0)):
+            cpu_rate(path, procs, procs, pool)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            pool.map(_cpu_worker, [(path, np.random.default_rng(i).random(3) / CPU_SAMPLE_NKFFT, CPU_SAMPLE_NKFFT)
+                                   for i in range(procs)], chunksize=1)
+        wall = time.perf_counter() - t
+    finally:
+        pool.close()
+        pool.join()
+        os.unlink(path)
+    nk = args.steps * procs * CPU_SAMPLE_NKFFT ** 3
+    value = nk / wall
+    sample = (f"{procs} oracle processes x one {CPU_SAMPLE_NKFFT}^3 block each per step of the nw=32 MDRS "
+              f"system (AHC, {NEF} E_F)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128/f64",
+            "data": "synthetic", "config": config_dict(args, 'fp64-cpu'),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_dict(args, precision):
+    return {"workload": "random TB nw=32, triclinic, R in [-4,4]^3 + MDRS(mp 9), 192^3 k in 24^3 blocks, "
+                        "AHC 1001 E_F", "num_wann": NW, "NKFFT": NKFFT, "NKdiv": NKDIV,
+            "blocks_per_step": args.blocks_per_step, "k_per_step": args.blocks_per_step * NKFFT ** 3,
+            "precision": precision, "parallelism": f"blocks sharded over {args.gpus} GPU(s)",
+            "l2": "inputs larger than L2 (GB-scale fields per step)"}
+
+
+# ---------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv', prefix='wbclk_')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = [r.split(',') for r in open(self.path).read().strip().splitlines() if r.count(',') >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == 'active'})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows)}
+
+
+def probe_peak(torch, fp64):
+    import ctypes
+    from wbgpu import _lib
+    from wbgpu.engine import _ptr, _stream
+    lib = _lib.load()
+    blocks, threads, iters = 152 * 8, 256, 2048 if fp64 else 16384
+    out = torch.empty(blocks * threads, dtype=torch.float64 if fp64 else torch.float32, device='cuda')
+    fl = ctypes.c_double(0)
+    _lib.check(lib.wbg_probe_fma(int(fp64), blocks, threads, 16, _ptr(out), ctypes.byref(fl), _stream()), "probe")
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        _lib.check(lib.wbg_probe_fma(int(fp64), blocks, threads, iters, _ptr(out), ctypes.byref(fl), _stream()), "probe")
+        e.record()
+        e.synchronize()
+        best = max(best, fl.value / (s.elapsed_time(e) * 1e-3))
+    return best / 1e9  # GFLOP/s
+
+
+def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
+    """Algorithmic work per launch of the given stage (per k-point figures as defined in the design doc)."""
+    n = NW
+    per_launch_ms = ms_total / max(n_calls, 1)
+    if stage == 'eigh':
+        work = 20.0 * n ** 3 * k_per_call          # FP64 flops, convention 20 nw^3 per matrix
+        bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
+    elif stage == 'rotate':
+        work = 16.0 * n ** 3 * 9 * k_per_call      # two complex GEMMs per field, 9 fields
+        if precision == 'fp64':
+            bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
+        else:
+            bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
+    elif stage.startswith('r2k'):
+        s = 16 if stage == 'r2k_fp64' else 8
+        work = 2.0 * nF_fields[stage] * n * n * s * k_per_call   # bytes: write + read back of each field
+        bound, unit, peak, src = 'hbm', 'GB/s', peaks['hbm'], 'MEASURED_PEAKS.json hbm_gbs'
+    else:  # berry_omega
+        s = 16 if precision == 'fp64' else 8
+        work = 9.0 * n * n * s * k_per_call
+        bound, unit, peak, src = 'hbm', 'GB/s', peaks['hbm'], 'MEASURED_PEAKS.json hbm_gbs'
+    achieved = work / (per_launch_ms * 1e-3) / 1e9
+    return {"kernel": stage, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak if peak else None, "peak_source": src, "ms_per_launch": per_launch_ms,
+            "work_per_launch": work, "traffic": None}
+
+
+def run_gpu(args):
+    import torch
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', str(args.gpus)))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    s = build_system()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        path = save_system_npz(s)
+        try:
+            rate, wall = cpu_rate(path, procs, procs)
+        finally:
+            os.unlink(path)
+        cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"{procs} spawned oracle processes, one {CPU_SAMPLE_NKFFT}^3 block each of the same nw=32 "
+                         f"MDRS system (AHC, {NEF} E_F), {wall:.1f} s wall"}
+    import wbgpu
+    from wbgpu import engine, _lib
+    from wbgpu.calculators import AHC
+    _lib.load()
+    torch.cuda.init()
+    grid = wbgpu.Grid(s, NKdiv=NKDIV, NKFFT=NKFFT)
+    nblocks = grid.nblocks
+    shifts = grid.block_shifts()
+    mine = np.arange(rank, nblocks, world)
+    B = args.blocks_per_step
+    nk = grid.nk_per_block
+    EF = np.linspace(-2, 2, NEF)
+
+    def step_blocks(i):
+        idx = [(i * B + j) % len(mine) for j in range(B)]
+        return mine[idx]
+
+    dev = engine.DeviceSystem(s)
+    calc = AHC(Efermi=EF)
+    quantities = calc.quantities(s)
+    calc.reset(dev.device)
+
+    def step(i, precision, c=calc):
+        bd = engine.band_data(dev, shifts[step_blocks(i)], grid.FFT, quantities, precision)
+        c.accumulate(bd, s)
+        return bd
+
+    def timed_loop(precision, K, W, timer=None):
+        for i in range(W):
+            step(i, precision)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        engine.set_timer(timer)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for i in range(W, W + K):
+            bd = step(i, precision)
+        t1.record()
+        torch.cuda.synchronize()
+        engine.set_timer(None)
+        engine.check_flag(bd)
+        ms = t0.elapsed_time(t1)
+        if world > 1:
+            tt = torch.tensor([ms], device='cuda')
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms
+
+    precision = args.precision
+    clocks = ClockSampler(local)
+    timer = engine.StageTimer()
+    clocks.start()
+    ms = timed_loop(precision, args.steps, args.warmup, timer)
+    clk = clocks.stop()
+    total_k = world * args.steps * B * nk
+    value = total_k / (ms * 1e-3)
+    stage_ms = timer.totals_ms()
+    counts = timer.counts()
+    kernels_per_call = {'r2k_fp64': 3, 'r2k_fp32': 3, 'eigh': 3, 'rotate': 1, 'berry_omega': 1}
+    gpu_launches = int(sum(counts[k] * kernels_per_call[k] for k in counts))
+
+    # plain FP64 drop-in throughput on the same blocks, and the mixed-vs-FP64 error of one step
+    fp64_value = None
+    err = None
+    if precision == 'mixed' and not args.no_fp64_compare:
+        K64 = max(1, min(args.steps, 3))
+        ms64 = timed_loop('fp64', K64, 1)
+        fp64_value = world * K64 * B * nk / (ms64 * 1e-3)
+        c1, c2 = AHC(Efermi=EF), AHC(Efermi=EF)
+        c1.reset(dev.device)
+        c2.reset(dev.device)
+        step(0, 'mixed', c1)
+        step(0, 'fp64', c2)
+        a = c1.finalize(s.cell_volume, nk)
+        b = c2.finalize(s.cell_volume, nk)
+        err = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    # end-to-end through the public API: fresh device upload of the R-space matrices from
+    # pinned host memory, run() over this step's blocks, result read back to the host
+    Ke = max(1, min(args.steps, 5))
+    h2d = 0
+    for i in range(args.warmup):  # warm-up of the e2e path
+        wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=precision, blocks=step_blocks(i))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(Ke):
+        dsys = engine.DeviceSystem(s)
+        r = wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=precision, blocks=step_blocks(i), dev_system=dsys)
+        h2d = dsys.h2d_bytes
+        _ = r['ahc'].data  # already on the host (device->host copy inside run())
+    e1.record()
+    torch.cuda.synchronize()
+    ems = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ems], device='cuda')
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ems = float(tt.item())
+    e2e = {"value": world * Ke * B * nk / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": NEF * 3 * 8}
+
+    peaks = {'fp64': probe_peak(torch, True), 'fp32': probe_peak(torch, False)}
+    try:
+        mp_ = json.load(open(os.path.join(REPO, 'MEASURED_PEAKS.json')))
+        peaks['hbm'] = float(mp_['hbm_gbs'])
+    except (OSError, KeyError, ValueError):
+        peaks['hbm'] = 6800.0  # fallback figure of the profiling recipe
+    nF_fields = {'r2k_fp64': 10 if precision == 'fp64' else 1, 'r2k_fp32': 9}
+    dominant = max(stage_ms, key=stage_ms.get)
+    roof = stage_roofline(dominant, stage_ms[dominant], counts[dominant], B * nk, precision, peaks, nF_fields)
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64 eigh/scan + fp32 fields" if precision == 'mixed' else "fp64",
+            "data": "synthetic (seeded random TB model)", "config": config_dict(args, precision),
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clk,
+            "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
+            "fp64_dropin_value": fp64_value, "max_rel_err_vs_fp64": err,
+            "peaks_measured_gflops": {"fp64": peaks['fp64'], "fp32": peaks['fp32']}}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gpu', choices=['gpu', 'reference'])
+    ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
+    ap.add_argument('--blocks-per-step', type=int, default=4)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-fp64-compare', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -105,6 +105,12 @@ int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA
 /* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);
 
+/* ---- measurement helper (no reference counterpart) ----------------------------------------
+ * FMA throughput probe giving the roofline denominator of FP64- / FP32-pipe-bound kernels:
+ * blocks*threads threads run 8 independent FMA chains of `iters` steps; out holds
+ * blocks*threads elements of the probed type; *flops_per_launch receives the flop count. */
+int wbg_probe_fma(int fp64, int blocks, int threads, int iters, void* out, double* flops_per_launch, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

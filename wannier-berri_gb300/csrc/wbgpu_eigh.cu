@@ -213,7 +213,9 @@ __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __re
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;
-  double2* Us = reinterpret_cast<double2*>(sme + (size_t)grp * (2 * n * n + 3 * n));  // [i][j]
+  // per-group stride rounded up to an even number of doubles so U (double2) stays 16-byte aligned
+  const int gstride = (2 * n * n + 3 * n + 1) & ~1;
+  double2* Us = reinterpret_cast<double2*>(sme + (size_t)grp * gstride);  // [i][j]
   double* Zs = reinterpret_cast<double*>(Us);  // Z(i, j) = Zs[2 * (i * n + j)]
   double* ds = Zs + 2 * n * n;
   double* es = ds + n;
@@ -356,7 +358,7 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   cudaFuncSetAttribute(eigh_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   eigh_tridiag<<<(nk + G - 1) / G, G * L, G * smT, stream>>>((const double2*)H, strideH, n, nk, L, G, Vh, tau, d, e);
   eigh_ql<<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
-  const size_t smV = (2 * (size_t)n * n + 3 * n) * sizeof(double);
+  const size_t smV = (size_t)((2 * n * n + 3 * n + 1) & ~1) * sizeof(double);
   int GV = (2 * 32) / L;
   while (GV > 1 && GV * smV > 96 * 1024) GV /= 2;
   if (GV * smV > 220 * 1024) return WBG_ERR_SIZE;

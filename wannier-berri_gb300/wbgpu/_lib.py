@@ -12,7 +12,7 @@ from . import build as _build
 
 EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_workspace_size', 'wbg_r2k',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_rotate', 'wbg_berry_omega',
-           'wbg_scan_finalize']
+           'wbg_scan_finalize', 'wbg_probe_fma']
 
 STATUS_OK = 0
 
@@ -48,6 +48,7 @@ _SIGS = {
     'wbg_rotate': (_I, [_P, _LL, _P, _I, _P, _P, _I, _P, _I, _I, _I, _P]),
     'wbg_berry_omega': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
+    'wbg_probe_fma': (_I, [_I, _I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), _P]),
 }
 
 _lib = None

@@ -13,6 +13,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import engine
 from .engine import _ptr, _stream
 from .factors import factor_ahc
 from .result import EnergyResult
@@ -83,7 +84,7 @@ class AHC(StaticCalculator):
         sc = self.scan_struct()
         iA = bd.index.get('A', 0)
         iO = bd.index.get('O', 0)
-        st = _lib.load().wbg_berry_omega(_ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], bd.index['V'], iA, iO, bd.nw,
+        st = engine._timed('berry_omega', _lib.load().wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], bd.index['V'], iA, iO, bd.nw,
                                          bd.nk_total, ctypes.byref(sc), int(self.internal_terms), int(ext),
                                          _ptr(self._hist), int(bd.fp64_fields), _stream())
         _lib.check(st, "wbg_berry_omega")

@@ -31,6 +31,43 @@ QUANTITY_ORDER = ['V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C']
 MOM0, DER1, DER2, ROT, DROT = 0, 1, 2, 3, 4
 
 
+class StageTimer:
+    """CUDA events recorded on the launching (current) stream around each stage call."""
+
+    def __init__(self):
+        self.events = {}
+
+    def wrap(self, name, fn, *a, **k):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        r = fn(*a, **k)
+        e.record()
+        self.events.setdefault(name, []).append((s, e))
+        return r
+
+    def totals_ms(self):
+        torch.cuda.synchronize()
+        return {k: sum(s.elapsed_time(e) for s, e in v) for k, v in self.events.items()}
+
+    def counts(self):
+        return {k: len(v) for k, v in self.events.items()}
+
+
+_TIMER = None
+
+
+def set_timer(timer):
+    global _TIMER
+    _TIMER = timer
+
+
+def _timed(name, fn, *a, **k):
+    if _TIMER is None:
+        return fn(*a, **k)
+    return _TIMER.wrap(name, fn, *a, **k)
+
+
 def require_cuda():
     if not torch.cuda.is_available():
         raise RuntimeError("wbgpu needs a CUDA device (sm_103a); no CPU fallback exists")
@@ -81,6 +118,22 @@ class RGeometry:
         return out
 
 
+def host_pinned(system, key, order):
+    """Pinned host copy of XX_R[key] in sorted R order, [ncomp][nR][nw*nw] complex128,
+    cached on the system object so repeated uploads start from page-locked memory."""
+    cache = system.__dict__.setdefault('_pinned_cache', {})
+    if key not in cache:
+        X = system.get_R_mat(key)[order]
+        nR, nw = X.shape[0], X.shape[1]
+        if X.ndim == 3:
+            a = X.reshape(1, nR, nw * nw)
+        else:
+            a = np.moveaxis(X, 3, 0).reshape(X.shape[3], nR, nw * nw)
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        cache[key] = t.pin_memory() if torch.cuda.is_available() else t
+    return cache[key]
+
+
 class DeviceSystem:
     """R-space matrices of one system resident on the GPU (uploaded once)."""
 
@@ -93,8 +146,8 @@ class DeviceSystem:
         self.geom = RGeometry(system.iRvec)
         self.lattice = np.array(system.real_lattice, dtype=float)
         self.wcc = np.array(system.wannier_centers_cart, dtype=float)
-        self._bases = {}
         self._cache = {}
+        self.h2d_bytes = 0
 
     def bases_for(self, keys):
         """Base-field list for the R->k launch: Ham, then 3 components of each extra key."""
@@ -104,16 +157,24 @@ class DeviceSystem:
                 names += [(key, c) for c in range(3)]
         return names
 
+    def _key_fp64(self, key):
+        """Device copy (FP64, sorted R order) of one real-space matrix, [ncomp][nR][nw*nw]."""
+        ck = ('R', key)
+        if ck not in self._cache:
+            host = host_pinned(self.system, key, self.geom.order)
+            self._cache[ck] = host.to(self.device, non_blocking=True)
+            self.h2d_bytes += host.numel() * host.element_size()
+        return self._cache[ck]
+
     def XR(self, names, fp64):
+        """Base fields [nBase][nR][nw*nw] for one R->k launch (FP32 copies are cast on the device)."""
         ck = (tuple(names), fp64)
         if ck not in self._cache:
-            order = self.geom.order
-            arrs = []
+            parts = []
             for key, c in names:
-                X = self.system.get_R_mat(key)
-                arrs.append(X[order] if c is None else X[order][..., c])
-            a = np.stack(arrs).reshape(len(names), len(order), self.nw * self.nw)
-            t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+                t = self._key_fp64(key)
+                parts.append(t[0:1] if c is None else t[c:c + 1])
+            t = torch.cat(parts, dim=0).contiguous()
             self._cache[ck] = t if fp64 else t.to(torch.complex64)
         return self._cache[ck]
 
@@ -232,7 +293,7 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
     fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
     gt = dev.geom_tensors()
     X = dev.XR(names, fp64)
-    st = lib.wbg_r2k(_ptr(X), _ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
+    st = _timed('r2k_fp64' if fp64 else 'r2k_fp32', lib.wbg_r2k, _ptr(X), _ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
                      _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[1]), _ptr(ph[2]), _ptr(fd), nF,
                      _ptr(dev.wcc_tensor(fp64)), order, nb, int(fp64), _ptr(workspace), ctypes.c_size_t(workspace.numel()),
                      _ptr(out), ctypes.byref(geo), ctypes.byref(lat), _stream())
@@ -251,7 +312,7 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None):
     if U is None:
         U = torch.empty((nk, nw, nw), dtype=torch.complex128, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    st = lib.wbg_eigh_batched(_ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw, _ptr(work),
+    st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw, _ptr(work),
                               ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
     _lib.check(st, "wbg_eigh_batched")
     return E, U, flag
@@ -265,7 +326,7 @@ def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
         out = torch.empty((nk, len(sel), nw, nw), dtype=cdt, device=dev)
     s = torch.tensor(sel, dtype=torch.int32, device=dev)
     h = torch.tensor(herm, dtype=torch.int32, device=dev)
-    st = lib.wbg_rotate(_ptr(U), nw * nw, _ptr(fields), nFin, _ptr(s), _ptr(h), len(sel), _ptr(out), nw, nk,
+    st = _timed('rotate', lib.wbg_rotate, _ptr(U), nw * nw, _ptr(fields), nFin, _ptr(s), _ptr(h), len(sel), _ptr(out), nw, nk,
                         int(fp64), _stream())
     _lib.check(st, "wbg_rotate")
     return out, (s, h)

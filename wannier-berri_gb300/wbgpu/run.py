@@ -22,7 +22,11 @@ def choose_batch(nw, nk, nblocks, quantities, precision, max_kpoints=1 << 17, bu
 
 
 def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, device='cuda', dev_system=None,
-        **_ignored):
+        blocks=None, **_ignored):
+    """Integrate ``calculators`` over ``grid``.  precision: 'fp64' (plain) or 'mixed'
+    (FP64 H(k) + eigh + scan, FP32 fields and rotations).  ``blocks`` restricts the
+    run to a subset of the division-grid K-points (indices into Grid.block_shifts());
+    the result then carries the same 1/prod(NKdiv) weight per block."""
     engine.require_cuda()
     dev = dev_system or engine.DeviceSystem(system, device)
     quantities = set()
@@ -31,6 +35,8 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
     for c in calculators.values():
         c.reset(dev.device)
     shifts = grid.block_shifts()
+    if blocks is not None:
+        shifts = shifts[np.asarray(blocks)]
     nk = grid.nk_per_block
     nb = blocks_per_batch or choose_batch(dev.nw, nk, len(shifts), quantities, precision)
     for i0 in range(0, len(shifts), nb):
