@@ -137,8 +137,8 @@ def run_reference(args):
 
 def config_dict(args, precision):
     return {"workload": "random TB nw=32, triclinic, R in [-4,4]^3 + MDRS(mp 9), 192^3 k in 24^3 blocks, "
-                        "AHC 1001 E_F", "num_wann": NW, "NKFFT": NKFFT, "NKdiv": NKDIV,
-            "blocks_per_step": args.blocks_per_step, "k_per_step": args.blocks_per_step * NKFFT ** 3,
+                        "AHC 1001 E_F", "num_wann": NW, "NKFFT": args.nkfft, "NKdiv": NKDIV,
+            "blocks_per_step": args.blocks_per_step, "k_per_step": args.blocks_per_step * args.nkfft ** 3,
             "precision": precision, "parallelism": f"blocks sharded over {args.gpus} GPU(s)",
             "l2": "inputs larger than L2 (GB-scale fields per step)"}
 
@@ -255,7 +255,7 @@ def run_gpu(args):
     from wbgpu.calculators import AHC
     _lib.load()
     torch.cuda.init()
-    grid = wbgpu.Grid(s, NKdiv=NKDIV, NKFFT=NKFFT)
+    grid = wbgpu.Grid(s, NKdiv=NKDIV, NKFFT=args.nkfft)
     nblocks = grid.nblocks
     shifts = grid.block_shifts()
     mine = np.arange(rank, nblocks, world)
@@ -387,6 +387,7 @@ def main():
     ap.add_argument('--impl', default='gpu', choices=['gpu', 'reference'])
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--blocks-per-step', type=int, default=4)
+    ap.add_argument('--nkfft', type=int, default=NKFFT, help='FFT block edge (smaller only for profiling captures)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64-compare', action='store_true')
     args = ap.parse_args()
