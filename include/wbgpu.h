@@ -63,34 +63,40 @@ int wbg_abi_version(void);
 const char* wbg_status_string(int status);
 
 /* ---- stage 1: R -> k --------------------------------------------------------------------
- * XR          [nBase][nR][nw][nw] complex, R in sorted order, block phase NOT applied
- * pair_start  [nP+1] first sorted R of each pair;  r2 [nR] third R component
- * slice_start [nU+1] first pair of each slice;     pair_r1 [nP];  slice_r0 [nU]
- * ph0/ph1/ph2 [nblocks][N_d][nr_d] complex: exp(2 pi i R_d (j/N_d + dK_d)), R_d = rmin_d + r
- * field_desc  [nfields][4] int: (kind, base, a, b) -- kind 0: plain transform of `base`;
- *             1: d/dk_a; 2: d/dk_a d/dk_b; 3: curl component a of d A (A = bases base..base+2);
- *             4: d/dk_b of that curl.  Derivatives are i (R + t_n - t_m) as in
- *             fourier/rvectors.py:355-369,487-494, with t = wcc [nw][3] Cartesian.
- * order       0, 1, 2: highest derivative order the fields use
- * fields_out  [nblocks*nk][nfields][nw][nw] complex
+ * wbg_r2k_fields (once per system and field set): R-space arrays of the k-space fields,
+ *   XR       [nBase][nR][nw][nw] complex128 base matrices (Ham, then A x/y/z, ...), R sorted
+ *   iR       [nR][3] int, the sorted R-vectors;  wcc [nw][3] Cartesian Wannier centres t
+ *   field_desc [nfields][4] int (kind, base, a, b): 0 X; 1 i w_a X; 2 -w_a w_b X;
+ *            3 curl component a of i w A (A = bases base..base+2); 4 i w_b times that curl,
+ *            with w = R + t_n - t_m in Cartesian coordinates (fourier/rvectors.py:355-369,
+ *            487-494; data_K/data_K_R.py:48-51)
+ *   XF       [nfields][nR][nw][nw] complex (fp64 ? double : float)
+ * wbg_r2k (per batch of FFT blocks): fields_out[b*nk + k][f] = sum_R exp(2 pi i R.(j_k/N + dK_b)) XF[f][R]
+ *   pair_start [nP+1] first sorted R of each pair;  r2 [nR] third R component
+ *   slice_start [nU+1] first pair of each slice;    pair_r1 [nP];  slice_r0 [nU]
+ *   ph0/ph1/ph2 [nblocks][N_d][nr_d] complex: exp(2 pi i R_d (j/N_d + dK_d)), R_d = rmin_d + r
+ *   fields_out [nblocks*nk][nfields][nw][nw] complex, k = (j0*N1 + j1)*N2 + j2
  */
-int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int order, int nblocks, int fp64, size_t* bytes);
-int wbg_r2k(const void* XR, const int* pair_start, const int* r2, const int* slice_start, const int* pair_r1,
-            const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, const int* field_desc,
-            int nfields, const void* wcc, int order, int nblocks, int fp64, void* workspace,
-            size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g, const wbg_lattice* lat,
+int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, const int* field_desc, int nfields,
+                   const double* wcc, const wbg_lattice* lat, int fp64, void* XF, void* stream);
+int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int fp64, size_t* bytes);
+int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, const int* slice_start,
+            const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, int nblocks,
+            int fp64, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
             void* stream);
 
-/* ---- stage 2: batched Hermitian eigensolver (FP64) --------------------------------------
+/* ---- stage 2: batched Hermitian eigensolver ---------------------------------------------
  * H: matrix k at H + k*strideH (complex128 elements), symmetrised as 1/2 (H + H^dagger).
- * E [nk][nw] ascending; U: matrix k at U + k*strideU, column n = eigenvector n.
+ * Tridiagonalisation, eigenvalues and inverse iteration run in FP64.
+ * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n,
+ * complex128 if fp64_vectors else complex64 (the back-transform then runs in FP32).
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
-                     void* workspace, size_t workspace_bytes, int* errflag, void* stream);
+                     int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
 
 /* ---- stage 3: U^dagger X U ----------------------------------------------------------------
- * X [nk][nFin][nw][nw] (precision fp64), U complex128 with stride strideU.
+ * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.
  * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U, Hermitian part if herm[f]. */
 int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);

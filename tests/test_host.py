@@ -38,7 +38,7 @@ def test_workspace_queries_without_gpu():
     b = ctypes.c_size_t(0)
     assert lib.wbg_r2k_workspace_size(ctypes.byref(g), 1, 2, 1, ctypes.byref(b)) == 0
     assert b.value > 0
-    assert lib.wbg_r2k_workspace_size(ctypes.byref(g), 3, 2, 1, ctypes.byref(b)) == 1
+    assert lib.wbg_r2k_workspace_size(ctypes.byref(g), 0, 2, 1, ctypes.byref(b)) == 1
     assert lib.wbg_eigh_workspace_size(200, 10, ctypes.byref(b)) == 1
     with pytest.raises(ValueError):
         _lib.check(1, "x")
@@ -109,6 +109,22 @@ def test_set_R_mat_hermitian_and_errors():
         s.set_R_mat('Ham', X)
     with pytest.raises(ValueError):
         s.get_R_mat('AA')
+
+
+def test_rspace_field_weights_match_reference_derivative():
+    """The R-space weights that wbg_r2k_fields applies (i(R + t_n - t_m), curl) are the
+    reference's derivative / rotAA (fourier/rvectors.py:487-494, data_K/data_K_R.py:48-51):
+    transforming weighted fields reproduces Xbar before rotation."""
+    d = models.config_system(2, small=True)
+    o = O.RSystem(d['real_lattice'], d['iRvec'], d['wannier_centers_cart'], d['XX_R'])
+    data = O.DataK(o, (2, 3, 2), np.array([0.1, 0.2, 0.3]) / 4)
+    # host restatement of the kernel's weights for DER1 and ROT
+    cR = o.cRvec_shifted()                                   # (nR, nw, nw, 3)
+    A = data.get_R_mat('AA')
+    rot = 1j * (cR[..., [1, 2, 0]] * A[..., [2, 0, 1]] - cR[..., [2, 0, 1]] * A[..., [1, 2, 0]])
+    assert np.allclose(rot, data.get_R_mat('rotAA'))
+    dH = 1j * cR * data.get_R_mat('Ham')[..., None]
+    assert np.allclose(dH, data.derivative(data.get_R_mat('Ham')))
 
 
 def test_field_plan_layout():

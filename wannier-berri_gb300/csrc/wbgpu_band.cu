@@ -19,7 +19,7 @@ namespace {
 // grid: nk blocks of 256 threads; shared: U, X, T (nw*nw each, precision T)
 // ---------------------------------------------------------------------------------------
 template <typename T>
-__global__ void rotate_kernel(const double2* __restrict__ U, long long strideU, const typename C2<T>::t* __restrict__ X,
+__global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long strideU, const typename C2<T>::t* __restrict__ X,
                               int nFin, const int* __restrict__ fsel, const int* __restrict__ herm, int nFrot,
                               typename C2<T>::t* __restrict__ Xbar, int nw) {
   typedef typename C2<T>::t V;
@@ -29,10 +29,7 @@ __global__ void rotate_kernel(const double2* __restrict__ U, long long strideU, 
   V* Ts = Xs + nw * nw;
   const long long k = blockIdx.x;
   const int nw2 = nw * nw;
-  for (int i = threadIdx.x; i < nw2; i += blockDim.x) {
-    const double2 u = U[k * strideU + i];
-    Us[i] = mkc<T>((T)u.x, (T)u.y);
-  }
+  for (int i = threadIdx.x; i < nw2; i += blockDim.x) Us[i] = U[k * strideU + i];
   for (int f = 0; f < nFrot; ++f) {
     const int fs = fsel[f];
     const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
@@ -244,7 +241,7 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
                                                    nFrot, (double2*)Xbar, nw);
   } else {
     cudaFuncSetAttribute(rotate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    rotate_kernel<float><<<nk, 256, sm, stream>>>((const double2*)U, strideU, (const float2*)X, nFin, fsel, herm,
+    rotate_kernel<float><<<nk, 256, sm, stream>>>((const float2*)U, strideU, (const float2*)X, nFin, fsel, herm,
                                                   nFrot, (float2*)Xbar, nw);
   }
   return wbg_cuda_status(cudaGetLastError());

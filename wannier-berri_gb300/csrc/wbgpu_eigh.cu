@@ -162,11 +162,13 @@ __global__ void eigh_ql(const double* __restrict__ dIn, const double* __restrict
         for (i = m - 1; i >= l; --i) {
           double f = s * e[i];
           const double b = c * e[i];
-          r = hypot(f, g);
+          // Givens rotation: one sqrt and one reciprocal (f, g are O(|T|): no overflow concern)
+          r = sqrt(fma(f, f, g * g));
           e[i + 1] = r;
           if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; underflow = true; break; }
-          s = f / r;
-          c = g / r;
+          const double rinv = 1.0 / r;
+          s = f * rinv;
+          c = g * rinv;
           g = d[i + 1] - p;
           r = (d[i] - g) * s + 2.0 * c * b;
           p = s * r;
@@ -199,83 +201,82 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 }
 
 // ---------------------------------------------------------------------------------------
-// 3. Eigenvectors: inverse iteration on T, clusters re-orthogonalised, U = Q Z.
+// 3. Eigenvectors: inverse iteration on T (FP64), clusters re-orthogonalised, U = Q Z.
 // grid: ceil(nk/G) blocks of G*L threads; lane j computes eigenvectors j, j+L, ...
-// Shared memory per group: U[n][n] complex; the real inverse-iteration vectors Z live in
-// the real parts of U (Z(i,j) = U[i][j].x) until the back-transform turns them complex.
+// The back-transform by the Householder reflectors runs in precision TU (double, or float
+// when the caller consumes U in FP32).  Shared memory per group: U[n][n] complex(TU) with the
+// real inverse-iteration vectors Z(i,j) kept in a separate real(double) array.
 // ---------------------------------------------------------------------------------------
+template <typename TU>
 __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __restrict__ tauIn,
                              const double* __restrict__ dIn, const double* __restrict__ eIn,
-                             const double* __restrict__ E, int n, int nk, int L, int G, double2* __restrict__ Uout,
-                             long long strideU) {
+                             const double* __restrict__ E, int n, int nk, int L, int G,
+                             typename C2<TU>::t* __restrict__ Uout, long long strideU) {
+  typedef typename C2<TU>::t VU;
   extern __shared__ double sme[];
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;
-  // per-group stride rounded up to an even number of doubles so U (double2) stays 16-byte aligned
-  const int gstride = (2 * n * n + 3 * n + 1) & ~1;
-  double2* Us = reinterpret_cast<double2*>(sme + (size_t)grp * gstride);  // [i][j]
-  double* Zs = reinterpret_cast<double*>(Us);  // Z(i, j) = Zs[2 * (i * n + j)]
-  double* ds = Zs + 2 * n * n;
+  // per-group layout (in doubles, 16-byte aligned pieces): Z [n*n], d, e, lam [n each], U
+  const int zsz = (n * n + 3 * n + 1) & ~1;
+  const int usz = (int)(((size_t)n * n * sizeof(VU) + 15) / 16 * 2);
+  double* Zs = sme + (size_t)grp * (zsz + usz);  // Z(i,j) = Zs[i*n + j]
+  double* ds = Zs + n * n;
   double* es = ds + n;
   double* lam = es + n;
+  VU* Us = reinterpret_cast<VU*>(Zs + zsz);      // [i][j]
   for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = E[k * n + i]; }
   __syncwarp();
-  // matrix scale for tiny-pivot replacement and cluster tolerance
   double tnorm = 0.0;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(ds[i]) + fabs(es[i]) + (i > 0 ? fabs(es[i - 1]) : 0.0));
   tnorm = fmax(tnorm, DBL_MIN);
   const double tiny = DBL_EPSILON * tnorm;
   const double ortol = 1e-5 * tnorm;
   const double pertol = 10.0 * DBL_EPSILON * tnorm;
-  double u0[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
+  double u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
   unsigned char piv[WBG_EIGH_NMAX];
   for (int j = lane; j < n; j += L) {
-    // shift, separated from a numerically equal lower neighbour
     double shift = lam[j];
     for (int jj = j - 1; jj >= 0 && shift - lam[jj] < pertol; --jj) shift = lam[jj] + pertol * (j - jj);
-    // LU with partial pivoting of T - shift I
+    // LU with partial pivoting of T - shift I; u0i holds reciprocal pivots
     double ca = ds[0] - shift, cb = n > 1 ? es[0] : 0.0;
     for (int i = 0; i < n - 1; ++i) {
       const double ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : 0.0;
       if (fabs(ca) >= fabs(ci)) {
-        if (ca == 0.0) ca = tiny;
-        const double mlt = ci / ca;
-        u0[i] = ca; u1[i] = cb; u2[i] = 0.0; lm[i] = mlt; piv[i] = 0;
+        if (fabs(ca) < tiny) ca = ca >= 0.0 ? tiny : -tiny;
+        const double rc = 1.0 / ca;
+        const double mlt = ci * rc;
+        u0i[i] = rc; u1[i] = cb; u2[i] = 0.0; lm[i] = mlt; piv[i] = 0;
         ca = ai1 - mlt * cb;
         cb = bi1;
       } else {
-        const double mlt = ca / ci;
-        u0[i] = ci; u1[i] = ai1; u2[i] = bi1; lm[i] = mlt; piv[i] = 1;
+        const double rc = 1.0 / ci;
+        const double mlt = ca * rc;
+        u0i[i] = rc; u1[i] = ai1; u2[i] = bi1; lm[i] = mlt; piv[i] = 1;
         ca = cb - mlt * ai1;
         cb = -mlt * bi1;
       }
     }
     if (fabs(ca) < tiny) ca = ca >= 0.0 ? tiny : -tiny;
-    u0[n - 1] = ca;
-    for (int i = 0; i < n - 1; ++i)
-      if (fabs(u0[i]) < tiny) u0[i] = u0[i] >= 0.0 ? tiny : -tiny;
+    u0i[n - 1] = 1.0 / ca;
     for (int i = 0; i < n; ++i) x[i] = hash_uniform((unsigned)j + 1u, (unsigned)i + 7u);
     for (int it = 0; it < 3; ++it) {
-      // forward: apply the row operations to the right-hand side
       double rp = x[0];
       for (int i = 0; i < n - 1; ++i) {
         const double y1 = x[i + 1];
         if (piv[i] == 0) { x[i] = rp; rp = y1 - lm[i] * rp; }
         else { x[i] = y1; rp = rp - lm[i] * y1; }
       }
-      x[n - 1] = rp;
-      // back substitution
-      x[n - 1] = x[n - 1] / u0[n - 1];
-      if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) / u0[n - 2];
-      for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) / u0[i];
+      x[n - 1] = rp * u0i[n - 1];
+      if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0i[n - 2];
+      for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0i[i];
       double nrm = 0.0;
       for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
-      nrm = 1.0 / sqrt(nrm);
+      nrm = rsqrt(nrm);
       for (int i = 0; i < n; ++i) x[i] *= nrm;
     }
-    for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] = x[i];
+    for (int i = 0; i < n; ++i) Zs[i * n + j] = x[i];
   }
   __syncwarp();
   // modified Gram-Schmidt inside clusters (eigenvalues closer than ortol), in eigenvalue order
@@ -290,13 +291,13 @@ __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __re
           for (int q = jp + 1; q <= j; ++q) same &= (lam[q] - lam[q - 1] < ortol);
           if (same) {
             double dot = 0.0;
-            for (int i = 0; i < n; ++i) dot = fma(Zs[2 * (i * n + jp)], Zs[2 * (i * n + j)], dot);
-            for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] -= dot * Zs[2 * (i * n + jp)];
+            for (int i = 0; i < n; ++i) dot = fma(Zs[i * n + jp], Zs[i * n + j], dot);
+            for (int i = 0; i < n; ++i) Zs[i * n + j] -= dot * Zs[i * n + jp];
             if (j == jp + 1) {
               double nrm = 0.0;
-              for (int i = 0; i < n; ++i) nrm = fma(Zs[2 * (i * n + j)], Zs[2 * (i * n + j)], nrm);
-              nrm = 1.0 / sqrt(nrm);
-              for (int i = 0; i < n; ++i) Zs[2 * (i * n + j)] *= nrm;
+              for (int i = 0; i < n; ++i) nrm = fma(Zs[i * n + j], Zs[i * n + j], nrm);
+              nrm = rsqrt(nrm);
+              for (int i = 0; i < n; ++i) Zs[i * n + j] *= nrm;
             }
           }
         }
@@ -304,19 +305,23 @@ __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __re
       __syncwarp();
     }
   }
-  // back-transform: u = H_0 H_1 ... H_{n-2} z
+  // back-transform: u = H_0 H_1 ... H_{n-2} z  (precision TU)
   for (int j = lane; j < n; j += L) {
-    for (int i = 0; i < n; ++i) Us[i * n + j].y = 0.0;
+    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>((TU)Zs[i * n + j], (TU)0);
     for (int c = n - 2; c >= 0; --c) {
-      const double2 tau = tauIn[k * n + c];
-      if (tau.x == 0.0 && tau.y == 0.0) continue;
+      const double2 tau64 = tauIn[k * n + c];
+      if (tau64.x == 0.0 && tau64.y == 0.0) continue;
+      const VU tau = mkc<TU>((TU)tau64.x, (TU)tau64.y);
       const double2* v = Vh + (k * n + c) * n;
-      double2 s = make_double2(0.0, 0.0);
-      for (int i = c + 1; i < n; ++i) cfmac(s, v[i], Us[i * n + j]);
-      const double2 ts = cmul(tau, s);
+      VU sacc = czero<VU>();
       for (int i = c + 1; i < n; ++i) {
-        double2 u = Us[i * n + j];
-        const double2 vv = v[i];
+        const VU vv = mkc<TU>((TU)v[i].x, (TU)v[i].y);
+        cfmac(sacc, vv, Us[i * n + j]);
+      }
+      const VU ts = cmul(tau, sacc);
+      for (int i = c + 1; i < n; ++i) {
+        VU u = Us[i * n + j];
+        const VU vv = mkc<TU>((TU)v[i].x, (TU)v[i].y);
         u.x -= vv.x * ts.x - vv.y * ts.y;
         u.y -= vv.x * ts.y + vv.y * ts.x;
         Us[i * n + j] = u;
@@ -342,7 +347,7 @@ size_t wbg_eigh_workspace_bytes(int n, int nk) {
 }
 
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU,
-                 void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
+                 int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
   if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
   char* w = (char*)workspace;
@@ -358,12 +363,20 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   cudaFuncSetAttribute(eigh_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   eigh_tridiag<<<(nk + G - 1) / G, G * L, G * smT, stream>>>((const double2*)H, strideH, n, nk, L, G, Vh, tau, d, e);
   eigh_ql<<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
-  const size_t smV = (size_t)((2 * n * n + 3 * n + 1) & ~1) * sizeof(double);
+  const size_t zsz = (size_t)((n * n + 3 * n + 1) & ~1);
+  const size_t usz = ((size_t)n * n * (fp64_vectors ? 16 : 8) + 15) / 16 * 2;
+  const size_t smV = (zsz + usz) * sizeof(double);
   int GV = (2 * 32) / L;
   while (GV > 1 && GV * smV > 96 * 1024) GV /= 2;
   if (GV * smV > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  eigh_vectors<<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
-                                                                 (double2*)U, strideU);
+  if (fp64_vectors) {
+    cudaFuncSetAttribute(eigh_vectors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    eigh_vectors<double><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L,
+                                                                           GV, (double2*)U, strideU);
+  } else {
+    cudaFuncSetAttribute(eigh_vectors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    eigh_vectors<float><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L,
+                                                                          GV, (float2*)U, strideU);
+  }
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -2,302 +2,256 @@
 //
 // Replaces fourier/fft.py:133-192 (scatter + ifftn), fourier/rvectors.py:477-506
 // (expdK phase, derivative i(R + t_n - t_m)) and data_K/data_K_R.py:28-51,91-97
-// (rotAA, Xbar before rotation).
+// (rotAA and the R-space matrices behind Xbar).
 //
-// X(k_j) = sum_R exp(2 pi i R.(j/N + dK)) w(R) X_R is evaluated as a pruned
-// separable DFT over the R-vectors actually present (sorted by (R0,R1,R2)):
-//   stage A: contract R2 for every (R0,R1) "pair"       -> Z[pair][k2]
-//   stage B: contract R1 for every R0 "slice"           -> Y[slice][k1][k2]
-//   stage C: contract R0, then build Cartesian fields   -> fields[k][f]
-// Reduced-coordinate polynomial weights R_j, R_j R_l ride along each stage so that
-// first and second k-derivatives come out as moments; stage C turns the moments into
-// Cartesian derivatives with the Wannier-centre term (t_n - t_m) exactly as
-// rvectors.py:355-369,487-494 define them.  The same code runs in FP64 and FP32.
+// Two parts:
+//  * r2k_weights (once per system and field set): the R-space derivative / curl weights of
+//    rvectors.py:487-494 and data_K_R.py:48-51 applied to the base matrices, giving one
+//    R-space array per k-space field, XF[f][R][mn] -- the reference does the same in R-space
+//    before its FFT.
+//  * the per-block transform X(k_j) = sum_R exp(2 pi i R.(j/N + dK)) XF_R as a pruned
+//    separable DFT over the R-vectors actually present (sorted by (R0,R1,R2)):
+//      stage A: contract R2 inside each (R0,R1) "pair"   -> Z[blk][f][pair][k2]
+//      stage B: contract R1 inside each R0 "slice"       -> Y[blk][f][slice][k1][k2]
+//      stage C: contract R0                              -> out[blk*nk + k][f]
+//    Each thread keeps the (<= MAXL) inputs of its matrix elements in registers and loops
+//    over the output index; the per-axis phase tables are broadcast from shared memory.
 #include "wbgpu_common.cuh"
 #include "wbgpu_r2k.cuh"
 
 namespace {
 
-// moment q (0..9) -> (stage-B variant, power of R0); see header for the variant order
-__constant__ int kMomB[3][10] = {{0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
-                                 {0, 0, 1, 2, 0, 0, 0, 0, 0, 0},
-                                 {0, 0, 1, 3, 0, 1, 3, 2, 4, 5}};
-__constant__ int kMomE[3][10] = {{0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
-                                 {0, 1, 0, 0, 0, 0, 0, 0, 0, 0},
-                                 {0, 1, 0, 0, 2, 1, 1, 0, 0, 0}};
-// stage-B variant v -> (stage-A variant, power of R1)
-__constant__ int kVarA[3][6] = {{0, 0, 0, 0, 0, 0}, {0, 0, 1, 0, 0, 0}, {0, 0, 0, 1, 1, 2}};
-__constant__ int kVarT[3][6] = {{0, 0, 0, 0, 0, 0}, {0, 1, 0, 0, 0, 0}, {0, 1, 2, 0, 1, 0}};
+constexpr int kThreads = 128;
 
+// ---------------- R-space weights (once per system + field set) ----------------
+// grid: (ceil(nR*nw2/256), nF); XR [nBase][nR][nw2]; iR [nR][3] (sorted order)
 template <typename T>
-WBG_D T ipow(int r, int e) {
-  return e == 0 ? T(1) : (e == 1 ? T(r) : T(r) * T(r));
+__global__ void r2k_weights(const double2* __restrict__ XR, const int* __restrict__ iR, const int4* __restrict__ fdesc,
+                            const double* __restrict__ wcc, R2KLattice lat, int nBase, int nR, int nw,
+                            typename C2<T>::t* __restrict__ XF) {
+  typedef typename C2<T>::t V;
+  const int f = blockIdx.y;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nw2 = nw * nw;
+  if (idx >= (long long)nR * nw2) return;
+  const int r = (int)(idx / nw2), mn = (int)(idx % nw2);
+  const int m = mn / nw, n = mn % nw;
+  const int4 fd = fdesc[f];
+  // R + t_n - t_m (Cartesian), rvectors.py:355-360
+  double w[3];
+  for (int a = 0; a < 3; ++a)
+    w[a] = iR[r * 3 + 0] * lat.L[0 * 3 + a] + iR[r * 3 + 1] * lat.L[1 * 3 + a] + iR[r * 3 + 2] * lat.L[2 * 3 + a] +
+           wcc[n * 3 + a] - wcc[m * 3 + a];
+  const bool idx_ok = fd.z >= 0 && fd.z < 3 && fd.w >= 0 && fd.w < 3 && fd.y >= 0;
+  const bool ok = idx_ok && ((fd.x <= R2K_DER2 && fd.y < nBase) || (fd.x >= R2K_ROT && fd.y + 2 < nBase)) &&
+                  fd.x >= 0 && fd.x <= R2K_DROT;
+  double2 v = make_double2(0.0, 0.0);
+  if (!ok) {
+    v = make_double2(0.0 / 0.0, 0.0 / 0.0);  // invalid descriptor: NaN, no out-of-range read
+  } else if (fd.x == R2K_MOM0) {
+    v = XR[((long long)fd.y * nR + r) * nw2 + mn];
+  } else if (fd.x == R2K_DER1) {  // i w_a X
+    v = cmuli(cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], w[fd.z]));
+  } else if (fd.x == R2K_DER2) {  // -w_a w_b X
+    v = cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], -w[fd.z] * w[fd.w]);
+  } else {
+    // rotAA_g = i w_alpha A_beta - i w_beta A_alpha, (alpha, beta) = ((1,2),(2,0),(0,1))[g]
+    const int al = (fd.z + 1) % 3, be = (fd.z + 2) % 3;
+    const double2 Ab = XR[((long long)(fd.y + be) * nR + r) * nw2 + mn];
+    const double2 Aa = XR[((long long)(fd.y + al) * nR + r) * nw2 + mn];
+    v = cmuli(csub(cscale(Ab, w[al]), cscale(Aa, w[be])));
+    if (fd.x == R2K_DROT) v = cmuli(cscale(v, w[fd.w]));  // derivative of the curl
+  }
+  XF[((long long)f * nR + r) * nw2 + mn] = mkc<T>((T)v.x, (T)v.y);
+}
+
+// One separable contraction: out[col][j] = sum_{i < len} tab[j][idx[i]] in[col][i]
+// for every output index j < Nj.  `in` values of this thread stay in registers.
+template <typename T, int MAXL>
+WBG_D void contract(const typename C2<T>::t* x, int len, const typename C2<T>::t* tab_s, const int* ridx, int nr,
+                    int Nj, typename C2<T>::t* out, long long out_stride) {
+  typedef typename C2<T>::t V;
+  for (int j = 0; j < Nj; ++j) {
+    V acc = czero<V>();
+#pragma unroll
+    for (int i = 0; i < MAXL; ++i)
+      if (i < len) cfma(acc, tab_s[j * nr + ridx[i]], x[i]);
+    out[(long long)j * out_stride] = acc;
+  }
 }
 
 // ---------------- stage A: contract R2 inside each (R0,R1) pair ----------------
-// grid: (nP, nb*nBase, ceil(nw2/TILE)); block: TILE threads (one per matrix element)
-template <typename T>
-__global__ void r2k_stageA(const typename C2<T>::t* __restrict__ X, const int* __restrict__ pairStart,
-                           const int* __restrict__ r2, const typename C2<T>::t* __restrict__ ph2,
-                           typename C2<T>::t* __restrict__ Z, R2KGeom g, int order) {
+// grid: (ceil(nF*nw2/kThreads), nP, nb); XF [nF][nR][nw2] -> Z [nb][nF][nP][N2][nw2]
+template <typename T, int MAXL>
+__global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* __restrict__ XF,
+                                                       const int* __restrict__ pairStart, const int* __restrict__ r2,
+                                                       const typename C2<T>::t* __restrict__ ph2,
+                                                       typename C2<T>::t* __restrict__ Z, R2KGeom g, int nF) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smem_raw[];
-  V* Xs = reinterpret_cast<V*>(smem_raw);
-  const int p = blockIdx.x;
-  const int blk = blockIdx.y / g.nBase, b = blockIdx.y % g.nBase;
-  const int mn = blockIdx.z * blockDim.x + threadIdx.x;
-  const int nA = order + 1;
-  const int r0 = pairStart[p], len = pairStart[p + 1] - r0;
-  if (mn < g.nw2) {
-    for (int i = 0; i < len; ++i) Xs[i * blockDim.x + threadIdx.x] = X[((size_t)b * g.nR + r0 + i) * g.nw2 + mn];
-  }
+  extern __shared__ unsigned char smr[];
+  V* tab = reinterpret_cast<V*>(smr);  // [N2][nr2]
+  const int p = blockIdx.y, blk = blockIdx.z;
+  for (int i = threadIdx.x; i < g.N2 * g.nr2; i += blockDim.x) tab[i] = ph2[(long long)blk * g.N2 * g.nr2 + i];
   __syncthreads();
-  if (mn >= g.nw2) return;
-  const V* ph = ph2 + (size_t)blk * g.N2 * g.nr2;
-  for (int k2 = 0; k2 < g.N2; ++k2) {
-    V acc[3] = {czero<V>(), czero<V>(), czero<V>()};
-    for (int i = 0; i < len; ++i) {
-      const int R2 = r2[r0 + i];
-      V t = cmul(ph[k2 * g.nr2 + (R2 - g.rmin2)], Xs[i * blockDim.x + threadIdx.x]);
-      acc[0] = cadd(acc[0], t);
-      if (nA > 1) { cfma(acc[1], t, mkc<T>(T(R2), T(0))); }
-      if (nA > 2) { cfma(acc[2], t, mkc<T>(T(R2) * T(R2), T(0))); }
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (long long)nF * g.nw2) return;
+  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
+  const int r0 = pairStart[p], len = pairStart[p + 1] - r0;
+  V x[MAXL];
+  int ri[MAXL];
+#pragma unroll
+  for (int i = 0; i < MAXL; ++i) {
+    if (i < len) {
+      x[i] = XF[((long long)f * g.nR + r0 + i) * g.nw2 + mn];
+      ri[i] = r2[r0 + i] - g.rmin2;
+    } else {
+      x[i] = czero<V>();
+      ri[i] = 0;
     }
-    for (int s = 0; s < nA; ++s)
-      Z[((((size_t)blk * g.nBase + b) * nA + s) * g.nP + p) * ((size_t)g.N2 * g.nw2) + (size_t)k2 * g.nw2 + mn] = acc[s];
   }
+  V* out = Z + ((((long long)blk * nF + f) * g.nP + p) * g.N2) * g.nw2 + mn;
+  contract<T, MAXL>(x, len, tab, ri, g.nr2, g.N2, out, g.nw2);
 }
 
 // ---------------- stage B: contract R1 inside each R0 slice ----------------
-// grid: (nU*N2, nb*nBase, tiles); block: TILE threads
-template <typename T>
-__global__ void r2k_stageB(const typename C2<T>::t* __restrict__ Z, const int* __restrict__ sliceStart,
-                           const int* __restrict__ pairR1, const typename C2<T>::t* __restrict__ ph1,
-                           typename C2<T>::t* __restrict__ Y, R2KGeom g, int order) {
+// grid: (ceil(nF*nw2/kThreads), nU*N2, nb); Z -> Y [nb][nF][nU][N1][N2][nw2]
+template <typename T, int MAXL>
+__global__ void __launch_bounds__(kThreads) r2k_stageB(const typename C2<T>::t* __restrict__ Z,
+                                                       const int* __restrict__ sliceStart,
+                                                       const int* __restrict__ pairR1,
+                                                       const typename C2<T>::t* __restrict__ ph1,
+                                                       typename C2<T>::t* __restrict__ Y, R2KGeom g, int nF) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smem_raw[];
-  V* Zs = reinterpret_cast<V*>(smem_raw);
-  const int u = blockIdx.x / g.N2, k2 = blockIdx.x % g.N2;
-  const int blk = blockIdx.y / g.nBase, b = blockIdx.y % g.nBase;
-  const int mn = blockIdx.z * blockDim.x + threadIdx.x;
-  const int nA = order + 1, nB = order == 0 ? 1 : (order == 1 ? 3 : 6);
+  extern __shared__ unsigned char smr[];
+  V* tab = reinterpret_cast<V*>(smr);  // [N1][nr1]
+  const int u = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
+  for (int i = threadIdx.x; i < g.N1 * g.nr1; i += blockDim.x) tab[i] = ph1[(long long)blk * g.N1 * g.nr1 + i];
+  __syncthreads();
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (long long)nF * g.nw2) return;
+  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
   const int p0 = sliceStart[u], len = sliceStart[u + 1] - p0;
-  const int TILE = blockDim.x;
-  if (mn < g.nw2) {
-    for (int s = 0; s < nA; ++s)
-      for (int i = 0; i < len; ++i)
-        Zs[(s * len + i) * TILE + threadIdx.x] =
-            Z[((((size_t)blk * g.nBase + b) * nA + s) * g.nP + p0 + i) * ((size_t)g.N2 * g.nw2) + (size_t)k2 * g.nw2 + mn];
-  }
-  __syncthreads();
-  if (mn >= g.nw2) return;
-  const V* ph = ph1 + (size_t)blk * g.N1 * g.nr1;
-  for (int k1 = 0; k1 < g.N1; ++k1) {
-    V acc[6];
+  V x[MAXL];
+  int ri[MAXL];
 #pragma unroll
-    for (int v = 0; v < 6; ++v) acc[v] = czero<V>();
-    for (int i = 0; i < len; ++i) {
-      const int R1 = pairR1[p0 + i];
-      const V e = ph[k1 * g.nr1 + (R1 - g.rmin1)];
-#pragma unroll
-      for (int v = 0; v < 6; ++v) {
-        if (v < nB) {
-          const int sa = kVarA[order][v], t = kVarT[order][v];
-          V term = cmul(e, Zs[(sa * len + i) * TILE + threadIdx.x]);
-          acc[v] = cadd(acc[v], cscale(term, ipow<T>(R1, t)));
-        }
-      }
+  for (int i = 0; i < MAXL; ++i) {
+    if (i < len) {
+      x[i] = Z[((((long long)blk * nF + f) * g.nP + p0 + i) * g.N2 + k2) * g.nw2 + mn];
+      ri[i] = pairR1[p0 + i] - g.rmin1;
+    } else {
+      x[i] = czero<V>();
+      ri[i] = 0;
     }
-    const size_t plane = (size_t)g.N1 * g.N2 * g.nw2;
-    for (int v = 0; v < nB; ++v)
-      Y[((((size_t)blk * g.nBase + b) * nB + v) * g.nU + u) * plane + ((size_t)k1 * g.N2 + k2) * g.nw2 + mn] = acc[v];
   }
+  V* out = Y + (((((long long)blk * nF + f) * g.nU + u) * g.N1) * g.N2 + k2) * g.nw2 + mn;
+  contract<T, MAXL>(x, len, tab, ri, g.nr1, g.N1, out, (long long)g.N2 * g.nw2);
 }
 
-// Cartesian first / second moments from reduced ones (R_cart,a = sum_j iR_j L[j][a]).
-template <typename T, typename V>
-WBG_D V cart1(const V* M, const T* L, int a) {  // M[1..3] reduced first moments
-  V r = czero<V>();
-  for (int j = 0; j < 3; ++j) r = cadd(r, cscale(M[1 + j], L[j * 3 + a]));
-  return r;
-}
-template <typename T, typename V>
-WBG_D V cart2(const V* M, const T* L, int a, int b) {  // M[4..9] = 00,01,02,11,12,22
-  const int idx[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
-  V r = czero<V>();
-  for (int j = 0; j < 3; ++j)
-    for (int l = 0; l < 3; ++l) r = cadd(r, cscale(M[idx[j][l]], L[j * 3 + a] * L[l * 3 + b]));
-  return r;
-}
-// d/dk_a X = i (C_a + d_a M0)
-template <typename T, typename V>
-WBG_D V der1(const V* M, const T* L, const T* d, int a) {
-  return cmuli(cadd(cart1<T, V>(M, L, a), cscale(M[0], d[a])));
-}
-// d/dk_a d/dk_b X = -(C_ab + d_a C_b + d_b C_a + d_a d_b M0)
-template <typename T, typename V>
-WBG_D V der2(const V* M, const T* L, const T* d, int a, int b) {
-  V r = cart2<T, V>(M, L, a, b);
-  r = cadd(r, cscale(cart1<T, V>(M, L, b), d[a]));
-  r = cadd(r, cscale(cart1<T, V>(M, L, a), d[b]));
-  r = cadd(r, cscale(M[0], d[a] * d[b]));
-  return cscale(r, T(-1));
-}
-
-// ---------------- stage C: contract R0 and emit Cartesian fields ----------------
-// grid: (N1*N2, nb, tiles); block: TILE threads
-template <typename T>
-__global__ void r2k_stageC(const typename C2<T>::t* __restrict__ Y, const int* __restrict__ sliceR0,
-                           const typename C2<T>::t* __restrict__ ph0, const int4* __restrict__ fdesc,
-                           const T* __restrict__ wcc, typename C2<T>::t* __restrict__ out, R2KGeom g, int order,
-                           int nF, R2KLattice lat) {
+// ---------------- stage C: contract R0 ----------------
+// grid: (ceil(nF*nw2/kThreads), N1*N2, nb); Y -> out [nb*nk][nF][nw2]
+template <typename T, int MAXL>
+__global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* __restrict__ Y,
+                                                       const int* __restrict__ sliceR0,
+                                                       const typename C2<T>::t* __restrict__ ph0,
+                                                       typename C2<T>::t* __restrict__ out, R2KGeom g, int nF) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smem_raw[];
-  const int TILE = blockDim.x;
-  const int nB = order == 0 ? 1 : (order == 1 ? 3 : 6);
-  const int nM = order == 0 ? 1 : (order == 1 ? 4 : 10);
-  V* Ys = reinterpret_cast<V*>(smem_raw);                          // [nBase*nB][nU][TILE]
-  V* Ms = Ys + (size_t)g.nBase * nB * g.nU * TILE;                  // [nBase][nM][TILE]
-  const int k1 = blockIdx.x / g.N2, k2 = blockIdx.x % g.N2;
-  const int blk = blockIdx.y;
-  const int mn = blockIdx.z * TILE + threadIdx.x;
-  const bool active = mn < g.nw2;
-  const size_t plane = (size_t)g.N1 * g.N2 * g.nw2;
-  if (active) {
-    for (int bv = 0; bv < g.nBase * nB; ++bv)
-      for (int u = 0; u < g.nU; ++u)
-        Ys[((size_t)bv * g.nU + u) * TILE + threadIdx.x] =
-            Y[(((size_t)blk * g.nBase * nB + bv) * g.nU + u) * plane + ((size_t)k1 * g.N2 + k2) * g.nw2 + mn];
-  }
+  extern __shared__ unsigned char smr[];
+  V* tab = reinterpret_cast<V*>(smr);  // [N0][nr0]
+  const int k1 = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
+  for (int i = threadIdx.x; i < g.N0 * g.nr0; i += blockDim.x) tab[i] = ph0[(long long)blk * g.N0 * g.nr0 + i];
   __syncthreads();
-  if (!active) return;
-  T L[9];
-  for (int i = 0; i < 9; ++i) L[i] = (T)lat.L[i];
-  const int m = mn / g.nw, n = mn % g.nw;
-  T d[3];
-  for (int a = 0; a < 3; ++a) d[a] = wcc[n * 3 + a] - wcc[m * 3 + a];
-  const V* ph = ph0 + (size_t)blk * g.N0 * g.nr0;
-  V* myM = Ms + threadIdx.x;
-  for (int k0 = 0; k0 < g.N0; ++k0) {
-    const size_t k = ((size_t)k0 * g.N1 + k1) * g.N2 + k2;
-    for (int b = 0; b < g.nBase; ++b) {
-      V acc[10];
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (long long)nF * g.nw2) return;
+  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
+  const int len = g.nU;
+  V x[MAXL];
+  int ri[MAXL];
 #pragma unroll
-      for (int q = 0; q < 10; ++q) acc[q] = czero<V>();
-      for (int u = 0; u < g.nU; ++u) {
-        const int R0 = sliceR0[u];
-        const V e = ph[k0 * g.nr0 + (R0 - g.rmin0)];
-        const T r = T(R0);
-#pragma unroll
-        for (int q = 0; q < 10; ++q) {
-          if (q < nM) {
-            V t = cmul(e, Ys[((size_t)(b * nB + kMomB[order][q]) * g.nU + u) * TILE + threadIdx.x]);
-            const int ee = kMomE[order][q];
-            if (ee >= 1) t = cscale(t, r);
-            if (ee >= 2) t = cscale(t, r);
-            acc[q] = cadd(acc[q], t);
-          }
-        }
-      }
-      for (int q = 0; q < nM; ++q) myM[((size_t)b * nM + q) * TILE] = acc[q];
-    }
-    // epilogue: build the requested fields for element (m, n)
-    V Mb[10], Mc[10];
-    for (int f = 0; f < nF; ++f) {
-      const int4 fd = fdesc[f];
-      V val = czero<V>();
-      // descriptors live in device memory: validate here, emit NaN for an invalid one
-      const bool idx_ok = fd.z >= 0 && fd.z < 3 && fd.w >= 0 && fd.w < 3 && fd.y >= 0;
-      const bool ok = idx_ok && ((fd.x == R2K_MOM0 && fd.y < g.nBase) ||
-                                 (fd.x == R2K_DER1 && order >= 1 && fd.y < g.nBase) ||
-                                 (fd.x == R2K_DER2 && order >= 2 && fd.y < g.nBase) ||
-                                 (fd.x == R2K_ROT && order >= 1 && fd.y + 2 < g.nBase) ||
-                                 (fd.x == R2K_DROT && order >= 2 && fd.y + 2 < g.nBase));
-      if (!ok) {
-        const T nan = T(0) / T(0);
-        val = mkc<T>(nan, nan);
-      } else if (fd.x == R2K_MOM0) {
-        val = myM[((size_t)fd.y * nM + 0) * TILE];
-      } else if (fd.x == R2K_DER1) {
-        for (int q = 0; q < 4; ++q) Mb[q] = myM[((size_t)fd.y * nM + q) * TILE];
-        val = der1<T, V>(Mb, L, d, fd.z);
-      } else if (fd.x == R2K_DER2) {
-        for (int q = 0; q < 10; ++q) Mb[q] = myM[((size_t)fd.y * nM + q) * TILE];
-        val = der2<T, V>(Mb, L, d, fd.z, fd.w);
-      } else if (fd.x == R2K_ROT || fd.x == R2K_DROT) {
-        // rotAA_g = d_alpha A_beta - d_beta A_alpha with (alpha, beta) = ((1,2),(2,0),(0,1))[g]
-        const int al = (fd.z + 1) % 3, be = (fd.z + 2) % 3;
-        const int nq = fd.x == R2K_ROT ? 4 : 10;
-        for (int q = 0; q < nq; ++q) {
-          Mb[q] = myM[((size_t)(fd.y + be) * nM + q) * TILE];
-          Mc[q] = myM[((size_t)(fd.y + al) * nM + q) * TILE];
-        }
-        if (fd.x == R2K_ROT)
-          val = csub(der1<T, V>(Mb, L, d, al), der1<T, V>(Mc, L, d, be));
-        else
-          val = csub(der2<T, V>(Mb, L, d, fd.w, al), der2<T, V>(Mc, L, d, fd.w, be));
-      }
-      out[((size_t)blk * g.nk + k) * ((size_t)nF * g.nw2) + (size_t)f * g.nw2 + mn] = val;
+  for (int i = 0; i < MAXL; ++i) {
+    if (i < len) {
+      x[i] = Y[(((((long long)blk * nF + f) * g.nU + i) * g.N1 + k1) * g.N2 + k2) * g.nw2 + mn];
+      ri[i] = sliceR0[i] - g.rmin0;
+    } else {
+      x[i] = czero<V>();
+      ri[i] = 0;
     }
   }
+  const long long kstride = (long long)g.N1 * g.N2 * nF * g.nw2;  // k0 -> k0+1
+  V* o = out + (((long long)blk * g.nk + (long long)k1 * g.N2 + k2) * nF + f) * g.nw2 + mn;
+  contract<T, MAXL>(x, len, tab, ri, g.nr0, g.N0, o, kstride);
+}
+
+template <typename T, int MAXL>
+void launch_stages(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart,
+                   const int* pairR1, const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z,
+                   void* Y, void* out, const R2KGeom& g, int nb, cudaStream_t stream) {
+  typedef typename C2<T>::t V;
+  const unsigned colBlocks = (unsigned)(((long long)nF * g.nw2 + kThreads - 1) / kThreads);
+  r2k_stageA<T, MAXL><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
+      (const V*)XF, pairStart, r2, (const V*)ph2, (V*)Z, g, nF);
+  r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, (size_t)g.N1 * g.nr1 * sizeof(V), stream>>>(
+      (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF);
+  r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, (size_t)g.N0 * g.nr0 * sizeof(V), stream>>>(
+      (const V*)Y, sliceR0, (const V*)ph0, (V*)out, g, nF);
 }
 
 template <typename T>
-int launch_r2k(const void* X, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
-               const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, const int4* fdesc,
-               const void* wcc, void* Z, void* Y, void* out, const R2KGeom& g, int order, int nF,
-               const R2KLattice& lat, int nb, cudaStream_t stream) {
-  typedef typename C2<T>::t V;
-  const int nA = order + 1, nB = order == 0 ? 1 : (order == 1 ? 3 : 6);
-  const int nM = order == 0 ? 1 : (order == 1 ? 4 : 10);
-  // tile sizes: largest power of two <= 64 whose shared-memory footprint fits
-  int tileC = 64;
-  auto smemC = [&](int t) { return (size_t)t * sizeof(V) * ((size_t)g.nBase * nB * g.nU + (size_t)g.nBase * nM); };
-  while (tileC > 8 && smemC(tileC) > 200 * 1024) tileC /= 2;
-  if (smemC(tileC) > 220 * 1024) return WBG_ERR_SIZE;
-  const int tileA = 64, tileB = 64;
-  const size_t smemA = (size_t)tileA * g.maxPairLen * sizeof(V);
-  const size_t smemB = (size_t)tileB * nA * g.maxSliceLen * sizeof(V);
-  if (smemA > 220 * 1024 || smemB > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(r2k_stageA<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  cudaFuncSetAttribute(r2k_stageB<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  cudaFuncSetAttribute(r2k_stageC<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  dim3 gA(g.nP, nb * g.nBase, (g.nw2 + tileA - 1) / tileA);
-  r2k_stageA<T><<<gA, tileA, smemA, stream>>>((const V*)X, pairStart, r2, (const V*)ph2, (V*)Z, g, order);
-  dim3 gB(g.nU * g.N2, nb * g.nBase, (g.nw2 + tileB - 1) / tileB);
-  r2k_stageB<T><<<gB, tileB, smemB, stream>>>((const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, order);
-  dim3 gC(g.N1 * g.N2, nb, (g.nw2 + tileC - 1) / tileC);
-  r2k_stageC<T><<<gC, tileC, smemC(tileC), stream>>>((const V*)Y, sliceR0, (const V*)ph0, fdesc, (const T*)wcc,
-                                                     (V*)out, g, order, nF, lat);
+int launch_r2k(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
+               const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z, void* Y, void* out,
+               const R2KGeom& g, int nb, cudaStream_t stream) {
+  const int maxlen = max(max(g.maxPairLen, g.maxSliceLen), g.nU);
+  if (maxlen <= 8)
+    launch_stages<T, 8>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+  else if (maxlen <= 16)
+    launch_stages<T, 16>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+  else if (maxlen <= 24)
+    launch_stages<T, 24>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+  else if (maxlen <= WBG_R2K_MAXLEN)
+    launch_stages<T, WBG_R2K_MAXLEN>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
+                                     nb, stream);
+  else
+    return WBG_ERR_SIZE;
   return wbg_cuda_status(cudaGetLastError());
 }
 
 }  // namespace
 
-size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int order, int nb, int fp64) {
+size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int fp64) {
   const size_t cs = fp64 ? sizeof(double2) : sizeof(float2);
-  const int nA = order + 1, nB = order == 0 ? 1 : (order == 1 ? 3 : 6);
-  const size_t z = (size_t)nb * g->nBase * nA * g->nP * g->N2 * g->nw2 * cs;
-  const size_t y = (size_t)nb * g->nBase * nB * g->nU * g->N1 * g->N2 * g->nw2 * cs;
+  const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
+  const size_t y = (size_t)nb * nF * g->nU * g->N1 * g->N2 * g->nw2 * cs;
   return ((z + 255) / 256) * 256 + y;
 }
 
-int wbg_r2k_run(const void* X, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
-                const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, const int4* fdesc,
-                const void* wcc, void* workspace, size_t workspace_bytes, void* out, const R2KGeom* g, int order,
-                int nF, const R2KLattice* lat, int nb, int fp64, cudaStream_t stream) {
-  if (!g || !lat || order < 0 || order > 2 || nF <= 0 || nb <= 0) return WBG_ERR_ARG;
+int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, int nw, const int4* fdesc, int nF,
+                       const double* wcc, const R2KLattice* lat, int fp64, void* XF, cudaStream_t stream) {
+  if (!XR || !iRsorted || !fdesc || !wcc || !lat || !XF || nBase < 1 || nR < 1 || nw < 1 || nF < 1)
+    return WBG_ERR_ARG;
+  const long long n = (long long)nR * nw * nw;
+  dim3 grid((unsigned)((n + 255) / 256), nF);
+  if (fp64)
+    r2k_weights<double><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+                                                  (double2*)XF);
+  else
+    r2k_weights<float><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+                                                 (float2*)XF);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
+                const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
+                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int fp64, cudaStream_t stream) {
+  if (!g || nF <= 0 || nb <= 0) return WBG_ERR_ARG;
   if (g->nw2 != g->nw * g->nw || g->nk != g->N0 * g->N1 * g->N2) return WBG_ERR_ARG;
-  const size_t need = wbg_r2k_workspace_bytes(g, order, nb, fp64);
-  if (workspace_bytes < need) return WBG_ERR_WORKSPACE;
+  if (g->nU < 1 || g->nP < 1 || g->maxPairLen < 1 || g->maxSliceLen < 1) return WBG_ERR_ARG;
+  if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, fp64)) return WBG_ERR_WORKSPACE;
   const size_t cs = fp64 ? sizeof(double2) : sizeof(float2);
-  const int nA = order + 1;
-  const size_t z = (size_t)nb * g->nBase * nA * g->nP * g->N2 * g->nw2 * cs;
+  const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   char* Z = (char*)workspace;
   char* Y = Z + ((z + 255) / 256) * 256;
   if (fp64)
-    return launch_r2k<double>(X, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, fdesc, wcc, Z, Y, out,
-                              *g, order, nF, *lat, nb, stream);
-  return launch_r2k<float>(X, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, fdesc, wcc, Z, Y, out, *g,
-                           order, nF, *lat, nb, stream);
+    return launch_r2k<double>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+                              stream);
+  return launch_r2k<float>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+                           stream);
 }

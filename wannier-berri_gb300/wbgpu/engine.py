@@ -183,7 +183,7 @@ class DeviceSystem:
             g = self.geom
             mk = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).to(self.device)
             self._cache['geom'] = dict(pair_start=mk(g.pair_start), r2=mk(g.r2), slice_start=mk(g.slice_start),
-                                       pair_r1=mk(g.pair_r1), slice_r0=mk(g.slice_r0))
+                                       pair_r1=mk(g.pair_r1), slice_r0=mk(g.slice_r0), iR=mk(g.R))
         return self._cache['geom']
 
     def wcc_tensor(self, fp64):
@@ -261,47 +261,69 @@ class BandData:
         return self.nblocks * self.nk
 
 
-def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
-    """Run the R->k stage for a batch of blocks; returns (fields, index, nF)."""
-    NKFFT = [int(n) for n in NKFFT]
-    keys = extra_keys_for(quantities)
-    names = dev.bases_for(keys)
-    order = order_for(quantities)
-    desc, index = field_plan(quantities, with_H, keys)
-    nF = len(desc)
-    nb = len(dKs)
+def r2k_geometry(dev, NKFFT):
     g = dev.geom
     nw = dev.nw
+    return _lib.R2KGeom(nR=len(g.R), nw=nw, nw2=nw * nw, nBase=0, nP=g.nP, nU=g.nU,
+                        N0=NKFFT[0], N1=NKFFT[1], N2=NKFFT[2], nk=int(np.prod(NKFFT)),
+                        nr0=int(g.nr[0]), nr1=int(g.nr[1]), nr2=int(g.nr[2]),
+                        rmin0=int(g.rmin[0]), rmin1=int(g.rmin[1]), rmin2=int(g.rmin[2]),
+                        maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
+
+
+def field_arrays(dev, quantities, with_H, fp64):
+    """R-space arrays XF[f][R][mn] of the requested k-space fields (wbg_r2k_fields), cached on
+    the device system: the derivative / curl weights depend on the system only, not on dK."""
+    keys = extra_keys_for(quantities)
+    desc, index = field_plan(quantities, with_H, keys)
+    ck = ('XF', tuple(sorted(quantities)), with_H, fp64)
+    if ck not in dev._cache:
+        names = dev.bases_for(keys)
+        X = dev.XR(names, True)
+        nR, nw = len(dev.geom.R), dev.nw
+        lat = _lib.Lattice()
+        for i, v in enumerate(dev.lattice.reshape(-1)):
+            lat.L[i] = float(v)
+        fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
+        XF = torch.empty((len(desc), nR, nw * nw), dtype=torch.complex128 if fp64 else torch.complex64,
+                         device=dev.device)
+        st = _lib.load().wbg_r2k_fields(_ptr(X), len(names), _ptr(dev.geom_tensors()['iR']), nR, nw, _ptr(fd),
+                                        len(desc), _ptr(dev.wcc_tensor(True)), ctypes.byref(lat), int(fp64), _ptr(XF),
+                                        _stream())
+        _lib.check(st, "wbg_r2k_fields")
+        dev._cache[ck] = (XF, index, len(desc), fd)
+    return dev._cache[ck]
+
+
+def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
+    """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive)."""
+    NKFFT = [int(n) for n in NKFFT]
+    XF, index, nF, _ = field_arrays(dev, quantities, with_H, fp64)
+    nb = len(dKs)
+    nw = dev.nw
     nk = int(np.prod(NKFFT))
-    geo = _lib.R2KGeom(nR=len(g.R), nw=nw, nw2=nw * nw, nBase=len(names), nP=g.nP, nU=g.nU,
-                       N0=NKFFT[0], N1=NKFFT[1], N2=NKFFT[2], nk=nk,
-                       nr0=int(g.nr[0]), nr1=int(g.nr[1]), nr2=int(g.nr[2]),
-                       rmin0=int(g.rmin[0]), rmin1=int(g.rmin[1]), rmin2=int(g.rmin[2]),
-                       maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
-    lat = _lib.Lattice()
-    for i, v in enumerate(dev.lattice.reshape(-1)):
-        lat.L[i] = float(v)
+    geo = r2k_geometry(dev, NKFFT)
     lib = _lib.load()
     ws = ctypes.c_size_t(0)
-    _lib.check(lib.wbg_r2k_workspace_size(ctypes.byref(geo), order, nb, int(fp64), ctypes.byref(ws)), "wbg_r2k_workspace_size")
+    _lib.check(lib.wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, int(fp64), ctypes.byref(ws)),
+               "wbg_r2k_workspace_size")
     cdt = torch.complex128 if fp64 else torch.complex64
     if workspace is None or workspace.numel() < ws.value:
         workspace = torch.empty(int(ws.value), dtype=torch.uint8, device=dev.device)
     if out is None:
         out = torch.empty((nb * nk, nF, nw, nw), dtype=cdt, device=dev.device)
-    ph = [torch.from_numpy(p).to(dev.device).to(cdt).contiguous() for p in g.phases(dKs, NKFFT)]
-    fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
+    ph = [torch.from_numpy(p).to(dev.device).to(cdt).contiguous() for p in dev.geom.phases(dKs, NKFFT)]
     gt = dev.geom_tensors()
-    X = dev.XR(names, fp64)
-    st = _timed('r2k_fp64' if fp64 else 'r2k_fp32', lib.wbg_r2k, _ptr(X), _ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
-                     _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[1]), _ptr(ph[2]), _ptr(fd), nF,
-                     _ptr(dev.wcc_tensor(fp64)), order, nb, int(fp64), _ptr(workspace), ctypes.c_size_t(workspace.numel()),
-                     _ptr(out), ctypes.byref(geo), ctypes.byref(lat), _stream())
+    st = _timed('r2k_fp64' if fp64 else 'r2k_fp32', lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
+                _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']), _ptr(gt['slice_r0']),
+                _ptr(ph[0]), _ptr(ph[1]), _ptr(ph[2]), nb, int(fp64), _ptr(workspace),
+                ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
     _lib.check(st, "wbg_r2k")
-    return out, index, nF, (ph, fd, workspace)
+    return out, index, nF, (ph, workspace)
 
 
-def eigh(Hfields, strideH, nw, nk, E=None, U=None):
+def eigh(Hfields, strideH, nw, nk, E=None, U=None, fp64_vectors=True):
+    """Batched eigensolver; U is complex128 (fp64_vectors) or complex64."""
     lib = _lib.load()
     dev = Hfields.device
     ws = ctypes.c_size_t(0)
@@ -310,10 +332,10 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None):
     if E is None:
         E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
     if U is None:
-        U = torch.empty((nk, nw, nw), dtype=torch.complex128, device=dev)
+        U = torch.empty((nk, nw, nw), dtype=torch.complex128 if fp64_vectors else torch.complex64, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw, _ptr(work),
-                              ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
+    st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw,
+                int(fp64_vectors), _ptr(work), ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
     _lib.check(st, "wbg_eigh_batched")
     return E, U, flag
 
@@ -349,7 +371,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
     elif precision == 'mixed':
         Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, True)
         keep.append(k0)
-        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk)
+        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, fp64_vectors=False)
         del Hf
         fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, False, False)
         keep.append(k1)
