@@ -66,6 +66,96 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
   }
 }
 
+// Register-tiled rotation for nw % 4 == 0: each thread owns a 4x4 tile of the nw x nw
+// output; KB k-points per CTA.  X rows are padded (stride nw+1) so the column reads of
+// different tile rows fall in different banks.  Same math as rotate_kernel.
+template <typename T>
+__global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long strideU,
+                             const typename C2<T>::t* __restrict__ X, int nFin, const int* __restrict__ fsel,
+                             const int* __restrict__ herm, int nFrot, typename C2<T>::t* __restrict__ Xbar, int nw,
+                             int nk, int KB) {
+  typedef typename C2<T>::t V;
+  extern __shared__ unsigned char smr[];
+  const int nt = nw / 4;                 // tiles per dimension
+  const int tpk = nt * nt;               // threads per k-point
+  const int kl = threadIdx.x / tpk, tid = threadIdx.x % tpk;
+  const int ty = tid / nt, tx = tid % nt;
+  const int ldx = nw + 1;
+  V* base = reinterpret_cast<V*>(smr) + (size_t)kl * (nw * nw + nw * ldx + nw * nw);
+  V* Us = base;                          // [nw][nw]
+  V* Xs = Us + nw * nw;                  // [nw][nw+1]
+  V* Ts = Xs + nw * ldx;                 // [nw][nw]
+  long long k = (long long)blockIdx.x * KB + kl;
+  const bool valid = k < nk;
+  if (!valid) k = nk - 1;
+  const int nw2 = nw * nw;
+  for (int i = tid; i < nw2; i += tpk) Us[i] = U[k * strideU + i];
+  const int m0 = 4 * ty, n0 = 4 * tx;
+  for (int f = 0; f < nFrot; ++f) {
+    const int fs = fsel[f];
+    const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
+    const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw2;
+    const T nan = T(0) / T(0);
+    for (int i = tid; i < nw2; i += tpk) Xs[(i / nw) * ldx + (i % nw)] = fok ? src[i] : mkc<T>(nan, nan);
+    __syncthreads();
+    V acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = czero<V>();
+    for (int j = 0; j < nw; ++j) {  // T = X U
+      V xa[4], ub[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) xa[a] = Xs[(m0 + a) * ldx + j];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) ub[b] = Us[j * nw + n0 + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cfma(acc[a][b], xa[a], ub[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) Ts[(m0 + a) * nw + n0 + b] = acc[a][b];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = czero<V>();
+    for (int j = 0; j < nw; ++j) {  // Y = U^dagger T
+      V ua[4], tb[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) ua[a] = Us[j * nw + m0 + a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) tb[b] = Ts[j * nw + n0 + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cfmac(acc[a][b], ua[a], tb[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) Xs[(m0 + a) * ldx + n0 + b] = acc[a][b];
+    __syncthreads();
+    V* dst = Xbar + (k * nFrot + f) * (long long)nw2;
+    const bool h = herm[f] != 0;
+    if (valid) {
+      for (int i = tid; i < nw2; i += tpk) {
+        const int m = i / nw, n = i % nw;
+        V y = Xs[m * ldx + n];
+        if (h) {
+          const V yt = Xs[n * ldx + m];
+          y = mkc<T>((T)0.5 * (y.x + yt.x), (T)0.5 * (y.y - yt.y));
+        }
+        dst[i] = y;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 WBG_D int group_sum_i(int v, int L) {
   for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
@@ -227,24 +317,36 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
+template <typename T>
+int launch_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
+                  int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
+  typedef typename C2<T>::t V;
+  if (nw % 4 == 0 && nw >= 8) {
+    const int tpk = (nw / 4) * (nw / 4);
+    const size_t per_k = ((size_t)nw * nw * 2 + (size_t)nw * (nw + 1)) * sizeof(V);
+    int KB = 1;
+    while (KB * 2 * tpk <= 256 && (KB * 2) * per_k <= 64 * 1024) KB *= 2;
+    if (KB * per_k <= 200 * 1024) {
+      cudaFuncSetAttribute(rotate_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      rotate_tiled<T><<<(nk + KB - 1) / KB, KB * tpk, KB * per_k, stream>>>((const V*)U, strideU, (const V*)X, nFin,
+                                                                           fsel, herm, nFrot, (V*)Xbar, nw, nk, KB);
+      return wbg_cuda_status(cudaGetLastError());
+    }
+  }
+  const size_t sm = 3 * (size_t)nw * nw * sizeof(V);
+  if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  cudaFuncSetAttribute(rotate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  rotate_kernel<T><<<nk, 256, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm, nFrot, (V*)Xbar, nw);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
 }  // namespace
 
 int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream) {
   if (nw < 1 || nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
-  const size_t cs = fp64 ? sizeof(double2) : sizeof(float2);
-  const size_t sm = 3 * (size_t)nw * nw * cs;
-  if (sm > 220 * 1024) return WBG_ERR_SIZE;
-  if (fp64) {
-    cudaFuncSetAttribute(rotate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    rotate_kernel<double><<<nk, 256, sm, stream>>>((const double2*)U, strideU, (const double2*)X, nFin, fsel, herm,
-                                                   nFrot, (double2*)Xbar, nw);
-  } else {
-    cudaFuncSetAttribute(rotate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    rotate_kernel<float><<<nk, 256, sm, stream>>>((const float2*)U, strideU, (const float2*)X, nFin, fsel, herm,
-                                                  nFrot, (float2*)Xbar, nw);
-  }
-  return wbg_cuda_status(cudaGetLastError());
+  if (fp64) return launch_rotate<double>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
+  return launch_rotate<float>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
 }
 
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,

@@ -25,9 +25,17 @@ WBG_D double group_sum(double v, int L) {
 
 // ---------------------------------------------------------------------------------------
 // 1. Householder tridiagonalisation.  grid: ceil(nk/G) blocks of G*L threads.
+// Only the lower triangle of the Hermitian matrix is kept up to date (row stride n+1 avoids
+// shared-memory bank conflicts).  Lane l of a group owns the mirrored row pairs
+// (2Lt + l, 2Lt + 2L-1-l), so the triangular rank-2 update is balanced across lanes;
+// L = max(4, pow2ceil(n)/2), i.e. two matrices share a warp for 16 < n <= 32.
 // Outputs: Vh[k][c][i] (v of reflector c, v_{c+1}=1, zeros for i<=c), tau[k][c],
 //          d[k][i], e[k][i] (e[n-1] = 0).
 // ---------------------------------------------------------------------------------------
+WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
+  return 2 * L * t + (half ? 2 * L - 1 - l : l);
+}
+
 __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, int n, int nk, int L, int G,
                              double2* __restrict__ Vh, double2* __restrict__ tauOut, double* __restrict__ dOut,
                              double* __restrict__ eOut) {
@@ -36,22 +44,29 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;  // redundant work keeps every lane of the warp in the same control flow
-  double2* A = sm + (size_t)grp * (n * n + 2 * n);
-  double2* vs = A + n * n;
+  const int ld = n + 1;
+  double2* A = sm + (size_t)grp * (n * ld + 2 * n);
+  double2* vs = A + n * ld;
   double2* ws = vs + n;
   const double2* Hk = H + k * strideK;
   for (int idx = lane; idx < n * n; idx += L) {
     const int i = idx / n, j = idx % n;
-    const double2 a = Hk[i * n + j], b = Hk[j * n + i];
-    A[idx] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    if (j <= i) {
+      const double2 a = Hk[i * n + j], b = Hk[j * n + i];
+      A[i * ld + j] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    }
   }
   __syncwarp();
+  const int T = (n + 2 * L - 1) / (2 * L);
   for (int c = 0; c < n - 1; ++c) {
     double xn = 0.0;
-    for (int i = lane; i < n; i += L)
-      if (i >= c + 2) { const double2 x = A[i * n + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
+    for (int t = 0; t < T; ++t)
+      for (int h = 0; h < 2; ++h) {
+        const int i = owned_row(t, h, lane, L);
+        if (i < n && i >= c + 2) { const double2 x = A[i * ld + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
+      }
     xn = group_sum(xn, L);
-    const double2 alpha = A[(c + 1) * n + c];
+    const double2 alpha = A[(c + 1) * ld + c];
     double beta, tr = 0.0, ti = 0.0;
     double2 scale = make_double2(0.0, 0.0);
     if (xn == 0.0 && alpha.y == 0.0) {
@@ -59,28 +74,35 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
     } else {
       const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
       beta = alpha.x >= 0.0 ? -nrm : nrm;
-      tr = (beta - alpha.x) / beta;
-      ti = -alpha.y / beta;
+      const double rb = 1.0 / beta;
+      tr = (beta - alpha.x) * rb;
+      ti = -alpha.y * rb;
       // scale = 1 / (alpha - beta)
       const double ar = alpha.x - beta, ai = alpha.y;
-      const double den = ar * ar + ai * ai;
-      scale = make_double2(ar / den, -ai / den);
+      const double rden = 1.0 / (ar * ar + ai * ai);
+      scale = make_double2(ar * rden, -ai * rden);
     }
     const double2 tau = make_double2(tr, ti);
     // executed unconditionally (tau = 0 makes it a no-op) so that every lane of the warp
     // reaches the same __syncwarp / shuffle calls when several matrices share a warp
-    {
-      for (int i = lane; i < n; i += L) {
-        if (i == c + 1) { vs[i] = make_double2(1.0, 0.0); A[i * n + c] = vs[i]; }
-        else if (i >= c + 2) { const double2 v = cmul(A[i * n + c], scale); vs[i] = v; A[i * n + c] = v; }
+    for (int t = 0; t < T; ++t)
+      for (int h = 0; h < 2; ++h) {
+        const int i = owned_row(t, h, lane, L);
+        if (i < n) {
+          if (i == c + 1) { vs[i] = make_double2(1.0, 0.0); A[i * ld + c] = vs[i]; }
+          else if (i >= c + 2) { const double2 v = cmul(A[i * ld + c], scale); vs[i] = v; A[i * ld + c] = v; }
+        }
       }
-      __syncwarp();
-      // p = tau * A v ; partial dot w^dagger v
-      double dr = 0.0, di = 0.0;
-      for (int i = lane; i < n; i += L) {
-        if (i >= c + 1) {
+    __syncwarp();
+    // p = tau * A v over the full Hermitian row: lower part A[i][j], upper part conj(A[j][i])
+    double dr = 0.0, di = 0.0;
+    for (int t = 0; t < T; ++t)
+      for (int h = 0; h < 2; ++h) {
+        const int i = owned_row(t, h, lane, L);
+        if (i < n && i >= c + 1) {
           double2 acc = make_double2(0.0, 0.0);
-          for (int j = c + 1; j < n; ++j) cfma(acc, A[i * n + j], vs[j]);
+          for (int j = c + 1; j <= i; ++j) cfma(acc, A[i * ld + j], vs[j]);
+          for (int j = i + 1; j < n; ++j) cfmac(acc, A[j * ld + i], vs[j]);
           const double2 p = cmul(tau, acc);
           ws[i] = p;
           const double2 v = vs[i];
@@ -88,44 +110,45 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
           di = fma(p.x, v.y, fma(-p.y, v.x, di));
         }
       }
-      dr = group_sum(dr, L);
-      di = group_sum(di, L);
-      // alpha2 = -1/2 tau (w^dagger v)
-      const double2 a2 = cscale(cmul(tau, make_double2(dr, di)), -0.5);
-      for (int i = lane; i < n; i += L)
-        if (i >= c + 1) cfma(ws[i], a2, vs[i]);
-      __syncwarp();
-      for (int i = lane; i < n; i += L) {
-        if (i >= c + 1) {
+    dr = group_sum(dr, L);
+    di = group_sum(di, L);
+    // alpha2 = -1/2 tau (w^dagger v)
+    const double2 a2 = cscale(cmul(tau, make_double2(dr, di)), -0.5);
+    for (int t = 0; t < T; ++t)
+      for (int h = 0; h < 2; ++h) {
+        const int i = owned_row(t, h, lane, L);
+        if (i < n && i >= c + 1) cfma(ws[i], a2, vs[i]);
+      }
+    __syncwarp();
+    // lower-triangle rank-2 update: A[i][j] -= v_i conj(w_j) + w_i conj(v_j), c+1 <= j <= i
+    for (int t = 0; t < T; ++t)
+      for (int h = 0; h < 2; ++h) {
+        const int i = owned_row(t, h, lane, L);
+        if (i < n && i >= c + 1) {
           const double2 vi = vs[i], wi = ws[i];
-          for (int j = c + 1; j < n; ++j) {
-            double2 a = A[i * n + j];
+          for (int j = c + 1; j <= i; ++j) {
+            double2 a = A[i * ld + j];
             const double2 vj = vs[j], wj = ws[j];
-            // a -= v_i conj(w_j) + w_i conj(v_j)
             a.x -= vi.x * wj.x + vi.y * wj.y + wi.x * vj.x + wi.y * vj.y;
             a.y -= vi.y * wj.x - vi.x * wj.y + wi.y * vj.x - wi.x * vj.y;
-            A[i * n + j] = a;
+            A[i * ld + j] = a;
           }
         }
       }
-      __syncwarp();
-    }
+    __syncwarp();
     if (valid) {
-      for (int i = lane; i < n; i += L) {
-        double2 v = make_double2(0.0, 0.0);
-        if (tr != 0.0 || ti != 0.0) { if (i >= c + 1) v = A[i * n + c]; }
-        Vh[(k * n + c) * n + i] = v;
-      }
+      const bool refl = (tr != 0.0 || ti != 0.0);
+      for (int i = lane; i < n; i += L) Vh[(k * n + c) * n + i] = (refl && i >= c + 1) ? A[i * ld + c] : make_double2(0.0, 0.0);
       if (lane == 0) {
         tauOut[k * n + c] = tau;
         eOut[k * n + c] = beta;
-        dOut[k * n + c] = A[c * n + c].x;
+        dOut[k * n + c] = A[c * ld + c].x;
       }
     }
     __syncwarp();
   }
   if (valid && lane == 0) {
-    dOut[k * n + n - 1] = A[(n - 1) * n + n - 1].x;
+    dOut[k * n + n - 1] = A[(n - 1) * ld + n - 1].x;
     eOut[k * n + n - 1] = 0.0;
     tauOut[k * n + n - 1] = make_double2(0.0, 0.0);
   }
@@ -356,12 +379,14 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   double* d = (double*)w; w += (size_t)nk * n * 8;
   double* e = (double*)w;
   const int L = lanes_for(n);
-  const size_t smT = ((size_t)n * n + 2 * n) * sizeof(double2);
-  int G = (4 * 32) / L;
+  const int LT = L >= 8 ? L / 2 : 4;  // tridiagonalisation: mirrored row pairs, half the lanes
+  const size_t smT = ((size_t)n * (n + 1) + 2 * n) * sizeof(double2);
+  int G = (4 * 32) / LT;
   while (G > 1 && G * smT > 96 * 1024) G /= 2;
   if (G * smT > 220 * 1024) return WBG_ERR_SIZE;
   cudaFuncSetAttribute(eigh_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  eigh_tridiag<<<(nk + G - 1) / G, G * L, G * smT, stream>>>((const double2*)H, strideH, n, nk, L, G, Vh, tau, d, e);
+  eigh_tridiag<<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const double2*)H, strideH, n, nk, LT, G, Vh, tau, d,
+                                                               e);
   eigh_ql<<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
   const size_t zsz = (size_t)((n * n + 3 * n + 1) & ~1);
   const size_t usz = ((size_t)n * n * (fp64_vectors ? 16 : 8) + 15) / 16 * 2;
