@@ -55,6 +55,7 @@ class StageTimer:
 
 
 _TIMER = None
+_INDEX_CACHE = {}
 
 
 def set_timer(timer):
@@ -312,11 +313,15 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
         workspace = torch.empty(int(ws.value), dtype=torch.uint8, device=dev.device)
     if out is None:
         out = torch.empty((nb * nk, nF, nw, nw), dtype=cdt, device=dev.device)
-    ph = [torch.from_numpy(p).to(dev.device).to(cdt).contiguous() for p in dev.geom.phases(dKs, NKFFT)]
+    ph = []
+    for p in dev.geom.phases(dKs, NKFFT):  # page-locked staging so the upload does not stall the host
+        host = torch.from_numpy(p.astype(np.complex128 if fp64 else np.complex64)).pin_memory()
+        ph.append(host.to(dev.device, non_blocking=True))
+        ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
     st = _timed('r2k_fp64' if fp64 else 'r2k_fp32', lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
                 _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']), _ptr(gt['slice_r0']),
-                _ptr(ph[0]), _ptr(ph[1]), _ptr(ph[2]), nb, int(fp64), _ptr(workspace),
+                _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, int(fp64), _ptr(workspace),
                 ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
     _lib.check(st, "wbg_r2k")
     return out, index, nF, (ph, workspace)
@@ -346,8 +351,11 @@ def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
     cdt = torch.complex128 if fp64 else torch.complex64
     if out is None:
         out = torch.empty((nk, len(sel), nw, nw), dtype=cdt, device=dev)
-    s = torch.tensor(sel, dtype=torch.int32, device=dev)
-    h = torch.tensor(herm, dtype=torch.int32, device=dev)
+    key = (tuple(sel), tuple(herm), str(dev))
+    if key not in _INDEX_CACHE:
+        _INDEX_CACHE[key] = (torch.tensor(sel, dtype=torch.int32, device=dev),
+                             torch.tensor(herm, dtype=torch.int32, device=dev))
+    s, h = _INDEX_CACHE[key]
     st = _timed('rotate', lib.wbg_rotate, _ptr(U), nw * nw, _ptr(fields), nFin, _ptr(s), _ptr(h), len(sel), _ptr(out), nw, nk,
                         int(fp64), _stream())
     _lib.check(st, "wbg_rotate")
