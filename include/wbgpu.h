@@ -95,6 +95,21 @@ int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
 
+/* Allocation-free variant of wbg_eigh_batched (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- inside stream capture, under a host
+ * framework whose allocator owns the device memory, or in loops that forbid allocation --
+ * the workspace is a fixed file-scope device array of WBG_EIGH_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library keeps until process exit.  Same arguments and results as
+ * wbg_eigh_batched minus the workspace.  A batch needs
+ *   nk * (16*nw*nw + 32*nw) + 1024 <= WBG_EIGH_NOALLOC_SCRATCH_BYTES
+ * (nw = 32: nk <= 1920); larger batches return WBG_STATUS_TOO_LARGE without launching.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU race, so serialise them.  No allocation or free is performed. */
+#define WBG_EIGH_NOALLOC_SCRATCH_BYTES (32u << 20)
+int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
+                             long long strideU, int fp64_vectors, int* errflag, void* stream);
+
 /* ---- stage 3: U^dagger X U ----------------------------------------------------------------
  * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.
  * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U, Hermitian part if herm[f]. */

@@ -405,3 +405,55 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   }
   return wbg_cuda_status(cudaGetLastError());
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of wbg_eigh_batched.
+//
+// Some callers cannot call cudaMalloc at all: code running inside a CUDA-graph capture or
+// a stream-ordered region that must not synchronise, plugins living in a host process
+// whose allocator owns all device memory (a framework caching allocator, an embedding
+// application with a fixed memory budget), and real-time loops that forbid allocation
+// after start-up.  For them the eigensolver's workspace lives in a fixed file-scope device
+// array instead of a caller- or library-allocated buffer.  The array is part of the module:
+// every GPU that loads this library holds WBG_EIGH_NOALLOC_SCRATCH_BYTES of it until the
+// process exits.  All calls share it, so calls whose work overlaps on the GPU (different
+// streams, or different host threads on one device) race and must be serialised by the
+// caller.  Every workspace word is written by the kernels before it is read, so the
+// contents left by a previous call never need clearing.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_eigh_noalloc_scratch[WBG_EIGH_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device.  In host code the array's
+// name is only a host-side stand-in, so the address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) and cached.
+int noalloc_scratch(void** ptr) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return WBG_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_eigh_noalloc_scratch) != cudaSuccess || !p) return WBG_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return WBG_OK;
+}
+}  // namespace
+
+extern "C" int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
+                                        long long strideU, int fp64_vectors, int* errflag, void* stream) {
+  if (nw < 1 || nw > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
+  const size_t need = wbg_eigh_workspace_bytes(nw, nk);
+  if (need > (size_t)WBG_EIGH_NOALLOC_SCRATCH_BYTES) return WBG_ERR_SIZE;  // batch too large for the scratch
+  void* ws = nullptr;
+  const int st = noalloc_scratch(&ws);
+  if (st != WBG_OK) return st;
+  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, fp64_vectors, ws, need, errflag, (cudaStream_t)stream);
+}

@@ -11,7 +11,8 @@ import os
 from . import build as _build
 
 EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
-           'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_rotate', 'wbg_berry_omega',
+           'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate',
+           'wbg_berry_omega',
            'wbg_scan_finalize', 'wbg_probe_fma']
 
 STATUS_OK = 0
@@ -45,6 +46,7 @@ _SIGS = {
     'wbg_r2k': (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _SZ, _P, ctypes.POINTER(R2KGeom), _P]),
     'wbg_eigh_workspace_size': (_I, [_I, _I, ctypes.POINTER(_SZ)]),
     'wbg_eigh_batched': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _SZ, _P, _P]),
+    'wbg_eigh_batched_noalloc': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _P]),
     'wbg_rotate': (_I, [_P, _LL, _P, _I, _P, _P, _I, _P, _I, _I, _I, _P]),
     'wbg_berry_omega': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
