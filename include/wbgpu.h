@@ -87,13 +87,17 @@ int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, c
 
 /* ---- stage 2: batched Hermitian eigensolver ---------------------------------------------
  * H: matrix k at H + k*strideH (complex128 elements), symmetrised as 1/2 (H + H^dagger).
- * Tridiagonalisation, eigenvalues and inverse iteration run in FP64.
- * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n,
- * complex128 if fp64_vectors else complex64 (the back-transform then runs in FP32).
+ * mode 0: tridiagonalisation, eigenvalues and inverse iteration in FP64, back-transform in
+ *         FP32, U complex64;
+ * mode 1: everything in FP64, U complex128 (the plain FP64 path);
+ * mode 2: tridiagonalisation, eigenvalues and inverse iteration in double-float arithmetic
+ *         (pairs of FP32, 48-bit significand, on the FP32 pipe), back-transform in FP32,
+ *         U complex64 (the mixed-precision path).
+ * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
-                     int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
+                     int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
 
 /* Allocation-free variant of wbg_eigh_batched (no counterpart in the reference).
  * For callers that cannot allocate device memory -- inside stream capture, under a host
@@ -108,7 +112,7 @@ int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E
  * work overlaps on the GPU race, so serialise them.  No allocation or free is performed. */
 #define WBG_EIGH_NOALLOC_SCRATCH_BYTES (32u << 20)
 int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
-                             long long strideU, int fp64_vectors, int* errflag, void* stream);
+                             long long strideU, int mode, int* errflag, void* stream);
 
 /* ---- stage 3: U^dagger X U ----------------------------------------------------------------
  * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.

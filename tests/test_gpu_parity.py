@@ -59,8 +59,11 @@ def test_r2k_fields(c2small, fp64, tol, NKFFT):
             assert maxrel(got, ref) < tol, (name, ib, maxrel(got, ref))
 
 
+@pytest.mark.parametrize("mode", [1, 0, 2])
 @pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
-def test_eigh_random(nw):
+def test_eigh_random(nw, mode):
+    """mode 1: FP64; mode 0: FP64 solve + FP32 vectors; mode 2: double-float solve + FP32 vectors.
+    Energies to 1e-12 |E| nw in every mode; vectors to FP64 or FP32 accuracy."""
     rng = np.random.default_rng(nw)
     nk = 300
     H = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
@@ -73,18 +76,19 @@ def test_eigh_random(nw):
             w[1] = w[0] + 1e-9
         H[k] = (v * w) @ v.conj().T
     Ht = torch.from_numpy(H).cuda()
-    E, U, flag = engine.eigh(Ht, nw * nw, nw, nk)
+    E, U, flag = engine.eigh(Ht, nw * nw, nw, nk, mode=mode)
     torch.cuda.synchronize()
     assert int(flag.item()) == 0
-    E, U = E.cpu().numpy(), U.cpu().numpy()
+    E, U = E.cpu().numpy(), U.cpu().numpy().astype(np.complex128)
+    vtol = 1e-10 if mode == 1 else 1e-5
     Href = 0.5 * (H + H.conj().swapaxes(1, 2))
     Eref = np.linalg.eigvalsh(Href)
     scale = np.abs(Eref).max()
     assert np.max(np.abs(E - Eref)) < 1e-12 * max(scale, 1) * nw
     I = np.eye(nw)
-    assert np.max(np.abs(np.einsum('kmi,kmj->kij', U.conj(), U) - I)) < 1e-10
+    assert np.max(np.abs(np.einsum('kmi,kmj->kij', U.conj(), U) - I)) < vtol
     R = np.einsum('kmi,kmn,knj->kij', U.conj(), Href, U) - E[:, None, :] * I
-    assert np.max(np.abs(R)) < 1e-11 * max(scale, 1) * nw
+    assert np.max(np.abs(R)) < 0.1 * vtol * max(scale, 1) * nw
 
 
 def test_ahc_golden_random(golden_dir):

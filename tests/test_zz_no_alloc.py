@@ -44,7 +44,7 @@ def test_noalloc_matches_allocating_eigh(nw, fp64_vectors):
     assert nk * (16 * nw * nw + 32 * nw) + 1024 <= SCRATCH_BYTES
     for call in range(2):  # two calls in a row share (and overwrite) the scratch
         H = _hermitian_batch(100 * nw + call, nk, nw)
-        E_ref, U_ref, flag_ref = engine.eigh(H, nw * nw, nw, nk, fp64_vectors=fp64_vectors)
+        E_ref, U_ref, flag_ref = engine.eigh(H, nw * nw, nw, nk, mode=int(fp64_vectors))
         st, E, U, flag = _noalloc(lib, H, nw, nk, fp64_vectors)
         assert st == 0, lib.wbg_status_string(st).decode()
         torch.cuda.synchronize()

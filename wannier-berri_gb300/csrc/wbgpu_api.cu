@@ -51,8 +51,8 @@ int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes) {
 }
 
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
-                     int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, void* stream) {
-  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, fp64_vectors, workspace, workspace_bytes, errflag,
+                     int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream) {
+  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, mode, workspace, workspace_bytes, errflag,
                       (cudaStream_t)stream);
 }
 

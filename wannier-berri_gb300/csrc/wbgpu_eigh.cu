@@ -1,26 +1,39 @@
-// Batched Hermitian eigensolver in FP64 (stage 2 of the path): H(k) -> E_K (ascending), UU_K.
+// Batched Hermitian eigensolver (stage 2 of the path): H(k) -> E_K (ascending), UU_K.
 //
 // Replaces np.linalg.eigh in data_K/data_K.py:211-218 (E_K, UU_K) applied to
 // HH_K = 1/2 (H + H^dagger) (fourier/fft.py:183-186, data_K/data_K_R.py:24-26).
 //
 // GB300 runs FP64 at ~1.9 DFMA/clk/SM and a warp instruction costs the same whether
 // one lane or 32 lanes are active, so each phase is mapped so that every lane does
-// useful FP64 work:
+// useful work:
 //   1. eigh_tridiag : Householder reduction to real tridiagonal T = Q^dagger H Q,
-//                     one group of L lanes per matrix, lane owns rows (shared memory).
+//                     lower triangle only, mirrored row pairs per lane (shared memory).
 //   2. eigh_ql      : implicit QL (Wilkinson shift) eigenvalues of T, one thread per matrix.
 //   3. eigh_vectors : inverse iteration on T (partial-pivot LU), one lane per eigenvector,
 //                     modified Gram-Schmidt inside clusters, back-transform by the
 //                     Householder reflectors (U = Q Z).
+// The three kernels are templates over the real type R of the solve: native double, or
+// df64 (double-float on the FP32 pipe, 48-bit significand) for the mixed-precision path.
+// The back-transform runs in precision TU (double or float).
 #include <float.h>
 #include "wbgpu_common.cuh"
+#include "wbgpu_df64.cuh"
 #include "wbgpu_eigh.cuh"
 
 namespace {
 
-WBG_D double group_sum(double v, int L) {
-  for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+template <typename R>
+WBG_D R group_sum(R v, int L) {
+  for (int off = L / 2; off > 0; off >>= 1) v = v + shfl_xor(v, off);
   return v;
+}
+
+template <typename R>
+WBG_D typename C2<R>::t from_c64(double2 a) {
+  typename C2<R>::t r;
+  r.x = Arith<R>::from(a.x);
+  r.y = Arith<R>::from(a.y);
+  return r;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -29,83 +42,90 @@ WBG_D double group_sum(double v, int L) {
 // shared-memory bank conflicts).  Lane l of a group owns the mirrored row pairs
 // (2Lt + l, 2Lt + 2L-1-l), so the triangular rank-2 update is balanced across lanes;
 // L = max(4, pow2ceil(n)/2), i.e. two matrices share a warp for 16 < n <= 32.
-// Outputs: Vh[k][c][i] (v of reflector c, v_{c+1}=1, zeros for i<=c), tau[k][c],
-//          d[k][i], e[k][i] (e[n-1] = 0).
+// Outputs (real type R): Vh[k][c][i] (v of reflector c, v_{c+1}=1, zeros for i<=c),
+// tau[k][c], d[k][i], e[k][i] (e[n-1] = 0).
 // ---------------------------------------------------------------------------------------
 WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
 
+template <typename R>
 __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, int n, int nk, int L, int G,
-                             double2* __restrict__ Vh, double2* __restrict__ tauOut, double* __restrict__ dOut,
-                             double* __restrict__ eOut) {
-  extern __shared__ double2 sm[];
+                             typename C2<R>::t* __restrict__ Vh, typename C2<R>::t* __restrict__ tauOut,
+                             R* __restrict__ dOut, R* __restrict__ eOut) {
+  typedef typename C2<R>::t CR;
+  typedef Arith<R> A;
+  extern __shared__ unsigned char smt[];
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;  // redundant work keeps every lane of the warp in the same control flow
   const int ld = n + 1;
-  double2* A = sm + (size_t)grp * (n * ld + 2 * n);
-  double2* vs = A + n * ld;
-  double2* ws = vs + n;
+  CR* Am = reinterpret_cast<CR*>(smt) + (size_t)grp * (n * ld + 2 * n);
+  CR* vs = Am + n * ld;
+  CR* ws = vs + n;
   const double2* Hk = H + k * strideK;
   for (int idx = lane; idx < n * n; idx += L) {
     const int i = idx / n, j = idx % n;
     if (j <= i) {
       const double2 a = Hk[i * n + j], b = Hk[j * n + i];
-      A[i * ld + j] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+      Am[i * ld + j] = from_c64<R>(make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)));
     }
   }
   __syncwarp();
+  const R zero = A::from(0.0), one = A::from(1.0), mhalf = A::from(-0.5);
   const int T = (n + 2 * L - 1) / (2 * L);
   for (int c = 0; c < n - 1; ++c) {
-    double xn = 0.0;
+    R xn = zero;
     for (int t = 0; t < T; ++t)
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
-        if (i < n && i >= c + 2) { const double2 x = A[i * ld + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
+        if (i < n && i >= c + 2) { const CR x = Am[i * ld + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
       }
     xn = group_sum(xn, L);
-    const double2 alpha = A[(c + 1) * ld + c];
-    double beta, tr = 0.0, ti = 0.0;
-    double2 scale = make_double2(0.0, 0.0);
-    if (xn == 0.0 && alpha.y == 0.0) {
+    const CR alpha = Am[(c + 1) * ld + c];
+    R beta, tr = zero, ti = zero;
+    CR scale = czero<CR>();
+    if (xn == zero && alpha.y == zero) {
       beta = alpha.x;  // H = I
     } else {
-      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
-      beta = alpha.x >= 0.0 ? -nrm : nrm;
-      const double rb = 1.0 / beta;
+      const R nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
+      beta = alpha.x >= zero ? -nrm : nrm;
+      const R rb = one / beta;
       tr = (beta - alpha.x) * rb;
       ti = -alpha.y * rb;
       // scale = 1 / (alpha - beta)
-      const double ar = alpha.x - beta, ai = alpha.y;
-      const double rden = 1.0 / (ar * ar + ai * ai);
-      scale = make_double2(ar * rden, -ai * rden);
+      const R ar = alpha.x - beta, ai = alpha.y;
+      const R rden = one / (ar * ar + ai * ai);
+      scale.x = ar * rden;
+      scale.y = -ai * rden;
     }
-    const double2 tau = make_double2(tr, ti);
+    CR tau;
+    tau.x = tr;
+    tau.y = ti;
     // executed unconditionally (tau = 0 makes it a no-op) so that every lane of the warp
     // reaches the same __syncwarp / shuffle calls when several matrices share a warp
     for (int t = 0; t < T; ++t)
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n) {
-          if (i == c + 1) { vs[i] = make_double2(1.0, 0.0); A[i * ld + c] = vs[i]; }
-          else if (i >= c + 2) { const double2 v = cmul(A[i * ld + c], scale); vs[i] = v; A[i * ld + c] = v; }
+          if (i == c + 1) { CR v1; v1.x = one; v1.y = zero; vs[i] = v1; Am[i * ld + c] = v1; }
+          else if (i >= c + 2) { const CR v = cmul(Am[i * ld + c], scale); vs[i] = v; Am[i * ld + c] = v; }
         }
       }
     __syncwarp();
     // p = tau * A v over the full Hermitian row: lower part A[i][j], upper part conj(A[j][i])
-    double dr = 0.0, di = 0.0;
+    R dr = zero, di = zero;
     for (int t = 0; t < T; ++t)
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
-          double2 acc = make_double2(0.0, 0.0);
-          for (int j = c + 1; j <= i; ++j) cfma(acc, A[i * ld + j], vs[j]);
-          for (int j = i + 1; j < n; ++j) cfmac(acc, A[j * ld + i], vs[j]);
-          const double2 p = cmul(tau, acc);
+          CR acc = czero<CR>();
+          for (int j = c + 1; j <= i; ++j) cfma(acc, Am[i * ld + j], vs[j]);
+          for (int j = i + 1; j < n; ++j) cfmac(acc, Am[j * ld + i], vs[j]);
+          const CR p = cmul(tau, acc);
           ws[i] = p;
-          const double2 v = vs[i];
+          const CR v = vs[i];
           dr = fma(p.x, v.x, fma(p.y, v.y, dr));  // conj(p) v
           di = fma(p.x, v.y, fma(-p.y, v.x, di));
         }
@@ -113,7 +133,10 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
     dr = group_sum(dr, L);
     di = group_sum(di, L);
     // alpha2 = -1/2 tau (w^dagger v)
-    const double2 a2 = cscale(cmul(tau, make_double2(dr, di)), -0.5);
+    CR dd;
+    dd.x = dr;
+    dd.y = di;
+    const CR a2 = cscale(cmul(tau, dd), mhalf);
     for (int t = 0; t < T; ++t)
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
@@ -125,83 +148,91 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
-          const double2 vi = vs[i], wi = ws[i];
+          const CR vi = vs[i], wi = ws[i];
           for (int j = c + 1; j <= i; ++j) {
-            double2 a = A[i * ld + j];
-            const double2 vj = vs[j], wj = ws[j];
-            a.x -= vi.x * wj.x + vi.y * wj.y + wi.x * vj.x + wi.y * vj.y;
-            a.y -= vi.y * wj.x - vi.x * wj.y + wi.y * vj.x - wi.x * vj.y;
-            A[i * ld + j] = a;
+            CR a = Am[i * ld + j];
+            const CR vj = vs[j], wj = ws[j];
+            a.x = fma(-vi.x, wj.x, a.x);
+            a.x = fma(-vi.y, wj.y, a.x);
+            a.x = fma(-wi.x, vj.x, a.x);
+            a.x = fma(-wi.y, vj.y, a.x);
+            a.y = fma(-vi.y, wj.x, a.y);
+            a.y = fma(vi.x, wj.y, a.y);
+            a.y = fma(-wi.y, vj.x, a.y);
+            a.y = fma(wi.x, vj.y, a.y);
+            Am[i * ld + j] = a;
           }
         }
       }
     __syncwarp();
     if (valid) {
-      const bool refl = (tr != 0.0 || ti != 0.0);
-      for (int i = lane; i < n; i += L) Vh[(k * n + c) * n + i] = (refl && i >= c + 1) ? A[i * ld + c] : make_double2(0.0, 0.0);
+      const bool refl = (tr != zero || ti != zero);
+      for (int i = lane; i < n; i += L) Vh[(k * n + c) * n + i] = (refl && i >= c + 1) ? Am[i * ld + c] : czero<CR>();
       if (lane == 0) {
         tauOut[k * n + c] = tau;
         eOut[k * n + c] = beta;
-        dOut[k * n + c] = A[c * ld + c].x;
+        dOut[k * n + c] = Am[c * ld + c].x;
       }
     }
     __syncwarp();
   }
   if (valid && lane == 0) {
-    dOut[k * n + n - 1] = A[(n - 1) * ld + n - 1].x;
-    eOut[k * n + n - 1] = 0.0;
-    tauOut[k * n + n - 1] = make_double2(0.0, 0.0);
+    dOut[k * n + n - 1] = Am[(n - 1) * ld + n - 1].x;
+    eOut[k * n + n - 1] = zero;
+    tauOut[k * n + n - 1] = czero<CR>();
   }
   if (valid)
-    for (int i = lane; i < n; i += L) Vh[(k * n + n - 1) * n + i] = make_double2(0.0, 0.0);
+    for (int i = lane; i < n; i += L) Vh[(k * n + n - 1) * n + i] = czero<CR>();
 }
 
 // ---------------------------------------------------------------------------------------
 // 2. Implicit QL eigenvalues of the real symmetric tridiagonal (d, e), thread per matrix.
 // ---------------------------------------------------------------------------------------
-__global__ void eigh_ql(const double* __restrict__ dIn, const double* __restrict__ eIn, int n, int nk,
-                        double* __restrict__ Eout, int* __restrict__ errflag) {
+template <typename R>
+__global__ void eigh_ql(const R* __restrict__ dIn, const R* __restrict__ eIn, int n, int nk, double* __restrict__ Eout,
+                        int* __restrict__ errflag) {
+  typedef Arith<R> A;
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nk) return;
-  double d[WBG_EIGH_NMAX], e[WBG_EIGH_NMAX];
+  R d[WBG_EIGH_NMAX], e[WBG_EIGH_NMAX];
+  const R zero = A::from(0.0), one = A::from(1.0), two = A::from(2.0), eps = A::eps();
   for (int i = 0; i < n; ++i) { d[i] = dIn[k * n + i]; e[i] = eIn[k * n + i]; }
-  e[n - 1] = 0.0;
+  e[n - 1] = zero;
   bool ok = true;
   for (int l = 0; l < n; ++l) {
     int iter = 0, m;
     do {
       for (m = l; m < n - 1; ++m) {
-        const double dd = fabs(d[m]) + fabs(d[m + 1]);
-        if (fabs(e[m]) <= DBL_EPSILON * dd) break;
+        const R dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= eps * dd) break;
       }
       if (m != l) {
         if (iter++ >= 60) { ok = false; break; }
-        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-        double r = hypot(g, 1.0);
+        R g = (d[l + 1] - d[l]) / (two * e[l]);
+        R r = sqrt(fma(g, g, one));
         g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-        double s = 1.0, c = 1.0, p = 0.0;
-        int i;
+        R s = one, c = one, p = zero;
         bool underflow = false;
-        for (i = m - 1; i >= l; --i) {
-          double f = s * e[i];
-          const double b = c * e[i];
+        for (int i = m - 1; i >= l; --i) {
+          const R f = s * e[i];
+          const R b = c * e[i];
           // Givens rotation: one sqrt and one reciprocal (f, g are O(|T|): no overflow concern)
           r = sqrt(fma(f, f, g * g));
           e[i + 1] = r;
-          if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; underflow = true; break; }
-          const double rinv = 1.0 / r;
+          if (r == zero) { d[i + 1] = d[i + 1] - p; e[m] = zero; underflow = true; break; }
+          const R rinv = one / r;
           s = f * rinv;
           c = g * rinv;
           g = d[i + 1] - p;
-          r = (d[i] - g) * s + 2.0 * c * b;
+          r = (d[i] - g) * s + two * c * b;
           p = s * r;
           d[i + 1] = g + p;
           g = c * r - b;
         }
         if (underflow) continue;
-        d[l] -= p;
+        d[l] = d[l] - p;
         e[l] = g;
-        e[m] = 0.0;
+        e[m] = zero;
       }
     } while (m != l);
     if (!ok) break;
@@ -209,12 +240,12 @@ __global__ void eigh_ql(const double* __restrict__ dIn, const double* __restrict
   if (!ok) atomicOr(errflag, WBG_FLAG_QL_NOCONV);
   // ascending insertion sort
   for (int i = 1; i < n; ++i) {
-    const double x = d[i];
+    const R x = d[i];
     int j = i - 1;
     while (j >= 0 && d[j] > x) { d[j + 1] = d[j]; --j; }
     d[j + 1] = x;
   }
-  for (int i = 0; i < n; ++i) Eout[k * n + i] = d[i];
+  for (int i = 0; i < n; ++i) Eout[k * n + i] = A::to(d[i]);
 }
 
 WBG_D double hash_uniform(unsigned int a, unsigned int b) {
@@ -224,80 +255,81 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 }
 
 // ---------------------------------------------------------------------------------------
-// 3. Eigenvectors: inverse iteration on T (FP64), clusters re-orthogonalised, U = Q Z.
+// 3. Eigenvectors: inverse iteration on T (real type R), clusters re-orthogonalised, U = Q Z.
 // grid: ceil(nk/G) blocks of G*L threads; lane j computes eigenvectors j, j+L, ...
-// The back-transform by the Householder reflectors runs in precision TU (double, or float
-// when the caller consumes U in FP32).  Shared memory per group: U[n][n] complex(TU) with the
-// real inverse-iteration vectors Z(i,j) kept in a separate real(double) array.
+// The back-transform by the Householder reflectors runs in precision TU.  Shared memory
+// per group: Z [n][n], d, e, lam [n] (type R), then U[n][n] complex(TU).
 // ---------------------------------------------------------------------------------------
-template <typename TU>
-__global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __restrict__ tauIn,
-                             const double* __restrict__ dIn, const double* __restrict__ eIn,
-                             const double* __restrict__ E, int n, int nk, int L, int G,
-                             typename C2<TU>::t* __restrict__ Uout, long long strideU) {
+template <typename R, typename TU>
+__global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typename C2<R>::t* __restrict__ tauIn,
+                             const R* __restrict__ dIn, const R* __restrict__ eIn, const double* __restrict__ E, int n,
+                             int nk, int L, int G, typename C2<TU>::t* __restrict__ Uout, long long strideU) {
   typedef typename C2<TU>::t VU;
-  extern __shared__ double sme[];
+  typedef typename C2<R>::t CR;
+  typedef Arith<R> A;
+  extern __shared__ unsigned char smv[];
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;
-  // per-group layout (in doubles, 16-byte aligned pieces): Z [n*n], d, e, lam [n each], U
-  const int zsz = (n * n + 3 * n + 1) & ~1;
-  const int usz = (int)(((size_t)n * n * sizeof(VU) + 15) / 16 * 2);
-  double* Zs = sme + (size_t)grp * (zsz + usz);  // Z(i,j) = Zs[i*n + j]
-  double* ds = Zs + n * n;
-  double* es = ds + n;
-  double* lam = es + n;
-  VU* Us = reinterpret_cast<VU*>(Zs + zsz);      // [i][j]
-  for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = E[k * n + i]; }
+  const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
+  const size_t ubytes = ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
+  unsigned char* gbase = smv + (size_t)grp * (zbytes + ubytes);
+  R* Zs = reinterpret_cast<R*>(gbase);  // Z(i,j) = Zs[i*n + j]
+  R* ds = Zs + n * n;
+  R* es = ds + n;
+  R* lam = es + n;
+  VU* Us = reinterpret_cast<VU*>(gbase + zbytes);  // [i][j]
+  for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = A::from(E[k * n + i]); }
   __syncwarp();
-  double tnorm = 0.0;
-  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(ds[i]) + fabs(es[i]) + (i > 0 ? fabs(es[i - 1]) : 0.0));
-  tnorm = fmax(tnorm, DBL_MIN);
-  const double tiny = DBL_EPSILON * tnorm;
-  const double ortol = 1e-5 * tnorm;
-  const double pertol = 10.0 * DBL_EPSILON * tnorm;
-  double u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
+  const R zero = A::from(0.0), one = A::from(1.0);
+  R tnorm = zero;
+  for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(ds[i]) + fabs(es[i]) + (i > 0 ? fabs(es[i - 1]) : zero));
+  tnorm = fmax(tnorm, A::tiny_norm());
+  const R tiny = A::eps() * tnorm;
+  const R ortol = A::from(1e-5) * tnorm;
+  const R pertol = A::from(10.0) * A::eps() * tnorm;
+  R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
   unsigned char piv[WBG_EIGH_NMAX];
   for (int j = lane; j < n; j += L) {
-    double shift = lam[j];
-    for (int jj = j - 1; jj >= 0 && shift - lam[jj] < pertol; --jj) shift = lam[jj] + pertol * (j - jj);
+    R shift = lam[j];
+    for (int jj = j - 1; jj >= 0 && shift - lam[jj] < pertol; --jj) shift = lam[jj] + pertol * A::from((double)(j - jj));
     // LU with partial pivoting of T - shift I; u0i holds reciprocal pivots
-    double ca = ds[0] - shift, cb = n > 1 ? es[0] : 0.0;
+    R ca = ds[0] - shift, cb = n > 1 ? es[0] : zero;
     for (int i = 0; i < n - 1; ++i) {
-      const double ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : 0.0;
+      const R ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : zero;
       if (fabs(ca) >= fabs(ci)) {
-        if (fabs(ca) < tiny) ca = ca >= 0.0 ? tiny : -tiny;
-        const double rc = 1.0 / ca;
-        const double mlt = ci * rc;
-        u0i[i] = rc; u1[i] = cb; u2[i] = 0.0; lm[i] = mlt; piv[i] = 0;
+        if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
+        const R rc = one / ca;
+        const R mlt = ci * rc;
+        u0i[i] = rc; u1[i] = cb; u2[i] = zero; lm[i] = mlt; piv[i] = 0;
         ca = ai1 - mlt * cb;
         cb = bi1;
       } else {
-        const double rc = 1.0 / ci;
-        const double mlt = ca * rc;
+        const R rc = one / ci;
+        const R mlt = ca * rc;
         u0i[i] = rc; u1[i] = ai1; u2[i] = bi1; lm[i] = mlt; piv[i] = 1;
         ca = cb - mlt * ai1;
         cb = -mlt * bi1;
       }
     }
-    if (fabs(ca) < tiny) ca = ca >= 0.0 ? tiny : -tiny;
-    u0i[n - 1] = 1.0 / ca;
-    for (int i = 0; i < n; ++i) x[i] = hash_uniform((unsigned)j + 1u, (unsigned)i + 7u);
+    if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
+    u0i[n - 1] = one / ca;
+    for (int i = 0; i < n; ++i) x[i] = A::from(hash_uniform((unsigned)j + 1u, (unsigned)i + 7u));
     for (int it = 0; it < 3; ++it) {
-      double rp = x[0];
+      R rp = x[0];
       for (int i = 0; i < n - 1; ++i) {
-        const double y1 = x[i + 1];
+        const R y1 = x[i + 1];
         if (piv[i] == 0) { x[i] = rp; rp = y1 - lm[i] * rp; }
         else { x[i] = y1; rp = rp - lm[i] * y1; }
       }
       x[n - 1] = rp * u0i[n - 1];
       if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0i[n - 2];
       for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0i[i];
-      double nrm = 0.0;
+      R nrm = zero;
       for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
       nrm = rsqrt(nrm);
-      for (int i = 0; i < n; ++i) x[i] *= nrm;
+      for (int i = 0; i < n; ++i) x[i] = x[i] * nrm;
     }
     for (int i = 0; i < n; ++i) Zs[i * n + j] = x[i];
   }
@@ -313,14 +345,14 @@ __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __re
           bool same = true;
           for (int q = jp + 1; q <= j; ++q) same &= (lam[q] - lam[q - 1] < ortol);
           if (same) {
-            double dot = 0.0;
+            R dot = zero;
             for (int i = 0; i < n; ++i) dot = fma(Zs[i * n + jp], Zs[i * n + j], dot);
-            for (int i = 0; i < n; ++i) Zs[i * n + j] -= dot * Zs[i * n + jp];
+            for (int i = 0; i < n; ++i) Zs[i * n + j] = Zs[i * n + j] - dot * Zs[i * n + jp];
             if (j == jp + 1) {
-              double nrm = 0.0;
+              R nrm = zero;
               for (int i = 0; i < n; ++i) nrm = fma(Zs[i * n + j], Zs[i * n + j], nrm);
               nrm = rsqrt(nrm);
-              for (int i = 0; i < n; ++i) Zs[i * n + j] *= nrm;
+              for (int i = 0; i < n; ++i) Zs[i * n + j] = Zs[i * n + j] * nrm;
             }
           }
         }
@@ -330,21 +362,21 @@ __global__ void eigh_vectors(const double2* __restrict__ Vh, const double2* __re
   }
   // back-transform: u = H_0 H_1 ... H_{n-2} z  (precision TU)
   for (int j = lane; j < n; j += L) {
-    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>((TU)Zs[i * n + j], (TU)0);
+    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>((TU)A::to(Zs[i * n + j]), (TU)0);
     for (int c = n - 2; c >= 0; --c) {
-      const double2 tau64 = tauIn[k * n + c];
-      if (tau64.x == 0.0 && tau64.y == 0.0) continue;
-      const VU tau = mkc<TU>((TU)tau64.x, (TU)tau64.y);
-      const double2* v = Vh + (k * n + c) * n;
+      const CR tauR = tauIn[k * n + c];
+      if (tauR.x == zero && tauR.y == zero) continue;
+      const VU tau = mkc<TU>((TU)A::to(tauR.x), (TU)A::to(tauR.y));
+      const CR* v = Vh + (k * n + c) * n;
       VU sacc = czero<VU>();
       for (int i = c + 1; i < n; ++i) {
-        const VU vv = mkc<TU>((TU)v[i].x, (TU)v[i].y);
+        const VU vv = mkc<TU>((TU)A::to(v[i].x), (TU)A::to(v[i].y));
         cfmac(sacc, vv, Us[i * n + j]);
       }
       const VU ts = cmul(tau, sacc);
       for (int i = c + 1; i < n; ++i) {
         VU u = Us[i * n + j];
-        const VU vv = mkc<TU>((TU)v[i].x, (TU)v[i].y);
+        const VU vv = mkc<TU>((TU)A::to(v[i].x), (TU)A::to(v[i].y));
         u.x -= vv.x * ts.x - vv.y * ts.y;
         u.y -= vv.x * ts.y + vv.y * ts.x;
         Us[i * n + j] = u;
@@ -362,48 +394,53 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
-}  // namespace
-
-size_t wbg_eigh_workspace_bytes(int n, int nk) {
-  // Vh (n*n complex) + tau (n complex) + d, e (n real each) per matrix
-  return (size_t)nk * ((size_t)n * n * 16 + (size_t)n * 16 + 2 * (size_t)n * 8) + 1024;
-}
-
-int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU,
-                 int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
-  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
-  if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
+template <typename R, typename TU>
+int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, void* workspace,
+                int* errflag, cudaStream_t stream) {
+  typedef typename C2<R>::t CR;
+  typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
-  double2* Vh = (double2*)w; w += (size_t)nk * n * n * 16;
-  double2* tau = (double2*)w; w += (size_t)nk * n * 16;
-  double* d = (double*)w; w += (size_t)nk * n * 8;
-  double* e = (double*)w;
+  CR* Vh = (CR*)w; w += (size_t)nk * n * n * 16;
+  CR* tau = (CR*)w; w += (size_t)nk * n * 16;
+  R* d = (R*)w; w += (size_t)nk * n * 8;
+  R* e = (R*)w;
   const int L = lanes_for(n);
   const int LT = L >= 8 ? L / 2 : 4;  // tridiagonalisation: mirrored row pairs, half the lanes
-  const size_t smT = ((size_t)n * (n + 1) + 2 * n) * sizeof(double2);
+  const size_t smT = ((size_t)n * (n + 1) + 2 * n) * sizeof(CR);
   int G = (4 * 32) / LT;
   while (G > 1 && G * smT > 96 * 1024) G /= 2;
   if (G * smT > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  eigh_tridiag<<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const double2*)H, strideH, n, nk, LT, G, Vh, tau, d,
-                                                               e);
-  eigh_ql<<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
-  const size_t zsz = (size_t)((n * n + 3 * n + 1) & ~1);
-  const size_t usz = ((size_t)n * n * (fp64_vectors ? 16 : 8) + 15) / 16 * 2;
-  const size_t smV = (zsz + usz) * sizeof(double);
+  cudaFuncSetAttribute(eigh_tridiag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  eigh_tridiag<R><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const double2*)H, strideH, n, nk, LT, G, Vh, tau, d,
+                                                                  e);
+  eigh_ql<R><<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
+  const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
+  const size_t ubytes = ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
+  const size_t smV = zbytes + ubytes;
   int GV = (2 * 32) / L;
   while (GV > 1 && GV * smV > 96 * 1024) GV /= 2;
   if (GV * smV > 220 * 1024) return WBG_ERR_SIZE;
-  if (fp64_vectors) {
-    cudaFuncSetAttribute(eigh_vectors<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    eigh_vectors<double><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L,
-                                                                           GV, (double2*)U, strideU);
-  } else {
-    cudaFuncSetAttribute(eigh_vectors<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    eigh_vectors<float><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L,
-                                                                          GV, (float2*)U, strideU);
-  }
+  cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  eigh_vectors<R, TU><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
+                                                                        (VU*)U, strideU);
   return wbg_cuda_status(cudaGetLastError());
+}
+
+}  // namespace
+
+size_t wbg_eigh_workspace_bytes(int n, int nk) {
+  // Vh (n*n complex) + tau (n complex) + d, e (n real each) per matrix; 8-byte reals in both modes
+  return (size_t)nk * ((size_t)n * n * 16 + (size_t)n * 16 + 2 * (size_t)n * 8) + 1024;
+}
+
+int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int mode,
+                 void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
+  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
+  if (mode < 0 || mode > 2) return WBG_ERR_ARG;
+  if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
+  if (mode == 1) return launch_eigh<double, double>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  if (mode == 0) return launch_eigh<double, float>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  return launch_eigh<df64, float>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -448,12 +485,12 @@ int noalloc_scratch(void** ptr) {
 }  // namespace
 
 extern "C" int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
-                                        long long strideU, int fp64_vectors, int* errflag, void* stream) {
+                                        long long strideU, int mode, int* errflag, void* stream) {
   if (nw < 1 || nw > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
   const size_t need = wbg_eigh_workspace_bytes(nw, nk);
   if (need > (size_t)WBG_EIGH_NOALLOC_SCRATCH_BYTES) return WBG_ERR_SIZE;  // batch too large for the scratch
   void* ws = nullptr;
   const int st = noalloc_scratch(&ws);
   if (st != WBG_OK) return st;
-  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, fp64_vectors, ws, need, errflag, (cudaStream_t)stream);
+  return wbg_eigh_run(H, strideH, nw, nk, E, U, strideU, mode, ws, need, errflag, (cudaStream_t)stream);
 }

@@ -8,4 +8,4 @@
 
 size_t wbg_eigh_workspace_bytes(int n, int nk);
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU,
-                 int fp64_vectors, void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream);
+                 int mode, void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream);

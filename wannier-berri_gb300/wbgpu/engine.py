@@ -327,8 +327,10 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
     return out, index, nF, (ph, workspace)
 
 
-def eigh(Hfields, strideH, nw, nk, E=None, U=None, fp64_vectors=True):
-    """Batched eigensolver; U is complex128 (fp64_vectors) or complex64."""
+def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1):
+    """Batched eigensolver (wbg_eigh_batched).  mode 1: FP64 throughout, U complex128;
+    mode 0: FP64 solve, FP32 back-transform; mode 2: double-float solve, FP32 back-transform
+    (U complex64 in modes 0 and 2)."""
     lib = _lib.load()
     dev = Hfields.device
     ws = ctypes.c_size_t(0)
@@ -337,10 +339,10 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None, fp64_vectors=True):
     if E is None:
         E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
     if U is None:
-        U = torch.empty((nk, nw, nw), dtype=torch.complex128 if fp64_vectors else torch.complex64, device=dev)
+        U = torch.empty((nk, nw, nw), dtype=torch.complex128 if mode == 1 else torch.complex64, device=dev)
     flag = torch.zeros(1, dtype=torch.int32, device=dev)
     st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw,
-                int(fp64_vectors), _ptr(work), ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
+                int(mode), _ptr(work), ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
     _lib.check(st, "wbg_eigh_batched")
     return E, U, flag
 
@@ -379,7 +381,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
     elif precision == 'mixed':
         Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, True)
         keep.append(k0)
-        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, fp64_vectors=False)
+        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, mode=2)
         del Hf
         fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, False, False)
         keep.append(k1)
