@@ -206,9 +206,14 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
     """Algorithmic work per launch of the given stage (per k-point figures as defined in the design doc)."""
     n = NW
     per_launch_ms = ms_total / max(n_calls, 1)
-    if stage == 'eigh':
+    if stage == 'eigh' and precision == 'fp64':
         work = 20.0 * n ** 3 * k_per_call          # FP64 flops, convention 20 nw^3 per matrix
         bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
+    elif stage == 'eigh':
+        # double-float solve on the FP32 pipe: 20 nw^3 FP64-equivalent flops per matrix, each
+        # costing 8.5 FP32 flops (a double-float FMA = 3 FMA + 1 MUL + 10 ADD = 17 FP32 flops)
+        work = 20.0 * n ** 3 * 8.5 * k_per_call
+        bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
     elif stage == 'rotate':
         work = 16.0 * n ** 3 * 9 * k_per_call      # two complex GEMMs per field, 9 fields
         if precision == 'fp64':

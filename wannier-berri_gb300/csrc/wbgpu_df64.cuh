@@ -124,12 +124,16 @@ template <> struct Arith<double> {
   static __device__ __forceinline__ double to(double x) { return x; }
   static __device__ __forceinline__ double eps() { return 2.220446049250313e-16; }
   static __device__ __forceinline__ double tiny_norm() { return 2.2250738585072014e-308; }
+  // relative floor for inverse-iteration pivots: growth per tiny pivot stays within range
+  static __device__ __forceinline__ double pivot_floor() { return 2.220446049250313e-16; }
 };
 template <> struct Arith<df64> {
   static __device__ __forceinline__ df64 from(double x) { return df_from(x); }
   static __device__ __forceinline__ double to(df64 x) { return df_to_double(x); }
   static __device__ __forceinline__ df64 eps() { return df_from(7.105427357601002e-15); }  // 2^-47
   static __device__ __forceinline__ df64 tiny_norm() { return df_from(1e-30); }
+  // FP32 exponent range: a floor of 1e-12 keeps three consecutive tiny pivots below 1e36
+  static __device__ __forceinline__ df64 pivot_floor() { return df_from(1e-12); }
 };
 
 // complex df64 (same 16-byte footprint as double2)

@@ -286,7 +286,7 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
   R tnorm = zero;
   for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(ds[i]) + fabs(es[i]) + (i > 0 ? fabs(es[i - 1]) : zero));
   tnorm = fmax(tnorm, A::tiny_norm());
-  const R tiny = A::eps() * tnorm;
+  const R tiny = A::pivot_floor() * tnorm;
   const R ortol = A::from(1e-5) * tnorm;
   const R pertol = A::from(10.0) * A::eps() * tnorm;
   R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
@@ -326,8 +326,12 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
       x[n - 1] = rp * u0i[n - 1];
       if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0i[n - 2];
       for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0i[i];
+      // scale by the largest component before the 2-norm so squares cannot overflow
+      R amax = zero;
+      for (int i = 0; i < n; ++i) amax = fmax(amax, fabs(x[i]));
+      const R ra = one / amax;
       R nrm = zero;
-      for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
+      for (int i = 0; i < n; ++i) { x[i] = x[i] * ra; nrm = fma(x[i], x[i], nrm); }
       nrm = rsqrt(nrm);
       for (int i = 0; i < n; ++i) x[i] = x[i] * nrm;
     }
