@@ -127,6 +127,41 @@ int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA
                     const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
                     void* stream);
 
+/* Orbital moment, Morb_Hpm = Morb_H + E_av Omega (formula/covariant.py:375-449), the non-additive
+ * formula of the Morb calculator (calculators/static.py:231-247): group values are differences
+ * of traces over [0, n) at the group borders (calculators/static.py:109-117).  Xbar holds
+ * V at iV, A (Hermitian part) at iA, rotA at iO, B at iB, C at iC (3 fields each).
+ * hist [scan.nEF][3] is accumulated.  The Morb calculator combines it with a wbg_berry_omega
+ * histogram: M(E_F) = [cumsum(hist_Hpm) - 2 E_F cumsum(hist_Omega)] * factor / nk. */
+int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
+                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                   void* stream);
+
+/* Berry-curvature dipole, DerOmega (formula/covariant.py:212-259) with DerDcov
+ * (formula/elementary.py:55-70) and the generalised derivatives of A and rotA
+ * (formula/formula.py:95-118); BerryDipole_FermiSea (calculators/static.py:472-487).
+ * Xbar: V at iV (3), A at iA (3), rotA at iO (3), d_a d_b H at iW (9, [a][b]),
+ * d_d A_b at idA (9, [b][d]), d_d rotA_c at idO (9, [c][d]).
+ * hist [scan.nEF][3][3] ([c][d], before the calculator's swap of the last two axes). */
+int wbg_berry_deromega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
+                       int idO, int nw, int nk, const wbg_scan* scan, int internal_terms, int external_terms,
+                       double* hist, int fp64, void* stream);
+
+/* Kubo optical conductivity (calculators/dynamic.py:71-114,170-196).
+ * Groups over all bands (degen_thresh); for every ordered pair of groups not pruned by
+ * `nonzero`, f_w(E1,E2) f_E(E1,E2) M^{ab} is added to out[iEF][iw][a][b] (complex128,
+ * accumulated, not normalised: the calculator multiplies by factor_opt / (nk * V)).
+ * efermi [nEF] and omega [nOmega] are device arrays; gaussian != 0 selects the Gaussian
+ * smearing of the imaginary part, else Lorentzian.  Xbar: V at iV, A at iA (3 fields each). */
+typedef struct {
+  double EFmin, EFmax, kBT, eta, degen_thresh;
+  int nEF, nOmega, gaussian, reserved;
+} wbg_kubo_params;
+int wbg_kubo_workspace_size(int nw, int nk, int nEF, size_t* bytes);
+int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
+             const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
+             size_t workspace_bytes, double* out, int fp64, void* stream);
+
 /* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);
 

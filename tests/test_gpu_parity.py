@@ -130,3 +130,63 @@ def test_ahc_internal_only(c2small):
     res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=1, NKFFT=4), {'ahc': wbgpu.calculators.AHC(Efermi=EF, **kw)})
     ref = O.run(o, (1, 1, 1), (4, 4, 4), {'ahc': O.AHC(Efermi=EF, **kw)})
     assert maxrel(res['ahc'].data, ref['ahc'].data) < 1e-9
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_morb_c2small(c2small, precision, tol):
+    s, o = c2small
+    EF = np.linspace(-2, 2, 101)
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(3, 4, 3)), {'morb': wbgpu.calculators.Morb(Efermi=EF)},
+                    precision=precision)
+    ref = O.run(o, (2, 2, 2), (3, 4, 3), {'morb': O.Morb(Efermi=EF)})
+    assert maxrel(res['morb'].data, ref['morb'].data) < tol
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_bcd_c2small(c2small, precision, tol):
+    s, o = c2small
+    EF = np.linspace(-2, 2, 101)
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(3, 4, 3)),
+                    {'bcd': wbgpu.calculators.BerryDipole_FermiSea(Efermi=EF)}, precision=precision)
+    ref = O.run(o, (2, 2, 2), (3, 4, 3), {'bcd': O.BerryDipole_FermiSea(Efermi=EF)})
+    assert res['bcd'].data.shape == ref['bcd'].data.shape
+    assert maxrel(res['bcd'].data, ref['bcd'].data) < tol
+
+
+def test_bcd_internal_only(c2small):
+    s, o = c2small
+    EF = np.linspace(-2, 2, 41)
+    kw = dict(kwargs_formula={'external_terms': False})
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=1, NKFFT=4), {'bcd': wbgpu.calculators.BerryDipole_FermiSea(Efermi=EF, **kw)})
+    ref = O.run(o, (1, 1, 1), (4, 4, 4), {'bcd': O.BerryDipole_FermiSea(Efermi=EF, **kw)})
+    assert maxrel(res['bcd'].data, ref['bcd'].data) < 1e-9
+
+
+@pytest.mark.parametrize("smr,kBT", [('Lorentzian', 0.0), ('Gaussian', 0.0), ('Lorentzian', 0.05)])
+def test_optcond_c3small(smr, kBT):
+    d = models.config_system(3, small=True)
+    s = wsys.System_R.from_dict(d)
+    EF = np.linspace(-1, 1, 11)
+    om = np.linspace(0, 4, 40)
+    kw = dict(Efermi=EF, omega=om, smr_fixed_width=0.05, smr_type=smr, kBT=kBT)
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=4), {'opt': wbgpu.calculators.OpticalConductivity(**kw)})
+    ref = O.run(osys(d), (2, 2, 2), (4, 4, 4), {'opt': O.OpticalConductivity(**kw)})
+    # FP32 band sums with FP64 denominators: 1e-5 relative
+    assert maxrel(res['opt'].data, ref['opt'].data) < 1e-5
+
+
+def test_golden_random_morb_and_opt(golden_dir):
+    """The reference's golden random-Morb and random-opt_conductivity (tests/test_run.py:653-669)."""
+    import os
+    f = np.load(os.path.join(golden_dir, 'random_system.npz'))
+    XX = {k[5:]: f[k] for k in f.files if k.startswith('XX_R_')}
+    s = wsys.System_R.from_arrays(f['real_lattice'], f['iRvec'], f['wannier_centers_cart'], XX)
+    ref = np.load(os.path.join(golden_dir, 'random_results.npz'))
+    calcs = {'Morb': wbgpu.calculators.Morb(Efermi=np.linspace(-2, 2, 5)),
+             'opt': wbgpu.calculators.OpticalConductivity(Efermi=np.array([17.0, 18.0]), omega=np.arange(0.0, 7.1, 1.0),
+                                                         smr_fixed_width=0.20, smr_type="Gaussian")}
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=3), calcs)
+    m = ref['Morb_data']
+    assert np.max(np.abs(res['Morb'].data - m)) < 1e-8 * np.max(np.abs(m))
+    oc = ref['opt_conductivity_data']
+    assert np.max(np.abs(res['opt'].data - oc)) < 1e-5 * np.max(np.abs(oc))

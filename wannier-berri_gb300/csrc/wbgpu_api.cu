@@ -4,6 +4,7 @@
 #include "wbgpu_r2k.cuh"
 #include "wbgpu_eigh.cuh"
 #include "wbgpu_band.cuh"
+#include "wbgpu_kubo.cuh"
 
 extern "C" {
 
@@ -66,6 +67,33 @@ int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA
                     void* stream) {
   return wbg_berry_omega_run(E, Xbar, nFbar, iV, iA, iO, nw, nk, scan, internal_terms, external_terms, hist, fp64,
                              (cudaStream_t)stream);
+}
+
+int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
+                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                   void* stream) {
+  return wbg_berry_morb_run(E, Xbar, nFbar, iV, iA, iO, iB, iC, nw, nk, scan, internal_terms, external_terms, hist, fp64,
+                            (cudaStream_t)stream);
+}
+
+int wbg_berry_deromega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
+                       int idO, int nw, int nk, const wbg_scan* scan, int internal_terms, int external_terms,
+                       double* hist, int fp64, void* stream) {
+  return wbg_berry_deromega_run(E, Xbar, nFbar, iV, iA, iO, iW, idA, idO, nw, nk, scan, internal_terms, external_terms,
+                                hist, fp64, (cudaStream_t)stream);
+}
+
+int wbg_kubo_workspace_size(int nw, int nk, int nEF, size_t* bytes) {
+  if (!bytes || nw < 1 || nk < 1 || nEF < 1) return WBG_STATUS_BAD_ARGUMENT;
+  *bytes = wbg_kubo_workspace_bytes(nw, nk, nEF);
+  return WBG_STATUS_OK;
+}
+
+int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
+             const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
+             size_t workspace_bytes, double* out, int fp64, void* stream) {
+  return wbg_kubo_run(E, Xbar, nFbar, iV, iA, nw, nk, external_terms, params, efermi, omega, workspace,
+                      workspace_bytes, out, fp64, (cudaStream_t)stream);
 }
 
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream) {

@@ -160,6 +160,10 @@ WBG_D int group_sum_i(int v, int L) {
   for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
 }
+WBG_D double group_sum_d(double v, int L) {
+  for (int off = L / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
 WBG_D int group_min_i(int v, int L) {
   for (int off = L / 2; off > 0; off >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, off));
   return v;
@@ -299,6 +303,418 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
     if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
 }
 
+// ---------------------------------------------------------------------------------------
+// Orbital moment, Morb_Hpm (formula/covariant.py:375-449): non-additive, so the trace over
+// inn = [0, n), out = [n, nw) is needed at every group border n (calculators/static.py:109-117).
+// The trace splits into pair functions of bands (m in inn, l in out / n' in inn):
+//   T(n) = sum_{m<n} [ sum_{l>=n} F(m,l) + sum_{n'<n} G(m,n') + H(m) ]
+//        = sum_{m<n} [ sum_{l>=n} (F - G)(m,l) + Gtot(m) + H(m) ]
+// with (component g, (a,b) = ((1,2),(2,0),(0,1))[g], D_ml = -V_ml/(E_m - E_l)):
+//   F = 2Re[-i D^a_ml E_l D^b_lm - D^a_ml B^b_lm + D^b_ml B^a_lm]                  (Morb_H)
+//     + E_m 2Re[-i D^a_ml D^b_lm - D^a_ml A^b_lm + D^b_ml A^a_lm]                   (E_m Omega)
+//   G = (E_n' + E_m) 2Re[-i A^a_mn' A^b_n'm],   H = Re C^g_mm + E_m Re O^g_mm.
+// Lane m walks n downwards keeping the running suffix sum; one warp reduction per n gives T(n).
+// Group values T(ge) - T(gs) are binned like the Omega kernel.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void berry_morb_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
+                                  int iV, int iA, int iO, int iB, int iC, int nw, int nk, int L, int G, WbgScan sp,
+                                  int internal_terms, int external_terms, double* __restrict__ hist) {
+  typedef typename C2<T>::t V;
+  extern __shared__ double smb[];
+  double* sh = smb;                                      // [nEF][3]
+  double* Es = sh + 3 * sp.nEF;                          // [G][nw]
+  double* Tn = Es + G * nw;                              // [G][nw+1][3]
+  int* start = reinterpret_cast<int*>(Tn + 3 * G * (nw + 1));  // [G][nw]
+  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  double* myE = Es + grp * nw;
+  double* myT = Tn + 3 * grp * (nw + 1);
+  int* myS = start + grp * nw;
+  const long long nw2 = (long long)nw * nw;
+  for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
+    const long long k = base + grp;
+    const bool valid = k < nk;
+    const long long kk = valid ? k : nk - 1;
+    for (int i = lane; i < nw; i += L) myE[i] = E[kk * nw + i];
+    __syncwarp();
+    for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
+    __syncwarp();
+    int below = 0, f0 = nw;
+    for (int n = lane; n < nw; n += L) {
+      below += myE[n] < sp.EFmin;
+      if (myS[n]) {
+        int g1 = n + 1;
+        while (g1 < nw && !myS[g1]) ++g1;
+        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+      }
+    }
+    below = group_sum_i(below, L);
+    f0 = group_min_i(f0, L);
+    const int bandmax = min(below, f0);
+    const V* Xk = Xbar + kk * nFbar * nw2;
+    // per band: Gtot + H (constant part) and running suffix of F - G
+    const int nb_lane = (nw + L - 1) / L;  // bands per lane (<= WBG_BAND_MAXPER)
+    double cst[WBG_BAND_MAXPER][3], run[WBG_BAND_MAXPER][3];
+    for (int q = 0; q < nb_lane; ++q) {
+      const int m = lane + q * L;
+      for (int g = 0; g < 3; ++g) { cst[q][g] = 0.0; run[q][g] = 0.0; }
+      if (m >= nw || !external_terms) continue;
+      const double Em = myE[m];
+      for (int np = 0; np < nw; ++np) {
+        const double w = myE[np] + Em;
+#pragma unroll
+        for (int g = 0; g < 3; ++g) {
+          const int al = (g + 1) % 3, be = (g + 2) % 3;
+          V acc = cmul(Xk[(iA + al) * nw2 + m * nw + np], Xk[(iA + be) * nw2 + np * nw + m]);
+          cst[q][g] += w * 2.0 * (double)acc.y;  // 2 Re(-i acc) = 2 Im(acc)
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < 3; ++g)
+        cst[q][g] += (double)Xk[(iC + g) * nw2 + m * nw + m].x + Em * (double)Xk[(iO + g) * nw2 + m * nw + m].x;
+    }
+    for (int n = nw; n >= 1; --n) {
+      double part[3] = {0.0, 0.0, 0.0};
+      for (int q = 0; q < nb_lane; ++q) {
+        const int m = lane + q * L;
+        if (m >= n) continue;
+        if (n < nw) {
+          const int l = n;  // add (F - G)(m, l=n) to the running suffix sum
+          const double Em = myE[m], El = myE[l];
+          const double dE = Em - El;
+          const T dinv = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+          V Dml[3], Dlm[3], Blm[3], Alm[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            Dml[a] = cscale(Xk[(iV + a) * nw2 + m * nw + l], -dinv);
+            Dlm[a] = cscale(Xk[(iV + a) * nw2 + l * nw + m], dinv);
+            Blm[a] = external_terms ? Xk[(iB + a) * nw2 + l * nw + m] : czero<V>();
+            Alm[a] = external_terms ? Xk[(iA + a) * nw2 + l * nw + m] : czero<V>();
+          }
+#pragma unroll
+          for (int g = 0; g < 3; ++g) {
+            const int al = (g + 1) % 3, be = (g + 2) % 3;
+            double f = 0.0;
+            if (internal_terms) {
+              const V dd = cmul(Dml[al], Dlm[be]);  // 2Re(-i x) = 2 Im(x)
+              f += 2.0 * (El + Em) * (double)dd.y;
+            }
+            if (external_terms) {
+              V xb = csub(cmul(Dml[be], Blm[al]), cmul(Dml[al], Blm[be]));
+              V xa = csub(cmul(Dml[be], Alm[al]), cmul(Dml[al], Alm[be]));
+              f += 2.0 * ((double)xb.x + Em * (double)xa.x);
+              const V aa = cmul(Xk[(iA + al) * nw2 + m * nw + l], Xk[(iA + be) * nw2 + l * nw + m]);
+              f -= (El + Em) * 2.0 * (double)aa.y;  // minus G(m, l)
+            }
+            run[q][g] += f;
+          }
+        }
+#pragma unroll
+        for (int g = 0; g < 3; ++g) part[g] += run[q][g] + cst[q][g];
+      }
+      for (int g = 0; g < 3; ++g) {
+        const double t = group_sum_d(part[g], L);
+        if (lane == 0) myT[n * 3 + g] = t;
+      }
+    }
+    if (lane == 0)
+      for (int g = 0; g < 3; ++g) myT[g] = 0.0;  // T(0): empty inner set
+    __syncwarp();
+    if (valid) {
+      for (int n = lane; n < nw; n += L) {
+        int gs = -1, ge = -1;
+        bool sea = false;
+        if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; sea = true; }
+        else if (n >= bandmax && myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
+        }
+        if (gs < 0) continue;
+        double esum = 0.0;
+        for (int q = gs; q < ge; ++q) esum += myE[q];
+        int bin = -1;
+        if (sea) bin = 0;
+        else {
+          const double Em = esum / (double)(ge - gs);
+          if (Em < sp.EFmin) bin = 0;
+          else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
+        }
+        if (bin >= 0 && bin < sp.nEF)
+          for (int g = 0; g < 3; ++g) atomicAdd(&sh[bin * 3 + g], myT[ge * 3 + g] - myT[gs * 3 + g]);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
+    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Berry-curvature dipole, DerOmega (formula/covariant.py:212-259), additive, 3x3 per group.
+// For band m of group G (inn = G, out = the rest), with D_xy = -V_xy/(E_x - E_y):
+//   dD_lm^{bd} = -[W^{bd}_lm + sum_{p notin G}(V^b_lp D^d_pm + V^d_lp D^b_pm)
+//                            - sum_{q in G}(D^b_lq V^d_qm + D^d_lq V^b_qm)] / (E_l - E_m)
+//   dD_ml^{ad} = -[W^{ad}_ml + sum_{p in G}(V^a_mp D^d_pl + V^d_mp D^a_pl)
+//                            - sum_{q notin G}(D^a_mq V^d_ql + D^d_mq V^a_ql)] / (E_m - E_l)
+//   dA_lm^{bd} = dAc^{bd}_lm - sum_{q in G} D^d_lq A^b_qm + sum_{p notin G} A^b_lp D^d_pm
+//   dA_n'm^{bd} = dAc^{bd}_n'm - sum_{l notin G} D^d_n'l A^b_lm + sum_{l notin G} A^b_n'l D^d_lm
+//   dO_mm^{cd} = dOc^{cd}_mm - sum_{l notin G} D^d_ml O^c_lm + sum_{l notin G} O^c_ml D^d_lm
+// (elementary.py:55-70 DerDcov, formula.py:95-118 Matrix_GenDer_ln) and
+//   S^{cd} = 1/2 dO^{cd}_mm + sum_{(s,a,b)} [ -i s sum_l D^a_ml dD^{bd}_lm
+//            - s sum_l D^a_ml dA^{bd}_lm - s sum_l dD^{ad}_ml A^b_lm - i s sum_n' A^a_mn' dA^{bd}_n'm ]
+// over (s,a,b) in {(+1, alpha_c, beta_c), (-1, beta_c, alpha_c)}; the group value is
+// sum_{m in G} 2 Re S^{cd}.  hist is [nEF][3][3] (c, d) -- the calculator swaps c and d.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void berry_deromega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar,
+                                      int nFbar, int iV, int iA, int iO, int iW, int idA, int idO, int nw, int nk,
+                                      int L, int G, WbgScan sp, int internal_terms, int external_terms,
+                                      double* __restrict__ hist) {
+  typedef typename C2<T>::t V;
+  extern __shared__ double smb[];
+  double* sh = smb;                                   // [nEF][9]
+  double* Es = sh + 9 * sp.nEF;                       // [G][nw]
+  double* tv = Es + G * nw;                           // [G][nw][9]
+  T* dinvS = reinterpret_cast<T*>(tv + 9 * G * nw);   // [G][nw][nw]
+  int* start = reinterpret_cast<int*>(dinvS + (size_t)G * nw * nw);  // [G][nw]
+  for (int i = threadIdx.x; i < 9 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  double* myE = Es + grp * nw;
+  double* myT = tv + 9 * grp * nw;
+  T* myDinv = dinvS + (size_t)grp * nw * nw;
+  int* myS = start + grp * nw;
+  const long long nw2 = (long long)nw * nw;
+  for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
+    const long long k = base + grp;
+    const bool valid = k < nk;
+    const long long kk = valid ? k : nk - 1;
+    for (int i = lane; i < nw; i += L) myE[i] = E[kk * nw + i];
+    __syncwarp();
+    for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
+    for (int idx = lane; idx < nw * nw; idx += L) {  // dinv(x, y) = 1/(E_x - E_y), 0 below 1e-7
+      const int x = idx / nw, y = idx % nw;
+      const double dE = myE[x] - myE[y];
+      myDinv[idx] = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+    }
+    __syncwarp();
+    int below = 0, f0 = nw;
+    for (int n = lane; n < nw; n += L) {
+      below += myE[n] < sp.EFmin;
+      if (myS[n]) {
+        int g1 = n + 1;
+        while (g1 < nw && !myS[g1]) ++g1;
+        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+      }
+    }
+    below = group_sum_i(below, L);
+    f0 = group_min_i(f0, L);
+    const int bandmax = min(below, f0);
+    const V* Xk = Xbar + kk * nFbar * nw2;
+#define XV(a, x, y) Xk[(iV + (a)) * nw2 + (x) * nw + (y)]
+#define XA(a, x, y) Xk[(iA + (a)) * nw2 + (x) * nw + (y)]
+#define XO(a, x, y) Xk[(iO + (a)) * nw2 + (x) * nw + (y)]
+#define XW(a, b, x, y) Xk[(iW + 3 * (a) + (b)) * nw2 + (x) * nw + (y)]
+#define XdA(b, d, x, y) Xk[(idA + 3 * (b) + (d)) * nw2 + (x) * nw + (y)]
+#define XdO(c, d, x, y) Xk[(idO + 3 * (c) + (d)) * nw2 + (x) * nw + (y)]
+#define DV(a, x, y) cscale(XV(a, x, y), -myDinv[(x) * nw + (y)])
+    for (int m = lane; m < nw; m += L) {
+      int gs = m, ge = m + 1;
+      while (!myS[gs]) --gs;
+      while (ge < nw && !myS[ge]) ++ge;
+      bool ingroup;
+      if (m < bandmax) { gs = 0; ge = bandmax; ingroup = true; }
+      else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
+      double val[9];
+      for (int i = 0; i < 9; ++i) val[i] = 0.0;
+      if (ingroup) {
+        for (int l = 0; l < nw; ++l) {
+          if (l >= gs && l < ge) continue;
+          const T dlm = myDinv[l * nw + m];  // 1/(E_l - E_m)
+          V dDlm[9], dDml[9], dAlm[9];
+          for (int i = 0; i < 9; ++i) { dDlm[i] = czero<V>(); dDml[i] = czero<V>(); dAlm[i] = czero<V>(); }
+          for (int p = 0; p < nw; ++p) {
+            const bool inG = (p >= gs && p < ge);
+            V Vlp[3], Vpm[3], Vmp[3], Vpl[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { Vlp[a] = XV(a, l, p); Vpm[a] = XV(a, p, m); Vmp[a] = XV(a, m, p); Vpl[a] = XV(a, p, l); }
+            if (!inG) {
+              // dD_lm: + V^b_lp D^d_pm ; dD_ml: - D^a_mp V^d_pl ; dA_lm: + A^b_lp D^d_pm
+              const T dpm = myDinv[p * nw + m], dmp = myDinv[m * nw + p];
+              V Dpm[3], Dmp[3], Alp[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                Dpm[a] = cscale(Vpm[a], -dpm);
+                Dmp[a] = cscale(Vmp[a], -dmp);
+                Alp[a] = external_terms ? XA(a, l, p) : czero<V>();
+              }
+#pragma unroll
+              for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                  cfma(dDlm[3 * b + d], Vlp[b], Dpm[d]);
+                  dDml[3 * b + d] = csub(dDml[3 * b + d], cmul(Dmp[b], Vpl[d]));
+                  cfma(dAlm[3 * b + d], Alp[b], Dpm[d]);
+                }
+            } else {
+              // dD_lm: - D^b_lp V^d_pm ; dD_ml: + V^a_mp D^d_pl ; dA_lm: - D^d_lp A^b_pm
+              const T dlp = myDinv[l * nw + p], dpl = myDinv[p * nw + l];
+              V Dlp[3], Dpl[3], Apm[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                Dlp[a] = cscale(Vlp[a], -dlp);
+                Dpl[a] = cscale(Vpl[a], -dpl);
+                Apm[a] = external_terms ? XA(a, p, m) : czero<V>();
+              }
+#pragma unroll
+              for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                  dDlm[3 * b + d] = csub(dDlm[3 * b + d], cmul(Dlp[b], Vpm[d]));
+                  cfma(dDml[3 * b + d], Vmp[b], Dpl[d]);
+                  dAlm[3 * b + d] = csub(dAlm[3 * b + d], cmul(Dlp[d], Apm[b]));
+                }
+            }
+          }
+          const T dml = myDinv[m * nw + l];  // 1/(E_m - E_l)
+          // symmetrise in (b, d) (the bracket is symmetric, W = d_b d_d H too) and scale
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int d = b; d < 3; ++d) {
+              const V t1 = cadd(cadd(dDlm[3 * b + d], dDlm[3 * d + b]), XW(b, d, l, m));
+              const V t2 = cadd(cadd(dDml[3 * b + d], dDml[3 * d + b]), XW(b, d, m, l));
+              dDlm[3 * b + d] = cscale(t1, -dlm);
+              dDml[3 * b + d] = cscale(t2, -dml);
+            }
+#pragma unroll
+          for (int b = 1; b < 3; ++b)
+#pragma unroll
+            for (int d = 0; d < b; ++d) { dDlm[3 * b + d] = dDlm[3 * d + b]; dDml[3 * b + d] = dDml[3 * d + b]; }
+          if (external_terms) {
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) dAlm[3 * b + d] = cadd(dAlm[3 * b + d], XdA(b, d, l, m));
+          }
+          V Dml[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) Dml[a] = DV(a, m, l);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const int al = (c + 1) % 3, be = (c + 2) % 3;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              double acc = 0.0;
+              for (int t = 0; t < 2; ++t) {
+                const double sg = t == 0 ? 1.0 : -1.0;
+                const int a = t == 0 ? al : be, b = t == 0 ? be : al;
+                if (internal_terms) acc += sg * (double)cmul(Dml[a], dDlm[3 * b + d]).y;  // Re(-i s x) = s Im x
+                if (external_terms) {
+                  acc -= sg * (double)cmul(Dml[a], dAlm[3 * b + d]).x;
+                  acc -= sg * (double)cmul(dDml[3 * a + d], XA(b, l, m)).x;
+                }
+              }
+              if (external_terms) {  // 1/2 dO_mm: - D^d_ml O^c_lm + O^c_ml D^d_lm
+                const V Dlm_d = DV(d, l, m);
+                acc += 0.5 * ((double)cmul(Dml[d], XO(c, l, m)).x * -1.0 + (double)cmul(XO(c, m, l), Dlm_d).x);
+              }
+              val[3 * c + d] += 2.0 * acc;
+            }
+          }
+        }
+        if (external_terms) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) val[3 * c + d] += (double)XdO(c, d, m, m).x;  // 2 Re(1/2 dOc_mm)
+          // -i s sum_{n' in G} A^a_mn' dA^{bd}_n'm
+          for (int np = gs; np < ge; ++np) {
+            V dAn[9];
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) dAn[3 * b + d] = XdA(b, d, np, m);
+            for (int l = 0; l < nw; ++l) {
+              if (l >= gs && l < ge) continue;
+              V Dnl[3], Dlm[3], Alm[3], Anl[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                Dnl[a] = DV(a, np, l);
+                Dlm[a] = DV(a, l, m);
+                Alm[a] = XA(a, l, m);
+                Anl[a] = XA(a, np, l);
+              }
+#pragma unroll
+              for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                  dAn[3 * b + d] = csub(dAn[3 * b + d], cmul(Dnl[d], Alm[b]));
+                  cfma(dAn[3 * b + d], Anl[b], Dlm[d]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const int al = (c + 1) % 3, be = (c + 2) % 3;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) {
+                const double x1 = (double)cmul(XA(al, m, np), dAn[3 * be + d]).y;
+                const double x2 = (double)cmul(XA(be, m, np), dAn[3 * al + d]).y;
+                val[3 * c + d] += 2.0 * (x1 - x2);  // 2 Re(-i s A dA) = 2 s Im(A dA)
+              }
+            }
+          }
+        }
+      }
+      for (int i = 0; i < 9; ++i) myT[m * 9 + i] = val[i];
+    }
+#undef XV
+#undef XA
+#undef XO
+#undef XW
+#undef XdA
+#undef XdO
+#undef DV
+    __syncwarp();
+    if (valid) {
+      for (int n = lane; n < nw; n += L) {
+        int gs = -1, ge = -1;
+        bool sea = false;
+        if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; sea = true; }
+        else if (n >= bandmax && myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
+        }
+        if (gs < 0) continue;
+        double v[9], esum = 0.0;
+        for (int i = 0; i < 9; ++i) v[i] = 0.0;
+        for (int q = gs; q < ge; ++q) {
+          for (int i = 0; i < 9; ++i) v[i] += myT[q * 9 + i];
+          esum += myE[q];
+        }
+        int bin = -1;
+        if (sea) bin = 0;
+        else {
+          const double Em = esum / (double)(ge - gs);
+          if (Em < sp.EFmin) bin = 0;
+          else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
+        }
+        if (bin >= 0 && bin < sp.nEF)
+          for (int i = 0; i < 9; ++i) atomicAdd(&sh[bin * 9 + i], v[i]);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 9 * sp.nEF; i += blockDim.x)
+    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+}
+
 // cumulative sum over Fermi levels and normalisation: out[ie][c] = scale * sum_{j<=ie} hist[j][c]
 __global__ void scan_finalize_kernel(const double* __restrict__ hist, int nEF, int ncomp, double scale,
                                      double* __restrict__ out) {
@@ -373,6 +789,71 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
     cudaFuncSetAttribute(berry_omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
                                                                 G, *sp, internal_terms, external_terms, hist);
+  }
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
+                       int nk, const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
+                       cudaStream_t stream) {
+  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E || !Xbar) return WBG_ERR_ARG;
+  if (iV < 0 || iV + 3 > nFbar) return WBG_ERR_ARG;
+  if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar || iB < 0 || iB + 3 > nFbar ||
+                         iC < 0 || iC + 3 > nFbar))
+    return WBG_ERR_ARG;
+  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
+  const int L = lanes_for(nw);
+  if ((nw + L - 1) / L > WBG_BAND_MAXPER) return WBG_ERR_SIZE;
+  const int G = 128 / L;
+  const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * 8 + (size_t)G * (nw + 1) * 24 + (size_t)G * nw * 4;
+  if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  long long nblk = (nk + G - 1) / G;
+  const long long cap = (long long)sms * 8;
+  if (nblk > cap) nblk = cap;
+  if (fp64) {
+    cudaFuncSetAttribute(berry_morb_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_morb_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iB, iC,
+                                                                nw, nk, L, G, *sp, internal_terms, external_terms, hist);
+  } else {
+    cudaFuncSetAttribute(berry_morb_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_morb_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iB, iC, nw,
+                                                               nk, L, G, *sp, internal_terms, external_terms, hist);
+  }
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
+                           int idO, int nw, int nk, const WbgScan* sp, int internal_terms, int external_terms,
+                           double* hist, int fp64, cudaStream_t stream) {
+  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E || !Xbar) return WBG_ERR_ARG;
+  if (iV < 0 || iV + 3 > nFbar || iW < 0 || iW + 9 > nFbar) return WBG_ERR_ARG;
+  if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar || idA < 0 || idA + 9 > nFbar ||
+                         idO < 0 || idO + 9 > nFbar))
+    return WBG_ERR_ARG;
+  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
+  const int L = lanes_for(nw);
+  const int G = 64 / L > 0 ? 64 / L : 1;
+  const size_t tsz = fp64 ? 8 : 4;
+  const size_t sm = 9 * (size_t)sp->nEF * 8 + (size_t)G * nw * 8 + (size_t)G * nw * 72 + (size_t)G * nw * nw * tsz +
+                    (size_t)G * nw * 4;
+  if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  long long nblk = (nk + G - 1) / G;
+  const long long cap = (long long)sms * 8;
+  if (nblk > cap) nblk = cap;
+  if (fp64) {
+    cudaFuncSetAttribute(berry_deromega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_deromega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iW,
+                                                                    idA, idO, nw, nk, L, G, *sp, internal_terms,
+                                                                    external_terms, hist);
+  } else {
+    cudaFuncSetAttribute(berry_deromega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_deromega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA,
+                                                                   idO, nw, nk, L, G, *sp, internal_terms,
+                                                                   external_terms, hist);
   }
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -5,9 +5,18 @@
 
 typedef wbg_scan WbgScan;
 
+// bands per lane held in registers by the non-additive (Morb) kernel: nw <= 32 * WBG_BAND_MAXPER
+#define WBG_BAND_MAXPER 4
+
 int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream);
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                         const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
                         cudaStream_t stream);
+int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
+                       int nk, const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
+                       cudaStream_t stream);
+int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
+                           int idO, int nw, int nk, const WbgScan* sp, int internal_terms, int external_terms,
+                           double* hist, int fp64, cudaStream_t stream);
 int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);

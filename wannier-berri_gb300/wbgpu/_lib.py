@@ -12,7 +12,7 @@ from . import build as _build
 
 EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate',
-           'wbg_berry_omega',
+           'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
            'wbg_scan_finalize', 'wbg_probe_fma']
 
 STATUS_OK = 0
@@ -33,6 +33,12 @@ class Scan(ctypes.Structure):
                 ('degen_thresh', ctypes.c_double), ('nEF', ctypes.c_int), ('reserved', ctypes.c_int)]
 
 
+class KuboParams(ctypes.Structure):
+    _fields_ = [('EFmin', ctypes.c_double), ('EFmax', ctypes.c_double), ('kBT', ctypes.c_double),
+                ('eta', ctypes.c_double), ('degen_thresh', ctypes.c_double), ('nEF', ctypes.c_int),
+                ('nOmega', ctypes.c_int), ('gaussian', ctypes.c_int), ('reserved', ctypes.c_int)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _LL = ctypes.c_longlong
@@ -49,6 +55,11 @@ _SIGS = {
     'wbg_eigh_batched_noalloc': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _P]),
     'wbg_rotate': (_I, [_P, _LL, _P, _I, _P, _P, _I, _P, _I, _I, _I, _P]),
     'wbg_berry_omega': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),
+    'wbg_berry_morb': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),
+    'wbg_berry_deromega': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I,
+                                _P]),
+    'wbg_kubo_workspace_size': (_I, [_I, _I, _I, ctypes.POINTER(_SZ)]),
+    'wbg_kubo': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(KuboParams), _P, _P, _P, _SZ, _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
     'wbg_probe_fma': (_I, [_I, _I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), _P]),
 }

@@ -2,7 +2,8 @@
 
 Mirrors calculators/static.py:24-169 (StaticCalculator: Fermi-level scan with
 cumulative weights, /cell_volume /nk * constant_factor) for ``AHC``
-(calculators/static.py:353-364).  A calculator declares the band-basis quantities it
+(calculators/static.py:353-364), ``Morb`` (:231-247), ``BerryDipole_FermiSea``
+(:472-487), and calculators/dynamic.py:26-196 for ``OpticalConductivity``.  A calculator declares the band-basis quantities it
 needs (``quantities``), accumulates a device histogram per batch of blocks
 (``accumulate``) and turns it into an ``EnergyResult`` (``finalize``).  Formulae
 without a GPU kernel raise NotImplementedError: there is no CPU fallback.
@@ -15,7 +16,7 @@ import torch
 from . import _lib
 from . import engine
 from .engine import _ptr, _stream
-from .factors import factor_ahc
+from .factors import factor_ahc, factor_morb, factor_opt
 from .result import EnergyResult
 
 
@@ -91,3 +92,123 @@ class AHC(StaticCalculator):
 
     def result(self, cell_volume, nk, factor=1.0):
         return EnergyResult(self.Efermi, self.finalize(cell_volume, nk, factor))
+
+
+class Morb(StaticCalculator):
+    r"""Orbital magnetic moment per unit cell (mu_B): M = -\int [dk] (H + G - 2 E_f Omega) f
+    (calculators/static.py:231-247; formula Morb_Hpm, formula/covariant.py:424-449)."""
+
+    def __init__(self, constant_factor=factor_morb, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+    def quantities(self, system):
+        return {'V', 'A', 'O', 'B', 'C'} if self.external(system) else {'V'}
+
+    def reset(self, device):
+        super().reset(device)
+        self._hist_omega = torch.zeros_like(self._hist)
+
+    def accumulate(self, bd, system):
+        ext = self.external(system)
+        sc = self.scan_struct()
+        lib = _lib.load()
+        g = lambda q: bd.index.get(q, 0)
+        st = engine._timed('berry_morb', lib.wbg_berry_morb, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], g('V'),
+                           g('A'), g('O'), g('B'), g('C'), bd.nw, bd.nk_total, ctypes.byref(sc),
+                           int(self.internal_terms), int(ext), _ptr(self._hist), int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_morb")
+        st = engine._timed('berry_omega', lib.wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1],
+                           g('V'), g('A'), g('O'), bd.nw, bd.nk_total, ctypes.byref(sc), int(self.internal_terms),
+                           int(ext), _ptr(self._hist_omega), int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_omega")
+
+    def result(self, cell_volume, nk, factor=1.0):
+        H = self.finalize(cell_volume, nk, factor)
+        hist = self._hist
+        self._hist = self._hist_omega
+        O = self.finalize(cell_volume, nk, factor)
+        self._hist = hist
+        return EnergyResult(self.Efermi, (H - 2.0 * self.Efermi[:, None] * O) * cell_volume)
+
+
+class BerryDipole_FermiSea(StaticCalculator):
+    r"""Berry curvature dipole (dimensionless): D = \int [dk] d_b Omega_d f
+    (calculators/static.py:472-487; formula DerOmega, formula/covariant.py:212-259)."""
+    ncomp = 9
+
+    def quantities(self, system):
+        return {'V', 'W', 'A', 'O', 'dA', 'dO'} if self.external(system) else {'V', 'W'}
+
+    def accumulate(self, bd, system):
+        ext = self.external(system)
+        sc = self.scan_struct()
+        g = lambda q: bd.index.get(q, 0)
+        st = engine._timed('berry_deromega', _lib.load().wbg_berry_deromega, _ptr(bd.E), _ptr(bd.Xbar),
+                           bd.Xbar.shape[1], g('V'), g('A'), g('O'), g('W'), g('dA'), g('dO'), bd.nw, bd.nk_total,
+                           ctypes.byref(sc), int(self.internal_terms), int(ext), _ptr(self._hist),
+                           int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_deromega")
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self.finalize(cell_volume, nk, factor).reshape(-1, 3, 3)
+        return EnergyResult(self.Efermi, data.swapaxes(1, 2))
+
+
+class OpticalConductivity(Calculator):
+    r"""Kubo optical conductivity (calculators/dynamic.py:184-196, Formula_OptCond :170-181)."""
+
+    def __init__(self, Efermi=None, omega=None, kBT=0, smr_fixed_width=0.1, smr_type='Lorentzian',
+                 kwargs_formula=None, **kwargs):
+        super().__init__(**kwargs)
+        self.Efermi = np.array(Efermi, dtype=float).reshape(-1)
+        self.omega = np.array(omega, dtype=float)
+        self.kBT = kBT
+        self.smr_fixed_width = smr_fixed_width
+        if smr_type not in ('Lorentzian', 'Gaussian'):
+            raise ValueError(f"Invalid smearing type {smr_type}")
+        self.smr_type = smr_type
+        self.kwargs_formula = dict(kwargs_formula or {})
+        self.external_terms = self.kwargs_formula.get('external_terms', True)
+        self.constant_factor = factor_opt
+        self._out = None
+
+    def external(self, system):
+        return self.external_terms and not system.force_internal_terms_only
+
+    def quantities(self, system):
+        return {'V', 'A'} if self.external(system) else {'V'}
+
+    def reset(self, device):
+        self._out = torch.zeros((len(self.Efermi), len(self.omega), 9), dtype=torch.complex128, device=device)
+        self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
+        self._om = torch.tensor(self.omega, dtype=torch.float64, device=device)
+
+    def accumulate(self, bd, system, max_workspace=4 << 30):
+        lib = _lib.load()
+        ext = self.external(system)
+        kp = _lib.KuboParams(EFmin=float(self.Efermi.min()), EFmax=float(self.Efermi.max()), kBT=float(self.kBT),
+                             eta=float(self.smr_fixed_width), degen_thresh=float(self.degen_thresh),
+                             nEF=len(self.Efermi), nOmega=len(self.omega), gaussian=int(self.smr_type == 'Gaussian'),
+                             reserved=0)
+        nw, nkt = bd.nw, bd.nk_total
+        per_k = ctypes.c_size_t(0)
+        _lib.check(lib.wbg_kubo_workspace_size(nw, 1, len(self.Efermi), ctypes.byref(per_k)), "wbg_kubo_workspace_size")
+        chunk = max(1, min(nkt, int(max_workspace // per_k.value)))
+        ws = ctypes.c_size_t(0)
+        _lib.check(lib.wbg_kubo_workspace_size(nw, chunk, len(self.Efermi), ctypes.byref(ws)), "wbg_kubo_workspace_size")
+        work = torch.empty(int(ws.value), dtype=torch.uint8, device=bd.E.device)
+        nF = bd.Xbar.shape[1]
+        esz = bd.Xbar.element_size()
+        for k0 in range(0, nkt, chunk):
+            n = min(chunk, nkt - k0)
+            Xp = ctypes.c_void_p(bd.Xbar.data_ptr() + k0 * nF * nw * nw * esz)
+            Ep = ctypes.c_void_p(bd.E.data_ptr() + k0 * nw * 8)
+            st = engine._timed('kubo', lib.wbg_kubo, Ep, Xp, nF, bd.index['V'], bd.index.get('A', 0), nw, n, int(ext),
+                               ctypes.byref(kp), _ptr(self._ef), _ptr(self._om), _ptr(work),
+                               ctypes.c_size_t(work.numel()), _ptr(self._out), int(bd.fp64_fields), _stream())
+            _lib.check(st, "wbg_kubo")
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self._out.cpu().numpy().reshape(len(self.Efermi), len(self.omega), 3, 3)
+        data = data * (self.constant_factor / (nk * cell_volume) * factor)
+        return EnergyResult([self.Efermi, self.omega], data)
