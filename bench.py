@@ -221,7 +221,7 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
         else:
             bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
     elif stage.startswith('r2k'):
-        s = 16 if stage == 'r2k_fp64' else 8
+        s = 16 if stage in ('r2k_fp64', 'r2k_df64') else 8
         work = 2.0 * nF_fields[stage] * n * n * s * k_per_call   # bytes: write + read back of each field
         bound, unit, peak, src = 'hbm', 'GB/s', peaks['hbm'], 'MEASURED_PEAKS.json hbm_gbs'
     else:  # berry_omega
@@ -314,7 +314,7 @@ def run_gpu(args):
     value = total_k / (ms * 1e-3)
     stage_ms = timer.totals_ms()
     counts = timer.counts()
-    kernels_per_call = {'r2k_fp64': 3, 'r2k_fp32': 3, 'eigh': 3, 'rotate': 1, 'berry_omega': 1}
+    kernels_per_call = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'eigh': 3, 'rotate': 1, 'berry_omega': 1}
     gpu_launches = int(sum(counts[k] * kernels_per_call[k] for k in counts))
 
     # plain FP64 drop-in throughput on the same blocks, and the mixed-vs-FP64 error of one step
@@ -365,7 +365,7 @@ def run_gpu(args):
         peaks['hbm'] = float(mp_['hbm_gbs'])
     except (OSError, KeyError, ValueError):
         peaks['hbm'] = 6800.0  # fallback figure of the profiling recipe
-    nF_fields = {'r2k_fp64': 10 if precision == 'fp64' else 1, 'r2k_fp32': 9}
+    nF_fields = {'r2k_fp64': 10, 'r2k_df64': 1, 'r2k_fp32': 9}
     dominant = max(stage_ms, key=stage_ms.get)
     roof = stage_roofline(dominant, stage_ms[dominant], counts[dominant], B * nk, precision, peaks, nF_fields)
     if rank != 0:

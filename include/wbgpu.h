@@ -70,19 +70,21 @@ const char* wbg_status_string(int status);
  *            3 curl component a of i w A (A = bases base..base+2); 4 i w_b times that curl,
  *            with w = R + t_n - t_m in Cartesian coordinates (fourier/rvectors.py:355-369,
  *            487-494; data_K/data_K_R.py:48-51)
- *   XF       [nfields][nR][nw][nw] complex (fp64 ? double : float)
+ *   XF       [nfields][nR][nw][nw] complex: prec 0 float, 1 double, 2 double-float (re.hi, re.lo,
+ *            im.hi, im.lo floats: 48-bit significand on the FP32 pipe)
  * wbg_r2k (per batch of FFT blocks): fields_out[b*nk + k][f] = sum_R exp(2 pi i R.(j_k/N + dK_b)) XF[f][R]
  *   pair_start [nP+1] first sorted R of each pair;  r2 [nR] third R component
  *   slice_start [nU+1] first pair of each slice;    pair_r1 [nP];  slice_r0 [nU]
- *   ph0/ph1/ph2 [nblocks][N_d][nr_d] complex: exp(2 pi i R_d (j/N_d + dK_d)), R_d = rmin_d + r
- *   fields_out [nblocks*nk][nfields][nw][nw] complex, k = (j0*N1 + j1)*N2 + j2
+ *   ph0/ph1/ph2 [nblocks][N_d][nr_d] complex (precision prec): exp(2 pi i R_d (j/N_d + dK_d)),
+ *            R_d = rmin_d + r
+ *   fields_out [nblocks*nk][nfields][nw][nw] complex (precision prec), k = (j0*N1 + j1)*N2 + j2
  */
 int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, const int* field_desc, int nfields,
-                   const double* wcc, const wbg_lattice* lat, int fp64, void* XF, void* stream);
-int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int fp64, size_t* bytes);
+                   const double* wcc, const wbg_lattice* lat, int prec, void* XF, void* stream);
+int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int prec, size_t* bytes);
 int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, const int* slice_start,
             const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, int nblocks,
-            int fp64, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
+            int prec, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
             void* stream);
 
 /* ---- stage 2: batched Hermitian eigensolver ---------------------------------------------
@@ -92,7 +94,9 @@ int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, c
  * mode 1: everything in FP64, U complex128 (the plain FP64 path);
  * mode 2: tridiagonalisation, eigenvalues and inverse iteration in double-float arithmetic
  *         (pairs of FP32, 48-bit significand, on the FP32 pipe), back-transform in FP32,
- *         U complex64 (the mixed-precision path).
+ *         U complex64;
+ * mode 3: as mode 2 with H given as double-float complex (wbg_r2k prec 2 output; the
+ *         mixed-precision path).
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);

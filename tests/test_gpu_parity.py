@@ -59,6 +59,20 @@ def test_r2k_fields(c2small, fp64, tol, NKFFT):
             assert maxrel(got, ref) < tol, (name, ib, maxrel(got, ref))
 
 
+def test_r2k_double_float_hamiltonian(c2small):
+    """H(k) from the double-float transform (48-bit significand) against the oracle's FP64 FFT."""
+    s, o = c2small
+    dev = engine.DeviceSystem(s)
+    NKFFT = (4, 3, 5)
+    dK = np.array([[0.13, -0.21, 0.37]]) / np.array(NKFFT)
+    fields, index, nF, _ = engine.r2k(dev, dK, NKFFT, set(), True, engine.PREC_DF64)
+    raw = fields.cpu().numpy().view(np.float32).reshape(fields.shape[0], nF, s.num_wann, s.num_wann, 4)
+    got = (raw[..., 0].astype(np.float64) + raw[..., 1]) + 1j * (raw[..., 2].astype(np.float64) + raw[..., 3])
+    data = O.DataK(o, NKFFT, dK[0])
+    ref = data.R_to_k(data.get_R_mat('Ham'), 0, hermitian=False)
+    assert maxrel(got[:, 0], ref) < 1e-13
+
+
 @pytest.mark.parametrize("mode", [1, 0, 2])
 @pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
 def test_eigh_random(nw, mode):

@@ -23,26 +23,26 @@ const char* wbg_status_string(int status) {
 }
 
 int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, const int* field_desc, int nfields,
-                   const double* wcc, const wbg_lattice* lat, int fp64, void* XF, void* stream) {
-  return wbg_r2k_fields_run(XR, nBase, iR, nR, nw, reinterpret_cast<const int4*>(field_desc), nfields, wcc, lat, fp64,
+                   const double* wcc, const wbg_lattice* lat, int prec, void* XF, void* stream) {
+  return wbg_r2k_fields_run(XR, nBase, iR, nR, nw, reinterpret_cast<const int4*>(field_desc), nfields, wcc, lat, prec,
                             XF, (cudaStream_t)stream);
 }
 
-int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int fp64, size_t* bytes) {
-  if (!g || !bytes || nfields < 1 || nblocks < 1) return WBG_STATUS_BAD_ARGUMENT;
-  *bytes = wbg_r2k_workspace_bytes(g, nfields, nblocks, fp64);
+int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int prec, size_t* bytes) {
+  if (!g || !bytes || nfields < 1 || nblocks < 1 || prec < 0 || prec > 2) return WBG_STATUS_BAD_ARGUMENT;
+  *bytes = wbg_r2k_workspace_bytes(g, nfields, nblocks, prec);
   return WBG_STATUS_OK;
 }
 
 int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, const int* slice_start,
             const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, int nblocks,
-            int fp64, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
+            int prec, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
             void* stream) {
   if (!XF || !pair_start || !r2 || !slice_start || !pair_r1 || !slice_r0 || !ph0 || !ph1 || !ph2 || !workspace ||
       !fields_out || !g)
     return WBG_STATUS_BAD_ARGUMENT;
   return wbg_r2k_run(XF, nfields, pair_start, r2, slice_start, pair_r1, slice_r0, ph0, ph1, ph2, workspace,
-                     workspace_bytes, fields_out, g, nblocks, fp64, (cudaStream_t)stream);
+                     workspace_bytes, fields_out, g, nblocks, prec, (cudaStream_t)stream);
 }
 
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes) {

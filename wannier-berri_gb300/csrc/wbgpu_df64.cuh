@@ -155,3 +155,9 @@ __device__ __forceinline__ df64 shfl_xor(df64 v, int off) {
   return v;
 }
 
+// conversion of a double into each working real type
+template <typename T> __device__ __forceinline__ T real_from_double(double x);
+template <> __device__ __forceinline__ float real_from_double<float>(double x) { return (float)x; }
+template <> __device__ __forceinline__ double real_from_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ df64 real_from_double<df64>(double x) { return df_from(x); }
+

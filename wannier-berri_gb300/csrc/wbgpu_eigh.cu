@@ -35,6 +35,19 @@ WBG_D typename C2<R>::t from_c64(double2 a) {
   r.y = Arith<R>::from(a.y);
   return r;
 }
+// 1/2 (a + conj(b)) of two input elements, input either complex128 or double-float complex
+template <typename R>
+WBG_D typename C2<R>::t herm_avg(double2 a, double2 b) {
+  return from_c64<R>(make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)));
+}
+template <typename R>
+WBG_D typename C2<R>::t herm_avg(cdf a, cdf b) {
+  typename C2<R>::t r;
+  const df64 half = df_from_f(0.5f);
+  r.x = (a.x + b.x) * half;
+  r.y = (a.y - b.y) * half;
+  return r;
+}
 
 // ---------------------------------------------------------------------------------------
 // 1. Householder tridiagonalisation.  grid: ceil(nk/G) blocks of G*L threads.
@@ -49,8 +62,8 @@ WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
 
-template <typename R>
-__global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, int n, int nk, int L, int G,
+template <typename R, typename HIn>
+__global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n, int nk, int L, int G,
                              typename C2<R>::t* __restrict__ Vh, typename C2<R>::t* __restrict__ tauOut,
                              R* __restrict__ dOut, R* __restrict__ eOut) {
   typedef typename C2<R>::t CR;
@@ -64,13 +77,10 @@ __global__ void eigh_tridiag(const double2* __restrict__ H, long long strideK, i
   CR* Am = reinterpret_cast<CR*>(smt) + (size_t)grp * (n * ld + 2 * n);
   CR* vs = Am + n * ld;
   CR* ws = vs + n;
-  const double2* Hk = H + k * strideK;
+  const HIn* Hk = H + k * strideK;
   for (int idx = lane; idx < n * n; idx += L) {
     const int i = idx / n, j = idx % n;
-    if (j <= i) {
-      const double2 a = Hk[i * n + j], b = Hk[j * n + i];
-      Am[i * ld + j] = from_c64<R>(make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)));
-    }
+    if (j <= i) Am[i * ld + j] = herm_avg<R>(Hk[i * n + j], Hk[j * n + i]);
   }
   __syncwarp();
   const R zero = A::from(0.0), one = A::from(1.0), mhalf = A::from(-0.5);
@@ -398,7 +408,7 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
-template <typename R, typename TU>
+template <typename R, typename TU, typename HIn>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, void* workspace,
                 int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
@@ -414,9 +424,9 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   int G = (4 * 32) / LT;
   while (G > 1 && G * smT > 96 * 1024) G /= 2;
   if (G * smT > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_tridiag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  eigh_tridiag<R><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const double2*)H, strideH, n, nk, LT, G, Vh, tau, d,
-                                                                  e);
+  cudaFuncSetAttribute(eigh_tridiag<R, HIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  eigh_tridiag<R, HIn><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G, Vh, tau,
+                                                                       d, e);
   eigh_ql<R><<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
   const size_t ubytes = ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
@@ -440,11 +450,14 @@ size_t wbg_eigh_workspace_bytes(int n, int nk) {
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int mode,
                  void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
   if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
-  if (mode < 0 || mode > 2) return WBG_ERR_ARG;
+  if (mode < 0 || mode > 3) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
-  if (mode == 1) return launch_eigh<double, double>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
-  if (mode == 0) return launch_eigh<double, float>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
-  return launch_eigh<df64, float>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  if (mode == 1)
+    return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  if (mode == 0)
+    return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  if (mode == 2) return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
 }
 
 // ---------------------------------------------------------------------------------------

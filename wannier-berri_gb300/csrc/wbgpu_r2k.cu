@@ -17,6 +17,7 @@
 //    Each thread keeps the (<= MAXL) inputs of its matrix elements in registers and loops
 //    over the output index; the per-axis phase tables are broadcast from shared memory.
 #include "wbgpu_common.cuh"
+#include "wbgpu_df64.cuh"
 #include "wbgpu_r2k.cuh"
 
 namespace {
@@ -62,7 +63,7 @@ __global__ void r2k_weights(const double2* __restrict__ XR, const int* __restric
     v = cmuli(csub(cscale(Ab, w[al]), cscale(Aa, w[be])));
     if (fd.x == R2K_DROT) v = cmuli(cscale(v, w[fd.w]));  // derivative of the curl
   }
-  XF[((long long)f * nR + r) * nw2 + mn] = mkc<T>((T)v.x, (T)v.y);
+  XF[((long long)f * nR + r) * nw2 + mn] = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
 }
 
 // One separable contraction: out[col][j] = sum_{i < len} tab[j][idx[i]] in[col][i]
@@ -216,22 +217,26 @@ int launch_r2k(const void* XF, int nF, const int* pairStart, const int* r2, cons
 
 }  // namespace
 
-size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int fp64) {
-  const size_t cs = fp64 ? sizeof(double2) : sizeof(float2);
+size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int prec) {
+  const size_t cs = prec ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   const size_t y = (size_t)nb * nF * g->nU * g->N1 * g->N2 * g->nw2 * cs;
   return ((z + 255) / 256) * 256 + y;
 }
 
 int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, int nw, const int4* fdesc, int nF,
-                       const double* wcc, const R2KLattice* lat, int fp64, void* XF, cudaStream_t stream) {
+                       const double* wcc, const R2KLattice* lat, int prec, void* XF, cudaStream_t stream) {
   if (!XR || !iRsorted || !fdesc || !wcc || !lat || !XF || nBase < 1 || nR < 1 || nw < 1 || nF < 1)
     return WBG_ERR_ARG;
   const long long n = (long long)nR * nw * nw;
   dim3 grid((unsigned)((n + 255) / 256), nF);
-  if (fp64)
+  if (prec < 0 || prec > 2) return WBG_ERR_ARG;
+  if (prec == 1)
     r2k_weights<double><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
                                                   (double2*)XF);
+  else if (prec == 2)
+    r2k_weights<df64><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+                                                (cdf*)XF);
   else
     r2k_weights<float><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
                                                  (float2*)XF);
@@ -240,18 +245,21 @@ int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, i
 
 int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
-                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int fp64, cudaStream_t stream) {
-  if (!g || nF <= 0 || nb <= 0) return WBG_ERR_ARG;
+                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, cudaStream_t stream) {
+  if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 2) return WBG_ERR_ARG;
   if (g->nw2 != g->nw * g->nw || g->nk != g->N0 * g->N1 * g->N2) return WBG_ERR_ARG;
   if (g->nU < 1 || g->nP < 1 || g->maxPairLen < 1 || g->maxSliceLen < 1) return WBG_ERR_ARG;
-  if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, fp64)) return WBG_ERR_WORKSPACE;
-  const size_t cs = fp64 ? sizeof(double2) : sizeof(float2);
+  if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, prec)) return WBG_ERR_WORKSPACE;
+  const size_t cs = prec ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   char* Z = (char*)workspace;
   char* Y = Z + ((z + 255) / 256) * 256;
-  if (fp64)
+  if (prec == 1)
     return launch_r2k<double>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                               stream);
+  if (prec == 2)
+    return launch_r2k<df64>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+                            stream);
   return launch_r2k<float>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                            stream);
 }

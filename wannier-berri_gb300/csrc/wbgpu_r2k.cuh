@@ -17,9 +17,9 @@ typedef wbg_lattice R2KLattice;
 #define R2K_ROT 3   // (A0 base, g)         curl of i (R + t_n - t_m) A_R, component g
 #define R2K_DROT 4  // (A0 base, g, d)      i (R + t_n - t_m)_d times that curl
 
-size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int fp64);
+size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int prec);
 int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, int nw, const int4* fdesc, int nF,
-                       const double* wcc, const R2KLattice* lat, int fp64, void* XF, cudaStream_t stream);
+                       const double* wcc, const R2KLattice* lat, int prec, void* XF, cudaStream_t stream);
 int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
-                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int fp64, cudaStream_t stream);
+                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, cudaStream_t stream);

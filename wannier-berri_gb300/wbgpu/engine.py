@@ -272,12 +272,40 @@ def r2k_geometry(dev, NKFFT):
                         maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
 
 
-def field_arrays(dev, quantities, with_H, fp64):
+PREC_FP32, PREC_FP64, PREC_DF64 = 0, 1, 2
+
+
+def _prec(p):
+    """precision argument: bool (True = FP64, False = FP32) or PREC_* code"""
+    if p is True:
+        return PREC_FP64
+    if p is False:
+        return PREC_FP32
+    return int(p)
+
+
+def _df64_pairs(z):
+    """complex128 array -> float32 array [..., 4] = (re.hi, re.lo, im.hi, im.lo) (double-float layout)."""
+    parts = []
+    for x in (z.real, z.imag):
+        hi = x.astype(np.float32)
+        lo = (x - hi.astype(np.float64)).astype(np.float32)
+        parts += [hi, lo]
+    return np.stack(parts, axis=-1)
+
+
+def _complex_tensor(shape, prec, device):
+    """storage for complex values of precision prec (double-float uses complex128-sized slots)"""
+    return torch.empty(shape, dtype=torch.complex64 if prec == PREC_FP32 else torch.complex128, device=device)
+
+
+def field_arrays(dev, quantities, with_H, prec):
     """R-space arrays XF[f][R][mn] of the requested k-space fields (wbg_r2k_fields), cached on
     the device system: the derivative / curl weights depend on the system only, not on dK."""
+    prec = _prec(prec)
     keys = extra_keys_for(quantities)
     desc, index = field_plan(quantities, with_H, keys)
-    ck = ('XF', tuple(sorted(quantities)), with_H, fp64)
+    ck = ('XF', tuple(sorted(quantities)), with_H, prec)
     if ck not in dev._cache:
         names = dev.bases_for(keys)
         X = dev.XR(names, True)
@@ -286,42 +314,46 @@ def field_arrays(dev, quantities, with_H, fp64):
         for i, v in enumerate(dev.lattice.reshape(-1)):
             lat.L[i] = float(v)
         fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
-        XF = torch.empty((len(desc), nR, nw * nw), dtype=torch.complex128 if fp64 else torch.complex64,
-                         device=dev.device)
+        XF = _complex_tensor((len(desc), nR, nw * nw), prec, dev.device)
         st = _lib.load().wbg_r2k_fields(_ptr(X), len(names), _ptr(dev.geom_tensors()['iR']), nR, nw, _ptr(fd),
-                                        len(desc), _ptr(dev.wcc_tensor(True)), ctypes.byref(lat), int(fp64), _ptr(XF),
+                                        len(desc), _ptr(dev.wcc_tensor(True)), ctypes.byref(lat), prec, _ptr(XF),
                                         _stream())
         _lib.check(st, "wbg_r2k_fields")
         dev._cache[ck] = (XF, index, len(desc), fd)
     return dev._cache[ck]
 
 
-def r2k(dev, dKs, NKFFT, quantities, with_H, fp64, out=None, workspace=None):
-    """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive)."""
+def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None):
+    """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive).
+    prec: False/True (FP32/FP64) or PREC_DF64 (double-float, complex128-sized slots)."""
+    prec = _prec(prec)
     NKFFT = [int(n) for n in NKFFT]
-    XF, index, nF, _ = field_arrays(dev, quantities, with_H, fp64)
+    XF, index, nF, _ = field_arrays(dev, quantities, with_H, prec)
     nb = len(dKs)
     nw = dev.nw
     nk = int(np.prod(NKFFT))
     geo = r2k_geometry(dev, NKFFT)
     lib = _lib.load()
     ws = ctypes.c_size_t(0)
-    _lib.check(lib.wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, int(fp64), ctypes.byref(ws)),
+    _lib.check(lib.wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(ws)),
                "wbg_r2k_workspace_size")
-    cdt = torch.complex128 if fp64 else torch.complex64
     if workspace is None or workspace.numel() < ws.value:
         workspace = torch.empty(int(ws.value), dtype=torch.uint8, device=dev.device)
     if out is None:
-        out = torch.empty((nb * nk, nF, nw, nw), dtype=cdt, device=dev.device)
+        out = _complex_tensor((nb * nk, nF, nw, nw), prec, dev.device)
     ph = []
     for p in dev.geom.phases(dKs, NKFFT):  # page-locked staging so the upload does not stall the host
-        host = torch.from_numpy(p.astype(np.complex128 if fp64 else np.complex64)).pin_memory()
+        if prec == PREC_DF64:
+            host = torch.from_numpy(_df64_pairs(p)).pin_memory()
+        else:
+            host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64)).pin_memory()
         ph.append(host.to(dev.device, non_blocking=True))
         ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
-    st = _timed('r2k_fp64' if fp64 else 'r2k_fp32', lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
+    name = {PREC_FP32: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
+    st = _timed(name, lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
                 _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']), _ptr(gt['slice_r0']),
-                _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, int(fp64), _ptr(workspace),
+                _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, prec, _ptr(workspace),
                 ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
     _lib.check(st, "wbg_r2k")
     return out, index, nF, (ph, workspace)
@@ -379,9 +411,9 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
         E, U, flag = eigh(fields, nF * nw * nw, nw, nb * nk)
         fp64_fields = True
     elif precision == 'mixed':
-        Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, True)
+        Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, PREC_DF64)
         keep.append(k0)
-        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, mode=2)
+        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, mode=3)
         del Hf
         fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, False, False)
         keep.append(k1)
