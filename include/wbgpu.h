@@ -120,7 +120,9 @@ int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, d
 
 /* ---- stage 3: U^dagger X U ----------------------------------------------------------------
  * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.
- * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U, Hermitian part if herm[f]. */
+ * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U; herm[f] = 1: its Hermitian part;
+ * herm[f] = 2: at least the diagonal of the Hermitian part (real) is written -- for fields
+ * whose consumers read the diagonal only (rotA in Omega / Morb_Hpm). */
 int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);
 

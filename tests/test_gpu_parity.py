@@ -204,3 +204,16 @@ def test_golden_random_morb_and_opt(golden_dir):
     assert np.max(np.abs(res['Morb'].data - m)) < 1e-8 * np.max(np.abs(m))
     oc = ref['opt_conductivity_data']
     assert np.max(np.abs(res['opt'].data - oc)) < 1e-5 * np.max(np.abs(oc))
+
+
+def test_ahc_morb_bcd_together(c2small):
+    """Calculators sharing one band-data pass: BCD needs the full rotated rotA, AHC/Morb only its diagonal."""
+    s, o = c2small
+    EF = np.linspace(-2, 2, 61)
+    C = wbgpu.calculators
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=4), {'ahc': C.AHC(Efermi=EF), 'morb': C.Morb(Efermi=EF),
+                                                        'bcd': C.BerryDipole_FermiSea(Efermi=EF)}, precision='mixed')
+    ref = O.run(o, (2, 2, 2), (4, 4, 4), {'ahc': O.AHC(Efermi=EF), 'morb': O.Morb(Efermi=EF),
+                                          'bcd': O.BerryDipole_FermiSea(Efermi=EF)})
+    for key in ('ahc', 'morb', 'bcd'):
+        assert maxrel(res[key].data, ref[key].data) < 1e-5, key

@@ -119,6 +119,17 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
 #pragma unroll
       for (int b = 0; b < 4; ++b) Ts[(m0 + a) * nw + n0 + b] = acc[a][b];
     __syncthreads();
+    const int hmode = herm[f];
+    if (hmode == 2) {  // diagonal only: Y_mm = sum_j conj(U_jm) T_jm, Hermitian part = Re
+      V* dstd = Xbar + (k * nFrot + f) * (long long)nw2;
+      for (int m = tid; m < nw; m += tpk) {
+        V y = czero<V>();
+        for (int j = 0; j < nw; ++j) cfmac(y, Us[j * nw + m], Ts[j * nw + m]);
+        if (valid) dstd[m * nw + m] = mkc<T>(y.x, (T)0);
+      }
+      __syncthreads();
+      continue;
+    }
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -140,7 +151,7 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
       for (int b = 0; b < 4; ++b) Xs[(m0 + a) * ldx + n0 + b] = acc[a][b];
     __syncthreads();
     V* dst = Xbar + (k * nFrot + f) * (long long)nw2;
-    const bool h = herm[f] != 0;
+    const bool h = hmode != 0;
     if (valid) {
       for (int i = tid; i < nw2; i += tpk) {
         const int m = i / nw, n = i % nw;
@@ -751,6 +762,8 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
   }
   const size_t sm = 3 * (size_t)nw * nw * sizeof(V);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  // rotate_kernel writes every element (treats herm == 2 like 1): the full Hermitian part is a
+  // valid superset of the diagonal-only request
   cudaFuncSetAttribute(rotate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   rotate_kernel<T><<<nk, 256, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm, nFrot, (V*)Xbar, nw);
   return wbg_cuda_status(cudaGetLastError());

@@ -78,13 +78,13 @@ class AHC(StaticCalculator):
         super().__init__(constant_factor=constant_factor, **kwargs)
 
     def quantities(self, system):
-        return {'V', 'A', 'O'} if self.external(system) else {'V'}
+        return {'V', 'A', 'Od'} if self.external(system) else {'V'}
 
     def accumulate(self, bd, system):
         ext = self.external(system)
         sc = self.scan_struct()
         iA = bd.index.get('A', 0)
-        iO = bd.index.get('O', 0)
+        iO = bd.index.get('Od', 0)
         st = engine._timed('berry_omega', _lib.load().wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], bd.index['V'], iA, iO, bd.nw,
                                          bd.nk_total, ctypes.byref(sc), int(self.internal_terms), int(ext),
                                          _ptr(self._hist), int(bd.fp64_fields), _stream())
@@ -102,7 +102,7 @@ class Morb(StaticCalculator):
         super().__init__(constant_factor=constant_factor, **kwargs)
 
     def quantities(self, system):
-        return {'V', 'A', 'O', 'B', 'C'} if self.external(system) else {'V'}
+        return {'V', 'A', 'Od', 'B', 'C'} if self.external(system) else {'V'}
 
     def reset(self, device):
         super().reset(device)
@@ -114,11 +114,11 @@ class Morb(StaticCalculator):
         lib = _lib.load()
         g = lambda q: bd.index.get(q, 0)
         st = engine._timed('berry_morb', lib.wbg_berry_morb, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], g('V'),
-                           g('A'), g('O'), g('B'), g('C'), bd.nw, bd.nk_total, ctypes.byref(sc),
+                           g('A'), g('Od'), g('B'), g('C'), bd.nw, bd.nk_total, ctypes.byref(sc),
                            int(self.internal_terms), int(ext), _ptr(self._hist), int(bd.fp64_fields), _stream())
         _lib.check(st, "wbg_berry_morb")
         st = engine._timed('berry_omega', lib.wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1],
-                           g('V'), g('A'), g('O'), bd.nw, bd.nk_total, ctypes.byref(sc), int(self.internal_terms),
+                           g('V'), g('A'), g('Od'), bd.nw, bd.nk_total, ctypes.byref(sc), int(self.internal_terms),
                            int(ext), _ptr(self._hist_omega), int(bd.fp64_fields), _stream())
         _lib.check(st, "wbg_berry_omega")
 

@@ -23,11 +23,12 @@ QUANTITIES = {
     'A': dict(order=0, herm=1, ncomp=3),
     'dA': dict(order=1, herm=1, ncomp=9),
     'O': dict(order=1, herm=1, ncomp=3),
+    'Od': dict(order=1, herm=2, ncomp=3),  # rotA when only its diagonal is read (Omega, Morb_Hpm)
     'dO': dict(order=2, herm=1, ncomp=9),
     'B': dict(order=0, herm=0, ncomp=3),
     'C': dict(order=0, herm=0, ncomp=3),
 }
-QUANTITY_ORDER = ['V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C']
+QUANTITY_ORDER = ['V', 'A', 'O', 'Od', 'W', 'dA', 'dO', 'B', 'C']
 MOM0, DER1, DER2, ROT, DROT = 0, 1, 2, 3, 4
 
 
@@ -219,7 +220,7 @@ def field_plan(quantities, with_H, extra_keys):
             desc += [(MOM0, base_of['AA'] + b, 0, 0) for b in range(3)]
         elif q == 'dA':
             desc += [(DER1, base_of['AA'] + b, d, 0) for b in range(3) for d in range(3)]
-        elif q == 'O':
+        elif q in ('O', 'Od'):
             desc += [(ROT, base_of['AA'], g, 0) for g in range(3)]
         elif q == 'dO':
             desc += [(DROT, base_of['AA'], g, d) for g in range(3) for d in range(3)]
@@ -232,7 +233,7 @@ def field_plan(quantities, with_H, extra_keys):
 
 def extra_keys_for(quantities):
     keys = []
-    if quantities & {'A', 'dA', 'O', 'dO'}:
+    if quantities & {'A', 'dA', 'O', 'Od', 'dO'}:
         keys.append('AA')
     if 'B' in quantities:
         keys.append('BB')
@@ -247,6 +248,7 @@ def order_for(quantities):
 
 class BandData:
     """Band-basis data of a batch of FFT blocks (the reference Data_K content).
+    ``index['O']`` (full rotA) also answers diagonal-only requests (``index['Od']``).
 
     E: (nk_tot, nw) float64; U: (nk_tot, nw, nw) complex128 (view into ``Ubuf``);
     Xbar: (nk_tot, nF, nw, nw) complex (float64 or float32 parts); index: quantity -> first field.
@@ -401,6 +403,8 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
     'mixed': H(k) and eigh in FP64, the other fields and the rotation in FP32."""
     require_cuda()
     quantities = set(quantities)
+    if 'O' in quantities:
+        quantities.discard('Od')  # a full rotation also serves diagonal-only readers
     nw = dev.nw
     nk = int(np.prod(NKFFT))
     nb = len(dKs)
@@ -432,6 +436,8 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
         keep.append(k2)
     else:
         Xbar = None
+    if 'O' in bindex:
+        bindex['Od'] = bindex['O']
     bd = BandData(E, U, Xbar, bindex, nb, nk, nw, fp64_fields)
     bd._keep = keep
     bd._flag = flag
