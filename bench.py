@@ -263,22 +263,28 @@ def run_gpu(args):
     grid = wbgpu.Grid(s, NKdiv=NKDIV, NKFFT=args.nkfft)
     nblocks = grid.nblocks
     shifts = grid.block_shifts()
-    mine = np.arange(rank, nblocks, world)
+    # contiguous shard of the division grid per rank (blocks are independent: weak scaling)
+    per = nblocks // world
+    mine = np.arange(rank * per, (rank + 1) * per)
     B = args.blocks_per_step
     nk = grid.nk_per_block
     EF = np.linspace(-2, 2, NEF)
 
     def step_blocks(i):
-        idx = [(i * B + j) % len(mine) for j in range(B)]
-        return mine[idx]
+        start = (i * B) % (len(mine) - B + 1)
+        return mine[start:start + B]
 
     dev = engine.DeviceSystem(s)
     calc = AHC(Efermi=EF)
     quantities = calc.quantities(s)
     calc.reset(dev.device)
+    phases = {p: dev.grid_phases(shifts, grid.FFT, p)
+              for p in (engine.PREC_FP64, engine.PREC_DF64, engine.PREC_FP32)}
 
     def step(i, precision, c=calc):
-        bd = engine.band_data(dev, shifts[step_blocks(i)], grid.FFT, quantities, precision)
+        blocks = step_blocks(i)
+        bd = engine.band_data(dev, shifts[blocks], grid.FFT, quantities, precision, phases=phases,
+                              block_start=int(blocks[0]))
         c.accumulate(bd, s)
         return bd
 

@@ -188,6 +188,33 @@ class DeviceSystem:
                                        pair_r1=mk(g.pair_r1), slice_r0=mk(g.slice_r0), iR=mk(g.R))
         return self._cache['geom']
 
+    def buffer(self, name, shape, dtype):
+        """Persistent device buffer reused by every batch (grow-only), viewed as `dtype[shape]`:
+        keeps GB-sized per-batch allocations out of the caching allocator's way."""
+        nbytes = int(np.prod(shape)) * torch.empty((), dtype=dtype).element_size()
+        key = ('buf', name)
+        buf = self._cache.get(key)
+        if buf is None or buf.numel() < nbytes:
+            self._cache.pop(key, None)
+            buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+            self._cache[key] = buf
+        return buf[:nbytes].view(dtype).view(shape)
+
+    def grid_phases(self, shifts, NKFFT, prec):
+        """Device-resident per-axis phase tables for every block of a grid (built once per grid)."""
+        shifts = np.ascontiguousarray(shifts, dtype=np.float64)
+        key = ('phases', tuple(int(n) for n in NKFFT), int(prec), hash(shifts.tobytes()), shifts.shape)
+        if key not in self._cache:
+            tabs = []
+            for p in self.geom.phases(shifts, NKFFT):
+                if prec == PREC_DF64:
+                    host = torch.from_numpy(_df64_pairs(p))
+                else:
+                    host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64))
+                tabs.append(host.to(self.device))
+            self._cache[key] = tabs
+        return self._cache[key]
+
     def wcc_tensor(self, fp64):
         k = ('wcc', fp64)
         if k not in self._cache:
@@ -325,9 +352,10 @@ def field_arrays(dev, quantities, with_H, prec):
     return dev._cache[ck]
 
 
-def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None):
+def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, phases=None, block_start=0):
     """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive).
-    prec: False/True (FP32/FP64) or PREC_DF64 (double-float, complex128-sized slots)."""
+    prec: False/True (FP32/FP64) or PREC_DF64 (double-float, complex128-sized slots).
+    phases: optional device tables from DeviceSystem.grid_phases (then block_start indexes them)."""
     prec = _prec(prec)
     NKFFT = [int(n) for n in NKFFT]
     XF, index, nF, _ = field_arrays(dev, quantities, with_H, prec)
@@ -344,13 +372,18 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None):
     if out is None:
         out = _complex_tensor((nb * nk, nF, nw, nw), prec, dev.device)
     ph = []
-    for p in dev.geom.phases(dKs, NKFFT):  # page-locked staging so the upload does not stall the host
-        if prec == PREC_DF64:
-            host = torch.from_numpy(_df64_pairs(p)).pin_memory()
-        else:
-            host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64)).pin_memory()
-        ph.append(host.to(dev.device, non_blocking=True))
-        ph.append(host)  # keep the staging buffer alive until the copy has run
+    if phases is not None:
+        for t in phases:
+            sub = t[block_start:block_start + nb]
+            ph += [sub, sub]
+    else:
+        for p in dev.geom.phases(dKs, NKFFT):  # page-locked staging so the upload does not stall the host
+            if prec == PREC_DF64:
+                host = torch.from_numpy(_df64_pairs(p)).pin_memory()
+            else:
+                host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64)).pin_memory()
+            ph.append(host.to(dev.device, non_blocking=True))
+            ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
     name = {PREC_FP32: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
     st = _timed(name, lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
@@ -361,7 +394,7 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None):
     return out, index, nF, (ph, workspace)
 
 
-def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1):
+def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1, work=None, flag=None):
     """Batched eigensolver (wbg_eigh_batched).  mode 1: FP64 throughout, U complex128;
     mode 0: FP64 solve, FP32 back-transform; mode 2: double-float solve, FP32 back-transform
     (U complex64 in modes 0 and 2)."""
@@ -369,12 +402,14 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1):
     dev = Hfields.device
     ws = ctypes.c_size_t(0)
     _lib.check(lib.wbg_eigh_workspace_size(nw, nk, ctypes.byref(ws)), "wbg_eigh_workspace_size")
-    work = torch.empty(int(ws.value), dtype=torch.uint8, device=dev)
+    if work is None or work.numel() < ws.value:
+        work = torch.empty(int(ws.value), dtype=torch.uint8, device=dev)
     if E is None:
         E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
     if U is None:
         U = torch.empty((nk, nw, nw), dtype=torch.complex128 if mode == 1 else torch.complex64, device=dev)
-    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    if flag is None:
+        flag = torch.zeros(1, dtype=torch.int32, device=dev)
     st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw,
                 int(mode), _ptr(work), ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
     _lib.check(st, "wbg_eigh_batched")
@@ -398,28 +433,53 @@ def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
     return out, (s, h)
 
 
-def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
+def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_start=0):
     """Stages 1-3 for a batch of blocks.  precision 'fp64': everything in FP64;
-    'mixed': H(k) and eigh in FP64, the other fields and the rotation in FP32."""
+    'mixed': H(k) transform and eigh in double-float, the other fields and the rotation in FP32.
+    All per-batch arrays live in persistent buffers of `dev` (reused by the next call: consume
+    the returned BandData before calling again).  `phases` maps a precision code to the tables
+    of DeviceSystem.grid_phases; `block_start` is the index of dKs[0] in that grid."""
     require_cuda()
     quantities = set(quantities)
     if 'O' in quantities:
         quantities.discard('Od')  # a full rotation also serves diagonal-only readers
     nw = dev.nw
+    NKFFT = [int(n) for n in NKFFT]
     nk = int(np.prod(NKFFT))
     nb = len(dKs)
+    nkt = nb * nk
     keep = []
+    ph = (lambda p: None if phases is None else phases.get(p))
+    flag = dev.buffer('flag', (1,), torch.int32)
+    flag.zero_()
+
+    def fields_for(q, with_H, prec, name):
+        _, _, nF, _ = field_arrays(dev, q, with_H, prec)
+        out = dev.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec == PREC_FP32 else torch.complex128)
+        geo = r2k_geometry(dev, NKFFT)
+        ws = ctypes.c_size_t(0)
+        _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(ws)),
+                   "wbg_r2k_workspace_size")
+        work = dev.buffer('r2k_ws', (int(ws.value),), torch.uint8)
+        return r2k(dev, dKs, NKFFT, q, with_H, prec, out=out, workspace=work, phases=ph(prec),
+                   block_start=block_start)
+
+    E = dev.buffer('E', (nkt, nw), torch.float64)
+    ews = ctypes.c_size_t(0)
+    _lib.check(_lib.load().wbg_eigh_workspace_size(nw, nkt, ctypes.byref(ews)), "wbg_eigh_workspace_size")
+    ework = dev.buffer('eigh_ws', (int(ews.value),), torch.uint8)
     if precision == 'fp64':
-        fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, True, True)
+        fields, index, nF, k1 = fields_for(quantities, True, PREC_FP64, 'fields')
         keep.append(k1)
-        E, U, flag = eigh(fields, nF * nw * nw, nw, nb * nk)
+        U = dev.buffer('U', (nkt, nw, nw), torch.complex128)
+        E, U, flag = eigh(fields, nF * nw * nw, nw, nkt, E=E, U=U, mode=1, work=ework, flag=flag)
         fp64_fields = True
     elif precision == 'mixed':
-        Hf, _, _, k0 = r2k(dev, dKs, NKFFT, set(), True, PREC_DF64)
+        Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H')
         keep.append(k0)
-        E, U, flag = eigh(Hf, nw * nw, nw, nb * nk, mode=3)
-        del Hf
-        fields, index, nF, k1 = r2k(dev, dKs, NKFFT, quantities, False, False)
+        U = dev.buffer('U32', (nkt, nw, nw), torch.complex64)
+        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3, work=ework, flag=flag)
+        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32, 'fields')
         keep.append(k1)
         fp64_fields = False
     else:
@@ -432,7 +492,8 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64'):
             sel += list(range(index[q], index[q] + n))
             herm += [QUANTITIES[q]['herm']] * n
     if sel:
-        Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nb * nk, fp64_fields)
+        Xb = dev.buffer('Xbar', (nkt, len(sel), nw, nw), torch.complex128 if fp64_fields else torch.complex64)
+        Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nkt, fp64_fields, out=Xb)
         keep.append(k2)
     else:
         Xbar = None

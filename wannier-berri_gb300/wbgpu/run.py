@@ -39,8 +39,11 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
         shifts = shifts[np.asarray(blocks)]
     nk = grid.nk_per_block
     nb = blocks_per_batch or choose_batch(dev.nw, nk, len(shifts), quantities, precision)
+    precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32]
+    phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
     for i0 in range(0, len(shifts), nb):
-        bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision)
+        bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
+                              block_start=i0)
         for c in calculators.values():
             c.accumulate(bd, system)
         engine.check_flag(bd)
