@@ -49,38 +49,53 @@ WBG_D typename C2<R>::t herm_avg(cdf a, cdf b) {
   return r;
 }
 
+// Rounding of a solver real into the back-transform precision.  df64 -> float adds the two
+// halves on the FP32 pipe (|lo| <= ulp(hi)/2, so hi + lo is the correctly rounded float up
+// to a tie); no value passes through the FP64 pipe.
+template <typename TU> WBG_D TU to_tu(double x);
+template <> WBG_D double to_tu<double>(double x) { return x; }
+template <> WBG_D float to_tu<float>(double x) { return (float)x; }
+template <typename TU> WBG_D TU to_tu(df64 x);
+template <> WBG_D float to_tu<float>(df64 x) { return x.hi + x.lo; }
+template <typename TU, typename CR> WBG_D typename C2<TU>::t to_tu_c(CR a) {
+  return mkc<TU>(to_tu<TU>(a.x), to_tu<TU>(a.y));
+}
+
 // ---------------------------------------------------------------------------------------
 // 1. Householder tridiagonalisation.  grid: ceil(nk/G) blocks of G*L threads.
-// Only the lower triangle of the Hermitian matrix is kept up to date (row stride n+1 avoids
-// shared-memory bank conflicts).  Lane l of a group owns the mirrored row pairs
+// Only the lower triangle of the Hermitian matrix is kept, packed row by row
+// (element (i, j <= i) at i(i+1)/2 + j): half the shared memory of a full matrix, so twice
+// the matrices per SM.  Lane l of a group owns the mirrored row pairs
 // (2Lt + l, 2Lt + 2L-1-l), so the triangular rank-2 update is balanced across lanes;
 // L = max(4, pow2ceil(n)/2), i.e. two matrices share a warp for 16 < n <= 32.
-// Outputs (real type R): Vh[k][c][i] (v of reflector c, v_{c+1}=1, zeros for i<=c),
-// tau[k][c], d[k][i], e[k][i] (e[n-1] = 0).
+// Outputs: d[k][i], e[k][i] (e[n-1] = 0) in the solver type R; Vh[k][c][i] (v of reflector
+// c, v_{c+1}=1, zeros for i<=c) and tau[k][c] rounded to the back-transform type TV.
 // ---------------------------------------------------------------------------------------
 WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
+WBG_D int tri(int i) { return (i * (i + 1)) >> 1; }  // start of packed row i
 
-template <typename R, typename HIn>
+template <typename R, typename HIn, typename TV>
 __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n, int nk, int L, int G,
-                             typename C2<R>::t* __restrict__ Vh, typename C2<R>::t* __restrict__ tauOut,
+                             typename C2<TV>::t* __restrict__ Vh, typename C2<TV>::t* __restrict__ tauOut,
                              R* __restrict__ dOut, R* __restrict__ eOut) {
   typedef typename C2<R>::t CR;
+  typedef typename C2<TV>::t CV;
   typedef Arith<R> A;
   extern __shared__ unsigned char smt[];
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   long long k = (long long)blockIdx.x * G + grp;
   const bool valid = k < nk;
   if (!valid) k = nk - 1;  // redundant work keeps every lane of the warp in the same control flow
-  const int ld = n + 1;
-  CR* Am = reinterpret_cast<CR*>(smt) + (size_t)grp * (n * ld + 2 * n);
-  CR* vs = Am + n * ld;
+  const int ntri = tri(n);
+  CR* Am = reinterpret_cast<CR*>(smt) + (size_t)grp * (ntri + 2 * n);
+  CR* vs = Am + ntri;
   CR* ws = vs + n;
   const HIn* Hk = H + k * strideK;
   for (int idx = lane; idx < n * n; idx += L) {
     const int i = idx / n, j = idx % n;
-    if (j <= i) Am[i * ld + j] = herm_avg<R>(Hk[i * n + j], Hk[j * n + i]);
+    if (j <= i) Am[tri(i) + j] = herm_avg<R>(Hk[i * n + j], Hk[j * n + i]);
   }
   __syncwarp();
   const R zero = A::from(0.0), one = A::from(1.0), mhalf = A::from(-0.5);
@@ -90,10 +105,10 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
     for (int t = 0; t < T; ++t)
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
-        if (i < n && i >= c + 2) { const CR x = Am[i * ld + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
+        if (i < n && i >= c + 2) { const CR x = Am[tri(i) + c]; xn = fma(x.x, x.x, fma(x.y, x.y, xn)); }
       }
     xn = group_sum(xn, L);
-    const CR alpha = Am[(c + 1) * ld + c];
+    const CR alpha = Am[tri(c + 1) + c];
     R beta, tr = zero, ti = zero;
     CR scale = czero<CR>();
     if (xn == zero && alpha.y == zero) {
@@ -119,8 +134,8 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n) {
-          if (i == c + 1) { CR v1; v1.x = one; v1.y = zero; vs[i] = v1; Am[i * ld + c] = v1; }
-          else if (i >= c + 2) { const CR v = cmul(Am[i * ld + c], scale); vs[i] = v; Am[i * ld + c] = v; }
+          if (i == c + 1) { CR v1; v1.x = one; v1.y = zero; vs[i] = v1; Am[tri(i) + c] = v1; }
+          else if (i >= c + 2) { const CR v = cmul(Am[tri(i) + c], scale); vs[i] = v; Am[tri(i) + c] = v; }
         }
       }
     __syncwarp();
@@ -131,8 +146,9 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
           CR acc = czero<CR>();
-          for (int j = c + 1; j <= i; ++j) cfma(acc, Am[i * ld + j], vs[j]);
-          for (int j = i + 1; j < n; ++j) cfmac(acc, Am[j * ld + i], vs[j]);
+          const CR* Ai = Am + tri(i);
+          for (int j = c + 1; j <= i; ++j) cfma(acc, Ai[j], vs[j]);
+          for (int j = i + 1; j < n; ++j) cfmac(acc, Am[tri(j) + i], vs[j]);
           const CR p = cmul(tau, acc);
           ws[i] = p;
           const CR v = vs[i];
@@ -159,8 +175,9 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
           const CR vi = vs[i], wi = ws[i];
+          CR* Ai = Am + tri(i);
           for (int j = c + 1; j <= i; ++j) {
-            CR a = Am[i * ld + j];
+            CR a = Ai[j];
             const CR vj = vs[j], wj = ws[j];
             a.x = fma(-vi.x, wj.x, a.x);
             a.x = fma(-vi.y, wj.y, a.x);
@@ -170,29 +187,30 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
             a.y = fma(vi.x, wj.y, a.y);
             a.y = fma(-wi.y, vj.x, a.y);
             a.y = fma(wi.x, vj.y, a.y);
-            Am[i * ld + j] = a;
+            Ai[j] = a;
           }
         }
       }
     __syncwarp();
     if (valid) {
       const bool refl = (tr != zero || ti != zero);
-      for (int i = lane; i < n; i += L) Vh[(k * n + c) * n + i] = (refl && i >= c + 1) ? Am[i * ld + c] : czero<CR>();
+      for (int i = lane; i < n; i += L)
+        Vh[(k * n + c) * n + i] = (refl && i >= c + 1) ? to_tu_c<TV>(Am[tri(i) + c]) : czero<CV>();
       if (lane == 0) {
-        tauOut[k * n + c] = tau;
+        tauOut[k * n + c] = to_tu_c<TV>(tau);
         eOut[k * n + c] = beta;
-        dOut[k * n + c] = Am[c * ld + c].x;
+        dOut[k * n + c] = Am[tri(c) + c].x;
       }
     }
     __syncwarp();
   }
   if (valid && lane == 0) {
-    dOut[k * n + n - 1] = Am[(n - 1) * ld + n - 1].x;
+    dOut[k * n + n - 1] = Am[tri(n - 1) + n - 1].x;
     eOut[k * n + n - 1] = zero;
-    tauOut[k * n + n - 1] = czero<CR>();
+    tauOut[k * n + n - 1] = czero<CV>();
   }
   if (valid)
-    for (int i = lane; i < n; i += L) Vh[(k * n + n - 1) * n + i] = czero<CR>();
+    for (int i = lane; i < n; i += L) Vh[(k * n + n - 1) * n + i] = czero<CV>();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -267,15 +285,21 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 // ---------------------------------------------------------------------------------------
 // 3. Eigenvectors: inverse iteration on T (real type R), clusters re-orthogonalised, U = Q Z.
 // grid: ceil(nk/G) blocks of G*L threads; lane j computes eigenvectors j, j+L, ...
-// The back-transform by the Householder reflectors runs in precision TU.  Shared memory
-// per group: Z [n][n], d, e, lam [n] (type R), then U[n][n] complex(TU).
+// The back-transform by the Householder reflectors runs in precision TU, one reflector at a
+// time staged in shared memory for all lanes.  Shared memory per group: Z [n][n], d, e,
+// lam [n] (type R), then U[n][n] and the staged reflector [n], complex(TU).  The iterate of
+// lane j lives in column j of Z.  When complex(TU) and R have the same size (df64 solve,
+// float vectors) U overlays Z: element (i, j) is converted in place by the lane that owns
+// column j, so the group needs half the shared memory.
 // ---------------------------------------------------------------------------------------
 template <typename R, typename TU>
-__global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typename C2<R>::t* __restrict__ tauIn,
+constexpr bool kUOverlaysZ = sizeof(typename C2<TU>::t) == sizeof(R);
+
+template <typename R, typename TU>
+__global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const typename C2<TU>::t* __restrict__ tauIn,
                              const R* __restrict__ dIn, const R* __restrict__ eIn, const double* __restrict__ E, int n,
                              int nk, int L, int G, typename C2<TU>::t* __restrict__ Uout, long long strideU) {
   typedef typename C2<TU>::t VU;
-  typedef typename C2<R>::t CR;
   typedef Arith<R> A;
   extern __shared__ unsigned char smv[];
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
@@ -283,13 +307,15 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
   const bool valid = k < nk;
   if (!valid) k = nk - 1;
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
-  const size_t ubytes = ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
-  unsigned char* gbase = smv + (size_t)grp * (zbytes + ubytes);
+  const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
+  const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
+  unsigned char* gbase = smv + (size_t)grp * (zbytes + ubytes + vbytes);
   R* Zs = reinterpret_cast<R*>(gbase);  // Z(i,j) = Zs[i*n + j]
   R* ds = Zs + n * n;
   R* es = ds + n;
   R* lam = es + n;
-  VU* Us = reinterpret_cast<VU*>(gbase + zbytes);  // [i][j]
+  VU* Us = kUOverlaysZ<R, TU> ? reinterpret_cast<VU*>(gbase) : reinterpret_cast<VU*>(gbase + zbytes);  // [i][j]
+  VU* vsh = reinterpret_cast<VU*>(gbase + zbytes + ubytes);
   for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = A::from(E[k * n + i]); }
   __syncwarp();
   const R zero = A::from(0.0), one = A::from(1.0);
@@ -299,7 +325,7 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
   const R tiny = A::pivot_floor() * tnorm;
   const R ortol = A::from(1e-5) * tnorm;
   const R pertol = A::from(10.0) * A::eps() * tnorm;
-  R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX], x[WBG_EIGH_NMAX];
+  R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX];
   unsigned char piv[WBG_EIGH_NMAX];
   for (int j = lane; j < n; j += L) {
     R shift = lam[j];
@@ -325,27 +351,32 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
     }
     if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
     u0i[n - 1] = one / ca;
-    for (int i = 0; i < n; ++i) x[i] = A::from(hash_uniform((unsigned)j + 1u, (unsigned)i + 7u));
+    R* x = Zs + j;  // x[i * n]: column j of Z
+    for (int i = 0; i < n; ++i) x[i * n] = A::from(hash_uniform((unsigned)j + 1u, (unsigned)i + 7u));
     for (int it = 0; it < 3; ++it) {
       R rp = x[0];
       for (int i = 0; i < n - 1; ++i) {
-        const R y1 = x[i + 1];
-        if (piv[i] == 0) { x[i] = rp; rp = y1 - lm[i] * rp; }
-        else { x[i] = y1; rp = rp - lm[i] * y1; }
+        const R y1 = x[(i + 1) * n];
+        if (piv[i] == 0) { x[i * n] = rp; rp = y1 - lm[i] * rp; }
+        else { x[i * n] = y1; rp = rp - lm[i] * y1; }
       }
-      x[n - 1] = rp * u0i[n - 1];
-      if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0i[n - 2];
-      for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0i[i];
+      R xi1 = rp * u0i[n - 1], xi2 = zero;  // x[i+1], x[i+2] of the back substitution
+      x[(n - 1) * n] = xi1;
+      R amax = fabs(xi1);
+      for (int i = n - 2; i >= 0; --i) {
+        const R xi = (x[i * n] - u1[i] * xi1 - u2[i] * xi2) * u0i[i];
+        x[i * n] = xi;
+        amax = fmax(amax, fabs(xi));
+        xi2 = xi1;
+        xi1 = xi;
+      }
       // scale by the largest component before the 2-norm so squares cannot overflow
-      R amax = zero;
-      for (int i = 0; i < n; ++i) amax = fmax(amax, fabs(x[i]));
       const R ra = one / amax;
       R nrm = zero;
-      for (int i = 0; i < n; ++i) { x[i] = x[i] * ra; nrm = fma(x[i], x[i], nrm); }
+      for (int i = 0; i < n; ++i) { const R xs = x[i * n] * ra; x[i * n] = xs; nrm = fma(xs, xs, nrm); }
       nrm = rsqrt(nrm);
-      for (int i = 0; i < n; ++i) x[i] = x[i] * nrm;
+      for (int i = 0; i < n; ++i) x[i * n] = x[i * n] * nrm;
     }
-    for (int i = 0; i < n; ++i) Zs[i * n + j] = x[i];
   }
   __syncwarp();
   // modified Gram-Schmidt inside clusters (eigenvalues closer than ortol), in eigenvalue order
@@ -375,27 +406,28 @@ __global__ void eigh_vectors(const typename C2<R>::t* __restrict__ Vh, const typ
     }
   }
   // back-transform: u = H_0 H_1 ... H_{n-2} z  (precision TU)
-  for (int j = lane; j < n; j += L) {
-    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>((TU)A::to(Zs[i * n + j]), (TU)0);
-    for (int c = n - 2; c >= 0; --c) {
-      const CR tauR = tauIn[k * n + c];
-      if (tauR.x == zero && tauR.y == zero) continue;
-      const VU tau = mkc<TU>((TU)A::to(tauR.x), (TU)A::to(tauR.y));
-      const CR* v = Vh + (k * n + c) * n;
-      VU sacc = czero<VU>();
-      for (int i = c + 1; i < n; ++i) {
-        const VU vv = mkc<TU>((TU)A::to(v[i].x), (TU)A::to(v[i].y));
-        cfmac(sacc, vv, Us[i * n + j]);
+  for (int j = lane; j < n; j += L)
+    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>(to_tu<TU>(Zs[i * n + j]), (TU)0);
+  for (int c = n - 2; c >= 0; --c) {
+    // every lane passes the same __syncwarp calls: groups sharing a warp have different tau
+    const VU tau = tauIn[k * n + c];
+    const bool act = (tau.x != (TU)0 || tau.y != (TU)0);
+    for (int i = c + 1 + lane; i < n; i += L) vsh[i] = Vh[(k * n + c) * n + i];
+    __syncwarp();
+    if (act)
+      for (int j = lane; j < n; j += L) {
+        VU sacc = czero<VU>();
+        for (int i = c + 1; i < n; ++i) cfmac(sacc, vsh[i], Us[i * n + j]);
+        const VU ts = cmul(tau, sacc);
+        for (int i = c + 1; i < n; ++i) {
+          VU u = Us[i * n + j];
+          const VU vv = vsh[i];
+          u.x -= vv.x * ts.x - vv.y * ts.y;
+          u.y -= vv.x * ts.y + vv.y * ts.x;
+          Us[i * n + j] = u;
+        }
       }
-      const VU ts = cmul(tau, sacc);
-      for (int i = c + 1; i < n; ++i) {
-        VU u = Us[i * n + j];
-        const VU vv = mkc<TU>((TU)A::to(v[i].x), (TU)A::to(v[i].y));
-        u.x -= vv.x * ts.x - vv.y * ts.y;
-        u.y -= vv.x * ts.y + vv.y * ts.x;
-        Us[i * n + j] = u;
-      }
-    }
+    __syncwarp();
   }
   __syncwarp();
   if (valid)
@@ -408,33 +440,52 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
+// Shared memory of one SM (228 KB, 1 KB of it reserved per resident block) and the largest
+// dynamic allocation this file asks of one block.
+constexpr size_t kSmemPerSM = 228 * 1024, kSmemPerBlockReserved = 1024, kMaxBlockSmem = 220 * 1024;
+
+// Matrices per block for a kernel whose groups take `smem` bytes of shared memory and
+// `threads` threads each: the power of two up to gmax that keeps the most matrices resident
+// on one SM (shared memory, 2048 threads and 32 blocks per SM); 0 if one group does not fit.
+int pick_group(size_t smem, int threads, int gmax) {
+  int best = 0, bestres = 0;
+  for (int g = 1; g <= (gmax < 1 ? 1 : gmax); g *= 2) {
+    const size_t blk = (size_t)g * smem;
+    if (blk > kMaxBlockSmem) break;
+    int bps = (int)(kSmemPerSM / (blk + kSmemPerBlockReserved));
+    if (bps > 2048 / (g * threads)) bps = 2048 / (g * threads);
+    if (bps > 32) bps = 32;
+    if (bps * g >= bestres) { bestres = bps * g; best = g; }
+  }
+  return best;
+}
+
 template <typename R, typename TU, typename HIn>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, void* workspace,
                 int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
   typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
-  CR* Vh = (CR*)w; w += (size_t)nk * n * n * 16;
-  CR* tau = (CR*)w; w += (size_t)nk * n * 16;
+  VU* Vh = (VU*)w; w += (size_t)nk * n * n * 16;
+  VU* tau = (VU*)w; w += (size_t)nk * n * 16;
   R* d = (R*)w; w += (size_t)nk * n * 8;
   R* e = (R*)w;
   const int L = lanes_for(n);
   const int LT = L >= 8 ? L / 2 : 4;  // tridiagonalisation: mirrored row pairs, half the lanes
-  const size_t smT = ((size_t)n * (n + 1) + 2 * n) * sizeof(CR);
-  int G = (4 * 32) / LT;
-  while (G > 1 && G * smT > 96 * 1024) G /= 2;
-  if (G * smT > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_tridiag<R, HIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  eigh_tridiag<R, HIn><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G, Vh, tau,
-                                                                       d, e);
+  const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
+  const int G = pick_group(smT, LT, 128 / LT);
+  if (G == 0) return WBG_ERR_SIZE;
+  cudaFuncSetAttribute(eigh_tridiag<R, HIn, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
+  eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G, Vh,
+                                                                           tau, d, e);
   eigh_ql<R><<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
-  const size_t ubytes = ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
-  const size_t smV = zbytes + ubytes;
-  int GV = (2 * 32) / L;
-  while (GV > 1 && GV * smV > 96 * 1024) GV /= 2;
-  if (GV * smV > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
+  const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
+  const size_t smV = zbytes + ubytes + vbytes;
+  const int GV = pick_group(smV, L, 64 / L);
+  if (GV == 0) return WBG_ERR_SIZE;
+  cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_vectors<R, TU><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
                                                                         (VU*)U, strideU);
   return wbg_cuda_status(cudaGetLastError());
