@@ -86,6 +86,17 @@ int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, c
             const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, int nblocks,
             int prec, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,
             void* stream);
+/* wbg_r2k restricted to a list of elements: cols[c] = f*nw*nw + m*nw + n (0 <= c < ncols).
+ * Only those elements of fields_out are written.  The mixed-precision path asks for the
+ * lower triangle (m >= n) of the Hermitian fields and lets each consumer mirror the upper
+ * triangle, so the fields are exactly Hermitian and the transform costs half.  H, AA and rotAA
+ * are symmetrised as 1/2 (X + X^dagger) by the reference too (fourier/fft.py:183-186,
+ * data_K/data_K_R.py:26,87); the derivatives of H are Hermitian analytically, so for them the
+ * mirror removes only rounding noise. */
+int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, const int* pair_start, const int* r2,
+                    const int* slice_start, const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1,
+                    const void* ph2, int nblocks, int prec, void* workspace, size_t workspace_bytes, void* fields_out,
+                    const wbg_r2k_geom* g, void* stream);
 
 /* ---- stage 2: batched Hermitian eigensolver ---------------------------------------------
  * H: matrix k at H + k*strideH (complex128 elements), symmetrised as 1/2 (H + H^dagger).
@@ -97,8 +108,12 @@ int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, c
  *         U complex64;
  * mode 3: as mode 2 with H given as double-float complex (wbg_r2k prec 2 output; the
  *         mixed-precision path).
+ * mode | 4 (WBG_EIGH_LOWER): only the lower triangle (m >= n) of H is read and taken as the
+ *         Hermitian matrix (imaginary part of the diagonal ignored) -- the output of
+ *         wbg_r2k_columns on the lower triangle.
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
+#define WBG_EIGH_LOWER 4
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
@@ -122,7 +137,9 @@ int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, d
  * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.
  * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U; herm[f] = 1: its Hermitian part;
  * herm[f] = 2: at least the diagonal of the Hermitian part (real) is written -- for fields
- * whose consumers read the diagonal only (rotA in Omega / Morb_Hpm). */
+ * whose consumers read the diagonal only (rotA in Omega / Morb_Hpm).
+ * herm[f] | 4: X[fsel[f]] holds only its lower triangle (wbg_r2k_columns output); it is read
+ * as the Hermitian matrix with that lower triangle and a real diagonal. */
 int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);
 

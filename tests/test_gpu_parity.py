@@ -73,6 +73,87 @@ def test_r2k_double_float_hamiltonian(c2small):
     assert maxrel(got[:, 0], ref) < 1e-13
 
 
+@pytest.mark.parametrize("prec", [engine.PREC_FP32, engine.PREC_FP64, engine.PREC_DF64])
+def test_r2k_columns_lower_triangle(c2small, prec):
+    """wbg_r2k_columns on the lower triangle of the Hermitian fields: those elements are
+    bit-identical to the full transform, the others (upper triangles) are left unwritten."""
+    s, _ = c2small
+    dev = engine.DeviceSystem(s)
+    NKFFT = (4, 3, 5)
+    dKs = np.array([[0.13, -0.21, 0.37], [0.3, 0.1, -0.2]]) / np.array(NKFFT)
+    q = {'V', 'A', 'O', 'B', 'C'}
+    full, index, nF, _ = engine.r2k(dev, dKs, NKFFT, q, True, prec)
+    full = full.clone()
+    out = torch.empty_like(full)
+    out.view(torch.float32).fill_(float('nan'))  # both parts (a complex fill leaves imag at 0)
+    low, _, _, _ = engine.r2k(dev, dKs, NKFFT, q, True, prec, out=out, lower=True)
+    cols, lower = engine.column_list(dev, q, True, True)
+    nw = s.num_wann
+    a = full.view(torch.int32).reshape(full.shape[0], nF * nw * nw, -1).cpu().numpy()  # raw bits
+    b = low.view(torch.int32).reshape(full.shape[0], nF * nw * nw, -1).cpu().numpy()
+    c = cols.cpu().numpy()
+    assert np.array_equal(a[:, c], b[:, c])
+    rest = np.setdiff1d(np.arange(nF * nw * nw), c)
+    assert np.isnan(low.view(torch.float32).reshape(b.shape).cpu().numpy()[:, rest]).all()
+    # the non-Hermitian B, C fields are complete, the Hermitian ones lower-triangular
+    assert [lower[index[k]] for k in ('H', 'V', 'A', 'O', 'B', 'C')] == [True] * 4 + [False] * 2
+    assert len(c) == (nF - 6) * nw * (nw + 1) // 2 + 6 * nw * nw
+
+
+def _df64_complex(H):
+    """complex128 numpy -> torch complex128-sized double-float layout (re.hi, re.lo, im.hi, im.lo)."""
+    return torch.from_numpy(engine._df64_pairs(H)).contiguous().view(torch.complex128).reshape(H.shape)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("nw", [5, 32, 48])
+def test_eigh_lower_triangle_input(nw, mode):
+    """mode | WBG_EIGH_LOWER reads only the lower triangle: NaN above the diagonal and a
+    non-zero imaginary diagonal change nothing against the full Hermitian input."""
+    rng = np.random.default_rng(100 + nw)
+    nk = 200
+    H = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
+    H = H + H.conj().swapaxes(1, 2)
+    Hl = H.copy()
+    iu = np.triu_indices(nw, 1)
+    Hl[:, iu[0], iu[1]] = np.nan
+    Hl[:, np.arange(nw), np.arange(nw)] += 3.0j
+    conv = _df64_complex if mode == 3 else torch.from_numpy
+    E0, U0, f0 = engine.eigh(conv(H).cuda(), nw * nw, nw, nk, mode=mode)
+    E0, U0 = E0.clone(), U0.clone()
+    E1, U1, f1 = engine.eigh(conv(Hl).cuda(), nw * nw, nw, nk, mode=mode | engine.EIGH_LOWER)
+    torch.cuda.synchronize()
+    assert int(f0.item()) == 0 and int(f1.item()) == 0
+    assert torch.equal(E0, E1) and torch.equal(U0, U1)
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+@pytest.mark.parametrize("nw", [6, 32])
+def test_rotate_lower_triangle_input(fp64, nw):
+    """herm | 4: the field is read from its lower triangle (mirrored, real diagonal) -- equal
+    to rotating the full Hermitian matrix, for plain, Hermitian-part and diagonal outputs."""
+    rng = np.random.default_rng(7 + nw)
+    nk = 64
+    cdt = torch.complex128 if fp64 else torch.complex64
+    X = rng.standard_normal((nk, 3, nw, nw)) + 1j * rng.standard_normal((nk, 3, nw, nw))
+    X = X + X.conj().swapaxes(-1, -2)
+    U = np.linalg.qr(rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw)))[0]
+    Xl = X.copy()
+    iu = np.triu_indices(nw, 1)
+    Xl[..., iu[0], iu[1]] = np.nan
+    Ut = torch.from_numpy(U).to(cdt).cuda()
+    Xt = torch.from_numpy(X).to(cdt).cuda()
+    Xlt = torch.from_numpy(Xl).to(cdt).cuda()
+    sel = [0, 1, 2]
+    a, _ = engine.rotate(Ut, Xt, 3, sel, [0, 1, 2], nw, nk, fp64)
+    a = a.clone()
+    b, _ = engine.rotate(Ut, Xlt, 3, sel, [4, 5, 6], nw, nk, fp64)
+    torch.cuda.synchronize()
+    assert torch.equal(a[:, :2], b[:, :2])
+    d = torch.arange(nw, device=a.device)
+    assert torch.equal(a[:, 2, d, d].real, b[:, 2, d, d].real)
+
+
 @pytest.mark.parametrize("mode", [1, 0, 2])
 @pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
 def test_eigh_random(nw, mode):

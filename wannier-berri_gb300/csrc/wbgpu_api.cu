@@ -42,7 +42,18 @@ int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, c
       !fields_out || !g)
     return WBG_STATUS_BAD_ARGUMENT;
   return wbg_r2k_run(XF, nfields, pair_start, r2, slice_start, pair_r1, slice_r0, ph0, ph1, ph2, workspace,
-                     workspace_bytes, fields_out, g, nblocks, prec, (cudaStream_t)stream);
+                     workspace_bytes, fields_out, g, nblocks, prec, nullptr, 0, (cudaStream_t)stream);
+}
+
+int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, const int* pair_start, const int* r2,
+                    const int* slice_start, const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1,
+                    const void* ph2, int nblocks, int prec, void* workspace, size_t workspace_bytes, void* fields_out,
+                    const wbg_r2k_geom* g, void* stream) {
+  if (!XF || !cols || !pair_start || !r2 || !slice_start || !pair_r1 || !slice_r0 || !ph0 || !ph1 || !ph2 ||
+      !workspace || !fields_out || !g)
+    return WBG_STATUS_BAD_ARGUMENT;
+  return wbg_r2k_run(XF, nfields, pair_start, r2, slice_start, pair_r1, slice_r0, ph0, ph1, ph2, workspace,
+                     workspace_bytes, fields_out, g, nblocks, prec, cols, ncols, (cudaStream_t)stream);
 }
 
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes) {

@@ -14,8 +14,22 @@
 
 namespace {
 
+// Element i = m*nw + n of input field src.  lower: src holds only its lower triangle (m >= n)
+// of a Hermitian matrix; the upper triangle is the conjugate mirror, the diagonal is real.
+template <typename V>
+WBG_D V load_field(const V* src, int i, int nw, bool lower) {
+  if (!lower) return src[i];
+  const int m = i / nw, n = i % nw;
+  V v = src[m >= n ? i : n * nw + m];
+  if (m < n) v.y = -v.y;
+  if (m == n) v.y = 0;
+  return v;
+}
+
 // ---------------------------------------------------------------------------------------
 // rotation: Xbar[k][f] = U^dagger X[k][fsel[f]] U  (optionally Hermitian-symmetrised)
+// herm[f] bits 0-1: 0 plain, 1 Hermitian part, 2 diagonal (real) only; bit 2: X[fsel[f]]
+// holds only its lower triangle (wbg_r2k_columns output).
 // grid: nk blocks of 256 threads; shared: U, X, T (nw*nw each, precision T)
 // ---------------------------------------------------------------------------------------
 template <typename T>
@@ -35,7 +49,8 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
     const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
     const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw2;
     const T nan = T(0) / T(0);
-    for (int i = threadIdx.x; i < nw2; i += blockDim.x) Xs[i] = fok ? src[i] : mkc<T>(nan, nan);
+    const bool lower = (herm[f] & 4) != 0;
+    for (int i = threadIdx.x; i < nw2; i += blockDim.x) Xs[i] = fok ? load_field(src, i, nw, lower) : mkc<T>(nan, nan);
     __syncthreads();
     for (int i = threadIdx.x; i < nw2; i += blockDim.x) {  // T = X U
       const int m = i / nw, n = i % nw;
@@ -52,7 +67,7 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
     }
     __syncthreads();
     V* dst = Xbar + (k * nFrot + f) * (long long)nw2;
-    const bool h = herm[f] != 0;
+    const bool h = (herm[f] & 3) != 0;
     for (int i = threadIdx.x; i < nw2; i += blockDim.x) {
       V y = Xs[i];
       if (h) {
@@ -96,7 +111,9 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
     const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
     const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw2;
     const T nan = T(0) / T(0);
-    for (int i = tid; i < nw2; i += tpk) Xs[(i / nw) * ldx + (i % nw)] = fok ? src[i] : mkc<T>(nan, nan);
+    const bool lower = (herm[f] & 4) != 0;
+    for (int i = tid; i < nw2; i += tpk)
+      Xs[(i / nw) * ldx + (i % nw)] = fok ? load_field(src, i, nw, lower) : mkc<T>(nan, nan);
     __syncthreads();
     V acc[4][4];
 #pragma unroll
@@ -119,7 +136,7 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
 #pragma unroll
       for (int b = 0; b < 4; ++b) Ts[(m0 + a) * nw + n0 + b] = acc[a][b];
     __syncthreads();
-    const int hmode = herm[f];
+    const int hmode = herm[f] & 3;
     if (hmode == 2) {  // diagonal only: Y_mm = sum_j conj(U_jm) T_jm, Hermitian part = Re
       V* dstd = Xbar + (k * nFrot + f) * (long long)nw2;
       for (int m = tid; m < nw; m += tpk) {
@@ -185,6 +202,39 @@ template <> WBG_D double recip_gap<double>(double dE) { return 1.0 / dE; }
 // FP64 difference (no cancellation loss), FP32 reciprocal
 template <> WBG_D float recip_gap<float>(double dE) { return 1.0f / (float)dE; }
 
+// 1/(E_n - E_l), 0 below 1e-7 (degenerate pairs).  FP64 path: native doubles.  FP32 path: the
+// energies are held as double-float pairs (Eh + El = E to 48 bits); Eh_n - Eh_l is exact when
+// the two are within a factor of two, so the gap keeps FP32 relative accuracy however close
+// the bands, and nothing runs on the FP64 pipe.
+template <typename T> WBG_D T inv_gap(const double* E, const float* Eh, const float* El, int n, int l);
+template <> WBG_D double inv_gap<double>(const double* E, const float*, const float*, int n, int l) {
+  const double dE = E[n] - E[l];
+  return fabs(dE) < 1e-7 ? 0.0 : 1.0 / dE;
+}
+template <> WBG_D float inv_gap<float>(const double*, const float* Eh, const float* El, int n, int l) {
+  const float dE = (Eh[n] - Eh[l]) + (El[n] - El[l]);
+  return fabsf(dE) < 1e-7f ? 0.0f : __frcp_rn(dE);
+}
+
+// Trace accumulator: a double in the FP64 path; in the FP32 path a float sum with its
+// rounding error carried along (Knuth two-sum), ~2^-48 relative, all on the FP32 pipe.
+template <typename T> struct TraceSum;
+template <> struct TraceSum<double> {
+  double s = 0.0;
+  WBG_D void add(double x) { s += x; }
+  WBG_D double value() const { return s; }
+};
+template <> struct TraceSum<float> {
+  float s = 0.0f, c = 0.0f;
+  WBG_D void add(float x) {
+    const float t = s + x;
+    const float v = t - s;
+    c += (s - (t - v)) + (x - v);
+    s = t;
+  }
+  WBG_D double value() const { return (double)s + (double)c; }
+};
+
 // ---------------------------------------------------------------------------------------
 // Fused Omega traces + Fermi-level histogram.
 // grid: persistent blocks of G*L threads; each group of L lanes takes one k-point at a time.
@@ -200,19 +250,28 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
   double* sh = smb;                                   // [nEF][3]
   double* Es = sh + 3 * sp.nEF;                       // [G][nw]
   double* tv = Es + G * nw;                           // [G][nw][3]
-  int* start = reinterpret_cast<int*>(tv + 3 * G * nw);  // [G][nw]
+  float* Ehl = reinterpret_cast<float*>(tv + 3 * G * nw);  // [G][2][nw]: double-float energies
+  int* start = reinterpret_cast<int*>(Ehl + 2 * G * nw);   // [G][nw]
   for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
   double* myT = tv + 3 * grp * nw;
+  float* myEh = Ehl + 2 * grp * nw;
+  float* myEl = myEh + nw;
   int* myS = start + grp * nw;
   const long long nw2 = (long long)nw * nw;
   for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
     const long long k = base + grp;
     const bool valid = k < nk;
     const long long kk = valid ? k : nk - 1;
-    for (int i = lane; i < nw; i += L) myE[i] = E[kk * nw + i];
+    for (int i = lane; i < nw; i += L) {
+      const double e = E[kk * nw + i];
+      const float eh = (float)e;
+      myE[i] = e;
+      myEh[i] = eh;
+      myEl[i] = (float)(e - (double)eh);
+    }
     __syncwarp();
     for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
     __syncwarp();
@@ -238,12 +297,10 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
       else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
       double t[3] = {0.0, 0.0, 0.0};
       if (ingroup) {
-        const double En = myE[n];
-        double sr[3] = {0.0, 0.0, 0.0}, si[3] = {0.0, 0.0, 0.0};
+        TraceSum<T> sr[3];  // real part of the trace; its imaginary part is not needed
         for (int l = 0; l < nw; ++l) {
           if (l >= gs && l < ge) continue;
-          const double dE = En - myE[l];
-          const T dinv = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+          const T dinv = inv_gap<T>(myE, myEh, myEl, n, l);
           V Dnl[3], Dln[3], Aln[3];
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
@@ -258,24 +315,21 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
             if (internal_terms) acc = cmuli(cmul(Dnl[al], Dln[be]));  // i D D (sign applied below)
             V accx = czero<V>();
             if (external_terms) { cfma(accx, Dnl[be], Aln[al]); accx = csub(accx, cmul(Dnl[al], Aln[be])); }
-            // S += -i D^a_nl D^b_ln - D^a_nl A^b_ln + D^b_nl A^a_ln
-            sr[g] += (double)(-acc.x) + (double)accx.x;
-            si[g] += (double)(-acc.y) + (double)accx.y;
+            // Re S += Re[-i D^a_nl D^b_ln - D^a_nl A^b_ln + D^b_nl A^a_ln]
+            sr[g].add(accx.x - acc.x);
           }
         }
         if (external_terms) {
 #pragma unroll
           for (int g = 0; g < 3; ++g) {
             const int al = (g + 1) % 3, be = (g + 2) % 3;
-            sr[g] += 0.5 * (double)Xk[(iO + g) * nw2 + n * nw + n].x;
+            sr[g].add((T)0.5 * Xk[(iO + g) * nw2 + n * nw + n].x);
             V acc = czero<V>();
             for (int np = gs; np < ge; ++np) cfma(acc, Xk[(iA + al) * nw2 + n * nw + np], Xk[(iA + be) * nw2 + np * nw + n]);
-            // -i * acc
-            sr[g] += (double)acc.y;
-            si[g] -= (double)acc.x;
+            sr[g].add(acc.y);  // Re(-i acc)
           }
         }
-        for (int g = 0; g < 3; ++g) t[g] = 2.0 * sr[g];
+        for (int g = 0; g < 3; ++g) t[g] = 2.0 * sr[g].value();
       }
       for (int g = 0; g < 3; ++g) myT[n * 3 + g] = t[g];
     }
@@ -787,7 +841,7 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   const int L = lanes_for(nw);
   const int G = 128 / L;
-  const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * (8 + 24 + 4);
+  const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * (8 + 24 + 8 + 4);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);

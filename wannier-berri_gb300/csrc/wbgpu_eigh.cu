@@ -49,6 +49,17 @@ WBG_D typename C2<R>::t herm_avg(cdf a, cdf b) {
   return r;
 }
 
+// Element (i, j <= i) of a matrix given by its lower triangle; the diagonal is taken real.
+template <typename R>
+WBG_D typename C2<R>::t lower_elem(double2 a, bool diag) {
+  return from_c64<R>(make_double2(a.x, diag ? 0.0 : a.y));
+}
+template <typename R>
+WBG_D typename C2<R>::t lower_elem(cdf a, bool diag) {
+  if (diag) a.y = Arith<R>::from(0.0);
+  return a;
+}
+
 // Rounding of a solver real into the back-transform precision.  df64 -> float adds the two
 // halves on the FP32 pipe (|lo| <= ulp(hi)/2, so hi + lo is the correctly rounded float up
 // to a tie); no value passes through the FP64 pipe.
@@ -77,7 +88,7 @@ WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1
 WBG_D int tri(int i) { return (i * (i + 1)) >> 1; }  // start of packed row i
 
 template <typename R, typename HIn, typename TV>
-__global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n, int nk, int L, int G,
+__global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n, int nk, int L, int G, int lowerIn,
                              typename C2<TV>::t* __restrict__ Vh, typename C2<TV>::t* __restrict__ tauOut,
                              R* __restrict__ dOut, R* __restrict__ eOut) {
   typedef typename C2<R>::t CR;
@@ -95,7 +106,8 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
   const HIn* Hk = H + k * strideK;
   for (int idx = lane; idx < n * n; idx += L) {
     const int i = idx / n, j = idx % n;
-    if (j <= i) Am[tri(i) + j] = herm_avg<R>(Hk[i * n + j], Hk[j * n + i]);
+    if (j <= i)
+      Am[tri(i) + j] = lowerIn ? lower_elem<R>(Hk[i * n + j], i == j) : herm_avg<R>(Hk[i * n + j], Hk[j * n + i]);
   }
   __syncwarp();
   const R zero = A::from(0.0), one = A::from(1.0), mhalf = A::from(-0.5);
@@ -215,52 +227,59 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
 
 // ---------------------------------------------------------------------------------------
 // 2. Implicit QL eigenvalues of the real symmetric tridiagonal (d, e), thread per matrix.
+// d and e of thread t live in shared memory at [i * blockDim + t] (conflict-free, no
+// local-memory traffic).
 // ---------------------------------------------------------------------------------------
 template <typename R>
 __global__ void eigh_ql(const R* __restrict__ dIn, const R* __restrict__ eIn, int n, int nk, double* __restrict__ Eout,
                         int* __restrict__ errflag) {
   typedef Arith<R> A;
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ unsigned char smq[];
+  const int B = blockDim.x;
+  const long long k = (long long)blockIdx.x * B + threadIdx.x;
   if (k >= nk) return;
-  R d[WBG_EIGH_NMAX], e[WBG_EIGH_NMAX];
+  R* ds = reinterpret_cast<R*>(smq) + threadIdx.x;
+  R* es = ds + (size_t)n * B;
+  auto d = [&](int i) -> R& { return ds[i * B]; };
+  auto e = [&](int i) -> R& { return es[i * B]; };
   const R zero = A::from(0.0), one = A::from(1.0), two = A::from(2.0), eps = A::eps();
-  for (int i = 0; i < n; ++i) { d[i] = dIn[k * n + i]; e[i] = eIn[k * n + i]; }
-  e[n - 1] = zero;
+  for (int i = 0; i < n; ++i) { d(i) = dIn[k * n + i]; e(i) = eIn[k * n + i]; }
+  e(n - 1) = zero;
   bool ok = true;
   for (int l = 0; l < n; ++l) {
     int iter = 0, m;
     do {
       for (m = l; m < n - 1; ++m) {
-        const R dd = fabs(d[m]) + fabs(d[m + 1]);
-        if (fabs(e[m]) <= eps * dd) break;
+        const R dd = fabs(d(m)) + fabs(d(m + 1));
+        if (fabs(e(m)) <= eps * dd) break;
       }
       if (m != l) {
         if (iter++ >= 60) { ok = false; break; }
-        R g = (d[l + 1] - d[l]) / (two * e[l]);
+        R g = (d(l + 1) - d(l)) / (two * e(l));
         R r = sqrt(fma(g, g, one));
-        g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+        g = d(m) - d(l) + e(l) / (g + copysign(r, g));
         R s = one, c = one, p = zero;
         bool underflow = false;
         for (int i = m - 1; i >= l; --i) {
-          const R f = s * e[i];
-          const R b = c * e[i];
+          const R f = s * e(i);
+          const R b = c * e(i);
           // Givens rotation: one sqrt and one reciprocal (f, g are O(|T|): no overflow concern)
           r = sqrt(fma(f, f, g * g));
-          e[i + 1] = r;
-          if (r == zero) { d[i + 1] = d[i + 1] - p; e[m] = zero; underflow = true; break; }
+          e(i + 1) = r;
+          if (r == zero) { d(i + 1) = d(i + 1) - p; e(m) = zero; underflow = true; break; }
           const R rinv = one / r;
           s = f * rinv;
           c = g * rinv;
-          g = d[i + 1] - p;
-          r = (d[i] - g) * s + two * c * b;
+          g = d(i + 1) - p;
+          r = (d(i) - g) * s + two * c * b;
           p = s * r;
-          d[i + 1] = g + p;
+          d(i + 1) = g + p;
           g = c * r - b;
         }
         if (underflow) continue;
-        d[l] = d[l] - p;
-        e[l] = g;
-        e[m] = zero;
+        d(l) = d(l) - p;
+        e(l) = g;
+        e(m) = zero;
       }
     } while (m != l);
     if (!ok) break;
@@ -268,12 +287,12 @@ __global__ void eigh_ql(const R* __restrict__ dIn, const R* __restrict__ eIn, in
   if (!ok) atomicOr(errflag, WBG_FLAG_QL_NOCONV);
   // ascending insertion sort
   for (int i = 1; i < n; ++i) {
-    const R x = d[i];
+    const R x = d(i);
     int j = i - 1;
-    while (j >= 0 && d[j] > x) { d[j + 1] = d[j]; --j; }
-    d[j + 1] = x;
+    while (j >= 0 && d(j) > x) { d(j + 1) = d(j); --j; }
+    d(j + 1) = x;
   }
-  for (int i = 0; i < n; ++i) Eout[k * n + i] = A::to(d[i]);
+  for (int i = 0; i < n; ++i) Eout[k * n + i] = A::to(d(i));
 }
 
 WBG_D double hash_uniform(unsigned int a, unsigned int b) {
@@ -461,8 +480,8 @@ int pick_group(size_t smem, int threads, int gmax) {
 }
 
 template <typename R, typename TU, typename HIn>
-int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, void* workspace,
-                int* errflag, cudaStream_t stream) {
+int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int lowerIn,
+                void* workspace, int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
   typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
@@ -476,9 +495,13 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   const int G = pick_group(smT, LT, 128 / LT);
   if (G == 0) return WBG_ERR_SIZE;
   cudaFuncSetAttribute(eigh_tridiag<R, HIn, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
-  eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G, Vh,
-                                                                           tau, d, e);
-  eigh_ql<R><<<(nk + 127) / 128, 128, 0, stream>>>(d, e, n, nk, (double*)E, errflag);
+  eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G,
+                                                                           lowerIn, Vh, tau, d, e);
+  int BQ = 128;  // threads (matrices) per block: d and e take 2 n sizeof(R) bytes of shared memory each
+  while (BQ > 32 && (size_t)BQ * 2 * n * sizeof(R) > 64 * 1024) BQ /= 2;
+  const size_t smQ = (size_t)BQ * 2 * n * sizeof(R);
+  cudaFuncSetAttribute(eigh_ql<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
+  eigh_ql<R><<<(nk + BQ - 1) / BQ, BQ, smQ, stream>>>(d, e, n, nk, (double*)E, errflag);
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
   const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
   const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
@@ -501,14 +524,15 @@ size_t wbg_eigh_workspace_bytes(int n, int nk) {
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int mode,
                  void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
   if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
-  if (mode < 0 || mode > 3) return WBG_ERR_ARG;
+  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER)) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
-  if (mode == 1)
-    return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
-  if (mode == 0)
-    return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
-  if (mode == 2) return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
-  return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, workspace, errflag, stream);
+  const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
+  switch (mode & 3) {
+    case 1: return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
+    case 0: return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
+    case 2: return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
+    default: return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
+  }
 }
 
 // ---------------------------------------------------------------------------------------

@@ -16,6 +16,10 @@
 //      stage C: contract R0                              -> out[blk*nk + k][f]
 //    Each thread keeps the (<= MAXL) inputs of its matrix elements in registers and loops
 //    over the output index; the per-axis phase tables are broadcast from shared memory.
+//    A thread owns one "column" (field f, element mn).  An optional column list restricts the
+//    transform to a subset of elements -- the lower triangle of fields that are Hermitian by
+//    construction, whose upper triangle the consumers mirror -- so the result is exactly
+//    Hermitian and costs about half.
 #include "wbgpu_common.cuh"
 #include "wbgpu_df64.cuh"
 #include "wbgpu_r2k.cuh"
@@ -66,6 +70,17 @@ __global__ void r2k_weights(const double2* __restrict__ XR, const int* __restric
   XF[((long long)f * nR + r) * nw2 + mn] = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
 }
 
+// Column c of the launch -> (field, element).  cols == nullptr: all nF * nw2 columns.
+WBG_D bool decode_col(const int* cols, int ncols, int nF, int nw2, int& f, int& mn) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return false;
+  const int fm = cols ? cols[c] : c;
+  if (fm < 0 || fm >= nF * nw2) return false;  // list lives in device memory: validate here
+  f = fm / nw2;
+  mn = fm % nw2;
+  return true;
+}
+
 // One separable contraction: out[col][j] = sum_{i < len} tab[j][idx[i]] in[col][i]
 // for every output index j < Nj.  `in` values of this thread stay in registers.
 template <typename T, int MAXL>
@@ -87,16 +102,16 @@ template <typename T, int MAXL>
 __global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* __restrict__ XF,
                                                        const int* __restrict__ pairStart, const int* __restrict__ r2,
                                                        const typename C2<T>::t* __restrict__ ph2,
-                                                       typename C2<T>::t* __restrict__ Z, R2KGeom g, int nF) {
+                                                       typename C2<T>::t* __restrict__ Z, R2KGeom g, int nF,
+                                                       const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smr[];
   V* tab = reinterpret_cast<V*>(smr);  // [N2][nr2]
   const int p = blockIdx.y, blk = blockIdx.z;
   for (int i = threadIdx.x; i < g.N2 * g.nr2; i += blockDim.x) tab[i] = ph2[(long long)blk * g.N2 * g.nr2 + i];
   __syncthreads();
-  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= (long long)nF * g.nw2) return;
-  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
+  int f, mn;
+  if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
   const int r0 = pairStart[p], len = pairStart[p + 1] - r0;
   V x[MAXL];
   int ri[MAXL];
@@ -121,16 +136,16 @@ __global__ void __launch_bounds__(kThreads) r2k_stageB(const typename C2<T>::t* 
                                                        const int* __restrict__ sliceStart,
                                                        const int* __restrict__ pairR1,
                                                        const typename C2<T>::t* __restrict__ ph1,
-                                                       typename C2<T>::t* __restrict__ Y, R2KGeom g, int nF) {
+                                                       typename C2<T>::t* __restrict__ Y, R2KGeom g, int nF,
+                                                       const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smr[];
   V* tab = reinterpret_cast<V*>(smr);  // [N1][nr1]
   const int u = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
   for (int i = threadIdx.x; i < g.N1 * g.nr1; i += blockDim.x) tab[i] = ph1[(long long)blk * g.N1 * g.nr1 + i];
   __syncthreads();
-  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= (long long)nF * g.nw2) return;
-  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
+  int f, mn;
+  if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
   const int p0 = sliceStart[u], len = sliceStart[u + 1] - p0;
   V x[MAXL];
   int ri[MAXL];
@@ -154,16 +169,16 @@ template <typename T, int MAXL>
 __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* __restrict__ Y,
                                                        const int* __restrict__ sliceR0,
                                                        const typename C2<T>::t* __restrict__ ph0,
-                                                       typename C2<T>::t* __restrict__ out, R2KGeom g, int nF) {
+                                                       typename C2<T>::t* __restrict__ out, R2KGeom g, int nF,
+                                                       const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smr[];
   V* tab = reinterpret_cast<V*>(smr);  // [N0][nr0]
   const int k1 = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
   for (int i = threadIdx.x; i < g.N0 * g.nr0; i += blockDim.x) tab[i] = ph0[(long long)blk * g.N0 * g.nr0 + i];
   __syncthreads();
-  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= (long long)nF * g.nw2) return;
-  const int f = (int)(col / g.nw2), mn = (int)(col % g.nw2);
+  int f, mn;
+  if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
   const int len = g.nU;
   V x[MAXL];
   int ri[MAXL];
@@ -185,31 +200,34 @@ __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* 
 template <typename T, int MAXL>
 void launch_stages(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart,
                    const int* pairR1, const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z,
-                   void* Y, void* out, const R2KGeom& g, int nb, cudaStream_t stream) {
+                   void* Y, void* out, const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   typedef typename C2<T>::t V;
-  const unsigned colBlocks = (unsigned)(((long long)nF * g.nw2 + kThreads - 1) / kThreads);
+  const unsigned colBlocks = (unsigned)((ncols + kThreads - 1) / kThreads);
   r2k_stageA<T, MAXL><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
-      (const V*)XF, pairStart, r2, (const V*)ph2, (V*)Z, g, nF);
+      (const V*)XF, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
   r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, (size_t)g.N1 * g.nr1 * sizeof(V), stream>>>(
-      (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF);
+      (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF, cols, ncols);
   r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, (size_t)g.N0 * g.nr0 * sizeof(V), stream>>>(
-      (const V*)Y, sliceR0, (const V*)ph0, (V*)out, g, nF);
+      (const V*)Y, sliceR0, (const V*)ph0, (V*)out, g, nF, cols, ncols);
 }
 
 template <typename T>
 int launch_r2k(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z, void* Y, void* out,
-               const R2KGeom& g, int nb, cudaStream_t stream) {
+               const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   const int maxlen = max(max(g.maxPairLen, g.maxSliceLen), g.nU);
   if (maxlen <= 8)
-    launch_stages<T, 8>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+    launch_stages<T, 8>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+                         ncols, stream);
   else if (maxlen <= 16)
-    launch_stages<T, 16>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+    launch_stages<T, 16>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+                         ncols, stream);
   else if (maxlen <= 24)
-    launch_stages<T, 24>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, stream);
+    launch_stages<T, 24>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+                         ncols, stream);
   else if (maxlen <= WBG_R2K_MAXLEN)
     launch_stages<T, WBG_R2K_MAXLEN>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
-                                     nb, stream);
+                                     nb, cols, ncols, stream);
   else
     return WBG_ERR_SIZE;
   return wbg_cuda_status(cudaGetLastError());
@@ -245,8 +263,11 @@ int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, i
 
 int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
-                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, cudaStream_t stream) {
+                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, const int* cols, int ncols,
+                cudaStream_t stream) {
   if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 2) return WBG_ERR_ARG;
+  if (!cols) ncols = nF * g->nw2;
+  if (ncols < 1 || ncols > nF * g->nw2) return WBG_ERR_ARG;
   if (g->nw2 != g->nw * g->nw || g->nk != g->N0 * g->N1 * g->N2) return WBG_ERR_ARG;
   if (g->nU < 1 || g->nP < 1 || g->maxPairLen < 1 || g->maxSliceLen < 1) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, prec)) return WBG_ERR_WORKSPACE;
@@ -256,10 +277,10 @@ int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, con
   char* Y = Z + ((z + 255) / 256) * 256;
   if (prec == 1)
     return launch_r2k<double>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
-                              stream);
+                              cols, ncols, stream);
   if (prec == 2)
     return launch_r2k<df64>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
-                            stream);
+                            cols, ncols, stream);
   return launch_r2k<float>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
-                           stream);
+                           cols, ncols, stream);
 }

@@ -22,4 +22,5 @@ int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, i
                        const double* wcc, const R2KLattice* lat, int prec, void* XF, cudaStream_t stream);
 int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
-                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, cudaStream_t stream);
+                size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, const int* cols, int ncols,
+                cudaStream_t stream);

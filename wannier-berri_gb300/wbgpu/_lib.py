@@ -11,6 +11,7 @@ import os
 from . import build as _build
 
 EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
+           'wbg_r2k_columns',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
            'wbg_scan_finalize', 'wbg_probe_fma']
@@ -50,6 +51,8 @@ _SIGS = {
     'wbg_r2k_fields': (_I, [_P, _I, _P, _I, _I, _P, _I, _P, ctypes.POINTER(Lattice), _I, _P, _P]),
     'wbg_r2k_workspace_size': (_I, [ctypes.POINTER(R2KGeom), _I, _I, _I, ctypes.POINTER(_SZ)]),
     'wbg_r2k': (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _SZ, _P, ctypes.POINTER(R2KGeom), _P]),
+    'wbg_r2k_columns': (_I, [_P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _SZ, _P,
+                             ctypes.POINTER(R2KGeom), _P]),
     'wbg_eigh_workspace_size': (_I, [_I, _I, ctypes.POINTER(_SZ)]),
     'wbg_eigh_batched': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _SZ, _P, _P]),
     'wbg_eigh_batched_noalloc': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _P]),

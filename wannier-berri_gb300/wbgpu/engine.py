@@ -258,6 +258,36 @@ def field_plan(quantities, with_H, extra_keys):
     return desc, index
 
 
+def hermitian_fields(quantities, with_H):
+    """Per field of field_plan: True when the k-space field is Hermitian by construction
+    (H, its derivatives, AA and its derivatives / curl); BB and CC are not."""
+    keys = extra_keys_for(quantities)
+    desc, _ = field_plan(quantities, with_H, keys)
+    nonherm = set()
+    base = 1
+    for key in keys:
+        if key in ('BB', 'CC'):
+            nonherm |= {base, base + 1, base + 2}
+        base += 3
+    return [d[1] not in nonherm for d in desc]
+
+
+def column_list(dev, quantities, with_H, lower):
+    """Device int32 list of the elements f*nw2 + m*nw + n that wbg_r2k_columns computes: the
+    lower triangle (m >= n) of the Hermitian fields when ``lower``, every element otherwise."""
+    key = ('cols', tuple(sorted(quantities)), with_H, bool(lower))
+    if key not in dev._cache:
+        nw = dev.nw
+        herm = hermitian_fields(quantities, with_H)
+        m, n = np.meshgrid(np.arange(nw), np.arange(nw), indexing='ij')
+        full = (m * nw + n).reshape(-1)
+        tril = (m * nw + n)[m >= n]
+        cols = np.concatenate([f * nw * nw + (tril if (lower and h) else full) for f, h in enumerate(herm)])
+        dev._cache[key] = (torch.tensor(cols.astype(np.int32), device=dev.device),
+                           [bool(lower and h) for h in herm])
+    return dev._cache[key]
+
+
 def extra_keys_for(quantities):
     keys = []
     if quantities & {'A', 'dA', 'O', 'Od', 'dO'}:
@@ -302,6 +332,7 @@ def r2k_geometry(dev, NKFFT):
 
 
 PREC_FP32, PREC_FP64, PREC_DF64 = 0, 1, 2
+EIGH_LOWER = 4  # wbg_eigh_batched mode bit: H given by its lower triangle
 
 
 def _prec(p):
@@ -352,10 +383,13 @@ def field_arrays(dev, quantities, with_H, prec):
     return dev._cache[ck]
 
 
-def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, phases=None, block_start=0):
+def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, phases=None, block_start=0,
+        lower=False):
     """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive).
     prec: False/True (FP32/FP64) or PREC_DF64 (double-float, complex128-sized slots).
-    phases: optional device tables from DeviceSystem.grid_phases (then block_start indexes them)."""
+    phases: optional device tables from DeviceSystem.grid_phases (then block_start indexes them).
+    lower: compute only the lower triangle of the Hermitian fields (wbg_r2k_columns); their
+    upper triangle is left unwritten for the consumers to mirror."""
     prec = _prec(prec)
     NKFFT = [int(n) for n in NKFFT]
     XF, index, nF, _ = field_arrays(dev, quantities, with_H, prec)
@@ -386,18 +420,24 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, pha
             ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
     name = {PREC_FP32: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
-    st = _timed(name, lib.wbg_r2k, _ptr(XF), nF, _ptr(gt['pair_start']),
-                _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']), _ptr(gt['slice_r0']),
-                _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, prec, _ptr(workspace),
-                ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
-    _lib.check(st, "wbg_r2k")
+    common = (_ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
+              _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, prec, _ptr(workspace),
+              ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
+    if lower:
+        cols, _ = column_list(dev, quantities, with_H, True)
+        st = _timed(name, lib.wbg_r2k_columns, _ptr(XF), nF, _ptr(cols), cols.numel(), *common)
+        _lib.check(st, "wbg_r2k_columns")
+    else:
+        st = _timed(name, lib.wbg_r2k, _ptr(XF), nF, *common)
+        _lib.check(st, "wbg_r2k")
     return out, index, nF, (ph, workspace)
 
 
 def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1, work=None, flag=None):
     """Batched eigensolver (wbg_eigh_batched).  mode 1: FP64 throughout, U complex128;
-    mode 0: FP64 solve, FP32 back-transform; mode 2: double-float solve, FP32 back-transform
-    (U complex64 in modes 0 and 2)."""
+    mode 0: FP64 solve, FP32 back-transform; mode 2: double-float solve, FP32 back-transform;
+    mode 3: as 2 with double-float H (U complex64 in modes 0, 2, 3).  mode | EIGH_LOWER: H is
+    read from its lower triangle."""
     lib = _lib.load()
     dev = Hfields.device
     ws = ctypes.c_size_t(0)
@@ -407,7 +447,7 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1, work=None, flag=None)
     if E is None:
         E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
     if U is None:
-        U = torch.empty((nk, nw, nw), dtype=torch.complex128 if mode == 1 else torch.complex64, device=dev)
+        U = torch.empty((nk, nw, nw), dtype=torch.complex128 if (mode & 3) == 1 else torch.complex64, device=dev)
     if flag is None:
         flag = torch.zeros(1, dtype=torch.int32, device=dev)
     st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw,
@@ -453,7 +493,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     flag = dev.buffer('flag', (1,), torch.int32)
     flag.zero_()
 
-    def fields_for(q, with_H, prec, name):
+    def fields_for(q, with_H, prec, name, lower=False):
         _, _, nF, _ = field_arrays(dev, q, with_H, prec)
         out = dev.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec == PREC_FP32 else torch.complex128)
         geo = r2k_geometry(dev, NKFFT)
@@ -462,7 +502,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
                    "wbg_r2k_workspace_size")
         work = dev.buffer('r2k_ws', (int(ws.value),), torch.uint8)
         return r2k(dev, dKs, NKFFT, q, with_H, prec, out=out, workspace=work, phases=ph(prec),
-                   block_start=block_start)
+                   block_start=block_start, lower=lower)
 
     E = dev.buffer('E', (nkt, nw), torch.float64)
     ews = ctypes.c_size_t(0)
@@ -475,12 +515,14 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         E, U, flag = eigh(fields, nF * nw * nw, nw, nkt, E=E, U=U, mode=1, work=ework, flag=flag)
         fp64_fields = True
     elif precision == 'mixed':
-        Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H')
+        # lower triangles of the Hermitian fields only: exactly Hermitian, half the transform
+        Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=True)
         keep.append(k0)
         U = dev.buffer('U32', (nkt, nw, nw), torch.complex64)
-        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3, work=ework, flag=flag)
-        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32, 'fields')
+        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | EIGH_LOWER, work=ework, flag=flag)
+        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32, 'fields', lower=True)
         keep.append(k1)
+        lower_in = column_list(dev, quantities, False, True)[1]
         fp64_fields = False
     else:
         raise ValueError(f"unknown precision mode {precision!r}")
@@ -491,6 +533,10 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
             n = QUANTITIES[q]['ncomp']
             sel += list(range(index[q], index[q] + n))
             herm += [QUANTITIES[q]['herm']] * n
+    if not fp64_fields:
+        # mirrored (exactly Hermitian) inputs: flag them, and keep the Hermitian part of their
+        # rotation, which drops only the FP32 rounding noise of U^dagger X U
+        herm = [(h or 1) | 4 if lower_in[f] else h for f, h in zip(sel, herm)]
     if sel:
         Xb = dev.buffer('Xbar', (nkt, len(sel), nw, nw), torch.complex128 if fp64_fields else torch.complex64)
         Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nkt, fp64_fields, out=Xb)
