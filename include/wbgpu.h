@@ -139,9 +139,18 @@ int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, d
  * herm[f] = 2: at least the diagonal of the Hermitian part (real) is written -- for fields
  * whose consumers read the diagonal only (rotA in Omega / Morb_Hpm).
  * herm[f] | 4: X[fsel[f]] holds only its lower triangle (wbg_r2k_columns output); it is read
- * as the Hermitian matrix with that lower triangle and a real diagonal. */
+ * as the Hermitian matrix with that lower triangle and a real diagonal.
+ * fp64 == 0 and nw == 32 run on the tensor cores (tcgen05, products split into three TF32
+ * terms, FP32 accumulation); other sizes and fp64 != 0 on the CUDA cores. */
 int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);
+
+/* Device-side error word of the library (bitmask, sticky until cleared).
+ * WBG_DEVICE_FLAG_TC_TIMEOUT: a tensor-core kernel's wait for its MMAs exceeded its 1 s bound;
+ * that launch's results are invalid.  Synchronises the current device, then reads (and with
+ * clear != 0 resets) the word. */
+#define WBG_DEVICE_FLAG_TC_TIMEOUT 1
+int wbg_device_flags(unsigned int* flags, int clear);
 
 /* ---- stage 4: Berry curvature traces + Fermi-level histogram ----------------------------
  * Xbar [nk][nFbar][nw][nw]: velocity dH/dk at iV..iV+2, A at iA..iA+2, rotA at iO..iO+2.

@@ -154,6 +154,41 @@ def test_rotate_lower_triangle_input(fp64, nw):
     assert torch.equal(a[:, 2, d, d].real, b[:, 2, d, d].real)
 
 
+@pytest.mark.parametrize("nF", [1, 4, 9])
+@pytest.mark.parametrize("lower", [False, True])
+def test_rotate_tensor_core_vs_fp64(nF, lower):
+    """FP32 rotation at nw = 32 (tcgen05, 3xTF32 products, FP32 accumulation) against the FP64
+    CUDA-core rotation: every output mode, field counts that leave partial 128-row tiles, a
+    batch that is not a multiple of the persistent grid.  Relative error < 2e-6 of max |Xbar|."""
+    nw, nk = 32, 1000
+    rng = np.random.default_rng(31 + nF)
+    X = rng.standard_normal((nk, nF, nw, nw)) + 1j * rng.standard_normal((nk, nF, nw, nw))
+    if lower:
+        X = X + X.conj().swapaxes(-1, -2)
+    U = np.linalg.qr(rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw)))[0]
+    modes = [(f % 3) | (4 if lower else 0) for f in range(nF)]
+    sel = list(range(nF))[::-1]
+    Xd, Ud = torch.from_numpy(X).cuda(), torch.from_numpy(U).cuda()
+    ref, _ = engine.rotate(Ud, Xd, nF, sel, [m & 3 for m in modes], nw, nk, True)
+    ref = ref.clone()
+    Xl = Xd.to(torch.complex64)
+    if lower:  # the upper triangle is not read
+        iu = torch.triu_indices(nw, nw, 1)
+        Xl[:, :, iu[0], iu[1]] = complex(float('nan'), float('nan'))
+    got, _ = engine.rotate(Ud.to(torch.complex64), Xl, nF, sel, modes, nw, nk, False)
+    torch.cuda.synchronize()
+    assert engine.device_flags() == 0
+    got = got.to(torch.complex128)
+    scale = float(ref.abs().max())
+    d = torch.arange(nw, device=ref.device)
+    for f, m in enumerate(modes):
+        if m & 3 == 2:  # diagonal of the Hermitian part only
+            err = float((got[:, f, d, d].real - ref[:, f, d, d].real).abs().max())
+        else:
+            err = float((got[:, f] - ref[:, f]).abs().max())
+        assert err < 2e-6 * scale, (f, m, err / scale)
+
+
 @pytest.mark.parametrize("mode", [1, 0, 2])
 @pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
 def test_eigh_random(nw, mode):

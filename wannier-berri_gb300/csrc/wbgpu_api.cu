@@ -73,6 +73,8 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
   return wbg_rotate_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, fp64, (cudaStream_t)stream);
 }
 
+int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
+
 int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                     const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
                     void* stream) {

@@ -1,0 +1,377 @@
+// Band-basis rotation Xbar = U^dagger X U on the 5th-generation tensor cores (tcgen05) for
+// nw = 32, FP32 path (data_K/data_K.py:130-132 _rotate, data_K/data_K_R.py:69-89 Xbar).
+//
+// Complex products are embedded in real ones:
+//   GEMM1  T = X U       A1[(f,m)][j']  = [Re X_f[m][j] | Im X_f[m][j]]          (K = 2 nw)
+//                        B[j'][n']      = [[Re U, Im U], [-Im U, Re U]]          (N = 2 nw)
+//                        D1[(f,m)][n']  = [Re T_f[m][n] | Im T_f[m][n]]
+//   GEMM2  Y^H = T^H U   A2[(f,m)][j']  = [Re T_f[j][m] | -Im T_f[j][m]]         (same B)
+//                        D2[(f,m)][n']  = [Re Y_f^H[m][n] | Im Y_f^H[m][n]]
+// so both GEMMs share the embedded U operand, and the fields of one k-point stack along M:
+// a 128-row tile holds 4 fields of 32 rows, tiles run over the requested fields.
+// Each operand is split as x = hi + lo with hi, lo rounded to TF32 (cvt.rna), and
+// A.B = Ah.Bh + (Ah.Bl + Al.Bh) in FP32 (3xTF32, ~2^-21 relative per product).  The tensor
+// cores round each accumulation step toward zero, so long chains in one accumulator drift;
+// the main products therefore go to NMAIN accumulators over separate K ranges, the small
+// correction products to one more, and the partial sums are added on the CUDA cores with
+// round-to-nearest -- the result is as accurate as an FP32 CUDA-core GEMM.  Operands live in shared memory in the no-swizzle K-major
+// layout: 8-row x 16-byte core matrices, K-adjacent core matrices 144 bytes apart (16 bytes
+// of padding) so that the transposed writes of the epilogue hit 32 distinct banks.
+// One thread issues the MMAs; completion is tracked with an mbarrier whose every wait is
+// bounded in time: on timeout the kernel records WBG_DEVICE_FLAG_TC_TIMEOUT in the
+// library's device error word, releases its tensor memory and returns.
+#include "wbgpu_common.cuh"
+#include "wbgpu_band.cuh"
+
+__device__ unsigned int g_wbg_device_flags;
+
+namespace {
+
+constexpr int NW = 32;                     // Wannier functions handled here
+constexpr int KD = 2 * NW;                 // real-embedded contraction length
+constexpr int ND = 2 * NW;                 // real-embedded output columns (re | im)
+constexpr int TM = 128;                    // MMA M: one tile = 4 fields x 32 rows
+constexpr int FPT = TM / NW;               // fields per tile
+constexpr int NTHR = 128;                  // warp q owns TMEM lanes 32q..32q+31 = field q of the tile
+constexpr int LBO = 144;                   // bytes between K-adjacent core matrices
+constexpr int SBO = (KD / 4) * LBO;        // bytes between 8-row groups
+constexpr int A_BYTES = (TM / 8) * SBO;    // one copy (hi or lo) of a tile operand
+constexpr int B_BYTES = (ND / 8) * SBO;    // one copy of the embedded U
+constexpr int SMEM_BYTES = 2 * B_BYTES + 2 * A_BYTES;
+#ifndef WBG_TC_NMAIN
+#define WBG_TC_NMAIN 2
+#endif
+constexpr int NMAIN = WBG_TC_NMAIN;        // accumulators of the main (hi.hi) products
+constexpr int NACC = NMAIN + 1;            // + one for the correction products
+static_assert((KD / 8) % NMAIN == 0, "K steps must split evenly over the main accumulators");
+constexpr uint32_t TMEM_COLS = NACC * ND <= 128 ? 128 : NACC * ND <= 256 ? 256 : 512;  // GEMM1 and GEMM2 share them
+constexpr int STAGE_LD = NW + 1;           // float2 row stride of the Hermitian-part staging
+constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on every mbarrier wait
+
+static_assert(4 * NW * STAGE_LD * 8 <= A_BYTES, "staging must fit in the A operand buffer");
+
+// Instruction descriptor of tcgen05.mma kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
+// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(ND >> 3) << 17) |
+                           ((uint32_t)(TM >> 4) << 24);
+
+WBG_D uint32_t op_off(int r, int k) { return (r >> 3) * SBO + (k >> 2) * LBO + (r & 7) * 16 + (k & 3) * 4; }
+
+WBG_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+WBG_D uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// x = hi + lo, both rounded to TF32, stored at byte offset off of the two operand copies
+WBG_D void put_split(unsigned char* hi, unsigned char* lo, uint32_t off, float x) {
+  const uint32_t h = tf32_rna(x);
+  const uint32_t l = tf32_rna(x - __uint_as_float(h));
+  *reinterpret_cast<uint32_t*>(hi + off) = h;
+  *reinterpret_cast<uint32_t*>(lo + off) = l;
+}
+
+// Shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), version 1 at bit 46,
+// base offset 0, no swizzle.
+WBG_D uint64_t make_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) | ((uint64_t)(SBO >> 4) << 32) |
+         (1ull << 46);
+}
+
+WBG_D void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+
+WBG_D void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+WBG_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+WBG_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+WBG_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+WBG_D unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for phase `parity` of the mbarrier to complete, for at most WAIT_NS.
+WBG_D bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (global_ns() - t0 > WAIT_NS) return false;
+  }
+}
+
+WBG_D void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+// the loaded registers are valid only after tcgen05.wait::ld; passing them through an asm
+// after the wait keeps every use behind it
+WBG_D void tmem_ld_wait16(uint32_t* r) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+               "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+               "+r"(r[14]), "+r"(r[15])::"memory");
+}
+// The 64 columns (re | im) of this thread's TMEM lane, summed over the NACC accumulators
+// (correction first, then the main ones) on the CUDA cores with round-to-nearest.
+WBG_D void tmem_row64(uint32_t taddr, float (&v)[64]) {
+#pragma unroll
+  for (int a = 0; a < NACC; ++a) {
+    uint32_t r[64];
+    const uint32_t col = (uint32_t)(a == 0 ? NMAIN : a - 1) * ND;
+    tmem_ld16(taddr + col + 0, r + 0);
+    tmem_ld16(taddr + col + 16, r + 16);
+    tmem_ld16(taddr + col + 32, r + 32);
+    tmem_ld16(taddr + col + 48, r + 48);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    tmem_ld_wait16(r + 0);
+    tmem_ld_wait16(r + 16);
+    tmem_ld_wait16(r + 32);
+    tmem_ld_wait16(r + 48);
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = a == 0 ? __uint_as_float(r[i]) : v[i] + __uint_as_float(r[i]);
+  }
+}
+
+// Accumulators (ND columns each) from column d: main products of K range q at d + q*ND
+// (q < NMAIN), correction products at d + NMAIN*ND.
+WBG_D void issue_gemm(uint32_t d, const unsigned char* Ah, const unsigned char* Al, const unsigned char* Bh,
+                      const unsigned char* Bl) {
+  const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
+  constexpr int SPQ = (KD / 8) / NMAIN;  // K steps per main accumulator
+#pragma unroll
+  for (int s = 0; s < KD / 8; ++s) {  // K = 8 tf32 per instruction = two core matrices
+    const uint32_t so = (uint32_t)s * 2 * LBO;
+    const uint32_t dm = d + (uint32_t)(s / SPQ) * ND, dc = d + (uint32_t)NMAIN * ND;
+    mma_tf32(dc, make_desc(al + so), make_desc(bh + so), s > 0);
+    mma_tf32(dc, make_desc(ah + so), make_desc(bl + so), 1);
+    mma_tf32(dm, make_desc(ah + so), make_desc(bh + so), s % SPQ != 0);
+  }
+}
+
+// Every thread waits on the MMA barrier; a timeout anywhere aborts the whole CTA.
+WBG_D bool wait_all(uint32_t mbar, uint32_t parity, volatile int* abort_s) {
+  if (!mbar_wait(mbar, parity)) {
+    *abort_s = 1;
+    atomicOr(&g_wbg_device_flags, (unsigned)WBG_DEVICE_FLAG_TC_TIMEOUT);
+  }
+  __syncthreads();
+  return *abort_s == 0;
+}
+
+__global__ void __launch_bounds__(NTHR, 2)
+    rotate_tc_kernel(const float2* __restrict__ U, long long strideU, const float2* __restrict__ X, int nFin,
+                     const int* __restrict__ fsel, const int* __restrict__ herm, int nFrot, float2* __restrict__ Xbar,
+                     int nk) {
+  extern __shared__ __align__(128) unsigned char smt[];
+  unsigned char* Bh = smt;
+  unsigned char* Bl = Bh + B_BYTES;
+  unsigned char* Ah = Bl + B_BYTES;
+  unsigned char* Al = Ah + A_BYTES;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t mb = smem_u32(&mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_s = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = tmem_base_s;
+  const uint32_t D1 = tbase, D2 = tbase;  // GEMM2 reuses GEMM1's accumulators once D1 is read
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;  // TMEM lanes of this warp
+  uint32_t phase = 0;
+  const int ntiles = (nFrot + FPT - 1) / FPT;
+  float2* stage = reinterpret_cast<float2*>(Ah) + warp * NW * STAGE_LD;
+  for (long long k = blockIdx.x; k < nk && !abort_s; k += gridDim.x) {
+    // ---- embedded U_k (B operand, hi / lo)
+    const float2* Uk = U + k * strideU;
+    {
+      constexpr int PER = NW * NW / NTHR;
+      float2 uv[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) uv[i] = Uk[i * NTHR + tid];  // all loads in flight at once
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int e = i * NTHR + tid, j = e / NW, n = e % NW;
+        put_split(Bh, Bl, op_off(n, j), uv[i].x);
+        put_split(Bh, Bl, op_off(n, NW + j), -uv[i].y);
+        put_split(Bh, Bl, op_off(NW + n, j), uv[i].y);
+        put_split(Bh, Bl, op_off(NW + n, NW + j), uv[i].x);
+      }
+    }
+    for (int t = 0; t < ntiles; ++t) {
+      // ---- A1: rows (fl, m) of the tile's fields, K = [Re X[m][:] | Im X[m][:]].
+      // Thread tid owns element n = lane of rows m = 4 i + warp: every load of the tile is
+      // issued before the first store.
+      {
+        constexpr int PER = FPT * NW * NW / NTHR;
+        float2 xv[PER];
+        int code[FPT];  // per field: -1 padding, -2 invalid selection, else source field | lower << 30
+#pragma unroll
+        for (int fl = 0; fl < FPT; ++fl) {
+          const int f = t * FPT + fl;
+          if (f >= nFrot) {
+            code[fl] = -1;
+          } else {
+            const int fs = fsel[f];  // selection lives in device memory: validate here
+            code[fl] = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int e = i * NTHR + tid, fl = e / (NW * NW), m = (e / NW) % NW, n = e % NW;
+          const int c = code[fl];
+          const bool lower = c >= 0 && (c >> 30);
+          xv[i] = make_float2(0.f, 0.f);
+          if (c == -2) xv[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+          else if (c >= 0 && (!lower || m >= n))
+            xv[i] = X[(k * nFin + (c & 0x3fffffff)) * (long long)(NW * NW) + m * NW + n];
+        }
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int e = i * NTHR + tid, fl = e / (NW * NW), m = (e / NW) % NW, n = e % NW;
+          const int c = code[fl];
+          const bool lower = c >= 0 && (c >> 30);
+          const int r = fl * NW;
+          const float xr = xv[i].x, xi = (lower && m == n) ? 0.f : xv[i].y;
+          if (!lower || m >= n) {
+            put_split(Ah, Al, op_off(r + m, n), xr);
+            put_split(Ah, Al, op_off(r + m, NW + n), xi);
+          }
+          if (lower && m > n) {  // upper triangle: X[n][m] = conj(X[m][n])
+            put_split(Ah, Al, op_off(r + n, m), xr);
+            put_split(Ah, Al, op_off(r + n, NW + m), -xi);
+          }
+        }
+      }
+      fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        issue_gemm(D1, Ah, Al, Bh, Bl);
+        mma_commit(mb);
+      }
+      if (!wait_all(mb, phase, &abort_s)) break;
+      phase ^= 1;
+      tc_fence_after();
+      {  // ---- D1 -> A2: thread (field q, row j) holds T[j][:]; writes column j of T^H
+        float r[64];
+        tmem_row64(D1 + lane_base, r);
+        const int row0 = warp * NW;
+#pragma unroll
+        for (int mp = 0; mp < NW; ++mp) {
+          put_split(Ah, Al, op_off(row0 + mp, lane), r[mp]);
+          put_split(Ah, Al, op_off(row0 + mp, NW + lane), -r[NW + mp]);
+        }
+      }
+      tc_fence_before();
+      fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        issue_gemm(D2, Ah, Al, Bh, Bl);
+        mma_commit(mb);
+      }
+      if (!wait_all(mb, phase, &abort_s)) break;
+      phase ^= 1;
+      tc_fence_after();
+      {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][:]
+        float r[64];
+        tmem_row64(D2 + lane_base, r);
+        const int f = t * FPT + warp;
+        if (f < nFrot) {  // warp-uniform
+          const int hm = herm[f] & 3;
+          float2* dst = Xbar + (k * nFrot + f) * (long long)(NW * NW);
+          if (hm == 0) {  // Y[n][m] = conj(Y^H[m][n]): coalesced over m
+#pragma unroll
+            for (int n = 0; n < NW; ++n) dst[n * NW + lane] = make_float2(r[n], -r[NW + n]);
+          } else if (hm == 2) {  // diagonal of the Hermitian part
+#pragma unroll
+            for (int n = 0; n < NW; ++n)
+              if (n == lane) dst[n * NW + n] = make_float2(r[n], 0.f);
+          } else {  // Hermitian part P = (Y^H + Y)/2; P[n][m] = conj(P[m][n])
+#pragma unroll
+            for (int n = 0; n < NW; ++n)
+              stage[lane * STAGE_LD + n] = make_float2(r[n], r[NW + n]);
+            __syncwarp();
+#pragma unroll
+            for (int n = 0; n < NW; ++n) {
+              const float2 s = stage[n * STAGE_LD + lane];  // Y^H[n][m]
+              const float pr = 0.5f * (r[n] + s.x);
+              const float pi = 0.5f * (r[NW + n] - s.y);
+              dst[n * NW + lane] = make_float2(pr, -pi);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncthreads();  // TMEM columns and the A buffers are reused by the next tile
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+}  // namespace
+
+bool wbg_rotate_tc_supported(int nw, int fp64) { return !fp64 && nw == NW; }
+
+int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
+                      int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
+  if (nw != NW) return WBG_ERR_SIZE;
+  if (nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return WBG_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return WBG_ERR_CUDA;
+  if (cudaFuncSetAttribute(rotate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
+    return WBG_ERR_CUDA;
+  const long long grid = nk < 2ll * sms ? nk : 2ll * sms;
+  rotate_tc_kernel<<<(unsigned)grid, NTHR, SMEM_BYTES, stream>>>((const float2*)U, strideU, (const float2*)X, nFin,
+                                                                fsel, herm, nFrot, (float2*)Xbar, nk);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_device_flags_run(unsigned int* flags, int clear) {
+  if (!flags) return WBG_ERR_ARG;
+  if (cudaDeviceSynchronize() != cudaSuccess) return WBG_ERR_CUDA;
+  if (cudaMemcpyFromSymbol(flags, g_wbg_device_flags, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+  if (clear) {
+    const unsigned int zero = 0;
+    if (cudaMemcpyToSymbol(g_wbg_device_flags, &zero, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+  }
+  return WBG_OK;
+}

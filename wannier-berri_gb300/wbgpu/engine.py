@@ -551,6 +551,13 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     return bd
 
 
+def device_flags(clear=True):
+    """Library device error word (wbg_device_flags); nonzero after a tensor-core wait timed out."""
+    v = ctypes.c_uint(0)
+    _lib.check(_lib.load().wbg_device_flags(ctypes.byref(v), int(clear)), "wbg_device_flags")
+    return int(v.value)
+
+
 def check_flag(bd):
     if int(bd._flag.item()) != 0:
         raise RuntimeError("wbg_eigh_batched: QL iteration did not converge for some k-point")
