@@ -279,7 +279,7 @@ def run_gpu(args):
     quantities = calc.quantities(s)
     calc.reset(dev.device)
     phases = {p: dev.grid_phases(shifts, grid.FFT, p)
-              for p in (engine.PREC_FP64, engine.PREC_DF64, engine.PREC_FP32)}
+              for p in (engine.PREC_FP64, engine.PREC_DF64, engine.PREC_FP32S)}
 
     def step(i, precision, c=calc):
         blocks = step_blocks(i)

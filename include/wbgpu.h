@@ -71,13 +71,17 @@ const char* wbg_status_string(int status);
  *            with w = R + t_n - t_m in Cartesian coordinates (fourier/rvectors.py:355-369,
  *            487-494; data_K/data_K_R.py:48-51)
  *   XF       [nfields][nR][nw][nw] complex: prec 0 float, 1 double, 2 double-float (re.hi, re.lo,
- *            im.hi, im.lo floats: 48-bit significand on the FP32 pipe)
+ *            im.hi, im.lo floats: 48-bit significand on the FP32 pipe); prec 3 float followed by
+ *            a second [nfields][nR][nw][nw] float array of the rounding residuals XF - float(XF)
  * wbg_r2k (per batch of FFT blocks): fields_out[b*nk + k][f] = sum_R exp(2 pi i R.(j_k/N + dK_b)) XF[f][R]
  *   pair_start [nP+1] first sorted R of each pair;  r2 [nR] third R component
  *   slice_start [nU+1] first pair of each slice;    pair_r1 [nP];  slice_r0 [nU]
  *   ph0/ph1/ph2 [nblocks][N_d][nr_d] complex (precision prec): exp(2 pi i R_d (j/N_d + dK_d)),
  *            R_d = rmin_d + r
  *   fields_out [nblocks*nk][nfields][nw][nw] complex (precision prec), k = (j0*N1 + j1)*N2 + j2
+ *   prec 3 (FP32 with split inputs): the first contraction also sums the residuals of XF, so
+ *            the k-independent R-space data -- whose rounding would be a systematic error of the
+ *            whole integral -- enter with 48 bits; phases, intermediates and output as prec 0.
  */
 int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, const int* field_desc, int nfields,
                    const double* wcc, const wbg_lattice* lat, int prec, void* XF, void* stream);

@@ -31,7 +31,7 @@ def c2small():
     return s, o
 
 
-@pytest.mark.parametrize("fp64,tol", [(True, 1e-12), (False, 2e-6)])
+@pytest.mark.parametrize("fp64,tol", [(True, 1e-12), (False, 2e-6), (engine.PREC_FP32S, 2e-6)])
 @pytest.mark.parametrize("NKFFT", [(4, 3, 5), (2, 2, 2)])
 def test_r2k_fields(c2small, fp64, tol, NKFFT):
     s, o = c2small
@@ -73,7 +73,7 @@ def test_r2k_double_float_hamiltonian(c2small):
     assert maxrel(got[:, 0], ref) < 1e-13
 
 
-@pytest.mark.parametrize("prec", [engine.PREC_FP32, engine.PREC_FP64, engine.PREC_DF64])
+@pytest.mark.parametrize("prec", [engine.PREC_FP32, engine.PREC_FP64, engine.PREC_DF64, engine.PREC_FP32S])
 def test_r2k_columns_lower_triangle(c2small, prec):
     """wbg_r2k_columns on the lower triangle of the Hermitian fields: those elements are
     bit-identical to the full transform, the others (upper triangles) are left unwritten."""

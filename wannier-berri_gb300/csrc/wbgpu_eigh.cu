@@ -157,10 +157,13 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
-          CR acc = czero<CR>();
+          // two independent accumulators (row part / column part) for instruction-level parallelism
+          CR acc = czero<CR>(), acc2 = czero<CR>();
           const CR* Ai = Am + tri(i);
           for (int j = c + 1; j <= i; ++j) cfma(acc, Ai[j], vs[j]);
-          for (int j = i + 1; j < n; ++j) cfmac(acc, Am[tri(j) + i], vs[j]);
+          for (int j = i + 1, idx = tri(i + 1) + i; j < n; idx += j + 1, ++j) cfmac(acc2, Am[idx], vs[j]);
+          acc.x = acc.x + acc2.x;
+          acc.y = acc.y + acc2.y;
           const CR p = cmul(tau, acc);
           ws[i] = p;
           const CR v = vs[i];
@@ -302,7 +305,8 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 }
 
 // ---------------------------------------------------------------------------------------
-// 3. Eigenvectors: inverse iteration on T (real type R), clusters re-orthogonalised, U = Q Z.
+// 3. Eigenvectors: inverse iteration on T (real type R, two solves from a pseudo-random
+//    start), clusters re-orthogonalised, U = Q Z.
 // grid: ceil(nk/G) blocks of G*L threads; lane j computes eigenvectors j, j+L, ...
 // The back-transform by the Householder reflectors runs in precision TU, one reflector at a
 // time staged in shared memory for all lanes.  Shared memory per group: Z [n][n], d, e,
@@ -344,46 +348,50 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
   const R tiny = A::pivot_floor() * tnorm;
   const R ortol = A::from(1e-5) * tnorm;
   const R pertol = A::from(10.0) * A::eps() * tnorm;
-  R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX], u2[WBG_EIGH_NMAX], lm[WBG_EIGH_NMAX];
-  unsigned char piv[WBG_EIGH_NMAX];
+  // Per lane: reciprocal pivots and first super-diagonal of U (the only factors that cannot
+  // be rebuilt), a row-swap bitmask; the iterate lives in column j of Z.
+  R u0i[WBG_EIGH_NMAX], u1[WBG_EIGH_NMAX];
   for (int j = lane; j < n; j += L) {
     R shift = lam[j];
     for (int jj = j - 1; jj >= 0 && shift - lam[jj] < pertol; --jj) shift = lam[jj] + pertol * A::from((double)(j - jj));
-    // LU with partial pivoting of T - shift I; u0i holds reciprocal pivots
-    R ca = ds[0] - shift, cb = n > 1 ? es[0] : zero;
-    for (int i = 0; i < n - 1; ++i) {
-      const R ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : zero;
-      if (fabs(ca) >= fabs(ci)) {
-        if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
-        const R rc = one / ca;
-        const R mlt = ci * rc;
-        u0i[i] = rc; u1[i] = cb; u2[i] = zero; lm[i] = mlt; piv[i] = 0;
-        ca = ai1 - mlt * cb;
-        cb = bi1;
-      } else {
-        const R rc = one / ci;
-        const R mlt = ca * rc;
-        u0i[i] = rc; u1[i] = ai1; u2[i] = bi1; lm[i] = mlt; piv[i] = 1;
-        ca = cb - mlt * ai1;
-        cb = -mlt * bi1;
-      }
-    }
-    if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
-    u0i[n - 1] = one / ca;
     R* x = Zs + j;  // x[i * n]: column j of Z
     for (int i = 0; i < n; ++i) x[i * n] = A::from(hash_uniform((unsigned)j + 1u, (unsigned)i + 7u));
-    for (int it = 0; it < 3; ++it) {
-      R rp = x[0];
+    for (int it = 0; it < 2; ++it) {  // the second solve squares the contamination left by the first
+      // LU with partial pivoting of T - shift I, fused with x := L^{-1} P x.  Row i of U is
+      // (1/u0i[i], u1[i], u2[i]); u2[i] = e[i+1] after a row swap at step i, else 0.
+      unsigned int swp[(WBG_EIGH_NMAX + 31) / 32];
+      for (int w = 0; w < (n + 31) / 32; ++w) swp[w] = 0u;
+      R ca = ds[0] - shift, cb = n > 1 ? es[0] : zero, xc = x[0];
       for (int i = 0; i < n - 1; ++i) {
-        const R y1 = x[(i + 1) * n];
-        if (piv[i] == 0) { x[i * n] = rp; rp = y1 - lm[i] * rp; }
-        else { x[i * n] = y1; rp = rp - lm[i] * y1; }
+        const R ci = es[i], ai1 = ds[i + 1] - shift, bi1 = (i + 1 < n - 1) ? es[i + 1] : zero;
+        const R xn = x[(i + 1) * n];
+        if (fabs(ca) >= fabs(ci)) {
+          if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
+          const R rc = one / ca;
+          const R mlt = ci * rc;
+          u0i[i] = rc; u1[i] = cb;
+          x[i * n] = xc;
+          xc = xn - mlt * xc;
+          ca = ai1 - mlt * cb;
+          cb = bi1;
+        } else {
+          const R rc = one / ci;
+          const R mlt = ca * rc;
+          u0i[i] = rc; u1[i] = ai1;
+          swp[i >> 5] |= 1u << (i & 31);
+          x[i * n] = xn;
+          xc = xc - mlt * xn;
+          ca = cb - mlt * ai1;
+          cb = -mlt * bi1;
+        }
       }
-      R xi1 = rp * u0i[n - 1], xi2 = zero;  // x[i+1], x[i+2] of the back substitution
+      if (fabs(ca) < tiny) ca = ca >= zero ? tiny : -tiny;
+      R xi1 = xc / ca, xi2 = zero;  // x[i+1], x[i+2] of the back substitution
       x[(n - 1) * n] = xi1;
       R amax = fabs(xi1);
       for (int i = n - 2; i >= 0; --i) {
-        const R xi = (x[i * n] - u1[i] * xi1 - u2[i] * xi2) * u0i[i];
+        const R u2 = ((swp[i >> 5] >> (i & 31)) & 1u) && (i + 1 < n - 1) ? es[i + 1] : zero;
+        const R xi = (x[i * n] - u1[i] * xi1 - u2 * xi2) * u0i[i];
         x[i * n] = xi;
         amax = fmax(amax, fabs(xi));
         xi2 = xi1;

@@ -20,6 +20,7 @@
 //    transform to a subset of elements -- the lower triangle of fields that are Hermitian by
 //    construction, whose upper triangle the consumers mirror -- so the result is exactly
 //    Hermitian and costs about half.
+#include <type_traits>
 #include "wbgpu_common.cuh"
 #include "wbgpu_df64.cuh"
 #include "wbgpu_r2k.cuh"
@@ -29,11 +30,13 @@ namespace {
 constexpr int kThreads = 128;
 
 // ---------------- R-space weights (once per system + field set) ----------------
-// grid: (ceil(nR*nw2/256), nF); XR [nBase][nR][nw2]; iR [nR][3] (sorted order)
+// grid: (ceil(nR*nw2/256), nF); XR [nBase][nR][nw2]; iR [nR][3] (sorted order).
+// XFlo (split precision, T = float): the rounding residual XF_R - float(XF_R), so that the
+// k-independent R-space data carry 48 bits into the transform.
 template <typename T>
 __global__ void r2k_weights(const double2* __restrict__ XR, const int* __restrict__ iR, const int4* __restrict__ fdesc,
                             const double* __restrict__ wcc, R2KLattice lat, int nBase, int nR, int nw,
-                            typename C2<T>::t* __restrict__ XF) {
+                            typename C2<T>::t* __restrict__ XF, typename C2<T>::t* __restrict__ XFlo) {
   typedef typename C2<T>::t V;
   const int f = blockIdx.y;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -67,7 +70,10 @@ __global__ void r2k_weights(const double2* __restrict__ XR, const int* __restric
     v = cmuli(csub(cscale(Ab, w[al]), cscale(Aa, w[be])));
     if (fd.x == R2K_DROT) v = cmuli(cscale(v, w[fd.w]));  // derivative of the curl
   }
-  XF[((long long)f * nR + r) * nw2 + mn] = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
+  const typename C2<T>::t h = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
+  XF[((long long)f * nR + r) * nw2 + mn] = h;
+  if constexpr (std::is_same<T, float>::value)
+    if (XFlo) XFlo[((long long)f * nR + r) * nw2 + mn] = mkc<T>((T)(v.x - (double)h.x), (T)(v.y - (double)h.y));
 }
 
 // Column c of the launch -> (field, element).  cols == nullptr: all nF * nw2 columns.
@@ -98,8 +104,9 @@ WBG_D void contract(const typename C2<T>::t* x, int len, const typename C2<T>::t
 
 // ---------------- stage A: contract R2 inside each (R0,R1) pair ----------------
 // grid: (ceil(nF*nw2/kThreads), nP, nb); XF [nF][nR][nw2] -> Z [nb][nF][nP][N2][nw2]
-template <typename T, int MAXL>
+template <typename T, int MAXL, bool SPLIT>
 __global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* __restrict__ XF,
+                                                       const typename C2<T>::t* __restrict__ XFlo,
                                                        const int* __restrict__ pairStart, const int* __restrict__ r2,
                                                        const typename C2<T>::t* __restrict__ ph2,
                                                        typename C2<T>::t* __restrict__ Z, R2KGeom g, int nF,
@@ -113,20 +120,36 @@ __global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* 
   int f, mn;
   if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
   const int r0 = pairStart[p], len = pairStart[p + 1] - r0;
-  V x[MAXL];
+  V x[MAXL], xl[SPLIT ? MAXL : 1];
   int ri[MAXL];
 #pragma unroll
   for (int i = 0; i < MAXL; ++i) {
     if (i < len) {
       x[i] = XF[((long long)f * g.nR + r0 + i) * g.nw2 + mn];
+      if (SPLIT) xl[i] = XFlo[((long long)f * g.nR + r0 + i) * g.nw2 + mn];
       ri[i] = r2[r0 + i] - g.rmin2;
     } else {
       x[i] = czero<V>();
+      if (SPLIT) xl[i] = czero<V>();
       ri[i] = 0;
     }
   }
   V* out = Z + ((((long long)blk * nF + f) * g.nP + p) * g.N2) * g.nw2 + mn;
-  contract<T, MAXL>(x, len, tab, ri, g.nr2, g.N2, out, g.nw2);
+  if (SPLIT) {  // sum_R tab (XF + XFlo): the residual products accumulate separately
+    for (int j = 0; j < g.N2; ++j) {
+      V acc = czero<V>(), accl = czero<V>();
+#pragma unroll
+      for (int i = 0; i < MAXL; ++i)
+        if (i < len) {
+          const V t = tab[j * g.nr2 + ri[i]];
+          cfma(acc, t, x[i]);
+          cfma(accl, t, xl[i]);
+        }
+      out[(long long)j * g.nw2] = cadd(acc, accl);
+    }
+  } else {
+    contract<T, MAXL>(x, len, tab, ri, g.nr2, g.N2, out, g.nw2);
+  }
 }
 
 // ---------------- stage B: contract R1 inside each R0 slice ----------------
@@ -198,13 +221,17 @@ __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* 
 }
 
 template <typename T, int MAXL>
-void launch_stages(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart,
+void launch_stages(const void* XF, const void* XFlo, int nF, const int* pairStart, const int* r2, const int* sliceStart,
                    const int* pairR1, const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z,
                    void* Y, void* out, const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   typedef typename C2<T>::t V;
   const unsigned colBlocks = (unsigned)((ncols + kThreads - 1) / kThreads);
-  r2k_stageA<T, MAXL><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
-      (const V*)XF, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
+  if (XFlo)
+    r2k_stageA<T, MAXL, true><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
+        (const V*)XF, (const V*)XFlo, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
+  else
+    r2k_stageA<T, MAXL, false><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
+        (const V*)XF, nullptr, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
   r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, (size_t)g.N1 * g.nr1 * sizeof(V), stream>>>(
       (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF, cols, ncols);
   r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, (size_t)g.N0 * g.nr0 * sizeof(V), stream>>>(
@@ -212,21 +239,21 @@ void launch_stages(const void* XF, int nF, const int* pairStart, const int* r2, 
 }
 
 template <typename T>
-int launch_r2k(const void* XF, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
+int launch_r2k(const void* XF, const void* XFlo, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z, void* Y, void* out,
                const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   const int maxlen = max(max(g.maxPairLen, g.maxSliceLen), g.nU);
   if (maxlen <= 8)
-    launch_stages<T, 8>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 8>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= 16)
-    launch_stages<T, 16>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 16>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= 24)
-    launch_stages<T, 24>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 24>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= WBG_R2K_MAXLEN)
-    launch_stages<T, WBG_R2K_MAXLEN>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
+    launch_stages<T, WBG_R2K_MAXLEN>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
                                      nb, cols, ncols, stream);
   else
     return WBG_ERR_SIZE;
@@ -236,7 +263,7 @@ int launch_r2k(const void* XF, int nF, const int* pairStart, const int* r2, cons
 }  // namespace
 
 size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int prec) {
-  const size_t cs = prec ? 16 : 8;
+  const size_t cs = (prec == 1 || prec == 2) ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   const size_t y = (size_t)nb * nF * g->nU * g->N1 * g->N2 * g->nw2 * cs;
   return ((z + 255) / 256) * 256 + y;
@@ -248,16 +275,16 @@ int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, i
     return WBG_ERR_ARG;
   const long long n = (long long)nR * nw * nw;
   dim3 grid((unsigned)((n + 255) / 256), nF);
-  if (prec < 0 || prec > 2) return WBG_ERR_ARG;
+  if (prec < 0 || prec > 3) return WBG_ERR_ARG;
   if (prec == 1)
     r2k_weights<double><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
-                                                  (double2*)XF);
+                                                  (double2*)XF, nullptr);
   else if (prec == 2)
     r2k_weights<df64><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
-                                                (cdf*)XF);
-  else
+                                                (cdf*)XF, nullptr);
+  else  // prec 3: residuals right after the rounded values
     r2k_weights<float><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
-                                                 (float2*)XF);
+                                                 (float2*)XF, prec == 3 ? (float2*)XF + n * nF : nullptr);
   return wbg_cuda_status(cudaGetLastError());
 }
 
@@ -265,22 +292,23 @@ int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, con
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
                 size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, const int* cols, int ncols,
                 cudaStream_t stream) {
-  if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 2) return WBG_ERR_ARG;
+  if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 3) return WBG_ERR_ARG;
   if (!cols) ncols = nF * g->nw2;
   if (ncols < 1 || ncols > nF * g->nw2) return WBG_ERR_ARG;
   if (g->nw2 != g->nw * g->nw || g->nk != g->N0 * g->N1 * g->N2) return WBG_ERR_ARG;
   if (g->nU < 1 || g->nP < 1 || g->maxPairLen < 1 || g->maxSliceLen < 1) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, prec)) return WBG_ERR_WORKSPACE;
-  const size_t cs = prec ? 16 : 8;
+  const size_t cs = (prec == 1 || prec == 2) ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   char* Z = (char*)workspace;
   char* Y = Z + ((z + 255) / 256) * 256;
   if (prec == 1)
-    return launch_r2k<double>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+    return launch_r2k<double>(XF, nullptr, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                               cols, ncols, stream);
   if (prec == 2)
-    return launch_r2k<df64>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+    return launch_r2k<df64>(XF, nullptr, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                             cols, ncols, stream);
-  return launch_r2k<float>(XF, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
+  const void* XFlo = prec == 3 ? (const void*)((const float2*)XF + (size_t)nF * g->nR * g->nw2) : nullptr;
+  return launch_r2k<float>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                            cols, ncols, stream);
 }

@@ -331,7 +331,10 @@ def r2k_geometry(dev, NKFFT):
                         maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
 
 
-PREC_FP32, PREC_FP64, PREC_DF64 = 0, 1, 2
+PREC_FP32, PREC_FP64, PREC_DF64, PREC_FP32S = 0, 1, 2, 3
+# PREC_FP32S: FP32 transform whose k-independent R-space inputs carry a rounding residual
+# (hi + lo pair), so they enter with 48 bits; output, intermediates and phases as PREC_FP32.
+C64_PRECS = (PREC_FP32, PREC_FP32S)
 EIGH_LOWER = 4  # wbg_eigh_batched mode bit: H given by its lower triangle
 
 
@@ -356,7 +359,7 @@ def _df64_pairs(z):
 
 def _complex_tensor(shape, prec, device):
     """storage for complex values of precision prec (double-float uses complex128-sized slots)"""
-    return torch.empty(shape, dtype=torch.complex64 if prec == PREC_FP32 else torch.complex128, device=device)
+    return torch.empty(shape, dtype=torch.complex64 if prec in C64_PRECS else torch.complex128, device=device)
 
 
 def field_arrays(dev, quantities, with_H, prec):
@@ -374,7 +377,7 @@ def field_arrays(dev, quantities, with_H, prec):
         for i, v in enumerate(dev.lattice.reshape(-1)):
             lat.L[i] = float(v)
         fd = torch.tensor(np.array(desc, dtype=np.int32).reshape(-1), dtype=torch.int32, device=dev.device)
-        XF = _complex_tensor((len(desc), nR, nw * nw), prec, dev.device)
+        XF = _complex_tensor(((2 if prec == PREC_FP32S else 1) * len(desc), nR, nw * nw), prec, dev.device)
         st = _lib.load().wbg_r2k_fields(_ptr(X), len(names), _ptr(dev.geom_tensors()['iR']), nR, nw, _ptr(fd),
                                         len(desc), _ptr(dev.wcc_tensor(True)), ctypes.byref(lat), prec, _ptr(XF),
                                         _stream())
@@ -419,7 +422,7 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, pha
             ph.append(host.to(dev.device, non_blocking=True))
             ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
-    name = {PREC_FP32: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
+    name = {PREC_FP32: 'r2k_fp32', PREC_FP32S: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
     common = (_ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
               _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, prec, _ptr(workspace),
               ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
@@ -495,7 +498,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
 
     def fields_for(q, with_H, prec, name, lower=False):
         _, _, nF, _ = field_arrays(dev, q, with_H, prec)
-        out = dev.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec == PREC_FP32 else torch.complex128)
+        out = dev.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec in C64_PRECS else torch.complex128)
         geo = r2k_geometry(dev, NKFFT)
         ws = ctypes.c_size_t(0)
         _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(ws)),
@@ -520,7 +523,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         keep.append(k0)
         U = dev.buffer('U32', (nkt, nw, nw), torch.complex64)
         E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | EIGH_LOWER, work=ework, flag=flag)
-        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32, 'fields', lower=True)
+        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True)
         keep.append(k1)
         lower_in = column_list(dev, quantities, False, True)[1]
         fp64_fields = False

@@ -24,7 +24,7 @@ def choose_batch(nw, nk, nblocks, quantities, precision, max_kpoints=1 << 17, bu
 def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, device='cuda', dev_system=None,
         blocks=None, **_ignored):
     """Integrate ``calculators`` over ``grid``.  precision: 'fp64' (plain) or 'mixed'
-    (FP64 H(k) + eigh + scan, FP32 fields and rotations).  ``blocks`` restricts the
+    (double-float H(k) and eigh, FP64 scan, FP32 fields and rotations).  ``blocks`` restricts the
     run to a subset of the division-grid K-points (indices into Grid.block_shifts());
     the result then carries the same 1/prod(NKdiv) weight per block."""
     engine.require_cuda()
@@ -39,7 +39,7 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
         shifts = shifts[np.asarray(blocks)]
     nk = grid.nk_per_block
     nb = blocks_per_batch or choose_batch(dev.nw, nk, len(shifts), quantities, precision)
-    precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32]
+    precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
     for i0 in range(0, len(shifts), nb):
         bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
