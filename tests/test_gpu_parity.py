@@ -189,8 +189,36 @@ def test_rotate_tensor_core_vs_fp64(nF, lower):
         assert err < 2e-6 * scale, (f, m, err / scale)
 
 
+@pytest.mark.parametrize("fp64", [True, False])
+@pytest.mark.parametrize("nw", [72, 96, 128])
+def test_rotate_large_nw(fp64, nw):
+    """Row-panel rotation (nw > 64) against numpy: plain, Hermitian part, diagonal only, and a
+    lower-triangle input; FP64 to 1e-12, FP32 to 2e-6 of max |Xbar|."""
+    rng = np.random.default_rng(nw)
+    nk, nF = 6, 4
+    X = rng.standard_normal((nk, nF, nw, nw)) + 1j * rng.standard_normal((nk, nF, nw, nw))
+    X[:, 3] = X[:, 3] + X[:, 3].conj().swapaxes(-1, -2)
+    U = np.linalg.qr(rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw)))[0]
+    U = np.ascontiguousarray(U)
+    cdt = torch.complex128 if fp64 else torch.complex64
+    Xl = X.copy()
+    iu = np.triu_indices(nw, 1)
+    Xl[:, 3][:, iu[0], iu[1]] = np.nan
+    got, _ = engine.rotate(torch.from_numpy(U).to(cdt).cuda(), torch.from_numpy(Xl).to(cdt).cuda(), nF,
+                           [0, 1, 2, 3], [0, 1, 2, 5], nw, nk, fp64)
+    got = got.cpu().numpy().astype(np.complex128)
+    Y = U.conj().swapaxes(-1, -2)[:, None] @ X @ U[:, None]
+    H = 0.5 * (Y + Y.conj().swapaxes(-1, -2))
+    tol = (1e-12 if fp64 else 2e-6) * np.abs(Y).max()
+    d = np.arange(nw)
+    assert np.abs(got[:, 0] - Y[:, 0]).max() < tol
+    assert np.abs(got[:, 1] - H[:, 1]).max() < tol
+    assert np.abs(got[:, 2][:, d, d].real - H[:, 2][:, d, d].real).max() < tol
+    assert np.abs(got[:, 3] - H[:, 3]).max() < tol
+
+
 @pytest.mark.parametrize("mode", [1, 0, 2])
-@pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48])
+@pytest.mark.parametrize("nw", [1, 2, 5, 8, 17, 32, 48, 96, 128])
 def test_eigh_random(nw, mode):
     """mode 1: FP64; mode 0: FP64 solve + FP32 vectors; mode 2: double-float solve + FP32 vectors.
     Energies to 1e-12 |E| nw in every mode; vectors to FP64 or FP32 accuracy."""
@@ -216,8 +244,9 @@ def test_eigh_random(nw, mode):
     scale = np.abs(Eref).max()
     assert np.max(np.abs(E - Eref)) < 1e-12 * max(scale, 1) * nw
     I = np.eye(nw)
-    assert np.max(np.abs(np.einsum('kmi,kmj->kij', U.conj(), U) - I)) < vtol
-    R = np.einsum('kmi,kmn,knj->kij', U.conj(), Href, U) - E[:, None, :] * I
+    Uh = U.conj().swapaxes(1, 2)
+    assert np.max(np.abs(Uh @ U - I)) < vtol
+    R = Uh @ Href @ U - E[:, None, :] * I
     assert np.max(np.abs(R)) < 0.1 * vtol * max(scale, 1) * nw
 
 
@@ -333,3 +362,41 @@ def test_ahc_morb_bcd_together(c2small):
                                           'bcd': O.BerryDipole_FermiSea(Efermi=EF)})
     for key in ('ahc', 'morb', 'bcd'):
         assert maxrel(res[key].data, ref[key].data) < 1e-5, key
+
+
+@pytest.fixture(scope="module")
+def tb128():
+    d = models.random_tb(128, 1, models.triclinic_lattice(np.random.default_rng(3)), 1.5, 4128, centers='random',
+                         keys=('Ham', 'AA'))
+    return wsys.System_R.from_dict(d)
+
+
+def test_bcd_large_nw_without_gap_table(tb128):
+    """nw = 128, FP64: 2201 Fermi levels leave no room for the per-k 1/(E_x - E_y) table, so the
+    kernel recomputes it; every 220th level must equal an 11-level run that uses the table."""
+    s = tb128
+    grid = wbgpu.Grid(s, NKdiv=1, NKFFT=2)
+    ef1, ef2 = np.linspace(-1, 1, 11), np.linspace(-1, 1, 2201)
+    r1 = wbgpu.run(s, grid, {'b': wbgpu.calculators.BerryDipole_FermiSea(Efermi=ef1)}, precision='fp64')['b'].data
+    r2 = wbgpu.run(s, grid, {'b': wbgpu.calculators.BerryDipole_FermiSea(Efermi=ef2)}, precision='fp64')['b'].data
+    assert np.abs(r2[::220] - r1).max() < 1e-10 * np.abs(r1).max()
+
+
+@pytest.mark.parametrize("nw", [96, 128])
+def test_mixed_vs_fp64_large_nw(nw, tb128):
+    """Large-nw paths (panel rotation, eigh at n = 96 / 128, Kubo) in mixed precision against FP64."""
+    if nw == 128:
+        s = tb128
+    else:
+        d = models.random_tb(96, 1, models.triclinic_lattice(np.random.default_rng(4)), 1.5, 4096, centers='random',
+                             keys=('Ham', 'AA'))
+        s = wsys.System_R.from_dict(d)
+    grid = wbgpu.Grid(s, NKdiv=1, NKFFT=4)
+    calcs = lambda: {'ahc': wbgpu.calculators.AHC(Efermi=np.linspace(-1, 1, 21)),
+                     'opt': wbgpu.calculators.OpticalConductivity(Efermi=np.linspace(-1, 1, 3),
+                                                                  omega=np.linspace(0.1, 2, 16))}
+    a = wbgpu.run(s, grid, calcs(), precision='mixed')
+    b = wbgpu.run(s, grid, calcs(), precision='fp64')
+    for key in ('ahc', 'opt'):
+        x, y = a[key].data, b[key].data
+        assert np.abs(x - y).max() < 2e-5 * np.abs(y).max(), (key, np.abs(x - y).max() / np.abs(y).max())

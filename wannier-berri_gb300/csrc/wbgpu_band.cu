@@ -236,6 +236,127 @@ template <> struct TraceSum<float> {
 };
 
 // ---------------------------------------------------------------------------------------
+// Row-panel rotation for large nw (the per-k matrices do not fit in shared memory together).
+// CTA = (row panel p of RP rows, field f, k-point): W = U[:, panel]^dagger Xh  (RP x nw), then
+// Y[panel, :] = W U, with Xh and U streamed through shared memory in chunks of KC rows.
+// Hermitian-part fields (herm 1, 2) are symmetrised on input, Xh = (X + X^dagger)/2 -- the
+// same Hermitian part (U^dagger X U + its adjoint)/2 -- and lower-triangle inputs (bit 2)
+// are mirrored; herm 2 writes the real diagonal only.  Threads own 4 x 4 output tiles.
+// ---------------------------------------------------------------------------------------
+constexpr int PANEL_RP = 32, PANEL_KC = 16;
+
+template <typename V>
+WBG_D V herm_in(const V* src, int i, int j, int nw, int mode) {  // element (i, j) of the rotated input
+  if (mode == 2) return load_field(src, i * nw + j, nw, true);     // lower triangle, mirrored
+  if (mode == 1) {                                                  // Hermitian part
+    const V a = src[i * nw + j], b = src[j * nw + i];
+    V r; r.x = (a.x + b.x) * 0.5f; r.y = (a.y - b.y) * 0.5f;
+    return r;
+  }
+  return src[i * nw + j];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __restrict__ U, long long strideU,
+                                                    const typename C2<T>::t* __restrict__ X, int nFin,
+                                                    const int* __restrict__ fsel, const int* __restrict__ herm,
+                                                    int nFrot, typename C2<T>::t* __restrict__ Xbar, int nw, int nk) {
+  typedef typename C2<T>::t V;
+  extern __shared__ unsigned char smp[];
+  const int np = (nw + PANEL_RP - 1) / PANEL_RP;
+  const long long b = blockIdx.x;
+  const int p = (int)(b % np), f = (int)((b / np) % nFrot);
+  const long long k = b / ((long long)np * nFrot);
+  if (k >= nk) return;
+  const int r0 = p * PANEL_RP;
+  const int ldw = nw + 1;
+  V* Ws = reinterpret_cast<V*>(smp);        // [RP][nw+1]
+  V* Cs = Ws + PANEL_RP * ldw;               // [KC][nw] chunk of Xh (phase 1) or U (phase 2)
+  V* Us = Cs + PANEL_KC * nw;                // [KC][RP] chunk of U[:, panel]
+  const int tx = threadIdx.x % ((nw + 3) / 4), ty = threadIdx.x / ((nw + 3) / 4);  // ty < RP/4
+  const int fs = fsel[f];
+  const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
+  const int hm = herm[f];
+  const int inmode = (hm & 4) ? 2 : ((hm & 3) != 0 ? 1 : 0);
+  const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw * nw;
+  const V* Uk = U + k * strideU;
+  const T nan = T(0) / T(0);
+  V acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = czero<V>();
+  // phase 1: W[a][j] = sum_i conj(U[i][r0 + a]) Xh[i][j]
+  for (int i0 = 0; i0 < nw; i0 += PANEL_KC) {
+    for (int e = threadIdx.x; e < PANEL_KC * nw; e += blockDim.x) {
+      const int ii = e / nw, j = e % nw, i = i0 + ii;
+      Cs[e] = i < nw ? (fok ? herm_in(src, i, j, nw, inmode) : mkc<T>(nan, nan)) : czero<V>();
+    }
+    for (int e = threadIdx.x; e < PANEL_KC * PANEL_RP; e += blockDim.x) {
+      const int ii = e / PANEL_RP, a = e % PANEL_RP, i = i0 + ii;
+      Us[e] = (i < nw && r0 + a < nw) ? Uk[i * nw + r0 + a] : czero<V>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ii = 0; ii < PANEL_KC; ++ii) {
+      V ua[4], xb[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) ua[a] = Us[ii * PANEL_RP + 4 * ty + a];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) xb[c] = (4 * tx + c < nw) ? Cs[ii * nw + 4 * tx + c] : czero<V>();
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) cfmac(acc[a][c], ua[a], xb[c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if (4 * tx + c < nw) Ws[(4 * ty + a) * ldw + 4 * tx + c] = acc[a][c];
+      acc[a][c] = czero<V>();
+    }
+  __syncthreads();
+  // phase 2: Y[r0 + a][n] = sum_j W[a][j] U[j][n]
+  for (int j0 = 0; j0 < nw; j0 += PANEL_KC) {
+    for (int e = threadIdx.x; e < PANEL_KC * nw; e += blockDim.x) {
+      const int jj = e / nw, n = e % nw, j = j0 + jj;
+      Cs[e] = j < nw ? Uk[j * nw + n] : czero<V>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < PANEL_KC; ++jj) {
+      if (j0 + jj >= nw) break;
+      V wa[4], ub[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) wa[a] = Ws[(4 * ty + a) * ldw + j0 + jj];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ub[c] = (4 * tx + c < nw) ? Cs[jj * nw + 4 * tx + c] : czero<V>();
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) cfma(acc[a][c], wa[a], ub[c]);
+    }
+    __syncthreads();
+  }
+  V* dst = Xbar + (k * nFrot + f) * (long long)nw * nw;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int m = r0 + 4 * ty + a, n = 4 * tx + c;
+      if (m >= nw || n >= nw) continue;
+      if ((hm & 3) == 2) {
+        if (m == n) dst[m * nw + n] = mkc<T>(acc[a][c].x, (T)0);
+      } else {
+        dst[m * nw + n] = acc[a][c];
+      }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // Fused Omega traces + Fermi-level histogram.
 // grid: persistent blocks of G*L threads; each group of L lanes takes one k-point at a time.
 // Xbar layout: [k][nFbar][nw][nw]; V at iV..iV+2, A at iA..iA+2, O(rotAA) at iO..iO+2.
@@ -537,15 +658,15 @@ __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C
 template <typename T>
 __global__ void berry_deromega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar,
                                       int nFbar, int iV, int iA, int iO, int iW, int idA, int idO, int nw, int nk,
-                                      int L, int G, WbgScan sp, int internal_terms, int external_terms,
+                                      int L, int G, int table, WbgScan sp, int internal_terms, int external_terms,
                                       double* __restrict__ hist) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][9]
   double* Es = sh + 9 * sp.nEF;                       // [G][nw]
   double* tv = Es + G * nw;                           // [G][nw][9]
-  T* dinvS = reinterpret_cast<T*>(tv + 9 * G * nw);   // [G][nw][nw]
-  int* start = reinterpret_cast<int*>(dinvS + (size_t)G * nw * nw);  // [G][nw]
+  T* dinvS = reinterpret_cast<T*>(tv + 9 * G * nw);   // [G][nw][nw] when table != 0
+  int* start = reinterpret_cast<int*>(dinvS + (table ? (size_t)G * nw * nw : 0));  // [G][nw]
   for (int i = threadIdx.x; i < 9 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
@@ -561,11 +682,12 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
     for (int i = lane; i < nw; i += L) myE[i] = E[kk * nw + i];
     __syncwarp();
     for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
-    for (int idx = lane; idx < nw * nw; idx += L) {  // dinv(x, y) = 1/(E_x - E_y), 0 below 1e-7
-      const int x = idx / nw, y = idx % nw;
-      const double dE = myE[x] - myE[y];
-      myDinv[idx] = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
-    }
+    if (table)
+      for (int idx = lane; idx < nw * nw; idx += L) {  // dinv(x, y) = 1/(E_x - E_y), 0 below 1e-7
+        const int x = idx / nw, y = idx % nw;
+        const double dE = myE[x] - myE[y];
+        myDinv[idx] = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+      }
     __syncwarp();
     int below = 0, f0 = nw;
     for (int n = lane; n < nw; n += L) {
@@ -586,7 +708,13 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
 #define XW(a, b, x, y) Xk[(iW + 3 * (a) + (b)) * nw2 + (x) * nw + (y)]
 #define XdA(b, d, x, y) Xk[(idA + 3 * (b) + (d)) * nw2 + (x) * nw + (y)]
 #define XdO(c, d, x, y) Xk[(idO + 3 * (c) + (d)) * nw2 + (x) * nw + (y)]
-#define DV(a, x, y) cscale(XV(a, x, y), -myDinv[(x) * nw + (y)])
+    // 1/(E_x - E_y) from the table, or recomputed when the table does not fit in shared memory
+    auto dinv = [&](int x, int y) -> T {
+      if (table) return myDinv[x * nw + y];
+      const double dE = myE[x] - myE[y];
+      return fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+    };
+#define DV(a, x, y) cscale(XV(a, x, y), -dinv((x), (y)))
     for (int m = lane; m < nw; m += L) {
       int gs = m, ge = m + 1;
       while (!myS[gs]) --gs;
@@ -599,7 +727,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
       if (ingroup) {
         for (int l = 0; l < nw; ++l) {
           if (l >= gs && l < ge) continue;
-          const T dlm = myDinv[l * nw + m];  // 1/(E_l - E_m)
+          const T dlm = dinv(l, m);  // 1/(E_l - E_m)
           V dDlm[9], dDml[9], dAlm[9];
           for (int i = 0; i < 9; ++i) { dDlm[i] = czero<V>(); dDml[i] = czero<V>(); dAlm[i] = czero<V>(); }
           for (int p = 0; p < nw; ++p) {
@@ -609,7 +737,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
             for (int a = 0; a < 3; ++a) { Vlp[a] = XV(a, l, p); Vpm[a] = XV(a, p, m); Vmp[a] = XV(a, m, p); Vpl[a] = XV(a, p, l); }
             if (!inG) {
               // dD_lm: + V^b_lp D^d_pm ; dD_ml: - D^a_mp V^d_pl ; dA_lm: + A^b_lp D^d_pm
-              const T dpm = myDinv[p * nw + m], dmp = myDinv[m * nw + p];
+              const T dpm = dinv(p, m), dmp = dinv(m, p);
               V Dpm[3], Dmp[3], Alp[3];
 #pragma unroll
               for (int a = 0; a < 3; ++a) {
@@ -627,7 +755,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
                 }
             } else {
               // dD_lm: - D^b_lp V^d_pm ; dD_ml: + V^a_mp D^d_pl ; dA_lm: - D^d_lp A^b_pm
-              const T dlp = myDinv[l * nw + p], dpl = myDinv[p * nw + l];
+              const T dlp = dinv(l, p), dpl = dinv(p, l);
               V Dlp[3], Dpl[3], Apm[3];
 #pragma unroll
               for (int a = 0; a < 3; ++a) {
@@ -645,7 +773,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
                 }
             }
           }
-          const T dml = myDinv[m * nw + l];  // 1/(E_m - E_l)
+          const T dml = dinv(m, l);  // 1/(E_m - E_l)
           // symmetrise in (b, d) (the bracket is symmetric, W = d_b d_d H too) and scale
 #pragma unroll
           for (int b = 0; b < 3; ++b)
@@ -802,6 +930,18 @@ template <typename T>
 int launch_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                   int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
   typedef typename C2<T>::t V;
+  if (nw > 64) {  // row panels: the per-k matrices no longer fit in shared memory together
+    if (nw > 4 * 256 / (PANEL_RP / 4)) return WBG_ERR_SIZE;  // threads = (RP/4) * ceil(nw/4) <= 256
+    const int np = (nw + PANEL_RP - 1) / PANEL_RP;
+    const int threads = (PANEL_RP / 4) * ((nw + 3) / 4);
+    const size_t sm = ((size_t)PANEL_RP * (nw + 1) + (size_t)PANEL_KC * nw + PANEL_KC * PANEL_RP) * sizeof(V);
+    const long long blocks = (long long)np * nFrot * nk;
+    if (sm > 220 * 1024 || blocks > 0x7fffffffll) return WBG_ERR_SIZE;
+    cudaFuncSetAttribute(rotate_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    rotate_panel<T><<<(unsigned)blocks, threads, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm,
+                                                               nFrot, (V*)Xbar, nw, nk);
+    return wbg_cuda_status(cudaGetLastError());
+  }
   if (nw % 4 == 0 && nw >= 8) {
     const int tpk = (nw / 4) * (nw / 4);
     const size_t per_k = ((size_t)nw * nw * 2 + (size_t)nw * (nw + 1)) * sizeof(V);
@@ -903,10 +1043,15 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
     return WBG_ERR_ARG;
   if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   const int L = lanes_for(nw);
-  const int G = 64 / L > 0 ? 64 / L : 1;
+  int G = 64 / L > 0 ? 64 / L : 1;
   const size_t tsz = fp64 ? 8 : 4;
-  const size_t sm = 9 * (size_t)sp->nEF * 8 + (size_t)G * nw * 8 + (size_t)G * nw * 72 + (size_t)G * nw * nw * tsz +
-                    (size_t)G * nw * 4;
+  auto smem = [&](int g, int table) {
+    return 9 * (size_t)sp->nEF * 8 + (size_t)g * nw * (8 + 72 + 4) + (table ? (size_t)g * nw * nw * tsz : 0);
+  };
+  int table = 1;  // k-point groups per block shrink before the 1/dE table is dropped
+  while (G > 1 && smem(G, 1) > 220 * 1024) G /= 2;
+  if (smem(G, 1) > 220 * 1024) table = 0;
+  const size_t sm = smem(G, table);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -916,12 +1061,12 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
   if (fp64) {
     cudaFuncSetAttribute(berry_deromega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iW,
-                                                                    idA, idO, nw, nk, L, G, *sp, internal_terms,
+                                                                    idA, idO, nw, nk, L, G, table, *sp, internal_terms,
                                                                     external_terms, hist);
   } else {
     cudaFuncSetAttribute(berry_deromega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA,
-                                                                   idO, nw, nk, L, G, *sp, internal_terms,
+                                                                   idO, nw, nk, L, G, table, *sp, internal_terms,
                                                                    external_terms, hist);
   }
   return wbg_cuda_status(cudaGetLastError());

@@ -321,7 +321,8 @@ constexpr bool kUOverlaysZ = sizeof(typename C2<TU>::t) == sizeof(R);
 template <typename R, typename TU>
 __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const typename C2<TU>::t* __restrict__ tauIn,
                              const R* __restrict__ dIn, const R* __restrict__ eIn, const double* __restrict__ E, int n,
-                             int nk, int L, int G, typename C2<TU>::t* __restrict__ Uout, long long strideU) {
+                             int nk, int L, int G, int CW, typename C2<TU>::t* __restrict__ Uout,
+                             long long strideU) {
   typedef typename C2<TU>::t VU;
   typedef Arith<R> A;
   extern __shared__ unsigned char smv[];
@@ -330,14 +331,14 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
   const bool valid = k < nk;
   if (!valid) k = nk - 1;
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
-  const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
+  const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * CW * sizeof(VU) + 15) / 16 * 16;
   const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
   unsigned char* gbase = smv + (size_t)grp * (zbytes + ubytes + vbytes);
   R* Zs = reinterpret_cast<R*>(gbase);  // Z(i,j) = Zs[i*n + j]
   R* ds = Zs + n * n;
   R* es = ds + n;
   R* lam = es + n;
-  VU* Us = kUOverlaysZ<R, TU> ? reinterpret_cast<VU*>(gbase) : reinterpret_cast<VU*>(gbase + zbytes);  // [i][j]
+  VU* Us = kUOverlaysZ<R, TU> ? reinterpret_cast<VU*>(gbase) : reinterpret_cast<VU*>(gbase + zbytes);  // [i][j-c0]
   VU* vsh = reinterpret_cast<VU*>(gbase + zbytes + ubytes);
   for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = A::from(E[k * n + i]); }
   __syncwarp();
@@ -432,33 +433,40 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
       __syncwarp();
     }
   }
-  // back-transform: u = H_0 H_1 ... H_{n-2} z  (precision TU)
-  for (int j = lane; j < n; j += L)
-    for (int i = 0; i < n; ++i) Us[i * n + j] = mkc<TU>(to_tu<TU>(Zs[i * n + j]), (TU)0);
-  for (int c = n - 2; c >= 0; --c) {
-    // every lane passes the same __syncwarp calls: groups sharing a warp have different tau
-    const VU tau = tauIn[k * n + c];
-    const bool act = (tau.x != (TU)0 || tau.y != (TU)0);
-    for (int i = c + 1 + lane; i < n; i += L) vsh[i] = Vh[(k * n + c) * n + i];
-    __syncwarp();
-    if (act)
-      for (int j = lane; j < n; j += L) {
-        VU sacc = czero<VU>();
-        for (int i = c + 1; i < n; ++i) cfmac(sacc, vsh[i], Us[i * n + j]);
-        const VU ts = cmul(tau, sacc);
-        for (int i = c + 1; i < n; ++i) {
-          VU u = Us[i * n + j];
-          const VU vv = vsh[i];
-          u.x -= vv.x * ts.x - vv.y * ts.y;
-          u.y -= vv.x * ts.y + vv.y * ts.x;
-          Us[i * n + j] = u;
+  // back-transform: u = H_0 H_1 ... H_{n-2} z  (precision TU), in chunks of CW columns (every
+  // column is independent; CW < n only when a full U does not fit in shared memory)
+  for (int c0 = 0; c0 < n; c0 += CW) {
+    const int cw = min(CW, n - c0);
+    for (int jj = lane; jj < cw; jj += L)
+      for (int i = 0; i < n; ++i) Us[i * CW + jj] = mkc<TU>(to_tu<TU>(Zs[i * n + c0 + jj]), (TU)0);
+    for (int c = n - 2; c >= 0; --c) {
+      // every lane passes the same __syncwarp calls: groups sharing a warp have different tau
+      const VU tau = tauIn[k * n + c];
+      const bool act = (tau.x != (TU)0 || tau.y != (TU)0);
+      for (int i = c + 1 + lane; i < n; i += L) vsh[i] = Vh[(k * n + c) * n + i];
+      __syncwarp();
+      if (act)
+        for (int jj = lane; jj < cw; jj += L) {
+          VU sacc = czero<VU>();
+          for (int i = c + 1; i < n; ++i) cfmac(sacc, vsh[i], Us[i * CW + jj]);
+          const VU ts = cmul(tau, sacc);
+          for (int i = c + 1; i < n; ++i) {
+            VU u = Us[i * CW + jj];
+            const VU vv = vsh[i];
+            u.x -= vv.x * ts.x - vv.y * ts.y;
+            u.y -= vv.x * ts.y + vv.y * ts.x;
+            Us[i * CW + jj] = u;
+          }
         }
+      __syncwarp();
+    }
+    if (valid)
+      for (int idx = lane; idx < n * cw; idx += L) {
+        const int i = idx / cw, jj = idx % cw;
+        Uout[k * strideU + i * n + c0 + jj] = Us[i * CW + jj];
       }
     __syncwarp();
   }
-  __syncwarp();
-  if (valid)
-    for (int idx = lane; idx < n * n; idx += L) Uout[k * strideU + idx] = Us[idx];
 }
 
 int lanes_for(int n) {
@@ -511,14 +519,16 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   cudaFuncSetAttribute(eigh_ql<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_ql<R><<<(nk + BQ - 1) / BQ, BQ, smQ, stream>>>(d, e, n, nk, (double*)E, errflag);
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
-  const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * n * sizeof(VU) + 15) / 16 * 16;
   const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
-  const size_t smV = zbytes + ubytes + vbytes;
+  int CW = n;  // back-transform chunk width: the whole U unless it does not fit next to Z
+  auto ub = [&](int cw) { return kUOverlaysZ<R, TU> ? (size_t)0 : ((size_t)n * cw * sizeof(VU) + 15) / 16 * 16; };
+  if (!kUOverlaysZ<R, TU> && zbytes + ub(n) + vbytes > kMaxBlockSmem) CW = 32;
+  const size_t smV = zbytes + ub(CW) + vbytes;
   const int GV = pick_group(smV, L, 64 / L);
   if (GV == 0) return WBG_ERR_SIZE;
   cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_vectors<R, TU><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
-                                                                        (VU*)U, strideU);
+                                                                        CW, (VU*)U, strideU);
   return wbg_cuda_status(cudaGetLastError());
 }
 
