@@ -7,7 +7,9 @@ through the C ABI of libwbgpu.so (include/wbgpu.h).
 from .system import System_R
 from .grid import Grid
 from .run import run
-from . import calculators, models, engine
+from . import calculators, models, engine, serve
 from .result import EnergyResult, ResultDict
+from .serve import Server, run_many
 
-__all__ = ['System_R', 'Grid', 'run', 'calculators', 'models', 'engine', 'EnergyResult', 'ResultDict']
+__all__ = ['System_R', 'Grid', 'run', 'calculators', 'models', 'engine', 'serve', 'Server', 'run_many', 'EnergyResult',
+           'ResultDict']

@@ -136,6 +136,32 @@ def host_pinned(system, key, order):
     return cache[key]
 
 
+class Workspace:
+    """Grow-only arena of named device buffers.  Every batch of a run reuses the same buffers
+    (stream order makes that safe); concurrent runs on different streams use separate
+    workspaces."""
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self._bufs = {}
+
+    def buffer(self, name, shape, dtype):
+        """Buffer `name` viewed as dtype[shape], grown when too small (old contents dropped)."""
+        nbytes = int(np.prod(shape)) * torch.empty((), dtype=dtype).element_size()
+        buf = self._bufs.get(name)
+        if buf is None or buf.numel() < nbytes:
+            self._bufs.pop(name, None)
+            buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+            self._bufs[name] = buf
+        return buf[:nbytes].view(dtype).view(shape)
+
+    def nbytes(self):
+        return sum(b.numel() for b in self._bufs.values())
+
+    def release(self):
+        self._bufs.clear()
+
+
 class DeviceSystem:
     """R-space matrices of one system resident on the GPU (uploaded once)."""
 
@@ -189,16 +215,11 @@ class DeviceSystem:
         return self._cache['geom']
 
     def buffer(self, name, shape, dtype):
-        """Persistent device buffer reused by every batch (grow-only), viewed as `dtype[shape]`:
-        keeps GB-sized per-batch allocations out of the caching allocator's way."""
-        nbytes = int(np.prod(shape)) * torch.empty((), dtype=dtype).element_size()
-        key = ('buf', name)
-        buf = self._cache.get(key)
-        if buf is None or buf.numel() < nbytes:
-            self._cache.pop(key, None)
-            buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
-            self._cache[key] = buf
-        return buf[:nbytes].view(dtype).view(shape)
+        """Persistent device buffer of the system's default workspace (grow-only), viewed as
+        `dtype[shape]`: keeps GB-sized per-batch allocations out of the caching allocator's way."""
+        if 'ws' not in self._cache:
+            self._cache['ws'] = Workspace(self.device)
+        return self._cache['ws'].buffer(name, shape, dtype)
 
     def grid_phases(self, shifts, NKFFT, prec):
         """Device-resident per-axis phase tables for every block of a grid (built once per grid)."""
@@ -476,12 +497,13 @@ def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
     return out, (s, h)
 
 
-def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_start=0):
+def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_start=0, ws=None):
     """Stages 1-3 for a batch of blocks.  precision 'fp64': everything in FP64;
     'mixed': H(k) transform and eigh in double-float, the other fields and the rotation in FP32.
     All per-batch arrays live in persistent buffers of `dev` (reused by the next call: consume
     the returned BandData before calling again).  `phases` maps a precision code to the tables
-    of DeviceSystem.grid_phases; `block_start` is the index of dKs[0] in that grid."""
+    of DeviceSystem.grid_phases; `block_start` is the index of dKs[0] in that grid.  `ws`: the
+    Workspace holding the per-batch arrays (default: the system's own), one per concurrent run."""
     require_cuda()
     quantities = set(quantities)
     if 'O' in quantities:
@@ -493,35 +515,36 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     nkt = nb * nk
     keep = []
     ph = (lambda p: None if phases is None else phases.get(p))
-    flag = dev.buffer('flag', (1,), torch.int32)
+    arena = ws if ws is not None else dev
+    flag = arena.buffer('flag', (1,), torch.int32)
     flag.zero_()
 
     def fields_for(q, with_H, prec, name, lower=False):
         _, _, nF, _ = field_arrays(dev, q, with_H, prec)
-        out = dev.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec in C64_PRECS else torch.complex128)
+        out = arena.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec in C64_PRECS else torch.complex128)
         geo = r2k_geometry(dev, NKFFT)
-        ws = ctypes.c_size_t(0)
-        _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(ws)),
+        wsz = ctypes.c_size_t(0)
+        _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(wsz)),
                    "wbg_r2k_workspace_size")
-        work = dev.buffer('r2k_ws', (int(ws.value),), torch.uint8)
+        work = arena.buffer('r2k_ws', (int(wsz.value),), torch.uint8)
         return r2k(dev, dKs, NKFFT, q, with_H, prec, out=out, workspace=work, phases=ph(prec),
                    block_start=block_start, lower=lower)
 
-    E = dev.buffer('E', (nkt, nw), torch.float64)
+    E = arena.buffer('E', (nkt, nw), torch.float64)
     ews = ctypes.c_size_t(0)
     _lib.check(_lib.load().wbg_eigh_workspace_size(nw, nkt, ctypes.byref(ews)), "wbg_eigh_workspace_size")
-    ework = dev.buffer('eigh_ws', (int(ews.value),), torch.uint8)
+    ework = arena.buffer('eigh_ws', (int(ews.value),), torch.uint8)
     if precision == 'fp64':
         fields, index, nF, k1 = fields_for(quantities, True, PREC_FP64, 'fields')
         keep.append(k1)
-        U = dev.buffer('U', (nkt, nw, nw), torch.complex128)
+        U = arena.buffer('U', (nkt, nw, nw), torch.complex128)
         E, U, flag = eigh(fields, nF * nw * nw, nw, nkt, E=E, U=U, mode=1, work=ework, flag=flag)
         fp64_fields = True
     elif precision == 'mixed':
         # lower triangles of the Hermitian fields only: exactly Hermitian, half the transform
         Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=True)
         keep.append(k0)
-        U = dev.buffer('U32', (nkt, nw, nw), torch.complex64)
+        U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
         E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | EIGH_LOWER, work=ework, flag=flag)
         fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True)
         keep.append(k1)
@@ -541,7 +564,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         # rotation, which drops only the FP32 rounding noise of U^dagger X U
         herm = [(h or 1) | 4 if lower_in[f] else h for f, h in zip(sel, herm)]
     if sel:
-        Xb = dev.buffer('Xbar', (nkt, len(sel), nw, nw), torch.complex128 if fp64_fields else torch.complex64)
+        Xb = arena.buffer('Xbar', (nkt, len(sel), nw, nw), torch.complex128 if fp64_fields else torch.complex64)
         Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nkt, fp64_fields, out=Xb)
         keep.append(k2)
     else:

@@ -1,0 +1,337 @@
+"""Continuous-batching integration server: resident systems, concurrent requests.
+
+The reference integrates one system per ``run()`` call (run_grid.py:118-403) and leaves
+concurrency to Ray processes (run_grid.py:79-109).  This module keeps many systems resident on
+one GPU and runs many integration requests at once:
+
+* ``Server.add_system`` uploads a system's R-space matrices once (engine.DeviceSystem); the
+  k-independent R-space fields and grid phase tables are built on first use and cached.
+* ``Server.submit`` queues a request (system, grid, calculators[, blocks]) and returns a
+  ``Ticket``.  Requests are admitted in arrival order while an active slot is free and the
+  request's estimated device memory fits in the HBM budget; nothing overtakes the queue head.
+* Every admitted request gets its own CUDA stream and buffer workspace, and its Fermi-level
+  histograms stay on the device.  The scheduler issues one block batch per active request per
+  round, so kernels of different requests overlap on the GPU; a request's completion is seen
+  through an event on its stream (no device-wide synchronisation).
+* Results are the same ``ResultDict`` as ``run()`` with the same block weighting; ``stats()``
+  reports p50 / p99 latency (submit to result) and k-points per second.
+
+No counterpart in the reference; the numerical path is exactly ``run()``'s.
+"""
+import threading
+import time
+from collections import deque
+
+import numpy as np
+import torch
+
+from . import engine
+from .result import ResultDict
+from .run import choose_batch
+
+
+def admit(pending_bytes, used_bytes, budget_bytes, free_slots):
+    """Admission rule: the longest prefix of the FIFO queue (sizes `pending_bytes`) that fits
+    in the free slots and the remaining memory budget.  Returns the number admitted.  A request
+    larger than the whole budget is admitted alone when nothing else is active (it could never
+    run otherwise)."""
+    n = 0
+    for size in pending_bytes:
+        if n >= free_slots:
+            break
+        if used_bytes + size > budget_bytes and not (used_bytes == 0 and n == 0):
+            break
+        used_bytes += size
+        n += 1
+    return n
+
+
+def request_bytes(nw, nk, nblocks_batch, quantities, precision):
+    """Device memory of one request's batch buffers (fields, H, U, Xbar, workspaces)."""
+    cs = 16 if precision == 'fp64' else 8
+    nf = 1 + sum(engine.QUANTITIES[q]['ncomp'] for q in quantities)
+    per_k = nw * nw * (2 * nf * cs + 16 * 3) + 64 * nw
+    return int(per_k * nk * nblocks_batch * 2)
+
+
+class Ticket:
+    """Handle of a submitted request: ``wait()`` returns its ResultDict (or raises its error)."""
+
+    def __init__(self, rid, key):
+        self.rid, self.key = rid, key
+        self.t_submit = time.perf_counter()
+        self.t_admit = None
+        self.t_done = None
+        self.nkpoints = 0
+        self._event = threading.Event()
+        self._result = None
+        self._error = None
+
+    def done(self):
+        return self._event.is_set()
+
+    def wait(self, timeout=None):
+        if not self._event.wait(timeout):
+            raise TimeoutError(f"request {self.rid} not finished after {timeout} s")
+        if self._error is not None:
+            raise self._error
+        return self._result
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_submit
+
+    def _finish(self, result=None, error=None):
+        self.t_done = time.perf_counter()
+        self._result, self._error = result, error
+        self._event.set()
+
+
+class _Request:
+    def __init__(self, ticket, key, grid, calculators, blocks):
+        self.ticket, self.key, self.grid, self.calculators = ticket, key, grid, calculators
+        self.blocks = blocks
+        self.stream = None
+        self.ws = None
+        self.batches = None
+        self.next_batch = 0
+        self.done_event = None
+        self.nbytes = 0
+        self.flags = []
+
+
+class Server:
+    """Continuous-batching server on one device.
+
+    precision: 'mixed' or 'fp64' (as run()); hbm_budget: bytes of per-request buffers allowed
+    at once; max_active: requests in flight (one CUDA stream each); max_kpoints: k-points per
+    block batch."""
+
+    def __init__(self, device='cuda', precision='mixed', hbm_budget=150 << 30, max_active=4, max_kpoints=1 << 17):
+        engine.require_cuda()
+        self.device = torch.device(device)
+        self.precision = precision
+        self.hbm_budget = int(hbm_budget)
+        self.max_active = int(max_active)
+        self.max_kpoints = int(max_kpoints)
+        self._systems = {}
+        self._pending = deque()
+        self._active = []
+        self._finished = []
+        self._lock = threading.Lock()
+        self._wake = threading.Event()
+        self._stop = False
+        self._thread = None
+        self._rid = 0
+        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.max_active)]
+        self._free_streams = list(self._streams)
+        self._prep_stream = torch.cuda.Stream(device=self.device)
+        self._used = 0
+        self._error = None
+
+    # ---------------------------------------------------------------- systems and requests
+    def add_system(self, key, system):
+        """Make `system` resident under `key` (R-space matrices uploaded now)."""
+        with torch.cuda.stream(self._prep_stream):
+            dev = engine.DeviceSystem(system, self.device)
+            for name in ['Ham'] + [k for k in ('AA', 'BB', 'CC') if system.has_R_mat(k)]:
+                dev._key_fp64(name)  # upload now: requests find the matrices resident
+        self._prep_stream.synchronize()
+        self._systems[key] = (system, dev)
+        return dev
+
+    def submit(self, key, grid, calculators, blocks=None):
+        """Queue an integration of `calculators` over `grid` (optionally a subset `blocks` of its
+        division-grid K-points) for the system registered as `key`; returns a Ticket."""
+        if key not in self._systems:
+            raise ValueError(f"unknown system {key!r}: add_system() first")
+        with self._lock:
+            self._rid += 1
+            t = Ticket(self._rid, key)
+            self._pending.append(_Request(t, key, grid, dict(calculators), blocks))
+        self._wake.set()
+        return t
+
+    # ---------------------------------------------------------------- scheduling
+    def _estimate(self, req):
+        system, dev = self._systems[req.key]
+        q = set()
+        for c in req.calculators.values():
+            q |= c.quantities(system)
+        nb = choose_batch(dev.nw, req.grid.nk_per_block, len(self._blocks_of(req)), q, self.precision,
+                          max_kpoints=self.max_kpoints)
+        return q, nb, request_bytes(dev.nw, req.grid.nk_per_block, nb, q, self.precision)
+
+    @staticmethod
+    def _blocks_of(req):
+        shifts = req.grid.block_shifts()
+        return np.arange(len(shifts)) if req.blocks is None else np.asarray(req.blocks)
+
+    def _admit(self):
+        with self._lock:
+            sizes, plans = [], []
+            for req in self._pending:
+                if len(plans) >= len(self._free_streams):
+                    break
+                plan = self._estimate(req)
+                plans.append(plan)
+                sizes.append(plan[2])
+            n = admit(sizes, self._used, self.hbm_budget, len(self._free_streams))
+            taken = [self._pending.popleft() for _ in range(n)]
+        for req, (q, nb, nbytes) in zip(taken, plans):
+            self._start(req, q, nb, nbytes)
+
+    def _start(self, req, quantities, nb, nbytes):
+        system, dev = self._systems[req.key]
+        req.ticket.t_admit = time.perf_counter()
+        req.stream = self._free_streams.pop()
+        req.nbytes = nbytes
+        self._used += nbytes
+        req.ws = engine.Workspace(self.device)
+        blocks = self._blocks_of(req)
+        shifts = req.grid.block_shifts()
+        precs = [engine.PREC_FP64] if self.precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
+        # cached, k-independent data (R-space fields, phase tables) are built on the preparation
+        # stream; the request's stream waits for them once
+        with torch.cuda.stream(self._prep_stream):
+            req.phases = {p: dev.grid_phases(shifts, req.grid.FFT, p) for p in precs}
+            if self.precision == 'fp64':
+                engine.field_arrays(dev, quantities, True, engine.PREC_FP64)
+            else:
+                engine.field_arrays(dev, set(), True, engine.PREC_DF64)
+                engine.field_arrays(dev, quantities, False, engine.PREC_FP32S)
+            ready = torch.cuda.Event()
+            ready.record(self._prep_stream)
+        req.stream.wait_event(ready)
+        req.quantities = quantities
+        req.batches = [blocks[i:i + nb] for i in range(0, len(blocks), nb)]
+        req.ticket.nkpoints = len(blocks) * req.grid.nk_per_block
+        with torch.cuda.stream(req.stream):
+            for c in req.calculators.values():
+                c.reset(self.device)
+            if not req.batches:
+                req.done_event = torch.cuda.Event()
+                req.done_event.record(req.stream)
+        self._active.append(req)
+
+    def _issue(self, req):
+        system, dev = self._systems[req.key]
+        idx = req.batches[req.next_batch]
+        req.next_batch += 1
+        shifts = req.grid.block_shifts()
+        with torch.cuda.stream(req.stream):
+            contiguous = np.all(np.diff(idx) == 1)
+            if contiguous:
+                bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision,
+                                      phases=req.phases, block_start=int(idx[0]), ws=req.ws)
+            else:
+                bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
+            for c in req.calculators.values():
+                c.accumulate(bd, system)
+            # the QL convergence flag is read once the request has finished
+            req.flags.append(bd._flag.clone())
+            if req.next_batch == len(req.batches):
+                req.done_event = torch.cuda.Event()
+                req.done_event.record(req.stream)
+
+    def _finish(self, req):
+        system, dev = self._systems[req.key]
+        try:
+            with torch.cuda.stream(req.stream):
+                if any(int(f.item()) != 0 for f in req.flags):
+                    raise RuntimeError("wbg_eigh_batched: QL iteration did not converge for some k-point")
+                nk = req.grid.nk_per_block
+                factor = 1.0 / req.grid.nblocks
+                res = ResultDict({k: c.result(system.cell_volume, nk, factor) for k, c in req.calculators.items()})
+            req.ticket._finish(result=res)
+        except Exception as e:  # the request fails, the server keeps going
+            req.ticket._finish(error=e)
+        req.ws.release()
+        self._used -= req.nbytes
+        self._free_streams.append(req.stream)
+        self._finished.append(req.ticket)
+
+    def step(self):
+        """One scheduler round: admit, issue one batch per active request, retire finished
+        requests.  Returns True while there is work left."""
+        self._admit()
+        for req in list(self._active):
+            if req.next_batch < len(req.batches):
+                self._issue(req)
+        for req in list(self._active):
+            if req.next_batch == len(req.batches) and req.done_event.query():
+                self._active.remove(req)
+                self._finish(req)
+        with self._lock:
+            return bool(self._pending or self._active)
+
+    def run_until_idle(self, poll=0.0002):
+        """Drive the scheduler in the calling thread until every submitted request is done."""
+        while self.step():
+            if all(r.next_batch == len(r.batches) for r in self._active):
+                time.sleep(poll)
+
+    # ---------------------------------------------------------------- background thread
+    def _loop(self):
+        try:
+            while not self._stop:
+                if not self.step():
+                    self._wake.wait(0.01)
+                    self._wake.clear()
+                elif all(r.next_batch == len(r.batches) for r in self._active):
+                    time.sleep(0.0002)
+        except Exception as e:  # surface scheduler failures to every waiting ticket
+            self._error = e
+            with self._lock:
+                reqs = list(self._pending) + list(self._active)
+                self._pending.clear()
+            for r in reqs:
+                r.ticket._finish(error=e)
+
+    def start(self):
+        if self._thread is None:
+            self._stop = False
+            self._thread = threading.Thread(target=self._loop, name="wbgpu-server", daemon=True)
+            self._thread.start()
+        return self
+
+    def stop(self):
+        self._stop = True
+        self._wake.set()
+        if self._thread is not None:
+            self._thread.join()
+            self._thread = None
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    # ---------------------------------------------------------------- statistics
+    def stats(self, tickets=None):
+        """Latency percentiles (ms) and throughput over finished tickets."""
+        ts = [t for t in (tickets if tickets is not None else self._finished) if t.t_done is not None]
+        if not ts:
+            return {"requests": 0}
+        lat = np.array([t.latency for t in ts]) * 1e3
+        t0 = min(t.t_submit for t in ts)
+        t1 = max(t.t_done for t in ts)
+        nk = sum(t.nkpoints for t in ts)
+        return {"requests": len(ts), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "max_ms": float(lat.max()), "kpoints": int(nk), "kpoints_per_s": nk / max(t1 - t0, 1e-9)}
+
+
+def run_many(jobs, precision='mixed', max_active=4, device='cuda'):
+    """Integrate a list of (system, grid, calculators) jobs concurrently through one Server
+    (systems made resident once); returns the list of ResultDicts in job order."""
+    srv = Server(device=device, precision=precision, max_active=max_active)
+    keys = {}
+    tickets = []
+    for system, grid, calcs in jobs:
+        if id(system) not in keys:
+            keys[id(system)] = len(keys)
+            srv.add_system(keys[id(system)], system)
+        tickets.append(srv.submit(keys[id(system)], grid, calcs))
+    srv.run_until_idle()
+    return [t.wait() for t in tickets]
