@@ -384,10 +384,116 @@ def run_gpu(args):
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
             "fp64_dropin_value": fp64_value, "max_rel_err_vs_fp64": err,
             "peaks_measured_gflops": {"fp64": peaks['fp64'], "fp32": peaks['fp32']}}
+    if world == 1 and not args.no_serve:
+        for key, fn in (("batched", bench_batched), ("served", bench_served)):
+            try:
+                line[key] = fn()
+            except Exception as e:  # the headline line is still printed
+                line[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------------------
+# Batched and served workloads (scaled-down forms of the multi-system configurations)
+# ---------------------------------------------------------------------------------------
+def tb_pool(n, seed, nw_lo, nw_hi):
+    """n seeded random TB systems, num_wann log-uniform in [nw_lo, nw_hi], R half-width 1 or 2."""
+    import numpy as np
+    from wbgpu import models, System_R
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nw = int(round(np.exp(rng.uniform(np.log(nw_lo), np.log(nw_hi)))))
+        d = models.random_tb(nw, int(rng.integers(1, 3)), models.triclinic_lattice(rng), 1.5, seed + i,
+                             centers='random', keys=('Ham', 'AA'))
+        out.append(System_R.from_dict(d))
+    return out
+
+
+def bench_batched(nsys=32):
+    """AHC + Berry-curvature dipole of `nsys` systems (num_wann 4-128) on 16^3 grids: all jobs
+    through one continuous-batching server (mixed precision) against looping the plain FP64
+    run() system by system."""
+    import numpy as np
+    import torch
+    import wbgpu
+    from wbgpu.calculators import AHC, BerryDipole_FermiSea
+    ef = np.linspace(-1, 1, 201)
+    systems = tb_pool(nsys, 4000, 4, 128)
+    mk = lambda: {'ahc': AHC(Efermi=ef), 'bcd': BerryDipole_FermiSea(Efermi=ef)}
+    jobs = [(s, wbgpu.Grid(s, NKdiv=1, NKFFT=16), mk()) for s in systems]
+    wbgpu.run_many(jobs[:4], precision='mixed')  # build the library's lazy state
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    got = wbgpu.run_many(jobs, precision='mixed', max_active=8)
+    torch.cuda.synchronize()
+    t_b = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = [wbgpu.run(s, g, mk(), precision='fp64') for s, g, _ in jobs]
+    torch.cuda.synchronize()
+    t_p = time.perf_counter() - t0
+    nk = sum(g.nk_per_block * g.nblocks for _, g, _ in jobs)
+    err = {k: max(float(np.max(np.abs(a[k].data - b[k].data)) / np.max(np.abs(b[k].data))) for a, b in zip(got, ref))
+           for k in ('ahc', 'bcd')}
+    return {"workload": f"{nsys} systems, num_wann log-uniform 4-128 (seeded), R half-width 1-2, 16^3 k each, "
+                        "AHC + BCD at 201 E_F", "kpoints": nk, "kpoints_per_s": nk / t_b,
+            "plain_fp64_loop_kpoints_per_s": nk / t_p, "speedup_vs_plain_loop": t_p / t_b,
+            "max_rel_err_vs_fp64": err, "nw": [s.num_wann for s in systems]}
+
+
+def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
+    """Poisson arrivals (mean `rate` per s) of AHC requests over `nsys` resident systems
+    (num_wann 8-128), grids 8^3-32^3: p50 / p99 latency from submit to result and throughput,
+    against the plain FP64 run() of the first `nbase` requests one after the other."""
+    import numpy as np
+    import torch
+    import wbgpu
+    from wbgpu.calculators import AHC
+    ef = np.linspace(-1, 1, 201)
+    systems = tb_pool(nsys, 5000, 8, 128)
+    rng = np.random.default_rng(5001)
+    reqs = []
+    for i in range(nreq):
+        s = int(rng.integers(nsys))
+        nkfft, nkdiv = int(rng.choice([8, 16])), int(rng.choice([1, 2]))
+        reqs.append((s, nkdiv, nkfft))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    grids = {}
+    grid_of = lambda r: grids.setdefault(r, wbgpu.Grid(systems[r[0]], NKdiv=r[1], NKFFT=r[2]))
+    srv = wbgpu.Server(precision='mixed', max_active=8)
+    for i, s in enumerate(systems):
+        srv.add_system(i, s)
+    for r in set(reqs):  # warm the per-(system, grid) caches: R-space fields, phase tables
+        srv.submit(r[0], grid_of(r), {'ahc': AHC(Efermi=ef)})
+    srv.run_until_idle()
+    torch.cuda.synchronize()
+    srv._finished.clear()
+    tickets = []
+    with srv:
+        t0 = time.perf_counter()
+        for (s, nkdiv, nkfft), ta in zip(reqs, arrivals):
+            dt = t0 + ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(s, grid_of((s, nkdiv, nkfft)), {'ahc': AHC(Efermi=ef)}))
+        for t in tickets:
+            t.wait(600)
+    st = srv.stats(tickets)
+    t0 = time.perf_counter()
+    nkb = 0
+    for s, nkdiv, nkfft in reqs[:nbase]:
+        g = grid_of((s, nkdiv, nkfft))
+        wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision='fp64')
+        nkb += g.nk_per_block * g.nblocks
+    torch.cuda.synchronize()
+    st.update({"workload": f"{nreq} AHC requests, Poisson arrivals at {rate:g}/s over {nsys} resident systems "
+                           "(num_wann log-uniform 8-128, seeded), grids 8^3-32^3, 201 E_F, mixed precision",
+               "offered_rate_per_s": rate, "plain_fp64_serial_kpoints_per_s": nkb / (time.perf_counter() - t0),
+               "plain_fp64_serial_sample": f"first {nbase} requests run one after the other"})
+    return st
 
 
 def main():
@@ -401,6 +507,7 @@ def main():
     ap.add_argument('--nkfft', type=int, default=NKFFT, help='FFT block edge (smaller only for profiling captures)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64-compare', action='store_true')
+    ap.add_argument('--no-serve', action='store_true', help='skip the batched and served measurements')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
