@@ -264,8 +264,8 @@ def run_gpu(args):
     nblocks = grid.nblocks
     shifts = grid.block_shifts()
     # contiguous shard of the division grid per rank (blocks are independent: weak scaling)
-    per = nblocks // world
-    mine = np.arange(rank * per, (rank + 1) * per)
+    from wbgpu.distributed import shard_blocks
+    mine = shard_blocks(nblocks, rank, world)
     B = args.blocks_per_step
     nk = grid.nk_per_block
     EF = np.linspace(-2, 2, NEF)
