@@ -32,7 +32,7 @@ constexpr int KD = 2 * NW;                 // real-embedded contraction length
 constexpr int ND = 2 * NW;                 // real-embedded output columns (re | im)
 constexpr int TM = 128;                    // MMA M: one tile = 4 fields x 32 rows
 constexpr int FPT = TM / NW;               // fields per tile
-constexpr int NTHR = 128;                  // warp q owns TMEM lanes 32q..32q+31 = field q of the tile
+constexpr int NTHR = 256;                  // warps q and q+4 own TMEM lanes 32q..32q+31 = field q of the tile
 constexpr int LBO = 144;                   // bytes between K-adjacent core matrices
 constexpr int SBO = (KD / 4) * LBO;        // bytes between 8-row groups
 constexpr int A_BYTES = (TM / 8) * SBO;    // one copy (hi or lo) of a tile operand
@@ -48,7 +48,7 @@ constexpr uint32_t TMEM_COLS = NACC * ND <= 128 ? 128 : NACC * ND <= 256 ? 256 :
 constexpr int STAGE_LD = NW + 1;           // float2 row stride of the Hermitian-part staging
 constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on every mbarrier wait
 
-static_assert(4 * NW * STAGE_LD * 8 <= A_BYTES, "staging must fit in the A operand buffer");
+static_assert(FPT * NW * STAGE_LD * 8 <= A_BYTES, "staging must fit in the A operand buffer");
 
 // Instruction descriptor of tcgen05.mma kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
 // (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
@@ -131,24 +131,21 @@ WBG_D void tmem_ld_wait16(uint32_t* r) {
                "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
                "+r"(r[14]), "+r"(r[15])::"memory");
 }
-// The 64 columns (re | im) of this thread's TMEM lane, summed over the NACC accumulators
+// 16 columns (from col) of this thread's TMEM lane, summed over the NACC accumulators
 // (correction first, then the main ones) on the CUDA cores with round-to-nearest.
-WBG_D void tmem_row64(uint32_t taddr, float (&v)[64]) {
+WBG_D void tmem_cols16(uint32_t taddr, int col, float (&v)[16]) {
+  uint32_t r[NACC][16];
 #pragma unroll
-  for (int a = 0; a < NACC; ++a) {
-    uint32_t r[64];
-    const uint32_t col = (uint32_t)(a == 0 ? NMAIN : a - 1) * ND;
-    tmem_ld16(taddr + col + 0, r + 0);
-    tmem_ld16(taddr + col + 16, r + 16);
-    tmem_ld16(taddr + col + 32, r + 32);
-    tmem_ld16(taddr + col + 48, r + 48);
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    tmem_ld_wait16(r + 0);
-    tmem_ld_wait16(r + 16);
-    tmem_ld_wait16(r + 32);
-    tmem_ld_wait16(r + 48);
+  for (int a = 0; a < NACC; ++a) tmem_ld16(taddr + (uint32_t)(a == 0 ? NMAIN : a - 1) * ND + col, r[a]);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 64; ++i) v[i] = a == 0 ? __uint_as_float(r[i]) : v[i] + __uint_as_float(r[i]);
+  for (int a = 0; a < NACC; ++a) tmem_ld_wait16(r[a]);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    float x = __uint_as_float(r[0][i]);
+#pragma unroll
+    for (int a = 1; a < NACC; ++a) x += __uint_as_float(r[a][i]);
+    v[i] = x;
   }
 }
 
@@ -208,10 +205,11 @@ __global__ void __launch_bounds__(NTHR, 2)
   tc_fence_after();
   const uint32_t tbase = tmem_base_s;
   const uint32_t D1 = tbase, D2 = tbase;  // GEMM2 reuses GEMM1's accumulators once D1 is read
-  const uint32_t lane_base = (uint32_t)(32 * warp) << 16;  // TMEM lanes of this warp
+  const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter (= field of the tile), column half
+  const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;  // TMEM lanes of this warp
   uint32_t phase = 0;
   const int ntiles = (nFrot + FPT - 1) / FPT;
-  float2* stage = reinterpret_cast<float2*>(Ah) + warp * NW * STAGE_LD;
+  float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
   for (long long k = blockIdx.x; k < nk && !abort_s; k += gridDim.x) {
     // ---- embedded U_k (B operand, hi / lo)
     const float2* Uk = U + k * strideU;
@@ -231,8 +229,8 @@ __global__ void __launch_bounds__(NTHR, 2)
     }
     for (int t = 0; t < ntiles; ++t) {
       // ---- A1: rows (fl, m) of the tile's fields, K = [Re X[m][:] | Im X[m][:]].
-      // Thread tid owns element n = lane of rows m = 4 i + warp: every load of the tile is
-      // issued before the first store.
+      // Thread tid owns element n = lane of rows m = 8 i + warp (mod NW): every load of the
+      // tile is issued before the first store.
       {
         constexpr int PER = FPT * NW * NW / NTHR;
         float2 xv[PER];
@@ -284,14 +282,16 @@ __global__ void __launch_bounds__(NTHR, 2)
       if (!wait_all(mb, phase, &abort_s)) break;
       phase ^= 1;
       tc_fence_after();
-      {  // ---- D1 -> A2: thread (field q, row j) holds T[j][:]; writes column j of T^H
-        float r[64];
-        tmem_row64(D1 + lane_base, r);
-        const int row0 = warp * NW;
+      {  // ---- D1 -> A2: thread (field q, row j) holds T[j][:]; writes column j of T^H.
+        // Column half 0 (Re T) -> K block 0, half 1 (Im T) -> K block 1 with a minus sign.
+        const int row0 = quarter * NW;
 #pragma unroll
-        for (int mp = 0; mp < NW; ++mp) {
-          put_split(Ah, Al, op_off(row0 + mp, lane), r[mp]);
-          put_split(Ah, Al, op_off(row0 + mp, NW + lane), -r[NW + mp]);
+        for (int c = 0; c < 2; ++c) {
+          float v[16];
+          tmem_cols16(D1 + lane_base, NW * half + 16 * c, v);
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            put_split(Ah, Al, op_off(row0 + 16 * c + i, NW * half + lane), half ? -v[i] : v[i]);
         }
       }
       tc_fence_before();
@@ -305,32 +305,29 @@ __global__ void __launch_bounds__(NTHR, 2)
       if (!wait_all(mb, phase, &abort_s)) break;
       phase ^= 1;
       tc_fence_after();
-      {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][:]
-        float r[64];
-        tmem_row64(D2 + lane_base, r);
-        const int f = t * FPT + warp;
+      {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][n] for n in its column half
+        const int f = t * FPT + quarter;
+        const int hm = f < nFrot ? (herm[f] & 3) : 0;
+        float2* dst = Xbar + (k * nFrot + (f < nFrot ? f : 0)) * (long long)(NW * NW);
+        float re[16], im[16];
+        tmem_cols16(D2 + lane_base, 16 * half, re);
+        tmem_cols16(D2 + lane_base, NW + 16 * half, im);
         if (f < nFrot) {  // warp-uniform
-          const int hm = herm[f] & 3;
-          float2* dst = Xbar + (k * nFrot + f) * (long long)(NW * NW);
-          if (hm == 0) {  // Y[n][m] = conj(Y^H[m][n]): coalesced over m
 #pragma unroll
-            for (int n = 0; n < NW; ++n) dst[n * NW + lane] = make_float2(r[n], -r[NW + n]);
-          } else if (hm == 2) {  // diagonal of the Hermitian part
+          for (int i = 0; i < 16; ++i) {
+            const int n = 16 * half + i;
+            if (hm == 0) dst[n * NW + lane] = make_float2(re[i], -im[i]);  // Y[n][m] = conj(Y^H[m][n])
+            else if (hm == 2) { if (n == lane) dst[n * NW + n] = make_float2(re[i], 0.f); }
+            else stage[lane * STAGE_LD + n] = make_float2(re[i], im[i]);
+          }
+        }
+        __syncthreads();  // both column halves of every field are staged
+        if (f < nFrot && hm == 1) {  // Hermitian part P = (Y^H + Y)/2; P[n][m] = conj(P[m][n])
 #pragma unroll
-            for (int n = 0; n < NW; ++n)
-              if (n == lane) dst[n * NW + n] = make_float2(r[n], 0.f);
-          } else {  // Hermitian part P = (Y^H + Y)/2; P[n][m] = conj(P[m][n])
-#pragma unroll
-            for (int n = 0; n < NW; ++n)
-              stage[lane * STAGE_LD + n] = make_float2(r[n], r[NW + n]);
-            __syncwarp();
-#pragma unroll
-            for (int n = 0; n < NW; ++n) {
-              const float2 s = stage[n * STAGE_LD + lane];  // Y^H[n][m]
-              const float pr = 0.5f * (r[n] + s.x);
-              const float pi = 0.5f * (r[NW + n] - s.y);
-              dst[n * NW + lane] = make_float2(pr, -pi);
-            }
+          for (int i = 0; i < 16; ++i) {
+            const int n = 16 * half + i;
+            const float2 a = stage[lane * STAGE_LD + n], b = stage[n * STAGE_LD + lane];
+            dst[n * NW + lane] = make_float2(0.5f * (a.x + b.x), -0.5f * (a.y - b.y));
           }
         }
       }
