@@ -158,7 +158,10 @@ int wbg_device_flags(unsigned int* flags, int clear);
 
 /* ---- stage 4: Berry curvature traces + Fermi-level histogram ----------------------------
  * Xbar [nk][nFbar][nw][nw]: velocity dH/dk at iV..iV+2, A at iA..iA+2, rotA at iO..iO+2.
- * hist [scan.nEF][3] (double) is accumulated (not cleared). */
+ * hist [scan.nEF][3] (double) is accumulated (not cleared).
+ * fp64: 1 complex128 Xbar; 0 complex64; 2 complex64 whose V and A are exactly Hermitian
+ * (the mixed path's rotation output) -- then the (l, n) elements are taken as conj(X_nl) and
+ * every load is a coalesced row segment (nw <= 32). */
 int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                     const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
                     void* stream);

@@ -400,3 +400,32 @@ def test_mixed_vs_fp64_large_nw(nw, tb128):
     for key in ('ahc', 'opt'):
         x, y = a[key].data, b[key].data
         assert np.abs(x - y).max() < 2e-5 * np.abs(y).max(), (key, np.abs(x - y).max() / np.abs(y).max())
+
+
+def test_omega_hermitian_column_kernel(c2small):
+    """Mixed path: V and A of Xbar are exactly Hermitian, and the column-per-lane Omega kernel
+    (wbg_berry_omega fp64 = 2) matches the general FP32 kernel on the same band data (both FP32
+    traces; only the summation order differs)."""
+    import ctypes
+    from wbgpu import _lib
+    s, _ = c2small
+    dev = engine.DeviceSystem(s)
+    NKFFT = (6, 5, 4)
+    dKs = np.array([[0.1, 0.2, -0.3], [0.0, 0.5, 0.25]]) / np.array(NKFFT)
+    calc = wbgpu.calculators.AHC(Efermi=np.linspace(-2, 2, 41))
+    bd = engine.band_data(dev, dKs, NKFFT, calc.quantities(s), 'mixed')
+    assert bd.hermitian and bd.omega_mode == 2
+    nw = s.num_wann
+    iV = bd.index['V']
+    V = bd.Xbar[:, iV:iV + 3]
+    assert torch.equal(V, V.conj().transpose(-1, -2))
+    out = []
+    for mode in (2, 0):
+        calc.reset(dev.device)
+        sc = calc.scan_struct()
+        st = _lib.load().wbg_berry_omega(engine._ptr(bd.E), engine._ptr(bd.Xbar), bd.Xbar.shape[1], iV,
+                                         bd.index['A'], bd.index['Od'], nw, bd.nk_total, ctypes.byref(sc), 1, 1,
+                                         engine._ptr(calc._hist), mode, engine._stream())
+        _lib.check(st, "wbg_berry_omega")
+        out.append(calc._hist.cpu().numpy().copy())
+    assert np.abs(out[0] - out[1]).max() <= 1e-5 * np.abs(out[1]).max()

@@ -490,6 +490,145 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
 }
 
 // ---------------------------------------------------------------------------------------
+// Omega traces for exactly Hermitian V and A in FP32 (the mixed path: lower-triangle inputs,
+// Hermitian-part rotation), nw <= 32.  Lane l owns column l and the warp walks the rows n, so
+// every load is a coalesced row segment; the (l, n) elements come from V_ln = conj(V_nl) and
+// A_ln = conj(A_nl).  One warp reduction per row gives the trace t(n) (same terms as
+// berry_omega_kernel); grouping and binning are the same.  One warp per k-point.
+// ---------------------------------------------------------------------------------------
+__global__ void berry_omega_cols(const double* __restrict__ E, const float2* __restrict__ Xbar, int nFbar, int iV,
+                                 int iA, int iO, int nw, int nk, int G, WbgScan sp, int internal_terms,
+                                 int external_terms, double* __restrict__ hist) {
+  extern __shared__ double smb[];
+  double* sh = smb;                                        // [nEF][3]
+  double* Es = sh + 3 * sp.nEF;                            // [G][32]
+  double* tv = Es + G * 32;                                // [G][32][3]
+  float* Ehl = reinterpret_cast<float*>(tv + 3 * G * 32);  // [G][2][32]
+  int* start = reinterpret_cast<int*>(Ehl + 2 * G * 32);   // [G][32]
+  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* myE = Es + grp * 32;
+  double* myT = tv + 3 * grp * 32;
+  float* myEh = Ehl + 2 * grp * 32;
+  float* myEl = myEh + 32;
+  int* myS = start + grp * 32;
+  const long long nw2 = (long long)nw * nw;
+  for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
+    const long long k = base + grp;
+    const bool valid = k < nk;
+    const long long kk = valid ? k : nk - 1;
+    if (lane < nw) {
+      const double e = E[kk * nw + lane];
+      const float eh = (float)e;
+      myE[lane] = e;
+      myEh[lane] = eh;
+      myEl[lane] = (float)(e - (double)eh);
+    }
+    __syncwarp();
+    if (lane < nw) myS[lane] = (lane == 0) || (myE[lane] - myE[lane - 1] > sp.degen_thresh);
+    __syncwarp();
+    int below = 0, f0 = nw;
+    if (lane < nw) {
+      below = myE[lane] < sp.EFmin;
+      if (myS[lane]) {
+        int g1 = lane + 1;
+        while (g1 < nw && !myS[g1]) ++g1;
+        if (myE[g1 - 1] >= sp.EFmin && myE[lane] <= sp.EFmax) f0 = lane;
+      }
+    }
+    below = group_sum_i(below, 32);
+    f0 = group_min_i(f0, 32);
+    const int bandmax = min(below, f0);
+    const float2* Xk = Xbar + kk * nFbar * nw2;
+    const int l = lane;
+    for (int n = 0; n < nw; ++n) {  // warp-uniform
+      int gs = n, ge = n + 1;
+      while (!myS[gs]) --gs;
+      while (ge < nw && !myS[ge]) ++ge;
+      bool ingroup;
+      if (n < bandmax) { gs = 0; ge = bandmax; ingroup = true; }
+      else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
+      if (!ingroup) {
+        if (lane == 0) for (int g = 0; g < 3; ++g) myT[n * 3 + g] = 0.0;
+        continue;
+      }
+      float sr[3] = {0.f, 0.f, 0.f};  // Re of the trace terms of column l
+      if (l < nw) {
+        float2 Vn[3], An[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          Vn[a] = Xk[(iV + a) * nw2 + n * nw + l];
+          An[a] = external_terms ? Xk[(iA + a) * nw2 + n * nw + l] : make_float2(0.f, 0.f);
+        }
+        if (l < gs || l >= ge) {
+          const float dinv = inv_gap<float>(myE, myEh, myEl, n, l);
+          float2 Dnl[3], Dln[3], Aln[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            Dnl[a] = cscale(Vn[a], -dinv);         // D_nl = -V_nl / (E_n - E_l)
+            Dln[a] = cscale(cconj(Vn[a]), dinv);   // D_ln = -V_ln / (E_l - E_n), V_ln = conj(V_nl)
+            Aln[a] = cconj(An[a]);                  // A_ln = conj(A_nl)
+          }
+#pragma unroll
+          for (int g = 0; g < 3; ++g) {
+            const int al = (g + 1) % 3, be = (g + 2) % 3;
+            float2 acc = czero<float2>(), accx = czero<float2>();
+            if (internal_terms) acc = cmuli(cmul(Dnl[al], Dln[be]));
+            if (external_terms) { cfma(accx, Dnl[be], Aln[al]); accx = csub(accx, cmul(Dnl[al], Aln[be])); }
+            sr[g] += accx.x - acc.x;  // Re[-i D^a_nl D^b_ln - D^a_nl A^b_ln + D^b_nl A^a_ln]
+          }
+        } else if (external_terms) {  // within the group: Re(-i A^a_nl A^b_ln), plus 1/2 O_nn
+#pragma unroll
+          for (int g = 0; g < 3; ++g) {
+            const int al = (g + 1) % 3, be = (g + 2) % 3;
+            sr[g] += cmul(An[al], cconj(An[be])).y;
+            if (l == n) sr[g] += 0.5f * Xk[(iO + g) * nw2 + n * nw + n].x;
+          }
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < 3; ++g)
+        for (int off = 16; off > 0; off >>= 1) sr[g] += __shfl_xor_sync(0xffffffffu, sr[g], off);
+      if (lane == 0)
+        for (int g = 0; g < 3; ++g) myT[n * 3 + g] = 2.0 * (double)sr[g];
+    }
+    __syncwarp();
+    if (valid && lane < nw) {
+      const int n = lane;
+      int gs = -1, ge = -1;
+      bool sea = false;
+      if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; sea = true; }
+      else if (n >= bandmax && myS[n]) {
+        int g1 = n + 1;
+        while (g1 < nw && !myS[g1]) ++g1;
+        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
+      }
+      if (gs >= 0) {
+        double v[3] = {0.0, 0.0, 0.0}, esum = 0.0;
+        for (int q = gs; q < ge; ++q) {
+          for (int g = 0; g < 3; ++g) v[g] += myT[q * 3 + g];
+          esum += myE[q];
+        }
+        int bin = -1;
+        if (sea) bin = 0;
+        else {
+          const double Em = esum / (double)(ge - gs);
+          if (Em < sp.EFmin) bin = 0;
+          else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
+        }
+        if (bin >= 0 && bin < sp.nEF)
+          for (int g = 0; g < 3; ++g) atomicAdd(&sh[bin * 3 + g], v[g]);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
+    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+}
+
+// ---------------------------------------------------------------------------------------
 // Orbital moment, Morb_Hpm (formula/covariant.py:375-449): non-additive, so the trace over
 // inn = [0, n), out = [n, nw) is needed at every group border n (calculators/static.py:109-117).
 // The trace splits into pair functions of bands (m in inn, l in out / n' in inn):
@@ -981,6 +1120,22 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (iV < 0 || iV + 3 > nFbar) return WBG_ERR_ARG;
   if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar)) return WBG_ERR_ARG;
   if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
+  if (fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
+  if (fp64 == 2 && nw <= 32) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
+    const int G = 4;  // k-points (warps) per block
+    const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * (8 + 24 + 8 + 4);
+    if (sm > 220 * 1024) return WBG_ERR_SIZE;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    long long nblk = (nk + G - 1) / G;
+    const long long cap = (long long)sms * 16;
+    if (nblk > cap) nblk = cap;
+    cudaFuncSetAttribute(berry_omega_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_omega_cols<<<(int)nblk, 32 * G, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, G, *sp,
+                                                        internal_terms, external_terms, hist);
+    return wbg_cuda_status(cudaGetLastError());
+  }
+  if (fp64 == 2) fp64 = 0;  // the general FP32 kernel does not need the symmetry
   const int L = lanes_for(nw);
   const int G = 128 / L;
   const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * (8 + 24 + 8 + 4);

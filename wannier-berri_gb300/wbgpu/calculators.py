@@ -87,7 +87,7 @@ class AHC(StaticCalculator):
         iO = bd.index.get('Od', 0)
         st = engine._timed('berry_omega', _lib.load().wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], bd.index['V'], iA, iO, bd.nw,
                                          bd.nk_total, ctypes.byref(sc), int(self.internal_terms), int(ext),
-                                         _ptr(self._hist), int(bd.fp64_fields), _stream())
+                                         _ptr(self._hist), bd.omega_mode, _stream())
         _lib.check(st, "wbg_berry_omega")
 
     def result(self, cell_volume, nk, factor=1.0):
@@ -119,7 +119,7 @@ class Morb(StaticCalculator):
         _lib.check(st, "wbg_berry_morb")
         st = engine._timed('berry_omega', lib.wbg_berry_omega, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1],
                            g('V'), g('A'), g('Od'), bd.nw, bd.nk_total, ctypes.byref(sc), int(self.internal_terms),
-                           int(ext), _ptr(self._hist_omega), int(bd.fp64_fields), _stream())
+                           int(ext), _ptr(self._hist_omega), bd.omega_mode, _stream())
         _lib.check(st, "wbg_berry_omega")
 
     def result(self, cell_volume, nk, factor=1.0):

@@ -332,10 +332,16 @@ class BandData:
     Xbar: (nk_tot, nF, nw, nw) complex (float64 or float32 parts); index: quantity -> first field.
     """
 
-    def __init__(self, E, U, Xbar, index, nblocks, nk, nw, fp64_fields):
+    def __init__(self, E, U, Xbar, index, nblocks, nk, nw, fp64_fields, hermitian=False):
         self.E, self.U, self.Xbar, self.index = E, U, Xbar, index
         self.nblocks, self.nk, self.nw = nblocks, nk, nw
         self.fp64_fields = fp64_fields
+        self.hermitian = hermitian  # V and A of Xbar exactly Hermitian (mixed path)
+
+    @property
+    def omega_mode(self):
+        """`fp64` argument of wbg_berry_omega: 1 FP64, 2 FP32 with exactly Hermitian V, A, 0 FP32."""
+        return 1 if self.fp64_fields else (2 if self.hermitian else 0)
 
     @property
     def nk_total(self):
@@ -571,7 +577,11 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         Xbar = None
     if 'O' in bindex:
         bindex['Od'] = bindex['O']
-    bd = BandData(E, U, Xbar, bindex, nb, nk, nw, fp64_fields)
+    # mixed path: V and A come from mirrored (exactly Hermitian) inputs and their rotation keeps
+    # the Hermitian part, so Xbar's V and A blocks are exactly Hermitian
+    herm_out = (not fp64_fields) and all(lower_in[index[q] + c] for q in ('V', 'A') if q in index
+                                         for c in range(3))
+    bd = BandData(E, U, Xbar, bindex, nb, nk, nw, fp64_fields, hermitian=herm_out)
     bd._keep = keep
     bd._flag = flag
     return bd
