@@ -156,6 +156,15 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 #define WBG_DEVICE_FLAG_TC_TIMEOUT 1
 int wbg_device_flags(unsigned int* flags, int clear);
 
+/* ---- tabulation (calculators/tabulate.py:21-52 Tabulator with Energy, Velocity,
+ * BerryCurvature; evaluate_k.py:9-16 "energy", "band_gradients", "berry_curvature") ----------
+ * For every k and band n, the average over n's degenerate group (gap > degen_thresh) of
+ * E, Re V^a_nn and the Omega trace: tab [nk][nw][7] = (E, V_x, V_y, V_z, Omega_x, Omega_y,
+ * Omega_z) (double).  Xbar and fp64 as wbg_berry_omega (fp64 0 or 1). */
+int wbg_berry_tabulate(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
+                       double degen_thresh, int internal_terms, int external_terms, double* tab, int fp64,
+                       void* stream);
+
 /* ---- stage 4: Berry curvature traces + Fermi-level histogram ----------------------------
  * Xbar [nk][nFbar][nw][nw]: velocity dH/dk at iV..iV+2, A at iA..iA+2, rotA at iO..iO+2.
  * hist [scan.nEF][3] (double) is accumulated (not cleared).

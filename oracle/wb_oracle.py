@@ -553,6 +553,30 @@ class Morb_Hpm(_TermsFormula):  # formula/covariant.py:424-449
 # ---------------------------------------------------------------------------
 # Results (result/energyresult.py, minimal)
 # ---------------------------------------------------------------------------
+def evaluate_k(system, k, quantities, iband=None, degen_thresh=1e-4):
+    """evaluate_k.py:33-131 with the Tabulators of calculators/tabulate.py:21-52 and the named
+    quantities of evaluate_k.py:9-16: a 1x1x1 grid block at dK = k; every band gets the trace
+    of its degenerate group (whole band range, no sea group) divided by the group size."""
+    data = DataK(system, (1, 1, 1), np.array(k, dtype=float))
+    nw = system.num_wann
+    groups = data.get_bands_in_range_groups_ik(0, -np.inf, np.inf, degen_thresh=degen_thresh, sea=False)
+    formulas = {'energy': lambda: Eavln(data),
+                'band_gradients': lambda: data.covariant('Ham', gender=1),
+                'berry_curvature': lambda: Omega(data),
+                'berry_curvature_internal_terms': lambda: Omega(data, external_terms=False),
+                'berry_curvature_external_terms': lambda: Omega(data, internal_terms=False)}
+    out = {}
+    for q in quantities:
+        f = formulas[q]()
+        vals = np.zeros((nw,) + (3,) * f.ndim)
+        for (a, b) in groups:
+            inn = np.arange(a, b)
+            outer = np.concatenate((np.arange(0, a), np.arange(b, nw))).astype(int)
+            vals[a:b] = f.trace(0, inn, outer) / (b - a)
+        out[q] = vals if iband is None else vals[list(np.atleast_1d(iband))]
+    return out
+
+
 class EnergyResult:
     def __init__(self, Energies, data):
         self.Energies = Energies if isinstance(Energies, (list, tuple)) else [Energies]

@@ -18,6 +18,9 @@ Fixtures written (all small, complex128/float64):
   (Ham, AA, BB, CC only) and the stored formula traces
   ``tests/reference/formula/{Omega,DerOmega,Morb_H,Dcov,DerDcov,DEinv_ln}.npz``
   (settings of ``tests/test_formula.py:18-41,171-213``).
+* ``evaluate_k_ref.npz`` -- the reference's ``evaluate_k`` (energy, band_gradients,
+  berry_curvature and its internal / external parts) on the random system at three
+  k-points and on the Fe system at k = (0.1, 0.2, 0.3), bands 4 and 5.
 * ``synthetic_ref.npz`` -- outputs of the reference's ``wannierberri.run`` /
   ``Data_K_R`` on small seeded models with the structure of the benchmark
   configurations (cubic nw=8 / triclinic nw=6 with MDRS / spinor nw=8), made by
@@ -154,6 +157,23 @@ def main(ref_root):
     for k, v in r.items():
         out['c3_run_' + k] = v
     np.savez_compressed(os.path.join(HERE, 'synthetic_ref.npz'), **out)
+
+    # ---- 4. evaluate_k (evaluate_k.py:33-131) on the random and Fe systems
+    ev = {}
+    qs = ['energy', 'band_gradients', 'berry_curvature', 'berry_curvature_internal_terms',
+          'berry_curvature_external_terms']
+    kpts = np.array([[0.1, 0.2, 0.3], [0.0, 0.0, 0.0], [0.45, -0.31, 0.12]])
+    ev['random_k'] = kpts
+    for i, kp in enumerate(kpts):
+        r = wb.evaluate_k(rs, k=kp, quantities=qs, return_single_as_dict=True)
+        for q in qs:
+            ev[f'random_{i}_{q}'] = r[q]
+    fek = np.array([0.1, 0.2, 0.3])
+    ev['fe_k'] = fek
+    r = wb.evaluate_k(fe, k=fek, quantities=qs, iband=[4, 5], return_single_as_dict=True)
+    for q in qs:
+        ev[f'fe_{q}'] = r[q]
+    np.savez_compressed(os.path.join(HERE, 'evaluate_k_ref.npz'), **ev)
     print("wrote fixtures to", HERE)
 
 

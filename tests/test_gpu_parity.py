@@ -429,3 +429,48 @@ def test_omega_hermitian_column_kernel(c2small):
         _lib.check(st, "wbg_berry_omega")
         out.append(calc._hist.cpu().numpy().copy())
     assert np.abs(out[0] - out[1]).max() <= 1e-5 * np.abs(out[1]).max()
+
+
+EVK_QS = ['energy', 'band_gradients', 'berry_curvature', 'berry_curvature_internal_terms',
+          'berry_curvature_external_terms']
+
+
+def _golden_system(golden_dir, name):
+    import os
+    f = np.load(os.path.join(golden_dir, name))
+    XX = {k[5:]: f[k] for k in f.files if k.startswith('XX_R_')}
+    return wsys.System_R.from_arrays(f['real_lattice'], f['iRvec'], f['wannier_centers_cart'], XX)
+
+
+def test_evaluate_k_golden(golden_dir):
+    """wbgpu.evaluate_k (FP64) against the reference's own evaluate_k: random system at three
+    k-points, Fe (bands 4, 5) at k = (0.1, 0.2, 0.3); rel 1e-8 as tests/test_evaluate_k.py."""
+    import os
+    g = np.load(os.path.join(golden_dir, 'evaluate_k_ref.npz'))
+    rs = _golden_system(golden_dir, 'random_system.npz')
+    for i, kp in enumerate(g['random_k']):
+        got = wbgpu.evaluate_k(rs, k=kp, quantities=EVK_QS)
+        for q in EVK_QS:
+            ref = g[f'random_{i}_{q}']
+            assert np.allclose(got[q], ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), (i, q)
+    fe = _golden_system(golden_dir, 'fe_system.npz')
+    got = wbgpu.evaluate_k(fe, k=g['fe_k'], quantities=EVK_QS, iband=[4, 5])
+    for q in EVK_QS:
+        ref = g[f'fe_{q}']
+        assert np.allclose(got[q], ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), q
+    single = wbgpu.evaluate_k(rs, k=g['random_k'][0], quantities=['energy'])
+    assert np.allclose(single, g['random_0_energy'], rtol=1e-10)
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_tabulate_grid_vs_oracle(c2small, precision, tol):
+    """Grid tabulation (MDRS system) against the oracle's evaluate_k at every k-point."""
+    s, o = c2small
+    grid = wbgpu.Grid(s, NKdiv=2, NKFFT=(3, 2, 2))
+    tab = wbgpu.tabulate(s, grid, quantities=EVK_QS, precision=precision)
+    assert tab['kpoints'].shape == (grid.nblocks * 12, 3)
+    for ik in range(0, len(tab['kpoints']), 7):
+        ref = O.evaluate_k(o, tab['kpoints'][ik], EVK_QS)
+        for q in EVK_QS:
+            r = ref[q]
+            assert np.abs(tab[q][ik] - r).max() <= tol * max(np.abs(r).max(), 1e-12), (ik, q)

@@ -157,3 +157,29 @@ def test_synthetic_c3_run(synth):
                                         'ahc': O.AHC(Efermi=EF3)})
     assert maxrel(r['opt'].data, synth['c3_run_opt']) < 1e-10
     assert maxrel(r['ahc'].data, synth['c3_run_ahc']) < 1e-9
+
+
+EVK_QS = ['energy', 'band_gradients', 'berry_curvature', 'berry_curvature_internal_terms',
+          'berry_curvature_external_terms']
+
+
+def test_oracle_evaluate_k_golden(golden_dir):
+    """The oracle's evaluate_k against the reference's own evaluate_k (random system at three
+    k-points, Fe at one k-point, bands 4-5); acceptance of tests/test_evaluate_k.py: rel 1e-8."""
+    import os
+    g = np.load(os.path.join(golden_dir, 'evaluate_k_ref.npz'))
+    f = np.load(os.path.join(golden_dir, 'random_system.npz'))
+    rs = O.RSystem(f['real_lattice'], f['iRvec'], f['wannier_centers_cart'],
+                   {k[5:]: f[k] for k in f.files if k.startswith('XX_R_')})
+    for i, kp in enumerate(g['random_k']):
+        got = O.evaluate_k(rs, kp, EVK_QS)
+        for q in EVK_QS:
+            ref = g[f'random_{i}_{q}']
+            assert np.allclose(got[q], ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), (i, q)
+    f = np.load(os.path.join(golden_dir, 'fe_system.npz'))
+    fe = O.RSystem(f['real_lattice'], f['iRvec'], f['wannier_centers_cart'],
+                   {k[5:]: f[k] for k in f.files if k.startswith('XX_R_')})
+    got = O.evaluate_k(fe, g['fe_k'], EVK_QS, iband=[4, 5])
+    for q in EVK_QS:
+        ref = g[f'fe_{q}']
+        assert np.allclose(got[q], ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), q

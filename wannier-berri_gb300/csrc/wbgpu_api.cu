@@ -75,6 +75,21 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 
 int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
 
+int wbg_berry_tabulate(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
+                       double degen_thresh, int internal_terms, int external_terms, double* tab, int fp64,
+                       void* stream) {
+  if (!tab) return WBG_STATUS_BAD_ARGUMENT;
+  WbgScan sp;
+  sp.EFmin = -1e300;  // every degenerate group is in the window; no sea group
+  sp.EFmax = 1e300;
+  sp.dEF = 1.0;
+  sp.degen_thresh = degen_thresh;
+  sp.nEF = 1;
+  sp.reserved = 0;
+  return wbg_berry_omega_run(E, Xbar, nFbar, iV, iA, iO, nw, nk, &sp, internal_terms, external_terms, nullptr,
+                             fp64 ? 1 : 0, (cudaStream_t)stream, tab);
+}
+
 int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                     const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
                     void* stream) {

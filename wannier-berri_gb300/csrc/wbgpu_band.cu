@@ -362,10 +362,14 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
 // Xbar layout: [k][nFbar][nw][nw]; V at iV..iV+2, A at iA..iA+2, O(rotAA) at iO..iO+2.
 // hist: [nEF][3] doubles, accumulated with atomics (FP64).
 // ---------------------------------------------------------------------------------------
+// With tab != nullptr (tabulation, calculators/tabulate.py:21-52): no histogram; every band n
+// gets the average over its degenerate group of the trace, the energy and Re V_nn, written to
+// tab[k][n][0..6] = (E, V_x, V_y, V_z, Omega_x, Omega_y, Omega_z).  The caller passes an
+// unbounded window (EFmin = -inf, EFmax = +inf), so there is no sea group.
 template <typename T>
 __global__ void berry_omega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                    int iV, int iA, int iO, int nw, int nk, int L, int G, WbgScan sp, int internal_terms,
-                                   int external_terms, double* __restrict__ hist) {
+                                   int external_terms, double* __restrict__ hist, double* __restrict__ tab) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][3]
@@ -455,7 +459,21 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
       for (int g = 0; g < 3; ++g) myT[n * 3 + g] = t[g];
     }
     __syncwarp();
-    if (valid) {
+    if (valid && tab) {
+      for (int n = lane; n < nw; n += L) {
+        int gs = n, ge = n + 1;
+        while (!myS[gs]) --gs;
+        while (ge < nw && !myS[ge]) ++ge;
+        double v[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int q = gs; q < ge; ++q) {
+          v[0] += myE[q];
+          for (int a = 0; a < 3; ++a) v[1 + a] += (double)Xk[(iV + a) * nw2 + q * nw + q].x;
+          for (int g = 0; g < 3; ++g) v[4 + g] += myT[q * 3 + g];
+        }
+        const double inv = 1.0 / (double)(ge - gs);
+        for (int i = 0; i < 7; ++i) tab[(k * nw + n) * 7 + i] = v[i] * inv;
+      }
+    } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
         bool sea = false;
@@ -485,8 +503,9 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
     __syncwarp();
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
-    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (hist)
+    for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
+      if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1115,13 +1134,13 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
 
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                         const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
-                        cudaStream_t stream) {
-  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E || !Xbar) return WBG_ERR_ARG;
+                        cudaStream_t stream, double* tab) {
+  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || (!hist && !tab) || !E || !Xbar) return WBG_ERR_ARG;
   if (iV < 0 || iV + 3 > nFbar) return WBG_ERR_ARG;
   if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar)) return WBG_ERR_ARG;
   if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   if (fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
-  if (fp64 == 2 && nw <= 32) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
+  if (fp64 == 2 && nw <= 32 && !tab) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
     const int G = 4;  // k-points (warps) per block
     const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * (8 + 24 + 8 + 4);
     if (sm > 220 * 1024) return WBG_ERR_SIZE;
@@ -1148,11 +1167,11 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (fp64) {
     cudaFuncSetAttribute(berry_omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                 G, *sp, internal_terms, external_terms, hist);
+                                                                 G, *sp, internal_terms, external_terms, hist, tab);
   } else {
     cudaFuncSetAttribute(berry_omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                G, *sp, internal_terms, external_terms, hist);
+                                                                G, *sp, internal_terms, external_terms, hist, tab);
   }
   return wbg_cuda_status(cudaGetLastError());
 }

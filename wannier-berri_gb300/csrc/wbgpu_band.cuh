@@ -16,7 +16,7 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream);
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                         const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
-                        cudaStream_t stream);
+                        cudaStream_t stream, double* tab = nullptr);
 int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
                        int nk, const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
                        cudaStream_t stream);

@@ -10,6 +10,7 @@ from .run import run
 from . import calculators, models, engine, serve
 from .result import EnergyResult, ResultDict
 from .serve import Server, run_many
+from .tabulate import evaluate_k, tabulate
 
-__all__ = ['System_R', 'Grid', 'run', 'calculators', 'models', 'engine', 'serve', 'Server', 'run_many', 'EnergyResult',
-           'ResultDict']
+__all__ = ['System_R', 'Grid', 'run', 'calculators', 'models', 'engine', 'serve', 'Server', 'run_many', 'evaluate_k',
+           'tabulate', 'EnergyResult', 'ResultDict']
