@@ -44,11 +44,13 @@ CPU_SAMPLE_NKFFT = 12
 THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
 
 
-def build_system():
+def build_system(device=None):
+    """The nw=32 MDRS model; device='cuda' runs the Wigner-Seitz replica search on the GPU
+    (same replica set as the host search)."""
     from wbgpu import models, System_R
     d = models.config_system(2)
     s = System_R.from_dict(d)
-    s.do_ws_dist(9)
+    s.do_ws_dist(9, device=device)
     return s
 
 
@@ -243,7 +245,7 @@ def run_gpu(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group('nccl')
-    s = build_system()
+    s = build_system(device='cuda')
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1

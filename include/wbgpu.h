@@ -86,6 +86,14 @@ const char* wbg_status_string(int status);
 int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, const int* field_desc, int nfields,
                    const double* wcc, const wbg_lattice* lat, int prec, void* XF, void* stream);
 int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int prec, size_t* bytes);
+/* MDRS replica search (system/system_R.py:572-588 do_ws_dist, fourier/rvectors.py:57-227):
+ * for every shift s (shifts [nshift][3], reduced t_n - t_m) and grid point p (pts [npt][3],
+ * the mp grid), the images R = pts[p] + sup[q] (sup [nsup][3], supercell offsets) with the
+ * smallest |(R + s) L|, ties within tol: count [nshift][npt], and the first maxrep image
+ * indices q in repq [nshift][npt][maxrep] (count > maxrep: repeat with more room).  Setup
+ * step, once per system; all pointers on the device. */
+int wbg_ws_replicas(const double* shifts, int nshift, const int* pts, int npt, const int* sup, int nsup,
+                    const wbg_lattice* lat, double tol, int maxrep, int* count, int* repq, void* stream);
 int wbg_r2k(const void* XF, int nfields, const int* pair_start, const int* r2, const int* slice_start,
             const int* pair_r1, const int* slice_r0, const void* ph0, const void* ph1, const void* ph2, int nblocks,
             int prec, void* workspace, size_t workspace_bytes, void* fields_out, const wbg_r2k_geom* g,

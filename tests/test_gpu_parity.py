@@ -474,3 +474,16 @@ def test_tabulate_grid_vs_oracle(c2small, precision, tol):
         for q in EVK_QS:
             r = ref[q]
             assert np.abs(tab[q][ik] - r).max() <= tol * max(np.abs(r).max(), 1e-12), (ik, q)
+
+
+@pytest.mark.parametrize("nw,half,mp", [(6, 1, 3), (16, 2, 5)])
+def test_mdrs_device_search_matches_host(nw, half, mp):
+    """do_ws_dist with the replica search on the GPU gives exactly the host's replica set and
+    matrices (triclinic lattice, random Wannier centres)."""
+    d = models.random_tb(nw, half, models.triclinic_lattice(np.random.default_rng(nw)), 1.5, 77 + nw,
+                         centers='random', keys=('Ham', 'AA'))
+    a = wsys.System_R.from_dict(d).do_ws_dist(mp)
+    b = wsys.System_R.from_dict(d).do_ws_dist(mp, device='cuda')
+    assert np.array_equal(a.iRvec, b.iRvec)
+    for key in ('Ham', 'AA'):
+        assert np.array_equal(a.get_R_mat(key), b.get_R_mat(key))

@@ -75,6 +75,12 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 
 int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
 
+int wbg_ws_replicas(const double* shifts, int nshift, const int* pts, int npt, const int* sup, int nsup,
+                    const wbg_lattice* lat, double tol, int maxrep, int* count, int* repq, void* stream) {
+  return wbg_ws_replicas_run(shifts, nshift, pts, npt, sup, nsup, lat, tol, maxrep, count, repq,
+                             (cudaStream_t)stream);
+}
+
 int wbg_berry_tabulate(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
                        double degen_thresh, int internal_terms, int external_terms, double* tab, int fp64,
                        void* stream) {

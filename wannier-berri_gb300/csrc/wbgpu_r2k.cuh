@@ -24,3 +24,5 @@ int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, con
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
                 size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, const int* cols, int ncols,
                 cudaStream_t stream);
+int wbg_ws_replicas_run(const double* shifts, int nshift, const int* pts, int npt, const int* sup, int nsup,
+                        const R2KLattice* lat, double tol, int maxrep, int* count, int* repq, cudaStream_t stream);

@@ -100,11 +100,12 @@ class System_R:
             rec[i] += max(R.max(), 0) - min(R.min(), 0)
         return rec
 
-    def do_ws_dist(self, mp_grid, ws_dist_tol=1e-5):
-        """MDRS: replace (iRvec, XX_R) by the Wigner-Seitz replica set (system/system_R.py:572-588)."""
+    def do_ws_dist(self, mp_grid, ws_dist_tol=1e-5, device=None):
+        """MDRS: replace (iRvec, XX_R) by the Wigner-Seitz replica set (system/system_R.py:572-588).
+        device: None searches the replicas on the host, 'cuda' with the wbg_ws_replicas kernel."""
         mp = np.array(mp_grid if np.ndim(mp_grid) else [mp_grid] * 3, dtype=int)
         self.iRvec, self._XX_R = mdrs_remap(self.real_lattice, self.wannier_centers_red, self.iRvec,
-                                            self._XX_R, mp, ws_dist_tol)
+                                            self._XX_R, mp, ws_dist_tol, device=device)
         self._NKFFT_recommended = mp
         return self
 
@@ -114,48 +115,98 @@ def _grid_points(mp):
     return g.reshape(-1, 3)
 
 
-def mdrs_remap(real_lattice, wcc_red, iRvec_old, XX_R, mp, tol=1e-5, search=3):
+def _ws_search_host(real_lattice, ushift, pts, sup, tol):
+    """Replica search on the host: for every shift s and grid point p, the supercell offsets q
+    with the smallest |(pts[p] + sup[q] + s) L|, ties within tol -> flat (s, p, q) arrays."""
+    cRs = (pts[:, None, :] + sup[None, :, :]).dot(real_lattice)  # (npt, nsup, 3)
+    out_s, out_p, out_q = [], [], []
+    for si, sh in enumerate(ushift):
+        dist = np.linalg.norm(cRs + sh.dot(real_lattice), axis=2)
+        sel = np.abs(dist - dist.min(axis=1, keepdims=True)) < tol
+        p, q = np.nonzero(sel)
+        out_s.append(np.full(len(p), si))
+        out_p.append(p)
+        out_q.append(q)
+    return np.concatenate(out_s), np.concatenate(out_p), np.concatenate(out_q)
+
+
+def _ws_search_device(real_lattice, ushift, pts, sup, tol, device):
+    """The same search with the wbg_ws_replicas kernel (one thread per (shift, grid point))."""
+    import ctypes
+    import torch
+    from . import _lib
+    lib = _lib.load()
+    dev = torch.device(device)
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
+    sh, pt, su = t(ushift, np.float64), t(pts, np.int32), t(sup, np.int32)
+    lat = _lib.Lattice()
+    for i, v in enumerate(np.asarray(real_lattice, dtype=float).reshape(-1)):
+        lat.L[i] = float(v)
+    nS, npt = len(ushift), len(pts)
+    maxrep = 8
+    while True:
+        count = torch.empty((nS, npt), dtype=torch.int32, device=dev)
+        repq = torch.empty((nS, npt, maxrep), dtype=torch.int32, device=dev)
+        st = lib.wbg_ws_replicas(ctypes.c_void_p(sh.data_ptr()), nS, ctypes.c_void_p(pt.data_ptr()), npt,
+                                 ctypes.c_void_p(su.data_ptr()), len(sup), ctypes.byref(lat), ctypes.c_double(tol),
+                                 maxrep, ctypes.c_void_p(count.data_ptr()), ctypes.c_void_p(repq.data_ptr()),
+                                 ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+        _lib.check(st, "wbg_ws_replicas")
+        c = count.cpu().numpy()
+        if c.max() <= maxrep:
+            break
+        maxrep = int(c.max())
+    r = repq.cpu().numpy()
+    s_idx, p_idx = np.nonzero(np.ones_like(c, dtype=bool))
+    n = c.reshape(-1)
+    keep = np.arange(maxrep)[None, :] < n[:, None]
+    return (np.repeat(s_idx, n), np.repeat(p_idx, n), r.reshape(-1, maxrep)[keep])
+
+
+def mdrs_remap(real_lattice, wcc_red, iRvec_old, XX_R, mp, tol=1e-5, search=3, device=None):
     """Vectorised MDRS.  For every distinct centre shift t_n - t_m (rounded like
     rvectors.py:75-82) each mp-grid point is mapped to its Wigner-Seitz-nearest
     replicas R (distance ties within ``tol``), the matrix element divided by the
-    number of replicas.  All-zero R-vectors are dropped (rvectors.py:111-123)."""
+    number of replicas.  All-zero R-vectors are dropped (rvectors.py:111-123).
+    ``device``: None searches on the host, a CUDA device runs the search kernel; both give
+    the same replica sets."""
     nw = wcc_red.shape[0]
     ndig = int(np.ceil(-np.log10(tol))) + 1
     shifts = np.round(-wcc_red[:, None, :] + wcc_red[None, :, :], ndig).reshape(-1, 3)
     ushift, sidx = np.unique(shifts, axis=0, return_inverse=True)
-    sidx = sidx.reshape(nw, nw)
+    sidx = sidx.reshape(-1)
     pts = _grid_points(mp)
     sup = np.stack(np.meshgrid(*[np.arange(-search, search + 1)] * 3, indexing='ij'), axis=-1).reshape(-1, 3) * mp
-    iRs = pts[:, None, :] + sup[None, :, :]                 # (npt, nsup, 3)
-    cRs = iRs.dot(real_lattice)
+    if device is None:
+        rs, rp, rq = _ws_search_host(real_lattice, ushift, pts, sup, tol)
+    else:
+        rs, rp, rq = _ws_search_device(real_lattice, ushift, pts, sup, tol, device)
+    # replicas sorted by shift: rows start[s] .. start[s+1] belong to shift s
+    order = np.lexsort((rq, rp, rs))
+    rs, rp, rq = rs[order], rp[order], rq[order]
+    ndeg = np.zeros((len(ushift), len(pts)), dtype=np.int64)
+    np.add.at(ndeg, (rs, rp), 1)
+    rw = 1.0 / ndeg[rs, rp]
+    rR = pts[rp] + sup[rq]
+    start = np.searchsorted(rs, np.arange(len(ushift) + 1))
     # grid representation of the old matrices: sum of R-vectors equal mod mp
     gidx_old = np.ravel_multi_index(tuple((iRvec_old % mp).T), tuple(mp))
-    grids = {}
+    allR, iR = np.unique(rR, axis=0, return_inverse=True)
+    iR = iR.reshape(-1)
+    # every (m, n) takes the replicas of its shift: one flat scatter for all elements
+    lens = (start[1:] - start[:-1])[sidx]
+    mn = np.repeat(np.arange(nw * nw), lens)
+    offs = np.arange(lens.sum()) - np.repeat(np.cumsum(lens) - lens, lens)
+    ridx = start[sidx[mn]] + offs
+    m_e, n_e = np.divmod(mn, nw)
+    new = {}
     for key, X in XX_R.items():
         g = np.zeros((len(pts),) + X.shape[1:], dtype=complex)
         np.add.at(g, gidx_old, X)
-        grids[key] = g
-    replicas = []
-    for s in ushift:
-        dist = np.linalg.norm(cRs + s.dot(real_lattice), axis=2)
-        sel = np.abs(dist - dist.min(axis=1, keepdims=True)) < tol
-        ndeg = sel.sum(axis=1)
-        p, q = np.nonzero(sel)
-        replicas.append((iRs[p, q], p, 1.0 / ndeg[p]))
-    allR = np.unique(np.concatenate([r[0] for r in replicas]), axis=0)
-    off = allR.min(axis=0)
-    span = allR.max(axis=0) - off + 1
-    code = lambda R: np.ravel_multi_index(tuple((R - off).T), tuple(span))
-    lookup = np.full(np.prod(span), -1, dtype=np.int64)
-    lookup[code(allR)] = np.arange(len(allR))
-    new = {key: np.zeros((len(allR),) + g.shape[1:], dtype=complex) for key, g in grids.items()}
-    for si, (R, p, w) in enumerate(replicas):
-        ms, ns = np.nonzero(sidx == si)
-        iR = lookup[code(R)]
-        for key, g in grids.items():
-            extra = (1,) * (g.ndim - 3)
-            new[key][iR[:, None], ms[None, :], ns[None, :]] = \
-                g[p[:, None], ms[None, :], ns[None, :]] * w.reshape((-1, 1) + extra)
+        out = np.zeros((len(allR),) + X.shape[1:], dtype=complex)
+        w = rw[ridx].reshape((-1,) + (1,) * (X.ndim - 3))
+        out[iR[ridx], m_e, n_e] = g[rp[ridx], m_e, n_e] * w
+        new[key] = out
     keep = np.zeros(len(allR), dtype=bool)
     for X in new.values():
         keep |= np.abs(X.reshape(len(allR), -1)).max(axis=1) > 1e-8
