@@ -164,6 +164,20 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 #define WBG_DEVICE_FLAG_TC_TIMEOUT 1
 int wbg_device_flags(unsigned int* flags, int clear);
 
+/* ---- generic Fermi-level scan of additive group traces (calculators/static.py:60-169) ------
+ * formula WBG_FORMULA_IDENTITY: group size (CumDOS / DOS, calculators/static.py:192-214), 1
+ *   component; WBG_FORMULA_INVMASS: the inverse-mass tensor dV^b/dk_d (formula/elementary.py:28-34,
+ *   Ohmic_FermiSea), Xbar: V at iV..iV+2, d^2H/dk_b dk_d at iW..iW+8, 9 components;
+ *   WBG_FORMULA_VELVEL: in-group V^a V^b (formula/covariant.py:817-820, Ohmic_FermiSurf), 9.
+ * sea != 0: Fermi-sea weights (fder 0), sea == 0: Fermi-surface groups only (fder >= 1; the
+ * caller takes the finite differences over the extended levels).  hist [nEF][ncomp] (double)
+ * is accumulated; component (b, d) at 3 b + d.  Xbar may be NULL for WBG_FORMULA_IDENTITY. */
+#define WBG_FORMULA_IDENTITY 0
+#define WBG_FORMULA_INVMASS 1
+#define WBG_FORMULA_VELVEL 2
+int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
+                   int formula, int sea, double* hist, int fp64, void* stream);
+
 /* ---- tabulation (calculators/tabulate.py:21-52 Tabulator with Energy, Velocity,
  * BerryCurvature; evaluate_k.py:9-16 "energy", "band_gradients", "berry_curvature") ----------
  * For every k and band n, the average over n's degenerate group (gap > degen_thresh) of

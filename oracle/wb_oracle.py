@@ -35,6 +35,8 @@ EV_AU = physical_constants['electron volt-hartree relationship'][0]
 FACTOR_AHC = -(elementary_charge ** 2 / hbar / angstrom)      # factors.py:25
 FACTOR_OPT = -FACTOR_AHC                                       # factors.py:36
 FACTOR_MORB = -EV_AU / BOHR ** 2                               # calculators/static.py:237
+TAU_UNIT = 1e-15                                               # factors.py:3
+FACTOR_OHMIC = (elementary_charge ** 2 / hbar / angstrom * TAU_UNIT * elementary_charge / hbar)  # factors.py:26
 
 
 # ---------------------------------------------------------------------------
@@ -437,6 +439,32 @@ class DerDcov(Dcov):  # formula/elementary.py:55-70
         return s
 
 
+class Identity(Formula_ln):  # formula/covariant.py:10-22
+    def __init__(self, data_K=None, **_):
+        self.ndim = 0
+
+    def nn(self, ik, inn, out):
+        return np.eye(len(inn))
+
+    def ln(self, ik, inn, out):
+        return np.zeros((len(out), len(inn)))
+
+
+class InvMass(Matrix_GenDer_ln):  # formula/elementary.py:28-34: generalised derivative of V
+    def __init__(self, data_K, **_):
+        super().__init__(data_K.covariant('Ham', commader=1), data_K.covariant('Ham', commader=2), data_K.Dcov)
+
+
+class VelVel(Formula_ln):  # formula/covariant.py:817-820 with formula/formula.py:121-151 (product of nn blocks)
+    def __init__(self, data_K, **_):
+        self.V = data_K.covariant('Ham', commader=1)
+        self.ndim = 2
+
+    def nn(self, ik, inn, out):
+        v = self.V.nn(ik, inn, out)
+        return np.einsum("LMa,MNb->LNab", v, v)
+
+
 class _TermsFormula(Formula_ln):
     """formula/formula.py:12-29: internal/external term switches."""
 
@@ -650,6 +678,35 @@ class StaticCalculator:
         restot /= data_K.nk
         restot *= self.constant_factor if self.use_factor else np.sign(self.constant_factor)
         return EnergyResult(self.Efermi, restot)
+
+
+class CumDOS(StaticCalculator):  # calculators/static.py:192-214 (_DOS, fder 0), times the cell volume
+    fder = 0
+    Formula = Identity
+
+    def __call__(self, data_K):
+        r = super().__call__(data_K)
+        return EnergyResult(r.Energies, r.data * data_K.cell_volume)
+
+
+class DOS(CumDOS):  # calculators/static.py:203-207 (fder 1)
+    fder = 1
+
+
+class Ohmic_FermiSea(StaticCalculator):  # calculators/static.py:379-390
+    fder = 0
+    Formula = InvMass
+
+    def __init__(self, constant_factor=FACTOR_OHMIC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class Ohmic_FermiSurf(StaticCalculator):  # calculators/static.py:393-403
+    fder = 1
+    Formula = VelVel
+
+    def __init__(self, constant_factor=FACTOR_OHMIC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
 
 
 class AHC(StaticCalculator):  # calculators/static.py:353-364

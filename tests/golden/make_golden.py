@@ -12,7 +12,8 @@ Fixtures written (all small, complex128/float64):
 
 * ``random_system.npz`` + ``random_results.npz`` -- the reference's own test
   system ``tests/data/random`` (nw=6, nR=20) and its stored golden results
-  ``tests/reference/integrate_files/random-{ahc,Morb,opt_conductivity}_iter-0000.npz``
+  ``tests/reference/integrate_files/random-{ahc,Morb,opt_conductivity,dos,cumdos,
+  conductivity_ohmic,conductivity_ohmic_fsurf}_iter-0000.npz``
   (settings of ``tests/test_run.py:653-669``: NK=6, NKFFT=3, E_F=linspace(-2,2,5)).
 * ``fe_system.npz`` + ``fe_formula.npz`` -- ``tests/reference/systems/system_Fe_sym_W90_OSD``
   (Ham, AA, BB, CC only) and the stored formula traces
@@ -98,7 +99,7 @@ def main(ref_root):
     rs = System_R.from_npz(path=os.path.join(ref_root, 'tests', 'data', 'random'), legacy=True)
     np.savez_compressed(os.path.join(HERE, 'random_system.npz'), **pack_system('', rs, ['Ham', 'AA', 'BB', 'CC']))
     res = {}
-    for q in ['ahc', 'Morb', 'opt_conductivity']:
+    for q in ['ahc', 'Morb', 'opt_conductivity', 'dos', 'cumdos', 'conductivity_ohmic', 'conductivity_ohmic_fsurf']:
         f = np.load(os.path.join(ref_root, 'tests', 'reference', 'integrate_files', f'random-{q}_iter-0000.npz'),
                     allow_pickle=True)
         res[q + '_data'] = f['data']

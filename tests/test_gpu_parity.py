@@ -487,3 +487,39 @@ def test_mdrs_device_search_matches_host(nw, half, mp):
     assert np.array_equal(a.iRvec, b.iRvec)
     for key in ('Ham', 'AA'):
         assert np.array_equal(a.get_R_mat(key), b.get_R_mat(key))
+
+
+@pytest.mark.parametrize("precision,rule", [('fp64', 1e-8), ('mixed', 1e-5)])
+def test_golden_random_dos_ohmic(golden_dir, precision, rule):
+    """DOS, CumDOS, Ohmic_FermiSea (inverse mass) and Ohmic_FermiSurf (v v f') against the
+    reference's own golden files random-{dos,cumdos,conductivity_ohmic,conductivity_ohmic_fsurf}
+    (tests/test_run.py:653-669 settings); FP64 with the reference's 1e-8 rule."""
+    import os
+    rs = _golden_system(golden_dir, 'random_system.npz')
+    ref = np.load(os.path.join(golden_dir, 'random_results.npz'))
+    EF = np.linspace(-2, 2, 5)
+    C = wbgpu.calculators
+    calcs = {'dos': C.DOS(Efermi=EF), 'cumdos': C.CumDOS(Efermi=EF), 'conductivity_ohmic': C.Ohmic_FermiSea(Efermi=EF),
+             'conductivity_ohmic_fsurf': C.Ohmic_FermiSurf(Efermi=EF), 'ahc': C.AHC(Efermi=EF)}
+    # the reference's random system is not Hermitian in R-space: the mixed path must keep full
+    # matrices and the reference's symmetrisation
+    assert engine.DeviceSystem(rs).hermitian_bases() == frozenset()
+    res = wbgpu.run(rs, wbgpu.Grid(rs, NKdiv=2, NKFFT=3), calcs, precision=precision)
+    for key in calcs:
+        got, exp = res[key].data, ref[key + '_data']
+        assert got.shape == exp.shape, (key, got.shape, exp.shape)
+        assert np.abs(got - exp).max() < rule * np.abs(exp).max(), (key, np.abs(got - exp).max() / np.abs(exp).max())
+
+
+def test_dos_ohmic_c2small_vs_oracle(c2small):
+    """Same calculators on the MDRS model against the oracle, FP64 to 1e-9."""
+    s, o = c2small
+    EF = np.linspace(-1.5, 1.5, 31)
+    C = wbgpu.calculators
+    got = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(4, 3, 3)),
+                    {'dos': C.DOS(Efermi=EF), 'cumdos': C.CumDOS(Efermi=EF), 'om': C.Ohmic_FermiSea(Efermi=EF),
+                     'os': C.Ohmic_FermiSurf(Efermi=EF)}, precision='fp64')
+    ref = O.run(o, (2, 2, 2), (4, 3, 3), {'dos': O.DOS(Efermi=EF), 'cumdos': O.CumDOS(Efermi=EF),
+                                          'om': O.Ohmic_FermiSea(Efermi=EF), 'os': O.Ohmic_FermiSurf(Efermi=EF)})
+    for key in ('dos', 'cumdos', 'om', 'os'):
+        assert maxrel(got[key].data, ref[key].data) < 1e-9, key

@@ -37,13 +37,15 @@ def random_res(golden_dir):
 @pytest.fixture(scope="module")
 def random_run(random_sys, random_res):
     EF = np.linspace(-2, 2, 5)
-    calcs = {'ahc': O.AHC(Efermi=EF), 'Morb': O.Morb(Efermi=EF),
+    calcs = {'ahc': O.AHC(Efermi=EF), 'Morb': O.Morb(Efermi=EF), 'dos': O.DOS(Efermi=EF), 'cumdos': O.CumDOS(Efermi=EF),
+             'conductivity_ohmic': O.Ohmic_FermiSea(Efermi=EF), 'conductivity_ohmic_fsurf': O.Ohmic_FermiSurf(Efermi=EF),
              'opt_conductivity': O.OpticalConductivity(Efermi=np.array([17.0, 18.0]), omega=np.arange(0.0, 7.1, 1.0),
                                                        smr_fixed_width=0.20, smr_type="Gaussian")}
     return O.run(random_sys, NKdiv=(2, 2, 2), NKFFT=(3, 3, 3), calculators=calcs)
 
 
-@pytest.mark.parametrize("quant", ['ahc', 'Morb', 'opt_conductivity'])
+@pytest.mark.parametrize("quant", ['ahc', 'Morb', 'opt_conductivity', 'dos', 'cumdos', 'conductivity_ohmic',
+                                   'conductivity_ohmic_fsurf'])
 def test_random_golden(random_run, random_res, quant):
     """Same acceptance rule as the reference: abs err < 1e-8 * max|ref| (tests/common_comparers.py:189-196)."""
     ref = random_res[quant + '_data']

@@ -75,6 +75,11 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 
 int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
 
+int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
+                   int formula, int sea, double* hist, int fp64, void* stream) {
+  return wbg_berry_scan_run(E, Xbar, nFbar, iV, iW, nw, nk, scan, formula, sea, hist, fp64, (cudaStream_t)stream);
+}
+
 int wbg_ws_replicas(const double* shifts, int nshift, const int* pts, int npt, const int* sup, int nsup,
                     const wbg_lattice* lat, double tol, int maxrep, int* count, int* repq, void* stream) {
   return wbg_ws_replicas_run(shifts, nshift, pts, npt, sup, nsup, lat, tol, maxrep, count, repq,

@@ -648,6 +648,132 @@ __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __r
 }
 
 // ---------------------------------------------------------------------------------------
+// Generic Fermi-level scan of additive group traces (calculators/static.py:60-169) for
+//   WBG_FORMULA_IDENTITY  (formula/covariant.py:10-22; CumDOS / DOS)      1 component:  1
+//   WBG_FORMULA_INVMASS   (formula/elementary.py:28-34; Ohmic_FermiSea)   9 components:
+//        Re W^{bd}_nn + sum_{l out of the group} Re(V^d_nl V^b_ln + V^b_nl V^d_ln) / (E_n - E_l)
+//        (the generalised derivative Wbar - D Vbar + Vbar D of formula/formula.py:95-118)
+//   WBG_FORMULA_VELVEL    (formula/covariant.py:817-820; Ohmic_FermiSurf) 9 components:
+//        sum_{n' in the group} Re V^a_nn' V^b_n'n
+// per band n; the group sums are binned like the Omega kernel.  sea != 0: Fermi-sea groups
+// (E below the window add to every level, the sea group); sea == 0: Fermi-surface groups only.
+// hist [nEF][ncomp] (component (b, d) at 3 b + d).
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void berry_scan_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
+                                  int iV, int iW, int nw, int nk, int L, int G, WbgScan sp, int formula, int sea,
+                                  double* __restrict__ hist) {
+  typedef typename C2<T>::t V;
+  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
+  extern __shared__ double smb[];
+  double* sh = smb;                                   // [nEF][nc]
+  double* Es = sh + nc * sp.nEF;                      // [G][nw]
+  double* tv = Es + G * nw;                           // [G][nw][9]
+  int* start = reinterpret_cast<int*>(tv + 9 * G * nw);  // [G][nw]
+  for (int i = threadIdx.x; i < nc * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  double* myE = Es + grp * nw;
+  double* myT = tv + 9 * grp * nw;
+  int* myS = start + grp * nw;
+  const long long nw2 = (long long)nw * nw;
+  for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
+    const long long k = base + grp;
+    const bool valid = k < nk;
+    const long long kk = valid ? k : nk - 1;
+    for (int i = lane; i < nw; i += L) myE[i] = E[kk * nw + i];
+    __syncwarp();
+    for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
+    __syncwarp();
+    int bandmax = 0;
+    if (sea) {
+      int below = 0, f0 = nw;
+      for (int n = lane; n < nw; n += L) {
+        below += myE[n] < sp.EFmin;
+        if (myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+        }
+      }
+      below = group_sum_i(below, L);
+      f0 = group_min_i(f0, L);
+      bandmax = min(below, f0);
+    }
+    const V* Xk = Xbar ? Xbar + kk * nFbar * nw2 : nullptr;
+    for (int n = lane; n < nw; n += L) {
+      int gs = n, ge = n + 1;
+      while (!myS[gs]) --gs;
+      while (ge < nw && !myS[ge]) ++ge;
+      if (n < bandmax) { gs = 0; ge = bandmax; }
+      double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      if (formula == WBG_FORMULA_IDENTITY) {
+        t[0] = 1.0;
+      } else if (formula == WBG_FORMULA_INVMASS) {
+        for (int b = 0; b < 3; ++b)
+          for (int d = 0; d < 3; ++d) t[3 * b + d] = (double)Xk[(iW + 3 * b + d) * nw2 + n * nw + n].x;
+        for (int l = 0; l < nw; ++l) {
+          if (l >= gs && l < ge) continue;
+          const double dE = myE[n] - myE[l];
+          const T dinv = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+          V Vnl[3], Vln[3];
+          for (int a = 0; a < 3; ++a) {
+            Vnl[a] = Xk[(iV + a) * nw2 + n * nw + l];
+            Vln[a] = Xk[(iV + a) * nw2 + l * nw + n];
+          }
+          for (int b = 0; b < 3; ++b)
+            for (int d = 0; d < 3; ++d)
+              t[3 * b + d] += (double)((cmul(Vnl[d], Vln[b]).x + cmul(Vnl[b], Vln[d]).x) * dinv);
+        }
+      } else {  // WBG_FORMULA_VELVEL
+        for (int np = gs; np < ge; ++np) {
+          V Vnp[3], Vpn[3];
+          for (int a = 0; a < 3; ++a) {
+            Vnp[a] = Xk[(iV + a) * nw2 + n * nw + np];
+            Vpn[a] = Xk[(iV + a) * nw2 + np * nw + n];
+          }
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) t[3 * a + b] += (double)cmul(Vnp[a], Vpn[b]).x;
+        }
+      }
+      for (int c = 0; c < 9; ++c) myT[n * 9 + c] = t[c];
+    }
+    __syncwarp();
+    if (valid) {
+      for (int n = lane; n < nw; n += L) {
+        int gs = -1, ge = -1;
+        bool seag = false;
+        if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; seag = true; }
+        else if (n >= bandmax && myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
+        }
+        if (gs < 0) continue;
+        double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, esum = 0.0;
+        for (int q = gs; q < ge; ++q) {
+          for (int c = 0; c < nc; ++c) v[c] += myT[q * 9 + c];
+          esum += myE[q];
+        }
+        int bin = -1;
+        if (seag) bin = 0;
+        else {
+          const double Em = esum / (double)(ge - gs);
+          if (Em < sp.EFmin) bin = 0;  // in range but below the first level: every level
+          else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
+        }
+        if (bin >= 0 && bin < sp.nEF)
+          for (int c = 0; c < nc; ++c) atomicAdd(&sh[bin * nc + c], v[c]);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nc * sp.nEF; i += blockDim.x)
+    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+}
+
+// ---------------------------------------------------------------------------------------
 // Orbital moment, Morb_Hpm (formula/covariant.py:375-449): non-additive, so the trace over
 // inn = [0, n), out = [n, nw) is needed at every group border n (calculators/static.py:109-117).
 // The trace splits into pair functions of bands (m in inn, l in out / n' in inn):
@@ -1172,6 +1298,34 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
     cudaFuncSetAttribute(berry_omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
                                                                 G, *sp, internal_terms, external_terms, hist, tab);
+  }
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const WbgScan* sp,
+                       int formula, int sea, double* hist, int fp64, cudaStream_t stream) {
+  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E) return WBG_ERR_ARG;
+  if (formula < WBG_FORMULA_IDENTITY || formula > WBG_FORMULA_VELVEL) return WBG_ERR_ARG;
+  if (formula != WBG_FORMULA_IDENTITY && (!Xbar || iV < 0 || iV + 3 > nFbar)) return WBG_ERR_ARG;
+  if (formula == WBG_FORMULA_INVMASS && (iW < 0 || iW + 9 > nFbar)) return WBG_ERR_ARG;
+  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
+  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
+  const int L = lanes_for(nw);
+  const int G = 128 / L;
+  const size_t sm = (size_t)nc * sp->nEF * 8 + (size_t)G * nw * (8 + 72 + 4);
+  if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  long long nblk = (nk + G - 1) / G;
+  if (nblk > (long long)sms * 8) nblk = (long long)sms * 8;
+  if (fp64) {
+    cudaFuncSetAttribute(berry_scan_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_scan_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
+                                                                *sp, formula, sea, hist);
+  } else {
+    cudaFuncSetAttribute(berry_scan_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    berry_scan_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
+                                                               *sp, formula, sea, hist);
   }
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -24,3 +24,5 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
                            int idO, int nw, int nk, const WbgScan* sp, int internal_terms, int external_terms,
                            double* hist, int fp64, cudaStream_t stream);
 int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);
+int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const WbgScan* sp,
+                       int formula, int sea, double* hist, int fp64, cudaStream_t stream);

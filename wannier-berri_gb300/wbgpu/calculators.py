@@ -16,7 +16,9 @@ import torch
 from . import _lib
 from . import engine
 from .engine import _ptr, _stream
-from .factors import factor_ahc, factor_morb, factor_opt
+from .factors import factor_ahc, factor_morb, factor_ohmic, factor_opt
+
+WBG_FORMULA_IDENTITY, WBG_FORMULA_INVMASS, WBG_FORMULA_VELVEL = 0, 1, 2  # include/wbgpu.h
 from .result import EnergyResult
 
 
@@ -152,6 +154,74 @@ class BerryDipole_FermiSea(StaticCalculator):
     def result(self, cell_volume, nk, factor=1.0):
         data = self.finalize(cell_volume, nk, factor).reshape(-1, 3, 3)
         return EnergyResult(self.Efermi, data.swapaxes(1, 2))
+
+
+class _ScanCalculator(StaticCalculator):
+    """Static calculators whose group traces go through wbg_berry_scan (calculators/static.py:60-169):
+    Fermi-sea (fder 0) or Fermi-surface (fder 1, central difference over the extended levels)."""
+    formula = None
+    fields = set()
+
+    def quantities(self, system):
+        return set(self.fields)
+
+    def accumulate(self, bd, system):
+        sc = self.scan_struct()
+        g = lambda q: bd.index.get(q, 0)
+        xbar = _ptr(bd.Xbar) if bd.Xbar is not None else None
+        nF = bd.Xbar.shape[1] if bd.Xbar is not None else 0
+        st = engine._timed('berry_scan', _lib.load().wbg_berry_scan, _ptr(bd.E), xbar, nF, g('V'), g('W'), bd.nw,
+                           bd.nk_total, ctypes.byref(sc), self.formula, int(self.fder == 0), _ptr(self._hist),
+                           int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_scan")
+
+    def _data(self, cell_volume, nk, factor):
+        data = self.finalize(cell_volume, nk, factor)
+        if self.fder == 1:  # calculators/static.py:137-140
+            data = (data[2:] - data[:-2]) / (2 * self.dEF)
+        return data
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self._data(cell_volume, nk, factor)
+        if self.ncomp == 9:
+            data = data.reshape(-1, 3, 3)
+        else:
+            data = data.reshape(-1)
+        return EnergyResult(self.Efermi, data)
+
+
+class CumDOS(_ScanCalculator):
+    r"""Cumulative density of states (calculators/static.py:192-214): states per cell below E_F."""
+    formula, fder, ncomp = WBG_FORMULA_IDENTITY, 0, 1
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self._data(cell_volume, nk, factor) * cell_volume  # _DOS.__call__ (static.py:198-200)
+        return EnergyResult(self.Efermi, data.reshape(-1))
+
+
+class DOS(CumDOS):
+    r"""Density of states (calculators/static.py:203-207): states per cell per eV."""
+    fder = 1
+
+
+class Ohmic_FermiSea(_ScanCalculator):
+    r"""Ohmic conductivity (S/m, tau = 1 fs) from the Fermi sea (calculators/static.py:379-390):
+    sigma_ab = e^2/hbar tau \int [dk] d_b v_a f (formula InvMass)."""
+    formula, fder, ncomp = WBG_FORMULA_INVMASS, 0, 9
+    fields = {'V', 'W'}
+
+    def __init__(self, constant_factor=factor_ohmic, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class Ohmic_FermiSurf(_ScanCalculator):
+    r"""Ohmic conductivity (S/m, tau = 1 fs) from the Fermi surface (calculators/static.py:393-403):
+    sigma_ab = -e^2/hbar tau \int [dk] v_a v_b f' (formula VelVel)."""
+    formula, fder, ncomp = WBG_FORMULA_VELVEL, 1, 9
+    fields = {'V'}
+
+    def __init__(self, constant_factor=factor_ohmic, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
 
 
 class OpticalConductivity(Calculator):

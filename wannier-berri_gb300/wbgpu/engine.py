@@ -177,6 +177,27 @@ class DeviceSystem:
         self._cache = {}
         self.h2d_bytes = 0
 
+    def hermitian_bases(self, rtol=1e-12):
+        """Base matrices whose R-space data are Hermitian, X_R = X_{-R}^dagger within rtol of
+        max |X| with every -R present: for them the k-space fields are exactly Hermitian and the
+        mixed path transforms only lower triangles.  Other bases keep the full-matrix path with
+        the reference's symmetrisation (checked once per system)."""
+        if 'herm_bases' not in self._cache:
+            iR = np.asarray(self.system.iRvec)
+            index = {tuple(r): i for i, r in enumerate(iR)}
+            neg = np.array([index.get(tuple(-r), -1) for r in iR])
+            out = set()
+            if (neg >= 0).all():
+                for key in ('Ham', 'AA'):
+                    if not self.system.has_R_mat(key):
+                        continue
+                    X = np.asarray(self.system.get_R_mat(key))
+                    diff = np.abs(X - X[neg].conj().swapaxes(1, 2)).max()
+                    if diff <= rtol * max(np.abs(X).max(), 1e-300):
+                        out.add(key)
+            self._cache['herm_bases'] = frozenset(out)
+        return self._cache['herm_bases']
+
     def bases_for(self, keys):
         """Base-field list for the R->k launch: Ham, then 3 components of each extra key."""
         names = [('Ham', None)]
@@ -279,15 +300,17 @@ def field_plan(quantities, with_H, extra_keys):
     return desc, index
 
 
-def hermitian_fields(quantities, with_H):
-    """Per field of field_plan: True when the k-space field is Hermitian by construction
-    (H, its derivatives, AA and its derivatives / curl); BB and CC are not."""
+def hermitian_fields(quantities, with_H, herm_bases=('Ham', 'AA')):
+    """Per field of field_plan: True when the k-space field is exactly Hermitian -- its base
+    (Ham for H and its derivatives, AA for A, its derivatives and curl) is in `herm_bases`, the
+    bases whose R-space matrices satisfy X_R = X_{-R}^dagger (DeviceSystem.hermitian_bases).
+    BB and CC are never taken as Hermitian."""
     keys = extra_keys_for(quantities)
     desc, _ = field_plan(quantities, with_H, keys)
-    nonherm = set()
+    nonherm = set() if 'Ham' in herm_bases else {0}
     base = 1
     for key in keys:
-        if key in ('BB', 'CC'):
+        if key in ('BB', 'CC') or key not in herm_bases:
             nonherm |= {base, base + 1, base + 2}
         base += 3
     return [d[1] not in nonherm for d in desc]
@@ -299,7 +322,7 @@ def column_list(dev, quantities, with_H, lower):
     key = ('cols', tuple(sorted(quantities)), with_H, bool(lower))
     if key not in dev._cache:
         nw = dev.nw
-        herm = hermitian_fields(quantities, with_H)
+        herm = hermitian_fields(quantities, with_H, dev.hermitian_bases())
         m, n = np.meshgrid(np.arange(nw), np.arange(nw), indexing='ij')
         full = (m * nw + n).reshape(-1)
         tril = (m * nw + n)[m >= n]
@@ -548,13 +571,18 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         fp64_fields = True
     elif precision == 'mixed':
         # lower triangles of the Hermitian fields only: exactly Hermitian, half the transform
-        Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=True)
+        lowerH = 'Ham' in dev.hermitian_bases()  # else the eigensolver symmetrises the full H(k)
+        Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=lowerH)
         keep.append(k0)
         U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
-        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | EIGH_LOWER, work=ework, flag=flag)
-        fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True)
-        keep.append(k1)
-        lower_in = column_list(dev, quantities, False, True)[1]
+        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | (EIGH_LOWER if lowerH else 0), work=ework,
+                          flag=flag)
+        if quantities:
+            fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True)
+            keep.append(k1)
+            lower_in = column_list(dev, quantities, False, True)[1]
+        else:  # energies only (DOS-type calculators): no band-basis fields
+            fields, index, nF, lower_in = None, {}, 0, []
         fp64_fields = False
     else:
         raise ValueError(f"unknown precision mode {precision!r}")

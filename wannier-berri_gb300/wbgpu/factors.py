@@ -6,3 +6,5 @@ eV_au = physical_constants['electron volt-hartree relationship'][0]
 factor_ahc = -(elementary_charge ** 2 / hbar / angstrom)
 factor_opt = -factor_ahc
 factor_morb = -eV_au / bohr ** 2
+TAU_UNIT = 1e-15  # relaxation time unit, fs (factors.py:3)
+factor_ohmic = (elementary_charge ** 2 / hbar / angstrom * TAU_UNIT * elementary_charge / hbar)  # factors.py:26
