@@ -123,9 +123,12 @@ int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, con
  * mode | 4 (WBG_EIGH_LOWER): only the lower triangle (m >= n) of H is read and taken as the
  *         Hermitian matrix (imaginary part of the diagonal ignored) -- the output of
  *         wbg_r2k_columns on the lower triangle.
+ * mode | 8 (WBG_EIGH_VALUES): eigenvalues only (np.linalg.eigvalsh; the tetrahedron corners,
+ *         data_K/data_K_R.py:121-141); U is not written and may be NULL.
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 #define WBG_EIGH_LOWER 4
+#define WBG_EIGH_VALUES 8
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
@@ -177,6 +180,59 @@ int wbg_device_flags(unsigned int* flags, int clear);
 #define WBG_FORMULA_VELVEL 2
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
                    int formula, int sea, double* hist, int fp64, void* stream);
+
+/* ---- tetrahedron method (calculators/static.py:80-125 with tetra=True; grid/tetrahedron.py:
+ * 15-281 TetraWeightsParal; corner energies data_K/data_K_R.py:121-141) ---------------------
+ * The parallelepiped k +- delta/2 (delta = 1/(NKdiv NKFFT) per axis) around each k-point is cut
+ * into 12 tetrahedra.  Its 8 corners are points of the dense grid shifted by +delta/2: corner
+ * block c (c = 0..NKdiv-1 per axis, flat index (c0 div1 + c1) div2 + c2) is the FFT grid at
+ * shift (c + 1/2) delta.  The caller computes their eigenvalues once (wbg_eigh_batched with
+ * WBG_EIGH_VALUES) into Ecorner[row][k][n] and passes corner_slot[flat corner block] = row for
+ * every corner block the batch touches (blocks i and i-1 per axis, i-1 = NKdiv-1 at i = 0).
+ * blocks[b]: flat division-grid index (C order) of batch block b; E [nblocks*nk][nw] the
+ * k-point energies of the batch (blocks in that order, k in C order of the FFT grid). */
+typedef struct {
+  int div[3]; /* NKdiv */
+  int fft[3]; /* NKFFT */
+} wbg_tetra_grid;
+
+/* Bands that take part (tetrahedron.py:215-262 weights_all_band_groups, Emin = -inf):
+ * sel [nblocks*nk][nw] = 1 when the band's degenerate group (by E, gap > degen_thresh) is in
+ * the window (largest corner energy >= EF0, smallest <= EF1); with sea != 0 (Fermi-sea
+ * calculators) = 2 for bands [0, bandmax), bandmax = 1 + the last band whose corners all lie
+ * below EF0, capped at the first in-range group; else 0. */
+int wbg_tetra_select(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks, int nblocks,
+                     const wbg_tetra_grid* grid, int nw, double EF0, double EF1, double degen_thresh, int sea,
+                     signed char* sel, void* stream);
+
+/* Per-band formula values for the tetrahedron method: the group traces of the histogram
+ * kernels, written per band instead of binned.  P [nk][nw][ncomp] = trace of the band's group
+ * / group size for sel 1, the trace of the sea group [0, bandmax) on band 0 for sel 2 (Morb:
+ * T(bandmax) - T(0)), 0 otherwise.  formula: WBG_FORMULA_IDENTITY / INVMASS / VELVEL (as
+ * wbg_berry_scan), WBG_FORMULA_OMEGA (wbg_berry_omega, 3), WBG_FORMULA_DEROMEGA
+ * (wbg_berry_deromega, 9, (c, d) at 3 c + d), WBG_FORMULA_MORB (wbg_berry_morb, 3).  fields:
+ * field indices into Xbar (unused entries ignored); fp64 0 / 1 as the histogram kernels. */
+#define WBG_FORMULA_OMEGA 3
+#define WBG_FORMULA_DEROMEGA 4
+#define WBG_FORMULA_MORB 5
+typedef struct {
+  int V, A, O, W, dA, dO, B, C;
+} wbg_field_index;
+int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_field_index* fields, int nw, int nk,
+                    int formula, int internal_terms, int external_terms, double degen_thresh,
+                    const signed char* sel, double* P, int fp64, void* stream);
+
+/* Weighted sum over the bands of every k-point: sum_n P[k][n][c] w_n(E_F) with the band weight
+ * w_n = 1/12 sum over the 12 tetrahedra (k-point + 3 corners) of the linear-tetrahedron
+ * occupation (der 0) or its E_F derivative (der 1) at efermi[0..nEF) -- weight 1 for sel 2
+ * bands (der 0).  hist [nEF][ncomp] is accumulated in difference form (hist[i] += P (w(i) -
+ * w(i-1))): wbg_scan_finalize turns it into the sum.  ascending != 0: efermi is sorted
+ * ascending and only the levels between a band's smallest and largest corner energy are
+ * evaluated. */
+int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
+                         int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
+                         int ncomp, const double* efermi, int nEF, int der, int ascending, double* hist,
+                         void* stream);
 
 /* ---- tabulation (calculators/tabulate.py:21-52 Tabulator with Energy, Velocity,
  * BerryCurvature; evaluate_k.py:9-16 "energy", "band_gradients", "berry_curvature") ----------

@@ -210,10 +210,13 @@ def grid_points(NKFFT):
 class DataK:
     """One FFT block at shift dK (reduced, K/NKFFT): data_K/data_K.py:73-111."""
 
-    def __init__(self, system, NKFFT, dK):
+    def __init__(self, system, NKFFT, dK, dk_cell=None):
         self.system = system
         self.NKFFT = np.array(NKFFT, dtype=int)
         self.dK = np.array(dK, dtype=float)
+        # spacing of the dense grid, Kpoint.dK_fullBZ = dK/NKFFT (grid/Kpoint.py:104-110):
+        # the parallelepiped around each k-point for the tetrahedron method
+        self.dk_cell = None if dk_cell is None else np.array(dk_cell, dtype=float) * np.ones(3)
         self.nk = int(np.prod(self.NKFFT))
         self.num_wann = system.num_wann
         self.cell_volume = system.cell_volume
@@ -264,6 +267,29 @@ class DataK:
     @property
     def E_K(self):
         return self._eigh()[0]
+
+    def E_K_corners_parallel(self):
+        """data_K/data_K_R.py:121-141: eigenvalues at the 8 corners k +- dk_cell/2 of the
+        parallelepiped around every k-point, (nk, 2, 2, 2, nw); corner index 0 is the minus side."""
+        if 'Ecorners' not in self._cache:
+            half = np.exp(2j * np.pi * self.system.iRvec * (self.dk_cell / 2)[None, :])
+            expdK = np.array([1. / half, half])
+            HR = self.system.XX_R['Ham'] * self.expdK[:, None, None]
+            Ec = np.zeros((self.nk, 2, 2, 2, self.num_wann))
+            for ix in 0, 1:
+                for iy in 0, 1:
+                    for iz in 0, 1:
+                        e = expdK[ix, :, 0] * expdK[iy, :, 1] * expdK[iz, :, 2]
+                        Hk = fft_R_to_k(HR * e[:, None, None], self.system.iRvec, self.NKFFT, hermitian=True)
+                        Ec[:, ix, iy, iz, :] = np.linalg.eigvalsh(Hk)
+            self._cache['Ecorners'] = Ec
+        return self._cache['Ecorners']
+
+    @property
+    def tetraWeights(self):  # data_K/data_K.py:160-164
+        if 'tetra' not in self._cache:
+            self._cache['tetra'] = TetraWeightsParal(self.E_K, self.E_K_corners_parallel())
+        return self._cache['tetra']
 
     @property
     def UU_K(self):
@@ -605,6 +631,102 @@ def evaluate_k(system, k, quantities, iband=None, degen_thresh=1e-4):
     return out
 
 
+# ---------------------------------------------------------------------------
+# Tetrahedron method (grid/tetrahedron.py:15-281)
+# ---------------------------------------------------------------------------
+def weights_tetra(efall, e0, e1, e2, e3, der=0):
+    """grid/tetrahedron.py:15-116: occupation of one linear tetrahedron with corner energies
+    e0..e3 at every Fermi level in efall (der 0, the accurate piecewise form), or its der-th
+    derivative from the expanded cubic polynomials (der 1..3).  Corners closer than 1e-12 are
+    pulled apart first, in sorted order."""
+    e = np.sort(np.array([e0, e1, e2, e3], dtype=float))
+    for i in range(3):
+        if e[i + 1] - e[i] < 1e-12:
+            e[i + 1] = e[i] + 1e-12
+    e1, e2, e3, e4 = e
+    ef = np.asarray(efall, dtype=float)
+    occ = np.zeros(ef.shape)
+    r1 = (ef >= e1) & (ef < e2)
+    r2 = (ef >= e2) & (ef < e3)
+    r3 = (ef >= e3) & (ef < e4)
+    if der == 0:
+        x = ef[r3]
+        occ[r3] = 1 - ((x - e4) / (e1 - e4)) * ((x - e4) / (e2 - e4)) * ((x - e4) / (e3 - e4))
+        x = ef[r2]
+        a13, a14 = (x - e1) / (e3 - e1), (x - e1) / (e4 - e1)
+        a23, a24 = (x - e2) / (e3 - e2), (x - e2) / (e4 - e2)
+        occ[r2] = a23 * a24 + a13 * (a14 * (1 - a24) + a24 * (1 - a23))
+        x = ef[r1]
+        occ[r1] = ((x - e1) / (e2 - e1)) * ((x - e1) / (e3 - e1)) * ((x - e1) / (e4 - e1))
+        occ[ef >= e4] = 1.
+        return occ
+    # occupation = c_r0 + c_r1 ef + c_r2 ef^2 + c_r3 ef^3 in region r (1: [e1,e2), 2: [e2,e3), 3: [e3,e4))
+    d1 = 1. / ((e2 - e1) * (e3 - e1) * (e4 - e1))
+    d2 = 1. / ((e3 - e1) * (e4 - e1) * (e3 - e2) * (e4 - e2))
+    d3 = 1. / ((e4 - e1) * (e4 - e2) * (e4 - e3))
+    c = {1: [None, 3 * e1 ** 2 * d1, -3 * e1 * d1, d1],
+         2: [None, (-2 * e1 * ((e3 - e2) * (e4 - e2)) + (2 * e2 * e4 + e2 ** 2) * (e1 - e3)
+                    + (e1 * e2 + e2 * e3 + e1 * e3) * (e2 - e4)) * d2,
+             (((e3 - e2) * (e4 - e2)) - (e1 - e3) * (2 * e2 + e4) - (e3 + e1 + e2) * (e2 - e4)) * d2,
+             d2 * (e1 + e2 - e3 - e4)],
+         3: [None, 3 * e4 ** 2 * d3, -3 * e4 * d3, d3]}
+    for r, m in ((1, r1), (2, r2), (3, r3)):
+        _, c1, c2, c3 = c[r]
+        x = ef[m]
+        if der == 1:
+            occ[m] = c1 + x * (2 * c2 + 3 * c3 * x)
+        elif der == 2:
+            occ[m] = 2 * c2 + 6 * c3 * x
+        elif der == 3:
+            occ[m] = 6 * c3
+        else:
+            raise NotImplementedError(der)
+    return occ
+
+
+class TetraWeightsParal:
+    """grid/tetrahedron.py:165-281 (TetraWeights with the parallelepiped corners): per k-point
+    and band, the average over the 12 tetrahedra (k-point, two corners of a face diagonal
+    triangle) of the linear-tetrahedron weight; groups of degenerate bands by the energies at
+    the k-points, in range when the corner energies reach the Fermi window."""
+
+    def __init__(self, eCenter, eCorners):
+        self.eCenter, self.eCorners = eCenter, eCorners
+        self.nk, self.nb = eCenter.shape
+        Eall = np.concatenate((eCenter[:, None, :], eCorners.reshape(self.nk, -1, self.nb)), axis=1)
+        self.Emin, self.Emax = Eall.min(axis=1), Eall.max(axis=1)
+
+    def weight_1k1b(self, efermi, ik, ib, der):
+        occ = np.zeros(efermi.shape)
+        c = self.eCorners[ik, ..., ib]
+        e0 = self.eCenter[ik, ib]
+        for iface in 0, 1:
+            for f in c[iface, :, :], c[:, iface, :], c[:, :, iface]:
+                occ += weights_tetra(efermi, e0, f[0, 0], f[0, 1], f[1, 1], der=der)
+                occ += weights_tetra(efermi, e0, f[0, 0], f[1, 0], f[1, 1], der=der)
+        return occ / 12.
+
+    def weights_all_band_groups(self, efermi, der, degen_thresh=-1):
+        """[{(ib1, ib2): weight per Fermi level} for every k] (tetrahedron.py:215-262, Emin = -inf)."""
+        res = []
+        for ik in range(self.nk):
+            E = self.eCenter[ik]
+            borders = [0] + list(np.where((E[1:] - E[:-1]) > degen_thresh)[0] + 1) + [len(E)]
+            groups = [(b1, b2) for b1, b2 in zip(borders, borders[1:])
+                      if self.Emax[ik, b1:b2].max() >= efermi[0] and self.Emin[ik, b1:b2].min() <= efermi[-1]]
+            w = {(b1, b2): sum(self.weight_1k1b(efermi, ik, ib, der) for ib in range(b1, b2)) / (b2 - b1)
+                 for b1, b2 in groups}
+            if der == 0:  # the Fermi sea: bands whose corners all lie below the window
+                below = np.where(self.Emax[ik] < efermi[0])[0]
+                bandmax = below[-1] + 1 if len(below) else 0
+                if groups:
+                    bandmax = min(bandmax, groups[0][0])
+                if bandmax > 0:
+                    w[(0, bandmax)] = np.ones(len(efermi))
+            res.append(w)
+        return res
+
+
 class EnergyResult:
     def __init__(self, Energies, data):
         self.Energies = Energies if isinstance(Energies, (list, tuple)) else [Energies]
@@ -621,12 +743,14 @@ class EnergyResult:
 # Static calculators (calculators/static.py:24-169, 231-247, 353-364, 472-487)
 # ---------------------------------------------------------------------------
 class StaticCalculator:
-    def __init__(self, Efermi, constant_factor=1., degen_thresh=1e-4, kwargs_formula=None, use_factor=True):
+    def __init__(self, Efermi, constant_factor=1., degen_thresh=1e-4, kwargs_formula=None, use_factor=True,
+                 tetra=False):
         self.Efermi = np.array(Efermi, dtype=float)
         self.constant_factor = constant_factor
         self.degen_thresh = degen_thresh
         self.kwargs_formula = dict(kwargs_formula or {})
         self.use_factor = use_factor
+        self.tetra = tetra
         self.extraEf = 0 if self.fder == 0 else 1 if self.fder in (1, 2) else 2
         self.dEF = self.Efermi[1] - self.Efermi[0] if len(self.Efermi) > 1 else 0.001
         self.EFmin = self.Efermi[0] - self.extraEf * self.dEF
@@ -637,8 +761,12 @@ class StaticCalculator:
         """Per-k group traces {(ib1,ib2): value} and group energies (static.py:64-117)."""
         formula = self.Formula(data_K, **self.kwargs_formula)
         NB = data_K.num_wann
-        weights = [data_K.get_bands_in_range_groups_ik(ik, self.EFmin, self.EFmax, self.degen_thresh,
-                                                       sea=(self.fder == 0)) for ik in range(data_K.nk)]
+        if self.tetra:  # static.py:80-85
+            weights = data_K.tetraWeights.weights_all_band_groups(self.Efermi, der=self.fder,
+                                                                  degen_thresh=self.degen_thresh)
+        else:
+            weights = [data_K.get_bands_in_range_groups_ik(ik, self.EFmin, self.EFmax, self.degen_thresh,
+                                                           sea=(self.fder == 0)) for ik in range(data_K.nk)]
         values = []
         for ik, bnd in enumerate(weights):
             v = {}
@@ -662,6 +790,15 @@ class StaticCalculator:
     def __call__(self, data_K):
         formula, weights, values = self.values(data_K)
         shape = (3,) * formula.ndim
+        if self.tetra:  # static.py:119-125: the weights carry the occupation (or its derivative)
+            restot = np.zeros(self.Efermi.shape + shape)
+            for ik, w in enumerate(weights):
+                for n, wn in w.items():
+                    restot += np.einsum("e,...->e...", wn, values[ik][n])
+            restot /= data_K.cell_volume
+            restot /= data_K.nk
+            restot *= self.constant_factor if self.use_factor else np.sign(self.constant_factor)
+            return EnergyResult(self.Efermi, restot)
         restot = np.zeros((self.nEF_extra,) + shape)
         for ik, w in enumerate(weights):
             for n, E in sorted(w.items()):
@@ -828,9 +965,10 @@ def run(system, NKdiv, NKFFT, calculators, blocks=None):
     if blocks is not None:
         shifts = shifts[blocks]
     factor = 1. / np.prod(NKdiv)
+    dk_cell = 1. / (np.array(NKdiv) * np.array(NKFFT))
     total = {}
     for dK in shifts:
-        data = DataK(system, NKFFT, dK)
+        data = DataK(system, NKFFT, dK, dk_cell=dk_cell)
         for key, calc in calculators.items():
             r = calc(data) * factor
             total[key] = r if key not in total else total[key] + r

@@ -27,6 +27,11 @@ Fixtures written (all small, complex128/float64):
   configurations (cubic nw=8 / triclinic nw=6 with MDRS / spinor nw=8), made by
   ``wbgpu.models``: per-block E_K, and AHC / Morb / BerryDipole_FermiSea /
   OpticalConductivity results.
+* ``tetra_ref.npz`` -- the tetrahedron method (``tetra=True``: AHC, Morb,
+  BerryDipole_FermiSea, DOS, CumDOS, Ohmic_FermiSea / FermiSurf) of the reference's
+  ``run`` on the random system (NKdiv 2, NKFFT 3, 21 Fermi levels) and AHC / DOS /
+  Ohmic_FermiSea on the triclinic MDRS model over an anisotropic grid (NKdiv (2,1,3),
+  NKFFT (3,4,2)).  ``python make_golden.py <reference root> tetra`` writes only this file.
 """
 import os
 import sys
@@ -175,8 +180,46 @@ def main(ref_root):
     for q in qs:
         ev[f'fe_{q}'] = r[q]
     np.savez_compressed(os.path.join(HERE, 'evaluate_k_ref.npz'), **ev)
+    tetra_fixtures(wb, rs)
     print("wrote fixtures to", HERE)
 
 
+def tetra_calculators(calc, EF):
+    """Static calculators with tetra=True (calculators/static.py:80-125)."""
+    return {'ahc': calc.static.AHC(Efermi=EF, tetra=True),
+            'morb': calc.static.Morb(Efermi=EF, tetra=True),
+            'bcd': calc.static.BerryDipole_FermiSea(Efermi=EF, tetra=True),
+            'dos': calc.static.DOS(Efermi=EF, tetra=True),
+            'cumdos': calc.static.CumDOS(Efermi=EF, tetra=True),
+            'conductivity_ohmic': calc.static.Ohmic_FermiSea(Efermi=EF, tetra=True),
+            'conductivity_ohmic_fsurf': calc.static.Ohmic_FermiSurf(Efermi=EF, tetra=True)}
+
+
+def tetra_fixtures(wb, rs):
+    """---- 5. the tetrahedron method (grid/tetrahedron.py, TetraWeightsParal) on the random
+    system (the reference's test grid NK=6 = 2 x 3) and on the config-2 structure with MDRS."""
+    from wannierberri import calculators as calc
+    from wbgpu import models
+    out = {}
+    EF = np.linspace(-2, 2, 21)
+    out['EF'] = EF
+    for k, v in run_ref(wb, rs, 2, 3, tetra_calculators(calc, EF)).items():
+        out['random_' + k] = v
+    s2 = ref_system_from_arrays(wb, models.config_system(2, small=True))
+    s2.do_ws_dist(mp_grid=3)
+    EF2 = np.linspace(-1.5, 1.5, 31)
+    out['EF2'] = EF2
+    cs = tetra_calculators(calc, EF2)
+    for k, v in run_ref(wb, s2, [2, 1, 3], [3, 4, 2], {q: cs[q] for q in ('ahc', 'dos', 'conductivity_ohmic')}).items():
+        out['c2_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'tetra_ref.npz'), **out)
+
+
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    if len(sys.argv) > 2 and sys.argv[2] == 'tetra':  # only section 5
+        wb = setup_reference(root)
+        from wannierberri.system.system_R import System_R
+        tetra_fixtures(wb, System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True))
+    else:
+        main(root)

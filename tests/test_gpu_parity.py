@@ -523,3 +523,106 @@ def test_dos_ohmic_c2small_vs_oracle(c2small):
                                           'om': O.Ohmic_FermiSea(Efermi=EF), 'os': O.Ohmic_FermiSurf(Efermi=EF)})
     for key in ('dos', 'cumdos', 'om', 'os'):
         assert maxrel(got[key].data, ref[key].data) < 1e-9, key
+
+
+# ---------------------------------------------------------------------------------------
+# tetrahedron method (tetra=True)
+# ---------------------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", [1, 3])
+@pytest.mark.parametrize("nw", [6, 32])
+def test_eigh_values_only(nw, mode):
+    """WBG_EIGH_VALUES: the same eigenvalues as the full solve, U untouched (may be NULL)."""
+    rng = np.random.default_rng(300 + nw)
+    nk = 300
+    H = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
+    H = H + H.conj().swapaxes(1, 2)
+    conv = _df64_complex if mode == 3 else torch.from_numpy
+    E0, _, f0 = engine.eigh(conv(H).cuda(), nw * nw, nw, nk, mode=mode)
+    E0 = E0.clone()
+    E1, U1, f1 = engine.eigh(conv(H).cuda(), nw * nw, nw, nk, mode=mode | engine.EIGH_VALUES)
+    torch.cuda.synchronize()
+    assert U1 is None and int(f0.item()) == 0 and int(f1.item()) == 0
+    assert torch.equal(E0, E1)
+
+
+def _tetra_calcs(EF, names):
+    C = wbgpu.calculators
+    cs = {'ahc': C.AHC, 'morb': C.Morb, 'bcd': C.BerryDipole_FermiSea, 'dos': C.DOS, 'cumdos': C.CumDOS,
+          'conductivity_ohmic': C.Ohmic_FermiSea, 'conductivity_ohmic_fsurf': C.Ohmic_FermiSurf}
+    return {k: cs[k](Efermi=EF, tetra=True) for k in names}
+
+
+TETRA_ALL = ['ahc', 'morb', 'bcd', 'dos', 'cumdos', 'conductivity_ohmic', 'conductivity_ohmic_fsurf']
+
+
+@pytest.mark.parametrize("precision,rule", [('fp64', 1e-8), ('mixed', 1e-5)])
+def test_tetra_golden_random(golden_dir, precision, rule):
+    """All seven static calculators with tetra=True on the reference's random system against
+    the reference's own run (tests/golden/tetra_ref.npz); FP64 with the 1e-8 acceptance rule."""
+    import os
+    rs = _golden_system(golden_dir, 'random_system.npz')
+    ref = np.load(os.path.join(golden_dir, 'tetra_ref.npz'))
+    res = wbgpu.run(rs, wbgpu.Grid(rs, NKdiv=2, NKFFT=3), _tetra_calcs(ref['EF'], TETRA_ALL), precision=precision)
+    for key in TETRA_ALL:
+        got, exp = res[key].data, ref['random_' + key]
+        assert got.shape == exp.shape, (key, got.shape, exp.shape)
+        assert np.abs(got - exp).max() < rule * np.abs(exp).max(), (key, np.abs(got - exp).max() / np.abs(exp).max())
+
+
+@pytest.mark.parametrize("precision,rule", [('fp64', 1e-9), ('mixed', 1e-5)])
+def test_tetra_golden_c2_anisotropic(golden_dir, c2small, precision, rule):
+    """Triclinic MDRS model over NKdiv (2,1,3) x NKFFT (3,4,2): every corner lookup of the
+    kernels (minus side of block 0 wrapping to the last corner block, index j-1) is exercised."""
+    import os
+    s, _ = c2small
+    ref = np.load(os.path.join(golden_dir, 'tetra_ref.npz'))
+    names = ['ahc', 'dos', 'conductivity_ohmic']
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=(2, 1, 3), NKFFT=(3, 4, 2)), _tetra_calcs(ref['EF2'], names),
+                    precision=precision)
+    for key in names:
+        assert maxrel(res[key].data, ref['c2_' + key]) < rule, key
+
+
+def test_tetra_c1_vs_oracle_blocks():
+    """nw = 8 cubic model, a subset of the blocks, 101 levels: GPU vs oracle in FP64; the corner
+    energies are computed only for the corner blocks the subset touches."""
+    s = wsys.System_R.from_dict(models.config_system(1))
+    o = O.RSystem(s.real_lattice, s.iRvec, s.wannier_centers_cart, s._XX_R)
+    EF = np.linspace(-2, 2, 101)
+    blocks = [0, 5, 7]
+    names = ['ahc', 'dos', 'cumdos']
+    got = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(3, 4, 5)), _tetra_calcs(EF, names), precision='fp64',
+                    blocks=blocks)
+    ocs = {'ahc': O.AHC(Efermi=EF, tetra=True), 'dos': O.DOS(Efermi=EF, tetra=True),
+           'cumdos': O.CumDOS(Efermi=EF, tetra=True)}
+    ref = O.run(o, (2, 2, 2), (3, 4, 5), ocs, blocks=blocks)
+    for key in names:
+        assert maxrel(got[key].data, ref[key].data) < 1e-9, key
+
+
+def test_tetra_cumdos_counts_states():
+    """Size-independent property: with E_F above every band CumDOS (tetra) is num_wann states per
+    cell, below every band 0; DOS integrates to the same count (trapezoid over a fine grid)."""
+    s = wsys.System_R.from_dict(models.config_system(1))
+    EF = np.linspace(-12, 12, 2401)
+    r = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=6), _tetra_calcs(EF, ['dos', 'cumdos']), precision='mixed')
+    cum, dos = r['cumdos'].data, r['dos'].data
+    assert abs(cum[0]) < 1e-12 and abs(cum[-1] - s.num_wann) < 1e-9
+    assert abs(np.trapezoid(dos, EF) - s.num_wann) < 1e-3 * s.num_wann
+
+
+def test_tetra_served_equals_run(c2small):
+    """tetra=True requests through the Server give run()'s results."""
+    s, _ = c2small
+    EF = np.linspace(-1.5, 1.5, 31)
+    grid = wbgpu.Grid(s, NKdiv=2, NKFFT=3)
+    alone = wbgpu.run(s, grid, _tetra_calcs(EF, ['ahc', 'dos']), precision='mixed')
+    srv = wbgpu.Server(precision='mixed')
+    srv.add_system('c2', s)
+    t1 = srv.submit('c2', grid, _tetra_calcs(EF, ['ahc', 'dos']))
+    t2 = srv.submit('c2', grid, {'ahc': wbgpu.calculators.AHC(Efermi=EF)})
+    srv.run_until_idle()
+    r1 = t1.wait()
+    t2.wait()
+    for key in ('ahc', 'dos'):
+        assert maxrel(r1[key].data, alone[key].data) < 1e-9, key

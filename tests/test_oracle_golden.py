@@ -185,3 +185,35 @@ def test_oracle_evaluate_k_golden(golden_dir):
     for q in EVK_QS:
         ref = g[f'fe_{q}']
         assert np.allclose(got[q], ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), q
+
+
+def tetra_oracle_calculators(EF, names):
+    """tetra=True static calculators of the oracle, the same set as tests/golden/make_golden.py."""
+    cs = {'ahc': O.AHC, 'morb': O.Morb, 'bcd': O.BerryDipole_FermiSea, 'dos': O.DOS, 'cumdos': O.CumDOS,
+          'conductivity_ohmic': O.Ohmic_FermiSea, 'conductivity_ohmic_fsurf': O.Ohmic_FermiSurf}
+    return {k: cs[k](Efermi=EF, tetra=True) for k in names}
+
+
+TETRA_RANDOM = ['ahc', 'morb', 'bcd', 'dos', 'cumdos', 'conductivity_ohmic', 'conductivity_ohmic_fsurf']
+
+
+def test_tetra_random_golden(random_sys, golden_dir):
+    """Tetrahedron method (grid/tetrahedron.py TetraWeightsParal, corner energies of
+    data_K/data_K_R.py:121-141) against the reference's run on its random system."""
+    g = np.load(os.path.join(golden_dir, 'tetra_ref.npz'))
+    r = O.run(random_sys, NKdiv=(2, 2, 2), NKFFT=(3, 3, 3), calculators=tetra_oracle_calculators(g['EF'], TETRA_RANDOM))
+    for k in TETRA_RANDOM:
+        ref = g['random_' + k]
+        assert r[k].data.shape == ref.shape, k
+        assert np.max(np.abs(r[k].data - ref)) < 1e-8 * np.max(np.abs(ref)), k
+
+
+def test_tetra_c2_anisotropic_golden(golden_dir):
+    """Triclinic MDRS model over NKdiv (2,1,3) x NKFFT (3,4,2): the corner k-points of every
+    block cross the block borders in all three directions."""
+    g = np.load(os.path.join(golden_dir, 'tetra_ref.npz'))
+    s2 = O.do_ws_dist(rsys(models.config_system(2, small=True)), mp_grid=(3, 3, 3))
+    names = ['ahc', 'dos', 'conductivity_ohmic']
+    r = O.run(s2, (2, 1, 3), (3, 4, 2), tetra_oracle_calculators(g['EF2'], names))
+    for k in names:
+        assert maxrel(r[k].data, g['c2_' + k]) < 1e-9, k

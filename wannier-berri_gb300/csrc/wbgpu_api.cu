@@ -5,6 +5,7 @@
 #include "wbgpu_eigh.cuh"
 #include "wbgpu_band.cuh"
 #include "wbgpu_kubo.cuh"
+#include "wbgpu_tetra.cuh"
 
 extern "C" {
 
@@ -133,6 +134,52 @@ int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int n
              size_t workspace_bytes, double* out, int fp64, void* stream) {
   return wbg_kubo_run(E, Xbar, nFbar, iV, iA, nw, nk, external_terms, params, efermi, omega, workspace,
                       workspace_bytes, out, fp64, (cudaStream_t)stream);
+}
+
+int wbg_tetra_select(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks, int nblocks,
+                     const wbg_tetra_grid* grid, int nw, double EF0, double EF1, double degen_thresh, int sea,
+                     signed char* sel, void* stream) {
+  return wbg_tetra_select_run(E, Ecorner, corner_slot, blocks, nblocks, grid, nw, EF0, EF1, degen_thresh, sea, sel,
+                              (cudaStream_t)stream);
+}
+
+int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_field_index* f, int nw, int nk,
+                    int formula, int internal_terms, int external_terms, double degen_thresh,
+                    const signed char* sel, double* P, int fp64, void* stream) {
+  if (!f || !sel || !P || (fp64 != 0 && fp64 != 1)) return WBG_STATUS_BAD_ARGUMENT;
+  WbgScan sp;
+  sp.EFmin = 0.0;  // groups come from sel; no histogram
+  sp.EFmax = 0.0;
+  sp.dEF = 1.0;
+  sp.degen_thresh = degen_thresh;
+  sp.nEF = 0;
+  sp.reserved = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (formula) {
+    case WBG_FORMULA_IDENTITY:
+    case WBG_FORMULA_INVMASS:
+    case WBG_FORMULA_VELVEL:
+      return wbg_berry_scan_run(E, Xbar, nFbar, f->V, f->W, nw, nk, &sp, formula, 0, nullptr, fp64, st, sel, P);
+    case WBG_FORMULA_OMEGA:
+      return wbg_berry_omega_run(E, Xbar, nFbar, f->V, f->A, f->O, nw, nk, &sp, internal_terms, external_terms,
+                                 nullptr, fp64, st, nullptr, sel, P);
+    case WBG_FORMULA_DEROMEGA:
+      return wbg_berry_deromega_run(E, Xbar, nFbar, f->V, f->A, f->O, f->W, f->dA, f->dO, nw, nk, &sp, internal_terms,
+                                    external_terms, nullptr, fp64, st, sel, P);
+    case WBG_FORMULA_MORB:
+      return wbg_berry_morb_run(E, Xbar, nFbar, f->V, f->A, f->O, f->B, f->C, nw, nk, &sp, internal_terms,
+                                external_terms, nullptr, fp64, st, sel, P);
+    default:
+      return WBG_STATUS_BAD_ARGUMENT;
+  }
+}
+
+int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
+                         int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
+                         int ncomp, const double* efermi, int nEF, int der, int ascending, double* hist,
+                         void* stream) {
+  return wbg_tetra_accumulate_run(E, Ecorner, corner_slot, blocks, nblocks, grid, nw, sel, P, ncomp, efermi, nEF, der,
+                                  ascending, hist, (cudaStream_t)stream);
 }
 
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream) {

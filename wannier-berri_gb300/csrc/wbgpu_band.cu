@@ -357,6 +357,48 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
 }
 
 // ---------------------------------------------------------------------------------------
+// Per-band values for the tetrahedron method (wbg_band_values).  sel[k][n]: 2 = band n is in
+// the Fermi-sea group [0, bandmax) (a prefix of the bands), 1 = its degenerate group is in the
+// Fermi window, 0 = not needed.  With sel set, a formula kernel takes its groups from sel
+// instead of the energy window and writes P[k][n][c] in place of the histogram: the group
+// trace divided by the group size for sel 1, the whole sea-group trace on band 0 for sel 2,
+// zero otherwise -- so that sum_n P[k][n] w_n(E_F) with per-band tetrahedron weights w_n is
+// the reference's sum over groups of trace x group-averaged weight.
+// ---------------------------------------------------------------------------------------
+struct BandSel {
+  const signed char* sel;
+  double* P;
+};
+
+WBG_D int sel_bandmax(const signed char* selk, int nw, int lane, int L) {
+  int c = 0;
+  for (int n = lane; n < nw; n += L) c += selk[n] == 2;
+  return group_sum_i(c, L);
+}
+
+// additive formulas: t[n * ts + c] is band n's row of the trace of its group (or of the sea)
+WBG_D void emit_band_values(double* P, long long k, int nw, int nc, int lane, int L, int bandmax,
+                            const signed char* selk, const int* myS, const double* t, int ts) {
+  for (int n = lane; n < nw; n += L) {
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (n < bandmax) {
+      if (n == 0)
+        for (int q = 0; q < bandmax; ++q)
+          for (int c = 0; c < nc; ++c) v[c] += t[q * ts + c];
+    } else if (selk[n] == 1) {
+      int gs = n, ge = n + 1;
+      while (!myS[gs]) --gs;
+      while (ge < nw && !myS[ge]) ++ge;
+      for (int q = gs; q < ge; ++q)
+        for (int c = 0; c < nc; ++c) v[c] += t[q * ts + c];
+      const double inv = 1.0 / (double)(ge - gs);
+      for (int c = 0; c < nc; ++c) v[c] *= inv;
+    }
+    for (int c = 0; c < nc; ++c) P[(k * nw + n) * nc + c] = v[c];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Fused Omega traces + Fermi-level histogram.
 // grid: persistent blocks of G*L threads; each group of L lanes takes one k-point at a time.
 // Xbar layout: [k][nFbar][nw][nw]; V at iV..iV+2, A at iA..iA+2, O(rotAA) at iO..iO+2.
@@ -369,7 +411,8 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
 template <typename T>
 __global__ void berry_omega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                    int iV, int iA, int iO, int nw, int nk, int L, int G, WbgScan sp, int internal_terms,
-                                   int external_terms, double* __restrict__ hist, double* __restrict__ tab) {
+                                   int external_terms, double* __restrict__ hist, double* __restrict__ tab,
+                                   BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][3]
@@ -400,18 +443,23 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
     __syncwarp();
     for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
     __syncwarp();
-    int below = 0, f0 = nw;
-    for (int n = lane; n < nw; n += L) {
-      below += myE[n] < sp.EFmin;
-      if (myS[n]) {
-        int g1 = n + 1;
-        while (g1 < nw && !myS[g1]) ++g1;
-        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+    int bandmax;
+    if (bs.sel) {
+      bandmax = sel_bandmax(bs.sel + kk * nw, nw, lane, L);
+    } else {
+      int below = 0, f0 = nw;
+      for (int n = lane; n < nw; n += L) {
+        below += myE[n] < sp.EFmin;
+        if (myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+        }
       }
+      below = group_sum_i(below, L);
+      f0 = group_min_i(f0, L);
+      bandmax = min(below, f0);
     }
-    below = group_sum_i(below, L);
-    f0 = group_min_i(f0, L);
-    const int bandmax = min(below, f0);
     const V* Xk = Xbar + kk * nFbar * nw2;
     for (int n = lane; n < nw; n += L) {
       int gs = n, ge = n + 1;
@@ -419,7 +467,7 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
       while (ge < nw && !myS[ge]) ++ge;
       bool ingroup;
       if (n < bandmax) { gs = 0; ge = bandmax; ingroup = true; }
-      else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
+      else ingroup = bs.sel ? bs.sel[kk * nw + n] == 1 : (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
       double t[3] = {0.0, 0.0, 0.0};
       if (ingroup) {
         TraceSum<T> sr[3];  // real part of the trace; its imaginary part is not needed
@@ -473,6 +521,8 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
         const double inv = 1.0 / (double)(ge - gs);
         for (int i = 0; i < 7; ++i) tab[(k * nw + n) * 7 + i] = v[i] * inv;
       }
+    } else if (valid && bs.P) {
+      emit_band_values(bs.P, k, nw, 3, lane, L, bandmax, bs.sel + k * nw, myS, myT, 3);
     } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
@@ -662,7 +712,7 @@ __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __r
 template <typename T>
 __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                   int iV, int iW, int nw, int nk, int L, int G, WbgScan sp, int formula, int sea,
-                                  double* __restrict__ hist) {
+                                  double* __restrict__ hist, BandSel bs) {
   typedef typename C2<T>::t V;
   const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
   extern __shared__ double smb[];
@@ -686,7 +736,9 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
     for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
     __syncwarp();
     int bandmax = 0;
-    if (sea) {
+    if (bs.sel) {
+      bandmax = sel_bandmax(bs.sel + kk * nw, nw, lane, L);
+    } else if (sea) {
       int below = 0, f0 = nw;
       for (int n = lane; n < nw; n += L) {
         below += myE[n] < sp.EFmin;
@@ -739,7 +791,9 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
       for (int c = 0; c < 9; ++c) myT[n * 9 + c] = t[c];
     }
     __syncwarp();
-    if (valid) {
+    if (valid && bs.P) {
+      emit_band_values(bs.P, k, nw, nc, lane, L, bandmax, bs.sel + k * nw, myS, myT, 9);
+    } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
         bool seag = false;
@@ -789,7 +843,7 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
 template <typename T>
 __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                   int iV, int iA, int iO, int iB, int iC, int nw, int nk, int L, int G, WbgScan sp,
-                                  int internal_terms, int external_terms, double* __restrict__ hist) {
+                                  int internal_terms, int external_terms, double* __restrict__ hist, BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
   double* sh = smb;                                      // [nEF][3]
@@ -811,18 +865,23 @@ __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C
     __syncwarp();
     for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
     __syncwarp();
-    int below = 0, f0 = nw;
-    for (int n = lane; n < nw; n += L) {
-      below += myE[n] < sp.EFmin;
-      if (myS[n]) {
-        int g1 = n + 1;
-        while (g1 < nw && !myS[g1]) ++g1;
-        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+    int bandmax;
+    if (bs.sel) {
+      bandmax = sel_bandmax(bs.sel + kk * nw, nw, lane, L);
+    } else {
+      int below = 0, f0 = nw;
+      for (int n = lane; n < nw; n += L) {
+        below += myE[n] < sp.EFmin;
+        if (myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+        }
       }
+      below = group_sum_i(below, L);
+      f0 = group_min_i(f0, L);
+      bandmax = min(below, f0);
     }
-    below = group_sum_i(below, L);
-    f0 = group_min_i(f0, L);
-    const int bandmax = min(below, f0);
     const V* Xk = Xbar + kk * nFbar * nw2;
     // per band: Gtot + H (constant part) and running suffix of F - G
     const int nb_lane = (nw + L - 1) / L;  // bands per lane (<= WBG_BAND_MAXPER)
@@ -892,7 +951,21 @@ __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C
     if (lane == 0)
       for (int g = 0; g < 3; ++g) myT[g] = 0.0;  // T(0): empty inner set
     __syncwarp();
-    if (valid) {
+    if (valid && bs.P) {  // group values T(ge) - T(gs), per band (the sea on band 0)
+      for (int n = lane; n < nw; n += L) {
+        double v[3] = {0.0, 0.0, 0.0};
+        if (n < bandmax) {
+          if (n == 0)
+            for (int g = 0; g < 3; ++g) v[g] = myT[bandmax * 3 + g] - myT[g];
+        } else if (bs.sel[k * nw + n] == 1) {
+          int gs = n, ge = n + 1;
+          while (!myS[gs]) --gs;
+          while (ge < nw && !myS[ge]) ++ge;
+          for (int g = 0; g < 3; ++g) v[g] = (myT[ge * 3 + g] - myT[gs * 3 + g]) / (double)(ge - gs);
+        }
+        for (int g = 0; g < 3; ++g) bs.P[(k * nw + n) * 3 + g] = v[g];
+      }
+    } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
         bool sea = false;
@@ -943,7 +1016,7 @@ template <typename T>
 __global__ void berry_deromega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar,
                                       int nFbar, int iV, int iA, int iO, int iW, int idA, int idO, int nw, int nk,
                                       int L, int G, int table, WbgScan sp, int internal_terms, int external_terms,
-                                      double* __restrict__ hist) {
+                                      double* __restrict__ hist, BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][9]
@@ -973,18 +1046,23 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
         myDinv[idx] = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
       }
     __syncwarp();
-    int below = 0, f0 = nw;
-    for (int n = lane; n < nw; n += L) {
-      below += myE[n] < sp.EFmin;
-      if (myS[n]) {
-        int g1 = n + 1;
-        while (g1 < nw && !myS[g1]) ++g1;
-        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+    int bandmax;
+    if (bs.sel) {
+      bandmax = sel_bandmax(bs.sel + kk * nw, nw, lane, L);
+    } else {
+      int below = 0, f0 = nw;
+      for (int n = lane; n < nw; n += L) {
+        below += myE[n] < sp.EFmin;
+        if (myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+        }
       }
+      below = group_sum_i(below, L);
+      f0 = group_min_i(f0, L);
+      bandmax = min(below, f0);
     }
-    below = group_sum_i(below, L);
-    f0 = group_min_i(f0, L);
-    const int bandmax = min(below, f0);
     const V* Xk = Xbar + kk * nFbar * nw2;
 #define XV(a, x, y) Xk[(iV + (a)) * nw2 + (x) * nw + (y)]
 #define XA(a, x, y) Xk[(iA + (a)) * nw2 + (x) * nw + (y)]
@@ -1005,7 +1083,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
       while (ge < nw && !myS[ge]) ++ge;
       bool ingroup;
       if (m < bandmax) { gs = 0; ge = bandmax; ingroup = true; }
-      else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
+      else ingroup = bs.sel ? bs.sel[kk * nw + m] == 1 : (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
       double val[9];
       for (int i = 0; i < 9; ++i) val[i] = 0.0;
       if (ingroup) {
@@ -1157,7 +1235,9 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
 #undef XdO
 #undef DV
     __syncwarp();
-    if (valid) {
+    if (valid && bs.P) {
+      emit_band_values(bs.P, k, nw, 9, lane, L, bandmax, bs.sel + k * nw, myS, myT, 9);
+    } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
         bool sea = false;
@@ -1259,14 +1339,18 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
 }
 
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
-                        const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
-                        cudaStream_t stream, double* tab) {
-  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || (!hist && !tab) || !E || !Xbar) return WBG_ERR_ARG;
+                        const WbgScan* sp_in, int internal_terms, int external_terms, double* hist, int fp64,
+                        cudaStream_t stream, double* tab, const signed char* sel, double* P) {
+  const BandSel bs{sel, P};
+  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
+  if (!sel && (sp_in->nEF < 1 || (!hist && !tab) || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
   if (iV < 0 || iV + 3 > nFbar) return WBG_ERR_ARG;
   if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar)) return WBG_ERR_ARG;
-  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   if (fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
-  if (fp64 == 2 && nw <= 32 && !tab) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
+  WbgScan spv = *sp_in;
+  if (sel) { spv.nEF = 0; hist = nullptr; tab = nullptr; }  // per-band values: no histogram
+  const WbgScan* sp = &spv;
+  if (fp64 == 2 && nw <= 32 && !tab && !sel) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
     const int G = 4;  // k-points (warps) per block
     const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * (8 + 24 + 8 + 4);
     if (sm > 220 * 1024) return WBG_ERR_SIZE;
@@ -1293,22 +1377,27 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (fp64) {
     cudaFuncSetAttribute(berry_omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                 G, *sp, internal_terms, external_terms, hist, tab);
+                                                                 G, *sp, internal_terms, external_terms, hist, tab, bs);
   } else {
     cudaFuncSetAttribute(berry_omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                G, *sp, internal_terms, external_terms, hist, tab);
+                                                                G, *sp, internal_terms, external_terms, hist, tab, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
-int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const WbgScan* sp,
-                       int formula, int sea, double* hist, int fp64, cudaStream_t stream) {
-  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E) return WBG_ERR_ARG;
+int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk,
+                       const WbgScan* sp_in, int formula, int sea, double* hist, int fp64, cudaStream_t stream,
+                       const signed char* sel, double* P) {
+  const BandSel bs{sel, P};
+  if (nw < 1 || nk < 1 || !sp_in || !E || (!sel) != (!P)) return WBG_ERR_ARG;
+  if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
+  WbgScan spv = *sp_in;
+  if (sel) { spv.nEF = 0; hist = nullptr; }
+  const WbgScan* sp = &spv;
   if (formula < WBG_FORMULA_IDENTITY || formula > WBG_FORMULA_VELVEL) return WBG_ERR_ARG;
   if (formula != WBG_FORMULA_IDENTITY && (!Xbar || iV < 0 || iV + 3 > nFbar)) return WBG_ERR_ARG;
   if (formula == WBG_FORMULA_INVMASS && (iW < 0 || iW + 9 > nFbar)) return WBG_ERR_ARG;
-  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
   const int L = lanes_for(nw);
   const int G = 128 / L;
@@ -1321,24 +1410,28 @@ int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int
   if (fp64) {
     cudaFuncSetAttribute(berry_scan_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_scan_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
-                                                                *sp, formula, sea, hist);
+                                                                *sp, formula, sea, hist, bs);
   } else {
     cudaFuncSetAttribute(berry_scan_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_scan_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
-                                                               *sp, formula, sea, hist);
+                                                               *sp, formula, sea, hist, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
 int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
-                       int nk, const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
-                       cudaStream_t stream) {
-  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E || !Xbar) return WBG_ERR_ARG;
+                       int nk, const WbgScan* sp_in, int internal_terms, int external_terms, double* hist, int fp64,
+                       cudaStream_t stream, const signed char* sel, double* P) {
+  const BandSel bs{sel, P};
+  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
+  if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
+  WbgScan spv = *sp_in;
+  if (sel) { spv.nEF = 0; hist = nullptr; }
+  const WbgScan* sp = &spv;
   if (iV < 0 || iV + 3 > nFbar) return WBG_ERR_ARG;
   if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar || iB < 0 || iB + 3 > nFbar ||
                          iC < 0 || iC + 3 > nFbar))
     return WBG_ERR_ARG;
-  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   const int L = lanes_for(nw);
   if ((nw + L - 1) / L > WBG_BAND_MAXPER) return WBG_ERR_SIZE;
   const int G = 128 / L;
@@ -1352,24 +1445,28 @@ int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int
   if (fp64) {
     cudaFuncSetAttribute(berry_morb_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_morb_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iB, iC,
-                                                                nw, nk, L, G, *sp, internal_terms, external_terms, hist);
+                                                                nw, nk, L, G, *sp, internal_terms, external_terms, hist, bs);
   } else {
     cudaFuncSetAttribute(berry_morb_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_morb_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iB, iC, nw,
-                                                               nk, L, G, *sp, internal_terms, external_terms, hist);
+                                                               nk, L, G, *sp, internal_terms, external_terms, hist, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
 int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
-                           int idO, int nw, int nk, const WbgScan* sp, int internal_terms, int external_terms,
-                           double* hist, int fp64, cudaStream_t stream) {
-  if (nw < 1 || nk < 1 || !sp || sp->nEF < 1 || !hist || !E || !Xbar) return WBG_ERR_ARG;
+                           int idO, int nw, int nk, const WbgScan* sp_in, int internal_terms, int external_terms,
+                           double* hist, int fp64, cudaStream_t stream, const signed char* sel, double* P) {
+  const BandSel bs{sel, P};
+  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
+  if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
+  WbgScan spv = *sp_in;
+  if (sel) { spv.nEF = 0; hist = nullptr; }
+  const WbgScan* sp = &spv;
   if (iV < 0 || iV + 3 > nFbar || iW < 0 || iW + 9 > nFbar) return WBG_ERR_ARG;
   if (external_terms && (iA < 0 || iA + 3 > nFbar || iO < 0 || iO + 3 > nFbar || idA < 0 || idA + 9 > nFbar ||
                          idO < 0 || idO + 9 > nFbar))
     return WBG_ERR_ARG;
-  if (!(sp->dEF > 0.0)) return WBG_ERR_ARG;
   const int L = lanes_for(nw);
   int G = 64 / L > 0 ? 64 / L : 1;
   const size_t tsz = fp64 ? 8 : 4;
@@ -1390,12 +1487,12 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
     cudaFuncSetAttribute(berry_deromega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iW,
                                                                     idA, idO, nw, nk, L, G, table, *sp, internal_terms,
-                                                                    external_terms, hist);
+                                                                    external_terms, hist, bs);
   } else {
     cudaFuncSetAttribute(berry_deromega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA,
                                                                    idO, nw, nk, L, G, table, *sp, internal_terms,
-                                                                   external_terms, hist);
+                                                                   external_terms, hist, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }

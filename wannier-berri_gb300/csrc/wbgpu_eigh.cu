@@ -497,7 +497,7 @@ int pick_group(size_t smem, int threads, int gmax) {
 
 template <typename R, typename TU, typename HIn>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int lowerIn,
-                void* workspace, int* errflag, cudaStream_t stream) {
+                int valuesOnly, void* workspace, int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
   typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
@@ -518,6 +518,7 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   const size_t smQ = (size_t)BQ * 2 * n * sizeof(R);
   cudaFuncSetAttribute(eigh_ql<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_ql<R><<<(nk + BQ - 1) / BQ, BQ, smQ, stream>>>(d, e, n, nk, (double*)E, errflag);
+  if (valuesOnly) return wbg_cuda_status(cudaGetLastError());
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
   const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
   int CW = n;  // back-transform chunk width: the whole U unless it does not fit next to Z
@@ -541,15 +542,20 @@ size_t wbg_eigh_workspace_bytes(int n, int nk) {
 
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int mode,
                  void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
-  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
-  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER)) return WBG_ERR_ARG;
+  const int vo = (mode & WBG_EIGH_VALUES) ? 1 : 0;
+  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || (!U && !vo) || !errflag) return WBG_ERR_ARG;
+  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES)) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
   const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
   switch (mode & 3) {
-    case 1: return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
-    case 0: return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
-    case 2: return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
-    default: return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, workspace, errflag, stream);
+    case 1:
+      return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+    case 0:
+      return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+    case 2:
+      return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+    default:
+      return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
   }
 }
 

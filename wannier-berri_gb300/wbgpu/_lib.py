@@ -14,7 +14,7 @@ EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_wo
            'wbg_r2k_columns', 'wbg_ws_replicas',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
-           'wbg_scan_finalize', 'wbg_probe_fma']
+           'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma']
 
 STATUS_OK = 0
 
@@ -38,6 +38,14 @@ class KuboParams(ctypes.Structure):
     _fields_ = [('EFmin', ctypes.c_double), ('EFmax', ctypes.c_double), ('kBT', ctypes.c_double),
                 ('eta', ctypes.c_double), ('degen_thresh', ctypes.c_double), ('nEF', ctypes.c_int),
                 ('nOmega', ctypes.c_int), ('gaussian', ctypes.c_int), ('reserved', ctypes.c_int)]
+
+
+class TetraGrid(ctypes.Structure):
+    _fields_ = [('div', ctypes.c_int * 3), ('fft', ctypes.c_int * 3)]
+
+
+class FieldIndex(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ['V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C']]
 
 
 _P = ctypes.c_void_p
@@ -68,6 +76,12 @@ _SIGS = {
     'wbg_kubo_workspace_size': (_I, [_I, _I, _I, ctypes.POINTER(_SZ)]),
     'wbg_kubo': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.POINTER(KuboParams), _P, _P, _P, _SZ, _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
+    'wbg_tetra_select': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_double, _I, _P, _P]),
+    'wbg_band_values': (_I, [_P, _P, _I, ctypes.POINTER(FieldIndex), _I, _I, _I, _I, _I, ctypes.c_double, _P, _P, _I,
+                             _P]),
+    'wbg_tetra_accumulate': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, _P, _P, _I, _P, _I, _I, _I, _P,
+                                  _P]),
     'wbg_probe_fma': (_I, [_I, _I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), _P]),
 }
 

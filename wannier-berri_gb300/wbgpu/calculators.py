@@ -3,10 +3,14 @@
 Mirrors calculators/static.py:24-169 (StaticCalculator: Fermi-level scan with
 cumulative weights, /cell_volume /nk * constant_factor) for ``AHC``
 (calculators/static.py:353-364), ``Morb`` (:231-247), ``BerryDipole_FermiSea``
-(:472-487), and calculators/dynamic.py:26-196 for ``OpticalConductivity``.  A calculator declares the band-basis quantities it
-needs (``quantities``), accumulates a device histogram per batch of blocks
-(``accumulate``) and turns it into an ``EnergyResult`` (``finalize``).  Formulae
-without a GPU kernel raise NotImplementedError: there is no CPU fallback.
+(:472-487), ``DOS`` / ``CumDOS`` (:192-214), ``Ohmic_FermiSea`` / ``Ohmic_FermiSurf``
+(:379-403), and calculators/dynamic.py:26-196 for ``OpticalConductivity``.  A calculator
+declares the band-basis quantities it needs (``quantities``), accumulates a device histogram
+per batch of blocks (``accumulate``) and turns it into an ``EnergyResult`` (``finalize``).
+With ``tetra=True`` the static calculators use the tetrahedron method (static.py:80-125,
+grid/tetrahedron.py): per-band values (wbg_band_values) weighted by the tetrahedron
+occupations of the corner energies (wbg_tetra_accumulate).  Formulae without a GPU kernel
+raise NotImplementedError: there is no CPU fallback.
 """
 import ctypes
 
@@ -19,6 +23,7 @@ from .engine import _ptr, _stream
 from .factors import factor_ahc, factor_morb, factor_ohmic, factor_opt
 
 WBG_FORMULA_IDENTITY, WBG_FORMULA_INVMASS, WBG_FORMULA_VELVEL = 0, 1, 2  # include/wbgpu.h
+WBG_FORMULA_OMEGA, WBG_FORMULA_DEROMEGA, WBG_FORMULA_MORB = 3, 4, 5
 from .result import EnergyResult
 
 
@@ -37,16 +42,19 @@ class StaticCalculator(Calculator):
     def __init__(self, Efermi, tetra=False, smoother=None, constant_factor=1., use_factor=True,
                  kwargs_formula=None, Emin=-np.inf, Emax=np.inf, hole_like=False, k_resolved=False, **kwargs):
         super().__init__(**kwargs)
-        if tetra or k_resolved or hole_like or smoother is not None:
-            raise NotImplementedError("tetra / k_resolved / hole_like / smoother are not supported by the GPU backend")
+        if k_resolved or hole_like or smoother is not None:
+            raise NotImplementedError("k_resolved / hole_like / smoother are not supported by the GPU backend")
+        if tetra and np.isfinite(Emin):
+            raise NotImplementedError("tetra=True with a finite Emin is not supported by the GPU backend")
+        self.tetra = bool(tetra)
         self.Efermi = np.array(Efermi, dtype=float)
         self.constant_factor = constant_factor
         self.use_factor = use_factor
         self.kwargs_formula = dict(kwargs_formula or {})
         self.internal_terms = self.kwargs_formula.get('internal_terms', True)
         self.external_terms = self.kwargs_formula.get('external_terms', True)
-        # calculators/static.py:53-58
-        self.extraEf = 0 if self.fder == 0 else 1 if self.fder in (1, 2) else 2
+        # calculators/static.py:53-58 (the tetrahedron weights need no extra levels)
+        self.extraEf = 0 if (self.fder == 0 or self.tetra) else 1 if self.fder in (1, 2) else 2
         self.dEF = self.Efermi[1] - self.Efermi[0] if len(self.Efermi) > 1 else 0.001
         self.EFmin = self.Efermi[0] - self.extraEf * self.dEF
         self.EFmax = self.Efermi[-1] + self.extraEf * self.dEF
@@ -62,6 +70,31 @@ class StaticCalculator(Calculator):
 
     def reset(self, device):
         self._hist = torch.zeros((self.nEF_extra, self.ncomp), dtype=torch.float64, device=device)
+        if self.tetra:
+            self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
+
+    def tetra_accumulate(self, bd, formula, hist, ncomp, fields, ext=False):
+        """Tetrahedron method for one batch (static.py:80-85,119-125): bands selected by their
+        corner energies (sea for fder 0), per-band values of `formula`, weighted sum into the
+        histogram in difference form (wbg_scan_finalize then yields the result)."""
+        tc = bd.tetra
+        if tc is None:
+            raise RuntimeError("tetra=True needs the corner energies of run() over a regular Grid")
+        lib = _lib.load()
+        sel = tc.selection(bd, self.Efermi[0], self.Efermi[-1], self.degen_thresh, int(self.fder == 0))
+        P = torch.empty((bd.nk_total, bd.nw, ncomp), dtype=torch.float64, device=bd.E.device)
+        fi = _lib.FieldIndex(**{k: int(bd.index.get(q, 0)) for k, q in fields.items()})
+        xbar = _ptr(bd.Xbar) if bd.Xbar is not None else None
+        nF = bd.Xbar.shape[1] if bd.Xbar is not None else 0
+        st = engine._timed('band_values', lib.wbg_band_values, _ptr(bd.E), xbar, nF, ctypes.byref(fi), bd.nw,
+                           bd.nk_total, formula, int(self.internal_terms), int(ext),
+                           ctypes.c_double(self.degen_thresh), _ptr(sel), _ptr(P), int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_band_values")
+        ascending = int(len(self.Efermi) < 2 or np.all(np.diff(self.Efermi) > 0))
+        st = engine._timed('tetra_accumulate', lib.wbg_tetra_accumulate, _ptr(bd.E), _ptr(tc.Ec), _ptr(tc.slot),
+                           _ptr(bd.tetra_blocks), bd.nblocks, ctypes.byref(tc.grid), bd.nw, _ptr(sel), _ptr(P), ncomp,
+                           _ptr(self._ef), len(self.Efermi), int(self.fder), ascending, _ptr(hist), _stream())
+        _lib.check(st, "wbg_tetra_accumulate")
 
     def finalize(self, cell_volume, nk, factor=1.0):
         """Cumulative scan and normalisation (static.py:127-155) times the K-point factor."""
@@ -84,6 +117,8 @@ class AHC(StaticCalculator):
 
     def accumulate(self, bd, system):
         ext = self.external(system)
+        if self.tetra:
+            return self.tetra_accumulate(bd, WBG_FORMULA_OMEGA, self._hist, 3, {'V': 'V', 'A': 'A', 'O': 'Od'}, ext)
         sc = self.scan_struct()
         iA = bd.index.get('A', 0)
         iO = bd.index.get('Od', 0)
@@ -112,6 +147,10 @@ class Morb(StaticCalculator):
 
     def accumulate(self, bd, system):
         ext = self.external(system)
+        if self.tetra:
+            f = {'V': 'V', 'A': 'A', 'O': 'Od', 'B': 'B', 'C': 'C'}
+            self.tetra_accumulate(bd, WBG_FORMULA_MORB, self._hist, 3, f, ext)
+            return self.tetra_accumulate(bd, WBG_FORMULA_OMEGA, self._hist_omega, 3, f, ext)
         sc = self.scan_struct()
         lib = _lib.load()
         g = lambda q: bd.index.get(q, 0)
@@ -143,6 +182,9 @@ class BerryDipole_FermiSea(StaticCalculator):
 
     def accumulate(self, bd, system):
         ext = self.external(system)
+        if self.tetra:
+            f = {'V': 'V', 'A': 'A', 'O': 'O', 'W': 'W', 'dA': 'dA', 'dO': 'dO'}
+            return self.tetra_accumulate(bd, WBG_FORMULA_DEROMEGA, self._hist, 9, f, ext)
         sc = self.scan_struct()
         g = lambda q: bd.index.get(q, 0)
         st = engine._timed('berry_deromega', _lib.load().wbg_berry_deromega, _ptr(bd.E), _ptr(bd.Xbar),
@@ -166,6 +208,8 @@ class _ScanCalculator(StaticCalculator):
         return set(self.fields)
 
     def accumulate(self, bd, system):
+        if self.tetra:
+            return self.tetra_accumulate(bd, self.formula, self._hist, self.ncomp, {'V': 'V', 'W': 'W'})
         sc = self.scan_struct()
         g = lambda q: bd.index.get(q, 0)
         xbar = _ptr(bd.Xbar) if bd.Xbar is not None else None
@@ -177,7 +221,7 @@ class _ScanCalculator(StaticCalculator):
 
     def _data(self, cell_volume, nk, factor):
         data = self.finalize(cell_volume, nk, factor)
-        if self.fder == 1:  # calculators/static.py:137-140
+        if self.fder == 1 and not self.tetra:  # calculators/static.py:137-140
             data = (data[2:] - data[:-2]) / (2 * self.dEF)
         return data
 

@@ -360,6 +360,7 @@ class BandData:
         self.nblocks, self.nk, self.nw = nblocks, nk, nw
         self.fp64_fields = fp64_fields
         self.hermitian = hermitian  # V and A of Xbar exactly Hermitian (mixed path)
+        self.tetra = None  # TetraCorners context, set by run() for tetra=True calculators
 
     @property
     def omega_mode(self):
@@ -386,6 +387,7 @@ PREC_FP32, PREC_FP64, PREC_DF64, PREC_FP32S = 0, 1, 2, 3
 # (hi + lo pair), so they enter with 48 bits; output, intermediates and phases as PREC_FP32.
 C64_PRECS = (PREC_FP32, PREC_FP32S)
 EIGH_LOWER = 4  # wbg_eigh_batched mode bit: H given by its lower triangle
+EIGH_VALUES = 8  # wbg_eigh_batched mode bit: eigenvalues only
 
 
 def _prec(p):
@@ -499,12 +501,13 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1, work=None, flag=None)
         work = torch.empty(int(ws.value), dtype=torch.uint8, device=dev)
     if E is None:
         E = torch.empty((nk, nw), dtype=torch.float64, device=dev)
-    if U is None:
+    if U is None and not mode & EIGH_VALUES:
         U = torch.empty((nk, nw, nw), dtype=torch.complex128 if (mode & 3) == 1 else torch.complex64, device=dev)
     if flag is None:
         flag = torch.zeros(1, dtype=torch.int32, device=dev)
-    st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E), _ptr(U), nw * nw,
-                int(mode), _ptr(work), ctypes.c_size_t(work.numel()), _ptr(flag), _stream())
+    st = _timed('eigh', lib.wbg_eigh_batched, _ptr(Hfields), strideH, nw, nk, _ptr(E),
+                None if U is None else _ptr(U), nw * nw, int(mode), _ptr(work), ctypes.c_size_t(work.numel()),
+                _ptr(flag), _stream())
     _lib.check(st, "wbg_eigh_batched")
     return E, U, flag
 
@@ -613,6 +616,114 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     bd._keep = keep
     bd._flag = flag
     return bd
+
+
+def energies(dev, dKs, NKFFT, precision='fp64', out=None, phases=None, block_start=0, ws=None):
+    """Eigenvalues of H(k) only (np.linalg.eigvalsh) for a batch of blocks: (nblocks*nk, nw)
+    float64 written to `out` when given.  FP64 ('fp64') or double-float ('mixed') transform and
+    tridiagonal QL, no eigenvectors.  Returns (E, flag)."""
+    require_cuda()
+    nw = dev.nw
+    NKFFT = [int(n) for n in NKFFT]
+    nkt = len(dKs) * int(np.prod(NKFFT))
+    arena = ws if ws is not None else dev
+    flag = arena.buffer('flag_E', (1,), torch.int32)
+    flag.zero_()
+    if precision == 'fp64':
+        prec, lower, mode = PREC_FP64, False, 1
+    elif precision == 'mixed':
+        lower = 'Ham' in dev.hermitian_bases()
+        prec, mode = PREC_DF64, 3 | (EIGH_LOWER if lower else 0)
+    else:
+        raise ValueError(f"unknown precision mode {precision!r}")
+    _, _, nF, _ = field_arrays(dev, set(), True, prec)
+    Hf = arena.buffer('fields_H', (nkt, nF, nw, nw), torch.complex128)
+    geo = r2k_geometry(dev, NKFFT)
+    wsz = ctypes.c_size_t(0)
+    _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, len(dKs), prec, ctypes.byref(wsz)),
+               "wbg_r2k_workspace_size")
+    work = arena.buffer('r2k_ws', (int(wsz.value),), torch.uint8)
+    Hf, _, _, keep = r2k(dev, dKs, NKFFT, set(), True, prec, out=Hf, workspace=work,
+                         phases=None if phases is None else phases.get(prec), block_start=block_start, lower=lower)
+    ews = ctypes.c_size_t(0)
+    _lib.check(_lib.load().wbg_eigh_workspace_size(nw, nkt, ctypes.byref(ews)), "wbg_eigh_workspace_size")
+    ework = arena.buffer('eigh_ws', (int(ews.value),), torch.uint8)
+    E = out if out is not None else arena.buffer('E', (nkt, nw), torch.float64)
+    E, _, flag = eigh(Hf, nF * nw * nw, nw, nkt, E=E, U=None, mode=mode | EIGH_VALUES, work=ework, flag=flag)
+    del keep
+    return E, flag
+
+
+class TetraCorners:
+    """Corner energies of the tetrahedron method for a run over `grid` (grid/tetrahedron.py
+    TetraWeightsParal, data_K/data_K_R.py:121-141).  The corners k +- delta/2 of every k-point
+    (delta = 1/(NKdiv NKFFT)) are the dense grid shifted by +delta/2; corner block c is the FFT
+    grid at shift (c + 1/2) delta.  The corner blocks that the run's blocks touch (i and i-1 per
+    axis) are evaluated once and stay resident: Ec (ncorner*nk, nw) float64, slot[flat corner
+    block] = its row (-1: not evaluated)."""
+
+    def __init__(self, dev, grid, blocks=None, precision='fp64', ws=None, batch=None):
+        div, fft = np.array(grid.div, dtype=int), np.array(grid.FFT, dtype=int)
+        self.grid = _lib.TetraGrid((ctypes.c_int * 3)(*div.tolist()), (ctypes.c_int * 3)(*fft.tolist()))
+        self.nblocks_total = int(np.prod(div))
+        blocks = np.arange(self.nblocks_total) if blocks is None else np.asarray(blocks, dtype=int)
+        idx = np.stack(np.unravel_index(blocks, div), axis=-1)
+        need = set()
+        for s in range(8):
+            c = idx.copy()
+            for a in range(3):
+                if not (s >> (2 - a)) & 1:
+                    c[:, a] = (c[:, a] - 1) % div[a]
+            need.update(np.ravel_multi_index(c.T, div).tolist())
+        cb = np.array(sorted(need), dtype=int)
+        slot = -np.ones(self.nblocks_total, dtype=np.int32)
+        slot[cb] = np.arange(len(cb), dtype=np.int32)
+        self.slot = torch.from_numpy(slot).to(dev.device)
+        shifts = (np.stack(np.unravel_index(cb, div), axis=-1) + 0.5) / (div * fft)[None, :]
+        nk = int(np.prod(fft))
+        nw = dev.nw
+        self.Ec = torch.empty((len(cb) * nk, nw), dtype=torch.float64, device=dev.device)
+        prec = PREC_FP64 if precision == 'fp64' else PREC_DF64
+        phases = {prec: dev.grid_phases(shifts, fft, prec)}
+        if batch is None:
+            from .run import choose_batch
+            batch = choose_batch(nw, nk, len(cb), set(), precision)
+        self.flags = []  # QL convergence flags, read by check() (no synchronisation here)
+        for i0 in range(0, len(cb), batch):
+            n = min(batch, len(cb) - i0)
+            _, flag = energies(dev, shifts[i0:i0 + n], fft, precision, out=self.Ec[i0 * nk:(i0 + n) * nk],
+                               phases=phases, block_start=i0, ws=ws)
+            self.flags.append(flag.clone())
+        self.device = dev.device
+
+    @staticmethod
+    def nbytes(grid, nblocks, nw):
+        """Upper bound of the resident corner energies for a run over `nblocks` blocks."""
+        ncorner = min(int(np.prod(grid.div)), 8 * int(nblocks))
+        return ncorner * int(np.prod(grid.FFT)) * nw * 8
+
+    def check(self):
+        if any(int(f.item()) != 0 for f in self.flags):
+            raise RuntimeError("wbg_eigh_batched: QL iteration did not converge for some corner k-point")
+
+    def attach(self, bd, block_ids):
+        """Give a batch's BandData its corner context (block_ids: flat division-grid indices)."""
+        bd.tetra = self
+        bd.tetra_blocks = torch.tensor(np.asarray(block_ids, dtype=np.int32), device=self.device)
+        bd.tetra_sel = {}
+        return bd
+
+    def selection(self, bd, EF0, EF1, degen_thresh, sea):
+        """wbg_tetra_select for a batch (cached per window on the BandData)."""
+        key = (float(EF0), float(EF1), float(degen_thresh), int(sea))
+        if key not in bd.tetra_sel:
+            sel = torch.empty((bd.nk_total, bd.nw), dtype=torch.int8, device=self.device)
+            st = _timed('tetra_select', _lib.load().wbg_tetra_select, _ptr(bd.E), _ptr(self.Ec), _ptr(self.slot),
+                        _ptr(bd.tetra_blocks), bd.nblocks, ctypes.byref(self.grid), bd.nw, ctypes.c_double(EF0),
+                        ctypes.c_double(EF1), ctypes.c_double(degen_thresh), int(sea), _ptr(sel), _stream())
+            _lib.check(st, "wbg_tetra_select")
+            bd.tetra_sel[key] = sel
+        return bd.tetra_sel[key]
 
 
 def device_flags(clear=True):

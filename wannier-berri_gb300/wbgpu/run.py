@@ -4,7 +4,8 @@ Blocks (K-points of the division grid) are processed in batches; each batch runs
 stages 1-3 once (engine.band_data) and every calculator accumulates its device
 histogram from the same band data.  Results are summed over blocks times the K-point
 factor 1/prod(NKdiv) (run_grid.py:59-66).  No symmetry reduction, refinement or
-restart files (those live outside the GPU hot path).
+restart files (those live outside the GPU hot path).  Calculators with tetra=True get
+the corner energies of the tetrahedron method (engine.TetraCorners), computed once per run.
 """
 import numpy as np
 import torch
@@ -35,18 +36,26 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
     for c in calculators.values():
         c.reset(dev.device)
     shifts = grid.block_shifts()
-    if blocks is not None:
-        shifts = shifts[np.asarray(blocks)]
+    block_ids = np.arange(len(shifts)) if blocks is None else np.asarray(blocks, dtype=int)
+    shifts = shifts[block_ids]
     nk = grid.nk_per_block
     nb = blocks_per_batch or choose_batch(dev.nw, nk, len(shifts), quantities, precision)
+    # tetrahedron method: corner energies of every block the run touches, once, kept resident
+    tetra = None
+    if any(getattr(c, 'tetra', False) for c in calculators.values()):
+        tetra = engine.TetraCorners(dev, grid, block_ids, precision)
     precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
     for i0 in range(0, len(shifts), nb):
         bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
                               block_start=i0)
+        if tetra is not None:
+            tetra.attach(bd, block_ids[i0:i0 + nb])
         for c in calculators.values():
             c.accumulate(bd, system)
         engine.check_flag(bd)
         del bd
+    if tetra is not None:
+        tetra.check()
     factor = 1.0 / grid.nblocks
     return ResultDict({k: c.result(system.cell_volume, nk, factor) for k, c in calculators.items()})

@@ -158,9 +158,16 @@ class Server:
         q = set()
         for c in req.calculators.values():
             q |= c.quantities(system)
-        nb = choose_batch(dev.nw, req.grid.nk_per_block, len(self._blocks_of(req)), q, self.precision,
-                          max_kpoints=self.max_kpoints)
-        return q, nb, request_bytes(dev.nw, req.grid.nk_per_block, nb, q, self.precision)
+        nblk = len(self._blocks_of(req))
+        nb = choose_batch(dev.nw, req.grid.nk_per_block, nblk, q, self.precision, max_kpoints=self.max_kpoints)
+        nbytes = request_bytes(dev.nw, req.grid.nk_per_block, nb, q, self.precision)
+        if self._tetra(req):  # resident corner energies of the tetrahedron method
+            nbytes += engine.TetraCorners.nbytes(req.grid, nblk, dev.nw)
+        return q, nb, nbytes
+
+    @staticmethod
+    def _tetra(req):
+        return any(getattr(c, 'tetra', False) for c in req.calculators.values())
 
     @staticmethod
     def _blocks_of(req):
@@ -209,6 +216,10 @@ class Server:
         with torch.cuda.stream(req.stream):
             for c in req.calculators.values():
                 c.reset(self.device)
+            req.tetra = None
+            if self._tetra(req):
+                req.tetra = engine.TetraCorners(dev, req.grid, blocks, self.precision, ws=req.ws)
+                req.flags.extend(req.tetra.flags)
             if not req.batches:
                 req.done_event = torch.cuda.Event()
                 req.done_event.record(req.stream)
@@ -226,6 +237,8 @@ class Server:
                                       phases=req.phases, block_start=int(idx[0]), ws=req.ws)
             else:
                 bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
+            if req.tetra is not None:
+                req.tetra.attach(bd, idx)
             for c in req.calculators.values():
                 c.accumulate(bd, system)
             # the QL convergence flag is read once the request has finished
