@@ -228,10 +228,13 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
  * bands (der 0).  hist [nEF][ncomp] is accumulated in difference form (hist[i] += P (w(i) -
  * w(i-1))): wbg_scan_finalize turns it into the sum.  ascending != 0: efermi is sorted
  * ascending and only the levels between a band's smallest and largest corner energy are
- * evaluated. */
+ * evaluated.  fp64 = 1: the reference's FP64 arithmetic (der 1 from its expanded cubic);
+ * fp64 = 0 (mixed precision): energies relative to each band's lowest one as double-float
+ * pairs, then FP32 relative to each tetrahedron's lowest corner (~1e-7 relative error per
+ * weight; der 1 from the product rule on the piecewise form, free of the cubic's cancellation). */
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
-                         int ncomp, const double* efermi, int nEF, int der, int ascending, double* hist,
+                         int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64, double* hist,
                          void* stream);
 
 /* ---- tabulation (calculators/tabulate.py:21-52 Tabulator with Energy, Velocity,

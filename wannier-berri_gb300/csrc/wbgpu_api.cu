@@ -176,10 +176,10 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
 
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
-                         int ncomp, const double* efermi, int nEF, int der, int ascending, double* hist,
-                         void* stream) {
+                         int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64,
+                         double* hist, void* stream) {
   return wbg_tetra_accumulate_run(E, Ecorner, corner_slot, blocks, nblocks, grid, nw, sel, P, ncomp, efermi, nEF, der,
-                                  ascending, hist, (cudaStream_t)stream);
+                                  ascending, fp64, hist, (cudaStream_t)stream);
 }
 
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream) {

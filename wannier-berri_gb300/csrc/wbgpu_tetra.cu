@@ -200,6 +200,94 @@ WBG_D double tet_dos(const Tet& q, double ef) {
   return c1 + ef * (2.0 * c2 + 3.0 * c3 * ef);
 }
 
+// ---- FP32 weights (mixed precision) -------------------------------------------------------
+// A band's 9 energies are taken relative to its lowest one, eb, as double-float pairs (hi, lo;
+// 48-bit significand), so sorting, the gaps and the 1e-12 separation lose nothing; everything
+// after is FP32 relative to the tetrahedron's lowest corner e1 (x = E_F - e1), so each factor
+// (x / gap) carries ~1e-7 relative error.  The derivative (der 1) is the product rule applied
+// to the accurate piecewise form, the same cubic as the reference's expanded polynomial
+// without its cancellation.
+struct TetF {
+  float c_hi, c_lo;                    // e1 - eb
+  float g2, g3, g4;                    // e2 - e1, e3 - e1, e4 - e1 (after the separation)
+  float r21, r31, r41, r32, r42, r43;  // reciprocals of the gaps
+};
+
+WBG_D bool df_less(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+
+WBG_D TetF make_tetf(float2 a, float2 b, float2 c, float2 d) {
+  float2 t;
+  if (df_less(b, a)) { t = a; a = b; b = t; }
+  if (df_less(d, c)) { t = c; c = d; d = t; }
+  if (df_less(c, a)) { t = a; a = c; c = t; }
+  if (df_less(d, b)) { t = b; b = d; d = t; }
+  if (df_less(c, b)) { t = b; b = c; c = t; }
+  const float sep = 1e-12f;
+  float d1 = (b.x - a.x) + (b.y - a.y);
+  float d2 = (c.x - b.x) + (c.y - b.y);
+  float d3 = (d.x - c.x) + (d.y - c.y);
+  if (d1 < sep) { d2 -= sep - d1; d1 = sep; }  // e2 = e1 + sep moves e2 up: the next gap shrinks
+  if (d2 < sep) { d3 -= sep - d2; d2 = sep; }
+  if (d3 < sep) d3 = sep;
+  TetF q;
+  q.c_hi = a.x;
+  q.c_lo = a.y;
+  q.g2 = d1;
+  q.g3 = d1 + d2;
+  q.g4 = d1 + d2 + d3;
+  q.r21 = __frcp_rn(d1);
+  q.r31 = __frcp_rn(q.g3);
+  q.r41 = __frcp_rn(q.g4);
+  q.r32 = __frcp_rn(d2);
+  q.r42 = __frcp_rn(d2 + d3);
+  q.r43 = __frcp_rn(d3);
+  return q;
+}
+
+WBG_D float tetf_occ(const TetF& q, float x) {
+  if (x >= q.g4) return 1.0f;
+  if (x < 0.0f) return 0.0f;
+  if (x >= q.g3) {
+    const float y = q.g4 - x;
+    return 1.0f - (y * q.r41) * (y * q.r42) * (y * q.r43);
+  }
+  if (x >= q.g2) {
+    const float x2 = x - q.g2;
+    const float a13 = x * q.r31, a14 = x * q.r41, a23 = x2 * q.r32, a24 = x2 * q.r42;
+    return a23 * a24 + a13 * (a14 * (1.0f - a24) + a24 * (1.0f - a23));
+  }
+  return (x * q.r21) * (x * q.r31) * (x * q.r41);
+}
+
+WBG_D float tetf_dos(const TetF& q, float x) {
+  if (x >= q.g4 || x < 0.0f) return 0.0f;
+  if (x >= q.g3) {
+    const float y = q.g4 - x;
+    return 3.0f * y * y * (q.r41 * q.r42 * q.r43);
+  }
+  if (x >= q.g2) {
+    const float x2 = x - q.g2;
+    const float a13 = x * q.r31, a14 = x * q.r41, a23 = x2 * q.r32, a24 = x2 * q.r42;
+    const float B = a14 * (1.0f - a24) + a24 * (1.0f - a23);
+    const float dB = q.r41 * (1.0f - a24) - a14 * q.r42 + q.r42 * (1.0f - a23) - a24 * q.r32;
+    return q.r32 * a24 + a23 * q.r42 + q.r31 * B + a13 * dB;
+  }
+  return 3.0f * x * x * (q.r21 * q.r31 * q.r41);
+}
+
+// s += v, compensated (error-free two-sum into s.y)
+WBG_D void two_sum_add(float2& s, float v) {
+  const float t = s.x + v;
+  const float bp = t - s.x;
+  s.y += (s.x - (t - bp)) + (v - bp);
+  s.x = t;
+}
+
+WBG_D float2 split_df(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
 // first index i with EF[i] >= x (EF ascending)
 WBG_D int lower_bound(const double* __restrict__ EF, int n, double x) {
   int lo = 0, hi = n;
@@ -212,6 +300,9 @@ WBG_D int lower_bound(const double* __restrict__ EF, int n, double x) {
 }
 
 constexpr int kWin = 32;  // Fermi levels per window chunk (per-lane column of shared memory)
+// shared memory per warp: window sums [kWin][32], level offsets [kWin][32] (FP32 weights only),
+// band energies [9][32]; 8 bytes each
+constexpr int kWarpSmem = (2 * kWin + 9) * 32;
 
 // ---------------------------------------------------------------------------------------
 // Weighted accumulation.  Lane n takes band n of its warp's k-point: for sel 1 the band weight
@@ -219,10 +310,11 @@ constexpr int kWin = 32;  // Fermi levels per window chunk (per-lane column of s
 // smallest and largest corner energy (0 below, 1 (der 0) / 0 (der 1) above); for sel 2 the
 // weight is 1 everywhere (the Fermi sea, der 0).  hist gets the contribution P[k][n] w(E_F) in
 // difference form -- hist[i] += P (w(i) - w(i-1)) -- so that the cumulative scan of
-// wbg_scan_finalize returns sum P w.  smem: the block's [nEF][nc] histogram when it fits
-// (else atomics go to hist directly) + per warp [kWin][32] window sums and [9][32] energies
-// (the 8 corners and the k-point of each lane's band).
+// wbg_scan_finalize returns sum P w.  F32: weights in FP32 (mixed precision, see TetF); else
+// the reference's FP64 arithmetic.  smem: the block's [nEF][nc] histogram when it fits (else
+// atomics go to hist directly) + kWarpSmem doubles per warp.
 // ---------------------------------------------------------------------------------------
+template <bool F32>
 __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const double* __restrict__ Ec,
                                         const int* __restrict__ slot, const int* __restrict__ blocks,
                                         wbg_tetra_grid g, int nw, long long nkt, const signed char* __restrict__ sel,
@@ -231,8 +323,11 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
   extern __shared__ double sm[];
   const int G = blockDim.x / 32, w = threadIdx.x / 32, lane = threadIdx.x % 32;
   double* acc = smem_hist ? sm : hist;
-  double* win = sm + (smem_hist ? (size_t)nEF * nc : 0) + (size_t)w * (kWin + 9) * 32;
-  double* ek = win + kWin * 32;  // [9][32]: corner s at s * 32 + lane, the k-point at 8 * 32 + lane
+  double* win = sm + (smem_hist ? (size_t)nEF * nc : 0) + (size_t)w * kWarpSmem;
+  float2* winf = reinterpret_cast<float2*>(win);            // F32: compensated window sums
+  float2* xs = reinterpret_cast<float2*>(win + kWin * 32);  // F32: E_F - eb per level
+  double* ek = win + 2 * kWin * 32;                         // [9][32]: corner s at s * 32 + lane
+  float2* ekf = reinterpret_cast<float2*>(ek);              // F32: e - eb as (hi, lo)
   if (smem_hist) {
     for (int i = threadIdx.x; i < nEF * nc; i += blockDim.x) sm[i] = 0.0;
     __syncthreads();
@@ -255,13 +350,22 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
       for (int c = 0; c < nc; ++c) pv[c] = Pn[c];
       const double e0 = E[kk * nw + n];
       double lo = e0, hi = e0;
+      double ev[8];
+#pragma unroll
       for (int s8 = 0; s8 < 8; ++s8) {
-        const double x = Ec[corner_row(g, blocks, slot, kk, s8) * nw + n];
-        ek[s8 * 32 + lane] = x;
-        lo = fmin(lo, x);
-        hi = fmax(hi, x);
+        ev[s8] = Ec[corner_row(g, blocks, slot, kk, s8) * nw + n];
+        lo = fmin(lo, ev[s8]);
+        hi = fmax(hi, ev[s8]);
       }
-      // below lo every weight is 0; from ilast on, E_F exceeds every (separated) tetrahedron top
+      if constexpr (F32) {
+#pragma unroll
+        for (int s8 = 0; s8 < 8; ++s8) ekf[s8 * 32 + lane] = split_df(ev[s8] - lo);
+        ekf[8 * 32 + lane] = split_df(e0 - lo);
+      } else {
+#pragma unroll
+        for (int s8 = 0; s8 < 8; ++s8) ek[s8 * 32 + lane] = ev[s8];
+      }
+      // below lo every weight is 0; from i1 on, E_F exceeds every (separated) tetrahedron top
       int i0 = 0, i1 = nEF;
       if (ascending) {
         i0 = lower_bound(EF, nEF, lo);
@@ -270,18 +374,41 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
       double wprev = 0.0;
       for (int c0 = i0; c0 < i1; c0 += kWin) {
         const int cn = min(kWin, i1 - c0);
-        for (int i = 0; i < cn; ++i) win[i * 32 + lane] = 0.0;
+        if constexpr (F32) {
+          for (int i = 0; i < cn; ++i) {
+            winf[i * 32 + lane] = make_float2(0.0f, 0.0f);
+            xs[i * 32 + lane] = split_df(__ldg(EF + c0 + i) - lo);
+          }
+        } else {
+          for (int i = 0; i < cn; ++i) win[i * 32 + lane] = 0.0;
+        }
 #pragma unroll 1
         for (int t = 0; t < 12; ++t) {
-          const Tet q = make_tet(e0, ek[kTetra[t][0] * 32 + lane], ek[kTetra[t][1] * 32 + lane],
-                                 ek[kTetra[t][2] * 32 + lane]);
-          if (der == 0)
-            for (int i = 0; i < cn; ++i) win[i * 32 + lane] += tet_occ(q, __ldg(EF + c0 + i));
-          else
-            for (int i = 0; i < cn; ++i) win[i * 32 + lane] += tet_dos(q, __ldg(EF + c0 + i));
+          if constexpr (F32) {
+            const TetF q = make_tetf(ekf[8 * 32 + lane], ekf[kTetra[t][0] * 32 + lane], ekf[kTetra[t][1] * 32 + lane],
+                                     ekf[kTetra[t][2] * 32 + lane]);
+            for (int i = 0; i < cn; ++i) {
+              const float2 xb = xs[i * 32 + lane];
+              const float x = (xb.x - q.c_hi) + (xb.y - q.c_lo);
+              two_sum_add(winf[i * 32 + lane], der == 0 ? tetf_occ(q, x) : tetf_dos(q, x));
+            }
+          } else {
+            const Tet q = make_tet(e0, ek[kTetra[t][0] * 32 + lane], ek[kTetra[t][1] * 32 + lane],
+                                   ek[kTetra[t][2] * 32 + lane]);
+            if (der == 0)
+              for (int i = 0; i < cn; ++i) win[i * 32 + lane] += tet_occ(q, __ldg(EF + c0 + i));
+            else
+              for (int i = 0; i < cn; ++i) win[i * 32 + lane] += tet_dos(q, __ldg(EF + c0 + i));
+          }
         }
         for (int i = 0; i < cn; ++i) {
-          const double wi = win[i * 32 + lane] / 12.0;
+          double wi;
+          if constexpr (F32) {
+            const float2 v = winf[i * 32 + lane];
+            wi = ((double)v.x + (double)v.y) / 12.0;
+          } else {
+            wi = win[i * 32 + lane] / 12.0;
+          }
           const double d = wi - wprev;
           wprev = wi;
           if (d != 0.0)
@@ -331,20 +458,27 @@ int wbg_tetra_select_run(const double* E, const double* Ec, const int* slot, con
 
 int wbg_tetra_accumulate_run(const double* E, const double* Ec, const int* slot, const int* blocks, int nblocks,
                              const wbg_tetra_grid* g, int nw, const signed char* sel, const double* P, int ncomp,
-                             const double* EF, int nEF, int der, int ascending, double* hist, cudaStream_t stream) {
+                             const double* EF, int nEF, int der, int ascending, int fp64, double* hist,
+                             cudaStream_t stream) {
   if (!E || !Ec || !slot || !blocks || !g || !sel || !P || !EF || !hist || nblocks < 1 || nw < 1 || nEF < 1 ||
       !grid_ok(g))
     return WBG_ERR_ARG;
-  if (ncomp < 1 || ncomp > 9 || der < 0 || der > 1) return WBG_ERR_ARG;
+  if (ncomp < 1 || ncomp > 9 || der < 0 || der > 1 || fp64 < 0 || fp64 > 1) return WBG_ERR_ARG;
   const long long nkt = (long long)nblocks * g->fft[0] * g->fft[1] * g->fft[2];
   const int G = 4;
-  const size_t wsm = (size_t)G * (kWin + 9) * 32 * 8;
+  const size_t wsm = (size_t)G * kWarpSmem * 8;
   const size_t hsm = (size_t)nEF * ncomp * 8;
-  const int smem_hist = wsm + hsm <= 160 * 1024;
+  const int smem_hist = wsm + hsm <= 200 * 1024;
   const size_t sm = wsm + (smem_hist ? hsm : 0);
-  cudaFuncSetAttribute(tetra_accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  tetra_accumulate_kernel<<<grid_cap(G, nkt, 4), 32 * G, sm, stream>>>(E, Ec, slot, blocks, *g, nw, nkt, sel, P,
-                                                                       ncomp, EF, nEF, der, ascending, smem_hist,
-                                                                       hist);
+  const int nblk = grid_cap(G, nkt, 4);
+  if (fp64) {
+    cudaFuncSetAttribute(tetra_accumulate_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    tetra_accumulate_kernel<false><<<nblk, 32 * G, sm, stream>>>(E, Ec, slot, blocks, *g, nw, nkt, sel, P, ncomp, EF,
+                                                                 nEF, der, ascending, smem_hist, hist);
+  } else {
+    cudaFuncSetAttribute(tetra_accumulate_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    tetra_accumulate_kernel<true><<<nblk, 32 * G, sm, stream>>>(E, Ec, slot, blocks, *g, nw, nkt, sel, P, ncomp, EF,
+                                                                nEF, der, ascending, smem_hist, hist);
+  }
   return wbg_cuda_status(cudaGetLastError());
 }

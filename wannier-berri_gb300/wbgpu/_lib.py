@@ -80,8 +80,8 @@ _SIGS = {
                               ctypes.c_double, _I, _P, _P]),
     'wbg_band_values': (_I, [_P, _P, _I, ctypes.POINTER(FieldIndex), _I, _I, _I, _I, _I, ctypes.c_double, _P, _P, _I,
                              _P]),
-    'wbg_tetra_accumulate': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, _P, _P, _I, _P, _I, _I, _I, _P,
-                                  _P]),
+    'wbg_tetra_accumulate': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, _P, _P, _I, _P, _I, _I, _I, _I,
+                                  _P, _P]),
     'wbg_probe_fma': (_I, [_I, _I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), _P]),
 }
 

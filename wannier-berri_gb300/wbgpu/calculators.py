@@ -93,7 +93,8 @@ class StaticCalculator(Calculator):
         ascending = int(len(self.Efermi) < 2 or np.all(np.diff(self.Efermi) > 0))
         st = engine._timed('tetra_accumulate', lib.wbg_tetra_accumulate, _ptr(bd.E), _ptr(tc.Ec), _ptr(tc.slot),
                            _ptr(bd.tetra_blocks), bd.nblocks, ctypes.byref(tc.grid), bd.nw, _ptr(sel), _ptr(P), ncomp,
-                           _ptr(self._ef), len(self.Efermi), int(self.fder), ascending, _ptr(hist), _stream())
+                           _ptr(self._ef), len(self.Efermi), int(self.fder), ascending, int(bd.fp64_fields),
+                           _ptr(hist), _stream())
         _lib.check(st, "wbg_tetra_accumulate")
 
     def finalize(self, cell_volume, nk, factor=1.0):
