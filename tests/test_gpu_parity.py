@@ -514,6 +514,8 @@ def test_golden_random_dos_ohmic(golden_dir, precision, rule):
 def test_dos_ohmic_c2small_vs_oracle(c2small):
     """Same calculators on the MDRS model against the oracle, FP64 to 1e-9."""
     s, o = c2small
+    # the seeded models are Hermitian in R-space: the mixed path takes the lower-triangle route
+    assert engine.DeviceSystem(s).hermitian_bases() == frozenset({'Ham', 'AA'})
     EF = np.linspace(-1.5, 1.5, 31)
     C = wbgpu.calculators
     got = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(4, 3, 3)),

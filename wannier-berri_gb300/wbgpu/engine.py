@@ -183,17 +183,23 @@ class DeviceSystem:
         mixed path transforms only lower triangles.  Other bases keep the full-matrix path with
         the reference's symmetrisation (checked once per system)."""
         if 'herm_bases' not in self._cache:
-            iR = np.asarray(self.system.iRvec)
-            index = {tuple(r): i for i, r in enumerate(iR)}
-            neg = np.array([index.get(tuple(-r), -1) for r in iR])
+            R = self.geom.R  # sorted by (R0, R1, R2): -R found by a binary search on the packed keys
+            span = 2 * int(np.abs(R).max()) + 1
+            pack = lambda a: ((a[:, 0] * span) + a[:, 1]) * span + a[:, 2]
+            keys = pack(R)
+            pos = np.searchsorted(keys, pack(-R))
+            pos = np.minimum(pos, len(keys) - 1)
             out = set()
-            if (neg >= 0).all():
+            if np.array_equal(keys[pos], pack(-R)):
+                neg = torch.from_numpy(pos).to(self.device)
+                nw = self.nw
                 for key in ('Ham', 'AA'):
                     if not self.system.has_R_mat(key):
                         continue
-                    X = np.asarray(self.system.get_R_mat(key))
-                    diff = np.abs(X - X[neg].conj().swapaxes(1, 2)).max()
-                    if diff <= rtol * max(np.abs(X).max(), 1e-300):
+                    X = self._key_fp64(key).reshape(-1, len(R), nw, nw)  # device, sorted R order
+                    Xd = X[:, neg].conj().transpose(2, 3)
+                    diff, mx = (X - Xd).abs().max(), X.abs().max()
+                    if float(diff) <= rtol * max(float(mx), 1e-300):
                         out.add(key)
             self._cache['herm_bases'] = frozenset(out)
         return self._cache['herm_bases']
