@@ -82,6 +82,9 @@ template <typename TU, typename CR> WBG_D typename C2<TU>::t to_tu_c(CR a) {
 // Outputs: d[k][i], e[k][i] (e[n-1] = 0) in the solver type R; Vh[k][c][i] (v of reflector
 // c, v_{c+1}=1, zeros for i<=c) and tau[k][c] rounded to the back-transform type TV.
 // ---------------------------------------------------------------------------------------
+#ifndef WBG_TRI_DIV
+#define WBG_TRI_DIV 2
+#endif
 WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
@@ -157,13 +160,26 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
       for (int h = 0; h < 2; ++h) {
         const int i = owned_row(t, h, lane, L);
         if (i < n && i >= c + 1) {
-          // two independent accumulators (row part / column part) for instruction-level parallelism
-          CR acc = czero<CR>(), acc2 = czero<CR>();
+          // four independent accumulators (two per part of the row): the double-float
+          // multiply-adds are long dependent chains, so the lane needs several in flight
+          CR acc = czero<CR>(), acc1 = czero<CR>(), acc2 = czero<CR>(), acc3 = czero<CR>();
           const CR* Ai = Am + tri(i);
-          for (int j = c + 1; j <= i; ++j) cfma(acc, Ai[j], vs[j]);
-          for (int j = i + 1, idx = tri(i + 1) + i; j < n; idx += j + 1, ++j) cfmac(acc2, Am[idx], vs[j]);
-          acc.x = acc.x + acc2.x;
-          acc.y = acc.y + acc2.y;
+          int j = c + 1;
+          for (; j < i; j += 2) {
+            cfma(acc, Ai[j], vs[j]);
+            cfma(acc1, Ai[j + 1], vs[j + 1]);
+          }
+          if (j == i) cfma(acc, Ai[j], vs[j]);
+          j = i + 1;
+          int idx = tri(i + 1) + i;
+          for (; j + 1 < n; j += 2) {
+            cfmac(acc2, Am[idx], vs[j]);
+            cfmac(acc3, Am[idx + j + 1], vs[j + 1]);
+            idx += 2 * j + 3;
+          }
+          if (j < n) cfmac(acc2, Am[idx], vs[j]);
+          acc.x = (acc.x + acc1.x) + (acc2.x + acc3.x);
+          acc.y = (acc.y + acc1.y) + (acc2.y + acc3.y);
           const CR p = cmul(tau, acc);
           ws[i] = p;
           const CR v = vs[i];
@@ -191,6 +207,7 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
         if (i < n && i >= c + 1) {
           const CR vi = vs[i], wi = ws[i];
           CR* Ai = Am + tri(i);
+#pragma unroll 2
           for (int j = c + 1; j <= i; ++j) {
             CR a = Ai[j];
             const CR vj = vs[j], wj = ws[j];
@@ -506,7 +523,7 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   R* d = (R*)w; w += (size_t)nk * n * 8;
   R* e = (R*)w;
   const int L = lanes_for(n);
-  const int LT = L >= 8 ? L / 2 : 4;  // tridiagonalisation: mirrored row pairs, half the lanes
+  const int LT = L >= 8 ? L / WBG_TRI_DIV : 4;  // tridiagonalisation lanes per matrix
   const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
   const int G = pick_group(smT, LT, 128 / LT);
   if (G == 0) return WBG_ERR_SIZE;

@@ -87,18 +87,73 @@ WBG_D bool decode_col(const int* cols, int ncols, int nF, int nw2, int& f, int& 
   return true;
 }
 
+// Phase tables in shared memory, transposed for the contraction: row r (an R index), Nj
+// columns padded to JP = 4 ceil(Nj / 4).  FP32 entries are float4 (t.x, t.x, -t.y, t.y): the
+// two register pairs of one 16-byte load feed the two packed FMAs of acc += t x
+// (acc = (t.x, t.x) (x.x, x.y) + acc, then (-t.y, t.y) (x.y, x.x) + acc -- the same two
+// roundings per component, in the same order, as four scalar FMAs).
+template <typename T> struct PhaseEntry { typedef typename C2<T>::t type; };
+template <> struct PhaseEntry<float> { typedef float4 type; };
+
+template <typename T> WBG_D typename PhaseEntry<T>::type make_entry(typename C2<T>::t t) { return t; }
+template <> WBG_D float4 make_entry<float>(float2 t) { return make_float4(t.x, t.x, -t.y, t.y); }
+
+WBG_HD int pad4(int n) { return (n + 3) & ~3; }
+
+template <typename T>
+WBG_D void load_phases(const typename C2<T>::t* __restrict__ ph, int Nj, int nr,
+                       typename PhaseEntry<T>::type* tabT) {
+  typedef typename C2<T>::t V;
+  const int JP = pad4(Nj);
+  for (int idx = threadIdx.x; idx < nr * JP; idx += blockDim.x) {
+    const int r = idx / JP, j = idx % JP;
+    tabT[idx] = make_entry<T>(j < Nj ? ph[j * nr + r] : czero<V>());
+  }
+}
+
+// acc += t x (xs = (x.y, x.x), used by the packed FP32 form)
+template <typename T>
+WBG_D void pmac(typename C2<T>::t& acc, const typename PhaseEntry<T>::type& t, typename C2<T>::t x,
+                typename C2<T>::t xs) {
+  cfma(acc, t, x);
+}
+template <>
+WBG_D void pmac<float>(float2& acc, const float4& t, float2 x, float2 xs) {
+  acc = __ffma2_rn(make_float2(t.x, t.y), x, acc);
+  acc = __ffma2_rn(make_float2(t.z, t.w), xs, acc);
+}
+
 // One separable contraction: out[col][j] = sum_{i < len} tab[j][idx[i]] in[col][i]
-// for every output index j < Nj.  `in` values of this thread stay in registers.
+// for every output index j < Nj, JB outputs per pass (independent accumulators, the sum over
+// i in order): 4 for FP32, 1 for the 16-byte types, whose accumulators cost occupancy.
+// `in` values of this thread stay in registers.
 template <typename T, int MAXL>
-WBG_D void contract(const typename C2<T>::t* x, int len, const typename C2<T>::t* tab_s, const int* ridx, int nr,
+WBG_D void contract(const typename C2<T>::t* x, int len, const typename PhaseEntry<T>::type* tabT, const int* ridx,
                     int Nj, typename C2<T>::t* out, long long out_stride) {
   typedef typename C2<T>::t V;
-  for (int j = 0; j < Nj; ++j) {
-    V acc = czero<V>();
+  typedef typename PhaseEntry<T>::type E;
+  constexpr int JB = std::is_same<T, float>::value ? 4 : 1;
+  const int JP = pad4(Nj);
+  V xs[MAXL];
+#pragma unroll
+  for (int i = 0; i < MAXL; ++i) {
+    xs[i].x = x[i].y;
+    xs[i].y = x[i].x;
+  }
+  for (int j0 = 0; j0 < Nj; j0 += JB) {
+    V a[JB];
+#pragma unroll
+    for (int q = 0; q < JB; ++q) a[q] = czero<V>();
 #pragma unroll
     for (int i = 0; i < MAXL; ++i)
-      if (i < len) cfma(acc, tab_s[j * nr + ridx[i]], x[i]);
-    out[(long long)j * out_stride] = acc;
+      if (i < len) {
+        const E* t = tabT + ridx[i] * JP + j0;
+#pragma unroll
+        for (int q = 0; q < JB; ++q) pmac<T>(a[q], t[q], x[i], xs[i]);
+      }
+#pragma unroll
+    for (int q = 0; q < JB; ++q)
+      if (j0 + q < Nj) out[(long long)(j0 + q) * out_stride] = a[q];
   }
 }
 
@@ -112,10 +167,11 @@ __global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* 
                                                        typename C2<T>::t* __restrict__ Z, R2KGeom g, int nF,
                                                        const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smr[];
-  V* tab = reinterpret_cast<V*>(smr);  // [N2][nr2]
+  typedef typename PhaseEntry<T>::type E;
+  extern __shared__ __align__(16) unsigned char smr[];
+  E* tab = reinterpret_cast<E*>(smr);  // [nr2][pad4(N2)]
   const int p = blockIdx.y, blk = blockIdx.z;
-  for (int i = threadIdx.x; i < g.N2 * g.nr2; i += blockDim.x) tab[i] = ph2[(long long)blk * g.N2 * g.nr2 + i];
+  load_phases<T>(ph2 + (long long)blk * g.N2 * g.nr2, g.N2, g.nr2, tab);
   __syncthreads();
   int f, mn;
   if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
@@ -136,19 +192,31 @@ __global__ void __launch_bounds__(kThreads) r2k_stageA(const typename C2<T>::t* 
   }
   V* out = Z + ((((long long)blk * nF + f) * g.nP + p) * g.N2) * g.nw2 + mn;
   if (SPLIT) {  // sum_R tab (XF + XFlo): the residual products accumulate separately
-    for (int j = 0; j < g.N2; ++j) {
-      V acc = czero<V>(), accl = czero<V>();
+    V xs[MAXL], xls[MAXL];
+#pragma unroll
+    for (int i = 0; i < MAXL; ++i) {
+      xs[i].x = x[i].y;
+      xs[i].y = x[i].x;
+      xls[i].x = xl[SPLIT ? i : 0].y;
+      xls[i].y = xl[SPLIT ? i : 0].x;
+    }
+    const int JP = pad4(g.N2);
+    for (int j0 = 0; j0 < g.N2; j0 += 2) {
+      V a0 = czero<V>(), l0 = czero<V>(), a1 = czero<V>(), l1 = czero<V>();
 #pragma unroll
       for (int i = 0; i < MAXL; ++i)
         if (i < len) {
-          const V t = tab[j * g.nr2 + ri[i]];
-          cfma(acc, t, x[i]);
-          cfma(accl, t, xl[i]);
+          const E* t = tab + ri[i] * JP + j0;
+          pmac<T>(a0, t[0], x[i], xs[i]);
+          pmac<T>(l0, t[0], xl[SPLIT ? i : 0], xls[i]);
+          pmac<T>(a1, t[1], x[i], xs[i]);
+          pmac<T>(l1, t[1], xl[SPLIT ? i : 0], xls[i]);
         }
-      out[(long long)j * g.nw2] = cadd(acc, accl);
+      out[(long long)j0 * g.nw2] = cadd(a0, l0);
+      if (j0 + 1 < g.N2) out[(long long)(j0 + 1) * g.nw2] = cadd(a1, l1);
     }
   } else {
-    contract<T, MAXL>(x, len, tab, ri, g.nr2, g.N2, out, g.nw2);
+    contract<T, MAXL>(x, len, tab, ri, g.N2, out, g.nw2);
   }
 }
 
@@ -162,10 +230,11 @@ __global__ void __launch_bounds__(kThreads) r2k_stageB(const typename C2<T>::t* 
                                                        typename C2<T>::t* __restrict__ Y, R2KGeom g, int nF,
                                                        const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smr[];
-  V* tab = reinterpret_cast<V*>(smr);  // [N1][nr1]
+  typedef typename PhaseEntry<T>::type E;
+  extern __shared__ __align__(16) unsigned char smr[];
+  E* tab = reinterpret_cast<E*>(smr);  // [nr1][pad4(N1)]
   const int u = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
-  for (int i = threadIdx.x; i < g.N1 * g.nr1; i += blockDim.x) tab[i] = ph1[(long long)blk * g.N1 * g.nr1 + i];
+  load_phases<T>(ph1 + (long long)blk * g.N1 * g.nr1, g.N1, g.nr1, tab);
   __syncthreads();
   int f, mn;
   if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
@@ -183,7 +252,7 @@ __global__ void __launch_bounds__(kThreads) r2k_stageB(const typename C2<T>::t* 
     }
   }
   V* out = Y + (((((long long)blk * nF + f) * g.nU + u) * g.N1) * g.N2 + k2) * g.nw2 + mn;
-  contract<T, MAXL>(x, len, tab, ri, g.nr1, g.N1, out, (long long)g.N2 * g.nw2);
+  contract<T, MAXL>(x, len, tab, ri, g.N1, out, (long long)g.N2 * g.nw2);
 }
 
 // ---------------- stage C: contract R0 ----------------
@@ -195,10 +264,11 @@ __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* 
                                                        typename C2<T>::t* __restrict__ out, R2KGeom g, int nF,
                                                        const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
-  extern __shared__ unsigned char smr[];
-  V* tab = reinterpret_cast<V*>(smr);  // [N0][nr0]
+  typedef typename PhaseEntry<T>::type E;
+  extern __shared__ __align__(16) unsigned char smr[];
+  E* tab = reinterpret_cast<E*>(smr);  // [nr0][pad4(N0)]
   const int k1 = blockIdx.y / g.N2, k2 = blockIdx.y % g.N2, blk = blockIdx.z;
-  for (int i = threadIdx.x; i < g.N0 * g.nr0; i += blockDim.x) tab[i] = ph0[(long long)blk * g.N0 * g.nr0 + i];
+  load_phases<T>(ph0 + (long long)blk * g.N0 * g.nr0, g.N0, g.nr0, tab);
   __syncthreads();
   int f, mn;
   if (!decode_col(cols, ncols, nF, g.nw2, f, mn)) return;
@@ -217,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* 
   }
   const long long kstride = (long long)g.N1 * g.N2 * nF * g.nw2;  // k0 -> k0+1
   V* o = out + (((long long)blk * g.nk + (long long)k1 * g.N2 + k2) * nF + f) * g.nw2 + mn;
-  contract<T, MAXL>(x, len, tab, ri, g.nr0, g.N0, o, kstride);
+  contract<T, MAXL>(x, len, tab, ri, g.N0, o, kstride);
 }
 
 template <typename T, int MAXL>
@@ -225,16 +295,24 @@ void launch_stages(const void* XF, const void* XFlo, int nF, const int* pairStar
                    const int* pairR1, const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z,
                    void* Y, void* out, const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   typedef typename C2<T>::t V;
+  typedef typename PhaseEntry<T>::type E;
   const unsigned colBlocks = (unsigned)((ncols + kThreads - 1) / kThreads);
-  if (XFlo)
-    r2k_stageA<T, MAXL, true><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
+  const size_t smA = (size_t)pad4(g.N2) * g.nr2 * sizeof(E), smB = (size_t)pad4(g.N1) * g.nr1 * sizeof(E),
+               smC = (size_t)pad4(g.N0) * g.nr0 * sizeof(E);
+  if (XFlo) {
+    cudaFuncSetAttribute(r2k_stageA<T, MAXL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    r2k_stageA<T, MAXL, true><<<dim3(colBlocks, g.nP, nb), kThreads, smA, stream>>>(
         (const V*)XF, (const V*)XFlo, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
-  else
-    r2k_stageA<T, MAXL, false><<<dim3(colBlocks, g.nP, nb), kThreads, (size_t)g.N2 * g.nr2 * sizeof(V), stream>>>(
+  } else {
+    cudaFuncSetAttribute(r2k_stageA<T, MAXL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    r2k_stageA<T, MAXL, false><<<dim3(colBlocks, g.nP, nb), kThreads, smA, stream>>>(
         (const V*)XF, nullptr, pairStart, r2, (const V*)ph2, (V*)Z, g, nF, cols, ncols);
-  r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, (size_t)g.N1 * g.nr1 * sizeof(V), stream>>>(
+  }
+  cudaFuncSetAttribute(r2k_stageB<T, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, smB, stream>>>(
       (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF, cols, ncols);
-  r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, (size_t)g.N0 * g.nr0 * sizeof(V), stream>>>(
+  cudaFuncSetAttribute(r2k_stageC<T, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, smC, stream>>>(
       (const V*)Y, sliceR0, (const V*)ph0, (V*)out, g, nF, cols, ncols);
 }
 
@@ -246,6 +324,9 @@ int launch_r2k(const void* XF, const void* XFlo, int nF, const int* pairStart, c
   if (maxlen <= 8)
     launch_stages<T, 8>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
+  else if (maxlen <= 12)
+    launch_stages<T, 12>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+                          ncols, stream);
   else if (maxlen <= 16)
     launch_stages<T, 16>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
