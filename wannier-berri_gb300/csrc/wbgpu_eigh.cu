@@ -82,9 +82,6 @@ template <typename TU, typename CR> WBG_D typename C2<TU>::t to_tu_c(CR a) {
 // Outputs: d[k][i], e[k][i] (e[n-1] = 0) in the solver type R; Vh[k][c][i] (v of reflector
 // c, v_{c+1}=1, zeros for i<=c) and tau[k][c] rounded to the back-transform type TV.
 // ---------------------------------------------------------------------------------------
-#ifndef WBG_TRI_DIV
-#define WBG_TRI_DIV 2
-#endif
 WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
@@ -523,7 +520,9 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   R* d = (R*)w; w += (size_t)nk * n * 8;
   R* e = (R*)w;
   const int L = lanes_for(n);
-  const int LT = L >= 8 ? L / WBG_TRI_DIV : 4;  // tridiagonalisation lanes per matrix
+  // tridiagonalisation: mirrored row pairs on half the lanes (balanced rows; one row per lane
+  // on all 32 lanes measured 22% slower at nw = 32)
+  const int LT = L >= 8 ? L / 2 : 4;
   const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
   const int G = pick_group(smT, LT, 128 / LT);
   if (G == 0) return WBG_ERR_SIZE;
