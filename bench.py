@@ -15,8 +15,11 @@ The GPU arm prints one JSON line with value (device-resident throughput), e2e
 (public-API run() with pinned host->device upload of the R-space matrices and the
 result read back every step), the roofline of the dominant kernel measured live with
 CUDA events, the CPU baseline (the oracle on the host cores) and SM clocks sampled
-during the timed region.  --impl reference times the reference algorithm's CPU
-restatement (oracle) on all host cores with the same metric.
+during the timed region, plus three secondary measurements: "batched" and "served"
+(multi-system runs through the continuous-batching server) and "tetra" (the same AHC with
+the tetrahedron method over the whole grid in one run()).  --impl reference times the
+reference algorithm's CPU restatement (oracle) on all host cores with the same metric.
+--tetra-only [--nkfft N --tetra-nkdiv D] runs the tetrahedron measurement alone.
 """
 import argparse
 import json
@@ -392,9 +395,63 @@ def run_gpu(args):
                 line[key] = fn()
             except Exception as e:  # the headline line is still printed
                 line[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if world == 1 and not args.no_tetra:
+        try:
+            line["tetra"] = bench_tetra(s, dev, args.nkfft, NKDIV)
+        except Exception as e:
+            line["tetra"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+# ---------------------------------------------------------------------------------------
+# Tetrahedron method: AHC with tetra=True over the whole grid in one run()
+# ---------------------------------------------------------------------------------------
+def bench_tetra(s, dev, nkfft, nkdiv, err_blocks=8):
+    """AHC (1001 E_F) with tetra=True over the NKdiv^3 x NKFFT^3 grid through run(): k-points/s
+    of the whole run (corner energies included, timed with a device synchronisation on both
+    sides) against the same run() without tetra, stage times, and the mixed-vs-FP64 error of the
+    tetrahedron AHC on the first `err_blocks` blocks."""
+    import numpy as np
+    import torch
+    import wbgpu
+    from wbgpu import engine
+    from wbgpu.calculators import AHC
+    ef = np.linspace(-2, 2, NEF)
+    grid = wbgpu.Grid(s, NKdiv=nkdiv, NKFFT=nkfft)
+    nk = grid.nk_per_block * grid.nblocks
+    few = list(range(min(err_blocks, grid.nblocks)))
+    wbgpu.run(s, grid, {'a': AHC(Efermi=ef, tetra=True)}, precision='mixed', dev_system=dev, blocks=few)
+    out = {}
+    for key, tetra in (("tetra", True), ("plain", False)):
+        timer = engine.StageTimer()
+        torch.cuda.synchronize()
+        engine.set_timer(timer)
+        t0 = time.perf_counter()
+        wbgpu.run(s, grid, {'a': AHC(Efermi=ef, tetra=tetra)}, precision='mixed', dev_system=dev)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        engine.set_timer(None)
+        out[key] = (nk / dt, {k: round(v, 2) for k, v in timer.totals_ms().items()})
+    a = wbgpu.run(s, grid, {'a': AHC(Efermi=ef, tetra=True)}, precision='mixed', dev_system=dev, blocks=few)['a'].data
+    b = wbgpu.run(s, grid, {'a': AHC(Efermi=ef, tetra=True)}, precision='fp64', dev_system=dev, blocks=few)['a'].data
+    return {"workload": f"AHC tetra=True, {NEF} E_F, {nkdiv * nkfft}^3 grid in {nkfft}^3 blocks, one run(), mixed",
+            "kpoints": nk, "kpoints_per_s": out["tetra"][0], "stage_ms": out["tetra"][1],
+            "without_tetra_kpoints_per_s": out["plain"][0],
+            "max_rel_err_vs_fp64": float(np.max(np.abs(a - b)) / np.max(np.abs(b))),
+            "err_sample": f"first {len(few)} blocks"}
+
+
+def run_tetra_only(args):
+    """--tetra-only: the tetrahedron measurement alone (profiling captures of its kernels)."""
+    import torch
+    from wbgpu import engine, _lib
+    s = build_system(device='cuda')
+    _lib.load()
+    torch.cuda.init()
+    print(json.dumps({"tetra": bench_tetra(s, engine.DeviceSystem(s), args.nkfft, args.tetra_nkdiv)}), flush=True)
     return 0
 
 
@@ -510,9 +567,14 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-fp64-compare', action='store_true')
     ap.add_argument('--no-serve', action='store_true', help='skip the batched and served measurements')
+    ap.add_argument('--no-tetra', action='store_true', help='skip the tetrahedron-method measurement')
+    ap.add_argument('--tetra-only', action='store_true', help='run only the tetrahedron-method measurement')
+    ap.add_argument('--tetra-nkdiv', type=int, default=NKDIV, help='NKdiv of --tetra-only')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.tetra_only:
+        return run_tetra_only(args)
     return run_gpu(args)
 
 
