@@ -17,7 +17,8 @@ result read back every step), the roofline of the dominant kernel measured live 
 CUDA events, the CPU baseline (the oracle on the host cores) and SM clocks sampled
 during the timed region, plus three secondary measurements: "batched" and "served"
 (multi-system runs through the continuous-batching server) and "tetra" (the same AHC with
-the tetrahedron method over the whole grid in one run()).  --impl reference times the
+the tetrahedron method over the whole grid in one run()), and "configs" (the cubic nw=8 and
+spinor nw=96 models through run(), with the oracle on one core beside them).  --impl reference times the
 reference algorithm's CPU restatement (oracle) on all host cores with the same metric.
 --tetra-only [--nkfft N --tetra-nkdiv D] runs the tetrahedron measurement alone.
 """
@@ -395,6 +396,11 @@ def run_gpu(args):
                 line[key] = fn()
             except Exception as e:  # the headline line is still printed
                 line[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if world == 1 and not args.no_configs:
+        try:
+            line["configs"] = bench_configs()
+        except Exception as e:
+            line["configs"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if world == 1 and not args.no_tetra:
         try:
             line["tetra"] = bench_tetra(s, dev, args.nkfft, NKDIV)
@@ -453,6 +459,75 @@ def run_tetra_only(args):
     torch.cuda.init()
     print(json.dumps({"tetra": bench_tetra(s, engine.DeviceSystem(s), args.nkfft, args.tetra_nkdiv)}), flush=True)
     return 0
+
+
+# ---------------------------------------------------------------------------------------
+# The other single-system configurations: cubic nw=8 (AHC) and spinor nw=96 (Kubo + AHC)
+# ---------------------------------------------------------------------------------------
+def _timed_run(s, grid, mk, precision, dev, blocks=None):
+    import torch
+    import wbgpu
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = wbgpu.run(s, grid, mk(), precision=precision, dev_system=dev, blocks=blocks)
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def _oracle_rate(s, nkfft, calcs):
+    """k-points/s of the oracle on one block of `s` (one host process, one BLAS thread)."""
+    from oracle import wb_oracle as O
+    o = O.RSystem(s.real_lattice, s.iRvec, s.wannier_centers_cart, s._XX_R)
+    data = O.DataK(o, nkfft, np.array([0.31, 0.17, 0.53]) / np.array(nkfft))
+    t0 = time.perf_counter()
+    for c in calcs.values():
+        c(data)
+    return int(np.prod(nkfft)) / (time.perf_counter() - t0)
+
+
+def bench_configs():
+    """run() throughput of the cubic nw = 8 model (AHC at 501 E_F, the whole 48^3 grid in 8^3
+    blocks) and of the spinor nw = 96 model with SOC (R in [-5,5]^3; OpticalConductivity at 11
+    E_F x 400 frequencies, Lorentzian 0.05 eV, + AHC; 2 of the 216 16^3 blocks of its 96^3
+    grid), mixed precision, with the error against the FP64 path on the same blocks and the oracle
+    on one host core (a small block of the same model) beside it."""
+    import wbgpu
+    from wbgpu import engine, models, System_R
+    from wbgpu.calculators import AHC, OpticalConductivity
+    from oracle import wb_oracle as O
+    out = {}
+    ef1 = np.linspace(-2, 2, 501)
+    s1 = System_R.from_dict(models.config_system(1))
+    g1 = wbgpu.Grid(s1, NKdiv=6, NKFFT=8)
+    d1 = engine.DeviceSystem(s1)
+    mk1 = lambda: {'ahc': AHC(Efermi=ef1)}
+    _timed_run(s1, g1, mk1, 'mixed', d1, blocks=[0])
+    r, dt = _timed_run(s1, g1, mk1, 'mixed', d1)
+    r64, dt64 = _timed_run(s1, g1, mk1, 'fp64', d1)
+    a, b = r['ahc'].data, r64['ahc'].data
+    out["c1"] = {"workload": "cubic nw=8, R in [-2,2]^3, AHC at 501 E_F, 48^3 k in 8^3 blocks, one run()",
+                 "kpoints_per_s": 48 ** 3 / dt, "fp64_kpoints_per_s": 48 ** 3 / dt64,
+                 "max_rel_err_vs_fp64": float(np.max(np.abs(a - b)) / np.max(np.abs(b))),
+                 "cpu_kpoints_per_s_per_core": _oracle_rate(s1, (8, 8, 8), {'ahc': O.AHC(Efermi=ef1)}),
+                 "cpu_sample": "oracle, one 8^3 block, one process"}
+    ef3, om = np.linspace(-1, 1, 11), np.linspace(0, 4, 400)
+    s3 = System_R.from_dict(models.config_system(3))
+    g3 = wbgpu.Grid(s3, NKdiv=6, NKFFT=16)
+    d3 = engine.DeviceSystem(s3)
+    mk3 = lambda: {'opt': OpticalConductivity(Efermi=ef3, omega=om, smr_fixed_width=0.05), 'ahc': AHC(Efermi=ef3)}
+    _timed_run(s3, g3, mk3, 'mixed', d3, blocks=[5])
+    blocks = [0, 1]
+    r, dt = _timed_run(s3, g3, mk3, 'mixed', d3, blocks=blocks)
+    r64, dt64 = _timed_run(s3, g3, mk3, 'fp64', d3, blocks=blocks)
+    err = {k: float(np.max(np.abs(r[k].data - r64[k].data)) / np.max(np.abs(r64[k].data))) for k in ('opt', 'ahc')}
+    nk3 = len(blocks) * 16 ** 3
+    ocs = {'opt': O.OpticalConductivity(Efermi=ef3, omega=om, smr_fixed_width=0.05), 'ahc': O.AHC(Efermi=ef3)}
+    out["c3"] = {"workload": "spinor nw=96 with SOC, R in [-5,5]^3, OpticalConductivity 11 E_F x 400 omega "
+                             "(Lorentzian 0.05 eV) + AHC, 2 blocks of 16^3 of the 96^3 grid, one run()",
+                 "kpoints_per_s": nk3 / dt, "fp64_kpoints_per_s": nk3 / dt64, "max_rel_err_vs_fp64": err,
+                 "cpu_kpoints_per_s_per_core": _oracle_rate(s3, (2, 2, 1), ocs),
+                 "cpu_sample": "oracle, one 2x2x1 block, one process"}
+    return out
 
 
 # ---------------------------------------------------------------------------------------
@@ -568,6 +643,8 @@ def main():
     ap.add_argument('--no-fp64-compare', action='store_true')
     ap.add_argument('--no-serve', action='store_true', help='skip the batched and served measurements')
     ap.add_argument('--no-tetra', action='store_true', help='skip the tetrahedron-method measurement')
+    ap.add_argument('--no-configs', action='store_true', help='skip the nw=8 and nw=96 configurations')
+    ap.add_argument('--configs-only', action='store_true', help='run only the nw=8 and nw=96 configurations')
     ap.add_argument('--tetra-only', action='store_true', help='run only the tetrahedron-method measurement')
     ap.add_argument('--tetra-nkdiv', type=int, default=NKDIV, help='NKdiv of --tetra-only')
     args = ap.parse_args()
@@ -575,6 +652,13 @@ def main():
         return run_reference(args)
     if args.tetra_only:
         return run_tetra_only(args)
+    if args.configs_only:
+        import torch
+        from wbgpu import _lib
+        _lib.load()
+        torch.cuda.init()
+        print(json.dumps({"configs": bench_configs()}), flush=True)
+        return 0
     return run_gpu(args)
 
 
