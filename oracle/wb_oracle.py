@@ -958,6 +958,58 @@ def block_shifts(NKdiv, NKFFT):
     return K / np.array(NKFFT)[None, :]
 
 
+def result_max(res):
+    """EnergyResult.max (result/energyresult.py:250-264) without smoothers: max |data|, its
+    2-norm and the 2-norm of its difference along the first energy axis."""
+    d = res.data
+    return np.array([np.abs(d).max(), np.linalg.norm(d), np.linalg.norm(d[1:] - d[:-1])])
+
+
+def run_adaptive(system, NKdiv, NKFFT, calculators, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1, periodic=(1, 1, 1)):
+    """run() with adaptive refinement, without symmetry (run_grid.py:290-403, Kpoint.divide at
+    grid/Kpoint.py:145-175): every iteration evaluates the new K-points, then the adpt_fac
+    K-points with the largest max(result) x factor per entry of ResultDict.max are divided into
+    adpt_mesh sub-points (factor / prod(mesh), the parent's factor set to 0).  Returns the summed
+    results {key: EnergyResult} and the final K-list (K, dK, factor)."""
+    NKdiv, NKFFT = np.array(NKdiv) * np.ones(3, int), np.array(NKFFT) * np.ones(3, int)
+    if adpt_num_iter < 0:
+        adpt_num_iter = -adpt_num_iter * np.prod(NKdiv) / np.prod(adpt_mesh) / adpt_fac / 3
+    adpt_num_iter = int(round(adpt_num_iter))
+    mesh = np.array(adpt_mesh) * np.ones(3, int)
+    if mesh.max() <= 1:
+        adpt_num_iter = 0
+    K = list(iterate_nd(NKdiv) / NKdiv[None, :])
+    dK = [1. / NKdiv for _ in K]
+    fac = [1. / np.prod(NKdiv) for _ in K]
+    res = []
+    for it in range(adpt_num_iter + 1):
+        for i in range(len(res), len(K)):
+            data = DataK(system, NKFFT, K[i] / NKFFT, dk_cell=dK[i] / NKFFT)
+            res.append({key: c(data) for key, c in calculators.items()})
+        if it >= adpt_num_iter:
+            break
+        Kmax = np.array([np.concatenate([result_max(r[key]) for key in calculators]) * f
+                         for r, f in zip(res, fac)]).T
+        select = set().union(*(np.argsort(km)[-adpt_fac:] for km in Kmax))
+        for iK in select:
+            nd = mesh.copy()
+            nd[np.logical_not(np.array(periodic, dtype=bool))] = 1
+            dka = dK[iK] / nd
+            shift = (-dK[iK] + dka) / 2.
+            for x in range(nd[0]):
+                for y in range(nd[1]):
+                    for z in range(nd[2]):
+                        K.append(K[iK] + shift + dka * np.array([x, y, z]))
+                        dK.append(dka)
+                        fac.append(fac[iK] / np.prod(nd))
+            fac[iK] = 0.
+    total = {}
+    for r, f in zip(res, fac):
+        for key in calculators:
+            total[key] = r[key] * f if key not in total else total[key] + r[key] * f
+    return total, (np.array(K), np.array(dK), np.array(fac))
+
+
 def run(system, NKdiv, NKFFT, calculators, blocks=None):
     """Serial run() over the FFT blocks without symmetry or refinement: sum of
     block results times factor 1/prod(NKdiv) (run_grid.py:59-66, grid/grid.py:152)."""

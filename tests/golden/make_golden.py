@@ -32,6 +32,10 @@ Fixtures written (all small, complex128/float64):
   ``run`` on the random system (NKdiv 2, NKFFT 3, 21 Fermi levels) and AHC / DOS /
   Ohmic_FermiSea on the triclinic MDRS model over an anisotropic grid (NKdiv (2,1,3),
   NKFFT (3,4,2)).  ``python make_golden.py <reference root> tetra`` writes only this file.
+* ``refine_ref.npz`` -- adaptive refinement (``adpt_num_iter``) of the reference's ``run``
+  without symmetry: the random system (3 iterations, AHC / DOS / CumDOS) and the triclinic
+  MDRS model (2 iterations, adpt_fac 2, adpt_mesh (2,1,3), AHC / BerryDipole_FermiSea).
+  ``python make_golden.py <reference root> refine`` writes only this file.
 """
 import os
 import sys
@@ -181,6 +185,7 @@ def main(ref_root):
         ev[f'fe_{q}'] = r[q]
     np.savez_compressed(os.path.join(HERE, 'evaluate_k_ref.npz'), **ev)
     tetra_fixtures(wb, rs)
+    refine_fixtures(wb, rs)
     print("wrote fixtures to", HERE)
 
 
@@ -215,11 +220,48 @@ def tetra_fixtures(wb, rs):
     np.savez_compressed(os.path.join(HERE, 'tetra_ref.npz'), **out)
 
 
+def run_ref_adaptive(wb, system, NKdiv, NKFFT, calculators, **adpt):
+    from wannierberri.grid import Grid
+    tmp = tempfile.mkdtemp(prefix='wbrun_')
+    grid = Grid(system=system, NKdiv=NKdiv, NKFFT=NKFFT, use_symmetry=False)
+    res = wb.run(system, grid=grid, calculators=calculators, parallel=False, use_irred_kpt=False,
+                 symmetrize=False, fout_name=os.path.join(tmp, 'r'), file_Klist_path=os.path.join(tmp, 'k'),
+                 print_progress_step_time=1e9, **adpt)
+    return {k: res.results[k].data for k in calculators}
+
+
+def refine_fixtures(wb, rs):
+    """---- 6. adaptive refinement (run_grid.py:290-403, grid/Kpoint.py:145-175) without
+    symmetry: the random system over NKdiv 2 x NKFFT 3 with 3 refinement iterations (AHC, DOS,
+    CumDOS; the K-points of largest max(result) x factor divided into 2^3), and the triclinic
+    MDRS model with adpt_fac 2 and an anisotropic adpt_mesh (2, 1, 3)."""
+    from wannierberri import calculators as calc
+    from wbgpu import models
+    out = {}
+    EF = np.linspace(-2, 2, 21)
+    out['EF'] = EF
+    cs = {'ahc': calc.static.AHC(Efermi=EF), 'dos': calc.static.DOS(Efermi=EF),
+          'cumdos': calc.static.CumDOS(Efermi=EF)}
+    for k, v in run_ref_adaptive(wb, rs, 2, 3, cs, adpt_num_iter=3, adpt_mesh=2, adpt_fac=1).items():
+        out['random_' + k] = v
+    s2 = ref_system_from_arrays(wb, models.config_system(2, small=True))
+    s2.do_ws_dist(mp_grid=3)
+    EF2 = np.linspace(-1.5, 1.5, 31)
+    out['EF2'] = EF2
+    cs = {'ahc': calc.static.AHC(Efermi=EF2), 'bcd': calc.static.BerryDipole_FermiSea(Efermi=EF2)}
+    for k, v in run_ref_adaptive(wb, s2, 2, [3, 4, 2], cs, adpt_num_iter=2, adpt_mesh=[2, 1, 3],
+                                 adpt_fac=2).items():
+        out['c2_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'refine_ref.npz'), **out)
+
+
 if __name__ == '__main__':
     root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    if len(sys.argv) > 2 and sys.argv[2] == 'tetra':  # only section 5
+    section = sys.argv[2] if len(sys.argv) > 2 else None
+    if section in ('tetra', 'refine'):  # one section only
         wb = setup_reference(root)
         from wannierberri.system.system_R import System_R
-        tetra_fixtures(wb, System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True))
+        rs = System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True)
+        (tetra_fixtures if section == 'tetra' else refine_fixtures)(wb, rs)
     else:
         main(root)

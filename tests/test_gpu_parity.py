@@ -628,3 +628,41 @@ def test_tetra_served_equals_run(c2small):
     t2.wait()
     for key in ('ahc', 'dos'):
         assert maxrel(r1[key].data, alone[key].data) < 1e-9, key
+
+
+# ---------------------------------------------------------------------------------------
+# adaptive refinement (adpt_num_iter)
+# ---------------------------------------------------------------------------------------
+def test_refine_golden_random(golden_dir):
+    """run(adpt_num_iter=3) against the reference's refinement on its random system (FP64, the
+    1e-8 rule); the mixed path selects the same K-points and agrees to 1e-5."""
+    import os
+    from wbgpu.run import run_adaptive
+    rs = _golden_system(golden_dir, 'random_system.npz')
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    C = wbgpu.calculators
+    mk = lambda: {'ahc': C.AHC(Efermi=g['EF']), 'dos': C.DOS(Efermi=g['EF']), 'cumdos': C.CumDOS(Efermi=g['EF'])}
+    grid = wbgpu.Grid(rs, NKdiv=2, NKFFT=3)
+    res = wbgpu.run(rs, grid, mk(), precision='fp64', adpt_num_iter=3, adpt_mesh=2)
+    for key in ('ahc', 'dos', 'cumdos'):
+        exp = g['random_' + key]
+        assert np.abs(res[key].data - exp).max() < 1e-8 * np.abs(exp).max(), key
+    dev = engine.DeviceSystem(rs)
+    r64, K64, _, f64 = run_adaptive(rs, grid, mk(), 'fp64', dev, 3)
+    rm, Km, _, fm = run_adaptive(rs, grid, mk(), 'mixed', dev, 3)
+    assert np.array_equal(K64, Km) and np.array_equal(f64, fm)
+    for key in ('ahc', 'dos', 'cumdos'):
+        assert np.abs(rm[key].data - r64[key].data).max() < 1e-5 * np.abs(r64[key].data).max(), key
+
+
+def test_refine_golden_c2_anisotropic(golden_dir, c2small):
+    """Triclinic MDRS model: adpt_fac 2, adpt_mesh (2, 1, 3), AHC and Berry-curvature dipole."""
+    import os
+    s, _ = c2small
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    C = wbgpu.calculators
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=(3, 4, 2)),
+                    {'ahc': C.AHC(Efermi=g['EF2']), 'bcd': C.BerryDipole_FermiSea(Efermi=g['EF2'])},
+                    precision='fp64', adpt_num_iter=2, adpt_mesh=(2, 1, 3), adpt_fac=2)
+    for key in ('ahc', 'bcd'):
+        assert maxrel(res[key].data, g['c2_' + key]) < 1e-9, key

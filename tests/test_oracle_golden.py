@@ -217,3 +217,27 @@ def test_tetra_c2_anisotropic_golden(golden_dir):
     r = O.run(s2, (2, 1, 3), (3, 4, 2), tetra_oracle_calculators(g['EF2'], names))
     for k in names:
         assert maxrel(r[k].data, g['c2_' + k]) < 1e-9, k
+
+
+def test_refine_random_golden(random_sys, golden_dir):
+    """Adaptive refinement (run_grid.py:290-403 without symmetry) against the reference's run on
+    its random system: 3 iterations, the largest K-point per ResultDict.max entry divided into 2^3."""
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    EF = g['EF']
+    calcs = {'ahc': O.AHC(Efermi=EF), 'dos': O.DOS(Efermi=EF), 'cumdos': O.CumDOS(Efermi=EF)}
+    r, (K, dK, fac) = O.run_adaptive(random_sys, (2, 2, 2), (3, 3, 3), calcs, adpt_num_iter=3, adpt_mesh=2)
+    assert abs(fac.sum() - 1.0) < 1e-12 and len(K) > 8
+    for k in calcs:
+        ref = g['random_' + k]
+        assert np.max(np.abs(r[k].data - ref)) < 1e-8 * np.max(np.abs(ref)), k
+
+
+def test_refine_c2_anisotropic_golden(golden_dir):
+    """Triclinic MDRS model, adpt_fac 2, adpt_mesh (2, 1, 3) over NKdiv 2 x NKFFT (3, 4, 2)."""
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    s2 = O.do_ws_dist(rsys(models.config_system(2, small=True)), mp_grid=(3, 3, 3))
+    EF = g['EF2']
+    calcs = {'ahc': O.AHC(Efermi=EF), 'bcd': O.BerryDipole_FermiSea(Efermi=EF)}
+    r, _ = O.run_adaptive(s2, (2, 2, 2), (3, 4, 2), calcs, adpt_num_iter=2, adpt_mesh=(2, 1, 3), adpt_fac=2)
+    for k in calcs:
+        assert maxrel(r[k].data, g['c2_' + k]) < 1e-9, k

@@ -377,6 +377,15 @@ class BandData:
     def nk_total(self):
         return self.nblocks * self.nk
 
+    def block(self, b):
+        """View of block b alone (per-block results, e.g. for adaptive refinement)."""
+        sl = slice(b * self.nk, (b + 1) * self.nk)
+        sub = BandData(self.E[sl], None if self.U is None else self.U[sl], None if self.Xbar is None else self.Xbar[sl],
+                       self.index, 1, self.nk, self.nw, self.fp64_fields, hermitian=self.hermitian)
+        sub._flag = getattr(self, '_flag', None)
+        sub._keep = getattr(self, '_keep', None)
+        return sub
+
 
 def r2k_geometry(dev, NKFFT):
     g = dev.geom

@@ -46,6 +46,14 @@ class EnergyResult:
     def add(self, other):
         self.data = self.data + other.data
 
+    @property
+    def max(self):
+        """EnergyResult.max (result/energyresult.py:250-264, no smoothers): max |data|, its 2-norm
+        and the 2-norm of its difference along the first energy axis -- the numbers by which
+        adaptive refinement ranks K-points."""
+        d = self.data
+        return np.array([np.abs(d).max(), np.linalg.norm(d), np.linalg.norm(d[1:] - d[:-1])])
+
     def savedata(self, name, prefix="", suffix="", i_iter=0):
         """Binary output like EnergyResult.save (npz with data and energy axes)."""
         fn = f"{prefix}-{name}{('-' + suffix) if suffix else ''}_iter-{i_iter:04d}.npz"
@@ -59,3 +67,8 @@ class ResultDict(dict):
     @property
     def results(self):
         return self
+
+    @property
+    def max(self):
+        """ResultDict.max (result/resultdict.py:62-63): the max entries of every result in order."""
+        return np.array([x for v in self.values() for x in v.max])
