@@ -580,12 +580,16 @@ def bench_batched(nsys=32):
 
 def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
     """Poisson arrivals (mean `rate` per s) of AHC requests over `nsys` resident systems
-    (num_wann 8-128), grids 8^3-32^3: p50 / p99 latency from submit to result and throughput,
-    against the plain FP64 run() of the first `nbase` requests one after the other."""
+    (num_wann 8-128), grids 8^3-32^3, each with 0-3 rounds of adaptive refinement (the
+    reference's policy: the largest K-point divided into 2^3 blocks per round): p50 / p99 latency
+    from submit to result and throughput, against the plain FP64 run() of the first `nbase`
+    requests (same refinement) one after the other."""
     import numpy as np
     import torch
     import wbgpu
+    from wbgpu import engine
     from wbgpu.calculators import AHC
+    from wbgpu.run import run_adaptive
     ef = np.linspace(-1, 1, 201)
     systems = tb_pool(nsys, 5000, 8, 128)
     rng = np.random.default_rng(5001)
@@ -593,14 +597,14 @@ def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
     for i in range(nreq):
         s = int(rng.integers(nsys))
         nkfft, nkdiv = int(rng.choice([8, 16])), int(rng.choice([1, 2]))
-        reqs.append((s, nkdiv, nkfft))
+        reqs.append((s, nkdiv, nkfft, int(rng.integers(0, 4))))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     grids = {}
-    grid_of = lambda r: grids.setdefault(r, wbgpu.Grid(systems[r[0]], NKdiv=r[1], NKFFT=r[2]))
+    grid_of = lambda r: grids.setdefault(r[:3], wbgpu.Grid(systems[r[0]], NKdiv=r[1], NKFFT=r[2]))
     srv = wbgpu.Server(precision='mixed', max_active=8)
     for i, s in enumerate(systems):
         srv.add_system(i, s)
-    for r in set(reqs):  # warm the per-(system, grid) caches: R-space fields, phase tables
+    for r in set(q[:3] for q in reqs):  # warm the per-(system, grid) caches: R-space fields, phase tables
         srv.submit(r[0], grid_of(r), {'ahc': AHC(Efermi=ef)})
     srv.run_until_idle()
     torch.cuda.synchronize()
@@ -608,23 +612,30 @@ def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
     tickets = []
     with srv:
         t0 = time.perf_counter()
-        for (s, nkdiv, nkfft), ta in zip(reqs, arrivals):
+        for (s, nkdiv, nkfft, nit), ta in zip(reqs, arrivals):
             dt = t0 + ta - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            tickets.append(srv.submit(s, grid_of((s, nkdiv, nkfft)), {'ahc': AHC(Efermi=ef)}))
+            tickets.append(srv.submit(s, grid_of((s, nkdiv, nkfft)), {'ahc': AHC(Efermi=ef)}, adpt_num_iter=nit))
         for t in tickets:
             t.wait(600)
     st = srv.stats(tickets)
+    devs = {}
     t0 = time.perf_counter()
     nkb = 0
-    for s, nkdiv, nkfft in reqs[:nbase]:
+    for s, nkdiv, nkfft, nit in reqs[:nbase]:
         g = grid_of((s, nkdiv, nkfft))
-        wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision='fp64')
-        nkb += g.nk_per_block * g.nblocks
+        dev = devs.setdefault(s, engine.DeviceSystem(systems[s]))
+        if nit:
+            K = run_adaptive(systems[s], g, {'ahc': AHC(Efermi=ef)}, 'fp64', dev, nit)[1]
+            nkb += g.nk_per_block * len(K)
+        else:
+            wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision='fp64', dev_system=dev)
+            nkb += g.nk_per_block * g.nblocks
     torch.cuda.synchronize()
     st.update({"workload": f"{nreq} AHC requests, Poisson arrivals at {rate:g}/s over {nsys} resident systems "
-                           "(num_wann log-uniform 8-128, seeded), grids 8^3-32^3, 201 E_F, mixed precision",
+                           "(num_wann log-uniform 8-128, seeded), grids 8^3-32^3, 0-3 refinement rounds each "
+                           "(reference policy), 201 E_F, mixed precision",
                "offered_rate_per_s": rate, "plain_fp64_serial_kpoints_per_s": nkb / (time.perf_counter() - t0),
                "plain_fp64_serial_sample": f"first {nbase} requests run one after the other"})
     return st

@@ -666,3 +666,24 @@ def test_refine_golden_c2_anisotropic(golden_dir, c2small):
                     precision='fp64', adpt_num_iter=2, adpt_mesh=(2, 1, 3), adpt_fac=2)
     for key in ('ahc', 'bcd'):
         assert maxrel(res[key].data, g['c2_' + key]) < 1e-9, key
+
+
+def test_refine_served_equals_run(c2small):
+    """A request with refinement rounds through the Server (next to a plain request) gives run()'s
+    adaptive result."""
+    s, _ = c2small
+    EF = np.linspace(-1.5, 1.5, 31)
+    C = wbgpu.calculators
+    grid = wbgpu.Grid(s, NKdiv=2, NKFFT=3)
+    alone = wbgpu.run(s, grid, {'ahc': C.AHC(Efermi=EF)}, precision='mixed', adpt_num_iter=2, adpt_fac=2)
+    srv = wbgpu.Server(precision='mixed')
+    srv.add_system('c2', s)
+    t1 = srv.submit('c2', grid, {'ahc': C.AHC(Efermi=EF)}, adpt_num_iter=2, adpt_fac=2)
+    t2 = srv.submit('c2', grid, {'dos': C.DOS(Efermi=EF)})
+    srv.run_until_idle()
+    r1 = t1.wait()
+    t2.wait()
+    assert maxrel(r1['ahc'].data, alone['ahc'].data) < 1e-9
+    from wbgpu.run import run_adaptive
+    _, K, _, _ = run_adaptive(s, grid, {'ahc': C.AHC(Efermi=EF)}, 'mixed', engine.DeviceSystem(s), 2, 2, 2)
+    assert t1.nkpoints == len(K) * 27 and len(K) > 8  # every K-point of every round, 3^3 k each

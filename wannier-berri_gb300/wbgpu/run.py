@@ -50,50 +50,76 @@ def block_results(dev, system, shifts, NKFFT, calculators, precision, dk_cell=No
     return out
 
 
-def run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_mesh=2, adpt_fac=1):
-    """run() with adaptive refinement, without symmetry (run_grid.py:290-403; Kpoint.divide at
-    grid/Kpoint.py:145-175): each iteration evaluates the new K-points (blocks), ranks all
-    K-points by max(result) x factor per entry of ResultDict.max, divides the adpt_fac largest
-    of each entry into prod(adpt_mesh) sub-blocks with factor / prod(adpt_mesh) (along periodic
-    directions only) and sets the parent's factor to 0.  Returns (ResultDict, K, dK, factor)."""
-    div, fft = np.array(grid.div, dtype=int), np.array(grid.FFT, dtype=int)
-    if adpt_num_iter < 0:
-        adpt_num_iter = -adpt_num_iter * np.prod(div) / np.prod(adpt_mesh) / adpt_fac / 3
-    adpt_num_iter = int(round(adpt_num_iter))
-    mesh = np.array(adpt_mesh, dtype=int) * np.ones(3, dtype=int)
-    if mesh.max() <= 1:
-        adpt_num_iter = 0
-    templates = {k: copy.deepcopy(c) for k, c in calculators.items()}
-    idx = np.stack(np.meshgrid(*[np.arange(n) for n in div], indexing='ij'), axis=-1).reshape(-1, 3)
-    K = list(idx / div[None, :])
-    dK = [1.0 / div for _ in K]
-    fac = [1.0 / np.prod(div) for _ in K]
-    res = []
-    periodic = np.array(getattr(system, 'periodic', (True, True, True)), dtype=bool)
-    for it in range(adpt_num_iter + 1):
-        new = np.array(K[len(res):])
-        res += block_results(dev, system, new / fft[None, :], fft, templates, precision)
-        if it >= adpt_num_iter:
-            break
-        Kmax = np.array([np.concatenate([r[key].max for key in templates]) * f for r, f in zip(res, fac)]).T
-        select = set().union(*(np.argsort(km)[-adpt_fac:] for km in Kmax))
+class Refinement:
+    """The reference's adaptive refinement without symmetry (run_grid.py:290-403; Kpoint.divide at
+    grid/Kpoint.py:145-175) on a K-point list: after each round of evaluations all K-points are
+    ranked by max(result) x factor per entry of ResultDict.max, the adpt_fac largest of each entry
+    are divided into prod(adpt_mesh) sub-blocks (periodic directions only) with factor /
+    prod(adpt_mesh), and the parent's factor is set to 0."""
+
+    def __init__(self, system, grid, calculators, adpt_num_iter, adpt_mesh=2, adpt_fac=1):
+        self.div, self.fft = np.array(grid.div, dtype=int), np.array(grid.FFT, dtype=int)
+        if adpt_num_iter < 0:
+            adpt_num_iter = -adpt_num_iter * np.prod(self.div) / np.prod(adpt_mesh) / adpt_fac / 3
+        self.num_iter = int(round(adpt_num_iter))
+        self.mesh = np.array(adpt_mesh, dtype=int) * np.ones(3, dtype=int)
+        if self.mesh.max() <= 1:
+            self.num_iter = 0
+        self.fac_top = int(adpt_fac)
+        self.periodic = np.array(getattr(system, 'periodic', (True, True, True)), dtype=bool)
+        self.templates = {k: copy.deepcopy(c) for k, c in calculators.items()}
+        idx = np.stack(np.meshgrid(*[np.arange(n) for n in self.div], indexing='ij'), axis=-1).reshape(-1, 3)
+        self.K = list(idx / self.div[None, :])
+        self.dK = [1.0 / self.div for _ in self.K]
+        self.fac = [1.0 / np.prod(self.div) for _ in self.K]
+        self.results = []
+        self.it = 0
+
+    def new_shifts(self):
+        """Block shifts dK = K / NKFFT of the K-points not evaluated yet."""
+        return np.array(self.K[len(self.results):]) / self.fft[None, :]
+
+    def add(self, results):
+        self.results += list(results)
+
+    def refine(self):
+        """Divide the selected K-points; False when the last iteration has been evaluated."""
+        if self.it >= self.num_iter:
+            return False
+        self.it += 1
+        Kmax = np.array([np.concatenate([r[key].max for key in self.templates]) * f
+                         for r, f in zip(self.results, self.fac)]).T
+        select = set().union(*(np.argsort(km)[-self.fac_top:] for km in Kmax))
         for iK in select:
-            nd = mesh.copy()
-            nd[~periodic] = 1
-            dka = dK[iK] / nd
-            shift = (-dK[iK] + dka) / 2.0
+            nd = self.mesh.copy()
+            nd[~self.periodic] = 1
+            dka = self.dK[iK] / nd
+            shift = (-self.dK[iK] + dka) / 2.0
             for x in range(nd[0]):
                 for y in range(nd[1]):
                     for z in range(nd[2]):
-                        K.append(K[iK] + shift + dka * np.array([x, y, z]))
-                        dK.append(dka)
-                        fac.append(fac[iK] / np.prod(nd))
-            fac[iK] = 0.0
-    total = {}
-    for r, f in zip(res, fac):
-        for key in templates:
-            total[key] = r[key] * f if key not in total else total[key] + r[key] * f
-    return ResultDict(total), np.array(K), np.array(dK), np.array(fac)
+                        self.K.append(self.K[iK] + shift + dka * np.array([x, y, z]))
+                        self.dK.append(dka)
+                        self.fac.append(self.fac[iK] / np.prod(nd))
+            self.fac[iK] = 0.0
+        return True
+
+    def total(self):
+        out = {}
+        for r, f in zip(self.results, self.fac):
+            for key in self.templates:
+                out[key] = r[key] * f if key not in out else out[key] + r[key] * f
+        return ResultDict(out)
+
+
+def run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_mesh=2, adpt_fac=1):
+    """run() with adaptive refinement (Refinement): returns (ResultDict, K, dK, factor)."""
+    ref = Refinement(system, grid, calculators, adpt_num_iter, adpt_mesh, adpt_fac)
+    while True:
+        ref.add(block_results(dev, system, ref.new_shifts(), ref.fft, ref.templates, precision))
+        if not ref.refine():
+            break
+    return ref.total(), np.array(ref.K), np.array(ref.dK), np.array(ref.fac)
 
 
 def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, device='cuda', dev_system=None,

@@ -15,9 +15,13 @@ one GPU and runs many integration requests at once:
   through an event on its stream (no device-wide synchronisation).
 * Results are the same ``ResultDict`` as ``run()`` with the same block weighting; ``stats()``
   reports p50 / p99 latency (submit to result) and k-points per second.
+* A request with ``adpt_num_iter`` > 0 runs in rounds of adaptive refinement (run.Refinement,
+  the reference's policy): each round's blocks get per-block results; when the round's event
+  fires, the host selects and divides K-points and queues the next round on the same stream.
 
 No counterpart in the reference; the numerical path is exactly ``run()``'s.
 """
+import copy
 import threading
 import time
 from collections import deque
@@ -27,7 +31,7 @@ import torch
 
 from . import engine
 from .result import ResultDict
-from .run import choose_batch
+from .run import Refinement, choose_batch
 
 
 def admit(pending_bytes, used_bytes, budget_bytes, free_slots):
@@ -88,9 +92,13 @@ class Ticket:
 
 
 class _Request:
-    def __init__(self, ticket, key, grid, calculators, blocks):
+    def __init__(self, ticket, key, grid, calculators, blocks, adapt=None):
         self.ticket, self.key, self.grid, self.calculators = ticket, key, grid, calculators
         self.blocks = blocks
+        self.adapt = adapt  # (adpt_num_iter, adpt_mesh, adpt_fac) or None
+        self.refine = None  # run.Refinement of an adaptive request
+        self.shifts = None  # block shifts of the current round (adaptive requests)
+        self.round_calcs = []
         self.stream = None
         self.ws = None
         self.batches = None
@@ -140,15 +148,23 @@ class Server:
         self._systems[key] = (system, dev)
         return dev
 
-    def submit(self, key, grid, calculators, blocks=None):
+    def submit(self, key, grid, calculators, blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1):
         """Queue an integration of `calculators` over `grid` (optionally a subset `blocks` of its
-        division-grid K-points) for the system registered as `key`; returns a Ticket."""
+        division-grid K-points, or with `adpt_num_iter` rounds of adaptive refinement) for the
+        system registered as `key`; returns a Ticket."""
         if key not in self._systems:
             raise ValueError(f"unknown system {key!r}: add_system() first")
+        adapt = None
+        if adpt_num_iter:
+            if blocks is not None:
+                raise ValueError("adaptive refinement runs over the whole grid (blocks must be None)")
+            if any(getattr(c, 'tetra', False) for c in calculators.values()):
+                raise NotImplementedError("tetra=True with adaptive refinement is not supported by the GPU backend")
+            adapt = (adpt_num_iter, adpt_mesh, adpt_fac)
         with self._lock:
             self._rid += 1
             t = Ticket(self._rid, key)
-            self._pending.append(_Request(t, key, grid, dict(calculators), blocks))
+            self._pending.append(_Request(t, key, grid, dict(calculators), blocks, adapt))
         self._wake.set()
         return t
 
@@ -206,13 +222,19 @@ class Server:
                 engine.field_arrays(dev, quantities, True, engine.PREC_FP64)
             else:
                 engine.field_arrays(dev, set(), True, engine.PREC_DF64)
-                engine.field_arrays(dev, quantities, False, engine.PREC_FP32S)
+                if quantities:  # energies-only requests (DOS-type) need no band-basis fields
+                    engine.field_arrays(dev, quantities, False, engine.PREC_FP32S)
             ready = torch.cuda.Event()
             ready.record(self._prep_stream)
         req.stream.wait_event(ready)
         req.quantities = quantities
-        req.batches = [blocks[i:i + nb] for i in range(0, len(blocks), nb)]
-        req.ticket.nkpoints = len(blocks) * req.grid.nk_per_block
+        req.nb = nb
+        if req.adapt is not None:
+            req.refine = Refinement(system, req.grid, req.calculators, *req.adapt)
+            self._plan_round(req)
+        else:
+            req.batches = [blocks[i:i + nb] for i in range(0, len(blocks), nb)]
+            req.ticket.nkpoints = len(blocks) * req.grid.nk_per_block
         with torch.cuda.stream(req.stream):
             for c in req.calculators.values():
                 c.reset(self.device)
@@ -225,6 +247,39 @@ class Server:
                 req.done_event.record(req.stream)
         self._active.append(req)
 
+    def _plan_round(self, req):
+        """Batches of the adaptive request's next round (the K-points not evaluated yet)."""
+        req.shifts = req.refine.new_shifts()
+        n = len(req.shifts)
+        req.batches = [np.arange(i, min(i + req.nb, n)) for i in range(0, n, req.nb)]
+        req.next_batch = 0
+        req.done_event = None
+        req.ticket.nkpoints += n * req.grid.nk_per_block
+
+    def _issue_adaptive(self, req, idx, system, dev):
+        bd = engine.band_data(dev, req.shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
+        for b in range(bd.nblocks):  # per-block results: fresh calculators for every block
+            sub = bd.block(b)
+            cs = {k: copy.deepcopy(c) for k, c in req.refine.templates.items()}
+            for c in cs.values():
+                c.reset(self.device)
+                c.accumulate(sub, system)
+            req.round_calcs.append(cs)
+        return bd
+
+    def _end_round(self, req):
+        """The round's kernels are done: per-block results, then the next round or the end."""
+        system, dev = self._systems[req.key]
+        with torch.cuda.stream(req.stream):
+            nk = req.grid.nk_per_block
+            req.refine.add([{k: c.result(system.cell_volume, nk, 1.0) for k, c in cs.items()}
+                            for cs in req.round_calcs])
+        req.round_calcs = []
+        if req.refine.refine():
+            self._plan_round(req)
+            return False
+        return True
+
     def _issue(self, req):
         system, dev = self._systems[req.key]
         idx = req.batches[req.next_batch]
@@ -232,7 +287,9 @@ class Server:
         shifts = req.grid.block_shifts()
         with torch.cuda.stream(req.stream):
             contiguous = np.all(np.diff(idx) == 1)
-            if contiguous:
+            if req.refine is not None:
+                bd = self._issue_adaptive(req, idx, system, dev)
+            elif contiguous:
                 bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision,
                                       phases=req.phases, block_start=int(idx[0]), ws=req.ws)
             else:
@@ -255,7 +312,11 @@ class Server:
                     raise RuntimeError("wbg_eigh_batched: QL iteration did not converge for some k-point")
                 nk = req.grid.nk_per_block
                 factor = 1.0 / req.grid.nblocks
-                res = ResultDict({k: c.result(system.cell_volume, nk, factor) for k, c in req.calculators.items()})
+                if req.refine is not None:
+                    res = req.refine.total()
+                else:
+                    res = ResultDict({k: c.result(system.cell_volume, nk, factor)
+                                      for k, c in req.calculators.items()})
             req.ticket._finish(result=res)
         except Exception as e:  # the request fails, the server keeps going
             req.ticket._finish(error=e)
@@ -273,6 +334,18 @@ class Server:
                 self._issue(req)
         for req in list(self._active):
             if req.next_batch == len(req.batches) and req.done_event.query():
+                if req.refine is not None:
+                    try:
+                        if not self._end_round(req):
+                            continue  # next refinement round queued on the same stream
+                    except Exception as e:
+                        req.ticket._finish(error=e)
+                        self._active.remove(req)
+                        req.ws.release()
+                        self._used -= req.nbytes
+                        self._free_streams.append(req.stream)
+                        self._finished.append(req.ticket)
+                        continue
                 self._active.remove(req)
                 self._finish(req)
         with self._lock:
