@@ -80,6 +80,23 @@ __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) {
   return df_quick(s.hi, s.lo + (e + c.lo));
 }
 
+// Lazy multiply-add chains: acc += a b with the exact two-sum of the leading parts and every
+// error term collected in acc.lo, without renormalising (12 instead of 15 FP32 instructions);
+// df_lazy_done renormalises once at the end of the chain (a full two-sum: after cancellation
+// |lo| may exceed |hi|).  Over a few hundred steps lo stays within a few hundred ulp(hi).
+__device__ __forceinline__ void df_lazy_fma(df64& acc, df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float s = acc.hi + p;
+  const float v = s - acc.hi;
+  const float t = (acc.hi - (s - v)) + (p - v);
+  acc.hi = s;
+  acc.lo = acc.lo + (t + e);
+}
+__device__ __forceinline__ df64 df_lazy_done(df64 acc) { return df_two_sum(acc.hi, acc.lo); }
+
 __device__ __forceinline__ bool operator<(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool operator>(df64 a, df64 b) { return b < a; }
 __device__ __forceinline__ bool operator<=(df64 a, df64 b) { return !(b < a); }

@@ -82,6 +82,30 @@ template <typename TU, typename CR> WBG_D typename C2<TU>::t to_tu_c(CR a) {
 // Outputs: d[k][i], e[k][i] (e[n-1] = 0) in the solver type R; Vh[k][c][i] (v of reflector
 // c, v_{c+1}=1, zeros for i<=c) and tau[k][c] rounded to the back-transform type TV.
 // ---------------------------------------------------------------------------------------
+// Lazy multiply-add chains (df_lazy_fma of wbgpu_df64.cuh for double-float; an ordinary fma
+// for double), renormalised once at the end of the chain by lz_done.
+WBG_D void lz_fma(double& acc, double a, double b) { acc = fma(a, b, acc); }
+WBG_D double lz_done(double acc) { return acc; }
+WBG_D void lz_fma(df64& acc, df64 a, df64 b) { df_lazy_fma(acc, a, b); }
+WBG_D df64 lz_done(df64 acc) { return df_lazy_done(acc); }
+template <typename CR> WBG_D void lz_cfma(CR& acc, const CR& a, const CR& b) {  // acc += a b
+  lz_fma(acc.x, a.x, b.x);
+  lz_fma(acc.x, -a.y, b.y);
+  lz_fma(acc.y, a.x, b.y);
+  lz_fma(acc.y, a.y, b.x);
+}
+template <typename CR> WBG_D void lz_cfmac(CR& acc, const CR& a, const CR& b) {  // acc += conj(a) b
+  lz_fma(acc.x, a.x, b.x);
+  lz_fma(acc.x, a.y, b.y);
+  lz_fma(acc.y, a.x, b.y);
+  lz_fma(acc.y, -a.y, b.x);
+}
+template <typename CR> WBG_D CR lz_cdone(CR a) {
+  a.x = lz_done(a.x);
+  a.y = lz_done(a.y);
+  return a;
+}
+
 WBG_D int owned_row(int t, int half, int l, int L) {  // half 0: 2Lt + l, half 1: 2Lt + 2L-1-l
   return 2 * L * t + (half ? 2 * L - 1 - l : l);
 }
@@ -163,18 +187,22 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
           const CR* Ai = Am + tri(i);
           int j = c + 1;
           for (; j < i; j += 2) {
-            cfma(acc, Ai[j], vs[j]);
-            cfma(acc1, Ai[j + 1], vs[j + 1]);
+            lz_cfma(acc, Ai[j], vs[j]);
+            lz_cfma(acc1, Ai[j + 1], vs[j + 1]);
           }
-          if (j == i) cfma(acc, Ai[j], vs[j]);
+          if (j == i) lz_cfma(acc, Ai[j], vs[j]);
           j = i + 1;
           int idx = tri(i + 1) + i;
           for (; j + 1 < n; j += 2) {
-            cfmac(acc2, Am[idx], vs[j]);
-            cfmac(acc3, Am[idx + j + 1], vs[j + 1]);
+            lz_cfmac(acc2, Am[idx], vs[j]);
+            lz_cfmac(acc3, Am[idx + j + 1], vs[j + 1]);
             idx += 2 * j + 3;
           }
-          if (j < n) cfmac(acc2, Am[idx], vs[j]);
+          if (j < n) lz_cfmac(acc2, Am[idx], vs[j]);
+          acc = lz_cdone(acc);
+          acc1 = lz_cdone(acc1);
+          acc2 = lz_cdone(acc2);
+          acc3 = lz_cdone(acc3);
           acc.x = (acc.x + acc1.x) + (acc2.x + acc3.x);
           acc.y = (acc.y + acc1.y) + (acc2.y + acc3.y);
           const CR p = cmul(tau, acc);
@@ -208,15 +236,15 @@ __global__ void eigh_tridiag(const HIn* __restrict__ H, long long strideK, int n
           for (int j = c + 1; j <= i; ++j) {
             CR a = Ai[j];
             const CR vj = vs[j], wj = ws[j];
-            a.x = fma(-vi.x, wj.x, a.x);
-            a.x = fma(-vi.y, wj.y, a.x);
-            a.x = fma(-wi.x, vj.x, a.x);
-            a.x = fma(-wi.y, vj.y, a.x);
-            a.y = fma(-vi.y, wj.x, a.y);
-            a.y = fma(vi.x, wj.y, a.y);
-            a.y = fma(-wi.y, vj.x, a.y);
-            a.y = fma(wi.x, vj.y, a.y);
-            Ai[j] = a;
+            lz_fma(a.x, -vi.x, wj.x);
+            lz_fma(a.x, -vi.y, wj.y);
+            lz_fma(a.x, -wi.x, vj.x);
+            lz_fma(a.x, -wi.y, vj.y);
+            lz_fma(a.y, -vi.y, wj.x);
+            lz_fma(a.y, vi.x, wj.y);
+            lz_fma(a.y, -wi.y, vj.x);
+            lz_fma(a.y, wi.x, vj.y);
+            Ai[j] = lz_cdone(a);
           }
         }
       }

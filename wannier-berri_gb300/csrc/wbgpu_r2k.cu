@@ -111,11 +111,24 @@ WBG_D void load_phases(const typename C2<T>::t* __restrict__ ph, int Nj, int nr,
   }
 }
 
-// acc += t x (xs = (x.y, x.x), used by the packed FP32 form)
+// acc += t x (xs = (x.y, x.x), used by the packed FP32 form); pdone ends an accumulation chain
 template <typename T>
 WBG_D void pmac(typename C2<T>::t& acc, const typename PhaseEntry<T>::type& t, typename C2<T>::t x,
                 typename C2<T>::t xs) {
   cfma(acc, t, x);
+}
+template <typename T> WBG_D void pdone(typename C2<T>::t&) {}
+// double-float: lazy chains (one renormalisation per output instead of one per term)
+template <>
+WBG_D void pmac<df64>(cdf& acc, const cdf& t, cdf x, cdf xs) {
+  df_lazy_fma(acc.x, t.x, x.x);
+  df_lazy_fma(acc.x, -t.y, x.y);
+  df_lazy_fma(acc.y, t.x, x.y);
+  df_lazy_fma(acc.y, t.y, x.x);
+}
+template <> WBG_D void pdone<df64>(cdf& a) {
+  a.x = df_lazy_done(a.x);
+  a.y = df_lazy_done(a.y);
 }
 template <>
 WBG_D void pmac<float>(float2& acc, const float4& t, float2 x, float2 xs) {
@@ -152,8 +165,10 @@ WBG_D void contract(const typename C2<T>::t* x, int len, const typename PhaseEnt
         for (int q = 0; q < JB; ++q) pmac<T>(a[q], t[q], x[i], xs[i]);
       }
 #pragma unroll
-    for (int q = 0; q < JB; ++q)
+    for (int q = 0; q < JB; ++q) {
+      pdone<T>(a[q]);
       if (j0 + q < Nj) out[(long long)(j0 + q) * out_stride] = a[q];
+    }
   }
 }
 
