@@ -156,7 +156,7 @@ int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, d
  * herm[f] | 4: X[fsel[f]] holds only its lower triangle (wbg_r2k_columns output); it is read
  * as the Hermitian matrix with that lower triangle and a real diagonal.
  * fp64 == 0 and nw == 32 run on the tensor cores (tcgen05, products split into three TF32
- * terms, FP32 accumulation); other sizes and fp64 != 0 on the CUDA cores. */
+ * terms, FP32 accumulation) when X is 16-byte aligned; other cases on the CUDA cores. */
 int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                int nFrot, void* Xbar, int nw, int nk, int fp64, void* stream);
 

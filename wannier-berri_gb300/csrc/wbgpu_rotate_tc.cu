@@ -72,6 +72,20 @@ WBG_D void put_split(unsigned char* hi, unsigned char* lo, uint32_t off, float x
   *reinterpret_cast<uint32_t*>(hi + off) = h;
   *reinterpret_cast<uint32_t*>(lo + off) = l;
 }
+// four K-consecutive values (k % 4 == 0: one 16-byte row of a core matrix) in one store each
+WBG_D void put_split4(unsigned char* hi, unsigned char* lo, uint32_t off, float a, float b, float c, float d) {
+  uint4 h, l;
+  h.x = tf32_rna(a);
+  h.y = tf32_rna(b);
+  h.z = tf32_rna(c);
+  h.w = tf32_rna(d);
+  l.x = tf32_rna(a - __uint_as_float(h.x));
+  l.y = tf32_rna(b - __uint_as_float(h.y));
+  l.z = tf32_rna(c - __uint_as_float(h.z));
+  l.w = tf32_rna(d - __uint_as_float(h.w));
+  *reinterpret_cast<uint4*>(hi + off) = h;
+  *reinterpret_cast<uint4*>(lo + off) = l;
+}
 
 // Shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), version 1 at bit 46,
 // base offset 0, no swizzle.
@@ -229,11 +243,14 @@ __global__ void __launch_bounds__(NTHR, 2)
     }
     for (int t = 0; t < ntiles; ++t) {
       // ---- A1: rows (fl, m) of the tile's fields, K = [Re X[m][:] | Im X[m][:]].
-      // Thread tid owns element n = lane of rows m = 8 i + warp (mod NW): every load of the
-      // tile is issued before the first store.
+      // A task is 4 consecutive elements n0..n0+3 of one row: a 16-byte store per operand half.
+      // A field given by its lower triangle is read as the Hermitian matrix it stands for
+      // (X[m][n] = conj(X[n][m]) above the diagonal, real diagonal).  Every load of the tile
+      // is issued before the first store.
       {
-        constexpr int PER = FPT * NW * NW / NTHR;
-        float2 xv[PER];
+        constexpr int CPR = NW / 4;              // tasks per row
+        constexpr int PER = FPT * NW * CPR / NTHR;
+        float2 xv[PER][4];
         int code[FPT];  // per field: -1 padding, -2 invalid selection, else source field | lower << 30
 #pragma unroll
         for (int fl = 0; fl < FPT; ++fl) {
@@ -247,29 +264,48 @@ __global__ void __launch_bounds__(NTHR, 2)
         }
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
-          const int e = i * NTHR + tid, fl = e / (NW * NW), m = (e / NW) % NW, n = e % NW;
+          const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
           const int c = code[fl];
           const bool lower = c >= 0 && (c >> 30);
-          xv[i] = make_float2(0.f, 0.f);
-          if (c == -2) xv[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-          else if (c >= 0 && (!lower || m >= n))
-            xv[i] = X[(k * nFin + (c & 0x3fffffff)) * (long long)(NW * NW) + m * NW + n];
+          const float2* Xf = X + (k * nFin + (c >= 0 ? (c & 0x3fffffff) : 0)) * (long long)(NW * NW);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) xv[i][q] = make_float2(0.f, 0.f);
+          if (c == -2) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) xv[i][q] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+          } else if (c >= 0) {
+            if (!lower || m >= n0 + 3) {  // the whole chunk is stored: two 16-byte loads
+              const float4* src = reinterpret_cast<const float4*>(Xf + m * NW + n0);
+              const float4 a = src[0], b = src[1];
+              xv[i][0] = make_float2(a.x, a.y);
+              xv[i][1] = make_float2(a.z, a.w);
+              xv[i][2] = make_float2(b.x, b.y);
+              xv[i][3] = make_float2(b.z, b.w);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                const int n = n0 + q;
+                if (m >= n) {
+                  xv[i][q] = Xf[m * NW + n];
+                } else {
+                  const float2 u = Xf[n * NW + m];
+                  xv[i][q] = make_float2(u.x, -u.y);
+                }
+              }
+            }
+            if (lower && m >= n0 && m < n0 + 4) {  // real diagonal
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (n0 + q == m) xv[i][q].y = 0.f;
+            }
+          }
         }
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
-          const int e = i * NTHR + tid, fl = e / (NW * NW), m = (e / NW) % NW, n = e % NW;
-          const int c = code[fl];
-          const bool lower = c >= 0 && (c >> 30);
-          const int r = fl * NW;
-          const float xr = xv[i].x, xi = (lower && m == n) ? 0.f : xv[i].y;
-          if (!lower || m >= n) {
-            put_split(Ah, Al, op_off(r + m, n), xr);
-            put_split(Ah, Al, op_off(r + m, NW + n), xi);
-          }
-          if (lower && m > n) {  // upper triangle: X[n][m] = conj(X[m][n])
-            put_split(Ah, Al, op_off(r + n, m), xr);
-            put_split(Ah, Al, op_off(r + n, NW + m), -xi);
-          }
+          const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
+          const int r = fl * NW + m;
+          put_split4(Ah, Al, op_off(r, n0), xv[i][0].x, xv[i][1].x, xv[i][2].x, xv[i][3].x);
+          put_split4(Ah, Al, op_off(r, NW + n0), xv[i][0].y, xv[i][1].y, xv[i][2].y, xv[i][3].y);
         }
       }
       fence_async_smem();
