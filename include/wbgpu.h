@@ -125,10 +125,16 @@ int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, con
  *         wbg_r2k_columns on the lower triangle.
  * mode | 8 (WBG_EIGH_VALUES): eigenvalues only (np.linalg.eigvalsh; the tetrahedron corners,
  *         data_K/data_K_R.py:121-141); U is not written and may be NULL.
+ * mode | 16 (WBG_EIGH_STAGE1): the tridiagonalisation only, kept in the workspace; a later call
+ *         with mode | 32 (WBG_EIGH_STAGE2) and the same nw, nk, base mode and workspace finishes
+ *         (eigenvalues, vectors; H is not read and may be NULL).  Lets a caller start
+ *         independent work on another stream between the two stages.
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 #define WBG_EIGH_LOWER 4
 #define WBG_EIGH_VALUES 8
+#define WBG_EIGH_STAGE1 16
+#define WBG_EIGH_STAGE2 32
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);

@@ -539,7 +539,7 @@ int pick_group(size_t smem, int threads, int gmax) {
 
 template <typename R, typename TU, typename HIn>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int lowerIn,
-                int valuesOnly, void* workspace, int* errflag, cudaStream_t stream) {
+                int valuesOnly, int stage, void* workspace, int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
   typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
@@ -551,12 +551,15 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   // tridiagonalisation: mirrored row pairs on half the lanes (balanced rows; one row per lane
   // on all 32 lanes measured 22% slower at nw = 32)
   const int LT = L >= 8 ? L / 2 : 4;
-  const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
-  const int G = pick_group(smT, LT, 128 / LT);
-  if (G == 0) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(eigh_tridiag<R, HIn, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
-  eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G,
-                                                                           lowerIn, Vh, tau, d, e);
+  if (stage != 2) {  // stage 1 (or both): the tridiagonalisation into the workspace
+    const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
+    const int G = pick_group(smT, LT, 128 / LT);
+    if (G == 0) return WBG_ERR_SIZE;
+    cudaFuncSetAttribute(eigh_tridiag<R, HIn, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
+    eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G,
+                                                                             lowerIn, Vh, tau, d, e);
+    if (stage == 1) return wbg_cuda_status(cudaGetLastError());
+  }
   int BQ = 128;  // threads (matrices) per block: d and e take 2 n sizeof(R) bytes of shared memory each
   while (BQ > 32 && (size_t)BQ * 2 * n * sizeof(R) > 64 * 1024) BQ /= 2;
   const size_t smQ = (size_t)BQ * 2 * n * sizeof(R);
@@ -587,19 +590,25 @@ size_t wbg_eigh_workspace_bytes(int n, int nk) {
 int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int mode,
                  void* workspace, size_t workspace_bytes, int* errflag, cudaStream_t stream) {
   const int vo = (mode & WBG_EIGH_VALUES) ? 1 : 0;
-  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !H || !E || (!U && !vo) || !errflag) return WBG_ERR_ARG;
-  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES)) return WBG_ERR_ARG;
+  const int stage = (mode & WBG_EIGH_STAGE1) ? 1 : (mode & WBG_EIGH_STAGE2) ? 2 : 0;
+  if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !E || (!U && !vo) || !errflag) return WBG_ERR_ARG;
+  if (!H && stage != 2) return WBG_ERR_ARG;
+  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES | WBG_EIGH_STAGE1 | WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
+  if ((mode & WBG_EIGH_STAGE1) && (mode & WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
   const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
   switch (mode & 3) {
     case 1:
-      return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+      return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
+                                                  stream);
     case 0:
-      return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+      return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
+                                                 stream);
     case 2:
-      return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+      return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
+                                               stream);
     default:
-      return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, workspace, errflag, stream);
+      return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag, stream);
   }
 }
 

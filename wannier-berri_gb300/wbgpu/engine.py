@@ -155,6 +155,12 @@ class Workspace:
             self._bufs[name] = buf
         return buf[:nbytes].view(dtype).view(shape)
 
+    def side_stream(self):
+        """A second CUDA stream of this workspace (independent stages of one batch)."""
+        if getattr(self, '_side', None) is None:
+            self._side = torch.cuda.Stream(device=self.device)
+        return self._side
+
     def nbytes(self):
         return sum(b.numel() for b in self._bufs.values())
 
@@ -244,9 +250,15 @@ class DeviceSystem:
     def buffer(self, name, shape, dtype):
         """Persistent device buffer of the system's default workspace (grow-only), viewed as
         `dtype[shape]`: keeps GB-sized per-batch allocations out of the caching allocator's way."""
+        return self.workspace().buffer(name, shape, dtype)
+
+    def workspace(self):
         if 'ws' not in self._cache:
             self._cache['ws'] = Workspace(self.device)
-        return self._cache['ws'].buffer(name, shape, dtype)
+        return self._cache['ws']
+
+    def side_stream(self):
+        return self.workspace().side_stream()
 
     def grid_phases(self, shifts, NKFFT, prec):
         """Device-resident per-axis phase tables for every block of a grid (built once per grid)."""
@@ -403,6 +415,7 @@ PREC_FP32, PREC_FP64, PREC_DF64, PREC_FP32S = 0, 1, 2, 3
 C64_PRECS = (PREC_FP32, PREC_FP32S)
 EIGH_LOWER = 4  # wbg_eigh_batched mode bit: H given by its lower triangle
 EIGH_VALUES = 8  # wbg_eigh_batched mode bit: eigenvalues only
+EIGH_STAGE1, EIGH_STAGE2 = 16, 32  # wbg_eigh_batched mode bits: tridiagonalise / finish
 
 
 def _prec(p):
@@ -566,14 +579,14 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     flag = arena.buffer('flag', (1,), torch.int32)
     flag.zero_()
 
-    def fields_for(q, with_H, prec, name, lower=False):
+    def fields_for(q, with_H, prec, name, lower=False, wsname='r2k_ws'):
         _, _, nF, _ = field_arrays(dev, q, with_H, prec)
         out = arena.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec in C64_PRECS else torch.complex128)
         geo = r2k_geometry(dev, NKFFT)
         wsz = ctypes.c_size_t(0)
         _lib.check(_lib.load().wbg_r2k_workspace_size(ctypes.byref(geo), nF, nb, prec, ctypes.byref(wsz)),
                    "wbg_r2k_workspace_size")
-        work = arena.buffer('r2k_ws', (int(wsz.value),), torch.uint8)
+        work = arena.buffer(wsname, (int(wsz.value),), torch.uint8)
         return r2k(dev, dKs, NKFFT, q, with_H, prec, out=out, workspace=work, phases=ph(prec),
                    block_start=block_start, lower=lower)
 
@@ -593,13 +606,26 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=lowerH)
         keep.append(k0)
         U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
-        E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=3 | (EIGH_LOWER if lowerH else 0), work=ework,
-                          flag=flag)
+        mode = 3 | (EIGH_LOWER if lowerH else 0)
         if quantities:
-            fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True)
+            # the FP32 fields do not depend on the eigensolver: their transform runs on a side
+            # stream next to the QL iteration (a few warps per SM, latency-bound), started once
+            # the tridiagonalisation (which fills the SMs' shared memory) is done
+            main = torch.cuda.current_stream()
+            side = arena.side_stream()
+            eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode | EIGH_STAGE1, work=ework, flag=flag)
+            tridiag_done = torch.cuda.Event()
+            tridiag_done.record(main)
+            with torch.cuda.stream(side):
+                side.wait_event(tridiag_done)
+                fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True,
+                                                   wsname='r2k_ws_fields')
+            E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode | EIGH_STAGE2, work=ework, flag=flag)
+            main.wait_stream(side)
             keep.append(k1)
             lower_in = column_list(dev, quantities, False, True)[1]
         else:  # energies only (DOS-type calculators): no band-basis fields
+            E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode, work=ework, flag=flag)
             fields, index, nF, lower_in = None, {}, 0, []
         fp64_fields = False
     else:
