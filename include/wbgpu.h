@@ -198,8 +198,11 @@ int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW,
  * blocks[b]: flat division-grid index (C order) of batch block b; E [nblocks*nk][nw] the
  * k-point energies of the batch (blocks in that order, k in C order of the FFT grid). */
 typedef struct {
-  int div[3]; /* NKdiv */
-  int fft[3]; /* NKFFT */
+  int div[3];    /* NKdiv */
+  int fft[3];    /* NKFFT */
+  int per_block; /* != 0: every block has its own 8 corner grids (refined blocks, whose cell
+                    differs from the grid's): corner s of k-point kl of block b at
+                    Ecorner row corner_slot[blocks[b]] * 8 + s, index kl */
 } wbg_tetra_grid;
 
 /* Bands that take part (tetrahedron.py:215-262 weights_all_band_groups, Emin = -inf):

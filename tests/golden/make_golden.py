@@ -34,7 +34,8 @@ Fixtures written (all small, complex128/float64):
   NKFFT (3,4,2)).  ``python make_golden.py <reference root> tetra`` writes only this file.
 * ``refine_ref.npz`` -- adaptive refinement (``adpt_num_iter``) of the reference's ``run``
   without symmetry: the random system (3 iterations, AHC / DOS / CumDOS) and the triclinic
-  MDRS model (2 iterations, adpt_fac 2, adpt_mesh (2,1,3), AHC / BerryDipole_FermiSea).
+  MDRS model (2 iterations, adpt_fac 2, adpt_mesh (2,1,3), AHC / BerryDipole_FermiSea), and
+  AHC / DOS with tetra=True on the random system (2 iterations).
   ``python make_golden.py <reference root> refine`` writes only this file.
 """
 import os
@@ -252,6 +253,10 @@ def refine_fixtures(wb, rs):
     for k, v in run_ref_adaptive(wb, s2, 2, [3, 4, 2], cs, adpt_num_iter=2, adpt_mesh=[2, 1, 3],
                                  adpt_fac=2).items():
         out['c2_' + k] = v
+    # the tetrahedron method on refined K-points (their corners follow each K-point's cell)
+    cs = {'ahc': calc.static.AHC(Efermi=EF, tetra=True), 'dos': calc.static.DOS(Efermi=EF, tetra=True)}
+    for k, v in run_ref_adaptive(wb, rs, 2, 3, cs, adpt_num_iter=2, adpt_mesh=2, adpt_fac=1).items():
+        out['tetra_random_' + k] = v
     np.savez_compressed(os.path.join(HERE, 'refine_ref.npz'), **out)
 
 

@@ -687,3 +687,34 @@ def test_refine_served_equals_run(c2small):
     from wbgpu.run import run_adaptive
     _, K, _, _ = run_adaptive(s, grid, {'ahc': C.AHC(Efermi=EF)}, 'mixed', engine.DeviceSystem(s), 2, 2, 2)
     assert t1.nkpoints == len(K) * 27 and len(K) > 8  # every K-point of every round, 3^3 k each
+
+
+@pytest.mark.parametrize("precision,rule", [('fp64', 1e-8), ('mixed', 1e-5)])
+def test_refine_tetra_golden(golden_dir, precision, rule):
+    """tetra=True with adaptive refinement against the reference: refined K-points get the 8
+    corner grids of their own cell (wbg_tetra_grid.per_block)."""
+    import os
+    rs = _golden_system(golden_dir, 'random_system.npz')
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    C = wbgpu.calculators
+    res = wbgpu.run(rs, wbgpu.Grid(rs, NKdiv=2, NKFFT=3),
+                    {'ahc': C.AHC(Efermi=g['EF'], tetra=True), 'dos': C.DOS(Efermi=g['EF'], tetra=True)},
+                    precision=precision, adpt_num_iter=2, adpt_mesh=2)
+    for key in ('ahc', 'dos'):
+        exp = g['tetra_random_' + key]
+        assert np.abs(res[key].data - exp).max() < rule * np.abs(exp).max(), key
+
+
+def test_refine_tetra_served(c2small):
+    """The same through the Server (corner grids per refined block on the request's stream)."""
+    s, _ = c2small
+    EF = np.linspace(-1.5, 1.5, 31)
+    C = wbgpu.calculators
+    grid = wbgpu.Grid(s, NKdiv=2, NKFFT=3)
+    mk = lambda: {'ahc': C.AHC(Efermi=EF, tetra=True)}
+    alone = wbgpu.run(s, grid, mk(), precision='mixed', adpt_num_iter=1)
+    srv = wbgpu.Server(precision='mixed')
+    srv.add_system('c2', s)
+    t = srv.submit('c2', grid, mk(), adpt_num_iter=1)
+    srv.run_until_idle()
+    assert maxrel(t.wait()['ahc'].data, alone['ahc'].data) < 1e-9

@@ -241,3 +241,14 @@ def test_refine_c2_anisotropic_golden(golden_dir):
     r, _ = O.run_adaptive(s2, (2, 2, 2), (3, 4, 2), calcs, adpt_num_iter=2, adpt_mesh=(2, 1, 3), adpt_fac=2)
     for k in calcs:
         assert maxrel(r[k].data, g['c2_' + k]) < 1e-9, k
+
+
+def test_refine_tetra_golden(random_sys, golden_dir):
+    """Tetrahedron method on refined K-points: each K-point's corners follow its own cell."""
+    g = np.load(os.path.join(golden_dir, 'refine_ref.npz'))
+    EF = g['EF']
+    calcs = {'ahc': O.AHC(Efermi=EF, tetra=True), 'dos': O.DOS(Efermi=EF, tetra=True)}
+    r, _ = O.run_adaptive(random_sys, (2, 2, 2), (3, 3, 3), calcs, adpt_num_iter=2, adpt_mesh=2)
+    for k in calcs:
+        ref = g['tetra_random_' + k]
+        assert np.max(np.abs(r[k].data - ref)) < 1e-8 * np.max(np.abs(ref)), k

@@ -30,6 +30,7 @@ WBG_D long long corner_row(const wbg_tetra_grid& g, const int* __restrict__ bloc
   const int b = (int)(kk / nk);
   int kl = (int)(kk % nk);
   int gb = blocks[b];
+  if (g.per_block) return ((long long)slot[gb] * 8 + s) * nk + kl;
   int i[3], j[3];
   i[2] = gb % g.div[2];
   gb /= g.div[2];
@@ -437,7 +438,7 @@ int grid_cap(int G, long long nkt, int per_sm) {
 bool grid_ok(const wbg_tetra_grid* g) {
   for (int a = 0; a < 3; ++a)
     if (g->div[a] < 1 || g->fft[a] < 1) return false;
-  return true;
+  return g->per_block == 0 || g->per_block == 1;
 }
 
 }  // namespace

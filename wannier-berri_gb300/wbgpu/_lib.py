@@ -41,7 +41,7 @@ class KuboParams(ctypes.Structure):
 
 
 class TetraGrid(ctypes.Structure):
-    _fields_ = [('div', ctypes.c_int * 3), ('fft', ctypes.c_int * 3)]
+    _fields_ = [('div', ctypes.c_int * 3), ('fft', ctypes.c_int * 3), ('per_block', ctypes.c_int)]
 
 
 class FieldIndex(ctypes.Structure):

@@ -396,6 +396,10 @@ class BandData:
                        self.index, 1, self.nk, self.nw, self.fp64_fields, hermitian=self.hermitian)
         sub._flag = getattr(self, '_flag', None)
         sub._keep = getattr(self, '_keep', None)
+        if self.tetra is not None:
+            sub.tetra = self.tetra
+            sub.tetra_blocks = self.tetra_blocks[b:b + 1]
+            sub.tetra_sel = {}
         return sub
 
 
@@ -705,7 +709,7 @@ class TetraCorners:
 
     def __init__(self, dev, grid, blocks=None, precision='fp64', ws=None, batch=None):
         div, fft = np.array(grid.div, dtype=int), np.array(grid.FFT, dtype=int)
-        self.grid = _lib.TetraGrid((ctypes.c_int * 3)(*div.tolist()), (ctypes.c_int * 3)(*fft.tolist()))
+        self.grid = _lib.TetraGrid((ctypes.c_int * 3)(*div.tolist()), (ctypes.c_int * 3)(*fft.tolist()), 0)
         self.nblocks_total = int(np.prod(div))
         blocks = np.arange(self.nblocks_total) if blocks is None else np.asarray(blocks, dtype=int)
         idx = np.stack(np.unravel_index(blocks, div), axis=-1)
@@ -765,6 +769,33 @@ class TetraCorners:
             _lib.check(st, "wbg_tetra_select")
             bd.tetra_sel[key] = sel
         return bd.tetra_sel[key]
+
+
+class BlockCorners(TetraCorners):
+    """Corner energies of arbitrary blocks, e.g. refined K-points whose cell differs from the
+    grid's (data_K/data_K_R.py:121-141 with Kpoint.dK_fullBZ of each K-point): block b at shift
+    dK_b with cell c_b = dK_block / NKFFT gets the 8 grids at dK_b + (+-c_b/2 per axis), corner
+    s = 4 sx + 2 sy + sz (0: minus side) at Ecorner row 8 b + s; the kernels address them through
+    wbg_tetra_grid.per_block.  Blocks are identified by their position in `shifts`."""
+
+    def __init__(self, dev, shifts, cells, NKFFT, precision='fp64', ws=None):
+        fft = np.array(NKFFT, dtype=int) * np.ones(3, dtype=int)
+        self.grid = _lib.TetraGrid((ctypes.c_int * 3)(1, 1, 1), (ctypes.c_int * 3)(*fft.tolist()), 1)
+        shifts, cells = np.asarray(shifts, dtype=float), np.asarray(cells, dtype=float)
+        nb, nk, nw = len(shifts), int(np.prod(fft)), dev.nw
+        sgn = np.array([[(s >> (2 - a)) & 1 for a in range(3)] for s in range(8)], dtype=float) - 0.5
+        corner_shifts = (shifts[:, None, :] + sgn[None, :, :] * cells[:, None, :]).reshape(-1, 3)
+        self.Ec = torch.empty((len(corner_shifts) * nk, nw), dtype=torch.float64, device=dev.device)
+        self.slot = torch.arange(nb, dtype=torch.int32, device=dev.device)
+        from .run import choose_batch
+        batch = choose_batch(nw, nk, len(corner_shifts), set(), precision)
+        self.flags = []
+        for i0 in range(0, len(corner_shifts), batch):
+            n = min(batch, len(corner_shifts) - i0)
+            _, flag = energies(dev, corner_shifts[i0:i0 + n], fft, precision, out=self.Ec[i0 * nk:(i0 + n) * nk],
+                               ws=ws)
+            self.flags.append(flag.clone())
+        self.device = dev.device
 
 
 def device_flags(clear=True):

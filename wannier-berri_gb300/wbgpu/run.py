@@ -25,18 +25,27 @@ def choose_batch(nw, nk, nblocks, quantities, precision, max_kpoints=1 << 17, bu
     return int(nb)
 
 
-def block_results(dev, system, shifts, NKFFT, calculators, precision, dk_cell=None):
+def block_results(dev, system, shifts, NKFFT, calculators, precision, cells=None):
     """One result per block -- what the reference's calculators return for one Data_K (normalised
     by the block's k-points, K-point factor 1): [{key: EnergyResult}] for the blocks at `shifts`.
-    Each block gets fresh copies of the calculators; batches of blocks share stages 1-3."""
+    Each block gets fresh copies of the calculators; batches of blocks share stages 1-3.
+    `cells`: each block's dense-grid cell (dK_block / NKFFT), for tetrahedron calculators."""
     quantities = set()
     for c in calculators.values():
         quantities |= c.quantities(system)
+    tetra = any(getattr(c, 'tetra', False) for c in calculators.values())
+    if tetra and cells is None:
+        raise ValueError("tetra=True needs the cell of every block")
     nk = int(np.prod(NKFFT))
     nb = choose_batch(dev.nw, nk, len(shifts), quantities, precision)
     out = []
     for i0 in range(0, len(shifts), nb):
+        corners = None
+        if tetra:  # computed before band_data: both use the system's default workspace
+            corners = engine.BlockCorners(dev, shifts[i0:i0 + nb], cells[i0:i0 + nb], NKFFT, precision)
         bd = engine.band_data(dev, shifts[i0:i0 + nb], NKFFT, quantities, precision)
+        if corners is not None:
+            corners.attach(bd, np.arange(bd.nblocks))
         for b in range(bd.nblocks):
             sub = bd.block(b)
             res = {}
@@ -47,6 +56,8 @@ def block_results(dev, system, shifts, NKFFT, calculators, precision, dk_cell=No
                 res[key] = cb.result(system.cell_volume, nk, 1.0)
             out.append(res)
         engine.check_flag(bd)
+        if corners is not None:
+            corners.check()
     return out
 
 
@@ -78,6 +89,10 @@ class Refinement:
     def new_shifts(self):
         """Block shifts dK = K / NKFFT of the K-points not evaluated yet."""
         return np.array(self.K[len(self.results):]) / self.fft[None, :]
+
+    def new_cells(self):
+        """Dense-grid cells dK / NKFFT of those K-points (the tetrahedra's parallelepipeds)."""
+        return np.array(self.dK[len(self.results):]) / self.fft[None, :]
 
     def add(self, results):
         self.results += list(results)
@@ -116,7 +131,7 @@ def run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_
     """run() with adaptive refinement (Refinement): returns (ResultDict, K, dK, factor)."""
     ref = Refinement(system, grid, calculators, adpt_num_iter, adpt_mesh, adpt_fac)
     while True:
-        ref.add(block_results(dev, system, ref.new_shifts(), ref.fft, ref.templates, precision))
+        ref.add(block_results(dev, system, ref.new_shifts(), ref.fft, ref.templates, precision, ref.new_cells()))
         if not ref.refine():
             break
     return ref.total(), np.array(ref.K), np.array(ref.dK), np.array(ref.fac)
@@ -134,8 +149,6 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
     if adpt_num_iter:
         if blocks is not None:
             raise ValueError("adaptive refinement runs over the whole grid (blocks must be None)")
-        if any(getattr(c, 'tetra', False) for c in calculators.values()):
-            raise NotImplementedError("tetra=True with adaptive refinement is not supported by the GPU backend")
         return run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_mesh, adpt_fac)[0]
     quantities = set()
     for c in calculators.values():

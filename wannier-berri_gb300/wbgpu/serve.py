@@ -98,6 +98,7 @@ class _Request:
         self.adapt = adapt  # (adpt_num_iter, adpt_mesh, adpt_fac) or None
         self.refine = None  # run.Refinement of an adaptive request
         self.shifts = None  # block shifts of the current round (adaptive requests)
+        self.cells = None  # and their dense-grid cells
         self.round_calcs = []
         self.stream = None
         self.ws = None
@@ -158,8 +159,6 @@ class Server:
         if adpt_num_iter:
             if blocks is not None:
                 raise ValueError("adaptive refinement runs over the whole grid (blocks must be None)")
-            if any(getattr(c, 'tetra', False) for c in calculators.values()):
-                raise NotImplementedError("tetra=True with adaptive refinement is not supported by the GPU backend")
             adapt = (adpt_num_iter, adpt_mesh, adpt_fac)
         with self._lock:
             self._rid += 1
@@ -250,6 +249,7 @@ class Server:
     def _plan_round(self, req):
         """Batches of the adaptive request's next round (the K-points not evaluated yet)."""
         req.shifts = req.refine.new_shifts()
+        req.cells = req.refine.new_cells()
         n = len(req.shifts)
         req.batches = [np.arange(i, min(i + req.nb, n)) for i in range(0, n, req.nb)]
         req.next_batch = 0
@@ -257,7 +257,14 @@ class Server:
         req.ticket.nkpoints += n * req.grid.nk_per_block
 
     def _issue_adaptive(self, req, idx, system, dev):
+        corners = None
+        if any(getattr(c, 'tetra', False) for c in req.refine.templates.values()):
+            corners = engine.BlockCorners(dev, req.shifts[idx], req.cells[idx], req.grid.FFT, self.precision,
+                                          ws=req.ws)
+            req.flags.extend(corners.flags)
         bd = engine.band_data(dev, req.shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
+        if corners is not None:
+            corners.attach(bd, np.arange(bd.nblocks))
         for b in range(bd.nblocks):  # per-block results: fresh calculators for every block
             sub = bd.block(b)
             cs = {k: copy.deepcopy(c) for k, c in req.refine.templates.items()}
