@@ -224,6 +224,10 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
         work = 16.0 * n ** 3 * 9 * k_per_call      # two complex GEMMs per field, 9 fields
         if precision == 'fp64':
             bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
+        elif peaks.get('tf32'):  # tcgen05 kind::tf32: three TF32 products per product (3xTF32)
+            work *= 3.0
+            bound, unit, peak, src = 'tensor', 'GFLOP/s', peaks['tf32'], \
+                'MEASURED_PEAKS.json bf16_tflops (burst) / 2: dense TF32 rate'
         else:
             bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
     elif stage.startswith('r2k'):
@@ -377,18 +381,27 @@ def run_gpu(args):
     try:
         mp_ = json.load(open(os.path.join(REPO, 'MEASURED_PEAKS.json')))
         peaks['hbm'] = float(mp_['hbm_gbs'])
+        peaks['tf32'] = float(mp_['bf16_tflops']) * 1e3 / 2.0  # GFLOP/s
     except (OSError, KeyError, ValueError):
-        peaks['hbm'] = 6800.0  # fallback figure of the profiling recipe
+        peaks['hbm'] = 6800.0  # fallback figures of the profiling recipe
+        peaks['tf32'] = 1.9e6 / 2.0
     nF_fields = {'r2k_fp64': 10, 'r2k_df64': 1, 'r2k_fp32': 9}
     dominant = max(stage_ms, key=stage_ms.get)
     roof = stage_roofline(dominant, stage_ms[dominant], args.steps, B * nk, precision, peaks, nF_fields)
+    # every stage against its own bound (stage times from CUDA events on the stage's stream; the
+    # field transform runs next to the eigensolver on a side stream, so its span is stretched)
+    stages_roof = {}
+    for st_name in stage_ms:
+        r_ = stage_roofline(st_name, stage_ms[st_name], args.steps, B * nk, precision, peaks, nF_fields)
+        stages_roof[st_name] = {k_: r_[k_] for k_ in ('bound', 'achieved', 'peak', 'unit', 'frac')}
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64 eigh/scan + fp32 fields" if precision == 'mixed' else "fp64",
             "data": "synthetic (seeded random TB model)", "config": config_dict(args, precision),
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clk,
+            "roofline": roof, "stages_roofline": stages_roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": gpu_launches, "clocks": clk,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
             "fp64_dropin_value": fp64_value, "max_rel_err_vs_fp64": err,
             "peaks_measured_gflops": {"fp64": peaks['fp64'], "fp32": peaks['fp32']}}
