@@ -1333,7 +1333,7 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream) {
   if (nw < 1 || nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
   // tensor cores (3xTF32) for the FP32 path at nw = 32; the kernel reads X in 16-byte pieces
-  if (wbg_rotate_tc_supported(nw, fp64) && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+  if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
     return wbg_rotate_tc_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   if (fp64) return launch_rotate<double>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   return launch_rotate<float>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);

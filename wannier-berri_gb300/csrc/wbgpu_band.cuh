@@ -8,7 +8,7 @@ typedef wbg_scan WbgScan;
 // bands per lane held in registers by the non-additive (Morb) kernel: nw <= 32 * WBG_BAND_MAXPER
 #define WBG_BAND_MAXPER 4
 
-bool wbg_rotate_tc_supported(int nw, int fp64);
+bool wbg_rotate_tc_supported(int nw, int fp64, int nFrot);
 int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                       int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream);
 int wbg_device_flags_run(unsigned int* flags, int clear);

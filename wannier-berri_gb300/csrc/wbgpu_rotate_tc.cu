@@ -47,6 +47,7 @@ static_assert((KD / 8) % NMAIN == 0, "K steps must split evenly over the main ac
 constexpr uint32_t TMEM_COLS = NACC * ND <= 128 ? 128 : NACC * ND <= 256 ? 256 : 512;  // GEMM1 and GEMM2 share them
 constexpr int STAGE_LD = NW + 1;           // float2 row stride of the Hermitian-part staging
 constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on every mbarrier wait
+constexpr int TMAP_MAX = 256;              // tile slots (fields + padding) of one launch
 
 static_assert(FPT * NW * STAGE_LD * 8 <= A_BYTES, "staging must fit in the A operand buffer");
 
@@ -201,12 +202,24 @@ __global__ void __launch_bounds__(NTHR, 2)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
+  // tile map: full fields first, then the diagonal-only fields (herm 2); a tile holding only
+  // diagonal-only fields stops after T = X U (diag(U^dagger T) by a reduction over the rows)
+  __shared__ short tmap_s[TMAP_MAX];
+  __shared__ int nfull_s, ntiles_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mb = smem_u32(&mbar);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_s = 0;
+    int nf = 0;
+    for (int f = 0; f < nFrot; ++f) nf += (herm[f] & 3) != 2;
+    const int nt = (nFrot + FPT - 1) / FPT;
+    for (int i = 0; i < nt * FPT; ++i) tmap_s[i] = -1;
+    int a = 0, b = nf;
+    for (int f = 0; f < nFrot; ++f) tmap_s[(herm[f] & 3) == 2 ? b++ : a++] = (short)f;
+    nfull_s = (nf + FPT - 1) / FPT;  // tiles from here on hold diagonal-only fields and padding
+    ntiles_s = nt;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
@@ -222,7 +235,7 @@ __global__ void __launch_bounds__(NTHR, 2)
   const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter (= field of the tile), column half
   const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;  // TMEM lanes of this warp
   uint32_t phase = 0;
-  const int ntiles = (nFrot + FPT - 1) / FPT;
+  const int ntiles = ntiles_s, nfull = nfull_s;
   float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
   for (long long k = blockIdx.x; k < nk && !abort_s; k += gridDim.x) {
     // ---- embedded U_k (B operand, hi / lo)
@@ -254,8 +267,8 @@ __global__ void __launch_bounds__(NTHR, 2)
         int code[FPT];  // per field: -1 padding, -2 invalid selection, else source field | lower << 30
 #pragma unroll
         for (int fl = 0; fl < FPT; ++fl) {
-          const int f = t * FPT + fl;
-          if (f >= nFrot) {
+          const int f = tmap_s[t * FPT + fl];
+          if (f < 0) {
             code[fl] = -1;
           } else {
             const int fs = fsel[f];  // selection lives in device memory: validate here
@@ -318,6 +331,36 @@ __global__ void __launch_bounds__(NTHR, 2)
       if (!wait_all(mb, phase, &abort_s)) break;
       phase ^= 1;
       tc_fence_after();
+      if (t >= nfull) {  // ---- diagonal-only fields: diag_n = Re sum_m conj(U_mn) T_mn
+        const int f = tmap_s[t * FPT + quarter];
+        float re[16], im[16];
+        tmem_cols16(D1 + lane_base, 16 * half, re);  // thread (field q, row m = lane)
+        tmem_cols16(D1 + lane_base, NW + 16 * half, im);
+        if (f >= 0) {  // warp-uniform
+          const float2* Um = U + k * strideU + lane * NW + 16 * half;
+          float sum[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float2 u = Um[i];
+            sum[i] = u.x * re[i] + u.y * im[i];
+          }
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < 16; ++i) sum[i] += __shfl_xor_sync(0xffffffffu, sum[i], off);
+          float v = 0.f;
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (i == lane) v = sum[i];
+          if (lane < 16) {
+            const int n = 16 * half + lane;
+            Xbar[(k * nFrot + f) * (long long)(NW * NW) + n * NW + n] = make_float2(v, 0.f);
+          }
+        }
+        tc_fence_before();
+        __syncthreads();  // TMEM columns and the A buffers are reused by the next tile
+        continue;
+      }
       {  // ---- D1 -> A2: thread (field q, row j) holds T[j][:]; writes column j of T^H.
         // Column half 0 (Re T) -> K block 0, half 1 (Im T) -> K block 1 with a minus sign.
         const int row0 = quarter * NW;
@@ -342,13 +385,13 @@ __global__ void __launch_bounds__(NTHR, 2)
       phase ^= 1;
       tc_fence_after();
       {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][n] for n in its column half
-        const int f = t * FPT + quarter;
-        const int hm = f < nFrot ? (herm[f] & 3) : 0;
-        float2* dst = Xbar + (k * nFrot + (f < nFrot ? f : 0)) * (long long)(NW * NW);
+        const int f = tmap_s[t * FPT + quarter];
+        const int hm = f >= 0 ? (herm[f] & 3) : 0;
+        float2* dst = Xbar + (k * nFrot + (f >= 0 ? f : 0)) * (long long)(NW * NW);
         float re[16], im[16];
         tmem_cols16(D2 + lane_base, 16 * half, re);
         tmem_cols16(D2 + lane_base, NW + 16 * half, im);
-        if (f < nFrot) {  // warp-uniform
+        if (f >= 0) {  // warp-uniform
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int n = 16 * half + i;
@@ -358,7 +401,7 @@ __global__ void __launch_bounds__(NTHR, 2)
           }
         }
         __syncthreads();  // both column halves of every field are staged
-        if (f < nFrot && hm == 1) {  // Hermitian part P = (Y^H + Y)/2; P[n][m] = conj(P[m][n])
+        if (f >= 0 && hm == 1) {  // Hermitian part P = (Y^H + Y)/2; P[n][m] = conj(P[m][n])
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int n = 16 * half + i;
@@ -381,11 +424,13 @@ __global__ void __launch_bounds__(NTHR, 2)
 
 }  // namespace
 
-bool wbg_rotate_tc_supported(int nw, int fp64) { return !fp64 && nw == NW; }
+bool wbg_rotate_tc_supported(int nw, int fp64, int nFrot) {
+  return !fp64 && nw == NW && nFrot >= 1 && nFrot <= TMAP_MAX - 2 * FPT;  // the tile map fits its array
+}
 
 int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                       int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
-  if (nw != NW) return WBG_ERR_SIZE;
+  if (nw != NW || nFrot > TMAP_MAX - 2 * FPT) return WBG_ERR_SIZE;
   if (nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return WBG_ERR_CUDA;
