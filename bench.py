@@ -209,7 +209,9 @@ def probe_peak(torch, fp64):
 
 
 def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
-    """Algorithmic work per launch of the given stage (per k-point figures as defined in the design doc)."""
+    """Algorithmic work per launch of the given stage: HBM bytes of the fields written and read
+    back (R->k, 2 F nw^2 s per k-point), 20 nw^3 FP64-equivalent flops per matrix (eigh), 16 nw^3
+    flops per field (rotation), 9 nw^2 s bytes per k-point (Omega)."""
     n = NW
     per_launch_ms = ms_total / max(n_calls, 1)
     if stage == 'eigh' and precision == 'fp64':

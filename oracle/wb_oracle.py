@@ -949,7 +949,7 @@ class OpticalConductivity:
 
 
 # ---------------------------------------------------------------------------
-# Driver (run_grid.py:118-403, grid/grid.py:149-189, grid/Kpoint.py:75-77)
+# run() over the K-points of a grid (run_grid.py:118-403, grid/grid.py:149-189, grid/Kpoint.py:75-77)
 # ---------------------------------------------------------------------------
 def block_shifts(NKdiv, NKFFT):
     """K-points of the division grid (C order) and their dK = K/NKFFT."""
