@@ -56,7 +56,6 @@ WBG_D long long corner_row(const wbg_tetra_grid& g, const int* __restrict__ bloc
   return (long long)row * nk + (jj[0] * g.fft[1] + jj[1]) * g.fft[2] + jj[2];
 }
 
-WBG_D int warp_sum_i(int v) { return __reduce_add_sync(0xffffffffu, v); }
 WBG_D int warp_min_i(int v) { return __reduce_min_sync(0xffffffffu, v); }
 WBG_D int warp_max_i(int v) { return __reduce_max_sync(0xffffffffu, v); }
 
