@@ -332,10 +332,9 @@ class DataK:
         return A
 
     def delE_K(self):  # data_K.py:236-242
-        d = np.einsum("klla->kla", self.Xbar('Ham', 1))
-        if np.abs(d.imag).max() > 1e-10:
-            raise RuntimeError("The band derivatives have considerable imaginary part")
-        return d.real
+        """Re diag(V).  The reference's guard compares the imaginary part of |diag(V)|, which is
+        always zero, so it never raises: the real part is taken whatever the imaginary part."""
+        return np.einsum("klla->kla", self.Xbar('Ham', 1)).real
 
     # --- band groups (data_K.py:172-198, grid/tetrahedron.py:132-162) ---
     def get_bands_in_range_groups_ik(self, ik, emin, emax, degen_thresh=-1, sea=False):
@@ -830,6 +829,18 @@ class DOS(CumDOS):  # calculators/static.py:203-207 (fder 1)
     fder = 1
 
 
+class Spin(StaticCalculator):  # calculators/static.py:217-228: Re tr_G S (formula/covariant.py:331-335)
+    fder = 0
+
+    @staticmethod
+    def Formula(data_K, **_):
+        return data_K.covariant('SS')
+
+    def __call__(self, data_K):
+        r = super().__call__(data_K)
+        return EnergyResult(r.Energies, r.data * data_K.cell_volume)
+
+
 class Ohmic_FermiSea(StaticCalculator):  # calculators/static.py:379-390
     fder = 0
     Formula = InvMass
@@ -904,21 +915,66 @@ def fermi_dirac(E, mu, kBT):
     return res
 
 
-class OpticalConductivity:
+class DynamicCalculator:
+    """calculators/dynamic.py:26-114: per k-point, every ordered pair of degenerate groups
+    (G1, G2) with energies (E1, E2) that `nonzero` keeps contributes
+    factor_omega(E1, E2)[w] * (FD(E2) - FD(E1))[E_F] * M(G1, G2), M = sum over n in G1, m in G2
+    of the formula's element tensor I[k, n, m, ...]; the sum is scaled by
+    constant_factor / (nk * cell volume) and laid out as [E_F, w, components]."""
+    dtype = complex
+    constant_factor = 1.
+
     def __init__(self, Efermi, omega, kBT=0, smr_fixed_width=0.1, smr_type='Lorentzian', degen_thresh=1e-4,
                  kwargs_formula=None):
         self.Efermi = np.array(Efermi, dtype=float).reshape(-1)
         self.omega = np.array(omega, dtype=float)
         self.kBT = kBT
         self.smr_fixed_width = smr_fixed_width
+        if smr_type not in ('Lorentzian', 'Gaussian'):
+            raise ValueError(f"Invalid smearing type {smr_type}")
         self.smr_type = smr_type
         self.degen_thresh = degen_thresh
         self.kwargs_formula = dict(kwargs_formula or {})
         self.eocc1max = self.Efermi.min() - 30 * kBT
         self.eocc0min = self.Efermi.max() + 30 * kBT
 
-    def nonzero(self, E1, E2):
+    def smear(self, x):  # dynamic.py:50-55
+        if self.smr_type == 'Lorentzian':
+            return lorentzian(x, self.smr_fixed_width)
+        return gaussian(x, self.smr_fixed_width)
+
+    def nonzero(self, E1, E2):  # dynamic.py:65-69
         return not ((E1 < self.eocc1max and E2 < self.eocc1max) or (E1 > self.eocc0min and E2 > self.eocc0min))
+
+    def external(self, data_K):  # formula/formula.py:12-29
+        return self.kwargs_formula.get('external_terms', True) and not data_K.force_internal_terms_only
+
+    def elements(self, data_K):
+        """I[k, n, m, comp] of the formula (its trace_ln sums it over n in G1, m in G2)."""
+        raise NotImplementedError
+
+    def __call__(self, data_K):
+        I = self.elements(data_K)
+        ncomp = int(np.prod(I.shape[3:]))
+        restot = np.zeros((len(self.omega), len(self.Efermi) * ncomp), dtype=self.dtype)
+        for ik in range(data_K.nk):
+            groups = data_K.get_bands_in_range_groups_ik(ik, -np.inf, np.inf, self.degen_thresh)
+            pairs = [(gm, gn, Em, En) for gm, Em in groups.items() for gn, En in groups.items()
+                     if self.nonzero(Em, En)]
+            if not pairs:
+                continue
+            M = np.array([I[ik, np.arange(*p[0])].sum(axis=0)[np.arange(*p[1])].sum(axis=0) for p in pairs])
+            fE = np.array([fermi_dirac(p[3], self.Efermi, self.kBT) - fermi_dirac(p[2], self.Efermi, self.kBT)
+                           for p in pairs])
+            fw = np.array([self.factor_omega(p[2], p[3]) for p in pairs]).T
+            restot += fw @ (fE[:, :, None] * M.reshape(len(pairs), -1)[:, None, :]).reshape(len(pairs), -1)
+        restot = restot.reshape((len(self.omega), len(self.Efermi)) + I.shape[3:]).swapaxes(0, 1)
+        restot = restot * (self.constant_factor / (data_K.nk * data_K.cell_volume))
+        return EnergyResult([self.Efermi, self.omega], restot)
+
+
+class OpticalConductivity(DynamicCalculator):  # dynamic.py:170-196
+    constant_factor = FACTOR_OPT
 
     def factor_omega(self, E1, E2):
         arg = E2 - E1 - self.omega
@@ -927,25 +983,130 @@ class OpticalConductivity:
             cfac.imag = np.pi * gaussian(arg, self.smr_fixed_width)
         return (E2 - E1) * cfac
 
-    def __call__(self, data_K):
-        external = self.kwargs_formula.get('external_terms', True) and not data_K.force_internal_terms_only
-        A = data_K.get_A_H(external_terms=external)
-        AA = 1j * A[:, :, :, :, None] * A.swapaxes(1, 2)[:, :, :, None, :]   # dynamic.py:172-175
-        restot = np.zeros((len(self.omega), len(self.Efermi) * 9), dtype=complex)
-        for ik in range(data_K.nk):
-            groups = data_K.get_bands_in_range_groups_ik(ik, -np.inf, np.inf, self.degen_thresh)
-            pairs = [(gm, gn, Em, En) for gm, Em in groups.items() for gn, En in groups.items()
-                     if self.nonzero(Em, En)]
-            if not pairs:
-                continue
-            M = np.array([AA[ik, np.arange(*p[0])].sum(axis=0)[np.arange(*p[1])].sum(axis=0) for p in pairs])
-            fE = np.array([fermi_dirac(p[3], self.Efermi, self.kBT) - fermi_dirac(p[2], self.Efermi, self.kBT)
-                           for p in pairs])
-            fw = np.array([self.factor_omega(p[2], p[3]) for p in pairs]).T
-            restot += fw @ (fE[:, :, None] * M.reshape(len(pairs), -1)[:, None, :]).reshape(len(pairs), -1)
-        restot = restot.reshape((len(self.omega), len(self.Efermi), 3, 3)).swapaxes(0, 1)
-        restot *= FACTOR_OPT / (data_K.nk * data_K.cell_volume)
-        return EnergyResult([self.Efermi, self.omega], restot)
+    def elements(self, data_K):  # Formula_OptCond: i A^a_nm A^b_mn
+        A = data_K.get_A_H(external_terms=self.external(data_K))
+        return 1j * A[:, :, :, :, None] * A.swapaxes(1, 2)[:, :, :, None, :]
+
+
+class JDOS(DynamicCalculator):  # dynamic.py:133-162
+    dtype = float
+
+    def nonzero(self, E1, E2):
+        return (E1 < self.Efermi.max()) and (E2 > self.Efermi.min()) and (
+            self.omega.min() - 5 * self.smr_fixed_width < E1 - E2 < self.omega.max() + 5 * self.smr_fixed_width)
+
+    def factor_omega(self, E1, E2):
+        return self.smear(E1 - E2 - self.omega)
+
+    def elements(self, data_K):  # Formula_dyn_ident: |G1| |G2|
+        return np.ones((data_K.nk, data_K.num_wann, data_K.num_wann))
+
+
+def spin_velocity(data_K, kind, external_terms=True):
+    """SpinVelocity.matrix[k, m, n, a, s] = <m|{v^a, S^s}|n> / 2 (formula/covariant.py:689-756):
+    J' of the chosen kind, then (J' + J'^dagger) / 2 over the band indices."""
+    E = data_K.E_K
+    SS = data_K.Xbar('SS')
+    if kind == 'simple':
+        V = data_K.Xbar('Ham', 1)
+        if external_terms:  # Velocity (covariant.py:321-328): + i A_mn (E_m - E_n)
+            V = V + 1j * data_K.Xbar('AA') * (E[:, :, None, None] - E[:, None, :, None])
+        J = np.einsum('klms,kmna->klnas', SS, V)
+    elif kind in ('qiao', 'ryoo'):
+        if not external_terms:
+            raise NotImplementedError(f"spin Hall {kind} without external terms")
+        if kind == 'qiao':
+            D = data_K.D_H
+            K = -1j * data_K.Xbar('SR') + np.einsum('knls,klma->knmas', SS, D)
+            L = -1j * data_K.Xbar('SHR') + np.einsum('knls,klma->knmas', data_K.Xbar('SH'), D)
+            J = (data_K.delE_K()[:, None, :, :, None] * SS[:, :, :, None, :]
+                 + E[:, None, :, None, None] * K - L)
+        else:
+            J = -1j * (E[:, None, :, None, None] * data_K.Xbar('SA') - data_K.Xbar('SHA'))
+            J = J + np.einsum('knls,klma->knmas', SS, data_K.Xbar('Ham', 1))
+    else:
+        raise ValueError(f"spin_current_type must be `qiao` or `ryoo` or `simple`, not {kind}")
+    return (J + J.swapaxes(1, 2).conj()) / 2
+
+
+class SHC(DynamicCalculator):  # dynamic.py:199-236 (Formula_SHC, SHC.factor_omega)
+    constant_factor = -FACTOR_AHC  # factors.py: factor_shc
+
+    def __init__(self, SHC_type='ryoo', shc_abc=None, **kw):
+        super().__init__(**kw)
+        self.SHC_type = SHC_type
+        self.shc_abc = shc_abc
+
+    def factor_omega(self, E1, E2):
+        arg = E1 - E2 - self.omega
+        cfac = 1. / (arg - 1j * self.smr_fixed_width)
+        if self.smr_type != 'Lorentzian':
+            cfac.imag = np.pi * self.smear(arg)
+        return cfac / 2
+
+    def elements(self, data_K):  # imAB[k, n, m, a, b, s] = Im(J[n, m, a, s] (-i A_H)[m, n, b])
+        ext = self.external(data_K)
+        J = spin_velocity(data_K, self.SHC_type, external_terms=ext)
+        B = -1j * data_K.get_A_H(external_terms=ext)
+        imAB = np.imag(J[:, :, :, :, None, :] * B.swapaxes(1, 2)[:, :, :, None, :, None])
+        if self.shc_abc is not None:
+            a, b, c = (x - 1 for x in self.shc_abc)
+            imAB = imAB[:, :, :, a, b, c]
+        return imAB
+
+
+class ShiftCurrent(DynamicCalculator):  # dynamic.py:239-316 (ShiftCurrentFormula, ShiftCurrent)
+    dtype = float
+    constant_factor = hbar / elementary_charge * np.pi * elementary_charge ** 3 / (4 * hbar ** 2)
+
+    def __init__(self, sc_eta, **kw):
+        super().__init__(**kw)
+        self.sc_eta = sc_eta
+
+    def factor_omega(self, E1, E2):
+        return self.smear(E1 - E2 - self.omega) + self.smear(E2 - E1 - self.omega)
+
+    def elements(self, data_K):
+        D = data_K.D_H
+        V = data_K.Xbar('Ham', 1)
+        W = data_K.Xbar('Ham', 2)
+        dinv = data_K.dEig_inv.swapaxes(2, 1)
+        E = data_K.E_K
+        dE = E[:, :, None] - E[:, None, :]
+        Dp = -V * (dE / (dE ** 2 + self.sc_eta ** 2))[:, :, :, None]  # principal-value D
+        ein = np.einsum
+        # [k, n, m, c, a]: the generalised-derivative direction a is the last index
+        sum_HD = (ein('knlc,klma->knmca', V, Dp) - ein('knnc,knma->knmca', V, Dp)
+                  - ein('knla,klmc->knmca', Dp, V) + ein('knma,kmmc->knmca', Dp, V))
+        DV = (ein('knmc,knna->knmca', D, V) - ein('knmc,kmma->knmca', D, V)
+              + ein('knma,knnc->knmca', D, V) - ein('knma,kmmc->knmca', D, V))
+        Ader = 1j * (W + sum_HD + DV) * dinv[:, :, :, None, None]
+        ext = self.external(data_K)
+        if ext:
+            Ab = data_K.Xbar('AA')
+            dAb = data_K.Xbar('AA', 1)
+            sum_AD = (ein('knlc,klma->knmca', Ab, Dp) - ein('knnc,knma->knmca', Ab, Dp)
+                      - ein('knla,klmc->knmca', Dp, Ab) + ein('knma,kmmc->knmca', Dp, Ab))
+            AD = (ein('knnc,knma->knmac', Ab, D) - ein('kmmc,knma->knmac', Ab, D)
+                  + ein('knna,knmc->knmac', Ab, D) - ein('kmma,knmc->knmac', Ab, D))
+            AA = ein('knnb,knma->knmab', Ab, Ab) - ein('kmmb,knma->knmab', Ab, Ab)
+            Ader = Ader + dAb + AD - 1j * AA + sum_AD
+        A = data_K.get_A_H(external_terms=ext)
+        I = -ein('knmca,kmnb->knmabc', Ader, A).imag
+        return I + I.swapaxes(4, 5)
+
+
+class InjectionCurrent(DynamicCalculator):  # dynamic.py:319-360
+    constant_factor = -np.pi * elementary_charge ** 3 / hbar ** 2 * TAU_UNIT
+
+    def factor_omega(self, E1, E2):
+        return self.smear(E1 - E2 - self.omega)
+
+    def elements(self, data_K):  # Imn[k, m, n, a, b, c] = (v_m - v_n)^a A^b_mn A^c_nm
+        A = data_K.get_A_H(external_terms=self.external(data_K))
+        v = data_K.delE_K()
+        dv = v[:, :, None, :] - v[:, None, :, :]
+        return np.einsum('kmna,kmnb,knmc->kmnabc', dv, A, A)
 
 
 # ---------------------------------------------------------------------------

@@ -13,7 +13,7 @@ Fixtures written (all small, complex128/float64):
 * ``random_system.npz`` + ``random_results.npz`` -- the reference's own test
   system ``tests/data/random`` (nw=6, nR=20) and its stored golden results
   ``tests/reference/integrate_files/random-{ahc,Morb,opt_conductivity,dos,cumdos,
-  conductivity_ohmic,conductivity_ohmic_fsurf}_iter-0000.npz``
+  conductivity_ohmic,conductivity_ohmic_fsurf,spin,opt_SHCqiao,opt_SHCryoo}_iter-0000.npz``
   (settings of ``tests/test_run.py:653-669``: NK=6, NKFFT=3, E_F=linspace(-2,2,5)).
 * ``fe_system.npz`` + ``fe_formula.npz`` -- ``tests/reference/systems/system_Fe_sym_W90_OSD``
   (Ham, AA, BB, CC only) and the stored formula traces
@@ -37,6 +37,11 @@ Fixtures written (all small, complex128/float64):
   MDRS model (2 iterations, adpt_fac 2, adpt_mesh (2,1,3), AHC / BerryDipole_FermiSea), and
   AHC / DOS with tetra=True on the random system (2 iterations).
   ``python make_golden.py <reference root> refine`` writes only this file.
+* ``dynamic_ref.npz`` -- JDOS, SHC (simple / qiao / ryoo, one shc_abc component),
+  ShiftCurrent, InjectionCurrent and the static Spin of the reference's ``run`` on the random
+  system (NKdiv 2, NKFFT 3), Lorentzian and Gaussian smearing.
+  ``python make_golden.py <reference root> dynamic`` writes only this file; ``random`` rewrites
+  only the random-system files (its spin matrices and the stored spin / SHC results included).
 """
 import os
 import sys
@@ -99,17 +104,19 @@ def run_ref(wb, system, NKdiv, NKFFT, calculators):
     return {k: res.results[k].data for k in calculators}
 
 
-def main(ref_root):
-    wb = setup_reference(ref_root)
-    from wannierberri.system.system_R import System_R
-    from wannierberri import calculators as calc
-    from wbgpu import models
+RANDOM_KEYS = ['Ham', 'AA', 'BB', 'CC', 'SS', 'SA', 'SHA', 'SR', 'SH', 'SHR']
+RANDOM_RESULTS = ['ahc', 'Morb', 'opt_conductivity', 'dos', 'cumdos', 'conductivity_ohmic',
+                  'conductivity_ohmic_fsurf', 'spin', 'opt_SHCqiao', 'opt_SHCryoo']
 
-    # ---- 1. the reference's own random system and stored results
+
+def random_fixtures(ref_root):
+    """---- 1. the reference's random test system (with its spin matrices) and its stored
+    results of tests/test_run.py:653-669."""
+    from wannierberri.system.system_R import System_R
     rs = System_R.from_npz(path=os.path.join(ref_root, 'tests', 'data', 'random'), legacy=True)
-    np.savez_compressed(os.path.join(HERE, 'random_system.npz'), **pack_system('', rs, ['Ham', 'AA', 'BB', 'CC']))
+    np.savez_compressed(os.path.join(HERE, 'random_system.npz'), **pack_system('', rs, RANDOM_KEYS))
     res = {}
-    for q in ['ahc', 'Morb', 'opt_conductivity', 'dos', 'cumdos', 'conductivity_ohmic', 'conductivity_ohmic_fsurf']:
+    for q in RANDOM_RESULTS:
         f = np.load(os.path.join(ref_root, 'tests', 'reference', 'integrate_files', f'random-{q}_iter-0000.npz'),
                     allow_pickle=True)
         res[q + '_data'] = f['data']
@@ -117,7 +124,44 @@ def main(ref_root):
         if 'Energies_1' in f:
             res[q + '_E1'] = f['Energies_1']
     np.savez_compressed(os.path.join(HERE, 'random_results.npz'), **res)
+    return rs
 
+
+def dynamic_fixtures(wb, rs):
+    """---- 7. dynamic calculators (calculators/dynamic.py) and the static Spin of the
+    reference's run on the random system (NKdiv 2 x NKFFT 3): JDOS, SHC of the three
+    spin-current kinds (and one shc_abc component), ShiftCurrent and InjectionCurrent, with
+    Lorentzian and Gaussian smearing, at zero and finite temperature."""
+    from wannierberri import calculators as calc
+    dyn = calc.dynamic
+    out = {}
+    EF = np.array([-1.0, 0.0, 1.0, 2.0])
+    om = np.linspace(0.0, 6.0, 13)
+    out['EF'], out['omega'] = EF, om
+    pL = dict(Efermi=EF, omega=om, smr_fixed_width=0.3)
+    pG = dict(Efermi=EF, omega=om, smr_fixed_width=0.2, smr_type='Gaussian', kBT=0.05)
+    cs = {'jdos_L': dyn.JDOS(**pL), 'jdos_G': dyn.JDOS(**pG),
+          'shc_simple_L': dyn.SHC(SHC_type='simple', **pL),
+          'shc_simple_int_G': dyn.SHC(SHC_type='simple', kwargs_formula={'external_terms': False}, **pG),
+          'shc_qiao_L': dyn.SHC(SHC_type='qiao', **pL), 'shc_ryoo_G': dyn.SHC(SHC_type='ryoo', **pG),
+          'shc_ryoo_abc_L': dyn.SHC(SHC_type='ryoo', shc_abc=(1, 2, 3), **pL),
+          'shift_G': dyn.ShiftCurrent(sc_eta=0.1, **pG), 'shift_int_L': dyn.ShiftCurrent(
+              sc_eta=0.1, kwargs_formula={'external_terms': False}, **pL),
+          'injection_G': dyn.InjectionCurrent(**pG), 'injection_L': dyn.InjectionCurrent(**pL),
+          'spin': calc.static.Spin(Efermi=np.linspace(-3, 3, 11))}
+    for k, v in run_ref(wb, rs, 2, 3, cs).items():
+        out['random_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'dynamic_ref.npz'), **out)
+
+
+def main(ref_root):
+    wb = setup_reference(ref_root)
+    from wannierberri.system.system_R import System_R
+    from wannierberri import calculators as calc
+    from wbgpu import models
+
+    # ---- 1. the reference's own random system and stored results
+    rs = random_fixtures(ref_root)
     # ---- 2. Fe formula system and stored formula traces
     fe = System_R.from_npz(os.path.join(ref_root, 'tests', 'reference', 'systems', 'system_Fe_sym_W90_OSD'),
                            matrices=['Ham', 'AA', 'BB', 'CC'])
@@ -187,6 +231,7 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, 'evaluate_k_ref.npz'), **ev)
     tetra_fixtures(wb, rs)
     refine_fixtures(wb, rs)
+    dynamic_fixtures(wb, rs)
     print("wrote fixtures to", HERE)
 
 
@@ -263,10 +308,13 @@ def refine_fixtures(wb, rs):
 if __name__ == '__main__':
     root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
     section = sys.argv[2] if len(sys.argv) > 2 else None
-    if section in ('tetra', 'refine'):  # one section only
+    if section in ('random', 'tetra', 'refine', 'dynamic'):  # one section only
         wb = setup_reference(root)
         from wannierberri.system.system_R import System_R
         rs = System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True)
-        (tetra_fixtures if section == 'tetra' else refine_fixtures)(wb, rs)
+        if section == 'random':
+            random_fixtures(root)
+        else:
+            {'tetra': tetra_fixtures, 'refine': refine_fixtures, 'dynamic': dynamic_fixtures}[section](wb, rs)
     else:
         main(root)

@@ -39,13 +39,17 @@ def random_run(random_sys, random_res):
     EF = np.linspace(-2, 2, 5)
     calcs = {'ahc': O.AHC(Efermi=EF), 'Morb': O.Morb(Efermi=EF), 'dos': O.DOS(Efermi=EF), 'cumdos': O.CumDOS(Efermi=EF),
              'conductivity_ohmic': O.Ohmic_FermiSea(Efermi=EF), 'conductivity_ohmic_fsurf': O.Ohmic_FermiSurf(Efermi=EF),
-             'opt_conductivity': O.OpticalConductivity(Efermi=np.array([17.0, 18.0]), omega=np.arange(0.0, 7.1, 1.0),
-                                                       smr_fixed_width=0.20, smr_type="Gaussian")}
+             'spin': O.Spin(Efermi=EF)}
+    popt = dict(Efermi=np.array([17.0, 18.0]), omega=np.arange(0.0, 7.1, 1.0), smr_fixed_width=0.20,
+                smr_type="Gaussian")
+    calcs['opt_conductivity'] = O.OpticalConductivity(**popt)
+    calcs['opt_SHCqiao'] = O.SHC(SHC_type="qiao", **popt)
+    calcs['opt_SHCryoo'] = O.SHC(SHC_type="ryoo", **popt)
     return O.run(random_sys, NKdiv=(2, 2, 2), NKFFT=(3, 3, 3), calculators=calcs)
 
 
 @pytest.mark.parametrize("quant", ['ahc', 'Morb', 'opt_conductivity', 'dos', 'cumdos', 'conductivity_ohmic',
-                                   'conductivity_ohmic_fsurf'])
+                                   'conductivity_ohmic_fsurf', 'spin', 'opt_SHCqiao', 'opt_SHCryoo'])
 def test_random_golden(random_run, random_res, quant):
     """Same acceptance rule as the reference: abs err < 1e-8 * max|ref| (tests/common_comparers.py:189-196)."""
     ref = random_res[quant + '_data']
@@ -252,3 +256,38 @@ def test_refine_tetra_golden(random_sys, golden_dir):
     for k in calcs:
         ref = g['tetra_random_' + k]
         assert np.max(np.abs(r[k].data - ref)) < 1e-8 * np.max(np.abs(ref)), k
+
+
+def dynamic_calculators(EF, om):
+    """The calculators of dynamic_ref.npz (tests/golden/make_golden.py, section 7)."""
+    pL = dict(Efermi=EF, omega=om, smr_fixed_width=0.3)
+    pG = dict(Efermi=EF, omega=om, smr_fixed_width=0.2, smr_type='Gaussian', kBT=0.05)
+    return {'jdos_L': O.JDOS(**pL), 'jdos_G': O.JDOS(**pG),
+            'shc_simple_L': O.SHC(SHC_type='simple', **pL),
+            'shc_simple_int_G': O.SHC(SHC_type='simple', kwargs_formula={'external_terms': False}, **pG),
+            'shc_qiao_L': O.SHC(SHC_type='qiao', **pL), 'shc_ryoo_G': O.SHC(SHC_type='ryoo', **pG),
+            'shc_ryoo_abc_L': O.SHC(SHC_type='ryoo', shc_abc=(1, 2, 3), **pL),
+            'shift_G': O.ShiftCurrent(sc_eta=0.1, **pG),
+            'shift_int_L': O.ShiftCurrent(sc_eta=0.1, kwargs_formula={'external_terms': False}, **pL),
+            'injection_G': O.InjectionCurrent(**pG), 'injection_L': O.InjectionCurrent(**pL),
+            'spin': O.Spin(Efermi=np.linspace(-3, 3, 11))}
+
+
+@pytest.fixture(scope="module")
+def dynamic_ref(golden_dir):
+    return np.load(os.path.join(golden_dir, 'dynamic_ref.npz'))
+
+
+@pytest.fixture(scope="module")
+def dynamic_run(random_sys, dynamic_ref):
+    return O.run(random_sys, (2, 2, 2), (3, 3, 3), dynamic_calculators(dynamic_ref['EF'], dynamic_ref['omega']))
+
+
+@pytest.mark.parametrize("quant", ['jdos_L', 'jdos_G', 'shc_simple_L', 'shc_simple_int_G', 'shc_qiao_L', 'shc_ryoo_G',
+                                   'shc_ryoo_abc_L', 'shift_G', 'shift_int_L', 'injection_G', 'injection_L', 'spin'])
+def test_dynamic_golden(dynamic_run, dynamic_ref, quant):
+    """JDOS, SHC, shift and injection currents, Spin: the reference's run() on the random system."""
+    ref = dynamic_ref['random_' + quant]
+    got = dynamic_run[quant].data
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))
