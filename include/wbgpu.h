@@ -177,13 +177,16 @@ int wbg_device_flags(unsigned int* flags, int clear);
  * formula WBG_FORMULA_IDENTITY: group size (CumDOS / DOS, calculators/static.py:192-214), 1
  *   component; WBG_FORMULA_INVMASS: the inverse-mass tensor dV^b/dk_d (formula/elementary.py:28-34,
  *   Ohmic_FermiSea), Xbar: V at iV..iV+2, d^2H/dk_b dk_d at iW..iW+8, 9 components;
- *   WBG_FORMULA_VELVEL: in-group V^a V^b (formula/covariant.py:817-820, Ohmic_FermiSurf), 9.
+ *   WBG_FORMULA_VELVEL: in-group V^a V^b (formula/covariant.py:817-820, Ohmic_FermiSurf), 9;
+ *   WBG_FORMULA_DIAG: Re X^c_nn of the 3-component field at iV (the spin expectation of
+ *   calculators/static.py:217-228 Spin, formula/covariant.py:331-335), 3.
  * sea != 0: Fermi-sea weights (fder 0), sea == 0: Fermi-surface groups only (fder >= 1; the
  * caller takes the finite differences over the extended levels).  hist [nEF][ncomp] (double)
  * is accumulated; component (b, d) at 3 b + d.  Xbar may be NULL for WBG_FORMULA_IDENTITY. */
 #define WBG_FORMULA_IDENTITY 0
 #define WBG_FORMULA_INVMASS 1
 #define WBG_FORMULA_VELVEL 2
+#define WBG_FORMULA_DIAG 6
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
                    int formula, int sea, double* hist, int fp64, void* stream);
 
@@ -217,8 +220,8 @@ int wbg_tetra_select(const double* E, const double* Ecorner, const int* corner_s
 /* Per-band formula values for the tetrahedron method: the group traces of the histogram
  * kernels, written per band instead of binned.  P [nk][nw][ncomp] = trace of the band's group
  * / group size for sel 1, the trace of the sea group [0, bandmax) on band 0 for sel 2 (Morb:
- * T(bandmax) - T(0)), 0 otherwise.  formula: WBG_FORMULA_IDENTITY / INVMASS / VELVEL (as
- * wbg_berry_scan), WBG_FORMULA_OMEGA (wbg_berry_omega, 3), WBG_FORMULA_DEROMEGA
+ * T(bandmax) - T(0)), 0 otherwise.  formula: WBG_FORMULA_IDENTITY / INVMASS / VELVEL / DIAG
+ * (as wbg_berry_scan; DIAG reads the field at fields->V), WBG_FORMULA_OMEGA (wbg_berry_omega, 3), WBG_FORMULA_DEROMEGA
  * (wbg_berry_deromega, 9, (c, d) at 3 c + d), WBG_FORMULA_MORB (wbg_berry_morb, 3).  fields:
  * field indices into Xbar (unused entries ignored); fp64 0 / 1 as the histogram kernels. */
 #define WBG_FORMULA_OMEGA 3
@@ -299,6 +302,46 @@ int wbg_kubo_workspace_size(int nw, int nk, int nEF, size_t* bytes);
 int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
              const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
              size_t workspace_bytes, double* out, int fp64, void* stream);
+
+/* ---- dynamic calculators (calculators/dynamic.py:26-360) -------------------------------------
+ * The Kubo pair scan of wbg_kubo for every formula of DynamicCalculator: per k-point, groups
+ * over all bands (degen_thresh), each ordered pair (G1, G2) kept by `nonzero` (dynamic.py:65-69;
+ * JDOS: E1 < EFmax, E2 > EFmin, omega_min - 5 eta < E1 - E2 < omega_max + 5 eta, :158-162) adds
+ * f_w(E1, E2) (FD(E2) - FD(E1)) M^c to out[iEF][iw][c] (complex128, accumulated, unnormalised).
+ * formula / M^c (n in G1, m in G2 summed; A = i D + Abar with Abar only when external_terms):
+ *   WBG_DYN_OPTCOND    i A^a_nm A^b_mn, c = 3 a + b (OpticalConductivity, :170-196; = wbg_kubo)
+ *   WBG_DYN_JDOS       1, one component (JDOS, :133-162)
+ *   WBG_DYN_SHC_*      Im(J^{as}_nm (-i A^b_mn)), c = 9 a + 3 b + s, J the spin current
+ *                      (J' + J'^dagger) / 2 of formula/covariant.py:721-756 of kind SIMPLE / QIAO /
+ *                      RYOO (QIAO and RYOO need external_terms); f_w = 1 / (E1 - E2 - w - i eta) / 2
+ *                      (SHC, :199-236)
+ *   WBG_DYN_SHIFT      -Im(dA^{ca}_nm A^b_mn) + (b <-> c), c-index 9 a + 3 b + c, dA the generalised
+ *                      derivative with the principal-value D of broadening sc_eta (ShiftCurrent,
+ *                      :239-316); f_w = smear(E1 - E2 - w) + smear(E2 - E1 - w), real
+ *   WBG_DYN_INJECTION  (v^a_n - v^a_m) A^b_nm A^c_mn, 9 a + 3 b + c (InjectionCurrent, :319-360);
+ *                      f_w = smear(E1 - E2 - w)
+ * smear: Lorentzian or (params->gaussian) Gaussian of width params->eta (utility.py:147-168).
+ * spec: the first Xbar field of each quantity (-1 where unused): V (3), A (3), W = d2H (9),
+ * dA = dAbar/dk (9, (c, d) at 3 c + d), S = SS (3), SH (3), SA, SHA, SR, SHR (9, (a, s) at
+ * 3 a + s).  Xbar may be NULL for JDOS.  ncomp: wbg_dynamic_ncomp(formula) (9, 1 or 27). */
+#define WBG_DYN_OPTCOND 0
+#define WBG_DYN_JDOS 1
+#define WBG_DYN_SHC_SIMPLE 2
+#define WBG_DYN_SHC_QIAO 3
+#define WBG_DYN_SHC_RYOO 4
+#define WBG_DYN_SHIFT 5
+#define WBG_DYN_INJECTION 6
+typedef struct {
+  int formula, external_terms;
+  int V, A, W, dA, S, SH, SA, SHA, SR, SHR;
+  double sc_eta;               /* ShiftCurrent */
+  double omega_min, omega_max; /* JDOS `nonzero` window */
+} wbg_dynamic_spec;
+int wbg_dynamic_ncomp(int formula);
+int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* bytes);
+int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spec, int nw, int nk,
+                const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
+                size_t workspace_bytes, double* out, int fp64, void* stream);
 
 /* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);

@@ -136,6 +136,21 @@ int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int n
                       workspace_bytes, out, fp64, (cudaStream_t)stream);
 }
 
+int wbg_dynamic_ncomp(int formula) { return ::wbg_dynamic_ncomp_impl(formula); }
+
+int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* bytes) {
+  if (!bytes || nw < 1 || nk < 1 || nEF < 1 || wbg_dynamic_ncomp(formula) == 0) return WBG_STATUS_BAD_ARGUMENT;
+  *bytes = wbg_dynamic_workspace_bytes(formula, nw, nk, nEF);
+  return WBG_STATUS_OK;
+}
+
+int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spec, int nw, int nk,
+                const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
+                size_t workspace_bytes, double* out, int fp64, void* stream) {
+  return wbg_dynamic_run(E, Xbar, nFbar, spec, nw, nk, params, efermi, omega, workspace, workspace_bytes, out, fp64,
+                         (cudaStream_t)stream);
+}
+
 int wbg_tetra_select(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks, int nblocks,
                      const wbg_tetra_grid* grid, int nw, double EF0, double EF1, double degen_thresh, int sea,
                      signed char* sel, void* stream) {
@@ -159,6 +174,7 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
     case WBG_FORMULA_IDENTITY:
     case WBG_FORMULA_INVMASS:
     case WBG_FORMULA_VELVEL:
+    case WBG_FORMULA_DIAG:
       return wbg_berry_scan_run(E, Xbar, nFbar, f->V, f->W, nw, nk, &sp, formula, 0, nullptr, fp64, st, sel, P);
     case WBG_FORMULA_OMEGA:
       return wbg_berry_omega_run(E, Xbar, nFbar, f->V, f->A, f->O, nw, nk, &sp, internal_terms, external_terms,

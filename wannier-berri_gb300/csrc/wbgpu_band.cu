@@ -705,6 +705,8 @@ __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __r
 //        (the generalised derivative Wbar - D Vbar + Vbar D of formula/formula.py:95-118)
 //   WBG_FORMULA_VELVEL    (formula/covariant.py:817-820; Ohmic_FermiSurf) 9 components:
 //        sum_{n' in the group} Re V^a_nn' V^b_n'n
+//   WBG_FORMULA_DIAG      (formula/covariant.py:331-335; Spin)            3 components:
+//        Re X^c_nn of the 3-component field starting at iV
 // per band n; the group sums are binned like the Omega kernel.  sea != 0: Fermi-sea groups
 // (E below the window add to every level, the sea group); sea == 0: Fermi-surface groups only.
 // hist [nEF][ncomp] (component (b, d) at 3 b + d).
@@ -714,7 +716,7 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
                                   int iV, int iW, int nw, int nk, int L, int G, WbgScan sp, int formula, int sea,
                                   double* __restrict__ hist, BandSel bs) {
   typedef typename C2<T>::t V;
-  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
+  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : formula == WBG_FORMULA_DIAG ? 3 : 9;
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][nc]
   double* Es = sh + nc * sp.nEF;                      // [G][nw]
@@ -761,6 +763,8 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
       double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       if (formula == WBG_FORMULA_IDENTITY) {
         t[0] = 1.0;
+      } else if (formula == WBG_FORMULA_DIAG) {
+        for (int c = 0; c < 3; ++c) t[c] = (double)Xk[(iV + c) * nw2 + n * nw + n].x;
       } else if (formula == WBG_FORMULA_INVMASS) {
         for (int b = 0; b < 3; ++b)
           for (int d = 0; d < 3; ++d) t[3 * b + d] = (double)Xk[(iW + 3 * b + d) * nw2 + n * nw + n].x;
@@ -1396,10 +1400,11 @@ int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int
   WbgScan spv = *sp_in;
   if (sel) { spv.nEF = 0; hist = nullptr; }
   const WbgScan* sp = &spv;
-  if (formula < WBG_FORMULA_IDENTITY || formula > WBG_FORMULA_VELVEL) return WBG_ERR_ARG;
+  if ((formula < WBG_FORMULA_IDENTITY || formula > WBG_FORMULA_VELVEL) && formula != WBG_FORMULA_DIAG)
+    return WBG_ERR_ARG;
   if (formula != WBG_FORMULA_IDENTITY && (!Xbar || iV < 0 || iV + 3 > nFbar)) return WBG_ERR_ARG;
   if (formula == WBG_FORMULA_INVMASS && (iW < 0 || iW + 9 > nFbar)) return WBG_ERR_ARG;
-  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : 9;
+  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : formula == WBG_FORMULA_DIAG ? 3 : 9;
   const int L = lanes_for(nw);
   const int G = 128 / L;
   const size_t sm = (size_t)nc * sp->nEF * 8 + (size_t)G * nw * (8 + 72 + 4);

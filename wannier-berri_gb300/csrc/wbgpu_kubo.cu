@@ -1,15 +1,26 @@
-// Kubo optical conductivity (stage 4, dynamic calculators).
+// Dynamic (Kubo-type) calculators (stage 4).
 //
-// Replaces calculators/dynamic.py:71-114 (DynamicCalculator.__call__), 170-181
-// (Formula_OptCond) and 184-196 (OpticalConductivity.factor_omega):
-//   restot[E_F][w][a][b] += sum_{group pairs} f_w(E1,E2) f_E(E1,E2) M^{ab}_{12}
-//   M^{ab}_{12} = sum_{n in G1, m in G2} i A^a_nm A^b_mn,   A = i D + Abar (data_K.py:328-334)
-//   f_E = FD(E2) - FD(E1),   f_w = (E2 - E1) / (E2 - E1 - w - i eta)  (Lorentzian; for the
-//   Gaussian smearing the imaginary part is pi * Gaussian(E2 - E1 - w), utility.py:147-182).
-// kubo_pairs:  one CTA per k-point builds the pair records (groups over all bands,
-//              degen_thresh; pairs pruned by `nonzero`, dynamic.py:65-69).
-// kubo_accum:  one thread per frequency accumulates over the records of a chunk of k-points
-//              in shared memory (FP32), then adds the chunk into out (FP64 atomics).
+// Replaces calculators/dynamic.py:26-360: DynamicCalculator.__call__ (:71-114) with the
+// formulas and frequency factors of OpticalConductivity (:170-196), JDOS (:133-162), SHC
+// (:199-236, spin current of formula/covariant.py:689-756), ShiftCurrent (:239-316) and
+// InjectionCurrent (:319-360):
+//   restot[E_F][w][c] += sum_{group pairs (G1, G2)} f_w(E1, E2) f_E(E1, E2) M^c(G1, G2)
+//   M^c = sum_{n in G1, m in G2} I^c_nm (the formula's trace_ln),  f_E = FD(E2) - FD(E1).
+// Element tensors (D_nm = -V_nm / (E_n - E_m), A = i D + Abar, data_K.py:290-334):
+//   optical conductivity  i A^a_nm A^b_mn                                   9 complex, (a, b)
+//   JDOS                  1                                                 1 real
+//   SHC                   Im(J^{as}_nm (-i A^b_mn))                         27 real, (a, b, s)
+//   shift current         -Im(dA^{ca}_nm A^b_mn) + (b <-> c)                27 real, (a, b, c)
+//   injection current     (v^a_n - v^a_m) A^b_nm A^c_mn                     27 complex, (a, b, c)
+// with J the spin-current matrix (simple / qiao / ryoo) and dA the generalised derivative of
+// A with principal-value D (broadening sc_eta).
+// kubo_pairs:  one CTA per k-point: groups over all bands (degen_thresh), one thread per
+//              ordered pair of groups kept by `nonzero` (dynamic.py:65-69; JDOS :158-162); the
+//              element tensors are computed in place from the band-basis fields, with sums over
+//              the intermediate bands for SHC and the shift current.  One record per pair:
+//              E2 - E1, f_E per level, M (FP32).
+// kubo_accum:  one thread per frequency, a chunk of levels per block (grid z), a chunk of
+//              k-points per block (grid y): FP32 accumulation in shared memory, FP64 atomics.
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_kubo.cuh"
@@ -23,13 +34,235 @@ __device__ double fermi_dirac(double E, double mu, double kBT) {
   return 1.0 / (exp((E - mu) / kBT) + 1.0);
 }
 
-// grid: nk blocks of 128 threads.  Records of k-point k occupy slots [k*P, k*P + count[k]).
+// the three spin-current kinds share SHC's frequency factor
+constexpr int kShcFactor = 100;
+
+__host__ __device__ constexpr int dyn_ncomp(int f) {
+  return f == WBG_DYN_OPTCOND ? 9 : f == WBG_DYN_JDOS ? 1 : 27;
+}
+
+// band-basis fields of one k-point
 template <typename T>
-__global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar, int iV,
-                           int iA, int nw, int external_terms, WbgKubo kp, const double* __restrict__ efermi,
+struct KBand {
+  typedef typename C2<T>::t V;
+  const V* X;
+  const double* E;
+  int nw;
+  long long nw2;
+  wbg_dynamic_spec f;
+  WBG_D V x(int fld, int p, int q) const { return X[fld * nw2 + (long long)p * nw + q]; }
+  WBG_D T dinv(int p, int q) const {  // dEig_inv (data_K.py:290-298)
+    const double d = E[p] - E[q];
+    return fabs(d) < 1e-7 ? T(0) : (T)(1.0 / d);
+  }
+  WBG_D V D(int a, int p, int q) const { return cscale(x(f.V + a, p, q), -dinv(p, q)); }
+  WBG_D V AH(int a, int p, int q) const {
+    V r = cmuli(D(a, p, q));
+    if (f.external_terms) r = cadd(r, x(f.A + a, p, q));
+    return r;
+  }
+  // principal-value D of the shift current: -V_pq (E_p - E_q) / ((E_p - E_q)^2 + eta^2)
+  WBG_D V Dp(int a, int p, int q) const {
+    const double d = E[p] - E[q];
+    return cscale(x(f.V + a, p, q), (T)(-d / (d * d + f.sc_eta * f.sc_eta)));
+  }
+};
+
+// J'[p][q][a][s] of the spin current before (J' + J'^dagger) / 2 (formula/covariant.py:721-756),
+// component 3 a + s
+template <typename T, int F>
+WBG_D void spin_current(const KBand<T>& b, int p, int q, typename C2<T>::t* out) {
+  typedef typename C2<T>::t V;
+  for (int i = 0; i < 9; ++i) out[i] = czero<V>();
+  const int nw = b.nw;
+  const T Eq = (T)b.E[q];
+  for (int l = 0; l < nw; ++l) {
+    V Ls[3], Ra[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const V S = b.x(b.f.S + s, p, l);
+      if (F == WBG_DYN_SHC_QIAO)  // E_q S - SH, against D: E_q (S D) - (SH D)
+        Ls[s] = csub(cscale(S, Eq), b.x(b.f.SH + s, p, l));
+      else
+        Ls[s] = S;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (F == WBG_DYN_SHC_QIAO) {
+        Ra[a] = b.D(a, l, q);
+      } else if (F == WBG_DYN_SHC_RYOO) {
+        Ra[a] = b.x(b.f.V + a, l, q);
+      } else {  // simple: the velocity with the external term i A_lq (E_l - E_q)
+        Ra[a] = b.x(b.f.V + a, l, q);
+        if (b.f.external_terms) Ra[a] = cadd(Ra[a], cscale(cmuli(b.x(b.f.A + a, l, q)), (T)(b.E[l] - b.E[q])));
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int s = 0; s < 3; ++s) cfma(out[3 * a + s], Ls[s], Ra[a]);
+  }
+  if (F == WBG_DYN_SHC_QIAO) {
+    // + delE_q^a S^s_pq + E_q (-i SR) - (-i SHR)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const T va = b.x(b.f.V + a, q, q).x;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const V t = csub(cscale(b.x(b.f.SR + 3 * a + s, p, q), Eq), b.x(b.f.SHR + 3 * a + s, p, q));
+        out[3 * a + s] = cadd(out[3 * a + s], cadd(cscale(b.x(b.f.S + s, p, q), va), cmuli(cscale(t, T(-1)))));
+      }
+    }
+  } else if (F == WBG_DYN_SHC_RYOO) {
+    // -i (E_q SA - SHA)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const V t = csub(cscale(b.x(b.f.SA + i, p, q), Eq), b.x(b.f.SHA + i, p, q));
+      out[i] = cadd(out[i], cmuli(cscale(t, T(-1))));
+    }
+  }
+}
+
+// M += I_nm of formula F for the element (n, m), n in G1, m in G2
+template <typename T, int F>
+WBG_D void add_element(const KBand<T>& b, int n, int m, typename C2<T>::t* M) {
+  typedef typename C2<T>::t V;
+  if (F == WBG_DYN_JDOS) {
+    M[0].x += T(1);
+  } else if (F == WBG_DYN_OPTCOND) {
+    V Anm[3], Amn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      Anm[a] = b.AH(a, n, m);
+      Amn[a] = b.AH(a, m, n);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) M[3 * a + c] = cadd(M[3 * a + c], cmuli(cmul(Anm[a], Amn[c])));
+  } else if (F == WBG_DYN_INJECTION) {
+    V Anm[3], Amn[3];
+    T dv[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      Anm[a] = b.AH(a, n, m);
+      Amn[a] = b.AH(a, m, n);
+      dv[a] = b.x(b.f.V + a, n, n).x - b.x(b.f.V + a, m, m).x;
+    }
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const V t = cmul(Anm[bb], Amn[c]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) M[9 * a + 3 * bb + c] = cadd(M[9 * a + 3 * bb + c], cscale(t, dv[a]));
+      }
+  } else if (F == WBG_DYN_SHC_SIMPLE || F == WBG_DYN_SHC_QIAO || F == WBG_DYN_SHC_RYOO) {
+    V J[9], Jt[9];
+    spin_current<T, F>(b, n, m, J);
+    spin_current<T, F>(b, m, n, Jt);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) J[i] = cscale(cadd(J[i], cconj(Jt[i])), T(0.5));
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) {
+      const V A = b.AH(bb, m, n);
+      const V B = mkc<T>(A.y, -A.x);  // -i A
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int s = 0; s < 3; ++s) M[9 * a + 3 * bb + s].x += cmul(J[3 * a + s], B).y;
+    }
+  } else {  // WBG_DYN_SHIFT
+    // H[3c+a] = W + sum_HD + DV (times i / (E_m - E_n) below), X[3c+a] = the external terms
+    V H[9], X[9];
+    const bool ext = b.f.external_terms;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        H[3 * c + a] = b.x(b.f.W + 3 * c + a, n, m);
+        X[3 * c + a] = ext ? b.x(b.f.dA + 3 * c + a, n, m) : czero<V>();
+      }
+    for (int l = 0; l < b.nw; ++l) {
+      V Vnl[3], Vlm[3], Dlm[3], Dnl[3], Anl[3], Alm[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Vnl[a] = b.x(b.f.V + a, n, l);
+        Vlm[a] = b.x(b.f.V + a, l, m);
+        Dlm[a] = b.Dp(a, l, m);
+        Dnl[a] = b.Dp(a, n, l);
+        if (ext) {
+          Anl[a] = b.x(b.f.A + a, n, l);
+          Alm[a] = b.x(b.f.A + a, l, m);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          cfma(H[3 * c + a], Vnl[c], Dlm[a]);
+          cfma(H[3 * c + a], cscale(Dnl[a], T(-1)), Vlm[c]);
+          if (ext) {
+            cfma(X[3 * c + a], Anl[c], Dlm[a]);
+            cfma(X[3 * c + a], cscale(Dnl[a], T(-1)), Alm[c]);
+          }
+        }
+    }
+    V Vnn[3], Vmm[3], Dnm[3], Pnm[3], Ann[3], Amm[3], Anm[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      Vnn[a] = b.x(b.f.V + a, n, n);
+      Vmm[a] = b.x(b.f.V + a, m, m);
+      Dnm[a] = b.D(a, n, m);
+      Pnm[a] = b.Dp(a, n, m);
+      if (ext) {
+        Ann[a] = b.x(b.f.A + a, n, n);
+        Amm[a] = b.x(b.f.A + a, m, m);
+        Anm[a] = b.x(b.f.A + a, n, m);
+      }
+    }
+    const T dinv_mn = b.dinv(m, n);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        V h = H[3 * c + a];
+        // - V_nn^c Dp_nm^a + Dp_nm^a V_mm^c  and  DV: D^c_nm (V^a_nn - V^a_mm) + D^a_nm (V^c_nn - V^c_mm)
+        h = cadd(h, cmul(Pnm[a], csub(Vmm[c], Vnn[c])));
+        h = cadd(h, cmul(Dnm[c], csub(Vnn[a], Vmm[a])));
+        h = cadd(h, cmul(Dnm[a], csub(Vnn[c], Vmm[c])));
+        V g = cscale(cmuli(h), dinv_mn);
+        if (ext) {
+          V x = X[3 * c + a];
+          x = cadd(x, cmul(Pnm[a], csub(Amm[c], Ann[c])));
+          x = cadd(x, cmul(Dnm[c], csub(Ann[a], Amm[a])));
+          x = cadd(x, cmul(Dnm[a], csub(Ann[c], Amm[c])));
+          x = csub(x, cmuli(cmul(csub(Ann[a], Amm[a]), Anm[c])));
+          g = cadd(g, x);
+        }
+        H[3 * c + a] = g;  // the generalised derivative dA^{c a}_nm
+      }
+    V Amn[3];
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) Amn[bb] = b.AH(bb, m, n);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          M[9 * a + 3 * bb + c].x -= cmul(H[3 * c + a], Amn[bb]).y + cmul(H[3 * bb + a], Amn[c]).y;
+  }
+}
+
+// grid: nk blocks of 128 threads.  Records of k-point k occupy slots [k*P, k*P + count[k]).
+template <typename T, int F>
+__global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
+                           wbg_dynamic_spec fs, int nw, WbgKubo kp, const double* __restrict__ efermi,
                            double* __restrict__ rec_dE, float* __restrict__ rec_fE, float2* __restrict__ rec_M,
                            int* __restrict__ count, int P) {
   typedef typename C2<T>::t V;
+  constexpr int NC = dyn_ncomp(F);
   extern __shared__ double smk[];
   double* Es = smk;                                   // [nw]
   double* Eg = Es + nw;                               // [nw] group mean energies
@@ -57,84 +290,103 @@ __global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t
     Eg[g] = s / (double)(gstart[g + 1] - gstart[g]);
   }
   __syncthreads();
-  const V* Xk = Xbar + k * nFbar * nw2;
+  KBand<T> band;
+  band.X = Xbar ? Xbar + k * nFbar * nw2 : nullptr;
+  band.E = Es;
+  band.nw = nw;
+  band.nw2 = nw2;
+  band.f = fs;
   const double eocc1max = kp.EFmin - 30.0 * kp.kBT, eocc0min = kp.EFmax + 30.0 * kp.kBT;
   for (int pr = threadIdx.x; pr < ng * ng; pr += blockDim.x) {
     const int g1 = pr / ng, g2 = pr % ng;
     if (g1 == g2) continue;  // f_E(E, E) = 0
     const double E1 = Eg[g1], E2 = Eg[g2];
-    if ((E1 < eocc1max && E2 < eocc1max) || (E1 > eocc0min && E2 > eocc0min)) continue;
-    // M^{ab} = sum_{n in G1, m in G2} i A^a_nm A^b_mn, A = i D + Abar, D_nm = -V_nm / (E_n - E_m)
-    V M[9];
-    for (int i = 0; i < 9; ++i) M[i] = czero<V>();
+    if (F == WBG_DYN_JDOS) {
+      const double d = E1 - E2;
+      if (!(E1 < kp.EFmax && E2 > kp.EFmin && fs.omega_min - 5 * kp.eta < d && d < fs.omega_max + 5 * kp.eta))
+        continue;
+    } else if ((E1 < eocc1max && E2 < eocc1max) || (E1 > eocc0min && E2 > eocc0min)) {
+      continue;
+    }
+    V M[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) M[i] = czero<V>();
     for (int n = gstart[g1]; n < gstart[g1 + 1]; ++n)
-      for (int m = gstart[g2]; m < gstart[g2 + 1]; ++m) {
-        const double dE = Es[n] - Es[m];
-        const T dnm = fabs(dE) < 1e-7 ? T(0) : (T)(1.0 / dE);
-        V Anm[3], Amn[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          // i D_nm = -i V_nm / (E_n - E_m);  i D_mn = -i V_mn / (E_m - E_n) = i V_mn / (E_n - E_m)
-          Anm[a] = cmuli(cscale(Xk[(iV + a) * nw2 + n * nw + m], -dnm));
-          Amn[a] = cmuli(cscale(Xk[(iV + a) * nw2 + m * nw + n], dnm));
-          if (external_terms) {
-            Anm[a] = cadd(Anm[a], Xk[(iA + a) * nw2 + n * nw + m]);
-            Amn[a] = cadd(Amn[a], Xk[(iA + a) * nw2 + m * nw + n]);
-          }
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) M[3 * a + b] = cadd(M[3 * a + b], cmuli(cmul(Anm[a], Amn[b])));
-      }
+      for (int m = gstart[g2]; m < gstart[g2 + 1]; ++m) add_element<T, F>(band, n, m, M);
     const int slot = atomicAdd(&cnt, 1);
     const long long r = k * (long long)P + slot;
     rec_dE[r] = E2 - E1;
     for (int e = 0; e < kp.nEF; ++e)
       rec_fE[r * kp.nEF + e] = (float)(fermi_dirac(E2, efermi[e], kp.kBT) - fermi_dirac(E1, efermi[e], kp.kBT));
-    for (int i = 0; i < 9; ++i) rec_M[r * 9 + i] = make_float2((float)M[i].x, (float)M[i].y);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) rec_M[r * NC + i] = make_float2((float)M[i].x, (float)M[i].y);
   }
   __syncthreads();
   if (threadIdx.x == 0) count[k] = cnt;
 }
 
-// grid: (ceil(nw_freq / TPB), nchunks); out [nEF][nOmega][9] complex128 (accumulated)
+// smearing of dynamic.py:50-55 (utility.py:147-168)
+__device__ float smear(float x, float eta, int gaussian) {
+  if (gaussian) {
+    const float y = x / eta;
+    return fabsf(x) < eta * 14.142135623730951f ? 0.5641895835477563f / eta * expf(-y * y) : 0.0f;
+  }
+  return 0.3183098861837907f * eta / (x * x + eta * eta);
+}
+
+// f_w(E1, E2) from dE = E2 - E1 (FP64 difference with the frequency, FP32 from there on)
+__device__ float2 factor_omega(int formula, double dE, double om, float eta, int gaussian) {
+  if (formula == WBG_DYN_OPTCOND || formula == kShcFactor) {
+    // optical: (E2 - E1) / (E2 - E1 - w - i eta);  SHC: 1 / (E1 - E2 - w - i eta) / 2
+    const bool opt = formula == WBG_DYN_OPTCOND;
+    const float delta = (float)(opt ? dE - om : -dE - om);
+    const float den = 1.0f / (delta * delta + eta * eta);
+    float cre = delta * den, cim = eta * den;
+    if (gaussian) {
+      const float x = delta / eta;
+      cim = fabsf(delta) < eta * 14.142135623730951f ? 1.7724538509055160f / eta * expf(-x * x) : 0.0f;
+    }
+    const float s = opt ? (float)dE : 0.5f;
+    return make_float2(s * cre, s * cim);
+  }
+  float v = smear((float)(-dE - om), eta, gaussian);  // JDOS, injection: smear(E1 - E2 - w)
+  if (formula == WBG_DYN_SHIFT) v += smear((float)(dE - om), eta, gaussian);
+  return make_float2(v, 0.0f);
+}
+
+// grid: (ceil(nOmega / TPB), k chunks, level chunks); out [nEF][nOmega][NC] complex128 (accumulated)
+template <int NC>
 __global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __restrict__ rec_fE,
                            const float2* __restrict__ rec_M, const int* __restrict__ count, int P, int nk, int kchunk,
-                           const double* __restrict__ omega, WbgKubo kp, double2* __restrict__ out) {
-  extern __shared__ float2 acc[];  // [nEF][9][blockDim.x]
+                           const double* __restrict__ omega, WbgKubo kp, int formula, int efc,
+                           double2* __restrict__ out) {
+  constexpr int nc = NC;
+  extern __shared__ float2 acc[];  // [efc][NC][blockDim.x]
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = w < kp.nOmega;
-  const int nE = kp.nEF;
-  for (int i = 0; i < nE * 9; ++i) acc[i * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
+  const int e0 = blockIdx.z * efc;
+  const int ne = min(efc, kp.nEF - e0);
+  for (int i = 0; i < ne * nc; ++i) acc[i * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
   const double om = active ? omega[w] : 0.0;
   const float eta = (float)kp.eta;
+  const int fgroup = formula >= WBG_DYN_SHC_SIMPLE && formula <= WBG_DYN_SHC_RYOO ? kShcFactor : formula;
   const long long k0 = (long long)blockIdx.y * kchunk;
   const long long k1 = min((long long)nk, k0 + kchunk);
   for (long long k = k0; k < k1; ++k) {
     const int nrec = count[k];
     for (int q = 0; q < nrec; ++q) {
       const long long r = k * (long long)P + q;
-      const double dE = rec_dE[r];
-      const float delta = (float)(dE - om);  // FP64 difference, FP32 from here on
-      const float fd = (float)dE;
-      float cre, cim;
-      const float den = 1.0f / (delta * delta + eta * eta);
-      cre = delta * den;
-      cim = eta * den;
-      if (kp.gaussian) {
-        const float x = delta / eta;
-        cim = fabsf(delta) < eta * 14.142135623730951f ? 1.7724538509055160f / eta * expf(-x * x) : 0.0f;
-      }
-      const float2 fw = make_float2(fd * cre, fd * cim);
-      float2 Mv[9];
-      for (int i = 0; i < 9; ++i) Mv[i] = rec_M[r * 9 + i];
-      for (int e = 0; e < nE; ++e) {
-        const float fe = rec_fE[r * nE + e];
+      const float2 fw = factor_omega(fgroup, rec_dE[r], om, eta, kp.gaussian);
+      float2 Mv[NC];
+#pragma unroll
+      for (int i = 0; i < NC; ++i) Mv[i] = rec_M[r * NC + i];
+      for (int e = 0; e < ne; ++e) {
+        const float fe = rec_fE[r * kp.nEF + e0 + e];
         if (fe == 0.0f) continue;
         const float2 c = make_float2(fe * fw.x, fe * fw.y);
-        for (int i = 0; i < 9; ++i) {
-          float2& a = acc[(e * 9 + i) * blockDim.x + threadIdx.x];
+#pragma unroll
+        for (int i = 0; i < NC; ++i) {
+          float2& a = acc[(e * NC + i) * blockDim.x + threadIdx.x];
           a.x = fmaf(c.x, Mv[i].x, fmaf(-c.y, Mv[i].y, a.x));
           a.y = fmaf(c.x, Mv[i].y, fmaf(c.y, Mv[i].x, a.y));
         }
@@ -142,55 +394,138 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __res
     }
   }
   if (!active) return;
-  for (int e = 0; e < nE; ++e)
-    for (int i = 0; i < 9; ++i) {
-      const float2 a = acc[(e * 9 + i) * blockDim.x + threadIdx.x];
-      double2* o = out + ((long long)e * kp.nOmega + w) * 9 + i;
+  for (int e = 0; e < ne; ++e)
+    for (int i = 0; i < nc; ++i) {
+      const float2 a = acc[(e * nc + i) * blockDim.x + threadIdx.x];
+      double2* o = out + ((long long)(e0 + e) * kp.nOmega + w) * nc + i;
       atomicAdd(&o->x, (double)a.x);
       atomicAdd(&o->y, (double)a.y);
     }
 }
 
+template <typename T>
+void launch_pairs(int formula, int nk, size_t smp, cudaStream_t stream, const double* E, const void* Xbar, int nFbar,
+                  const wbg_dynamic_spec& fs, int nw, const WbgKubo& kp, const double* efermi, double* rec_dE,
+                  float* rec_fE, float2* rec_M, int* count, int P) {
+  typedef typename C2<T>::t V;
+  const V* X = (const V*)Xbar;
+#define WBG_PAIRS(F) kubo_pairs<T, F><<<nk, 128, smp, stream>>>(E, X, nFbar, fs, nw, kp, efermi, rec_dE, rec_fE, \
+                                                                rec_M, count, P)
+  switch (formula) {
+    case WBG_DYN_OPTCOND: WBG_PAIRS(WBG_DYN_OPTCOND); break;
+    case WBG_DYN_JDOS: WBG_PAIRS(WBG_DYN_JDOS); break;
+    case WBG_DYN_SHC_SIMPLE: WBG_PAIRS(WBG_DYN_SHC_SIMPLE); break;
+    case WBG_DYN_SHC_QIAO: WBG_PAIRS(WBG_DYN_SHC_QIAO); break;
+    case WBG_DYN_SHC_RYOO: WBG_PAIRS(WBG_DYN_SHC_RYOO); break;
+    case WBG_DYN_SHIFT: WBG_PAIRS(WBG_DYN_SHIFT); break;
+    default: WBG_PAIRS(WBG_DYN_INJECTION); break;
+  }
+#undef WBG_PAIRS
+}
+
+bool field_ok(int first, int n, int nFbar) { return first >= 0 && first + n <= nFbar; }
+
 }  // namespace
 
-size_t wbg_kubo_workspace_bytes(int nw, int nk, int nEF) {
+int wbg_dynamic_ncomp_impl(int formula) {
+  return formula >= WBG_DYN_OPTCOND && formula <= WBG_DYN_INJECTION ? dyn_ncomp(formula) : 0;
+}
+
+size_t wbg_dynamic_workspace_bytes(int formula, int nw, int nk, int nEF) {
   const size_t P = (size_t)nw * nw;
-  return (size_t)nk * P * (8 + 4 * (size_t)nEF + 72) + (size_t)nk * 4 + 1024;
+  const size_t nc = (size_t)wbg_dynamic_ncomp_impl(formula);
+  return (size_t)nk * P * (8 + 4 * (size_t)nEF + 8 * nc) + (size_t)nk * 4 + 1024;
+}
+
+int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* fs, int nw, int nk,
+                    const WbgKubo* kp, const double* efermi, const double* omega, void* workspace,
+                    size_t workspace_bytes, double* out, int fp64, cudaStream_t stream) {
+  if (!E || !fs || !kp || !efermi || !omega || !workspace || !out || nw < 1 || nk < 1) return WBG_ERR_ARG;
+  const int F = fs->formula;
+  const int nc = wbg_dynamic_ncomp_impl(F);
+  if (nc == 0 || (fp64 != 0 && fp64 != 1)) return WBG_ERR_ARG;
+  if (kp->nEF < 1 || kp->nEF > 4096 || kp->nOmega < 1 || !(kp->eta > 0.0)) return WBG_ERR_ARG;
+  const int ext = fs->external_terms;
+  if (ext != 0 && ext != 1) return WBG_ERR_ARG;
+  if (F != WBG_DYN_JDOS) {  // fields each formula reads
+    if (!Xbar || !field_ok(fs->V, 3, nFbar)) return WBG_ERR_ARG;
+    const bool needA = ext || F == WBG_DYN_SHC_QIAO || F == WBG_DYN_SHC_RYOO;
+    if ((F == WBG_DYN_SHC_QIAO || F == WBG_DYN_SHC_RYOO) && !ext) return WBG_ERR_ARG;
+    if (needA && !field_ok(fs->A, 3, nFbar)) return WBG_ERR_ARG;
+    if (F >= WBG_DYN_SHC_SIMPLE && F <= WBG_DYN_SHC_RYOO && !field_ok(fs->S, 3, nFbar)) return WBG_ERR_ARG;
+    if (F == WBG_DYN_SHC_QIAO &&
+        !(field_ok(fs->SH, 3, nFbar) && field_ok(fs->SR, 9, nFbar) && field_ok(fs->SHR, 9, nFbar)))
+      return WBG_ERR_ARG;
+    if (F == WBG_DYN_SHC_RYOO && !(field_ok(fs->SA, 9, nFbar) && field_ok(fs->SHA, 9, nFbar))) return WBG_ERR_ARG;
+    if (F == WBG_DYN_SHIFT && (!field_ok(fs->W, 9, nFbar) || (ext && !field_ok(fs->dA, 9, nFbar)) ||
+                               !(fs->sc_eta > 0.0)))
+      return WBG_ERR_ARG;
+  }
+  if (workspace_bytes < wbg_dynamic_workspace_bytes(F, nw, nk, kp->nEF)) return WBG_ERR_WORKSPACE;
+  const int P = nw * nw;
+  char* w = (char*)workspace;
+  double* rec_dE = (double*)w; w += (size_t)nk * P * 8;
+  float2* rec_M = (float2*)w; w += (size_t)nk * P * 8 * nc;
+  float* rec_fE = (float*)w; w += (size_t)nk * P * 4 * kp->nEF;
+  int* count = (int*)w;
+  const size_t smp = (size_t)nw * 16 + (size_t)(2 * nw + 1) * 4;
+  if (fp64)
+    launch_pairs<double>(F, nk, smp, stream, E, Xbar, nFbar, *fs, nw, *kp, efermi, rec_dE, rec_fE, rec_M, count, P);
+  else
+    launch_pairs<float>(F, nk, smp, stream, E, Xbar, nFbar, *fs, nw, *kp, efermi, rec_dE, rec_fE, rec_M, count, P);
+  // threads per block and levels per block: fewest passes over the records
+  // (frequency blocks x level chunks), accumulators within 96 KB of shared memory
+  const size_t smax = 96 * 1024;
+  int tpb = 0, efc = 0;
+  long long best = -1;
+  for (int t = 128; t >= 32; t /= 2) {
+    const int e = (int)((size_t)smax / ((size_t)t * nc * sizeof(float2)));
+    if (e < 1) continue;
+    const int ec = e < kp->nEF ? e : kp->nEF;
+    const long long passes = (long long)((kp->nOmega + t - 1) / t) * ((kp->nEF + ec - 1) / ec);
+    if (best < 0 || passes < best) { best = passes; tpb = t; efc = ec; }
+  }
+  if (tpb == 0) return WBG_ERR_SIZE;
+  const size_t sma = (size_t)tpb * efc * nc * sizeof(float2);
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const int wblocks = (kp->nOmega + tpb - 1) / tpb;
+  const int eblocks = (kp->nEF + efc - 1) / efc;
+  int nchunks = (4 * sms + wblocks * eblocks - 1) / (wblocks * eblocks);
+  if (nchunks > nk) nchunks = nk;
+  const int kchunk = (nk + nchunks - 1) / nchunks;
+  nchunks = (nk + kchunk - 1) / kchunk;
+  const dim3 grid(wblocks, nchunks, eblocks);
+  if (nc == 1) {
+    cudaFuncSetAttribute(kubo_accum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+    kubo_accum<1><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
+                                              (double2*)out);
+  } else if (nc == 9) {
+    cudaFuncSetAttribute(kubo_accum<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+    kubo_accum<9><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
+                                              (double2*)out);
+  } else {
+    cudaFuncSetAttribute(kubo_accum<27>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+    kubo_accum<27><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
+                                               (double2*)out);
+  }
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+size_t wbg_kubo_workspace_bytes(int nw, int nk, int nEF) {
+  return wbg_dynamic_workspace_bytes(WBG_DYN_OPTCOND, nw, nk, nEF);
 }
 
 int wbg_kubo_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
                  const WbgKubo* kp, const double* efermi, const double* omega, void* workspace,
                  size_t workspace_bytes, double* out, int fp64, cudaStream_t stream) {
-  if (!E || !Xbar || !kp || !efermi || !omega || !workspace || !out || nw < 1 || nk < 1) return WBG_ERR_ARG;
-  if (kp->nEF < 1 || kp->nEF > 64 || kp->nOmega < 1 || !(kp->eta > 0.0)) return WBG_ERR_ARG;
-  if (iV < 0 || iV + 3 > nFbar || (external_terms && (iA < 0 || iA + 3 > nFbar))) return WBG_ERR_ARG;
-  if (workspace_bytes < wbg_kubo_workspace_bytes(nw, nk, kp->nEF)) return WBG_ERR_WORKSPACE;
-  const int P = nw * nw;
-  char* w = (char*)workspace;
-  double* rec_dE = (double*)w; w += (size_t)nk * P * 8;
-  float2* rec_M = (float2*)w; w += (size_t)nk * P * 72;
-  float* rec_fE = (float*)w; w += (size_t)nk * P * 4 * kp->nEF;
-  int* count = (int*)w;
-  const size_t smp = (size_t)nw * 16 + (size_t)(2 * nw + 1) * 4;
-  if (fp64)
-    kubo_pairs<double><<<nk, 128, smp, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, nw, external_terms, *kp,
-                                                  efermi, rec_dE, rec_fE, rec_M, count, P);
-  else
-    kubo_pairs<float><<<nk, 128, smp, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, nw, external_terms, *kp,
-                                                 efermi, rec_dE, rec_fE, rec_M, count, P);
-  int tpb = 128;
-  while (tpb > 32 && (size_t)tpb * kp->nEF * 9 * sizeof(float2) > 96 * 1024) tpb /= 2;
-  const size_t sma = (size_t)tpb * kp->nEF * 9 * sizeof(float2);
-  if (sma > 220 * 1024) return WBG_ERR_SIZE;
-  cudaFuncSetAttribute(kubo_accum, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-  const int wblocks = (kp->nOmega + tpb - 1) / tpb;
-  int nchunks = (4 * sms + wblocks - 1) / wblocks;
-  if (nchunks > nk) nchunks = nk;
-  const int kchunk = (nk + nchunks - 1) / nchunks;
-  nchunks = (nk + kchunk - 1) / kchunk;
-  kubo_accum<<<dim3(wblocks, nchunks), tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp,
-                                                           (double2*)out);
-  return wbg_cuda_status(cudaGetLastError());
+  if (!kp || kp->nEF > 64) return WBG_ERR_ARG;
+  wbg_dynamic_spec fs = {};
+  fs.formula = WBG_DYN_OPTCOND;
+  fs.external_terms = external_terms ? 1 : 0;
+  fs.V = iV;
+  fs.A = iA;
+  fs.W = fs.dA = fs.S = fs.SH = fs.SA = fs.SHA = fs.SR = fs.SHR = -1;
+  return wbg_dynamic_run(E, Xbar, nFbar, &fs, nw, nk, kp, efermi, omega, workspace, workspace_bytes, out, fp64,
+                         stream);
 }

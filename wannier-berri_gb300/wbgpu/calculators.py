@@ -4,7 +4,8 @@ Mirrors calculators/static.py:24-169 (StaticCalculator: Fermi-level scan with
 cumulative weights, /cell_volume /nk * constant_factor) for ``AHC``
 (calculators/static.py:353-364), ``Morb`` (:231-247), ``BerryDipole_FermiSea``
 (:472-487), ``DOS`` / ``CumDOS`` (:192-214), ``Ohmic_FermiSea`` / ``Ohmic_FermiSurf``
-(:379-403), and calculators/dynamic.py:26-196 for ``OpticalConductivity``.  A calculator
+(:379-403), ``Spin`` (:217-228), and calculators/dynamic.py:26-360 for ``OpticalConductivity``,
+``JDOS``, ``SHC``, ``ShiftCurrent`` and ``InjectionCurrent``.  A calculator
 declares the band-basis quantities it needs (``quantities``), accumulates a device histogram
 per batch of blocks (``accumulate``) and turns it into an ``EnergyResult`` (``finalize``).
 With ``tetra=True`` the static calculators use the tetrahedron method (static.py:80-125,
@@ -20,10 +21,13 @@ import torch
 from . import _lib
 from . import engine
 from .engine import _ptr, _stream
-from .factors import factor_ahc, factor_morb, factor_ohmic, factor_opt
+from .factors import (factor_ahc, factor_morb, factor_ohmic, factor_opt, factor_shc, factor_shift_current,
+                      factor_injection_current)
 
 WBG_FORMULA_IDENTITY, WBG_FORMULA_INVMASS, WBG_FORMULA_VELVEL = 0, 1, 2  # include/wbgpu.h
-WBG_FORMULA_OMEGA, WBG_FORMULA_DEROMEGA, WBG_FORMULA_MORB = 3, 4, 5
+WBG_FORMULA_OMEGA, WBG_FORMULA_DEROMEGA, WBG_FORMULA_MORB, WBG_FORMULA_DIAG = 3, 4, 5, 6
+(WBG_DYN_OPTCOND, WBG_DYN_JDOS, WBG_DYN_SHC_SIMPLE, WBG_DYN_SHC_QIAO, WBG_DYN_SHC_RYOO, WBG_DYN_SHIFT,
+ WBG_DYN_INJECTION) = range(7)
 from .result import EnergyResult
 
 
@@ -204,15 +208,16 @@ class _ScanCalculator(StaticCalculator):
     Fermi-sea (fder 0) or Fermi-surface (fder 1, central difference over the extended levels)."""
     formula = None
     fields = set()
+    field_map = {'V': 'V', 'W': 'W'}  # kernel argument -> band-basis quantity
 
     def quantities(self, system):
         return set(self.fields)
 
     def accumulate(self, bd, system):
         if self.tetra:
-            return self.tetra_accumulate(bd, self.formula, self._hist, self.ncomp, {'V': 'V', 'W': 'W'})
+            return self.tetra_accumulate(bd, self.formula, self._hist, self.ncomp, self.field_map)
         sc = self.scan_struct()
-        g = lambda q: bd.index.get(q, 0)
+        g = lambda arg: bd.index.get(self.field_map.get(arg), 0)
         xbar = _ptr(bd.Xbar) if bd.Xbar is not None else None
         nF = bd.Xbar.shape[1] if bd.Xbar is not None else 0
         st = engine._timed('berry_scan', _lib.load().wbg_berry_scan, _ptr(bd.E), xbar, nF, g('V'), g('W'), bd.nw,
@@ -230,6 +235,8 @@ class _ScanCalculator(StaticCalculator):
         data = self._data(cell_volume, nk, factor)
         if self.ncomp == 9:
             data = data.reshape(-1, 3, 3)
+        elif self.ncomp == 3:
+            data = data.reshape(-1, 3)
         else:
             data = data.reshape(-1)
         return EnergyResult(self.Efermi, data)
@@ -269,14 +276,32 @@ class Ohmic_FermiSurf(_ScanCalculator):
         super().__init__(constant_factor=constant_factor, **kwargs)
 
 
-class OpticalConductivity(Calculator):
-    r"""Kubo optical conductivity (calculators/dynamic.py:184-196, Formula_OptCond :170-181)."""
+class Spin(_ScanCalculator):
+    r"""Spin per unit cell (calculators/static.py:217-228): \int [dk] s f, the Fermi-sea sum of
+    Re <n|S|n> (formula Spin, formula/covariant.py:331-335) times the cell volume."""
+    formula, fder, ncomp = WBG_FORMULA_DIAG, 0, 3
+    fields = {'S'}
+    field_map = {'V': 'S'}
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self._data(cell_volume, nk, factor) * cell_volume
+        return EnergyResult(self.Efermi, data.reshape(-1, 3))
+
+
+class DynamicCalculator(Calculator):
+    r"""Kubo-type calculators (calculators/dynamic.py:26-114): every ordered pair of degenerate
+    groups at each k-point contributes f_w(E1, E2) (FD(E2) - FD(E1)) M(G1, G2); the result is
+    laid out [E_F, omega, components] and scaled by constant_factor / (nk * cell volume).  One
+    wbg_dynamic launch pair per chunk of k-points (pair records, then the frequency scan)."""
+    formula = None
+    real = False  # result dtype float (the reference's dtype=float calculators)
+    ndim = 2
 
     def __init__(self, Efermi=None, omega=None, kBT=0, smr_fixed_width=0.1, smr_type='Lorentzian',
                  kwargs_formula=None, **kwargs):
         super().__init__(**kwargs)
         self.Efermi = np.array(Efermi, dtype=float).reshape(-1)
-        self.omega = np.array(omega, dtype=float)
+        self.omega = np.array(omega, dtype=float).reshape(-1)
         self.kBT = kBT
         self.smr_fixed_width = smr_fixed_width
         if smr_type not in ('Lorentzian', 'Gaussian'):
@@ -284,46 +309,151 @@ class OpticalConductivity(Calculator):
         self.smr_type = smr_type
         self.kwargs_formula = dict(kwargs_formula or {})
         self.external_terms = self.kwargs_formula.get('external_terms', True)
-        self.constant_factor = factor_opt
+        self.sc_eta = 0.0
         self._out = None
 
     def external(self, system):
         return self.external_terms and not system.force_internal_terms_only
 
+    def formula_id(self):
+        return self.formula
+
     def quantities(self, system):
         return {'V', 'A'} if self.external(system) else {'V'}
 
+    @property
+    def ncomp(self):
+        return 1 if self.formula == WBG_DYN_JDOS else 9 if self.formula == WBG_DYN_OPTCOND else 27
+
     def reset(self, device):
-        self._out = torch.zeros((len(self.Efermi), len(self.omega), 9), dtype=torch.complex128, device=device)
+        self._out = torch.zeros((len(self.Efermi), len(self.omega), self.ncomp), dtype=torch.complex128,
+                                device=device)
         self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
         self._om = torch.tensor(self.omega, dtype=torch.float64, device=device)
 
+    def spec(self, bd, system):
+        g = lambda q: int(bd.index[q]) if q in bd.index else -1
+        return _lib.DynamicSpec(formula=self.formula_id(), external_terms=int(self.external(system)),
+                                V=g('V'), A=g('A'), W=g('W'), dA=g('dA'), S=g('S'), SH=g('SH'), SA=g('SA'),
+                                SHA=g('SHA'), SR=g('SR'), SHR=g('SHR'), sc_eta=float(self.sc_eta),
+                                omega_min=float(self.omega.min()), omega_max=float(self.omega.max()))
+
     def accumulate(self, bd, system, max_workspace=4 << 30):
         lib = _lib.load()
-        ext = self.external(system)
         kp = _lib.KuboParams(EFmin=float(self.Efermi.min()), EFmax=float(self.Efermi.max()), kBT=float(self.kBT),
                              eta=float(self.smr_fixed_width), degen_thresh=float(self.degen_thresh),
                              nEF=len(self.Efermi), nOmega=len(self.omega), gaussian=int(self.smr_type == 'Gaussian'),
                              reserved=0)
+        spec = self.spec(bd, system)
         nw, nkt = bd.nw, bd.nk_total
         per_k = ctypes.c_size_t(0)
-        _lib.check(lib.wbg_kubo_workspace_size(nw, 1, len(self.Efermi), ctypes.byref(per_k)), "wbg_kubo_workspace_size")
+        _lib.check(lib.wbg_dynamic_workspace_size(spec.formula, nw, 1, len(self.Efermi), ctypes.byref(per_k)),
+                   "wbg_dynamic_workspace_size")
         chunk = max(1, min(nkt, int(max_workspace // per_k.value)))
         ws = ctypes.c_size_t(0)
-        _lib.check(lib.wbg_kubo_workspace_size(nw, chunk, len(self.Efermi), ctypes.byref(ws)), "wbg_kubo_workspace_size")
+        _lib.check(lib.wbg_dynamic_workspace_size(spec.formula, nw, chunk, len(self.Efermi), ctypes.byref(ws)),
+                   "wbg_dynamic_workspace_size")
         work = torch.empty(int(ws.value), dtype=torch.uint8, device=bd.E.device)
-        nF = bd.Xbar.shape[1]
-        esz = bd.Xbar.element_size()
+        nF = bd.Xbar.shape[1] if bd.Xbar is not None else 0
+        esz = bd.Xbar.element_size() if bd.Xbar is not None else 0
         for k0 in range(0, nkt, chunk):
             n = min(chunk, nkt - k0)
-            Xp = ctypes.c_void_p(bd.Xbar.data_ptr() + k0 * nF * nw * nw * esz)
+            Xp = ctypes.c_void_p(bd.Xbar.data_ptr() + k0 * nF * nw * nw * esz) if bd.Xbar is not None else None
             Ep = ctypes.c_void_p(bd.E.data_ptr() + k0 * nw * 8)
-            st = engine._timed('kubo', lib.wbg_kubo, Ep, Xp, nF, bd.index['V'], bd.index.get('A', 0), nw, n, int(ext),
-                               ctypes.byref(kp), _ptr(self._ef), _ptr(self._om), _ptr(work),
-                               ctypes.c_size_t(work.numel()), _ptr(self._out), int(bd.fp64_fields), _stream())
-            _lib.check(st, "wbg_kubo")
+            st = engine._timed('kubo', lib.wbg_dynamic, Ep, Xp, nF, ctypes.byref(spec), nw, n, ctypes.byref(kp),
+                               _ptr(self._ef), _ptr(self._om), _ptr(work), ctypes.c_size_t(work.numel()),
+                               _ptr(self._out), int(bd.fp64_fields), _stream())
+            _lib.check(st, "wbg_dynamic")
+
+    def select(self, data):
+        """[E_F, omega, ncomp] -> the reference's result layout."""
+        return data.reshape((len(self.Efermi), len(self.omega)) + (3,) * self.ndim)
 
     def result(self, cell_volume, nk, factor=1.0):
-        data = self._out.cpu().numpy().reshape(len(self.Efermi), len(self.omega), 3, 3)
+        data = self.select(self._out.cpu().numpy())
         data = data * (self.constant_factor / (nk * cell_volume) * factor)
-        return EnergyResult([self.Efermi, self.omega], data)
+        return EnergyResult([self.Efermi, self.omega], data.real if self.real else data)
+
+
+class OpticalConductivity(DynamicCalculator):
+    r"""Kubo optical conductivity (calculators/dynamic.py:184-196, Formula_OptCond :170-181)."""
+    formula = WBG_DYN_OPTCOND
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self.constant_factor = factor_opt
+
+
+class JDOS(DynamicCalculator):
+    r"""Joint density of states (calculators/dynamic.py:145-162):
+    rho(w) = sum_k sum_{m,n} delta(E_m - E_n - w) (f(E_n) - f(E_m)), real."""
+    formula, real, ndim = WBG_DYN_JDOS, True, 0
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self.constant_factor = 1.
+
+    def quantities(self, system):
+        return set()
+
+
+class SHC(DynamicCalculator):
+    r"""Spin Hall conductivity (calculators/dynamic.py:199-236): Im(J^{as}_nm (-i A^b_mn)) with the
+    spin current J of kind SHC_type ('simple', 'qiao', 'ryoo'; formula/covariant.py:689-756);
+    shc_abc = (a, b, c) (1-based) selects one component."""
+    ndim = 3
+
+    def __init__(self, SHC_type="ryoo", shc_abc=None, **kwargs):
+        super().__init__(**kwargs)
+        kinds = {'simple': WBG_DYN_SHC_SIMPLE, 'qiao': WBG_DYN_SHC_QIAO, 'ryoo': WBG_DYN_SHC_RYOO}
+        if SHC_type not in kinds:
+            raise ValueError(f"spin_current_type must be `qiao` or `ryoo` or `simple`, not {SHC_type}")
+        self.SHC_type = SHC_type
+        self.formula = kinds[SHC_type]
+        if shc_abc is not None:
+            assert len(shc_abc) == 3
+            self.ndim = 0
+        self.shc_abc = shc_abc
+        self.constant_factor = factor_shc
+
+    def quantities(self, system):
+        ext = self.external(system)
+        if self.SHC_type != 'simple' and not ext:
+            raise NotImplementedError(f"spin Hall {self.SHC_type} without external terms is not implemented yet. "
+                                      "Use `SHC_type='simple'`")
+        q = {'V', 'S'} | ({'A'} if ext else set())
+        if self.SHC_type == 'qiao':
+            q |= {'SH', 'SR', 'SHR'}
+        elif self.SHC_type == 'ryoo':
+            q |= {'SA', 'SHA'}
+        return q
+
+    def select(self, data):
+        data = data.reshape(len(self.Efermi), len(self.omega), 3, 3, 3)
+        if self.shc_abc is not None:
+            a, b, c = (x - 1 for x in self.shc_abc)
+            data = data[:, :, a, b, c]
+        return data
+
+
+class ShiftCurrent(DynamicCalculator):
+    r"""Shift current (calculators/dynamic.py:302-316, ShiftCurrentFormula :243-299), real;
+    sc_eta broadens the principal-value D of the generalised derivative."""
+    formula, real, ndim = WBG_DYN_SHIFT, True, 3
+
+    def __init__(self, sc_eta, **kwargs):
+        super().__init__(**kwargs)
+        self.sc_eta = float(sc_eta)
+        self.constant_factor = factor_shift_current
+
+    def quantities(self, system):
+        return {'V', 'W', 'A', 'dA'} if self.external(system) else {'V', 'W'}
+
+
+class InjectionCurrent(DynamicCalculator):
+    r"""Injection current (calculators/dynamic.py:346-360, InjectionCurrentFormula :319-343)."""
+    formula, ndim = WBG_DYN_INJECTION, 3
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self.constant_factor = factor_injection_current

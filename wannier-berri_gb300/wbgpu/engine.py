@@ -27,8 +27,20 @@ QUANTITIES = {
     'dO': dict(order=2, herm=1, ncomp=9),
     'B': dict(order=0, herm=0, ncomp=3),
     'C': dict(order=0, herm=0, ncomp=3),
+    # spin matrices (system_R.py; SpinVelocity, formula/covariant.py:689-756): S = Xbar('SS')
+    # (Hermitian), SH = Xbar('SH'), and the (velocity a, spin s) pairs at 3 a + s of
+    # SA, SHA, SR, SHR
+    'S': dict(order=0, herm=1, ncomp=3),
+    'SH': dict(order=0, herm=0, ncomp=3),
+    'SA': dict(order=0, herm=0, ncomp=9),
+    'SHA': dict(order=0, herm=0, ncomp=9),
+    'SR': dict(order=0, herm=0, ncomp=9),
+    'SHR': dict(order=0, herm=0, ncomp=9),
 }
-QUANTITY_ORDER = ['V', 'A', 'O', 'Od', 'W', 'dA', 'dO', 'B', 'C']
+QUANTITY_ORDER = ['V', 'A', 'O', 'Od', 'W', 'dA', 'dO', 'B', 'C', 'S', 'SH', 'SA', 'SHA', 'SR', 'SHR']
+# R-space key of each plain (moment-0) quantity and the components of every extra key
+MOM0_KEY = {'B': 'BB', 'C': 'CC', 'S': 'SS', 'SH': 'SH', 'SA': 'SA', 'SHA': 'SHA', 'SR': 'SR', 'SHR': 'SHR'}
+KEY_NCOMP = {'AA': 3, 'BB': 3, 'CC': 3, 'SS': 3, 'SH': 3, 'SA': 9, 'SHA': 9, 'SR': 9, 'SHR': 9}
 MOM0, DER1, DER2, ROT, DROT = 0, 1, 2, 3, 4
 
 
@@ -127,10 +139,8 @@ def host_pinned(system, key, order):
     if key not in cache:
         X = system.get_R_mat(key)[order]
         nR, nw = X.shape[0], X.shape[1]
-        if X.ndim == 3:
-            a = X.reshape(1, nR, nw * nw)
-        else:
-            a = np.moveaxis(X, 3, 0).reshape(X.shape[3], nR, nw * nw)
+        nc = int(np.prod(X.shape[3:]))  # trailing component axes flattened in C order
+        a = np.moveaxis(X.reshape(nR, nw * nw, nc), 2, 0)
         t = torch.from_numpy(np.ascontiguousarray(a))
         cache[key] = t.pin_memory() if torch.cuda.is_available() else t
     return cache[key]
@@ -199,7 +209,7 @@ class DeviceSystem:
             if np.array_equal(keys[pos], pack(-R)):
                 neg = torch.from_numpy(pos).to(self.device)
                 nw = self.nw
-                for key in ('Ham', 'AA'):
+                for key in ('Ham', 'AA', 'SS'):
                     if not self.system.has_R_mat(key):
                         continue
                     X = self._key_fp64(key).reshape(-1, len(R), nw, nw)  # device, sorted R order
@@ -211,11 +221,11 @@ class DeviceSystem:
         return self._cache['herm_bases']
 
     def bases_for(self, keys):
-        """Base-field list for the R->k launch: Ham, then 3 components of each extra key."""
+        """Base-field list for the R->k launch: Ham, then the components of each extra key."""
         names = [('Ham', None)]
         for key in keys:
             if key != 'Ham':
-                names += [(key, c) for c in range(3)]
+                names += [(key, c) for c in range(KEY_NCOMP[key])]
         return names
 
     def _key_fp64(self, key):
@@ -285,12 +295,12 @@ class DeviceSystem:
 
 def field_plan(quantities, with_H, extra_keys):
     """Field descriptors (kind, base, a, b) for the requested quantities.
-    Bases: 0 = Ham, then AA x/y/z, then BB x/y/z, CC x/y/z as present in ``extra_keys``."""
+    Bases: 0 = Ham, then the components of each key of ``extra_keys`` in order (AA x/y/z, ...)."""
     base_of = {'Ham': 0}
     nb = 1
     for key in extra_keys:
         base_of[key] = nb
-        nb += 3
+        nb += KEY_NCOMP[key]
     desc, index = [], {}
     if with_H:
         index['H'] = 0
@@ -311,26 +321,25 @@ def field_plan(quantities, with_H, extra_keys):
             desc += [(ROT, base_of['AA'], g, 0) for g in range(3)]
         elif q == 'dO':
             desc += [(DROT, base_of['AA'], g, d) for g in range(3) for d in range(3)]
-        elif q == 'B':
-            desc += [(MOM0, base_of['BB'] + a, 0, 0) for a in range(3)]
-        elif q == 'C':
-            desc += [(MOM0, base_of['CC'] + a, 0, 0) for a in range(3)]
+        elif q in MOM0_KEY:
+            desc += [(MOM0, base_of[MOM0_KEY[q]] + a, 0, 0) for a in range(QUANTITIES[q]['ncomp'])]
     return desc, index
 
 
 def hermitian_fields(quantities, with_H, herm_bases=('Ham', 'AA')):
     """Per field of field_plan: True when the k-space field is exactly Hermitian -- its base
-    (Ham for H and its derivatives, AA for A, its derivatives and curl) is in `herm_bases`, the
-    bases whose R-space matrices satisfy X_R = X_{-R}^dagger (DeviceSystem.hermitian_bases).
-    BB and CC are never taken as Hermitian."""
+    (Ham for H and its derivatives, AA for A, its derivatives and curl, SS for S) is in
+    `herm_bases`, the bases whose R-space matrices satisfy X_R = X_{-R}^dagger
+    (DeviceSystem.hermitian_bases).  The other keys (BB, CC, SH, SA, SHA, SR, SHR) are never taken
+    as Hermitian."""
     keys = extra_keys_for(quantities)
     desc, _ = field_plan(quantities, with_H, keys)
     nonherm = set() if 'Ham' in herm_bases else {0}
     base = 1
     for key in keys:
-        if key in ('BB', 'CC') or key not in herm_bases:
-            nonherm |= {base, base + 1, base + 2}
-        base += 3
+        if key not in ('AA', 'SS') or key not in herm_bases:
+            nonherm |= set(range(base, base + KEY_NCOMP[key]))
+        base += KEY_NCOMP[key]
     return [d[1] not in nonherm for d in desc]
 
 
@@ -354,10 +363,9 @@ def extra_keys_for(quantities):
     keys = []
     if quantities & {'A', 'dA', 'O', 'Od', 'dO'}:
         keys.append('AA')
-    if 'B' in quantities:
-        keys.append('BB')
-    if 'C' in quantities:
-        keys.append('CC')
+    for q in QUANTITY_ORDER:
+        if q in quantities and q in MOM0_KEY:
+            keys.append(MOM0_KEY[q])
     return keys
 
 

@@ -1,5 +1,5 @@
 """Physical prefactors (same definitions as the reference factors.py:1-36, from scipy.constants)."""
-from scipy.constants import elementary_charge, hbar, physical_constants, angstrom
+from scipy.constants import elementary_charge, hbar, physical_constants, angstrom, pi
 
 bohr = physical_constants['Bohr radius'][0] / angstrom
 eV_au = physical_constants['electron volt-hartree relationship'][0]
@@ -8,3 +8,7 @@ factor_opt = -factor_ahc
 factor_morb = -eV_au / bohr ** 2
 TAU_UNIT = 1e-15  # relaxation time unit, fs (factors.py:3)
 factor_ohmic = (elementary_charge ** 2 / hbar / angstrom * TAU_UNIT * elementary_charge / hbar)  # factors.py:26
+factor_shc = -factor_ahc  # factors.py:37
+# factors.py:50-51
+factor_shift_current = hbar / elementary_charge * pi * elementary_charge ** 3 / (4 * hbar ** 2)
+factor_injection_current = - pi * elementary_charge ** 3 / (hbar ** 2) * TAU_UNIT
