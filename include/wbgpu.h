@@ -179,7 +179,10 @@ int wbg_device_flags(unsigned int* flags, int clear);
  *   Ohmic_FermiSea), Xbar: V at iV..iV+2, d^2H/dk_b dk_d at iW..iW+8, 9 components;
  *   WBG_FORMULA_VELVEL: in-group V^a V^b (formula/covariant.py:817-820, Ohmic_FermiSurf), 9;
  *   WBG_FORMULA_DIAG: Re X^c_nn of the 3-component field at iV (the spin expectation of
- *   calculators/static.py:217-228 Spin, formula/covariant.py:331-335), 3.
+ *   calculators/static.py:217-228 Spin, formula/covariant.py:331-335), 3;
+ *   WBG_FORMULA_VELVELVEL: in-group Re V^a V^b V^c (formula/covariant.py VelVelVel,
+ *   NLDrude_Fermider2 of calculators/static.py:545-556), 27, (a, b, c) at 9 a + 3 b + c.
+ * WBG_FORMULA_SPIN_OMEGA (the static spin Hall conductivity) goes through wbg_berry_shc (below).
  * sea != 0: Fermi-sea weights (fder 0), sea == 0: Fermi-surface groups only (fder >= 1; the
  * caller takes the finite differences over the extended levels).  hist [nEF][ncomp] (double)
  * is accumulated; component (b, d) at 3 b + d.  Xbar may be NULL for WBG_FORMULA_IDENTITY. */
@@ -187,6 +190,8 @@ int wbg_device_flags(unsigned int* flags, int clear);
 #define WBG_FORMULA_INVMASS 1
 #define WBG_FORMULA_VELVEL 2
 #define WBG_FORMULA_DIAG 6
+#define WBG_FORMULA_VELVELVEL 7
+#define WBG_FORMULA_SPIN_OMEGA 8
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
                    int formula, int sea, double* hist, int fp64, void* stream);
 
@@ -342,6 +347,15 @@ int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* byt
 int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spec, int nw, int nk,
                 const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
                 size_t workspace_bytes, double* out, int fp64, void* stream);
+
+/* Static spin Hall conductivity (calculators/static.py:647-660, formula SpinOmega of
+ * formula/covariant.py:759-788): the Fermi-sea scan (as wbg_berry_scan with sea != 0) of the
+ * additive group traces  sum_{n in G} sum_{l not in G} -2 Im( J^{as}_nl / (E_n - E_l)
+ * (D^b_ln - i Abar^b_ln) ), component 9 a + 3 b + s, J the spin current of kind
+ * spin->formula (WBG_DYN_SHC_SIMPLE / QIAO / RYOO) from the fields named in spin (see
+ * wbg_dynamic_spec; Abar only with spin->external_terms).  hist [nEF][27] accumulated. */
+int wbg_berry_shc(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spin, int nw, int nk,
+                  const wbg_scan* scan, double* hist, int fp64, void* stream);
 
 /* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);

@@ -37,6 +37,8 @@ FACTOR_OPT = -FACTOR_AHC                                       # factors.py:36
 FACTOR_MORB = -EV_AU / BOHR ** 2                               # calculators/static.py:237
 TAU_UNIT = 1e-15                                               # factors.py:3
 FACTOR_OHMIC = (elementary_charge ** 2 / hbar / angstrom * TAU_UNIT * elementary_charge / hbar)  # factors.py:26
+FACTOR_NLAHC = elementary_charge ** 3 / hbar ** 2 * TAU_UNIT                                      # factors.py:28
+FACTOR_NLDRUDE = -(elementary_charge ** 3 / hbar ** 2 * TAU_UNIT ** 2 * elementary_charge / hbar)  # factors.py:31-32
 
 
 # ---------------------------------------------------------------------------
@@ -490,6 +492,33 @@ class VelVel(Formula_ln):  # formula/covariant.py:817-820 with formula/formula.p
         return np.einsum("LMa,MNb->LNab", v, v)
 
 
+class VelVelVel(Formula_ln):  # formula/covariant.py VelVelVel: FormulaProduct of three velocities (formula.py:121-151)
+    def __init__(self, data_K, **_):
+        self.V = data_K.covariant('Ham', commader=1)
+        self.ndim = 3
+
+    def nn(self, ik, inn, out):
+        v = self.V.nn(ik, inn, out)
+        return np.einsum("LMa,MNb,NKc->LKabc", v, v, v)
+
+
+class SpinOmega(Formula_ln):  # formula/covariant.py:759-788, additive; nn block only
+    def __init__(self, data_K, spin_current_type="ryoo", external_terms=True, **_):
+        self.external_terms = external_terms and not data_K.force_internal_terms_only
+        self.A = data_K.covariant('AA') if self.external_terms else None
+        self.D = data_K.Dcov
+        self.J = Matrix_ln(spin_velocity(data_K, spin_current_type, external_terms=self.external_terms))
+        self.dEinv = data_K.dEig_inv
+        self.ndim = 3
+
+    def nn(self, ik, inn, out):
+        vde = self.D.ln(ik, inn, out).copy()  # v_ln / (E_n - E_l) = D_ln - i A_ln
+        if self.external_terms:
+            vde = vde - 1j * self.A.ln(ik, inn, out)
+        jde = self.J.ln(ik, out, inn) * self.dEinv[ik][inn][:, out][:, :, None, None]  # J_nl / (E_n - E_l)
+        return -2 * np.einsum("mlas,lnb->mnabs", jde, vde).imag
+
+
 class _TermsFormula(Formula_ln):
     """formula/formula.py:12-29: internal/external term switches."""
 
@@ -808,6 +837,8 @@ class StaticCalculator:
                     restot[iEf:] += values[ik][n]
         if self.fder == 1:
             restot = (restot[2:] - restot[:-2]) / (2 * self.dEF)
+        elif self.fder == 2:  # static.py:141-142
+            restot = (restot[2:] + restot[:-2] - 2 * restot[1:-1]) / (self.dEF ** 2)
         elif self.fder != 0:
             raise NotImplementedError()
         restot /= data_K.cell_volume
@@ -839,6 +870,22 @@ class Spin(StaticCalculator):  # calculators/static.py:217-228: Re tr_G S (formu
     def __call__(self, data_K):
         r = super().__call__(data_K)
         return EnergyResult(r.Energies, r.data * data_K.cell_volume)
+
+
+class NLDrude_Fermider2(StaticCalculator):  # calculators/static.py:545-556
+    fder = 2
+    Formula = VelVelVel
+
+    def __init__(self, constant_factor=FACTOR_NLDRUDE / 2, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class SHC_static(StaticCalculator):  # calculators/static.py:647-660 (SHC of the static module)
+    fder = 0
+    Formula = SpinOmega
+
+    def __init__(self, constant_factor=-FACTOR_AHC / 2, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
 
 
 class Ohmic_FermiSea(StaticCalculator):  # calculators/static.py:379-390
@@ -873,6 +920,11 @@ class BerryDipole_FermiSea(StaticCalculator):  # calculators/static.py:472-487
         res = super().__call__(data_K)
         res.data = res.data.swapaxes(1, 2)
         return res
+
+
+class NLAHC_FermiSea(BerryDipole_FermiSea):  # calculators/static.py:490-498
+    def __init__(self, constant_factor=FACTOR_NLAHC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
 
 
 class Morb(StaticCalculator):  # calculators/static.py:231-247

@@ -42,6 +42,9 @@ Fixtures written (all small, complex128/float64):
   system (NKdiv 2, NKFFT 3), Lorentzian and Gaussian smearing.
   ``python make_golden.py <reference root> dynamic`` writes only this file; ``random`` rewrites
   only the random-system files (its spin matrices and the stored spin / SHC results included).
+* ``static_ref.npz`` -- the static SHC (SpinOmega; simple, simple without external terms, qiao,
+  ryoo), NLDrude_Fermider2 and NLAHC_FermiSea of the reference's ``run`` on the random system.
+  ``python make_golden.py <reference root> static`` writes only this file.
 """
 import os
 import sys
@@ -154,6 +157,24 @@ def dynamic_fixtures(wb, rs):
     np.savez_compressed(os.path.join(HERE, 'dynamic_ref.npz'), **out)
 
 
+def static_fixtures(wb, rs):
+    """---- 8. more static calculators (calculators/static.py) of the reference's run on the
+    random system (NKdiv 2 x NKFFT 3): the static SHC (SpinOmega) of the three spin-current kinds,
+    NLDrude_Fermider2 (fder 2) and NLAHC_FermiSea."""
+    from wannierberri import calculators as calc
+    st = calc.static
+    EF = np.linspace(-2, 2, 21)
+    out = {'EF': EF}
+    cs = {'shc_simple': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'simple'}),
+          'shc_simple_int': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'simple', 'external_terms': False}),
+          'shc_qiao': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'qiao'}),
+          'shc_ryoo': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'ryoo'}),
+          'nldrude2': st.NLDrude_Fermider2(Efermi=EF), 'nlahc': st.NLAHC_FermiSea(Efermi=EF)}
+    for k, v in run_ref(wb, rs, 2, 3, cs).items():
+        out['random_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'static_ref.npz'), **out)
+
+
 def main(ref_root):
     wb = setup_reference(ref_root)
     from wannierberri.system.system_R import System_R
@@ -232,6 +253,7 @@ def main(ref_root):
     tetra_fixtures(wb, rs)
     refine_fixtures(wb, rs)
     dynamic_fixtures(wb, rs)
+    static_fixtures(wb, rs)
     print("wrote fixtures to", HERE)
 
 
@@ -308,13 +330,14 @@ def refine_fixtures(wb, rs):
 if __name__ == '__main__':
     root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
     section = sys.argv[2] if len(sys.argv) > 2 else None
-    if section in ('random', 'tetra', 'refine', 'dynamic'):  # one section only
+    if section in ('random', 'tetra', 'refine', 'dynamic', 'static'):  # one section only
         wb = setup_reference(root)
         from wannierberri.system.system_R import System_R
         rs = System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True)
         if section == 'random':
             random_fixtures(root)
         else:
-            {'tetra': tetra_fixtures, 'refine': refine_fixtures, 'dynamic': dynamic_fixtures}[section](wb, rs)
+            {'tetra': tetra_fixtures, 'refine': refine_fixtures, 'dynamic': dynamic_fixtures,
+             'static': static_fixtures}[section](wb, rs)
     else:
         main(root)

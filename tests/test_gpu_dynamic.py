@@ -1,10 +1,13 @@
 """GPU parity of the dynamic calculators (JDOS, SHC, shift and injection currents) and of the static
-Spin, through wbgpu.run (C ABI: wbg_dynamic, wbg_berry_scan with WBG_FORMULA_DIAG).
+Spin, SHC (SpinOmega), NLDrude_Fermider2 and NLAHC_FermiSea, through wbgpu.run (C ABI: wbg_dynamic,
+wbg_berry_scan with WBG_FORMULA_DIAG / WBG_FORMULA_VELVELVEL, wbg_berry_shc).
 
 * the reference's own stored results of tests/test_run.py:653-669 on its random system
   (random-spin, random-opt_SHCqiao, random-opt_SHCryoo);
 * dynamic_ref.npz: the reference's run() on the same system for every dynamic formula
   (tests/golden/make_golden.py, section 7);
+* static_ref.npz: the reference's run() for the static SHC, NLDrude_Fermider2, NLAHC_FermiSea
+  (section 8);
 * the oracle on the triclinic MDRS model (nw = 6, anisotropic FFT grid) for the formulas that need
   no spin matrices, FP64 and mixed precision.
 Pair records carry FP32 matrix elements and the frequency scan accumulates in FP32 (as the optical
@@ -108,3 +111,22 @@ def test_dynamic_argument_errors(golden_dir):
                   {'shc': C.SHC(SHC_type='qiao', Efermi=[0.0], omega=[1.0], kwargs_formula={'external_terms': False})})
     with pytest.raises(ValueError):
         C.SHC(SHC_type='other', Efermi=[0.0], omega=[1.0])
+
+
+@pytest.mark.parametrize("precision,tol", [('fp64', 1e-8), ('mixed', 1e-4)])
+def test_static_extra_reference_run(golden_dir, precision, tol):
+    """Static SHC (SpinOmega, three spin-current kinds), NLDrude_Fermider2 (fder 2), NLAHC_FermiSea
+    against the reference's run() on the random system (static_ref.npz)."""
+    s = _random_system(golden_dir)
+    ref = np.load(os.path.join(golden_dir, 'static_ref.npz'))
+    EF = ref['EF']
+    st = C.static
+    calcs = {'shc_simple': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'simple'}),
+             'shc_simple_int': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'simple',
+                                                                 'external_terms': False}),
+             'shc_qiao': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'qiao'}),
+             'shc_ryoo': st.SHC(Efermi=EF, kwargs_formula={'spin_current_type': 'ryoo'}),
+             'nldrude2': st.NLDrude_Fermider2(Efermi=EF), 'nlahc': st.NLAHC_FermiSea(Efermi=EF)}
+    res = wbgpu.run(s, wbgpu.Grid(s, NKdiv=2, NKFFT=3), calcs, precision=precision)
+    for q in calcs:
+        _close(res[q].data, ref['random_' + q], tol)

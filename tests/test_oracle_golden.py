@@ -291,3 +291,32 @@ def test_dynamic_golden(dynamic_run, dynamic_ref, quant):
     got = dynamic_run[quant].data
     assert got.shape == ref.shape
     assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))
+
+
+def static_calculators(EF):
+    """The calculators of static_ref.npz (tests/golden/make_golden.py, section 8)."""
+    return {'shc_simple': O.SHC_static(Efermi=EF, kwargs_formula={'spin_current_type': 'simple'}),
+            'shc_simple_int': O.SHC_static(Efermi=EF, kwargs_formula={'spin_current_type': 'simple',
+                                                                      'external_terms': False}),
+            'shc_qiao': O.SHC_static(Efermi=EF, kwargs_formula={'spin_current_type': 'qiao'}),
+            'shc_ryoo': O.SHC_static(Efermi=EF, kwargs_formula={'spin_current_type': 'ryoo'}),
+            'nldrude2': O.NLDrude_Fermider2(Efermi=EF), 'nlahc': O.NLAHC_FermiSea(Efermi=EF)}
+
+
+@pytest.fixture(scope="module")
+def static_ref(golden_dir):
+    return np.load(os.path.join(golden_dir, 'static_ref.npz'))
+
+
+@pytest.fixture(scope="module")
+def static_run(random_sys, static_ref):
+    return O.run(random_sys, (2, 2, 2), (3, 3, 3), static_calculators(static_ref['EF']))
+
+
+@pytest.mark.parametrize("quant", ['shc_simple', 'shc_simple_int', 'shc_qiao', 'shc_ryoo', 'nldrude2', 'nlahc'])
+def test_static_extra_golden(static_run, static_ref, quant):
+    """Static SHC (SpinOmega), NLDrude_Fermider2 (fder 2), NLAHC_FermiSea: the reference's run()."""
+    ref = static_ref['random_' + quant]
+    got = static_run[quant].data
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))

@@ -136,6 +136,13 @@ int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int n
                       workspace_bytes, out, fp64, (cudaStream_t)stream);
 }
 
+int wbg_berry_shc(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spin, int nw, int nk,
+                  const wbg_scan* scan, double* hist, int fp64, void* stream) {
+  if (!spin) return WBG_STATUS_BAD_ARGUMENT;
+  return wbg_berry_scan_run(E, Xbar, nFbar, spin->V, -1, nw, nk, scan, WBG_FORMULA_SPIN_OMEGA, 1, hist, fp64,
+                            (cudaStream_t)stream, nullptr, nullptr, spin);
+}
+
 int wbg_dynamic_ncomp(int formula) { return ::wbg_dynamic_ncomp_impl(formula); }
 
 int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* bytes) {
@@ -175,6 +182,7 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
     case WBG_FORMULA_INVMASS:
     case WBG_FORMULA_VELVEL:
     case WBG_FORMULA_DIAG:
+    case WBG_FORMULA_VELVELVEL:
       return wbg_berry_scan_run(E, Xbar, nFbar, f->V, f->W, nw, nk, &sp, formula, 0, nullptr, fp64, st, sel, P);
     case WBG_FORMULA_OMEGA:
       return wbg_berry_omega_run(E, Xbar, nFbar, f->V, f->A, f->O, nw, nk, &sp, internal_terms, external_terms,

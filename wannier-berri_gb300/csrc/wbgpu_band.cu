@@ -11,6 +11,7 @@
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_band.cuh"
+#include "wbgpu_spin.cuh"
 
 namespace {
 
@@ -380,21 +381,22 @@ WBG_D int sel_bandmax(const signed char* selk, int nw, int lane, int L) {
 WBG_D void emit_band_values(double* P, long long k, int nw, int nc, int lane, int L, int bandmax,
                             const signed char* selk, const int* myS, const double* t, int ts) {
   for (int n = lane; n < nw; n += L) {
-    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int qs = 0, qe = 0;  // bands summed into band n's value, times scale
+    double scale = 1.0;
     if (n < bandmax) {
-      if (n == 0)
-        for (int q = 0; q < bandmax; ++q)
-          for (int c = 0; c < nc; ++c) v[c] += t[q * ts + c];
+      if (n == 0) qe = bandmax;
     } else if (selk[n] == 1) {
-      int gs = n, ge = n + 1;
-      while (!myS[gs]) --gs;
-      while (ge < nw && !myS[ge]) ++ge;
-      for (int q = gs; q < ge; ++q)
-        for (int c = 0; c < nc; ++c) v[c] += t[q * ts + c];
-      const double inv = 1.0 / (double)(ge - gs);
-      for (int c = 0; c < nc; ++c) v[c] *= inv;
+      qs = n;
+      qe = n + 1;
+      while (!myS[qs]) --qs;
+      while (qe < nw && !myS[qe]) ++qe;
+      scale = 1.0 / (double)(qe - qs);
     }
-    for (int c = 0; c < nc; ++c) P[(k * nw + n) * nc + c] = v[c];
+    for (int c = 0; c < nc; ++c) {
+      double v = 0.0;
+      for (int q = qs; q < qe; ++q) v += t[q * ts + c];
+      P[(k * nw + n) * nc + c] = v * scale;
+    }
   }
 }
 
@@ -711,22 +713,58 @@ __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __r
 // (E below the window add to every level, the sea group); sea == 0: Fermi-surface groups only.
 // hist [nEF][ncomp] (component (b, d) at 3 b + d).
 // ---------------------------------------------------------------------------------------
-template <typename T>
+__host__ __device__ inline int scan_ncomp(int formula) {
+  return formula == WBG_FORMULA_IDENTITY ? 1
+         : formula == WBG_FORMULA_DIAG   ? 3
+         : (formula == WBG_FORMULA_VELVELVEL || formula == WBG_FORMULA_SPIN_OMEGA) ? 27
+                                           : 9;
+}
+
+// spin Berry curvature (formula/covariant.py:759-788, SpinOmega, additive) of band n:
+//   t[9 a + 3 b + s] += -2 Im( J^{as}_nl / (E_n - E_l) (D^b_ln - i Abar^b_ln) ),  l outside the group
+template <typename T, int K>
+__device__ void spin_omega_terms(const KBand<T>& kb, int n, int gs, int ge, double* t) {
+  typedef typename C2<T>::t V;
+  for (int l = 0; l < kb.nw; ++l) {
+    if (l >= gs && l < ge) continue;
+    V J[9], Jt[9];
+    spin_current<T, K>(kb, n, l, J);
+    spin_current<T, K>(kb, l, n, Jt);
+    const T dnl = kb.dinv(n, l);
+    V vde[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      vde[b] = kb.D(b, l, n);
+      if (kb.f.external_terms) vde[b] = csub(vde[b], cmuli(kb.x(kb.f.A + b, l, n)));
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const V j = cscale(cadd(J[3 * a + s], cconj(Jt[3 * a + s])), T(0.5) * dnl);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) t[9 * a + 3 * b + s] += -2.0 * (double)cmul(j, vde[b]).y;
+      }
+  }
+}
+
+// NCM: components held per band (9, or 27 for WBG_FORMULA_VELVELVEL / WBG_FORMULA_SPIN_OMEGA)
+template <typename T, int NCM>
 __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                   int iV, int iW, int nw, int nk, int L, int G, WbgScan sp, int formula, int sea,
-                                  double* __restrict__ hist, BandSel bs) {
+                                  double* __restrict__ hist, BandSel bs, wbg_dynamic_spec fs) {
   typedef typename C2<T>::t V;
-  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : formula == WBG_FORMULA_DIAG ? 3 : 9;
+  const int nc = scan_ncomp(formula);
   extern __shared__ double smb[];
   double* sh = smb;                                   // [nEF][nc]
   double* Es = sh + nc * sp.nEF;                      // [G][nw]
-  double* tv = Es + G * nw;                           // [G][nw][9]
-  int* start = reinterpret_cast<int*>(tv + 9 * G * nw);  // [G][nw]
+  double* tv = Es + G * nw;                           // [G][nw][NCM]
+  int* start = reinterpret_cast<int*>(tv + NCM * G * nw);  // [G][nw]
   for (int i = threadIdx.x; i < nc * sp.nEF; i += blockDim.x) sh[i] = 0.0;
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
-  double* myT = tv + 9 * grp * nw;
+  double* myT = tv + NCM * grp * nw;
   int* myS = start + grp * nw;
   const long long nw2 = (long long)nw * nw;
   for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
@@ -760,9 +798,37 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
       while (!myS[gs]) --gs;
       while (ge < nw && !myS[ge]) ++ge;
       if (n < bandmax) { gs = 0; ge = bandmax; }
-      double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      double t[NCM];
+#pragma unroll
+      for (int c = 0; c < NCM; ++c) t[c] = 0.0;
       if (formula == WBG_FORMULA_IDENTITY) {
         t[0] = 1.0;
+      } else if (NCM == 27 && formula == WBG_FORMULA_VELVELVEL) {
+        // sum_{n', n'' in the group} Re V^a_nn' V^b_n'n'' V^c_n''n (FormulaProduct VelVelVel)
+        for (int p = gs; p < ge; ++p)
+          for (int q = gs; q < ge; ++q) {
+            V A3[3], B3[3], C3[3];
+            for (int a = 0; a < 3; ++a) {
+              A3[a] = Xk[(iV + a) * nw2 + n * nw + p];
+              B3[a] = Xk[(iV + a) * nw2 + p * nw + q];
+              C3[a] = Xk[(iV + a) * nw2 + q * nw + n];
+            }
+            for (int a = 0; a < 3; ++a)
+              for (int b = 0; b < 3; ++b) {
+                const V ab = cmul(A3[a], B3[b]);
+                for (int c = 0; c < 3; ++c) t[9 * a + 3 * b + c] += (double)cmul(ab, C3[c]).x;
+              }
+          }
+      } else if (NCM == 27 && formula == WBG_FORMULA_SPIN_OMEGA) {
+        KBand<T> kb;
+        kb.X = Xk;
+        kb.E = myE;
+        kb.nw = nw;
+        kb.nw2 = nw2;
+        kb.f = fs;
+        if (fs.formula == WBG_DYN_SHC_QIAO) spin_omega_terms<T, WBG_DYN_SHC_QIAO>(kb, n, gs, ge, t);
+        else if (fs.formula == WBG_DYN_SHC_RYOO) spin_omega_terms<T, WBG_DYN_SHC_RYOO>(kb, n, gs, ge, t);
+        else spin_omega_terms<T, WBG_DYN_SHC_SIMPLE>(kb, n, gs, ge, t);
       } else if (formula == WBG_FORMULA_DIAG) {
         for (int c = 0; c < 3; ++c) t[c] = (double)Xk[(iV + c) * nw2 + n * nw + n].x;
       } else if (formula == WBG_FORMULA_INVMASS) {
@@ -792,11 +858,11 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
             for (int b = 0; b < 3; ++b) t[3 * a + b] += (double)cmul(Vnp[a], Vpn[b]).x;
         }
       }
-      for (int c = 0; c < 9; ++c) myT[n * 9 + c] = t[c];
+      for (int c = 0; c < NCM; ++c) myT[n * NCM + c] = t[c];
     }
     __syncwarp();
     if (valid && bs.P) {
-      emit_band_values(bs.P, k, nw, nc, lane, L, bandmax, bs.sel + k * nw, myS, myT, 9);
+      emit_band_values(bs.P, k, nw, nc, lane, L, bandmax, bs.sel + k * nw, myS, myT, NCM);
     } else if (valid) {
       for (int n = lane; n < nw; n += L) {
         int gs = -1, ge = -1;
@@ -808,9 +874,10 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
           if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
         }
         if (gs < 0) continue;
-        double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, esum = 0.0;
+        double v[NCM], esum = 0.0;
+        for (int c = 0; c < NCM; ++c) v[c] = 0.0;
         for (int q = gs; q < ge; ++q) {
-          for (int c = 0; c < nc; ++c) v[c] += myT[q * 9 + c];
+          for (int c = 0; c < nc; ++c) v[c] += myT[q * NCM + c];
           esum += myE[q];
         }
         int bin = -1;
@@ -1393,35 +1460,54 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
 
 int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk,
                        const WbgScan* sp_in, int formula, int sea, double* hist, int fp64, cudaStream_t stream,
-                       const signed char* sel, double* P) {
+                       const signed char* sel, double* P, const wbg_dynamic_spec* spin) {
   const BandSel bs{sel, P};
   if (nw < 1 || nk < 1 || !sp_in || !E || (!sel) != (!P)) return WBG_ERR_ARG;
   if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
   WbgScan spv = *sp_in;
   if (sel) { spv.nEF = 0; hist = nullptr; }
   const WbgScan* sp = &spv;
-  if ((formula < WBG_FORMULA_IDENTITY || formula > WBG_FORMULA_VELVEL) && formula != WBG_FORMULA_DIAG)
+  const bool plain = formula >= WBG_FORMULA_IDENTITY && formula <= WBG_FORMULA_VELVEL;
+  if (!plain && formula != WBG_FORMULA_DIAG && formula != WBG_FORMULA_VELVELVEL && formula != WBG_FORMULA_SPIN_OMEGA)
     return WBG_ERR_ARG;
   if (formula != WBG_FORMULA_IDENTITY && (!Xbar || iV < 0 || iV + 3 > nFbar)) return WBG_ERR_ARG;
   if (formula == WBG_FORMULA_INVMASS && (iW < 0 || iW + 9 > nFbar)) return WBG_ERR_ARG;
-  const int nc = formula == WBG_FORMULA_IDENTITY ? 1 : formula == WBG_FORMULA_DIAG ? 3 : 9;
+  wbg_dynamic_spec fs = {};
+  if (formula == WBG_FORMULA_SPIN_OMEGA) {  // the spin current's fields (as wbg_dynamic's SHC)
+    if (!spin) return WBG_ERR_ARG;
+    fs = *spin;
+    auto ok = [&](int first, int n) { return first >= 0 && first + n <= nFbar; };
+    const int K = fs.formula;
+    if (K < WBG_DYN_SHC_SIMPLE || K > WBG_DYN_SHC_RYOO || (fs.external_terms != 0 && fs.external_terms != 1))
+      return WBG_ERR_ARG;
+    if (!ok(fs.V, 3) || !ok(fs.S, 3) || (fs.external_terms && !ok(fs.A, 3))) return WBG_ERR_ARG;
+    if (K != WBG_DYN_SHC_SIMPLE && !fs.external_terms) return WBG_ERR_ARG;
+    if (K == WBG_DYN_SHC_QIAO && !(ok(fs.SH, 3) && ok(fs.SR, 9) && ok(fs.SHR, 9))) return WBG_ERR_ARG;
+    if (K == WBG_DYN_SHC_RYOO && !(ok(fs.SA, 9) && ok(fs.SHA, 9))) return WBG_ERR_ARG;
+  }
+  const int nc = scan_ncomp(formula);
   const int L = lanes_for(nw);
   const int G = 128 / L;
-  const size_t sm = (size_t)nc * sp->nEF * 8 + (size_t)G * nw * (8 + 72 + 4);
-  if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
   long long nblk = (nk + G - 1) / G;
   if (nblk > (long long)sms * 8) nblk = (long long)sms * 8;
-  if (fp64) {
-    cudaFuncSetAttribute(berry_scan_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    berry_scan_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
-                                                                *sp, formula, sea, hist, bs);
+#define WBG_SCAN(TT, NCM)                                                                                          \
+  do {                                                                                                             \
+    const size_t sm = (size_t)nc * sp->nEF * 8 + (size_t)G * nw * (8 + 8 * NCM + 4);                               \
+    if (sm > 220 * 1024) return WBG_ERR_SIZE;                                                                      \
+    cudaFuncSetAttribute(berry_scan_kernel<TT, NCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);     \
+    berry_scan_kernel<TT, NCM><<<(int)nblk, G * L, sm, stream>>>(E, (const typename C2<TT>::t*)Xbar, nFbar, iV, iW, \
+                                                                 nw, nk, L, G, *sp, formula, sea, hist, bs, fs);   \
+  } while (0)
+  if (nc == 27) {
+    if (fp64) WBG_SCAN(double, 27);
+    else WBG_SCAN(float, 27);
   } else {
-    cudaFuncSetAttribute(berry_scan_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    berry_scan_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iW, nw, nk, L, G,
-                                                               *sp, formula, sea, hist, bs);
+    if (fp64) WBG_SCAN(double, 9);
+    else WBG_SCAN(float, 9);
   }
+#undef WBG_SCAN
   return wbg_cuda_status(cudaGetLastError());
 }
 

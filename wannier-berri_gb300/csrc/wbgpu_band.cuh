@@ -30,4 +30,5 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
 int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);
 int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const WbgScan* sp,
                        int formula, int sea, double* hist, int fp64, cudaStream_t stream,
-                       const signed char* sel = nullptr, double* P = nullptr);
+                       const signed char* sel = nullptr, double* P = nullptr,
+                       const wbg_dynamic_spec* spin = nullptr);

@@ -14,7 +14,7 @@ EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_wo
            'wbg_r2k_columns', 'wbg_ws_replicas',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
-           'wbg_dynamic_ncomp', 'wbg_dynamic_workspace_size', 'wbg_dynamic',
+           'wbg_dynamic_ncomp', 'wbg_dynamic_workspace_size', 'wbg_dynamic', 'wbg_berry_shc',
            'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma']
 
 STATUS_OK = 0
@@ -86,6 +86,7 @@ _SIGS = {
     'wbg_dynamic_workspace_size': (_I, [_I, _I, _I, _I, ctypes.POINTER(_SZ)]),
     'wbg_dynamic': (_I, [_P, _P, _I, ctypes.POINTER(DynamicSpec), _I, _I, ctypes.POINTER(KuboParams), _P, _P, _P, _SZ,
                          _P, _I, _P]),
+    'wbg_berry_shc': (_I, [_P, _P, _I, ctypes.POINTER(DynamicSpec), _I, _I, ctypes.POINTER(Scan), _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
     'wbg_tetra_select': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, _I, _P, _P]),

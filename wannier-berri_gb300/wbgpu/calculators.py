@@ -21,11 +21,14 @@ import torch
 from . import _lib
 from . import engine
 from .engine import _ptr, _stream
+import types
+
 from .factors import (factor_ahc, factor_morb, factor_ohmic, factor_opt, factor_shc, factor_shift_current,
-                      factor_injection_current)
+                      factor_injection_current, factor_nlahc, factor_nldrude)
 
 WBG_FORMULA_IDENTITY, WBG_FORMULA_INVMASS, WBG_FORMULA_VELVEL = 0, 1, 2  # include/wbgpu.h
 WBG_FORMULA_OMEGA, WBG_FORMULA_DEROMEGA, WBG_FORMULA_MORB, WBG_FORMULA_DIAG = 3, 4, 5, 6
+WBG_FORMULA_VELVELVEL, WBG_FORMULA_SPIN_OMEGA = 7, 8
 (WBG_DYN_OPTCOND, WBG_DYN_JDOS, WBG_DYN_SHC_SIMPLE, WBG_DYN_SHC_QIAO, WBG_DYN_SHC_RYOO, WBG_DYN_SHIFT,
  WBG_DYN_INJECTION) = range(7)
 from .result import EnergyResult
@@ -203,6 +206,58 @@ class BerryDipole_FermiSea(StaticCalculator):
         return EnergyResult(self.Efermi, data.swapaxes(1, 2))
 
 
+class NLAHC_FermiSea(BerryDipole_FermiSea):
+    r"""Nonlinear anomalous Hall conductivity (S^2/A) from the Fermi sea (calculators/static.py:490-498):
+    the Berry-curvature dipole times e^3/hbar^2 tau."""
+
+    def __init__(self, constant_factor=factor_nlahc, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class SHC_static(StaticCalculator):
+    r"""Spin Hall conductivity with dc (S/m) from the Fermi sea (calculators/static.py:647-660, formula
+    SpinOmega of formula/covariant.py:759-788): -2 Im(J_nl (D_ln - i A_ln)) / (E_n - E_l) over l outside
+    each group, J the spin current of kwargs_formula['spin_current_type'] ('ryoo' default, 'qiao',
+    'simple').  Exposed as ``calculators.static.SHC``."""
+    ncomp = 27
+
+    def __init__(self, constant_factor=-factor_ahc / 2, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+        if self.tetra:
+            raise NotImplementedError("the static SHC with tetra=True is not supported by the GPU backend")
+        self.kind = self.kwargs_formula.get('spin_current_type', 'ryoo')
+        kinds = {'simple': WBG_DYN_SHC_SIMPLE, 'qiao': WBG_DYN_SHC_QIAO, 'ryoo': WBG_DYN_SHC_RYOO}
+        if self.kind not in kinds:
+            raise ValueError(f"spin_current_type must be `qiao` or `ryoo` or `simple`, not {self.kind}")
+        self.kind_id = kinds[self.kind]
+
+    def quantities(self, system):
+        ext = self.external(system)
+        if self.kind != 'simple' and not ext:
+            raise NotImplementedError(f"spin Hall {self.kind} without external terms is not implemented yet. "
+                                      "Use `SHC_type='simple'`")
+        q = {'V', 'S'} | ({'A'} if ext else set())
+        if self.kind == 'qiao':
+            q |= {'SH', 'SR', 'SHR'}
+        elif self.kind == 'ryoo':
+            q |= {'SA', 'SHA'}
+        return q
+
+    def accumulate(self, bd, system):
+        g = lambda q: int(bd.index[q]) if q in bd.index else -1
+        spec = _lib.DynamicSpec(formula=self.kind_id, external_terms=int(self.external(system)), V=g('V'), A=g('A'),
+                                W=-1, dA=-1, S=g('S'), SH=g('SH'), SA=g('SA'), SHA=g('SHA'), SR=g('SR'), SHR=g('SHR'),
+                                sc_eta=0.0, omega_min=0.0, omega_max=0.0)
+        sc = self.scan_struct()
+        st = engine._timed('berry_scan', _lib.load().wbg_berry_shc, _ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1],
+                           ctypes.byref(spec), bd.nw, bd.nk_total, ctypes.byref(sc), _ptr(self._hist),
+                           int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_shc")
+
+    def result(self, cell_volume, nk, factor=1.0):
+        return EnergyResult(self.Efermi, self.finalize(cell_volume, nk, factor).reshape(-1, 3, 3, 3))
+
+
 class _ScanCalculator(StaticCalculator):
     """Static calculators whose group traces go through wbg_berry_scan (calculators/static.py:60-169):
     Fermi-sea (fder 0) or Fermi-surface (fder 1, central difference over the extended levels)."""
@@ -229,11 +284,15 @@ class _ScanCalculator(StaticCalculator):
         data = self.finalize(cell_volume, nk, factor)
         if self.fder == 1 and not self.tetra:  # calculators/static.py:137-140
             data = (data[2:] - data[:-2]) / (2 * self.dEF)
+        elif self.fder == 2:  # calculators/static.py:141-142
+            data = (data[2:] + data[:-2] - 2 * data[1:-1]) / (self.dEF ** 2)
         return data
 
     def result(self, cell_volume, nk, factor=1.0):
         data = self._data(cell_volume, nk, factor)
-        if self.ncomp == 9:
+        if self.ncomp == 27:
+            data = data.reshape(-1, 3, 3, 3)
+        elif self.ncomp == 9:
             data = data.reshape(-1, 3, 3)
         elif self.ncomp == 3:
             data = data.reshape(-1, 3)
@@ -274,6 +333,18 @@ class Ohmic_FermiSurf(_ScanCalculator):
 
     def __init__(self, constant_factor=factor_ohmic, **kwargs):
         super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class NLDrude_Fermider2(_ScanCalculator):
+    r"""Drude conductivity (S^2/A) with the second derivative of the distribution
+    (calculators/static.py:545-556): -e^3/hbar^2 tau^2 \int [dk] v_b v_a v_c f'' / 2 (formula VelVelVel)."""
+    formula, fder, ncomp = WBG_FORMULA_VELVELVEL, 2, 27
+    fields = {'V'}
+
+    def __init__(self, constant_factor=factor_nldrude / 2, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+        if self.tetra:
+            raise NotImplementedError("fder=2 with tetra=True is not supported by the GPU backend")
 
 
 class Spin(_ScanCalculator):
@@ -457,3 +528,13 @@ class InjectionCurrent(DynamicCalculator):
     def __init__(self, **kwargs):
         super().__init__(**kwargs)
         self.constant_factor = factor_injection_current
+
+
+# the reference's calculator modules (calculators/static.py, calculators/dynamic.py): both define an SHC
+static = types.SimpleNamespace(
+    StaticCalculator=StaticCalculator, AHC=AHC, Morb=Morb, BerryDipole_FermiSea=BerryDipole_FermiSea,
+    NLAHC_FermiSea=NLAHC_FermiSea, DOS=DOS, CumDOS=CumDOS, Ohmic_FermiSea=Ohmic_FermiSea,
+    Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static)
+dynamic = types.SimpleNamespace(
+    DynamicCalculator=DynamicCalculator, OpticalConductivity=OpticalConductivity, JDOS=JDOS, SHC=SHC,
+    ShiftCurrent=ShiftCurrent, InjectionCurrent=InjectionCurrent)

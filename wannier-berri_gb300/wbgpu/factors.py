@@ -12,3 +12,5 @@ factor_shc = -factor_ahc  # factors.py:37
 # factors.py:50-51
 factor_shift_current = hbar / elementary_charge * pi * elementary_charge ** 3 / (4 * hbar ** 2)
 factor_injection_current = - pi * elementary_charge ** 3 / (hbar ** 2) * TAU_UNIT
+factor_nlahc = elementary_charge ** 3 / hbar ** 2 * TAU_UNIT  # factors.py:28
+factor_nldrude = -(elementary_charge ** 3 / hbar ** 2 * TAU_UNIT ** 2 * elementary_charge / hbar)  # factors.py:31-32
