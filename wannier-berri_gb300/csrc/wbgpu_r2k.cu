@@ -30,50 +30,51 @@ namespace {
 constexpr int kThreads = 128;
 
 // ---------------- R-space weights (once per system + field set) ----------------
-// grid: (ceil(nR*nw2/256), nF); XR [nBase][nR][nw2]; iR [nR][3] (sorted order).
+// grid: ceil(nR*nw2/256) blocks; one thread per (R, m, n) computes the Cartesian weight
+// R + t_n - t_m once (FP64) and writes every field.  XR [nBase][nR][nw2]; iR [nR][3] (sorted).
 // XFlo (split precision, T = float): the rounding residual XF_R - float(XF_R), so that the
 // k-independent R-space data carry 48 bits into the transform.
 template <typename T>
 __global__ void r2k_weights(const double2* __restrict__ XR, const int* __restrict__ iR, const int4* __restrict__ fdesc,
-                            const double* __restrict__ wcc, R2KLattice lat, int nBase, int nR, int nw,
+                            int nF, const double* __restrict__ wcc, R2KLattice lat, int nBase, int nR, int nw,
                             typename C2<T>::t* __restrict__ XF, typename C2<T>::t* __restrict__ XFlo) {
-  typedef typename C2<T>::t V;
-  const int f = blockIdx.y;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int nw2 = nw * nw;
   if (idx >= (long long)nR * nw2) return;
   const int r = (int)(idx / nw2), mn = (int)(idx % nw2);
   const int m = mn / nw, n = mn % nw;
-  const int4 fd = fdesc[f];
   // R + t_n - t_m (Cartesian), rvectors.py:355-360
   double w[3];
   for (int a = 0; a < 3; ++a)
     w[a] = iR[r * 3 + 0] * lat.L[0 * 3 + a] + iR[r * 3 + 1] * lat.L[1 * 3 + a] + iR[r * 3 + 2] * lat.L[2 * 3 + a] +
            wcc[n * 3 + a] - wcc[m * 3 + a];
-  const bool idx_ok = fd.z >= 0 && fd.z < 3 && fd.w >= 0 && fd.w < 3 && fd.y >= 0;
-  const bool ok = idx_ok && ((fd.x <= R2K_DER2 && fd.y < nBase) || (fd.x >= R2K_ROT && fd.y + 2 < nBase)) &&
-                  fd.x >= 0 && fd.x <= R2K_DROT;
-  double2 v = make_double2(0.0, 0.0);
-  if (!ok) {
-    v = make_double2(0.0 / 0.0, 0.0 / 0.0);  // invalid descriptor: NaN, no out-of-range read
-  } else if (fd.x == R2K_MOM0) {
-    v = XR[((long long)fd.y * nR + r) * nw2 + mn];
-  } else if (fd.x == R2K_DER1) {  // i w_a X
-    v = cmuli(cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], w[fd.z]));
-  } else if (fd.x == R2K_DER2) {  // -w_a w_b X
-    v = cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], -w[fd.z] * w[fd.w]);
-  } else {
-    // rotAA_g = i w_alpha A_beta - i w_beta A_alpha, (alpha, beta) = ((1,2),(2,0),(0,1))[g]
-    const int al = (fd.z + 1) % 3, be = (fd.z + 2) % 3;
-    const double2 Ab = XR[((long long)(fd.y + be) * nR + r) * nw2 + mn];
-    const double2 Aa = XR[((long long)(fd.y + al) * nR + r) * nw2 + mn];
-    v = cmuli(csub(cscale(Ab, w[al]), cscale(Aa, w[be])));
-    if (fd.x == R2K_DROT) v = cmuli(cscale(v, w[fd.w]));  // derivative of the curl
+  for (int f = 0; f < nF; ++f) {
+    const int4 fd = fdesc[f];
+    const bool idx_ok = fd.z >= 0 && fd.z < 3 && fd.w >= 0 && fd.w < 3 && fd.y >= 0;
+    const bool ok = idx_ok && ((fd.x <= R2K_DER2 && fd.y < nBase) || (fd.x >= R2K_ROT && fd.y + 2 < nBase)) &&
+                    fd.x >= 0 && fd.x <= R2K_DROT;
+    double2 v = make_double2(0.0, 0.0);
+    if (!ok) {
+      v = make_double2(0.0 / 0.0, 0.0 / 0.0);  // invalid descriptor: NaN, no out-of-range read
+    } else if (fd.x == R2K_MOM0) {
+      v = XR[((long long)fd.y * nR + r) * nw2 + mn];
+    } else if (fd.x == R2K_DER1) {  // i w_a X
+      v = cmuli(cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], w[fd.z]));
+    } else if (fd.x == R2K_DER2) {  // -w_a w_b X
+      v = cscale(XR[((long long)fd.y * nR + r) * nw2 + mn], -w[fd.z] * w[fd.w]);
+    } else {
+      // rotAA_g = i w_alpha A_beta - i w_beta A_alpha, (alpha, beta) = ((1,2),(2,0),(0,1))[g]
+      const int al = (fd.z + 1) % 3, be = (fd.z + 2) % 3;
+      const double2 Ab = XR[((long long)(fd.y + be) * nR + r) * nw2 + mn];
+      const double2 Aa = XR[((long long)(fd.y + al) * nR + r) * nw2 + mn];
+      v = cmuli(csub(cscale(Ab, w[al]), cscale(Aa, w[be])));
+      if (fd.x == R2K_DROT) v = cmuli(cscale(v, w[fd.w]));  // derivative of the curl
+    }
+    const typename C2<T>::t h = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
+    XF[((long long)f * nR + r) * nw2 + mn] = h;
+    if constexpr (std::is_same<T, float>::value)
+      if (XFlo) XFlo[((long long)f * nR + r) * nw2 + mn] = mkc<T>((T)(v.x - (double)h.x), (T)(v.y - (double)h.y));
   }
-  const typename C2<T>::t h = mkc<T>(real_from_double<T>(v.x), real_from_double<T>(v.y));
-  XF[((long long)f * nR + r) * nw2 + mn] = h;
-  if constexpr (std::is_same<T, float>::value)
-    if (XFlo) XFlo[((long long)f * nR + r) * nw2 + mn] = mkc<T>((T)(v.x - (double)h.x), (T)(v.y - (double)h.y));
 }
 
 // Column c of the launch -> (field, element).  cols == nullptr: all nF * nw2 columns.
@@ -370,16 +371,16 @@ int wbg_r2k_fields_run(const void* XR, int nBase, const int* iRsorted, int nR, i
   if (!XR || !iRsorted || !fdesc || !wcc || !lat || !XF || nBase < 1 || nR < 1 || nw < 1 || nF < 1)
     return WBG_ERR_ARG;
   const long long n = (long long)nR * nw * nw;
-  dim3 grid((unsigned)((n + 255) / 256), nF);
+  const unsigned grid = (unsigned)((n + 255) / 256);
   if (prec < 0 || prec > 3) return WBG_ERR_ARG;
   if (prec == 1)
-    r2k_weights<double><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+    r2k_weights<double><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, nF, wcc, *lat, nBase, nR, nw,
                                                   (double2*)XF, nullptr);
   else if (prec == 2)
-    r2k_weights<df64><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+    r2k_weights<df64><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, nF, wcc, *lat, nBase, nR, nw,
                                                 (cdf*)XF, nullptr);
   else  // prec 3: residuals right after the rounded values
-    r2k_weights<float><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, wcc, *lat, nBase, nR, nw,
+    r2k_weights<float><<<grid, 256, 0, stream>>>((const double2*)XR, iRsorted, fdesc, nF, wcc, *lat, nBase, nR, nw,
                                                  (float2*)XF, prec == 3 ? (float2*)XF + n * nF : nullptr);
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -109,6 +109,8 @@ WBG_D void mma_commit(uint32_t mbar) {
 WBG_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 WBG_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 WBG_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// hint: bring the 128-byte line holding p into L2 (no register result, no fault semantics)
+WBG_D void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 WBG_D unsigned long long global_ns() {
   unsigned long long t;
@@ -327,6 +329,27 @@ __global__ void __launch_bounds__(NTHR, 2)
         tc_fence_after();
         issue_gemm(D1, Ah, Al, Bh, Bl);
         mma_commit(mb);
+      }
+      {  // while the products and the epilogue of this tile run: L2 prefetch of the rows the next
+         // tile stages (or of the next k-point's U and first tile)
+        const bool last = t + 1 == ntiles;
+        const long long kn = last ? k + gridDim.x : k;
+        if (kn < nk) {
+          const int tn = last ? 0 : t + 1;
+          if (last && tid < NW * NW * 8 / 128) prefetch_l2(reinterpret_cast<const char*>(U + kn * strideU) + tid * 128);
+          constexpr int CPR = NW / 4;
+          constexpr int PER = FPT * NW * CPR / NTHR;
+#pragma unroll
+          for (int i = 0; i < PER; ++i) {
+            const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
+            if ((n0 & 15) != 0) continue;  // one prefetch per 128-byte line (16 complex floats)
+            const int f = tmap_s[tn * FPT + fl];
+            if (f < 0) continue;
+            const int fs = fsel[f];
+            if (fs < 0 || fs >= nFin) continue;
+            prefetch_l2(X + (kn * nFin + fs) * (long long)(NW * NW) + m * NW + n0);
+          }
+        }
       }
       if (!wait_all(mb, phase, &abort_s)) break;
       phase ^= 1;

@@ -187,7 +187,14 @@ class DeviceSystem:
         self.system = system
         self.device = torch.device(device)
         self.nw = system.num_wann
-        self.geom = RGeometry(system.iRvec)
+        # the R-vector structure is host metadata of the system: kept with it, keyed by its R-vectors
+        iR = np.ascontiguousarray(system.iRvec, dtype=np.int64)
+        gkey = (iR.shape, hash(iR.tobytes()))
+        cached = system.__dict__.get('_rgeom')
+        if cached is None or cached[0] != gkey:
+            cached = (gkey, RGeometry(iR))
+            system.__dict__['_rgeom'] = cached
+        self.geom = cached[1]
         self.lattice = np.array(system.real_lattice, dtype=float)
         self.wcc = np.array(system.wannier_centers_cart, dtype=float)
         self._cache = {}
@@ -197,28 +204,36 @@ class DeviceSystem:
         """Base matrices whose R-space data are Hermitian, X_R = X_{-R}^dagger within rtol of
         max |X| with every -R present: for them the k-space fields are exactly Hermitian and the
         mixed path transforms only lower triangles.  Other bases keep the full-matrix path with
-        the reference's symmetrisation (checked once per system)."""
+        the reference's symmetrisation.  The verdict is a property of the host matrices: it is
+        computed on the device once and kept with the system's pinned upload copies (dropped
+        when set_R_mat or do_ws_dist change the matrices)."""
         if 'herm_bases' not in self._cache:
-            R = self.geom.R  # sorted by (R0, R1, R2): -R found by a binary search on the packed keys
-            span = 2 * int(np.abs(R).max()) + 1
-            pack = lambda a: ((a[:, 0] * span) + a[:, 1]) * span + a[:, 2]
-            keys = pack(R)
-            pos = np.searchsorted(keys, pack(-R))
-            pos = np.minimum(pos, len(keys) - 1)
+            verdicts = self.system.__dict__.setdefault('_herm_cache', {})
             out = set()
-            if np.array_equal(keys[pos], pack(-R)):
-                neg = torch.from_numpy(pos).to(self.device)
-                nw = self.nw
-                for key in ('Ham', 'AA', 'SS'):
-                    if not self.system.has_R_mat(key):
-                        continue
-                    X = self._key_fp64(key).reshape(-1, len(R), nw, nw)  # device, sorted R order
-                    Xd = X[:, neg].conj().transpose(2, 3)
-                    diff, mx = (X - Xd).abs().max(), X.abs().max()
-                    if float(diff) <= rtol * max(float(mx), 1e-300):
-                        out.add(key)
+            for key in ('Ham', 'AA', 'SS'):
+                if not self.system.has_R_mat(key):
+                    continue
+                if (key, rtol) not in verdicts:
+                    verdicts[(key, rtol)] = self._hermitian_on_device(key, rtol)
+                if verdicts[(key, rtol)]:
+                    out.add(key)
             self._cache['herm_bases'] = frozenset(out)
         return self._cache['herm_bases']
+
+    def _hermitian_on_device(self, key, rtol):
+        R = self.geom.R  # sorted by (R0, R1, R2): -R found by a binary search on the packed keys
+        span = 2 * int(np.abs(R).max()) + 1
+        pack = lambda a: ((a[:, 0] * span) + a[:, 1]) * span + a[:, 2]
+        keys = pack(R)
+        pos = np.minimum(np.searchsorted(keys, pack(-R)), len(keys) - 1)
+        if not np.array_equal(keys[pos], pack(-R)):
+            return False
+        neg = torch.from_numpy(pos).to(self.device)
+        nw = self.nw
+        X = self._key_fp64(key).reshape(-1, len(R), nw, nw)  # device, sorted R order
+        Xd = X[:, neg].conj().transpose(2, 3)
+        diff, mx = (X - Xd).abs().max(), X.abs().max()
+        return float(diff) <= rtol * max(float(mx), 1e-300)
 
     def bases_for(self, keys):
         """Base-field list for the R->k launch: Ham, then the components of each extra key."""
@@ -271,18 +286,37 @@ class DeviceSystem:
         return self.workspace().side_stream()
 
     def grid_phases(self, shifts, NKFFT, prec):
-        """Device-resident per-axis phase tables for every block of a grid (built once per grid)."""
+        """Device-resident per-axis phase tables for every block of a grid (built once per grid):
+        the three tables of one precision go up in one copy (from page-locked memory when large)."""
         shifts = np.ascontiguousarray(shifts, dtype=np.float64)
-        key = ('phases', tuple(int(n) for n in NKFFT), int(prec), hash(shifts.tobytes()), shifts.shape)
+        skey = (tuple(int(n) for n in NKFFT), hash(shifts.tobytes()), shifts.shape)
+        key = ('phases',) + skey + (int(prec),)
         if key not in self._cache:
-            tabs = []
-            for p in self.geom.phases(shifts, NKFFT):
+            hkey = ('phases_host',) + skey
+            if hkey not in self._cache:
+                self._cache[hkey] = self.geom.phases(shifts, NKFFT)
+            parts = []
+            for p in self._cache[hkey]:
                 if prec == PREC_DF64:
-                    host = torch.from_numpy(_df64_pairs(p))
+                    parts.append(_df64_pairs(p))
                 else:
-                    host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64))
-                tabs.append(host.to(self.device))
+                    parts.append(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64))
+            # one flat buffer of the tables' real words (float64 for FP64, float32 otherwise); every
+            # table starts on a multiple of its element size
+            words = [a.reshape(-1).view(np.float64 if a.dtype == np.complex128 else np.float32) for a in parts]
+            host = torch.from_numpy(np.concatenate(words))
+            if torch.cuda.is_available() and host.numel() * host.element_size() > (4 << 20):
+                host = host.pin_memory()  # large tables: asynchronous copy from page-locked memory
+            dev_flat = host.to(self.device, non_blocking=host.is_pinned())
+            tabs, off = [], 0
+            for a, w in zip(parts, words):
+                t = dev_flat[off:off + w.size]
+                off += w.size
+                if np.iscomplexobj(a):
+                    t = torch.view_as_complex(t.view(-1, 2))
+                tabs.append(t.view(a.shape))
             self._cache[key] = tabs
+            self._cache[key + ('staging',)] = host  # page-locked source of the in-flight copy
         return self._cache[key]
 
     def wcc_tensor(self, fp64):

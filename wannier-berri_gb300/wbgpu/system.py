@@ -80,6 +80,7 @@ class System_R:
             f"{key}: expected shape ({self.nRvec}, {self.num_wann}, {self.num_wann}, ...), got {value.shape}"
         if Hermitian:
             value = 0.5 * (value + self.conj_XX_R(value))
+        self._drop_host_caches(key)
         if key in self._XX_R:
             if reset:
                 self._XX_R[key] = value
@@ -89,6 +90,19 @@ class System_R:
                 raise RuntimeError(f"setting {key} for the second time without explicit permission")
         else:
             self._XX_R[key] = value
+
+    def _drop_host_caches(self, key=None):
+        """Forget what the engine derived from the matrices on the host (pinned upload copies,
+        Hermiticity verdicts): for `key`, or all of them when the R-vectors change."""
+        for name in ('_pinned_cache', '_herm_cache'):
+            cache = self.__dict__.get(name)
+            if cache is None:
+                continue
+            if key is None:
+                cache.clear()
+            else:
+                for k in [k for k in cache if k == key or (isinstance(k, tuple) and k[0] == key)]:
+                    del cache[k]
 
     @property
     def NKFFT_recommended(self):
@@ -104,6 +118,7 @@ class System_R:
         """MDRS: replace (iRvec, XX_R) by the Wigner-Seitz replica set (system/system_R.py:572-588).
         device: None searches the replicas on the host, 'cuda' with the wbg_ws_replicas kernel."""
         mp = np.array(mp_grid if np.ndim(mp_grid) else [mp_grid] * 3, dtype=int)
+        self._drop_host_caches()
         self.iRvec, self._XX_R = mdrs_remap(self.real_lattice, self.wannier_centers_red, self.iRvec,
                                             self._XX_R, mp, ws_dist_tol, device=device)
         self._NKFFT_recommended = mp
