@@ -132,3 +132,35 @@ def test_field_plan_layout():
     assert index == {'H': 0, 'V': 1, 'A': 4, 'O': 7}
     assert desc[0] == (0, 0, 0, 0) and desc[1] == (1, 0, 0, 0) and desc[7] == (3, 1, 0, 0)
     assert engine.order_for({'V', 'A', 'O'}) == 1 and engine.order_for({'W'}) == 2
+
+
+def test_host_caches_follow_the_matrices():
+    """The pinned upload copies and Hermiticity verdicts kept with a system are dropped when
+    set_R_mat replaces or adds to a matrix, and all of them when do_ws_dist changes the R-vectors."""
+    d = models.config_system(2, small=True)
+    s = wsys.System_R.from_dict(d)
+    order = np.arange(s.nRvec)
+    first = engine.host_pinned(s, 'Ham', order).clone()
+    engine.host_pinned(s, 'AA', order)
+    s.__dict__.setdefault('_herm_cache', {})[('Ham', 1e-12)] = True
+    s.set_R_mat('Ham', 2 * s.get_R_mat('Ham'), reset=True)
+    assert ('Ham', 1e-12) not in s._herm_cache and 'AA' in s._pinned_cache
+    again = engine.host_pinned(s, 'Ham', order)
+    assert np.allclose(again.numpy(), 2 * first.numpy())
+    s.do_ws_dist(3)
+    assert not s._pinned_cache and not s._herm_cache
+    assert engine.host_pinned(s, 'Ham', np.arange(s.nRvec)).shape[1] == s.nRvec
+
+
+def test_spin_field_plan_and_hermitian_flags():
+    """Spin quantities: 9-component keys take 9 bases, SS follows its Hermiticity verdict, SA etc.
+    never count as Hermitian."""
+    keys = engine.extra_keys_for({'V', 'A', 'S', 'SA', 'SHA'})
+    assert keys == ['AA', 'SS', 'SA', 'SHA']
+    desc, index = engine.field_plan({'V', 'A', 'S', 'SA', 'SHA'}, False, keys)
+    assert [index[q] for q in ('V', 'A', 'S', 'SA', 'SHA')] == [0, 3, 6, 9, 18]
+    assert desc[9] == (0, 1 + 3 + 3, 0, 0) and desc[26] == (0, 1 + 3 + 3 + 9 + 8, 0, 0)
+    herm = engine.hermitian_fields({'V', 'A', 'S', 'SA'}, False, herm_bases=('Ham', 'AA', 'SS'))
+    assert herm == [True] * 9 + [False] * 9
+    herm = engine.hermitian_fields({'S'}, False, herm_bases=('Ham', 'AA'))
+    assert herm == [False] * 3
