@@ -656,9 +656,18 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         if quantities:
             # the FP32 fields do not depend on the eigensolver: their transform runs on a side
             # stream next to the QL iteration (a few warps per SM, latency-bound), started once
-            # the tridiagonalisation (which fills the SMs' shared memory) is done
+            # the tridiagonalisation (which fills the SMs' shared memory) is done.  A fresh system's
+            # upload of the other R-space matrices and their weights go ahead on the side stream
+            # right away (after the main stream's upload of H, which they also read).
             main = torch.cuda.current_stream()
             side = arena.side_stream()
+            ck = ('XF', tuple(sorted(quantities)), False, PREC_FP32S)
+            if ck not in dev._cache:
+                h_ready = torch.cuda.Event()
+                h_ready.record(main)
+                with torch.cuda.stream(side):
+                    side.wait_event(h_ready)
+                    field_arrays(dev, quantities, False, PREC_FP32S)
             eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode | EIGH_STAGE1, work=ework, flag=flag)
             tridiag_done = torch.cuda.Event()
             tridiag_done.record(main)
