@@ -360,6 +360,32 @@ int wbg_berry_shc(const double* E, const void* Xbar, int nFbar, const wbg_dynami
 /* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
 int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);
 
+/* ---- launch-shape table of the autotuner (no reference counterpart: the reference's numpy
+ * calls have no launch shapes) ------------------------------------------------------------------
+ * A host-side table, per (parameter, variant, nw), of launch shapes that a tuner measured to be
+ * fastest; 0 (the initial value) selects the built-in occupancy heuristic.  Parameters:
+ *   WBG_TUNE_EIGH_TRIDIAG_GROUP  matrices per block of the tridiagonalisation   variant: eigh mode & 3
+ *   WBG_TUNE_EIGH_QL_BLOCK       matrices (threads) per block of the QL sweep   variant: eigh mode & 3
+ *   WBG_TUNE_EIGH_VECTORS_GROUP  matrices per block of the inverse iteration and
+ *                                back-transform                                variant: eigh mode & 3
+ *   WBG_TUNE_ROTATE_KPOINTS      k-points per block of the CUDA-core tiled U^dagger X U  variant: fp64
+ *   WBG_TUNE_ROTATE_ENGINE       1 tensor cores, 2 CUDA cores (where both serve the case) variant: fp64
+ * wbg_tune_candidates lists the values that fit the launch limits of (parameter, nw, variant);
+ * wbg_tune_set accepts 0 or one of them (else WBG_STATUS_BAD_ARGUMENT), so every launch shape
+ * the table can select is one the kernels accept.  Results do not depend on the eigensolver and
+ * tiled-rotation shapes (each matrix or k-point is computed by the same code whatever the
+ * grouping); the rotation engine changes the FP32 rounding (both within the FP32 path's error
+ * budget).  The table is process-wide: set it before launching work that should use it. */
+#define WBG_TUNE_EIGH_TRIDIAG_GROUP 0
+#define WBG_TUNE_EIGH_QL_BLOCK 1
+#define WBG_TUNE_EIGH_VECTORS_GROUP 2
+#define WBG_TUNE_ROTATE_KPOINTS 3
+#define WBG_TUNE_ROTATE_ENGINE 4
+#define WBG_TUNE_NPARAM 5
+int wbg_tune_candidates(int param, int nw, int variant, int* values, int capacity, int* count);
+int wbg_tune_set(int param, int nw, int variant, int value);
+int wbg_tune_get(int param, int nw, int variant, int* value);
+
 /* ---- measurement helper (no reference counterpart) ----------------------------------------
  * FMA throughput probe giving the roofline denominator of FP64- / FP32-pipe-bound kernels:
  * blocks*threads threads run 8 independent FMA chains of `iters` steps; out holds

@@ -11,6 +11,7 @@
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_band.cuh"
+#include "wbgpu_tune.cuh"
 #include "wbgpu_spin.cuh"
 
 namespace {
@@ -1361,6 +1362,12 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
+// k-points per block of rotate_tiled that fit: a power of two, at most 256 threads and 200 KB of
+// shared memory per block
+bool tiled_kpoints_fit(int kb, int tpk, size_t per_k) {
+  return kb >= 1 && !(kb & (kb - 1)) && kb * tpk <= 256 && (size_t)kb * per_k <= 200 * 1024;
+}
+
 template <typename T>
 int launch_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                   int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
@@ -1383,6 +1390,8 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
     int KB = 1;
     while (KB * 2 * tpk <= 256 && (KB * 2) * per_k <= 64 * 1024) KB *= 2;
     if (KB * per_k <= 200 * 1024) {
+      const int t = wbg_tuned(WBG_TUNE_ROTATE_KPOINTS, sizeof(T) == 8 ? 1 : 0, nw);
+      if (t > 0 && tiled_kpoints_fit(t, tpk, per_k)) KB = t;
       cudaFuncSetAttribute(rotate_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       rotate_tiled<T><<<(nk + KB - 1) / KB, KB * tpk, KB * per_k, stream>>>((const V*)U, strideU, (const V*)X, nFin,
                                                                            fsel, herm, nFrot, (V*)Xbar, nw, nk, KB);
@@ -1403,11 +1412,32 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
 int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream) {
   if (nw < 1 || nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
-  // tensor cores (3xTF32) for the FP32 path at nw = 32; the kernel reads X in 16-byte pieces
-  if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+  // tensor cores (3xTF32) for the FP32 path at nw = 32 (unless the tuner chose the CUDA cores);
+  // the kernel reads X in 16-byte pieces
+  if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0 &&
+      wbg_tuned(WBG_TUNE_ROTATE_ENGINE, fp64 ? 1 : 0, nw) != 2)
     return wbg_rotate_tc_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   if (fp64) return launch_rotate<double>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   return launch_rotate<float>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
+}
+
+int wbg_rotate_tune_candidates(int param, int nw, int variant, int* values, int capacity) {
+  int count = 0;
+  if (param == WBG_TUNE_ROTATE_ENGINE) {
+    if (wbg_rotate_tc_supported(nw, variant, 1))
+      for (int v = 1; v <= 2 && count < capacity; ++v) values[count++] = v;
+    return count;
+  }
+  if (param != WBG_TUNE_ROTATE_KPOINTS || nw % 4 != 0 || nw < 8 || nw > 64) return 0;
+  // the tiled kernel serves this (nw, precision) when its built-in block fits (launch_rotate)
+  const int tpk = (nw / 4) * (nw / 4);
+  const size_t per_k = ((size_t)nw * nw * 2 + (size_t)nw * (nw + 1)) * (variant ? 16 : 8);
+  int KB = 1;
+  while (KB * 2 * tpk <= 256 && (KB * 2) * per_k <= 64 * 1024) KB *= 2;
+  if (KB * per_k > 200 * 1024) return 0;
+  for (int v = 1; v <= 256; v *= 2)
+    if (tiled_kpoints_fit(v, tpk, per_k) && count < capacity) values[count++] = v;
+  return count;
 }
 
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,

@@ -19,6 +19,7 @@
 #include "wbgpu_common.cuh"
 #include "wbgpu_df64.cuh"
 #include "wbgpu_eigh.cuh"
+#include "wbgpu_tune.cuh"
 
 namespace {
 
@@ -537,9 +538,68 @@ int pick_group(size_t smem, int threads, int gmax) {
   return best;
 }
 
+// Launch shapes of the three kernels for n x n matrices (R: arithmetic of the solve, TU: type of
+// the back-transform): lanes and shared memory per matrix, the largest group each kernel takes,
+// the built-in choices, and which other group sizes fit (the autotuner's candidates).
+template <typename R, typename TU>
+struct EighShape {
+  int L, LT, CW, gmaxT, gmaxV;
+  size_t smT, smQ1, smV;  // shared memory per matrix: tridiagonalisation, QL (d and e), vectors
+  explicit EighShape(int n) {
+    typedef typename C2<R>::t CR;
+    typedef typename C2<TU>::t VU;
+    L = lanes_for(n);
+    // tridiagonalisation: mirrored row pairs on half the lanes (balanced rows; one row per lane
+    // on all 32 lanes measured 22% slower at nw = 32)
+    LT = L >= 8 ? L / 2 : 4;
+    gmaxT = 128 / LT;
+    smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
+    smQ1 = 2 * (size_t)n * sizeof(R);  // d and e of one matrix (one thread per matrix)
+    const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
+    const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
+    CW = n;  // back-transform chunk width: the whole U unless it does not fit next to Z
+    auto ub = [&](int cw) { return kUOverlaysZ<R, TU> ? (size_t)0 : ((size_t)n * cw * sizeof(VU) + 15) / 16 * 16; };
+    if (!kUOverlaysZ<R, TU> && zbytes + ub(n) + vbytes > kMaxBlockSmem) CW = 32;
+    smV = zbytes + ub(CW) + vbytes;
+    gmaxV = 64 / L;
+  }
+  int tridiag_default() const { return pick_group(smT, LT, gmaxT); }
+  int ql_default() const {
+    int BQ = 128;  // threads (matrices) per block
+    while (BQ > 32 && (size_t)BQ * smQ1 > 64 * 1024) BQ /= 2;
+    return BQ;
+  }
+  int vectors_default() const { return pick_group(smV, L, gmaxV); }
+  // a group size fits: power of two up to gmax whose shared memory fits one block, and whole
+  // warps unless it is the largest size that fits (the heuristic's choice when memory-bound)
+  static bool group_fits(int g, size_t smem, int lanes, int gmax) {
+    if (g < 1 || g > gmax || (g & (g - 1)) || (size_t)g * smem > kMaxBlockSmem) return false;
+    const bool larger = 2 * g <= gmax && (size_t)2 * g * smem <= kMaxBlockSmem;
+    return (g * lanes) % 32 == 0 || !larger;
+  }
+  bool fits(int param, int v) const {
+    if (param == WBG_TUNE_EIGH_TRIDIAG_GROUP) return group_fits(v, smT, LT, gmaxT);
+    if (param == WBG_TUNE_EIGH_VECTORS_GROUP) return group_fits(v, smV, L, gmaxV);
+    if (param == WBG_TUNE_EIGH_QL_BLOCK)
+      return v >= 32 && v <= 256 && !(v & (v - 1)) && (size_t)v * smQ1 <= kMaxBlockSmem;
+    return false;
+  }
+  // the tuned value of `param` when one is set and fits, else the built-in choice
+  int choose(int param, int variant, int n, int dflt) const {
+    const int t = wbg_tuned(param, variant, n);
+    return (t > 0 && fits(param, t)) ? t : dflt;
+  }
+  int candidates(int param, int* values, int capacity) const {
+    int count = 0;
+    for (int v = 1; v <= 256; v *= 2)
+      if (fits(param, v) && count < capacity) values[count++] = v;
+    return count;
+  }
+};
+
 template <typename R, typename TU, typename HIn>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int lowerIn,
-                int valuesOnly, int stage, void* workspace, int* errflag, cudaStream_t stream) {
+                int valuesOnly, int stage, int variant, void* workspace, int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
   typedef typename C2<TU>::t VU;
   char* w = (char*)workspace;
@@ -547,33 +607,28 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   VU* tau = (VU*)w; w += (size_t)nk * n * 16;
   R* d = (R*)w; w += (size_t)nk * n * 8;
   R* e = (R*)w;
-  const int L = lanes_for(n);
-  // tridiagonalisation: mirrored row pairs on half the lanes (balanced rows; one row per lane
-  // on all 32 lanes measured 22% slower at nw = 32)
-  const int LT = L >= 8 ? L / 2 : 4;
+  const EighShape<R, TU> sh(n);
+  const int L = sh.L, LT = sh.LT;
   if (stage != 2) {  // stage 1 (or both): the tridiagonalisation into the workspace
-    const size_t smT = ((size_t)n * (n + 1) / 2 + 2 * n) * sizeof(CR);
-    const int G = pick_group(smT, LT, 128 / LT);
-    if (G == 0) return WBG_ERR_SIZE;
+    const size_t smT = sh.smT;
+    const int G0 = sh.tridiag_default();
+    if (G0 == 0) return WBG_ERR_SIZE;
+    const int G = sh.choose(WBG_TUNE_EIGH_TRIDIAG_GROUP, variant, n, G0);
     cudaFuncSetAttribute(eigh_tridiag<R, HIn, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
     eigh_tridiag<R, HIn, TU><<<(nk + G - 1) / G, G * LT, G * smT, stream>>>((const HIn*)H, strideH, n, nk, LT, G,
                                                                              lowerIn, Vh, tau, d, e);
     if (stage == 1) return wbg_cuda_status(cudaGetLastError());
   }
-  int BQ = 128;  // threads (matrices) per block: d and e take 2 n sizeof(R) bytes of shared memory each
-  while (BQ > 32 && (size_t)BQ * 2 * n * sizeof(R) > 64 * 1024) BQ /= 2;
-  const size_t smQ = (size_t)BQ * 2 * n * sizeof(R);
+  const int BQ = sh.choose(WBG_TUNE_EIGH_QL_BLOCK, variant, n, sh.ql_default());
+  const size_t smQ = (size_t)BQ * sh.smQ1;
   cudaFuncSetAttribute(eigh_ql<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_ql<R><<<(nk + BQ - 1) / BQ, BQ, smQ, stream>>>(d, e, n, nk, (double*)E, errflag);
   if (valuesOnly) return wbg_cuda_status(cudaGetLastError());
-  const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
-  const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
-  int CW = n;  // back-transform chunk width: the whole U unless it does not fit next to Z
-  auto ub = [&](int cw) { return kUOverlaysZ<R, TU> ? (size_t)0 : ((size_t)n * cw * sizeof(VU) + 15) / 16 * 16; };
-  if (!kUOverlaysZ<R, TU> && zbytes + ub(n) + vbytes > kMaxBlockSmem) CW = 32;
-  const size_t smV = zbytes + ub(CW) + vbytes;
-  const int GV = pick_group(smV, L, 64 / L);
-  if (GV == 0) return WBG_ERR_SIZE;
+  const int CW = sh.CW;
+  const size_t smV = sh.smV;
+  const int GV0 = sh.vectors_default();
+  if (GV0 == 0) return WBG_ERR_SIZE;
+  const int GV = sh.choose(WBG_TUNE_EIGH_VECTORS_GROUP, variant, n, GV0);
   cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
   eigh_vectors<R, TU><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
                                                                         CW, (VU*)U, strideU);
@@ -599,16 +654,26 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
   switch (mode & 3) {
     case 1:
-      return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
-                                                  stream);
+      return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 1, workspace,
+                                                  errflag, stream);
     case 0:
-      return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
-                                                 stream);
+      return launch_eigh<double, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 0, workspace,
+                                                 errflag, stream);
     case 2:
-      return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag,
-                                               stream);
+      return launch_eigh<df64, float, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 2, workspace,
+                                               errflag, stream);
     default:
-      return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, workspace, errflag, stream);
+      return launch_eigh<df64, float, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 3, workspace, errflag,
+                                           stream);
+  }
+}
+
+int wbg_eigh_tune_candidates(int param, int n, int variant, int* values, int capacity) {
+  if (n < 1 || n > WBG_EIGH_NMAX) return 0;
+  switch (variant) {  // eigh mode & 3: the (solve, back-transform) types of wbg_eigh_run
+    case 1: return EighShape<double, double>(n).candidates(param, values, capacity);
+    case 0: return EighShape<double, float>(n).candidates(param, values, capacity);
+    default: return EighShape<df64, float>(n).candidates(param, values, capacity);
   }
 }
 

@@ -15,7 +15,8 @@ EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_wo
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
            'wbg_dynamic_ncomp', 'wbg_dynamic_workspace_size', 'wbg_dynamic', 'wbg_berry_shc',
-           'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma']
+           'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma',
+           'wbg_tune_candidates', 'wbg_tune_set', 'wbg_tune_get']
 
 STATUS_OK = 0
 
@@ -95,6 +96,9 @@ _SIGS = {
     'wbg_tetra_accumulate': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, _P, _P, _I, _P, _I, _I, _I, _I,
                                   _P, _P]),
     'wbg_probe_fma': (_I, [_I, _I, _I, _I, _P, ctypes.POINTER(ctypes.c_double), _P]),
+    'wbg_tune_candidates': (_I, [_I, _I, _I, ctypes.POINTER(_I), _I, ctypes.POINTER(_I)]),
+    'wbg_tune_set': (_I, [_I, _I, _I, _I]),
+    'wbg_tune_get': (_I, [_I, _I, _I, ctypes.POINTER(_I)]),
 }
 
 _lib = None

@@ -138,14 +138,23 @@ def run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_
 
 
 def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, device='cuda', dev_system=None,
-        blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1, **_ignored):
+        blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1, cuda_graph=False, autotune=False, **_ignored):
     """Integrate ``calculators`` over ``grid``.  precision: 'fp64' (plain) or 'mixed'
     (double-float H(k) and eigh, FP64 scan, FP32 fields and rotations).  ``blocks`` restricts the
     run to a subset of the division-grid K-points (indices into Grid.block_shifts());
     the result then carries the same 1/prod(NKdiv) weight per block.  ``adpt_num_iter`` > 0:
-    adaptive refinement with the reference's policy (``adpt_mesh``, ``adpt_fac``)."""
+    adaptive refinement with the reference's policy (``adpt_mesh``, ``adpt_fac``).
+    ``cuda_graph``: stages 1-3 of every batch after the first two of a shape are replayed from
+    a CUDA graph (engine.band_data_graphed; bit-identical results, fewer host calls per batch).
+    The eigensolver's convergence flags are read once, after the last batch, so the host queues
+    batch after batch without waiting for the device.
+    ``autotune``: launch shapes of the eigensolver and the rotation for this num_wann and
+    precision from the autotuner (wbgpu.autotune.ensure: cached per device, measured once)."""
     engine.require_cuda()
     dev = dev_system or engine.DeviceSystem(system, device)
+    if autotune:
+        from . import autotune as _tune
+        _tune.ensure(dev.nw, precision, device=dev.device)
     if adpt_num_iter:
         if blocks is not None:
             raise ValueError("adaptive refinement runs over the whole grid (blocks must be None)")
@@ -166,15 +175,17 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
         tetra = engine.TetraCorners(dev, grid, block_ids, precision)
     precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
+    stages = engine.band_data_graphed if cuda_graph else engine.band_data
+    flags = []
     for i0 in range(0, len(shifts), nb):
-        bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
-                              block_start=i0)
+        bd = stages(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases, block_start=i0)
         if tetra is not None:
             tetra.attach(bd, block_ids[i0:i0 + nb])
         for c in calculators.values():
             c.accumulate(bd, system)
-        engine.check_flag(bd)
+        flags.append(bd._flag.clone())  # the batch's QL flag (its buffer is reused by the next batch)
         del bd
+    engine.check_flags(flags)
     if tetra is not None:
         tetra.check()
     factor = 1.0 / grid.nblocks

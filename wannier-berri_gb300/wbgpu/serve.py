@@ -114,12 +114,18 @@ class Server:
 
     precision: 'mixed' or 'fp64' (as run()); hbm_budget: bytes of per-request buffers allowed
     at once; max_active: requests in flight (one CUDA stream each); max_kpoints: k-points per
-    block batch."""
+    block batch; cuda_graph: replay stages 1-3 of a request's batches from CUDA graphs
+    (engine.band_data_graphed, one set per request workspace); autotune: launch shapes of each
+    resident system's num_wann from the autotuner (wbgpu.autotune.ensure, at add_system)."""
 
-    def __init__(self, device='cuda', precision='mixed', hbm_budget=150 << 30, max_active=4, max_kpoints=1 << 17):
+    def __init__(self, device='cuda', precision='mixed', hbm_budget=150 << 30, max_active=4, max_kpoints=1 << 17,
+                 cuda_graph=False, autotune=False):
         engine.require_cuda()
         self.device = torch.device(device)
         self.precision = precision
+        self.cuda_graph = bool(cuda_graph)
+        self.autotune = bool(autotune)
+        self._tuned = set()
         self.hbm_budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.max_kpoints = int(max_kpoints)
@@ -146,6 +152,10 @@ class Server:
             for name in ['Ham'] + [k for k in ('AA', 'BB', 'CC') if system.has_R_mat(k)]:
                 dev._key_fp64(name)  # upload now: requests find the matrices resident
         self._prep_stream.synchronize()
+        if self.autotune and dev.nw not in self._tuned:
+            from . import autotune as _tune
+            _tune.ensure(dev.nw, self.precision, device=self.device)
+            self._tuned.add(dev.nw)
         self._systems[key] = (system, dev)
         return dev
 
@@ -294,13 +304,14 @@ class Server:
         shifts = req.grid.block_shifts()
         with torch.cuda.stream(req.stream):
             contiguous = np.all(np.diff(idx) == 1)
+            stages = engine.band_data_graphed if self.cuda_graph else engine.band_data
             if req.refine is not None:
                 bd = self._issue_adaptive(req, idx, system, dev)
             elif contiguous:
-                bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision,
-                                      phases=req.phases, block_start=int(idx[0]), ws=req.ws)
+                bd = stages(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision,
+                            phases=req.phases, block_start=int(idx[0]), ws=req.ws)
             else:
-                bd = engine.band_data(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
+                bd = stages(dev, shifts[idx], req.grid.FFT, req.quantities, self.precision, ws=req.ws)
             if req.tetra is not None:
                 req.tetra.attach(bd, idx)
             for c in req.calculators.values():
@@ -415,10 +426,11 @@ class Server:
                 "max_ms": float(lat.max()), "kpoints": int(nk), "kpoints_per_s": nk / max(t1 - t0, 1e-9)}
 
 
-def run_many(jobs, precision='mixed', max_active=4, device='cuda'):
+def run_many(jobs, precision='mixed', max_active=4, device='cuda', cuda_graph=False, autotune=False):
     """Integrate a list of (system, grid, calculators) jobs concurrently through one Server
     (systems made resident once); returns the list of ResultDicts in job order."""
-    srv = Server(device=device, precision=precision, max_active=max_active)
+    srv = Server(device=device, precision=precision, max_active=max_active, cuda_graph=cuda_graph,
+                 autotune=autotune)
     keys = {}
     tickets = []
     for system, grid, calcs in jobs:
