@@ -418,6 +418,12 @@ def run_gpu(args):
             line["configs"] = bench_configs()
         except Exception as e:
             line["configs"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if world == 1 and not args.no_graphs_tune:
+        for key, fn in (("cuda_graph", bench_graphs), ("autotune", bench_autotune)):
+            try:
+                line[key] = fn()
+            except Exception as e:
+                line[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if world == 1 and not args.no_tetra:
         try:
             line["tetra"] = bench_tetra(s, dev, args.nkfft, NKDIV)
@@ -658,6 +664,61 @@ def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
     return st
 
 
+# ---------------------------------------------------------------------------------------
+# CUDA-graph replay and launch-shape autotuning
+# ---------------------------------------------------------------------------------------
+def bench_graphs(reps=3):
+    """run() over many small batches (the cubic nw=8 model, 512 blocks of 4^3, AHC at 501 E_F)
+    with plain launches and with stages 1-3 replayed from CUDA graphs (cuda_graph=True): the
+    regime where per-batch host dispatch, not the GPU, sets the pace."""
+    import numpy as np
+    import torch
+    import wbgpu
+    from wbgpu import engine, models
+    from wbgpu.calculators import AHC
+    s = wbgpu.System_R.from_dict(models.config_system(1))
+    grid = wbgpu.Grid(s, NKdiv=8, NKFFT=4)
+    ef = np.linspace(-2, 2, 501)
+    dev = engine.DeviceSystem(s)
+    nk = grid.nblocks * grid.nk_per_block
+    out = {"workload": "cubic nw=8 model, 32^3 k-points in 512 blocks of 4^3, AHC at 501 E_F, whole run()"}
+    for prec in ('mixed', 'fp64'):
+        for bpb in (4, 16):
+            r = {}
+            for g in (False, True):
+                call = lambda: wbgpu.run(s, grid, {'ahc': AHC(Efermi=ef)}, precision=prec, blocks_per_batch=bpb,
+                                         cuda_graph=g, dev_system=dev)
+                call()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    call()
+                torch.cuda.synchronize()
+                r["graph" if g else "plain"] = nk * reps / (time.perf_counter() - t0)
+            r["speedup"] = r["graph"] / r["plain"]
+            out[f"{prec}_blocks_per_batch_{bpb}_kpoints_per_s"] = r
+    return out
+
+
+def bench_autotune(nws=(8, 32, 96)):
+    """Eigensolver launch time (double-float solve, the mixed path) with the built-in shapes and
+    with the autotuner's choice, per num_wann; the table is restored afterwards."""
+    from wbgpu import autotune
+    out = {"workload": "wbg_eigh_batched mode 3 on seeded random Hermitian matrices "
+                       "(16384 x (32/nw)^3 matrices, clamped to 1024-32768)"}
+    for nw in nws:
+        autotune.reset([nw])
+        base = autotune.time_eigh(nw, 3)
+        t0 = time.perf_counter()
+        entry, _ = autotune.tune_eigh(nw, 3)
+        tune_s = time.perf_counter() - t0
+        tuned = autotune.time_eigh(nw, 3)
+        autotune.reset([nw])
+        out[f"nw{nw}"] = {"matrices": autotune.default_batch(nw), "builtin_ms": base, "tuned_ms": tuned,
+                          "choice": entry, "tuning_s": tune_s}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -675,9 +736,18 @@ def main():
     ap.add_argument('--configs-only', action='store_true', help='run only the nw=8 and nw=96 configurations')
     ap.add_argument('--tetra-only', action='store_true', help='run only the tetrahedron-method measurement')
     ap.add_argument('--tetra-nkdiv', type=int, default=NKDIV, help='NKdiv of --tetra-only')
+    ap.add_argument('--no-graphs-tune', action='store_true', help='skip the CUDA-graph and autotuner measurements')
+    ap.add_argument('--graphs-tune-only', action='store_true', help='run only the CUDA-graph and autotuner measurements')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.graphs_tune_only:
+        import torch
+        from wbgpu import _lib
+        _lib.load()
+        torch.cuda.init()
+        print(json.dumps({"cuda_graph": bench_graphs(), "autotune": bench_autotune()}), flush=True)
+        return 0
     if args.tetra_only:
         return run_tetra_only(args)
     if args.configs_only:

@@ -106,12 +106,10 @@ def default_batch(nw, nk=None):
     return int(min(max(nk, 1024), 32768))
 
 
-def tune_eigh(nw, mode, nk=None, reps=3, seed=0, device='cuda'):
-    """Tune the eigensolver's group sizes for (nw, eigh mode & 3) on nk random Hermitian
-    matrices; the table holds the choice afterwards.  Returns ({name: value}, {name: {value: ms}})."""
+def _eigh_runner(nw, mode, nk, seed, device):
+    """A closure launching wbg_eigh_batched on nk seeded random Hermitian matrices."""
     import torch
     from . import engine
-    nk = default_batch(nw, nk)
     rng = np.random.default_rng(seed)
     A = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
     H = 0.5 * (A + np.conj(np.swapaxes(A, 1, 2)))
@@ -132,8 +130,24 @@ def tune_eigh(nw, mode, nk=None, reps=3, seed=0, device='cuda'):
         _lib.check(lib.wbg_eigh_batched(engine._ptr(Hd), nw * nw, nw, nk, engine._ptr(E), engine._ptr(U), nw * nw,
                                         int(mode), engine._ptr(work), ctypes.c_size_t(work.numel()),
                                         engine._ptr(flag), engine._stream()), "wbg_eigh_batched")
+    return run
 
+
+def time_eigh(nw, mode, nk=None, reps=5, seed=0, device='cuda'):
+    """ms per wbg_eigh_batched launch of `default_batch(nw, nk)` matrices with the table's
+    current shapes."""
+    import torch
+    return _time_ms(torch, _eigh_runner(nw, mode, default_batch(nw, nk), seed, device), reps)
+
+
+def tune_eigh(nw, mode, nk=None, reps=3, seed=0, device='cuda'):
+    """Tune the eigensolver's group sizes for (nw, eigh mode & 3) on nk random Hermitian
+    matrices; the table holds the choice afterwards.  Returns ({name: value}, {name: {value: ms}})."""
+    import torch
+    variant = mode & 3
+    run = _eigh_runner(nw, mode, default_batch(nw, nk), seed, device)
     params = {p: candidates(p, nw, variant) for p in EIGH_PARAMS}
+    params = {p: c for p, c in params.items() if len(c) > 1}
     best, timings = coordinate_descent(params, lambda: _time_ms(torch, run, reps),
                                        lambda p, v: set_value(p, nw, variant, v))
     return ({PARAM_NAMES[p]: v for p, v in best.items()},
