@@ -39,6 +39,8 @@ TAU_UNIT = 1e-15                                               # factors.py:3
 FACTOR_OHMIC = (elementary_charge ** 2 / hbar / angstrom * TAU_UNIT * elementary_charge / hbar)  # factors.py:26
 FACTOR_NLAHC = elementary_charge ** 3 / hbar ** 2 * TAU_UNIT                                      # factors.py:28
 FACTOR_NLDRUDE = -(elementary_charge ** 3 / hbar ** 2 * TAU_UNIT ** 2 * elementary_charge / hbar)  # factors.py:31-32
+FACTOR_HALL_CLASSIC = -(elementary_charge ** 3 / hbar ** 2 * angstrom * TAU_UNIT ** 2 *
+                        elementary_charge ** 2 / hbar ** 2)  # factors.py:29-30
 
 
 # ---------------------------------------------------------------------------
@@ -502,6 +504,39 @@ class VelVelVel(Formula_ln):  # formula/covariant.py VelVelVel: FormulaProduct o
         return np.einsum("LMa,MNb,NKc->LKabc", v, v, v)
 
 
+class Product(Formula_ln):  # formula/formula.py:121-151 (FormulaProduct): in-group matrix product
+    """tr_G(F1_G F2_G ...) with every factor's nn block (the group's sub-matrix) multiplied over
+    the band index; the Cartesian indices of the factors follow one another."""
+
+    def __init__(self, factors):
+        self.factors = list(factors)
+        self.ndim = sum(f.ndim for f in self.factors)
+
+    def nn(self, ik, inn, out):
+        res = self.factors[0].nn(ik, inn, out)
+        for f in self.factors[1:]:
+            m = f.nn(ik, inn, out)
+            t = np.tensordot(res, m, axes=([1], [0]))  # (L, A..., N, B...)
+            res = np.moveaxis(t, res.ndim - 1, 1)
+        return res
+
+
+def VelOmega(data_K, **kw):  # formula/covariant.py:798-801
+    return Product([data_K.covariant('Ham', commader=1), Omega(data_K, **kw)])
+
+
+def MassVel(data_K, **_):  # formula/covariant.py:830-833
+    return Product([InvMass(data_K), data_K.covariant('Ham', commader=1)])
+
+
+def MassMass(data_K, **_):  # formula/covariant.py:836-839
+    return Product([InvMass(data_K), InvMass(data_K)])
+
+
+def VelMassVel(data_K, **_):  # formula/covariant.py:842-846
+    return Product([data_K.covariant('Ham', commader=1), InvMass(data_K), data_K.covariant('Ham', commader=1)])
+
+
 class SpinOmega(Formula_ln):  # formula/covariant.py:759-788, additive; nn block only
     def __init__(self, data_K, spin_current_type="ryoo", external_terms=True, **_):
         self.external_terms = external_terms and not data_K.force_internal_terms_only
@@ -925,6 +960,57 @@ class BerryDipole_FermiSea(StaticCalculator):  # calculators/static.py:472-487
 class NLAHC_FermiSea(BerryDipole_FermiSea):  # calculators/static.py:490-498
     def __init__(self, constant_factor=FACTOR_NLAHC, **kw):
         super().__init__(constant_factor=constant_factor, **kw)
+
+
+class BerryDipole_FermiSurf(StaticCalculator):  # calculators/static.py:449-458: -int v Omega f'
+    Formula = staticmethod(VelOmega)
+    fder = 1
+
+
+class NLAHC_FermiSurf(BerryDipole_FermiSurf):  # calculators/static.py:461-469
+    def __init__(self, constant_factor=FACTOR_NLAHC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class NLDrude_FermiSurf(StaticCalculator):  # calculators/static.py:532-542: int d_b v_a v_c f'
+    Formula = staticmethod(MassVel)
+    fder = 1
+
+    def __init__(self, constant_factor=FACTOR_NLDRUDE, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+def hall_curl(T):
+    """Both antisymmetrisations of the classical Hall tensor (calculators/static.py:418-420,
+    440-442): T[e, p, q, r, s] -> X[e, p, q, g] = T[.., BETA_g, ALPHA_g] - T[.., ALPHA_g, BETA_g],
+    then out[e, h, g] = (X[e, ALPHA_h, BETA_h, g] - X[e, BETA_h, ALPHA_h, g]) / 2."""
+    X = T[:, :, :, BETA, ALPHA] - T[:, :, :, ALPHA, BETA]
+    return 0.5 * (X[:, ALPHA, BETA, :] - X[:, BETA, ALPHA, :])
+
+
+class Hall_classic_FermiSurf(StaticCalculator):  # calculators/static.py:407-424: v_a d_r v_b v_g f'
+    Formula = staticmethod(VelMassVel)
+    fder = 1
+
+    def __init__(self, constant_factor=FACTOR_HALL_CLASSIC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        r = super().__call__(data_K)
+        return EnergyResult(r.Energies, hall_curl(r.data))
+
+
+class Hall_classic_FermiSea(StaticCalculator):  # calculators/static.py:427-446: d_g v_a d_r v_b f
+    Formula = staticmethod(MassMass)
+    fder = 0
+
+    def __init__(self, constant_factor=FACTOR_HALL_CLASSIC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        r = super().__call__(data_K)
+        # the second mass tensor's derivative index goes first (static.py:438)
+        return EnergyResult(r.Energies, hall_curl(r.data.transpose(0, 4, 1, 2, 3)))
 
 
 class Morb(StaticCalculator):  # calculators/static.py:231-247

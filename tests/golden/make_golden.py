@@ -45,6 +45,10 @@ Fixtures written (all small, complex128/float64):
 * ``static_ref.npz`` -- the static SHC (SpinOmega; simple, simple without external terms, qiao,
   ryoo), NLDrude_Fermider2 and NLAHC_FermiSea of the reference's ``run`` on the random system.
   ``python make_golden.py <reference root> static`` writes only this file.
+* ``products_ref.npz`` -- the product-formula calculators of calculators/static.py
+  (BerryDipole_FermiSurf with and without external terms, NLAHC_FermiSurf, NLDrude_FermiSurf,
+  Hall_classic_FermiSurf, Hall_classic_FermiSea) of the reference's ``run`` on the random system.
+  ``python make_golden.py <reference root> products`` writes only this file.
 """
 import os
 import sys
@@ -175,6 +179,22 @@ def static_fixtures(wb, rs):
     np.savez_compressed(os.path.join(HERE, 'static_ref.npz'), **out)
 
 
+def products_fixtures(wb, rs):
+    """---- 9. product formulas (formula/formula.py FormulaProduct: in-group matrix products) of the
+    reference's run on the random system (NKdiv 2 x NKFFT 3, 21 Fermi levels)."""
+    from wannierberri import calculators as calc
+    st = calc.static
+    EF = np.linspace(-2, 2, 21)
+    out = {'EF': EF}
+    cs = {'bcd_fsurf': st.BerryDipole_FermiSurf(Efermi=EF),
+          'bcd_fsurf_int': st.BerryDipole_FermiSurf(Efermi=EF, kwargs_formula={'external_terms': False}),
+          'nlahc_fsurf': st.NLAHC_FermiSurf(Efermi=EF), 'nldrude_fsurf': st.NLDrude_FermiSurf(Efermi=EF),
+          'hall_fsurf': st.Hall_classic_FermiSurf(Efermi=EF), 'hall_fsea': st.Hall_classic_FermiSea(Efermi=EF)}
+    for k, v in run_ref(wb, rs, 2, 3, cs).items():
+        out['random_' + k] = v
+    np.savez_compressed(os.path.join(HERE, 'products_ref.npz'), **out)
+
+
 def main(ref_root):
     wb = setup_reference(ref_root)
     from wannierberri.system.system_R import System_R
@@ -254,6 +274,7 @@ def main(ref_root):
     refine_fixtures(wb, rs)
     dynamic_fixtures(wb, rs)
     static_fixtures(wb, rs)
+    products_fixtures(wb, rs)
     print("wrote fixtures to", HERE)
 
 
@@ -330,7 +351,7 @@ def refine_fixtures(wb, rs):
 if __name__ == '__main__':
     root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
     section = sys.argv[2] if len(sys.argv) > 2 else None
-    if section in ('random', 'tetra', 'refine', 'dynamic', 'static'):  # one section only
+    if section in ('random', 'tetra', 'refine', 'dynamic', 'static', 'products'):  # one section only
         wb = setup_reference(root)
         from wannierberri.system.system_R import System_R
         rs = System_R.from_npz(path=os.path.join(root, 'tests', 'data', 'random'), legacy=True)
@@ -338,6 +359,6 @@ if __name__ == '__main__':
             random_fixtures(root)
         else:
             {'tetra': tetra_fixtures, 'refine': refine_fixtures, 'dynamic': dynamic_fixtures,
-             'static': static_fixtures}[section](wb, rs)
+             'static': static_fixtures, 'products': products_fixtures}[section](wb, rs)
     else:
         main(root)

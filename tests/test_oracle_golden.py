@@ -320,3 +320,32 @@ def test_static_extra_golden(static_run, static_ref, quant):
     got = static_run[quant].data
     assert got.shape == ref.shape
     assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))
+
+
+def product_calculators(EF):
+    """The calculators of products_ref.npz (tests/golden/make_golden.py, section 9)."""
+    return {'bcd_fsurf': O.BerryDipole_FermiSurf(Efermi=EF),
+            'bcd_fsurf_int': O.BerryDipole_FermiSurf(Efermi=EF, kwargs_formula={'external_terms': False}),
+            'nlahc_fsurf': O.NLAHC_FermiSurf(Efermi=EF), 'nldrude_fsurf': O.NLDrude_FermiSurf(Efermi=EF),
+            'hall_fsurf': O.Hall_classic_FermiSurf(Efermi=EF), 'hall_fsea': O.Hall_classic_FermiSea(Efermi=EF)}
+
+
+@pytest.fixture(scope="module")
+def products_ref(golden_dir):
+    return np.load(os.path.join(golden_dir, 'products_ref.npz'))
+
+
+@pytest.fixture(scope="module")
+def products_run(random_sys, products_ref):
+    return O.run(random_sys, (2, 2, 2), (3, 3, 3), product_calculators(products_ref['EF']))
+
+
+@pytest.mark.parametrize("quant", ['bcd_fsurf', 'bcd_fsurf_int', 'nlahc_fsurf', 'nldrude_fsurf', 'hall_fsurf',
+                                   'hall_fsea'])
+def test_product_formulas_golden(products_run, products_ref, quant):
+    """In-group matrix products (VelOmega, MassVel, VelMassVel, MassMass) and the classical Hall
+    antisymmetrisations: the reference's run() on the random system."""
+    ref = products_ref['random_' + quant]
+    got = products_run[quant].data
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 1e-8 * np.max(np.abs(ref))
