@@ -537,6 +537,28 @@ def VelMassVel(data_K, **_):  # formula/covariant.py:842-846
     return Product([data_K.covariant('Ham', commader=1), InvMass(data_K), data_K.covariant('Ham', commader=1)])
 
 
+class Der3E(Formula_ln):  # formula/covariant.py:126-151: third derivative of E within the group
+    """dW^{ab:c} + dV^{ac} D^b - dD^{bc} V^a terms of the covariant third derivative; W = Xbar('Ham', 2)
+    with its generalised derivative from Xbar('Ham', 3) (formula/elementary.py:37-43)."""
+
+    def __init__(self, data_K, **_):
+        self.V = data_K.covariant('Ham', commader=1)
+        self.D = data_K.Dcov
+        self.dV = InvMass(data_K)
+        self.dD = DerDcov(data_K)
+        self.dW = Matrix_GenDer_ln(data_K.covariant('Ham', commader=2), data_K.covariant('Ham', commader=3),
+                                   data_K.Dcov)
+        self.ndim = 3
+
+    def nn(self, ik, inn, out):
+        s = self.dW.nn(ik, inn, out).astype(complex)
+        s = s + np.einsum("mlac,lnb->mnabc", self.dV.nl(ik, inn, out), self.D.ln(ik, inn, out))
+        s = s + np.einsum("mla,lnbc->mnabc", self.V.nl(ik, inn, out), self.dD.ln(ik, inn, out))
+        s = s - np.einsum("mlbc,lna->mnabc", self.dD.nl(ik, inn, out), self.V.ln(ik, inn, out))
+        s = s - np.einsum("mlb,lnac->mnabc", self.D.nl(ik, inn, out), self.dV.ln(ik, inn, out))
+        return s
+
+
 class SpinOmega(Formula_ln):  # formula/covariant.py:759-788, additive; nn block only
     def __init__(self, data_K, spin_current_type="ryoo", external_terms=True, **_):
         self.external_terms = external_terms and not data_K.force_internal_terms_only
@@ -975,6 +997,14 @@ class NLAHC_FermiSurf(BerryDipole_FermiSurf):  # calculators/static.py:461-469
 class NLDrude_FermiSurf(StaticCalculator):  # calculators/static.py:532-542: int d_b v_a v_c f'
     Formula = staticmethod(MassVel)
     fder = 1
+
+    def __init__(self, constant_factor=FACTOR_NLDRUDE, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class NLDrude_FermiSea(StaticCalculator):  # calculators/static.py:519-529: -int d_bc v_a f
+    Formula = Der3E
+    fder = 0
 
     def __init__(self, constant_factor=FACTOR_NLDRUDE, **kw):
         super().__init__(constant_factor=constant_factor, **kw)

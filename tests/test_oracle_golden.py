@@ -327,7 +327,8 @@ def product_calculators(EF):
     return {'bcd_fsurf': O.BerryDipole_FermiSurf(Efermi=EF),
             'bcd_fsurf_int': O.BerryDipole_FermiSurf(Efermi=EF, kwargs_formula={'external_terms': False}),
             'nlahc_fsurf': O.NLAHC_FermiSurf(Efermi=EF), 'nldrude_fsurf': O.NLDrude_FermiSurf(Efermi=EF),
-            'hall_fsurf': O.Hall_classic_FermiSurf(Efermi=EF), 'hall_fsea': O.Hall_classic_FermiSea(Efermi=EF)}
+            'hall_fsurf': O.Hall_classic_FermiSurf(Efermi=EF), 'hall_fsea': O.Hall_classic_FermiSea(Efermi=EF),
+            'nldrude_fsea': O.NLDrude_FermiSea(Efermi=EF)}
 
 
 @pytest.fixture(scope="module")
@@ -341,10 +342,11 @@ def products_run(random_sys, products_ref):
 
 
 @pytest.mark.parametrize("quant", ['bcd_fsurf', 'bcd_fsurf_int', 'nlahc_fsurf', 'nldrude_fsurf', 'hall_fsurf',
-                                   'hall_fsea'])
+                                   'hall_fsea', 'nldrude_fsea'])
 def test_product_formulas_golden(products_run, products_ref, quant):
-    """In-group matrix products (VelOmega, MassVel, VelMassVel, MassMass) and the classical Hall
-    antisymmetrisations: the reference's run() on the random system."""
+    """In-group matrix products (VelOmega, MassVel, VelMassVel, MassMass), the classical Hall
+    antisymmetrisations and the third derivative of E (Der3E): the reference's run() on the
+    random system."""
     ref = products_ref['random_' + quant]
     got = products_run[quant].data
     assert got.shape == ref.shape
