@@ -28,7 +28,7 @@ ALPHA = np.array([1, 2, 0])
 BETA = np.array([2, 0, 1])
 
 # wannierberri/factors.py:1-26 (scipy.constants, CODATA values as shipped by scipy)
-from scipy.constants import elementary_charge, hbar, physical_constants, angstrom
+from scipy.constants import elementary_charge, hbar, physical_constants, angstrom, electron_mass
 
 BOHR = physical_constants['Bohr radius'][0] / angstrom
 EV_AU = physical_constants['electron volt-hartree relationship'][0]
@@ -41,6 +41,11 @@ FACTOR_NLAHC = elementary_charge ** 3 / hbar ** 2 * TAU_UNIT                    
 FACTOR_NLDRUDE = -(elementary_charge ** 3 / hbar ** 2 * TAU_UNIT ** 2 * elementary_charge / hbar)  # factors.py:31-32
 FACTOR_HALL_CLASSIC = -(elementary_charge ** 3 / hbar ** 2 * angstrom * TAU_UNIT ** 2 *
                         elementary_charge ** 2 / hbar ** 2)  # factors.py:29-30
+BOHR_MAGNETON = elementary_charge * hbar / (2 * electron_mass)                       # factors.py:6
+FAC_ORB_Z = elementary_charge / 2 / hbar * angstrom ** 2                              # factors.py:16
+FAC_SPIN_Z = hbar / (2 * electron_mass)                                               # factors.py:17
+FACTOR_GME_ORB = -(elementary_charge * angstrom ** 2) * elementary_charge / (2 * hbar) / angstrom ** 2  # factors.py:12,20
+FACTOR_GME_SPIN = -BOHR_MAGNETON / angstrom ** 2                                      # factors.py:22
 
 
 # ---------------------------------------------------------------------------
@@ -537,6 +542,30 @@ def VelMassVel(data_K, **_):  # formula/covariant.py:842-846
     return Product([data_K.covariant('Ham', commader=1), InvMass(data_K), data_K.covariant('Ham', commader=1)])
 
 
+def VelSpin(data_K, **_):  # formula/covariant.py VelSpin: FormulaProduct([V, Spin])
+    return Product([data_K.covariant('Ham', commader=1), data_K.covariant('SS')])
+
+
+def OmegaS(data_K, **kw):  # formula/covariant.py:849-852
+    return Product([Omega(data_K, **kw), data_K.covariant('SS')])
+
+
+def OmegaOmega_f(data_K, **kw):  # formula/covariant.py:855-858
+    return Product([Omega(data_K, **kw), Omega(data_K, **kw)])
+
+
+def VelHplus(data_K, **kw):  # formula/covariant.py:804-808: the product is additive although Morb_Hpm is not
+    return Product([data_K.covariant('Ham', commader=1), Morb_Hpm(data_K, sign=+1, **kw)])
+
+
+def OmegaHplus(data_K, **kw):  # formula/covariant.py:861-865
+    return Product([Omega(data_K, **kw), Morb_Hpm(data_K, sign=+1, **kw)])
+
+
+def DerSpin(data_K, **_):  # formula/covariant.py:338-342: generalised derivative of S
+    return data_K.covariant('SS', gender=1)
+
+
 class Der3E(Formula_ln):  # formula/covariant.py:126-151: third derivative of E within the group
     """dW^{ab:c} + dV^{ac} D^b - dD^{bc} V^a terms of the covariant third derivative; W = Xbar('Ham', 2)
     with its generalised derivative from Xbar('Ham', 3) (formula/elementary.py:37-43)."""
@@ -1008,6 +1037,67 @@ class NLDrude_FermiSea(StaticCalculator):  # calculators/static.py:519-529: -int
 
     def __init__(self, constant_factor=FACTOR_NLDRUDE, **kw):
         super().__init__(constant_factor=constant_factor, **kw)
+
+
+class GME_spin_FermiSurf(StaticCalculator):  # calculators/static.py:340-350: tau int v_a s_m f'
+    Formula = staticmethod(VelSpin)
+    fder = 1
+
+    def __init__(self, constant_factor=FACTOR_GME_SPIN, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class GME_spin_FermiSea(StaticCalculator):  # calculators/static.py:322-337: -int d_a s_m f
+    Formula = staticmethod(DerSpin)
+    fder = 0
+
+    def __init__(self, constant_factor=FACTOR_GME_SPIN, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        r = super().__call__(data_K)
+        return EnergyResult(r.Energies, r.data.swapaxes(1, 2))
+
+
+class GME_orb_FermiSurf(StaticCalculator):  # calculators/static.py:266-281: int v_a (H + G - 2 E_F Omega)_m f'
+    Formula = staticmethod(VelHplus)
+    fder = 1
+
+    def __init__(self, constant_factor=FACTOR_GME_ORB, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+        self.dipole = BerryDipole_FermiSurf(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        h = super().__call__(data_K)
+        om = self.dipole(data_K)
+        return EnergyResult(h.Energies, h.data - 2 * om.data * self.Efermi[:, None, None])
+
+
+class OmegaOmega(StaticCalculator):  # calculators/static.py:618-623
+    Formula = staticmethod(OmegaOmega_f)
+    fder = 1
+
+
+class AHC_Zeeman_spin(StaticCalculator):  # calculators/static.py:605-615: int Omega_d s_m f'
+    Formula = staticmethod(OmegaS)
+    fder = 1
+
+    def __init__(self, constant_factor=FAC_SPIN_Z * FACTOR_AHC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+
+
+class AHC_Zeeman_orb(StaticCalculator):  # calculators/static.py:626-644: int Omega_d (H + G - 2 E_F Omega)_m f'
+    Formula = staticmethod(OmegaHplus)
+    fder = 1
+
+    def __init__(self, constant_factor=FAC_ORB_Z * FACTOR_AHC, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+        self.omega2 = OmegaOmega(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        h = super().__call__(data_K)
+        om = self.omega2(data_K)
+        return EnergyResult(h.Energies, h.data - 2 * om.data * self.Efermi[:, None, None])
 
 
 def hall_curl(T):

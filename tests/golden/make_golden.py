@@ -47,8 +47,10 @@ Fixtures written (all small, complex128/float64):
   ``python make_golden.py <reference root> static`` writes only this file.
 * ``products_ref.npz`` -- the product-formula calculators of calculators/static.py
   (BerryDipole_FermiSurf with and without external terms, NLAHC_FermiSurf, NLDrude_FermiSurf,
-  Hall_classic_FermiSurf, Hall_classic_FermiSea) and NLDrude_FermiSea (the covariant third
-  derivative of the energy) of the reference's ``run`` on the random system.
+  Hall_classic_FermiSurf, Hall_classic_FermiSea), NLDrude_FermiSea (the covariant third
+  derivative of the energy), the gyrotropic GME_spin_FermiSurf / FermiSea and GME_orb_FermiSurf,
+  OmegaOmega and the Zeeman AHC corrections AHC_Zeeman_spin / orb of the reference's ``run`` on
+  the random system.
   ``python make_golden.py <reference root> products`` writes only this file.
 """
 import os
@@ -191,7 +193,10 @@ def products_fixtures(wb, rs):
           'bcd_fsurf_int': st.BerryDipole_FermiSurf(Efermi=EF, kwargs_formula={'external_terms': False}),
           'nlahc_fsurf': st.NLAHC_FermiSurf(Efermi=EF), 'nldrude_fsurf': st.NLDrude_FermiSurf(Efermi=EF),
           'hall_fsurf': st.Hall_classic_FermiSurf(Efermi=EF), 'hall_fsea': st.Hall_classic_FermiSea(Efermi=EF),
-          'nldrude_fsea': st.NLDrude_FermiSea(Efermi=EF)}
+          'nldrude_fsea': st.NLDrude_FermiSea(Efermi=EF), 'gme_spin_fsurf': st.GME_spin_FermiSurf(Efermi=EF),
+          'gme_spin_fsea': st.GME_spin_FermiSea(Efermi=EF), 'gme_orb_fsurf': st.GME_orb_FermiSurf(Efermi=EF),
+          'omegaomega': st.OmegaOmega(Efermi=EF), 'ahc_z_spin': st.AHC_Zeeman_spin(Efermi=EF),
+          'ahc_z_orb': st.AHC_Zeeman_orb(Efermi=EF)}
     for k, v in run_ref(wb, rs, 2, 3, cs).items():
         out['random_' + k] = v
     np.savez_compressed(os.path.join(HERE, 'products_ref.npz'), **out)
