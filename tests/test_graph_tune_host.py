@@ -219,3 +219,16 @@ def test_graph_skipped_under_stage_timer(monkeypatch):
     finally:
         engine.set_timer(None)
     assert [c[3] for c in rec.calls] == [False] * 3 and rec.replays == 0
+
+
+def test_graph_capture_only_when_replayed(monkeypatch):
+    rec = _Recorder(monkeypatch)
+    dev = _FakeDev()
+    NKFFT = (2, 2, 2)
+    dKs = np.zeros((2, 3))
+    for more in (True, False, False):  # the second batch would be captured, but nothing follows it
+        engine.band_data_graphed(dev, dKs, NKFFT, {'V'}, 'fp64', more=more)
+    assert [c[3] for c in rec.calls] == [False, False, False] and not dev.workspace().graphs
+    engine.band_data_graphed(dev, dKs, NKFFT, {'V'}, 'fp64', more=True)  # now captured
+    engine.band_data_graphed(dev, dKs, NKFFT, {'V'}, 'fp64', more=False)  # an existing graph replays
+    assert [c[3] for c in rec.calls[3:]] == [False, True] and rec.replays == 1

@@ -756,7 +756,8 @@ def _fill_phase_inputs(dev, tabs, dKs, NKFFT, phases, block_start):
             d.copy_(torch.from_numpy(a))
 
 
-def band_data_graphed(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_start=0, ws=None):
+def band_data_graphed(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_start=0, ws=None,
+                      more=True):
     """band_data (stages 1-3) replayed from a CUDA graph of its launch sequence.
 
     One graph per (FFT grid, blocks per batch, quantities, precision) and workspace.  The first
@@ -766,9 +767,10 @@ def band_data_graphed(dev, dKs, NKFFT, quantities, precision='fp64', phases=None
     replay the graph, so a batch costs a few host calls instead of one Python dispatch per kernel.
     The graph writes the same workspace buffers as band_data, so results are bit-identical to it.
     A graph is dropped when its workspace reallocates a buffer (Workspace.generation) or serves
-    another system.  Stage timers (set_timer) need plain launches: with a timer set this is
-    band_data itself.  The returned BandData is valid until the next batch on the same workspace,
-    as for band_data."""
+    another system.  ``more``: whether the caller will issue further batches of this shape on this
+    workspace; a capture (which synchronises the device) is made only then.  Stage timers
+    (set_timer) need plain launches: with a timer set this is band_data itself.  The returned
+    BandData is valid until the next batch on the same workspace, as for band_data."""
     if _TIMER is not None:
         return band_data(dev, dKs, NKFFT, quantities, precision, phases=phases, block_start=block_start, ws=ws)
     arena = ws if ws is not None else dev.workspace()
@@ -786,7 +788,7 @@ def band_data_graphed(dev, dKs, NKFFT, quantities, precision='fp64', phases=None
         ent.replays += 1
         return copy.copy(ent.bd)
     seen = arena.__dict__.setdefault('_graph_seen', set())
-    if (key, id(dev)) not in seen:
+    if (key, id(dev)) not in seen or not more:
         seen.add((key, id(dev)))
         return band_data(dev, dKs, NKFFT, quantities, precision, phases=phases, block_start=block_start, ws=ws)
     # capture: fixed inputs, one plain run on them (this batch's result; every buffer at its final

@@ -175,10 +175,16 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
         tetra = engine.TetraCorners(dev, grid, block_ids, precision)
     precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
-    stages = engine.band_data_graphed if cuda_graph else engine.band_data
     flags = []
     for i0 in range(0, len(shifts), nb):
-        bd = stages(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases, block_start=i0)
+        if cuda_graph:  # a graph is captured only when a later batch of this size will replay it
+            n_this = min(nb, len(shifts) - i0)
+            more = len(shifts) - (i0 + n_this) >= n_this
+            bd = engine.band_data_graphed(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
+                                          block_start=i0, more=more)
+        else:
+            bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
+                                  block_start=i0)
         if tetra is not None:
             tetra.attach(bd, block_ids[i0:i0 + nb])
         for c in calculators.values():

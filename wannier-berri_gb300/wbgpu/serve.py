@@ -304,7 +304,10 @@ class Server:
         shifts = req.grid.block_shifts()
         with torch.cuda.stream(req.stream):
             contiguous = np.all(np.diff(idx) == 1)
-            stages = engine.band_data_graphed if self.cuda_graph else engine.band_data
+            stages = engine.band_data
+            if self.cuda_graph:  # capture only when a later batch of this request has the same size
+                more = any(len(b) == len(idx) for b in req.batches[req.next_batch:])
+                stages = lambda *a, **k: engine.band_data_graphed(*a, more=more, **k)
             if req.refine is not None:
                 bd = self._issue_adaptive(req, idx, system, dev)
             elif contiguous:
