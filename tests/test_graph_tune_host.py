@@ -232,3 +232,15 @@ def test_graph_capture_only_when_replayed(monkeypatch):
     engine.band_data_graphed(dev, dKs, NKFFT, {'V'}, 'fp64', more=True)  # now captured
     engine.band_data_graphed(dev, dKs, NKFFT, {'V'}, 'fp64', more=False)  # an existing graph replays
     assert [c[3] for c in rec.calls[3:]] == [False, True] and rec.replays == 1
+
+
+def test_capture_hints_of_run_and_server():
+    from wbgpu.run import more_batches_of_size
+    from wbgpu.serve import later_batch_of_size
+    # 8 blocks in batches of 3: 3, 3, 2 -> only the first full batch is followed by another of its size
+    assert [more_batches_of_size(8, 3, i0) for i0 in (0, 3, 6)] == [True, False, False]
+    assert [more_batches_of_size(8, 2, i0) for i0 in (0, 2, 4, 6)] == [True, True, True, False]
+    assert more_batches_of_size(1, 4, 0) is False
+    batches = [np.arange(0, 2), np.arange(2, 4), np.arange(4, 5)]
+    assert later_batch_of_size(batches, 1, 2) and not later_batch_of_size(batches, 2, 2)
+    assert later_batch_of_size(batches, 2, 1) and not later_batch_of_size(batches, 3, 1)

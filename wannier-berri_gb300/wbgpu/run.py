@@ -25,6 +25,13 @@ def choose_batch(nw, nk, nblocks, quantities, precision, max_kpoints=1 << 17, bu
     return int(nb)
 
 
+def more_batches_of_size(nblocks, nb, i0):
+    """Whether the batch of `nblocks` blocks split into batches of `nb` that starts at block `i0`
+    is followed by another batch of the same size (the full batches all are, except the last)."""
+    n_this = min(nb, nblocks - i0)
+    return nblocks - (i0 + n_this) >= n_this
+
+
 def block_results(dev, system, shifts, NKFFT, calculators, precision, cells=None):
     """One result per block -- what the reference's calculators return for one Data_K (normalised
     by the block's k-points, K-point factor 1): [{key: EnergyResult}] for the blocks at `shifts`.
@@ -178,10 +185,8 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
     flags = []
     for i0 in range(0, len(shifts), nb):
         if cuda_graph:  # a graph is captured only when a later batch of this size will replay it
-            n_this = min(nb, len(shifts) - i0)
-            more = len(shifts) - (i0 + n_this) >= n_this
             bd = engine.band_data_graphed(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
-                                          block_start=i0, more=more)
+                                          block_start=i0, more=more_batches_of_size(len(shifts), nb, i0))
         else:
             bd = engine.band_data(dev, shifts[i0:i0 + nb], grid.FFT, quantities, precision, phases=phases,
                                   block_start=i0)

@@ -50,6 +50,11 @@ def admit(pending_bytes, used_bytes, budget_bytes, free_slots):
     return n
 
 
+def later_batch_of_size(batches, start, size):
+    """Whether a batch of `size` blocks is among batches[start:] (block-index arrays)."""
+    return any(len(b) == size for b in batches[start:])
+
+
 def request_bytes(nw, nk, nblocks_batch, quantities, precision):
     """Device memory of one request's batch buffers (fields, H, U, Xbar, workspaces)."""
     cs = 16 if precision == 'fp64' else 8
@@ -306,7 +311,7 @@ class Server:
             contiguous = np.all(np.diff(idx) == 1)
             stages = engine.band_data
             if self.cuda_graph:  # capture only when a later batch of this request has the same size
-                more = any(len(b) == len(idx) for b in req.batches[req.next_batch:])
+                more = later_batch_of_size(req.batches, req.next_batch, len(idx))
                 stages = lambda *a, **k: engine.band_data_graphed(*a, more=more, **k)
             if req.refine is not None:
                 bd = self._issue_adaptive(req, idx, system, dev)
