@@ -164,3 +164,21 @@ def test_spin_field_plan_and_hermitian_flags():
     assert herm == [True] * 9 + [False] * 9
     herm = engine.hermitian_fields({'S'}, False, herm_bases=('Ham', 'AA'))
     assert herm == [False] * 3
+
+
+def test_reference_static_calculator_names():
+    """Every static calculator of the reference (calculators/static.py, test variants aside) is
+    reachable by name; those without a GPU kernel raise NotImplementedError when constructed."""
+    from wbgpu import calculators as C
+    names = ['DOS', 'CumDOS', 'Spin', 'Morb', 'GME_orb_FermiSurf', 'GME_orb_FermiSea', 'GME_spin_FermiSea',
+             'GME_spin_FermiSurf', 'AHC', 'Ohmic_FermiSea', 'Ohmic_FermiSurf', 'Hall_classic_FermiSurf',
+             'Hall_classic_FermiSea', 'BerryDipole_FermiSurf', 'NLAHC_FermiSurf', 'BerryDipole_FermiSea',
+             'NLAHC_FermiSea', 'NLDrude_FermiSea', 'NLDrude_FermiSurf', 'NLDrude_Fermider2', 'eMChA_FermiSurf',
+             'NLDrude_Zeeman_spin', 'NLDrude_Zeeman_orb_Omega', 'NLDrude_Zeeman_orb', 'AHC_Zeeman_spin',
+             'OmegaOmega', 'AHC_Zeeman_orb', 'SHC', 'QuantumMetric_FermiSea', 'QuantumMetric_Vel_DQ']
+    for n in names:
+        assert hasattr(C.static, n), n
+    for n in C._NO_KERNEL:
+        with pytest.raises(NotImplementedError):
+            getattr(C.static, n)(Efermi=np.linspace(-1, 1, 5))
+    C.static.AHC(Efermi=np.linspace(-1, 1, 5))  # a calculator with a kernel constructs on the CPU

@@ -531,10 +531,32 @@ class InjectionCurrent(DynamicCalculator):
 
 
 # the reference's calculator modules (calculators/static.py, calculators/dynamic.py): both define an SHC
-static = types.SimpleNamespace(
+def _no_kernel(name, ref):
+    """A calculator of the reference (calculators/static.py) without a GPU kernel here: same name,
+    constructing it raises NotImplementedError (there is no CPU fallback)."""
+    def __init__(self, *args, **kwargs):
+        raise NotImplementedError(f"{name} ({ref}) has no GPU kernel in this backend; there is no CPU fallback")
+    return type(name, (StaticCalculator,), {'__init__': __init__, '__doc__': f"Not available: {ref}."})
+
+
+_NO_KERNEL = {
+    'BerryDipole_FermiSurf': 'calculators/static.py:449-458', 'NLAHC_FermiSurf': 'calculators/static.py:461-469',
+    'NLDrude_FermiSea': 'calculators/static.py:519-529', 'NLDrude_FermiSurf': 'calculators/static.py:532-542',
+    'Hall_classic_FermiSurf': 'calculators/static.py:407-424', 'Hall_classic_FermiSea': 'calculators/static.py:427-446',
+    'GME_orb_FermiSurf': 'calculators/static.py:266-281', 'GME_orb_FermiSea': 'calculators/static.py:284-300',
+    'GME_spin_FermiSea': 'calculators/static.py:322-337', 'GME_spin_FermiSurf': 'calculators/static.py:340-350',
+    'eMChA_FermiSurf': 'calculators/static.py:560-565', 'NLDrude_Zeeman_spin': 'calculators/static.py:568-573',
+    'NLDrude_Zeeman_orb_Omega': 'calculators/static.py:576-581', 'NLDrude_Zeeman_orb': 'calculators/static.py:584-600',
+    'AHC_Zeeman_spin': 'calculators/static.py:605-615', 'OmegaOmega': 'calculators/static.py:618-623',
+    'AHC_Zeeman_orb': 'calculators/static.py:626-644', 'QuantumMetric_FermiSea': 'calculators/static.py:663-670',
+    'QuantumMetric_Vel_DQ': 'calculators/static.py:673-680'}
+_no_kernel_classes = {n: _no_kernel(n, r) for n, r in _NO_KERNEL.items()}
+globals().update(_no_kernel_classes)
+
+static = types.SimpleNamespace(**_no_kernel_classes, **dict(
     StaticCalculator=StaticCalculator, AHC=AHC, Morb=Morb, BerryDipole_FermiSea=BerryDipole_FermiSea,
     NLAHC_FermiSea=NLAHC_FermiSea, DOS=DOS, CumDOS=CumDOS, Ohmic_FermiSea=Ohmic_FermiSea,
-    Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static)
+    Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static))
 dynamic = types.SimpleNamespace(
     DynamicCalculator=DynamicCalculator, OpticalConductivity=OpticalConductivity, JDOS=JDOS, SHC=SHC,
     ShiftCurrent=ShiftCurrent, InjectionCurrent=InjectionCurrent)
