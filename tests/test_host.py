@@ -182,3 +182,14 @@ def test_reference_static_calculator_names():
         with pytest.raises(NotImplementedError):
             getattr(C.static, n)(Efermi=np.linspace(-1, 1, 5))
     C.static.AHC(Efermi=np.linspace(-1, 1, 5))  # a calculator with a kernel constructs on the CPU
+
+
+def test_tabulate_and_sdct_names_point_elsewhere():
+    from wbgpu import calculators as C
+    for ns, names in ((C.tabulate, ['TabulatorAll', 'Energy', 'Velocity', 'BerryCurvature', 'OrbitalMoment']),
+                      (C.sdct, ['SDCT_asym', 'SDCT_sym', 'SDCT_sym_sea_I', 'SDCT_asym_surf_II'])):
+        for n in names:
+            with pytest.raises(NotImplementedError):
+                getattr(ns, n)()
+    with pytest.raises(NotImplementedError, match="wbgpu.tabulate.tabulate"):
+        C.TabulatorAll({})

@@ -557,6 +557,30 @@ static = types.SimpleNamespace(**_no_kernel_classes, **dict(
     StaticCalculator=StaticCalculator, AHC=AHC, Morb=Morb, BerryDipole_FermiSea=BerryDipole_FermiSea,
     NLAHC_FermiSea=NLAHC_FermiSea, DOS=DOS, CumDOS=CumDOS, Ohmic_FermiSea=Ohmic_FermiSea,
     Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static))
+def _elsewhere(name, ref, hint):
+    """A calculator class of the reference served differently here (or not at all): constructing it
+    raises NotImplementedError that says where the equivalent lives."""
+    def __init__(self, *args, **kwargs):
+        raise NotImplementedError(f"{name} ({ref}): {hint}")
+    return type(name, (Calculator,), {'__init__': __init__, '__doc__': f"Not available as a calculator: {ref}."})
+
+
+_TAB_HINT = ("tabulation runs through wbgpu.tabulate.tabulate(system, grid, quantities) (energy, band_gradients, "
+             "berry_curvature and its terms) and wbgpu.tabulate.evaluate_k, not as a run() calculator")
+tabulate = types.SimpleNamespace(**{n: _elsewhere(n, f'calculators/tabulate.py:{r}', _TAB_HINT) for n, r in {
+    'Tabulator': '12-53', 'TabulatorAll': '56-119', 'Energy': '122-125', 'Velocity': '128-131', 'InvMass': '134-138',
+    'Der3E': '141-145', 'BerryCurvature': '148-152', 'DerBerryCurvature': '155-159', 'Der2BerryCurvature': '162-166',
+    'Spin': '169-173', 'DerSpin': '176-180', 'Der2Spin': '183-186', 'OrbitalMoment': '189-193',
+    'DerOrbitalMoment': '196-200', 'Der2OrbitalMoment': '210-215', 'SpinBerry': '218-221'}.items()})
+sdct = types.SimpleNamespace(**{n: _elsewhere(n, f'calculators/sdct.py:{r}', "the spatially dispersive "
+                                              "conductivity has no GPU kernel in this backend; no CPU fallback exists")
+                                for n, r in {'SDCT_asym': '37-40', 'SDCT_sym': '43-46', 'SDCT_sym_sea_I': '77-84',
+                                             'SDCT_asym_sea_I': '87-94', 'SDCT_sym_sea_II': '97-104',
+                                             'SDCT_asym_sea_II': '107-114', 'SDCT_sym_surf_I': '123-130',
+                                             'SDCT_asym_surf_I': '133-140', 'SDCT_sym_surf_II': '143-150',
+                                             'SDCT_asym_surf_II': '153-160'}.items()})
+TabulatorAll = tabulate.TabulatorAll
+
 dynamic = types.SimpleNamespace(
     DynamicCalculator=DynamicCalculator, OpticalConductivity=OpticalConductivity, JDOS=JDOS, SHC=SHC,
     ShiftCurrent=ShiftCurrent, InjectionCurrent=InjectionCurrent)
