@@ -191,5 +191,5 @@ def test_tabulate_and_sdct_names_point_elsewhere():
         for n in names:
             with pytest.raises(NotImplementedError):
                 getattr(ns, n)()
-    with pytest.raises(NotImplementedError, match="wbgpu.tabulate.tabulate"):
+    with pytest.raises(NotImplementedError, match=r"wbgpu\.tabulate\(system, grid"):
         C.TabulatorAll({})

@@ -565,8 +565,8 @@ def _elsewhere(name, ref, hint):
     return type(name, (Calculator,), {'__init__': __init__, '__doc__': f"Not available as a calculator: {ref}."})
 
 
-_TAB_HINT = ("tabulation runs through wbgpu.tabulate.tabulate(system, grid, quantities) (energy, band_gradients, "
-             "berry_curvature and its terms) and wbgpu.tabulate.evaluate_k, not as a run() calculator")
+_TAB_HINT = ("tabulation runs through wbgpu.tabulate(system, grid, quantities) (energy, band_gradients, "
+             "berry_curvature and its terms) and wbgpu.evaluate_k, not as a run() calculator")
 tabulate = types.SimpleNamespace(**{n: _elsewhere(n, f'calculators/tabulate.py:{r}', _TAB_HINT) for n, r in {
     'Tabulator': '12-53', 'TabulatorAll': '56-119', 'Energy': '122-125', 'Velocity': '128-131', 'InvMass': '134-138',
     'Der3E': '141-145', 'BerryCurvature': '148-152', 'DerBerryCurvature': '155-159', 'Der2BerryCurvature': '162-166',
