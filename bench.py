@@ -208,6 +208,15 @@ def probe_peak(torch, fp64):
     return best / 1e9  # GFLOP/s
 
 
+# DRAM bytes per k-point of the mixed path's eigensolver kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum of eigh_tridiag<df64, cdf, float>, eigh_ql<df64> and
+# eigh_vectors<df64, float>) from one ncu --set full capture of the 16^3 case
+# (python bench.py --nkfft 16 --blocks-per-step 1 --steps 1 --warmup 3 --no-cpu-baseline
+# --no-fp64-compare --no-serve --no-tetra; 4096 matrices per launch).  Each matrix's traffic is
+# its own (H read, reflectors and U written, d / e / tau), so it scales with the matrices of a launch.
+EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 1.1 + 2.1 + 0.0 + 28.8 + 63.5) * 1e6 / 4096
+
+
 def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
     """Algorithmic work per launch of the given stage: HBM bytes of the fields written and read
     back (R->k, 2 F nw^2 s per k-point), 20 nw^3 FP64-equivalent flops per matrix (eigh), 16 nw^3
@@ -243,7 +252,17 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
     achieved = work / (per_launch_ms * 1e-3) / 1e9
     return {"kernel": stage, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak if peak else None, "peak_source": src, "ms_per_launch": per_launch_ms,
-            "work_per_launch": work, "traffic": None}
+            "work_per_launch": work, **_traffic(stage, precision, k_per_call)}
+
+
+def _traffic(stage, precision, k_per_call):
+    """DRAM traffic per launch where an ncu capture of the kernels exists (scaled from the
+    captured case by the k-points of a launch), else None."""
+    if stage == 'eigh' and precision == 'mixed':
+        return {"traffic": EIGH_MIXED_DRAM_BYTES_PER_K * k_per_call,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three eigh kernels, "
+                                  "16^3 case (4096 matrices) scaled to the k-points of a launch"}
+    return {"traffic": None}
 
 
 def run_gpu(args):
