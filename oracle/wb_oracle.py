@@ -718,6 +718,59 @@ class Morb_Hpm(_TermsFormula):  # formula/covariant.py:424-449
         return r
 
 
+class DerMorb(_TermsFormula):  # formula/covariant.py:463-518 (DerMorb_H) with 522-550 (DerMorb)
+    """k-derivative of the orbital moment H + sign (E Omega): non-additive (traces over [0, n));
+    index order (moment component c, derivative d)."""
+    additive = False
+
+    def __init__(self, data_K, sign=+1, **kw):
+        super().__init__(data_K, **kw)
+        self.sign = sign
+        self.D, self.dD = data_K.Dcov, DerDcov(data_K)
+        self.V = data_K.covariant('Ham', commader=1)
+        self.E = data_K.E_K
+        if self.external_terms:
+            self.A, self.dA = data_K.covariant('AA'), data_K.covariant('AA', gender=1)
+            self.B, self.dB = data_K.covariant('BB'), data_K.covariant('BB', gender=1)
+            self.dC = data_K.covariant('CC', gender=1)
+        if sign != 0:
+            self.O, self.dO, self.Eav = Omega(data_K, **kw), DerOmega(data_K, **kw), Eavln(data_K)
+        self.ndim = 2
+
+    @staticmethod
+    def _herm(x):
+        return 0.5 * (x + x.swapaxes(0, 1).conj())
+
+    def _dH(self, ik, inn, out):
+        s = np.zeros((len(inn), len(inn), 3, 3), dtype=complex)
+        Dnl, Dln, dDln = self.D.nl(ik, inn, out), self.D.ln(ik, inn, out), self.dD.ln(ik, inn, out)
+        Eo, Ei = self.E[ik][out], self.E[ik][inn]
+        pairs = ((+1, ALPHA, BETA), (-1, BETA, ALPHA))
+        if self.internal_terms:
+            s += -2j * np.einsum("mpc,pld,lnc->mncd", Dnl[:, :, ALPHA], self.V.ll(ik, inn, out), Dln[:, :, BETA])
+            for sg, a, b in pairs:
+                s += -2j * sg * np.einsum("mlc,lncd->mncd", Dnl[:, :, a], Eo[:, None, None, None] * dDln[:, :, b])
+        if self.external_terms:
+            Ann, dAnn = self.A.nn(ik, inn, out), self.dA.nn(ik, inn, out)
+            s += self.dC.nn(ik, inn, out)
+            s += -2j * np.einsum("mpc,pld,lnc->mncd", Ann[:, :, ALPHA], self.V.nn(ik, inn, out), Ann[:, :, BETA])
+            for sg, a, b in pairs:
+                s += -2j * sg * np.einsum("mlc,lncd->mncd", Ann[:, :, a] * Ei[None, :, None], dAnn[:, :, b, :])
+                s += -2 * sg * np.einsum("mlc,lncd->mncd", Dnl[:, :, a], self.dB.ln(ik, inn, out)[:, :, b, :])
+                s += -2 * sg * np.einsum("mlc,lncd->mncd", self.B.ln(ik, inn, out)[:, :, a].transpose(1, 0, 2).conj(),
+                                         dDln[:, :, b, :])
+        return self._herm(s)
+
+    def nn(self, ik, inn, out):
+        res = self._dH(ik, inn, out)
+        if self.sign != 0:
+            On, Vn = self.O.nn(ik, inn, out), self.V.nn(ik, inn, out)
+            t = self.Eav.nn(ik, inn, out)[:, :, None, None] * self.dO.nn(ik, inn, out)
+            t = t + 0.5 * np.einsum("mlc,lnd->mncd", On, Vn) + 0.5 * np.einsum("mld,lnc->mncd", Vn, On)
+            res = res + self.sign * self._herm(t)
+        return res
+
+
 # ---------------------------------------------------------------------------
 # Results (result/energyresult.py, minimal)
 # ---------------------------------------------------------------------------
@@ -1071,6 +1124,20 @@ class GME_orb_FermiSurf(StaticCalculator):  # calculators/static.py:266-281: int
         h = super().__call__(data_K)
         om = self.dipole(data_K)
         return EnergyResult(h.Energies, h.data - 2 * om.data * self.Efermi[:, None, None])
+
+
+class GME_orb_FermiSea(StaticCalculator):  # calculators/static.py:284-300: -int d_a (H + G - 2 E_F Omega)_m f
+    Formula = DerMorb
+    fder = 0
+
+    def __init__(self, constant_factor=FACTOR_GME_ORB, **kw):
+        super().__init__(constant_factor=constant_factor, **kw)
+        self.dipole = BerryDipole_FermiSea(constant_factor=constant_factor, **kw)
+
+    def __call__(self, data_K):
+        h = super().__call__(data_K)
+        om = self.dipole(data_K)
+        return EnergyResult(h.Energies, h.data.swapaxes(1, 2) - 2 * om.data * self.Efermi[:, None, None])
 
 
 class OmegaOmega(StaticCalculator):  # calculators/static.py:618-623

@@ -48,7 +48,8 @@ Fixtures written (all small, complex128/float64):
 * ``products_ref.npz`` -- the product-formula calculators of calculators/static.py
   (BerryDipole_FermiSurf with and without external terms, NLAHC_FermiSurf, NLDrude_FermiSurf,
   Hall_classic_FermiSurf, Hall_classic_FermiSea), NLDrude_FermiSea (the covariant third
-  derivative of the energy), the gyrotropic GME_spin_FermiSurf / FermiSea and GME_orb_FermiSurf,
+  derivative of the energy), the gyrotropic GME_spin_FermiSurf / FermiSea and GME_orb_FermiSurf /
+  FermiSea (the latter with and without external terms),
   OmegaOmega and the Zeeman AHC corrections AHC_Zeeman_spin / orb of the reference's ``run`` on
   the random system.
   ``python make_golden.py <reference root> products`` writes only this file.
@@ -196,7 +197,8 @@ def products_fixtures(wb, rs):
           'nldrude_fsea': st.NLDrude_FermiSea(Efermi=EF), 'gme_spin_fsurf': st.GME_spin_FermiSurf(Efermi=EF),
           'gme_spin_fsea': st.GME_spin_FermiSea(Efermi=EF), 'gme_orb_fsurf': st.GME_orb_FermiSurf(Efermi=EF),
           'omegaomega': st.OmegaOmega(Efermi=EF), 'ahc_z_spin': st.AHC_Zeeman_spin(Efermi=EF),
-          'ahc_z_orb': st.AHC_Zeeman_orb(Efermi=EF)}
+          'ahc_z_orb': st.AHC_Zeeman_orb(Efermi=EF), 'gme_orb_fsea': st.GME_orb_FermiSea(Efermi=EF),
+          'gme_orb_fsea_int': st.GME_orb_FermiSea(Efermi=EF, kwargs_formula={'external_terms': False})}
     for k, v in run_ref(wb, rs, 2, 3, cs).items():
         out['random_' + k] = v
     np.savez_compressed(os.path.join(HERE, 'products_ref.npz'), **out)

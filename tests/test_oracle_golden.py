@@ -331,7 +331,8 @@ def product_calculators(EF):
             'nldrude_fsea': O.NLDrude_FermiSea(Efermi=EF), 'gme_spin_fsurf': O.GME_spin_FermiSurf(Efermi=EF),
             'gme_spin_fsea': O.GME_spin_FermiSea(Efermi=EF), 'gme_orb_fsurf': O.GME_orb_FermiSurf(Efermi=EF),
             'omegaomega': O.OmegaOmega(Efermi=EF), 'ahc_z_spin': O.AHC_Zeeman_spin(Efermi=EF),
-            'ahc_z_orb': O.AHC_Zeeman_orb(Efermi=EF)}
+            'ahc_z_orb': O.AHC_Zeeman_orb(Efermi=EF), 'gme_orb_fsea': O.GME_orb_FermiSea(Efermi=EF),
+            'gme_orb_fsea_int': O.GME_orb_FermiSea(Efermi=EF, kwargs_formula={'external_terms': False})}
 
 
 @pytest.fixture(scope="module")
@@ -346,7 +347,7 @@ def products_run(random_sys, products_ref):
 
 @pytest.mark.parametrize("quant", ['bcd_fsurf', 'bcd_fsurf_int', 'nlahc_fsurf', 'nldrude_fsurf', 'hall_fsurf',
                                    'hall_fsea', 'nldrude_fsea', 'gme_spin_fsurf', 'gme_spin_fsea', 'gme_orb_fsurf',
-                                   'omegaomega', 'ahc_z_spin', 'ahc_z_orb'])
+                                   'omegaomega', 'ahc_z_spin', 'ahc_z_orb', 'gme_orb_fsea', 'gme_orb_fsea_int'])
 def test_product_formulas_golden(products_run, products_ref, quant):
     """In-group matrix products (VelOmega, MassVel, VelMassVel, MassMass), the classical Hall
     antisymmetrisations and the third derivative of E (Der3E): the reference's run() on the
