@@ -4,7 +4,10 @@ TEST INFRASTRUCTURE ONLY.  This module is a plain numpy restatement of the
 reference (wannier-berri) algorithm for the path R-space matrices -> k-space
 fields -> eigh -> U^dagger X U -> Berry-curvature / orbital-moment / dipole
 formulas -> Fermi-level scan, plus the Kubo optical-conductivity band sums and
-the MDRS (use_ws_distance) replica construction.  Only ``tests/``,
+the MDRS (use_ws_distance) replica construction.  It also restates calculators that
+the GPU path does not serve yet (the in-group product formulas: Fermi-surface Berry
+dipole, nonlinear Drude, classical Hall, gyrotropic and Zeeman terms), as the checker
+for their kernels.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference arm may
 import it, and only as the checker or the timed CPU baseline.  The GPU product
 never calls into this file.
