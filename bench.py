@@ -62,6 +62,9 @@ def build_system(device=None):
 # CPU side: the oracle on a process pool (spawned, so no CUDA state is inherited)
 # ---------------------------------------------------------------------------------------
 def _cpu_worker(args):
+    """One FFT block of the workload through the oracle (AHC at NEF levels): (seconds, the block's
+    AHC normalised by its k-points).  The AHC values are the checker of the GPU path on the same
+    blocks."""
     path, dK, nkfft = args
     sys.path.insert(0, REPO)
     from oracle import wb_oracle as O
@@ -70,8 +73,8 @@ def _cpu_worker(args):
     s = O.RSystem(f['real_lattice'], f['iRvec'], f['wcc'], XX)
     t = time.perf_counter()
     data = O.DataK(s, (nkfft,) * 3, dK)
-    O.AHC(Efermi=np.linspace(-2, 2, NEF))(data)
-    return time.perf_counter() - t
+    res = O.AHC(Efermi=np.linspace(-2, 2, NEF))(data)
+    return time.perf_counter() - t, np.asarray(res.data)
 
 
 def save_system_npz(s):
@@ -90,20 +93,27 @@ def spawn_pool(procs):
     return mp.get_context('spawn').Pool(procs)
 
 
-def cpu_rate(path, nblocks, procs, pool=None):
-    """k-points/s of the oracle AHC on `nblocks` 8^3 blocks of the workload spread over `procs` processes."""
-    rng = np.random.default_rng(1)
-    jobs = [(path, rng.random(3) / CPU_SAMPLE_NKFFT, CPU_SAMPLE_NKFFT) for _ in range(nblocks)]
+def cpu_blocks(nblocks, seed=1):
+    """Shifts dK of the CPU sample's blocks (random offsets of 12^3 FFT grids)."""
+    rng = np.random.default_rng(seed)
+    return [rng.random(3) / CPU_SAMPLE_NKFFT for _ in range(nblocks)]
+
+
+def cpu_rate(path, nblocks, procs, pool=None, seed=1):
+    """k-points/s of the oracle AHC on `nblocks` 12^3 blocks of the workload spread over `procs`
+    processes, the wall time, the blocks' shifts and their AHC results."""
+    dKs = cpu_blocks(nblocks, seed)
+    jobs = [(path, dK, CPU_SAMPLE_NKFFT) for dK in dKs]
     own = pool is None
     if own:
         pool = spawn_pool(procs)
     t = time.perf_counter()
-    pool.map(_cpu_worker, jobs, chunksize=1)
+    out = pool.map(_cpu_worker, jobs, chunksize=1)
     wall = time.perf_counter() - t
     if own:
         pool.close()
         pool.join()
-    return nblocks * CPU_SAMPLE_NKFFT ** 3 / wall, wall
+    return nblocks * CPU_SAMPLE_NKFFT ** 3 / wall, wall, dKs, [o[1] for o in out]
 
 
 def run_reference(args):
@@ -119,9 +129,9 @@ def run_reference(args):
         for _ in range(max(args.warmup - 1, 0)):
             cpu_rate(path, procs, procs, pool)
         t = time.perf_counter()
-        for _ in range(args.steps):
-            pool.map(_cpu_worker, [(path, np.random.default_rng(i).random(3) / CPU_SAMPLE_NKFFT, CPU_SAMPLE_NKFFT)
-                                   for i in range(procs)], chunksize=1)
+        for i in range(args.steps):
+            pool.map(_cpu_worker, [(path, dK, CPU_SAMPLE_NKFFT) for dK in cpu_blocks(procs, seed=100 + i)],
+                     chunksize=1)
         wall = time.perf_counter() - t
     finally:
         pool.close()
@@ -134,19 +144,27 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128/f64",
-            "data": "synthetic", "config": config_dict(args, 'fp64-cpu'),
+            "data": "synthetic (seeded random TB model)", "config": config_dict(args), "precision": "fp64 (CPU)",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def config_dict(args, precision):
+def config_dict(args):
+    """The workload, identical for the GPU arm and the reference arm (precision is a key of its own)."""
     return {"workload": "random TB nw=32, triclinic, R in [-4,4]^3 + MDRS(mp 9), 192^3 k in 24^3 blocks, "
                         "AHC 1001 E_F", "num_wann": NW, "NKFFT": args.nkfft, "NKdiv": NKDIV,
             "blocks_per_step": args.blocks_per_step, "k_per_step": args.blocks_per_step * args.nkfft ** 3,
-            "precision": precision, "parallelism": f"blocks sharded over {args.gpus} GPU(s)",
+            "parallelism": f"blocks sharded over {args.gpus} GPU(s)",
             "l2": "inputs larger than L2 (GB-scale fields per step)"}
+
+
+def dtype_of(precision):
+    if precision == 'fp64':
+        return "f64 / c128 throughout"
+    return ("f64 energies, gaps, scan; double-float (48-bit) H(k) and eigensolver; fp32 fields and "
+            "back-transform; 3xTF32 tensor-core rotation, fp32 accumulation")
 
 
 # ---------------------------------------------------------------------------------------
@@ -218,29 +236,36 @@ EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 1.1 + 2.1 + 0.0 + 28.8 + 63.5) * 1e6 / 409
 
 
 def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
-    """Algorithmic work per launch of the given stage: HBM bytes of the fields written and read
-    back (R->k, 2 F nw^2 s per k-point), 20 nw^3 FP64-equivalent flops per matrix (eigh), 16 nw^3
-    flops per field (rotation), 9 nw^2 s bytes per k-point (Omega)."""
+    """Roofline of one stage from its algorithmic work per launch alone:
+      R->k     2 F nw^2 s bytes per k-point (each field written and read back once; s = 16 B FP64,
+               8 B FP32 complex, 16 B double-float H);
+      eigh     20 nw^3 flops per matrix (FP64-class: tridiagonalisation, back-transform and
+               tridiagonal eigenvectors), against the pipe the arithmetic runs on -- the FP64 pipe
+               (FP64 path) or the FP32 pipe (double-float, mixed path);
+      rotation 16 nw^3 flops per field and k-point (two complex GEMMs; the three TF32 products of
+               the split count once), 9 fields, against dense TF32 (mixed) or the FP64 pipe;
+      Omega    9 nw^2 s bytes per k-point (V, A and the rotA diagonal read).
+    The extra arithmetic of the precision scheme (about 8.5 FP32 flops per double-float flop; three
+    tensor products per rotation product) is reported apart as `pipe_work_frac`, how busy the
+    pipe is, and does not enter `frac`."""
     n = NW
     per_launch_ms = ms_total / max(n_calls, 1)
-    if stage == 'eigh' and precision == 'fp64':
-        work = 20.0 * n ** 3 * k_per_call          # FP64 flops, convention 20 nw^3 per matrix
-        bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
-    elif stage == 'eigh':
-        # double-float solve on the FP32 pipe: 20 nw^3 FP64-equivalent flops per matrix, each
-        # costing 8.5 FP32 flops (a double-float FMA = 3 FMA + 1 MUL + 10 ADD = 17 FP32 flops)
-        work = 20.0 * n ** 3 * 8.5 * k_per_call
-        bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
+    pipe_factor = None
+    if stage == 'eigh':
+        work = 20.0 * n ** 3 * k_per_call
+        if precision == 'fp64':
+            bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
+        else:
+            bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
+            pipe_factor = 8.5  # FP32 flops per double-float flop (FMA = 3 FMA + 1 MUL + 10 ADD)
     elif stage == 'rotate':
         work = 16.0 * n ** 3 * 9 * k_per_call      # two complex GEMMs per field, 9 fields
         if precision == 'fp64':
             bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
-        elif peaks.get('tf32'):  # tcgen05 kind::tf32: three TF32 products per product (3xTF32)
-            work *= 3.0
+        else:  # tcgen05 kind::tf32, three TF32 products per product (3xTF32)
             bound, unit, peak, src = 'tensor', 'GFLOP/s', peaks['tf32'], \
                 'MEASURED_PEAKS.json bf16_tflops (burst) / 2: dense TF32 rate'
-        else:
-            bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
+            pipe_factor = 3.0
     elif stage.startswith('r2k'):
         s = 16 if stage in ('r2k_fp64', 'r2k_df64') else 8
         work = 2.0 * nF_fields[stage] * n * n * s * k_per_call   # bytes: write + read back of each field
@@ -250,9 +275,13 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
         work = 9.0 * n * n * s * k_per_call
         bound, unit, peak, src = 'hbm', 'GB/s', peaks['hbm'], 'MEASURED_PEAKS.json hbm_gbs'
     achieved = work / (per_launch_ms * 1e-3) / 1e9
-    return {"kernel": stage, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak if peak else None, "peak_source": src, "ms_per_launch": per_launch_ms,
-            "work_per_launch": work, **_traffic(stage, precision, k_per_call)}
+    out = {"kernel": stage, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+           "frac": achieved / peak if peak else None, "peak_source": src, "ms_per_launch": per_launch_ms,
+           "work_per_launch": work, **_traffic(stage, precision, k_per_call)}
+    if pipe_factor:
+        out["pipe_work_frac"] = achieved * pipe_factor / peak
+        out["pipe_work_factor"] = pipe_factor
+    return out
 
 
 def _traffic(stage, precision, k_per_call):
@@ -276,16 +305,20 @@ def run_gpu(args):
         dist.init_process_group('nccl')
     s = build_system(device='cuda')
     cpu = None
+    cpu_check = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         path = save_system_npz(s)
         try:
-            rate, wall = cpu_rate(path, procs, procs)
+            rate, wall, cdKs, cres = cpu_rate(path, procs, procs)
         finally:
             os.unlink(path)
+        cpu_check = (np.array(cdKs), np.sum(cres, axis=0) / len(cres))
         cpu = {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{procs} spawned oracle processes, one {CPU_SAMPLE_NKFFT}^3 block each of the same nw=32 "
-                         f"MDRS system (AHC, {NEF} E_F), {wall:.1f} s wall"}
+                         f"MDRS system (AHC, {NEF} E_F), {wall:.1f} s wall; the oracle is the reference's "
+                         "algorithm restated in numpy (per k-point, per band-group loops), measured 1.64x faster "
+                         "per core than the reference's own run() on the same block"}
     import wbgpu
     from wbgpu import engine, _lib
     from wbgpu.calculators import AHC
@@ -358,10 +391,12 @@ def run_gpu(args):
 
     # plain FP64 drop-in throughput on the same blocks, and the mixed-vs-FP64 error of one step
     fp64_value = None
+    fp64_timer = None
+    K64 = max(1, min(args.steps, 3))
     err = None
     if precision == 'mixed' and not args.no_fp64_compare:
-        K64 = max(1, min(args.steps, 3))
-        ms64 = timed_loop('fp64', K64, 1)
+        fp64_timer = engine.StageTimer()
+        ms64 = timed_loop('fp64', K64, 1, fp64_timer)
         fp64_value = world * K64 * B * nk / (ms64 * 1e-3)
         c1, c2 = AHC(Efermi=EF), AHC(Efermi=EF)
         c1.reset(dev.device)
@@ -372,31 +407,51 @@ def run_gpu(args):
         b = c2.finalize(s.cell_volume, nk)
         err = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
+    # both precisions against the oracle on the CPU baseline's blocks (the same system, 12^3 FFT
+    # blocks at the oracle's shifts): the checker of the benchmarked path
+    err_oracle = None
+    if cpu_check is not None:
+        cdKs, cref = cpu_check
+        nkc = CPU_SAMPLE_NKFFT ** 3
+        err_oracle = {"sample": f"{len(cdKs)} blocks of {CPU_SAMPLE_NKFFT}^3 k-points (the CPU baseline's), "
+                                "AHC at 1001 E_F, max over E_F and components / max |AHC|"}
+        for prec in ('mixed', 'fp64'):
+            c = AHC(Efermi=EF)
+            c.reset(dev.device)
+            bdc = engine.band_data(dev, cdKs, (CPU_SAMPLE_NKFFT,) * 3, quantities, prec)
+            c.accumulate(bdc, s)
+            got = c.finalize(s.cell_volume, nkc) / len(cdKs)
+            err_oracle[prec] = float(np.max(np.abs(got - cref)) / np.max(np.abs(cref)))
+
     # end-to-end through the public API: fresh device upload of the R-space matrices from
     # pinned host memory, run() over this step's blocks, result read back to the host
-    Ke = max(1, min(args.steps, 5))
-    h2d = 0
-    for i in range(args.warmup):  # warm-up of the e2e path
-        wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=precision, blocks=step_blocks(i))
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for i in range(Ke):
-        dsys = engine.DeviceSystem(s)
-        r = wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=precision, blocks=step_blocks(i), dev_system=dsys)
-        h2d = dsys.h2d_bytes
-        _ = r['ahc'].data  # already on the host (device->host copy inside run())
-    e1.record()
-    torch.cuda.synchronize()
-    ems = e0.elapsed_time(e1)
-    if world > 1:
-        tt = torch.tensor([ems], device='cuda')
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ems = float(tt.item())
-    e2e = {"value": world * Ke * B * nk / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": NEF * 3 * 8}
+    def e2e_run(prec):
+        Ke = max(1, min(args.steps, 5))
+        h2d = 0
+        for i in range(args.warmup):  # warm-up of the e2e path
+            wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=prec, blocks=step_blocks(i))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(Ke):
+            dsys = engine.DeviceSystem(s)
+            r = wbgpu.run(s, grid, {'ahc': AHC(Efermi=EF)}, precision=prec, blocks=step_blocks(i), dev_system=dsys)
+            h2d = dsys.h2d_bytes
+            _ = r['ahc'].data  # already on the host (device->host copy inside run())
+        e1.record()
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1)
+        if world > 1:
+            tt = torch.tensor([ems], device='cuda')
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ems = float(tt.item())
+        return {"value": world * Ke * B * nk / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": NEF * 3 * 8}
+
+    e2e = e2e_run(precision)
+    e2e64 = e2e_run('fp64') if fp64_value is not None else None
 
     peaks = {'fp64': probe_peak(torch, True), 'fp32': probe_peak(torch, False)}
     try:
@@ -415,16 +470,25 @@ def run_gpu(args):
     for st_name in stage_ms:
         r_ = stage_roofline(st_name, stage_ms[st_name], args.steps, B * nk, precision, peaks, nF_fields)
         stages_roof[st_name] = {k_: r_[k_] for k_ in ('bound', 'achieved', 'peak', 'unit', 'frac')}
+    fp64_dropin = None
+    if fp64_value is not None:
+        st64 = fp64_timer.totals_ms()
+        dom64 = max(st64, key=st64.get)
+        fp64_dropin = {"value": fp64_value, "unit": UNIT, "steps": K64, "dtype": dtype_of('fp64'),
+                       "e2e": e2e64,
+                       "roofline": stage_roofline(dom64, st64[dom64], K64, B * nk, 'fp64', peaks, nF_fields),
+                       "stage_ms_per_step": {k: v / K64 for k, v in st64.items()},
+                       "mixed_speedup": value / fp64_value, "mixed_e2e_speedup": e2e["value"] / e2e64["value"]}
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp64 eigh/scan + fp32 fields" if precision == 'mixed' else "fp64",
-            "data": "synthetic (seeded random TB model)", "config": config_dict(args, precision),
+            "vs_baseline": None, "dtype": dtype_of(precision), "precision": precision,
+            "data": "synthetic (seeded random TB model)", "config": config_dict(args),
             "roofline": roof, "stages_roofline": stages_roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clk,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
-            "fp64_dropin_value": fp64_value, "max_rel_err_vs_fp64": err,
+            "fp64_dropin": fp64_dropin, "max_rel_err_vs_fp64": err, "max_rel_err_vs_oracle": err_oracle,
             "peaks_measured_gflops": {"fp64": peaks['fp64'], "fp32": peaks['fp32']}}
     if world == 1 and not args.no_serve:
         for key, fn in (("batched", bench_batched), ("served", bench_served)):

@@ -140,16 +140,22 @@ int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
 
 /* Allocation-free variant of wbg_eigh_batched (no counterpart in the reference).
- * For callers that cannot allocate device memory -- inside stream capture, under a host
- * framework whose allocator owns the device memory, or in loops that forbid allocation --
- * the workspace is a fixed file-scope device array of WBG_EIGH_NOALLOC_SCRATCH_BYTES that
- * every GPU loading the library keeps until process exit.  Same arguments and results as
- * wbg_eigh_batched minus the workspace.  A batch needs
+ * For callers that cannot allocate device memory: a plugin inside a host application whose
+ * memory manager owns the GPU's memory (a caching allocator, a fixed budget), a real-time loop
+ * that forbids allocation after start-up (cudaMalloc / cudaFree may synchronise the device and
+ * take unbounded time), or an FFI binding with no device allocator of its own.  The workspace
+ * is a fixed file-scope device array of WBG_EIGH_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library keeps until process exit.  Same arguments, rules and results as
+ * wbg_eigh_batched minus the workspace (U may be NULL with WBG_EIGH_VALUES), except that the
+ * two-stage split WBG_EIGH_STAGE1 / WBG_EIGH_STAGE2 is refused (WBG_STATUS_BAD_ARGUMENT): any
+ * other call between the stages would overwrite the shared array.  A batch needs
  *   nk * (16*nw*nw + 32*nw) + 1024 <= WBG_EIGH_NOALLOC_SCRATCH_BYTES
  * (nw = 32: nk <= 1920); larger batches return WBG_STATUS_TOO_LARGE without launching.
- * The first call on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU race, so serialise them.  No allocation or free is performed. */
+ * The first call on a device (and the first call after that device's context was destroyed
+ * and recreated) looks up the array's device address with cudaGetSymbolAddress; make that
+ * first call before any stream capture.  All calls share the array, which keeps the last
+ * call's contents: calls whose work overlaps on the GPU race, so serialise them.  No device
+ * memory is allocated or freed. */
 #define WBG_EIGH_NOALLOC_SCRATCH_BYTES (32u << 20)
 int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
                              long long strideU, int mode, int* errflag, void* stream);

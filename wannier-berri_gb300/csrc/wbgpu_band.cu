@@ -344,6 +344,10 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
     __syncthreads();
   }
   V* dst = Xbar + (k * nFrot + f) * (long long)nw * nw;
+  // Hermitian part (herm 1): the lower triangle computed by this panel is written together
+  // with its conjugate mirror and the diagonal is taken real, so the stored matrix is Hermitian
+  // bit for bit (the consumers' pair terms rely on X_ln = conj(X_nl) exactly); the panel's
+  // upper-triangle products are dropped -- the panel of their row writes them.
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -352,6 +356,13 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
       if (m >= nw || n >= nw) continue;
       if ((hm & 3) == 2) {
         if (m == n) dst[m * nw + n] = mkc<T>(acc[a][c].x, (T)0);
+      } else if ((hm & 3) == 1) {
+        if (m == n) {
+          dst[m * nw + n] = mkc<T>(acc[a][c].x, (T)0);
+        } else if (m > n) {
+          dst[m * nw + n] = acc[a][c];
+          dst[n * nw + m] = mkc<T>(acc[a][c].x, -acc[a][c].y);
+        }
       } else {
         dst[m * nw + n] = acc[a][c];
       }
@@ -563,129 +574,172 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
 
 // ---------------------------------------------------------------------------------------
 // Omega traces for exactly Hermitian V and A in FP32 (the mixed path: lower-triangle inputs,
-// Hermitian-part rotation), nw <= 32.  Lane l owns column l and the warp walks the rows n, so
-// every load is a coalesced row segment; the (l, n) elements come from V_ln = conj(V_nl) and
-// A_ln = conj(A_nl).  One warp reduction per row gives the trace t(n) (same terms as
-// berry_omega_kernel); grouping and binning are the same.  One warp per k-point.
+// Hermitian rotation outputs), nw <= 32 C.  Lane l owns the bands (columns) l + 32 j, j < C,
+// and the warp walks the rows n, so every load is a coalesced row segment.  Each band sums its
+// own trace.  For a pair (l, n) in different degenerate groups the term of band l is
+// T(l, n) = Re[-i D^a_ln D^b_nl - D^a_ln A^b_nl + D^b_ln A^a_nl] = -T(n, l) (D anti-Hermitian,
+// A Hermitian); the two lanes that meet the pair both evaluate the one canonical term T(p, q),
+// p = min(l, n), q = max(l, n), from the element X_pq (X_nl itself, or the conjugate of it,
+// which is X_ln bit for bit), with the same arithmetic, so the two bands receive +T and -T
+// exactly.  Over any set of bands the scan adds together (the Fermi sea, or every level above
+// two groups) the pair terms then cancel without FP32 residue -- the terms of near-degenerate
+// pairs, |V|^2 / dE^2, can be 10^4 times the result.  A band's sum is compensated (TraceSum)
+// and kept as a double.  The sea group's trace is the sum of its bands' traces over their own
+// degenerate groups: equal to the reference's sea trace in exact arithmetic, since the
+// cross-group A A terms inside the sea cancel pairwise as well.  Grouping and binning as in
+// berry_omega_kernel.  One warp per k-point, G warps per block.
 // ---------------------------------------------------------------------------------------
+template <int C>
 __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __restrict__ Xbar, int nFbar, int iV,
                                  int iA, int iO, int nw, int nk, int G, WbgScan sp, int internal_terms,
                                  int external_terms, double* __restrict__ hist) {
+  constexpr int NWM = 32 * C;
   extern __shared__ double smb[];
-  double* sh = smb;                                        // [nEF][3]
-  double* Es = sh + 3 * sp.nEF;                            // [G][32]
-  double* tv = Es + G * 32;                                // [G][32][3]
-  float* Ehl = reinterpret_cast<float*>(tv + 3 * G * 32);  // [G][2][32]
-  int* start = reinterpret_cast<int*>(Ehl + 2 * G * 32);   // [G][32]
+  double* sh = smb;                                         // [nEF][3]
+  double* Es = sh + 3 * sp.nEF;                             // [G][NWM]
+  double* tv = Es + G * NWM;                                // [G][NWM][3]
+  float* Ehl = reinterpret_cast<float*>(tv + 3 * G * NWM);  // [G][2][NWM]
+  int* start = reinterpret_cast<int*>(Ehl + 2 * G * NWM);   // [G][NWM]
   for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
   __syncthreads();
   const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double* myE = Es + grp * 32;
-  double* myT = tv + 3 * grp * 32;
-  float* myEh = Ehl + 2 * grp * 32;
-  float* myEl = myEh + 32;
-  int* myS = start + grp * 32;
+  double* myE = Es + grp * NWM;
+  double* myT = tv + 3 * grp * NWM;
+  float* myEh = Ehl + 2 * grp * NWM;
+  float* myEl = myEh + NWM;
+  int* myS = start + grp * NWM;
   const long long nw2 = (long long)nw * nw;
   for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
     const long long k = base + grp;
     const bool valid = k < nk;
     const long long kk = valid ? k : nk - 1;
-    if (lane < nw) {
-      const double e = E[kk * nw + lane];
-      const float eh = (float)e;
-      myE[lane] = e;
-      myEh[lane] = eh;
-      myEl[lane] = (float)(e - (double)eh);
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      const int i = lane + 32 * j;
+      if (i < nw) {
+        const double e = E[kk * nw + i];
+        const float eh = (float)e;
+        myE[i] = e;
+        myEh[i] = eh;
+        myEl[i] = (float)(e - (double)eh);
+      }
     }
     __syncwarp();
-    if (lane < nw) myS[lane] = (lane == 0) || (myE[lane] - myE[lane - 1] > sp.degen_thresh);
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      const int i = lane + 32 * j;
+      if (i < nw) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
+    }
     __syncwarp();
     int below = 0, f0 = nw;
-    if (lane < nw) {
-      below = myE[lane] < sp.EFmin;
-      if (myS[lane]) {
-        int g1 = lane + 1;
-        while (g1 < nw && !myS[g1]) ++g1;
-        if (myE[g1 - 1] >= sp.EFmin && myE[lane] <= sp.EFmax) f0 = lane;
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      const int i = lane + 32 * j;
+      if (i < nw) {
+        below += myE[i] < sp.EFmin;
+        if (myS[i]) {
+          int g1 = i + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[i] <= sp.EFmax) f0 = min(f0, i);
+        }
       }
     }
     below = group_sum_i(below, 32);
     f0 = group_min_i(f0, 32);
     const int bandmax = min(below, f0);
-    const float2* Xk = Xbar + kk * nFbar * nw2;
-    const int l = lane;
-    for (int n = 0; n < nw; ++n) {  // warp-uniform
-      int gs = n, ge = n + 1;
-      while (!myS[gs]) --gs;
-      while (ge < nw && !myS[ge]) ++ge;
-      bool ingroup;
-      if (n < bandmax) { gs = 0; ge = bandmax; ingroup = true; }
-      else ingroup = (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
-      if (!ingroup) {
-        if (lane == 0) for (int g = 0; g < 3; ++g) myT[n * 3 + g] = 0.0;
-        continue;
-      }
-      float sr[3] = {0.f, 0.f, 0.f};  // Re of the trace terms of column l
+    // own bands: degenerate group [gs, ge) and whether the scan reads the band
+    int gs[C], ge[C];
+    bool need[C];
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      const int l = lane + 32 * j;
+      gs[j] = ge[j] = 0;
+      need[j] = false;
       if (l < nw) {
+        int a = l, b = l + 1;
+        while (!myS[a]) --a;
+        while (b < nw && !myS[b]) ++b;
+        gs[j] = a;
+        ge[j] = b;
+        need[j] = l < bandmax || (myE[b - 1] >= sp.EFmin && myE[a] <= sp.EFmax);
+      }
+    }
+    TraceSum<float> acc[C][3];
+    const float2* Xk = Xbar + kk * nFbar * nw2;
+    for (int n = 0; n < nw; ++n) {  // warp-uniform
+#pragma unroll
+      for (int j = 0; j < C; ++j) {
+        const int l = lane + 32 * j;
+        if (l >= nw || !need[j]) continue;
         float2 Vn[3], An[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           Vn[a] = Xk[(iV + a) * nw2 + n * nw + l];
           An[a] = external_terms ? Xk[(iA + a) * nw2 + n * nw + l] : make_float2(0.f, 0.f);
         }
-        if (l < gs || l >= ge) {
-          const float dinv = inv_gap<float>(myE, myEh, myEl, n, l);
-          float2 Dnl[3], Dln[3], Aln[3];
+        if (n < gs[j] || n >= ge[j]) {
+          // canonical pair (p, q) = (min, max): X_pq = X_nl if n < l, else X_ln = conj(X_nl)
+          const bool np = n < l;
+          const int p = np ? n : l, q = np ? l : n;
+          const float dinv = inv_gap<float>(myE, myEh, myEl, p, q);  // 1 / (E_p - E_q)
+          float2 Dpq[3], Dqp[3], Aqp[3];
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            Dnl[a] = cscale(Vn[a], -dinv);         // D_nl = -V_nl / (E_n - E_l)
-            Dln[a] = cscale(cconj(Vn[a]), dinv);   // D_ln = -V_ln / (E_l - E_n), V_ln = conj(V_nl)
-            Aln[a] = cconj(An[a]);                  // A_ln = conj(A_nl)
+            const float2 vpq = np ? Vn[a] : cconj(Vn[a]);
+            const float2 apq = np ? An[a] : cconj(An[a]);
+            Dpq[a] = cscale(vpq, -dinv);        // D_pq = -V_pq / (E_p - E_q)
+            Dqp[a] = cscale(cconj(vpq), dinv);  // D_qp = -V_qp / (E_q - E_p), V_qp = conj(V_pq)
+            Aqp[a] = cconj(apq);                // A_qp = conj(A_pq)
           }
 #pragma unroll
           for (int g = 0; g < 3; ++g) {
             const int al = (g + 1) % 3, be = (g + 2) % 3;
-            float2 acc = czero<float2>(), accx = czero<float2>();
-            if (internal_terms) acc = cmuli(cmul(Dnl[al], Dln[be]));
-            if (external_terms) { cfma(accx, Dnl[be], Aln[al]); accx = csub(accx, cmul(Dnl[al], Aln[be])); }
-            sr[g] += accx.x - acc.x;  // Re[-i D^a_nl D^b_ln - D^a_nl A^b_ln + D^b_nl A^a_ln]
+            float2 dd = czero<float2>(), dx = czero<float2>();
+            if (internal_terms) dd = cmuli(cmul(Dpq[al], Dqp[be]));
+            if (external_terms) { cfma(dx, Dpq[be], Aqp[al]); dx = csub(dx, cmul(Dpq[al], Aqp[be])); }
+            const float t = dx.x - dd.x;  // T(p, q) = Re[-i D^a_pq D^b_qp - D^a_pq A^b_qp + D^b_pq A^a_qp]
+            acc[j][g].add(np ? -t : t);   // band l = q receives T(q, p) = -T(p, q)
           }
-        } else if (external_terms) {  // within the group: Re(-i A^a_nl A^b_ln), plus 1/2 O_nn
+        } else if (external_terms) {  // n in l's group: Re(-i A^a_ln A^b_nl), plus 1/2 O_ll
 #pragma unroll
           for (int g = 0; g < 3; ++g) {
             const int al = (g + 1) % 3, be = (g + 2) % 3;
-            sr[g] += cmul(An[al], cconj(An[be])).y;
-            if (l == n) sr[g] += 0.5f * Xk[(iO + g) * nw2 + n * nw + n].x;
+            acc[j][g].add(cmul(cconj(An[al]), An[be]).y);
+            if (l == n) acc[j][g].add(0.5f * Xk[(iO + g) * nw2 + n * nw + n].x);
           }
         }
       }
+    }
 #pragma unroll
-      for (int g = 0; g < 3; ++g)
-        for (int off = 16; off > 0; off >>= 1) sr[g] += __shfl_xor_sync(0xffffffffu, sr[g], off);
-      if (lane == 0)
-        for (int g = 0; g < 3; ++g) myT[n * 3 + g] = 2.0 * (double)sr[g];
+    for (int j = 0; j < C; ++j) {
+      const int l = lane + 32 * j;
+      if (l < nw)
+        for (int g = 0; g < 3; ++g) myT[l * 3 + g] = need[j] ? 2.0 * acc[j][g].value() : 0.0;
     }
     __syncwarp();
-    if (valid && lane < nw) {
-      const int n = lane;
-      int gs = -1, ge = -1;
-      bool sea = false;
-      if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; sea = true; }
-      else if (n >= bandmax && myS[n]) {
-        int g1 = n + 1;
-        while (g1 < nw && !myS[g1]) ++g1;
-        if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
-      }
-      if (gs >= 0) {
+    if (valid) {
+#pragma unroll
+      for (int j = 0; j < C; ++j) {
+        const int n = lane + 32 * j;
+        if (n >= nw) continue;
+        int g0 = -1, g1 = -1;
+        bool sea = false;
+        if (n == 0 && bandmax > 0) { g0 = 0; g1 = bandmax; sea = true; }
+        else if (n >= bandmax && myS[n]) {
+          int e1 = n + 1;
+          while (e1 < nw && !myS[e1]) ++e1;
+          if (myE[e1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { g0 = n; g1 = e1; }
+        }
+        if (g0 < 0) continue;
         double v[3] = {0.0, 0.0, 0.0}, esum = 0.0;
-        for (int q = gs; q < ge; ++q) {
+        for (int q = g0; q < g1; ++q) {
           for (int g = 0; g < 3; ++g) v[g] += myT[q * 3 + g];
           esum += myE[q];
         }
         int bin = -1;
         if (sea) bin = 0;
         else {
-          const double Em = esum / (double)(ge - gs);
+          const double Em = esum / (double)(g1 - g0);
           if (Em < sp.EFmin) bin = 0;
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
@@ -1452,18 +1506,21 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   WbgScan spv = *sp_in;
   if (sel) { spv.nEF = 0; hist = nullptr; tab = nullptr; }  // per-band values: no histogram
   const WbgScan* sp = &spv;
-  if (fp64 == 2 && nw <= 32 && !tab && !sel) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
+  if (fp64 == 2 && nw <= 128 && !tab && !sel) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
+    const int C = (nw + 31) / 32;
     const int G = 4;  // k-points (warps) per block
-    const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * (8 + 24 + 8 + 4);
+    const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * C * (8 + 24 + 8 + 4);
     if (sm > 220 * 1024) return WBG_ERR_SIZE;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     long long nblk = (nk + G - 1) / G;
     const long long cap = (long long)sms * 16;
     if (nblk > cap) nblk = cap;
-    cudaFuncSetAttribute(berry_omega_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    berry_omega_cols<<<(int)nblk, 32 * G, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, G, *sp,
-                                                        internal_terms, external_terms, hist);
+    void (*kern)(const double*, const float2*, int, int, int, int, int, int, int, WbgScan, int, int, double*) =
+        C == 1 ? berry_omega_cols<1> : C == 2 ? berry_omega_cols<2> : C == 3 ? berry_omega_cols<3> : berry_omega_cols<4>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    kern<<<(int)nblk, 32 * G, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, G, *sp, internal_terms,
+                                           external_terms, hist);
     return wbg_cuda_status(cudaGetLastError());
   }
   if (fp64 == 2) fp64 = 0;  // the general FP32 kernel does not need the symmetry

@@ -680,47 +680,90 @@ int wbg_eigh_tune_candidates(int param, int n, int variant, int* values, int cap
 // ---------------------------------------------------------------------------------------
 // Allocation-free variant of wbg_eigh_batched.
 //
-// Some callers cannot call cudaMalloc at all: code running inside a CUDA-graph capture or
-// a stream-ordered region that must not synchronise, plugins living in a host process
-// whose allocator owns all device memory (a framework caching allocator, an embedding
-// application with a fixed memory budget), and real-time loops that forbid allocation
-// after start-up.  For them the eigensolver's workspace lives in a fixed file-scope device
-// array instead of a caller- or library-allocated buffer.  The array is part of the module:
-// every GPU that loads this library holds WBG_EIGH_NOALLOC_SCRATCH_BYTES of it until the
-// process exits.  All calls share it, so calls whose work overlaps on the GPU (different
-// streams, or different host threads on one device) race and must be serialised by the
-// caller.  Every workspace word is written by the kernels before it is read, so the
-// contents left by a previous call never need clearing.
+// Some callers cannot call cudaMalloc: a plugin inside a host application whose memory
+// manager owns all of the GPU's memory (a framework's caching allocator, an embedding
+// application with a fixed budget), a real-time loop that forbids allocation after start-up
+// because cudaMalloc / cudaFree may synchronise the device and take unbounded time, and a
+// thin FFI binding (ctypes, cgo) that has no device allocator of its own.  For them the
+// eigensolver's workspace lives in a fixed file-scope device array instead of a caller- or
+// library-allocated buffer.  The array is part of the module: every GPU that loads this
+// library holds WBG_EIGH_NOALLOC_SCRATCH_BYTES of it until the process exits.  All calls
+// share it, so calls whose work overlaps on the GPU (different streams, or different host
+// threads on one device) race and must be serialised by the caller.  Every workspace word is
+// written by the kernels before it is read, so the contents left by a previous call never
+// need clearing.  The two-call split (WBG_EIGH_STAGE1 / STAGE2) is refused here: any other
+// call between the two stages would overwrite the tridiagonal factors in the shared array.
 // ---------------------------------------------------------------------------------------
 #include <mutex>
+#include <cuda.h>
 
 static __device__ __align__(256) unsigned char g_eigh_noalloc_scratch[WBG_EIGH_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 constexpr int kMaxDevices = 64;
-void* g_noalloc_ptr[kMaxDevices] = {};
+struct NoallocSlot {
+  void* ptr = nullptr;
+  unsigned long long ctx_id = 0;  // context whose module the address belongs to
+};
+NoallocSlot g_noalloc[kMaxDevices];
 std::mutex g_noalloc_mutex;
 
-// Device address of the scratch array on the current device.  In host code the array's
-// name is only a host-side stand-in, so the address is looked up once per device with
-// cudaGetSymbolAddress (with that device current) and cached.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// Unique id of the current context (cuCtxGetId through the runtime's driver entry points, so
+// the library needs no link-time dependency on libcuda); 0 when the driver cannot say.
+unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS) return id;
+  return 0;
+}
+
+// Device address of the scratch array in the current context.  In host code the array's name
+// is only a host-side stand-in, so the address is looked up with cudaGetSymbolAddress (with
+// the device current) on the first call on each device and cached with the id of the context
+// it belongs to.  A context torn down and recreated (cudaDeviceReset, a released primary
+// context) reloads the module, and the array may then sit elsewhere: a call that finds a new
+// context id looks the address up again.
 int noalloc_scratch(void** ptr) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return WBG_ERR_CUDA;
+  const unsigned long long id = current_context_id();
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  NoallocSlot& slot = g_noalloc[dev];
+  if (!slot.ptr || id == 0 || slot.ctx_id != id) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_eigh_noalloc_scratch) != cudaSuccess || !p) return WBG_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
+    slot.ptr = p;
+    slot.ctx_id = id;
   }
-  *ptr = g_noalloc_ptr[dev];
+  *ptr = slot.ptr;
   return WBG_OK;
 }
 }  // namespace
 
 extern "C" int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, double* E, void* U,
                                         long long strideU, int mode, int* errflag, void* stream) {
-  if (nw < 1 || nw > WBG_EIGH_NMAX || nk < 1 || !H || !E || !U || !errflag) return WBG_ERR_ARG;
+  // the argument rules of wbg_eigh_batched (U may be NULL for eigenvalues only), without the
+  // two-stage split, whose tridiagonal factors could not survive another call in between
+  if (mode & (WBG_EIGH_STAGE1 | WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
+  if (nw < 1 || nw > WBG_EIGH_NMAX || nk < 1 || !H || !E || (!U && !(mode & WBG_EIGH_VALUES)) || !errflag)
+    return WBG_ERR_ARG;
   const size_t need = wbg_eigh_workspace_bytes(nw, nk);
   if (need > (size_t)WBG_EIGH_NOALLOC_SCRATCH_BYTES) return WBG_ERR_SIZE;  // batch too large for the scratch
   void* ws = nullptr;

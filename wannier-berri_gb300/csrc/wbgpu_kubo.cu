@@ -18,9 +18,11 @@
 //              ordered pair of groups kept by `nonzero` (dynamic.py:65-69; JDOS :158-162); the
 //              element tensors are computed in place from the band-basis fields, with sums over
 //              the intermediate bands for SHC and the shift current.  One record per pair:
-//              E2 - E1, f_E per level, M (FP32).
+//              E2 - E1 (FP64), f_E per level and M (FP32 in the mixed path, FP64 in the
+//              FP64 path).
 // kubo_accum:  one thread per frequency, a chunk of levels per block (grid z), a chunk of
-//              k-points per block (grid y): FP32 accumulation in shared memory, FP64 atomics.
+//              k-points per block (grid y): accumulation in shared memory in the records'
+//              precision, FP64 atomics into the result.
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_kubo.cuh"
@@ -178,7 +180,7 @@ WBG_D void add_element(const KBand<T>& b, int n, int m, typename C2<T>::t* M) {
 template <typename T, int F>
 __global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                            wbg_dynamic_spec fs, int nw, WbgKubo kp, const double* __restrict__ efermi,
-                           double* __restrict__ rec_dE, float* __restrict__ rec_fE, float2* __restrict__ rec_M,
+                           double* __restrict__ rec_dE, T* __restrict__ rec_fE, typename C2<T>::t* __restrict__ rec_M,
                            int* __restrict__ count, int P) {
   typedef typename C2<T>::t V;
   constexpr int NC = dyn_ncomp(F);
@@ -236,58 +238,64 @@ __global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t
     const long long r = k * (long long)P + slot;
     rec_dE[r] = E2 - E1;
     for (int e = 0; e < kp.nEF; ++e)
-      rec_fE[r * kp.nEF + e] = (float)(fermi_dirac(E2, efermi[e], kp.kBT) - fermi_dirac(E1, efermi[e], kp.kBT));
+      rec_fE[r * kp.nEF + e] = (T)(fermi_dirac(E2, efermi[e], kp.kBT) - fermi_dirac(E1, efermi[e], kp.kBT));
 #pragma unroll
-    for (int i = 0; i < NC; ++i) rec_M[r * NC + i] = make_float2((float)M[i].x, (float)M[i].y);
+    for (int i = 0; i < NC; ++i) rec_M[r * NC + i] = M[i];
   }
   __syncthreads();
   if (threadIdx.x == 0) count[k] = cnt;
 }
 
-// smearing of dynamic.py:50-55 (utility.py:147-168)
-__device__ float smear(float x, float eta, int gaussian) {
+// smearing of dynamic.py:50-55 (utility.py:147-168), in the precision R of the accumulation
+template <typename R>
+__device__ R smear(R x, R eta, int gaussian) {
   if (gaussian) {
-    const float y = x / eta;
-    return fabsf(x) < eta * 14.142135623730951f ? 0.5641895835477563f / eta * expf(-y * y) : 0.0f;
+    const R y = x / eta;
+    return fabs(x) < eta * R(14.142135623730951) ? R(0.5641895835477563) / eta * exp(-y * y) : R(0);
   }
-  return 0.3183098861837907f * eta / (x * x + eta * eta);
+  return R(0.3183098861837907) * eta / (x * x + eta * eta);
 }
 
-// f_w(E1, E2) from dE = E2 - E1 (FP64 difference with the frequency, FP32 from there on)
-__device__ float2 factor_omega(int formula, double dE, double om, float eta, int gaussian) {
+// f_w(E1, E2) from dE = E2 - E1 (FP64 difference with the frequency, precision R from there on:
+// FP32 in the mixed path, FP64 in the FP64 path)
+template <typename R>
+__device__ typename C2<R>::t factor_omega(int formula, double dE, double om, R eta, int gaussian) {
   if (formula == WBG_DYN_OPTCOND || formula == kShcFactor) {
     // optical: (E2 - E1) / (E2 - E1 - w - i eta);  SHC: 1 / (E1 - E2 - w - i eta) / 2
     const bool opt = formula == WBG_DYN_OPTCOND;
-    const float delta = (float)(opt ? dE - om : -dE - om);
-    const float den = 1.0f / (delta * delta + eta * eta);
-    float cre = delta * den, cim = eta * den;
+    const R delta = (R)(opt ? dE - om : -dE - om);
+    const R den = R(1) / (delta * delta + eta * eta);
+    R cre = delta * den, cim = eta * den;
     if (gaussian) {
-      const float x = delta / eta;
-      cim = fabsf(delta) < eta * 14.142135623730951f ? 1.7724538509055160f / eta * expf(-x * x) : 0.0f;
+      const R x = delta / eta;
+      cim = fabs(delta) < eta * R(14.142135623730951) ? R(1.7724538509055160) / eta * exp(-x * x) : R(0);
     }
-    const float s = opt ? (float)dE : 0.5f;
-    return make_float2(s * cre, s * cim);
+    const R s = opt ? (R)dE : R(0.5);
+    return mkc<R>(s * cre, s * cim);
   }
-  float v = smear((float)(-dE - om), eta, gaussian);  // JDOS, injection: smear(E1 - E2 - w)
-  if (formula == WBG_DYN_SHIFT) v += smear((float)(dE - om), eta, gaussian);
-  return make_float2(v, 0.0f);
+  R v = smear<R>((R)(-dE - om), eta, gaussian);  // JDOS, injection: smear(E1 - E2 - w)
+  if (formula == WBG_DYN_SHIFT) v += smear<R>((R)(dE - om), eta, gaussian);
+  return mkc<R>(v, R(0));
 }
 
 // grid: (ceil(nOmega / TPB), k chunks, level chunks); out [nEF][nOmega][NC] complex128 (accumulated)
-template <int NC>
-__global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __restrict__ rec_fE,
-                           const float2* __restrict__ rec_M, const int* __restrict__ count, int P, int nk, int kchunk,
-                           const double* __restrict__ omega, WbgKubo kp, int formula, int efc,
+// R: precision of the records and the accumulation (float: mixed path, double: FP64 path)
+template <int NC, typename R>
+__global__ void kubo_accum(const double* __restrict__ rec_dE, const R* __restrict__ rec_fE,
+                           const typename C2<R>::t* __restrict__ rec_M, const int* __restrict__ count, int P, int nk,
+                           int kchunk, const double* __restrict__ omega, WbgKubo kp, int formula, int efc,
                            double2* __restrict__ out) {
+  typedef typename C2<R>::t V;
   constexpr int nc = NC;
-  extern __shared__ float2 acc[];  // [efc][NC][blockDim.x]
+  extern __shared__ unsigned char smacc[];
+  V* acc = reinterpret_cast<V*>(smacc);  // [efc][NC][blockDim.x]
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = w < kp.nOmega;
   const int e0 = blockIdx.z * efc;
   const int ne = min(efc, kp.nEF - e0);
-  for (int i = 0; i < ne * nc; ++i) acc[i * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
+  for (int i = 0; i < ne * nc; ++i) acc[i * blockDim.x + threadIdx.x] = czero<V>();
   const double om = active ? omega[w] : 0.0;
-  const float eta = (float)kp.eta;
+  const R eta = (R)kp.eta;
   const int fgroup = formula >= WBG_DYN_SHC_SIMPLE && formula <= WBG_DYN_SHC_RYOO ? kShcFactor : formula;
   const long long k0 = (long long)blockIdx.y * kchunk;
   const long long k1 = min((long long)nk, k0 + kchunk);
@@ -295,19 +303,19 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __res
     const int nrec = count[k];
     for (int q = 0; q < nrec; ++q) {
       const long long r = k * (long long)P + q;
-      const float2 fw = factor_omega(fgroup, rec_dE[r], om, eta, kp.gaussian);
-      float2 Mv[NC];
+      const V fw = factor_omega<R>(fgroup, rec_dE[r], om, eta, kp.gaussian);
+      V Mv[NC];
 #pragma unroll
       for (int i = 0; i < NC; ++i) Mv[i] = rec_M[r * NC + i];
       for (int e = 0; e < ne; ++e) {
-        const float fe = rec_fE[r * kp.nEF + e0 + e];
-        if (fe == 0.0f) continue;
-        const float2 c = make_float2(fe * fw.x, fe * fw.y);
+        const R fe = rec_fE[r * kp.nEF + e0 + e];
+        if (fe == R(0)) continue;
+        const V c = mkc<R>(fe * fw.x, fe * fw.y);
 #pragma unroll
         for (int i = 0; i < NC; ++i) {
-          float2& a = acc[(e * NC + i) * blockDim.x + threadIdx.x];
-          a.x = fmaf(c.x, Mv[i].x, fmaf(-c.y, Mv[i].y, a.x));
-          a.y = fmaf(c.x, Mv[i].y, fmaf(c.y, Mv[i].x, a.y));
+          V& a = acc[(e * NC + i) * blockDim.x + threadIdx.x];
+          a.x = fma(c.x, Mv[i].x, fma(-c.y, Mv[i].y, a.x));
+          a.y = fma(c.x, Mv[i].y, fma(c.y, Mv[i].x, a.y));
         }
       }
     }
@@ -315,7 +323,7 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __res
   if (!active) return;
   for (int e = 0; e < ne; ++e)
     for (int i = 0; i < nc; ++i) {
-      const float2 a = acc[(e * nc + i) * blockDim.x + threadIdx.x];
+      const V a = acc[(e * nc + i) * blockDim.x + threadIdx.x];
       double2* o = out + ((long long)(e0 + e) * kp.nOmega + w) * nc + i;
       atomicAdd(&o->x, (double)a.x);
       atomicAdd(&o->y, (double)a.y);
@@ -325,11 +333,11 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const float* __res
 template <typename T>
 void launch_pairs(int formula, int nk, size_t smp, cudaStream_t stream, const double* E, const void* Xbar, int nFbar,
                   const wbg_dynamic_spec& fs, int nw, const WbgKubo& kp, const double* efermi, double* rec_dE,
-                  float* rec_fE, float2* rec_M, int* count, int P) {
+                  void* rec_fE, void* rec_M, int* count, int P) {
   typedef typename C2<T>::t V;
   const V* X = (const V*)Xbar;
-#define WBG_PAIRS(F) kubo_pairs<T, F><<<nk, 128, smp, stream>>>(E, X, nFbar, fs, nw, kp, efermi, rec_dE, rec_fE, \
-                                                                rec_M, count, P)
+#define WBG_PAIRS(F) kubo_pairs<T, F><<<nk, 128, smp, stream>>>(E, X, nFbar, fs, nw, kp, efermi, rec_dE, (T*)rec_fE, \
+                                                                (V*)rec_M, count, P)
   switch (formula) {
     case WBG_DYN_OPTCOND: WBG_PAIRS(WBG_DYN_OPTCOND); break;
     case WBG_DYN_JDOS: WBG_PAIRS(WBG_DYN_JDOS); break;
@@ -350,10 +358,12 @@ int wbg_dynamic_ncomp_impl(int formula) {
   return formula >= WBG_DYN_OPTCOND && formula <= WBG_DYN_INJECTION ? dyn_ncomp(formula) : 0;
 }
 
+// Records per pair slot: E2 - E1 (double), f_E per level and M (complex), both sized for the
+// FP64 path (the mixed path stores them in FP32 in the first half of each region).
 size_t wbg_dynamic_workspace_bytes(int formula, int nw, int nk, int nEF) {
   const size_t P = (size_t)nw * nw;
   const size_t nc = (size_t)wbg_dynamic_ncomp_impl(formula);
-  return (size_t)nk * P * (8 + 4 * (size_t)nEF + 8 * nc) + (size_t)nk * 4 + 1024;
+  return (size_t)nk * P * (8 + 8 * (size_t)nEF + 16 * nc) + (size_t)nk * 4 + 1024;
 }
 
 int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* fs, int nw, int nk,
@@ -384,8 +394,8 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
   const int P = nw * nw;
   char* w = (char*)workspace;
   double* rec_dE = (double*)w; w += (size_t)nk * P * 8;
-  float2* rec_M = (float2*)w; w += (size_t)nk * P * 8 * nc;
-  float* rec_fE = (float*)w; w += (size_t)nk * P * 4 * kp->nEF;
+  void* rec_M = w; w += (size_t)nk * P * 16 * nc;
+  void* rec_fE = w; w += (size_t)nk * P * 8 * kp->nEF;
   int* count = (int*)w;
   const size_t smp = (size_t)nw * 16 + (size_t)(2 * nw + 1) * 4;
   if (fp64)
@@ -395,17 +405,18 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
   // threads per block and levels per block: fewest passes over the records
   // (frequency blocks x level chunks), accumulators within 96 KB of shared memory
   const size_t smax = 96 * 1024;
+  const size_t vsz = fp64 ? 16 : 8;  // one complex accumulator
   int tpb = 0, efc = 0;
   long long best = -1;
   for (int t = 128; t >= 32; t /= 2) {
-    const int e = (int)((size_t)smax / ((size_t)t * nc * sizeof(float2)));
+    const int e = (int)((size_t)smax / ((size_t)t * nc * vsz));
     if (e < 1) continue;
     const int ec = e < kp->nEF ? e : kp->nEF;
     const long long passes = (long long)((kp->nOmega + t - 1) / t) * ((kp->nEF + ec - 1) / ec);
     if (best < 0 || passes < best) { best = passes; tpb = t; efc = ec; }
   }
   if (tpb == 0) return WBG_ERR_SIZE;
-  const size_t sma = (size_t)tpb * efc * nc * sizeof(float2);
+  const size_t sma = (size_t)tpb * efc * nc * vsz;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
   const int wblocks = (kp->nOmega + tpb - 1) / tpb;
@@ -415,19 +426,22 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
   const int kchunk = (nk + nchunks - 1) / nchunks;
   nchunks = (nk + kchunk - 1) / kchunk;
   const dim3 grid(wblocks, nchunks, eblocks);
-  if (nc == 1) {
-    cudaFuncSetAttribute(kubo_accum<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
-    kubo_accum<1><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
-                                              (double2*)out);
-  } else if (nc == 9) {
-    cudaFuncSetAttribute(kubo_accum<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
-    kubo_accum<9><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
-                                              (double2*)out);
+#define WBG_ACCUM(NC, R)                                                                                       \
+  do {                                                                                                         \
+    cudaFuncSetAttribute(kubo_accum<NC, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);           \
+    kubo_accum<NC, R><<<grid, tpb, sma, stream>>>(rec_dE, (const R*)rec_fE, (const typename C2<R>::t*)rec_M,   \
+                                                 count, P, nk, kchunk, omega, *kp, F, efc, (double2*)out);     \
+  } while (0)
+  if (fp64) {
+    if (nc == 1) WBG_ACCUM(1, double);
+    else if (nc == 9) WBG_ACCUM(9, double);
+    else WBG_ACCUM(27, double);
   } else {
-    cudaFuncSetAttribute(kubo_accum<27>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
-    kubo_accum<27><<<grid, tpb, sma, stream>>>(rec_dE, rec_fE, rec_M, count, P, nk, kchunk, omega, *kp, F, efc,
-                                               (double2*)out);
+    if (nc == 1) WBG_ACCUM(1, float);
+    else if (nc == 9) WBG_ACCUM(9, float);
+    else WBG_ACCUM(27, float);
   }
+#undef WBG_ACCUM
   return wbg_cuda_status(cudaGetLastError());
 }
 
