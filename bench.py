@@ -343,7 +343,7 @@ def run_gpu(args):
     quantities = calc.quantities(s)
     calc.reset(dev.device)
     phases = {p: dev.grid_phases(shifts, grid.FFT, p)
-              for p in (engine.PREC_FP64, engine.PREC_DF64, engine.PREC_FP32S)}
+              for p in sorted(set(engine.phase_precs('fp64') + engine.phase_precs('mixed')))}
 
     def step(i, precision, c=calc):
         blocks = step_blocks(i)
@@ -791,11 +791,11 @@ def bench_autotune(nws=(8, 32, 96)):
                        "(16384 x (32/nw)^3 matrices, clamped to 1024-32768)"}
     for nw in nws:
         autotune.reset([nw])
-        base = autotune.time_eigh(nw, 3)
+        base = autotune.time_eigh(nw, 3 | autotune.PRECISE_VECTORS)
         t0 = time.perf_counter()
-        entry, _ = autotune.tune_eigh(nw, 3)
+        entry, _ = autotune.tune_eigh(nw, 3 | autotune.PRECISE_VECTORS)
         tune_s = time.perf_counter() - t0
-        tuned = autotune.time_eigh(nw, 3)
+        tuned = autotune.time_eigh(nw, 3 | autotune.PRECISE_VECTORS)
         autotune.reset([nw])
         out[f"nw{nw}"] = {"matrices": autotune.default_batch(nw), "builtin_ms": base, "tuned_ms": tuned,
                           "choice": entry, "tuning_s": tune_s}

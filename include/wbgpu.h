@@ -79,6 +79,8 @@ const char* wbg_status_string(int status);
  *   ph0/ph1/ph2 [nblocks][N_d][nr_d] complex (precision prec): exp(2 pi i R_d (j/N_d + dK_d)),
  *            R_d = rmin_d + r
  *   fields_out [nblocks*nk][nfields][nw][nw] complex (precision prec), k = (j0*N1 + j1)*N2 + j2
+ *   prec 4 (double-float transform stored as complex64): XF, phases and workspace as prec 2,
+ *            fields_out complex64 -- each element rounded once from its double-float value.
  *   prec 3 (FP32 with split inputs): the first contraction also sums the residuals of XF, so
  *            the k-independent R-space data -- whose rounding would be a systematic error of the
  *            whole integral -- enter with 48 bits; phases, intermediates and output as prec 0.
@@ -129,12 +131,20 @@ int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, con
  *         with mode | 32 (WBG_EIGH_STAGE2) and the same nw, nk, base mode and workspace finishes
  *         (eigenvalues, vectors; H is not read and may be NULL).  Lets a caller start
  *         independent work on another stream between the two stages.
+ * mode | 64 (WBG_EIGH_PRECISE_VECTORS), modes 0, 2, 3: the Householder reflectors are kept and
+ *         the back-transform runs in the solve's precision (FP64, double-float), U is rounded to
+ *         complex64 once at the end -- eigenvectors as accurate as complex64 holds them, where the
+ *         FP32 back-transform loses ~sqrt(nw) ulps.
+ * mode | 64 | 128 (WBG_EIGH_DF64_VECTORS), modes 2, 3: as 64 with U kept in double-float complex
+ *         (re.hi, re.lo, im.hi, im.lo floats per element, 16 bytes) for a double-float rotation.
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
  * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
 #define WBG_EIGH_LOWER 4
 #define WBG_EIGH_VALUES 8
 #define WBG_EIGH_STAGE1 16
 #define WBG_EIGH_STAGE2 32
+#define WBG_EIGH_PRECISE_VECTORS 64
+#define WBG_EIGH_DF64_VECTORS 128
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
@@ -161,7 +171,9 @@ int wbg_eigh_batched_noalloc(const void* H, long long strideH, int nw, int nk, d
                              long long strideU, int mode, int* errflag, void* stream);
 
 /* ---- stage 3: U^dagger X U ----------------------------------------------------------------
- * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64) or complex64.
+ * X [nk][nFin][nw][nw] and U (matrix k at U + k*strideU) both complex128 (fp64 = 1), complex64
+ * (fp64 = 0) or double-float complex (fp64 = 2: products in double-float, Xbar rounded to
+ * complex64 -- the mixed path above nw = 32).
  * Xbar [nk][nFrot][nw][nw]: field f = U^dagger X[fsel[f]] U; herm[f] = 1: its Hermitian part;
  * herm[f] = 2: at least the diagonal of the Hermitian part (real) is written -- for fields
  * whose consumers read the diagonal only (rotA in Omega / Morb_Hpm).
@@ -370,7 +382,8 @@ int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, doub
  * calls have no launch shapes) ------------------------------------------------------------------
  * A host-side table, per (parameter, variant, nw), of launch shapes that a tuner measured to be
  * fastest; 0 (the initial value) selects the built-in occupancy heuristic.  Parameters:
- *   WBG_TUNE_EIGH_TRIDIAG_GROUP  matrices per block of the tridiagonalisation   variant: eigh mode & 3
+ *   WBG_TUNE_EIGH_TRIDIAG_GROUP  matrices per block of the tridiagonalisation   variant: eigh mode & 3,
+ *                                4 for modes 2 / 3 with WBG_EIGH_PRECISE_VECTORS
  *   WBG_TUNE_EIGH_QL_BLOCK       matrices (threads) per block of the QL sweep   variant: eigh mode & 3
  *   WBG_TUNE_EIGH_VECTORS_GROUP  matrices per block of the inverse iteration and
  *                                back-transform                                variant: eigh mode & 3

@@ -67,7 +67,7 @@ def models_and_oracle():
     c2 = wsys.System_R.from_dict(models.config_system(2))
     c2.do_ws_dist(9, device='cuda')
     c3 = wsys.System_R.from_dict(models.config_system(3))
-    p2, p3 = _save(c2, ('Ham', 'AA')), _save(c3, ('Ham', 'AA'))
+    p2, p3 = _save(c2, ('Ham', 'AA', 'BB', 'CC')), _save(c3, ('Ham', 'AA'))
     jobs = [('c2_ahc', p2, (1, 1, 1), (12, 12, 12), ['ahc1001']),
             ('c2_morb', p2, (1, 1, 1), (12, 12, 12), ['morb']),
             ('c2_bcd', p2, (1, 1, 1), (12, 12, 12), ['bcd']),

@@ -24,7 +24,7 @@ def _reset_table():
 
 def test_candidates_cover_every_nw():
     for nw in range(1, 129):
-        for variant in range(4):
+        for variant in range(5):
             for p in autotune.EIGH_PARAMS:
                 c = autotune.candidates(p, nw, variant)
                 assert c and c == sorted(c) and all(v & (v - 1) == 0 for v in c), (nw, variant, p)
@@ -51,7 +51,7 @@ def test_set_get_reject():
         assert autotune.get_value(p, nw, variant) == 0
     with pytest.raises(ValueError):
         autotune.set_value(autotune.ROTATE_ENGINE, 16, 0, 1)  # no tensor-core rotation at nw = 16
-    for args in [(-1, 8, 1, 0), (5, 8, 1, 0), (0, 0, 1, 0), (0, 129, 1, 0), (0, 8, 4, 0), (0, 8, 1, -1)]:
+    for args in [(-1, 8, 1, 0), (5, 8, 1, 0), (0, 0, 1, 0), (0, 129, 1, 0), (0, 8, 5, 0), (0, 8, 1, -1)]:
         with pytest.raises(ValueError):
             autotune.set_value(*args)
     autotune.set_value(autotune.EIGH_QL_BLOCK, 8, 1, 64)
@@ -87,8 +87,9 @@ def test_cache_round_trip(tmp_path):
     autotune.save_cache(data, path)
     assert autotune.load_cache(path) == data
     autotune.apply_entry(data['GB300|abi1|nw32|mixed'], 32, 'mixed')
-    assert autotune.get_value(autotune.EIGH_TRIDIAG_GROUP, 32, 3) == 4
-    assert autotune.get_value(autotune.EIGH_QL_BLOCK, 32, 3) == 64
+    v = autotune.eigh_variant(autotune.PRECISION_VARIANTS['mixed'][0])
+    assert autotune.get_value(autotune.EIGH_TRIDIAG_GROUP, 32, v) == 4
+    assert autotune.get_value(autotune.EIGH_QL_BLOCK, 32, v) == 64
     assert autotune.get_value(autotune.ROTATE_ENGINE, 32, 0) == 2
     assert autotune.get_value(autotune.EIGH_TRIDIAG_GROUP, 32, 1) == 0  # FP64 variant untouched
     with open(path, 'w') as f:

@@ -30,7 +30,7 @@ int wbg_r2k_fields(const void* XR, int nBase, const int* iR, int nR, int nw, con
 }
 
 int wbg_r2k_workspace_size(const wbg_r2k_geom* g, int nfields, int nblocks, int prec, size_t* bytes) {
-  if (!g || !bytes || nfields < 1 || nblocks < 1 || prec < 0 || prec > 3) return WBG_STATUS_BAD_ARGUMENT;
+  if (!g || !bytes || nfields < 1 || nblocks < 1 || prec < 0 || prec > 4) return WBG_STATUS_BAD_ARGUMENT;
   *bytes = wbg_r2k_workspace_bytes(g, nfields, nblocks, prec);
   return WBG_STATUS_OK;
 }

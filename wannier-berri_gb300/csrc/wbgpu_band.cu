@@ -10,11 +10,39 @@
 //              cumulative sum over Fermi levels is taken by scan_finalize).
 #include <float.h>
 #include "wbgpu_common.cuh"
+#include "wbgpu_df64.cuh"
 #include "wbgpu_band.cuh"
 #include "wbgpu_tune.cuh"
 #include "wbgpu_spin.cuh"
 
 namespace {
+
+// Real helpers of the rotation kernels in each arithmetic (float, double, double-float).
+template <typename T> WBG_D T rzero() { return T(0); }
+template <> WBG_D df64 rzero<df64>() { return df_from_f(0.0f); }
+template <typename T> WBG_D T rhalf(T x) { return x * T(0.5); }
+template <> WBG_D df64 rhalf<df64>(df64 x) { x.hi *= 0.5f; x.lo *= 0.5f; return x; }  // exact
+template <typename T> WBG_D T rnan() { return T(0) / T(0); }
+template <> WBG_D df64 rnan<df64>() {
+  const float q = __int_as_float(0x7fffffff);
+  df64 r;
+  r.hi = q;
+  r.lo = q;
+  return r;
+}
+// Stored rotation output: the arithmetic's own complex type, or complex64 rounded once from a
+// double-float result (the mixed path above nw = 32)
+template <typename VO, typename V> WBG_D VO rstore(V a) { return a; }
+template <> WBG_D float2 rstore<float2, cdf>(cdf a) { return make_float2(a.x.hi + a.x.lo, a.y.hi + a.y.lo); }
+template <typename V> WBG_D V real_only(V a) { a.y = a.y - a.y; return a; }
+template <> WBG_D cdf real_only<cdf>(cdf a) { a.y = df_from_f(0.0f); return a; }
+// (a + conj(b)) / 2: the (m, n) element of the Hermitian part from Y_mn = a and Y_nm = b
+template <typename V> WBG_D V herm_pair(V a, V b) {
+  V r;
+  r.x = rhalf(a.x + b.x);
+  r.y = rhalf(a.y - b.y);
+  return r;
+}
 
 // Element i = m*nw + n of input field src.  lower: src holds only its lower triangle (m >= n)
 // of a Hermitian matrix; the upper triangle is the conjugate mirror, the diagonal is real.
@@ -24,7 +52,7 @@ WBG_D V load_field(const V* src, int i, int nw, bool lower) {
   const int m = i / nw, n = i % nw;
   V v = src[m >= n ? i : n * nw + m];
   if (m < n) v.y = -v.y;
-  if (m == n) v.y = 0;
+  if (m == n) v = real_only(v);
   return v;
 }
 
@@ -34,10 +62,10 @@ WBG_D V load_field(const V* src, int i, int nw, bool lower) {
 // holds only its lower triangle (wbg_r2k_columns output).
 // grid: nk blocks of 256 threads; shared: U, X, T (nw*nw each, precision T)
 // ---------------------------------------------------------------------------------------
-template <typename T>
+template <typename T, typename VO>
 __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long strideU, const typename C2<T>::t* __restrict__ X,
                               int nFin, const int* __restrict__ fsel, const int* __restrict__ herm, int nFrot,
-                              typename C2<T>::t* __restrict__ Xbar, int nw) {
+                              VO* __restrict__ Xbar, int nw) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smr[];
   V* Us = reinterpret_cast<V*>(smr);
@@ -50,7 +78,7 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
     const int fs = fsel[f];
     const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
     const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw2;
-    const T nan = T(0) / T(0);
+    const T nan = rnan<T>();
     const bool lower = (herm[f] & 4) != 0;
     for (int i = threadIdx.x; i < nw2; i += blockDim.x) Xs[i] = fok ? load_field(src, i, nw, lower) : mkc<T>(nan, nan);
     __syncthreads();
@@ -68,16 +96,15 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
       Xs[i] = acc;
     }
     __syncthreads();
-    V* dst = Xbar + (k * nFrot + f) * (long long)nw2;
+    VO* dst = Xbar + (k * nFrot + f) * (long long)nw2;
     const bool h = (herm[f] & 3) != 0;
     for (int i = threadIdx.x; i < nw2; i += blockDim.x) {
       V y = Xs[i];
       if (h) {
         const int m = i / nw, n = i % nw;
-        const V yt = Xs[n * nw + m];
-        y = mkc<T>((T)0.5 * (y.x + yt.x), (T)0.5 * (y.y - yt.y));
+        y = herm_pair(y, Xs[n * nw + m]);
       }
-      dst[i] = y;
+      dst[i] = rstore<VO>(y);
     }
     __syncthreads();
   }
@@ -86,10 +113,10 @@ __global__ void rotate_kernel(const typename C2<T>::t* __restrict__ U, long long
 // Register-tiled rotation for nw % 4 == 0: each thread owns a 4x4 tile of the nw x nw
 // output; KB k-points per CTA.  X rows are padded (stride nw+1) so the column reads of
 // different tile rows fall in different banks.  Same math as rotate_kernel.
-template <typename T>
+template <typename T, typename VO>
 __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long strideU,
                              const typename C2<T>::t* __restrict__ X, int nFin, const int* __restrict__ fsel,
-                             const int* __restrict__ herm, int nFrot, typename C2<T>::t* __restrict__ Xbar, int nw,
+                             const int* __restrict__ herm, int nFrot, VO* __restrict__ Xbar, int nw,
                              int nk, int KB) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smr[];
@@ -112,7 +139,7 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
     const int fs = fsel[f];
     const bool fok = fs >= 0 && fs < nFin;  // selection lives in device memory: validate here
     const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw2;
-    const T nan = T(0) / T(0);
+    const T nan = rnan<T>();
     const bool lower = (herm[f] & 4) != 0;
     for (int i = tid; i < nw2; i += tpk)
       Xs[(i / nw) * ldx + (i % nw)] = fok ? load_field(src, i, nw, lower) : mkc<T>(nan, nan);
@@ -140,11 +167,11 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
     __syncthreads();
     const int hmode = herm[f] & 3;
     if (hmode == 2) {  // diagonal only: Y_mm = sum_j conj(U_jm) T_jm, Hermitian part = Re
-      V* dstd = Xbar + (k * nFrot + f) * (long long)nw2;
+      VO* dstd = Xbar + (k * nFrot + f) * (long long)nw2;
       for (int m = tid; m < nw; m += tpk) {
         V y = czero<V>();
         for (int j = 0; j < nw; ++j) cfmac(y, Us[j * nw + m], Ts[j * nw + m]);
-        if (valid) dstd[m * nw + m] = mkc<T>(y.x, (T)0);
+        if (valid) dstd[m * nw + m] = rstore<VO>(real_only(y));
       }
       __syncthreads();
       continue;
@@ -169,17 +196,14 @@ __global__ void rotate_tiled(const typename C2<T>::t* __restrict__ U, long long 
 #pragma unroll
       for (int b = 0; b < 4; ++b) Xs[(m0 + a) * ldx + n0 + b] = acc[a][b];
     __syncthreads();
-    V* dst = Xbar + (k * nFrot + f) * (long long)nw2;
+    VO* dst = Xbar + (k * nFrot + f) * (long long)nw2;
     const bool h = hmode != 0;
     if (valid) {
       for (int i = tid; i < nw2; i += tpk) {
         const int m = i / nw, n = i % nw;
         V y = Xs[m * ldx + n];
-        if (h) {
-          const V yt = Xs[n * ldx + m];
-          y = mkc<T>((T)0.5 * (y.x + yt.x), (T)0.5 * (y.y - yt.y));
-        }
-        dst[i] = y;
+        if (h) y = herm_pair(y, Xs[n * ldx + m]);
+        dst[i] = rstore<VO>(y);
       }
     }
     __syncthreads();
@@ -250,19 +274,15 @@ constexpr int PANEL_RP = 32, PANEL_KC = 16;
 template <typename V>
 WBG_D V herm_in(const V* src, int i, int j, int nw, int mode) {  // element (i, j) of the rotated input
   if (mode == 2) return load_field(src, i * nw + j, nw, true);     // lower triangle, mirrored
-  if (mode == 1) {                                                  // Hermitian part
-    const V a = src[i * nw + j], b = src[j * nw + i];
-    V r; r.x = (a.x + b.x) * 0.5f; r.y = (a.y - b.y) * 0.5f;
-    return r;
-  }
+  if (mode == 1) return herm_pair(src[i * nw + j], src[j * nw + i]);  // Hermitian part
   return src[i * nw + j];
 }
 
-template <typename T>
+template <typename T, typename VO>
 __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __restrict__ U, long long strideU,
                                                     const typename C2<T>::t* __restrict__ X, int nFin,
                                                     const int* __restrict__ fsel, const int* __restrict__ herm,
-                                                    int nFrot, typename C2<T>::t* __restrict__ Xbar, int nw, int nk) {
+                                                    int nFrot, VO* __restrict__ Xbar, int nw, int nk) {
   typedef typename C2<T>::t V;
   extern __shared__ unsigned char smp[];
   const int np = (nw + PANEL_RP - 1) / PANEL_RP;
@@ -282,7 +302,7 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
   const int inmode = (hm & 4) ? 2 : ((hm & 3) != 0 ? 1 : 0);
   const V* src = X + (k * nFin + (fok ? fs : 0)) * (long long)nw * nw;
   const V* Uk = U + k * strideU;
-  const T nan = T(0) / T(0);
+  const T nan = rnan<T>();
   V acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
@@ -343,7 +363,7 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
     }
     __syncthreads();
   }
-  V* dst = Xbar + (k * nFrot + f) * (long long)nw * nw;
+  VO* dst = Xbar + (k * nFrot + f) * (long long)nw * nw;
   // Hermitian part (herm 1): the lower triangle computed by this panel is written together
   // with its conjugate mirror and the diagonal is taken real, so the stored matrix is Hermitian
   // bit for bit (the consumers' pair terms rely on X_ln = conj(X_nl) exactly); the panel's
@@ -355,16 +375,16 @@ __global__ void __launch_bounds__(256) rotate_panel(const typename C2<T>::t* __r
       const int m = r0 + 4 * ty + a, n = 4 * tx + c;
       if (m >= nw || n >= nw) continue;
       if ((hm & 3) == 2) {
-        if (m == n) dst[m * nw + n] = mkc<T>(acc[a][c].x, (T)0);
+        if (m == n) dst[m * nw + n] = rstore<VO>(real_only(acc[a][c]));
       } else if ((hm & 3) == 1) {
         if (m == n) {
-          dst[m * nw + n] = mkc<T>(acc[a][c].x, (T)0);
+          dst[m * nw + n] = rstore<VO>(real_only(acc[a][c]));
         } else if (m > n) {
-          dst[m * nw + n] = acc[a][c];
-          dst[n * nw + m] = mkc<T>(acc[a][c].x, -acc[a][c].y);
+          dst[m * nw + n] = rstore<VO>(acc[a][c]);
+          dst[n * nw + m] = rstore<VO>(cconj(acc[a][c]));
         }
       } else {
-        dst[m * nw + n] = acc[a][c];
+        dst[m * nw + n] = rstore<VO>(acc[a][c]);
       }
     }
 }
@@ -1422,7 +1442,7 @@ bool tiled_kpoints_fit(int kb, int tpk, size_t per_k) {
   return kb >= 1 && !(kb & (kb - 1)) && kb * tpk <= 256 && (size_t)kb * per_k <= 200 * 1024;
 }
 
-template <typename T>
+template <typename T, typename VO = typename C2<T>::t>
 int launch_rotate(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                   int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
   typedef typename C2<T>::t V;
@@ -1433,9 +1453,9 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
     const size_t sm = ((size_t)PANEL_RP * (nw + 1) + (size_t)PANEL_KC * nw + PANEL_KC * PANEL_RP) * sizeof(V);
     const long long blocks = (long long)np * nFrot * nk;
     if (sm > 220 * 1024 || blocks > 0x7fffffffll) return WBG_ERR_SIZE;
-    cudaFuncSetAttribute(rotate_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    rotate_panel<T><<<(unsigned)blocks, threads, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm,
-                                                               nFrot, (V*)Xbar, nw, nk);
+    cudaFuncSetAttribute(rotate_panel<T, VO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    rotate_panel<T, VO><<<(unsigned)blocks, threads, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel,
+                                                                   herm, nFrot, (VO*)Xbar, nw, nk);
     return wbg_cuda_status(cudaGetLastError());
   }
   if (nw % 4 == 0 && nw >= 8) {
@@ -1446,9 +1466,9 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
     if (KB * per_k <= 200 * 1024) {
       const int t = wbg_tuned(WBG_TUNE_ROTATE_KPOINTS, sizeof(T) == 8 ? 1 : 0, nw);
       if (t > 0 && tiled_kpoints_fit(t, tpk, per_k)) KB = t;
-      cudaFuncSetAttribute(rotate_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-      rotate_tiled<T><<<(nk + KB - 1) / KB, KB * tpk, KB * per_k, stream>>>((const V*)U, strideU, (const V*)X, nFin,
-                                                                           fsel, herm, nFrot, (V*)Xbar, nw, nk, KB);
+      cudaFuncSetAttribute(rotate_tiled<T, VO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      rotate_tiled<T, VO><<<(nk + KB - 1) / KB, KB * tpk, KB * per_k, stream>>>(
+          (const V*)U, strideU, (const V*)X, nFin, fsel, herm, nFrot, (VO*)Xbar, nw, nk, KB);
       return wbg_cuda_status(cudaGetLastError());
     }
   }
@@ -1456,8 +1476,9 @@ int launch_rotate(const void* U, long long strideU, const void* X, int nFin, con
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   // rotate_kernel writes every element (treats herm == 2 like 1): the full Hermitian part is a
   // valid superset of the diagonal-only request
-  cudaFuncSetAttribute(rotate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  rotate_kernel<T><<<nk, 256, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm, nFrot, (V*)Xbar, nw);
+  cudaFuncSetAttribute(rotate_kernel<T, VO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  rotate_kernel<T, VO><<<nk, 256, sm, stream>>>((const V*)U, strideU, (const V*)X, nFin, fsel, herm, nFrot, (VO*)Xbar,
+                                                nw);
   return wbg_cuda_status(cudaGetLastError());
 }
 
@@ -1471,6 +1492,9 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
   if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0 &&
       wbg_tuned(WBG_TUNE_ROTATE_ENGINE, fp64 ? 1 : 0, nw) != 2)
     return wbg_rotate_tc_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
+  if (fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
+  if (fp64 == 2)  // double-float U and X, products in double-float, Xbar rounded to complex64
+    return launch_rotate<df64, float2>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   if (fp64) return launch_rotate<double>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
   return launch_rotate<float>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
 }

@@ -69,9 +69,19 @@ template <> WBG_D double to_tu<double>(double x) { return x; }
 template <> WBG_D float to_tu<float>(double x) { return (float)x; }
 template <typename TU> WBG_D TU to_tu(df64 x);
 template <> WBG_D float to_tu<float>(df64 x) { return x.hi + x.lo; }
+template <> WBG_D df64 to_tu<df64>(df64 x) { return x; }
 template <typename TU, typename CR> WBG_D typename C2<TU>::t to_tu_c(CR a) {
-  return mkc<TU>(to_tu<TU>(a.x), to_tu<TU>(a.y));
+  typename C2<TU>::t r;
+  r.x = to_tu<TU>(a.x);
+  r.y = to_tu<TU>(a.y);
+  return r;
 }
+// the stored eigenvectors: the back-transform type, or FP32 rounded from a more precise one
+template <typename VO, typename VU> WBG_D VO store_u(VU a) { return a; }
+template <> WBG_D float2 store_u<float2, double2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+template <> WBG_D float2 store_u<float2, cdf>(cdf a) { return make_float2(a.x.hi + a.x.lo, a.y.hi + a.y.lo); }
+template <typename V> WBG_D bool cnonzero(V a) { return a.x != 0 || a.y != 0; }
+template <> WBG_D bool cnonzero<cdf>(cdf a) { return a.x.hi != 0.0f || a.y.hi != 0.0f; }
 
 // ---------------------------------------------------------------------------------------
 // 1. Householder tridiagonalisation.  grid: ceil(nk/G) blocks of G*L threads.
@@ -361,11 +371,10 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 template <typename R, typename TU>
 constexpr bool kUOverlaysZ = sizeof(typename C2<TU>::t) == sizeof(R);
 
-template <typename R, typename TU>
+template <typename R, typename TU, typename VO>
 __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const typename C2<TU>::t* __restrict__ tauIn,
                              const R* __restrict__ dIn, const R* __restrict__ eIn, const double* __restrict__ E, int n,
-                             int nk, int L, int G, int CW, typename C2<TU>::t* __restrict__ Uout,
-                             long long strideU) {
+                             int nk, int L, int G, int CW, VO* __restrict__ Uout, long long strideU) {
   typedef typename C2<TU>::t VU;
   typedef Arith<R> A;
   extern __shared__ unsigned char smv[];
@@ -481,11 +490,15 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
   for (int c0 = 0; c0 < n; c0 += CW) {
     const int cw = min(CW, n - c0);
     for (int jj = lane; jj < cw; jj += L)
-      for (int i = 0; i < n; ++i) Us[i * CW + jj] = mkc<TU>(to_tu<TU>(Zs[i * n + c0 + jj]), (TU)0);
+      for (int i = 0; i < n; ++i) {
+        VU z = czero<VU>();
+        z.x = to_tu<TU>(Zs[i * n + c0 + jj]);
+        Us[i * CW + jj] = z;
+      }
     for (int c = n - 2; c >= 0; --c) {
       // every lane passes the same __syncwarp calls: groups sharing a warp have different tau
       const VU tau = tauIn[k * n + c];
-      const bool act = (tau.x != (TU)0 || tau.y != (TU)0);
+      const bool act = cnonzero(tau);
       for (int i = c + 1 + lane; i < n; i += L) vsh[i] = Vh[(k * n + c) * n + i];
       __syncwarp();
       if (act)
@@ -496,8 +509,8 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
           for (int i = c + 1; i < n; ++i) {
             VU u = Us[i * CW + jj];
             const VU vv = vsh[i];
-            u.x -= vv.x * ts.x - vv.y * ts.y;
-            u.y -= vv.x * ts.y + vv.y * ts.x;
+            u.x = u.x - (vv.x * ts.x - vv.y * ts.y);
+            u.y = u.y - (vv.x * ts.y + vv.y * ts.x);
             Us[i * CW + jj] = u;
           }
         }
@@ -506,7 +519,7 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
     if (valid)
       for (int idx = lane; idx < n * cw; idx += L) {
         const int i = idx / cw, jj = idx % cw;
-        Uout[k * strideU + i * n + c0 + jj] = Us[i * CW + jj];
+        Uout[k * strideU + i * n + c0 + jj] = store_u<VO, VU>(Us[i * CW + jj]);
       }
     __syncwarp();
   }
@@ -597,7 +610,7 @@ struct EighShape {
   }
 };
 
-template <typename R, typename TU, typename HIn>
+template <typename R, typename TU, typename HIn, typename VO = typename C2<TU>::t>
 int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU, int lowerIn,
                 int valuesOnly, int stage, int variant, void* workspace, int* errflag, cudaStream_t stream) {
   typedef typename C2<R>::t CR;
@@ -629,9 +642,9 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   const int GV0 = sh.vectors_default();
   if (GV0 == 0) return WBG_ERR_SIZE;
   const int GV = sh.choose(WBG_TUNE_EIGH_VECTORS_GROUP, variant, n, GV0);
-  cudaFuncSetAttribute(eigh_vectors<R, TU>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
-  eigh_vectors<R, TU><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L, GV,
-                                                                        CW, (VU*)U, strideU);
+  cudaFuncSetAttribute(eigh_vectors<R, TU, VO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxBlockSmem);
+  eigh_vectors<R, TU, VO><<<(nk + GV - 1) / GV, GV * L, GV * smV, stream>>>(Vh, tau, d, e, (const double*)E, n, nk, L,
+                                                                            GV, CW, (VO*)U, strideU);
   return wbg_cuda_status(cudaGetLastError());
 }
 
@@ -648,10 +661,35 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   const int stage = (mode & WBG_EIGH_STAGE1) ? 1 : (mode & WBG_EIGH_STAGE2) ? 2 : 0;
   if (n < 1 || n > WBG_EIGH_NMAX || nk < 1 || !E || (!U && !vo) || !errflag) return WBG_ERR_ARG;
   if (!H && stage != 2) return WBG_ERR_ARG;
-  if (mode < 0 || mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES | WBG_EIGH_STAGE1 | WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
+  if (mode < 0 ||
+      mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES | WBG_EIGH_STAGE1 | WBG_EIGH_STAGE2 | WBG_EIGH_PRECISE_VECTORS |
+              WBG_EIGH_DF64_VECTORS))
+    return WBG_ERR_ARG;
+  if ((mode & WBG_EIGH_DF64_VECTORS) && (!(mode & WBG_EIGH_PRECISE_VECTORS) || (mode & 3) < 2)) return WBG_ERR_ARG;
   if ((mode & WBG_EIGH_STAGE1) && (mode & WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
   const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
+  if ((mode & WBG_EIGH_PRECISE_VECTORS) && (mode & 3) != 1) {
+    // back-transform (and its reflectors) in the solve's precision, U rounded to complex64 once,
+    // or kept in double-float (WBG_EIGH_DF64_VECTORS)
+    if ((mode & WBG_EIGH_DF64_VECTORS) && (mode & 3) == 2)
+      return launch_eigh<df64, df64, double2, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 4, workspace,
+                                                    errflag, stream);
+    if ((mode & WBG_EIGH_DF64_VECTORS) && (mode & 3) == 3)
+      return launch_eigh<df64, df64, cdf, cdf>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 4, workspace,
+                                                errflag, stream);
+    switch (mode & 3) {
+      case 0:
+        return launch_eigh<double, double, double2, float2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 1,
+                                                             workspace, errflag, stream);
+      case 2:
+        return launch_eigh<df64, df64, double2, float2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 4,
+                                                         workspace, errflag, stream);
+      default:
+        return launch_eigh<df64, df64, cdf, float2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 4, workspace,
+                                                     errflag, stream);
+    }
+  }
   switch (mode & 3) {
     case 1:
       return launch_eigh<double, double, double2>(H, strideH, n, nk, E, U, strideU, lo, vo, stage, 1, workspace,
@@ -670,9 +708,10 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
 
 int wbg_eigh_tune_candidates(int param, int n, int variant, int* values, int capacity) {
   if (n < 1 || n > WBG_EIGH_NMAX) return 0;
-  switch (variant) {  // eigh mode & 3: the (solve, back-transform) types of wbg_eigh_run
+  switch (variant) {  // eigh mode & 3 (4: double-float solve and back-transform): the (solve, back-transform) types
     case 1: return EighShape<double, double>(n).candidates(param, values, capacity);
     case 0: return EighShape<double, float>(n).candidates(param, values, capacity);
+    case 4: return EighShape<df64, df64>(n).candidates(param, values, capacity);
     default: return EighShape<df64, float>(n).candidates(param, values, capacity);
   }
 }

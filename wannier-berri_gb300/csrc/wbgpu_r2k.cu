@@ -141,9 +141,14 @@ WBG_D void pmac<float>(float2& acc, const float4& t, float2 x, float2 xs) {
 // for every output index j < Nj, JB outputs per pass (independent accumulators, the sum over
 // i in order): 4 for FP32, 1 for the 16-byte types, whose accumulators cost occupancy.
 // `in` values of this thread stay in registers.
-template <typename T, int MAXL>
+// Stored element: the transform's own type, or complex64 rounded from double-float (the mixed
+// path's fields transformed in double-float, rounded once).
+template <typename VO, typename V> WBG_D VO store_out(V a) { return a; }
+template <> WBG_D float2 store_out<float2, cdf>(cdf a) { return make_float2(a.x.hi + a.x.lo, a.y.hi + a.y.lo); }
+
+template <typename T, int MAXL, typename VO = typename C2<T>::t>
 WBG_D void contract(const typename C2<T>::t* x, int len, const typename PhaseEntry<T>::type* tabT, const int* ridx,
-                    int Nj, typename C2<T>::t* out, long long out_stride) {
+                    int Nj, VO* out, long long out_stride) {
   typedef typename C2<T>::t V;
   typedef typename PhaseEntry<T>::type E;
   constexpr int JB = std::is_same<T, float>::value ? 4 : 1;
@@ -168,7 +173,7 @@ WBG_D void contract(const typename C2<T>::t* x, int len, const typename PhaseEnt
 #pragma unroll
     for (int q = 0; q < JB; ++q) {
       pdone<T>(a[q]);
-      if (j0 + q < Nj) out[(long long)(j0 + q) * out_stride] = a[q];
+      if (j0 + q < Nj) out[(long long)(j0 + q) * out_stride] = store_out<VO>(a[q]);
     }
   }
 }
@@ -273,11 +278,11 @@ __global__ void __launch_bounds__(kThreads) r2k_stageB(const typename C2<T>::t* 
 
 // ---------------- stage C: contract R0 ----------------
 // grid: (ceil(nF*nw2/kThreads), N1*N2, nb); Y -> out [nb*nk][nF][nw2]
-template <typename T, int MAXL>
+template <typename T, int MAXL, typename VO>
 __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* __restrict__ Y,
                                                        const int* __restrict__ sliceR0,
                                                        const typename C2<T>::t* __restrict__ ph0,
-                                                       typename C2<T>::t* __restrict__ out, R2KGeom g, int nF,
+                                                       VO* __restrict__ out, R2KGeom g, int nF,
                                                        const int* __restrict__ cols, int ncols) {
   typedef typename C2<T>::t V;
   typedef typename PhaseEntry<T>::type E;
@@ -302,11 +307,11 @@ __global__ void __launch_bounds__(kThreads) r2k_stageC(const typename C2<T>::t* 
     }
   }
   const long long kstride = (long long)g.N1 * g.N2 * nF * g.nw2;  // k0 -> k0+1
-  V* o = out + (((long long)blk * g.nk + (long long)k1 * g.N2 + k2) * nF + f) * g.nw2 + mn;
-  contract<T, MAXL>(x, len, tab, ri, g.N0, o, kstride);
+  VO* o = out + (((long long)blk * g.nk + (long long)k1 * g.N2 + k2) * nF + f) * g.nw2 + mn;
+  contract<T, MAXL, VO>(x, len, tab, ri, g.N0, o, kstride);
 }
 
-template <typename T, int MAXL>
+template <typename T, int MAXL, typename VO>
 void launch_stages(const void* XF, const void* XFlo, int nF, const int* pairStart, const int* r2, const int* sliceStart,
                    const int* pairR1, const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z,
                    void* Y, void* out, const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
@@ -327,30 +332,30 @@ void launch_stages(const void* XF, const void* XFlo, int nF, const int* pairStar
   cudaFuncSetAttribute(r2k_stageB<T, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   r2k_stageB<T, MAXL><<<dim3(colBlocks, g.nU * g.N2, nb), kThreads, smB, stream>>>(
       (const V*)Z, sliceStart, pairR1, (const V*)ph1, (V*)Y, g, nF, cols, ncols);
-  cudaFuncSetAttribute(r2k_stageC<T, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-  r2k_stageC<T, MAXL><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, smC, stream>>>(
-      (const V*)Y, sliceR0, (const V*)ph0, (V*)out, g, nF, cols, ncols);
+  cudaFuncSetAttribute(r2k_stageC<T, MAXL, VO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  r2k_stageC<T, MAXL, VO><<<dim3(colBlocks, g.N1 * g.N2, nb), kThreads, smC, stream>>>(
+      (const V*)Y, sliceR0, (const V*)ph0, (VO*)out, g, nF, cols, ncols);
 }
 
-template <typename T>
+template <typename T, typename VO = typename C2<T>::t>
 int launch_r2k(const void* XF, const void* XFlo, int nF, const int* pairStart, const int* r2, const int* sliceStart, const int* pairR1,
                const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* Z, void* Y, void* out,
                const R2KGeom& g, int nb, const int* cols, int ncols, cudaStream_t stream) {
   const int maxlen = max(max(g.maxPairLen, g.maxSliceLen), g.nU);
   if (maxlen <= 8)
-    launch_stages<T, 8>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 8, VO>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= 12)
-    launch_stages<T, 12>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 12, VO>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                           ncols, stream);
   else if (maxlen <= 16)
-    launch_stages<T, 16>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 16, VO>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= 24)
-    launch_stages<T, 24>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
+    launch_stages<T, 24, VO>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g, nb, cols,
                          ncols, stream);
   else if (maxlen <= WBG_R2K_MAXLEN)
-    launch_stages<T, WBG_R2K_MAXLEN>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
+    launch_stages<T, WBG_R2K_MAXLEN, VO>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, g,
                                      nb, cols, ncols, stream);
   else
     return WBG_ERR_SIZE;
@@ -359,8 +364,10 @@ int launch_r2k(const void* XF, const void* XFlo, int nF, const int* pairStart, c
 
 }  // namespace
 
+// prec: 0 FP32, 1 FP64, 2 double-float, 3 FP32 with R-space residuals, 4 double-float transform
+// stored as complex64 (workspace and inputs as prec 2)
 size_t wbg_r2k_workspace_bytes(const R2KGeom* g, int nF, int nb, int prec) {
-  const size_t cs = (prec == 1 || prec == 2) ? 16 : 8;
+  const size_t cs = (prec == 1 || prec == 2 || prec == 4) ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   const size_t y = (size_t)nb * nF * g->nU * g->N1 * g->N2 * g->nw2 * cs;
   return ((z + 255) / 256) * 256 + y;
@@ -389,13 +396,13 @@ int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, con
                 const int* sliceR0, const void* ph0, const void* ph1, const void* ph2, void* workspace,
                 size_t workspace_bytes, void* out, const R2KGeom* g, int nb, int prec, const int* cols, int ncols,
                 cudaStream_t stream) {
-  if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 3) return WBG_ERR_ARG;
+  if (!g || nF <= 0 || nb <= 0 || prec < 0 || prec > 4) return WBG_ERR_ARG;
   if (!cols) ncols = nF * g->nw2;
   if (ncols < 1 || ncols > nF * g->nw2) return WBG_ERR_ARG;
   if (g->nw2 != g->nw * g->nw || g->nk != g->N0 * g->N1 * g->N2) return WBG_ERR_ARG;
   if (g->nU < 1 || g->nP < 1 || g->maxPairLen < 1 || g->maxSliceLen < 1) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_r2k_workspace_bytes(g, nF, nb, prec)) return WBG_ERR_WORKSPACE;
-  const size_t cs = (prec == 1 || prec == 2) ? 16 : 8;
+  const size_t cs = (prec == 1 || prec == 2 || prec == 4) ? 16 : 8;
   const size_t z = (size_t)nb * nF * g->nP * g->N2 * g->nw2 * cs;
   char* Z = (char*)workspace;
   char* Y = Z + ((z + 255) / 256) * 256;
@@ -405,6 +412,9 @@ int wbg_r2k_run(const void* XF, int nF, const int* pairStart, const int* r2, con
   if (prec == 2)
     return launch_r2k<df64>(XF, nullptr, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                             cols, ncols, stream);
+  if (prec == 4)
+    return launch_r2k<df64, float2>(XF, nullptr, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y,
+                                    out, *g, nb, cols, ncols, stream);
   const void* XFlo = prec == 3 ? (const void*)((const float2*)XF + (size_t)nF * g->nR * g->nw2) : nullptr;
   return launch_r2k<float>(XF, XFlo, nF, pairStart, r2, sliceStart, pairR1, sliceR0, ph0, ph1, ph2, Z, Y, out, *g, nb,
                            cols, ncols, stream);

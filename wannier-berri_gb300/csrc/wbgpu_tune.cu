@@ -7,7 +7,7 @@
 #include "wbgpu_tune.cuh"
 
 namespace {
-constexpr int kVariants = 4;
+constexpr int kVariants = 5;
 int g_tune[WBG_TUNE_NPARAM][kVariants][WBG_EIGH_NMAX + 1];  // zero-initialised: heuristics
 
 bool valid_key(int param, int nw, int variant) {

@@ -30,8 +30,18 @@ PARAM_NAMES = {EIGH_TRIDIAG_GROUP: 'eigh_tridiag_group', EIGH_QL_BLOCK: 'eigh_ql
                ROTATE_ENGINE: 'rotate_engine'}
 EIGH_PARAMS = (EIGH_TRIDIAG_GROUP, EIGH_QL_BLOCK, EIGH_VECTORS_GROUP)
 ROTATE_PARAMS = (ROTATE_KPOINTS, ROTATE_ENGINE)
-# eigh mode (variant = mode & 3) and rotation variant (fp64 flag) of each precision of run()
-PRECISION_VARIANTS = {'fp64': (1, 1), 'mixed': (3, 0)}
+# eigh mode and rotation variant (fp64 flag) of each precision of run()
+PRECISE_VECTORS = 64  # wbg_eigh_batched mode bit WBG_EIGH_PRECISE_VECTORS
+PRECISION_VARIANTS = {'fp64': (1, 1), 'mixed': (3 | PRECISE_VECTORS, 0)}
+
+
+def eigh_variant(mode):
+    """The tuning table's eigensolver variant of a wbg_eigh_batched mode: mode & 3, except the
+    double-float solve with its double-float back-transform (4) and the FP64 solve with the FP64
+    back-transform rounded to FP32 (1, the launch shapes of mode 1)."""
+    if mode & PRECISE_VECTORS:
+        return {0: 1, 1: 1, 2: 4, 3: 4}[mode & 3]
+    return mode & 3
 
 
 def candidates(param, nw, variant):
@@ -58,7 +68,7 @@ def reset(nws=range(1, 129)):
     """Every entry of the given num_wann back to the built-in heuristics."""
     for nw in nws:
         for p in EIGH_PARAMS:
-            for v in range(4):
+            for v in range(5):
                 set_value(p, nw, v, 0)
         for p in ROTATE_PARAMS:
             for v in (0, 1):
@@ -113,13 +123,12 @@ def _eigh_runner(nw, mode, nk, seed, device):
     rng = np.random.default_rng(seed)
     A = rng.standard_normal((nk, nw, nw)) + 1j * rng.standard_normal((nk, nw, nw))
     H = 0.5 * (A + np.conj(np.swapaxes(A, 1, 2)))
-    variant = mode & 3
-    if variant == 3:
+    if (mode & 3) == 3:
         Hd = torch.from_numpy(engine._df64_pairs(H)).to(device)
     else:
         Hd = torch.from_numpy(H).to(device)
     E = torch.empty((nk, nw), dtype=torch.float64, device=device)
-    U = torch.empty((nk, nw, nw), dtype=torch.complex128 if variant == 1 else torch.complex64, device=device)
+    U = torch.empty((nk, nw, nw), dtype=torch.complex128 if (mode & 3) == 1 else torch.complex64, device=device)
     flag = torch.zeros(1, dtype=torch.int32, device=device)
     ws = ctypes.c_size_t(0)
     lib = _lib.load()
@@ -141,10 +150,10 @@ def time_eigh(nw, mode, nk=None, reps=5, seed=0, device='cuda'):
 
 
 def tune_eigh(nw, mode, nk=None, reps=3, seed=0, device='cuda'):
-    """Tune the eigensolver's group sizes for (nw, eigh mode & 3) on nk random Hermitian
+    """Tune the eigensolver's group sizes for (nw, eigh_variant(mode)) on nk random Hermitian
     matrices; the table holds the choice afterwards.  Returns ({name: value}, {name: {value: ms}})."""
     import torch
-    variant = mode & 3
+    variant = eigh_variant(mode)
     run = _eigh_runner(nw, mode, default_batch(nw, nk), seed, device)
     params = {p: candidates(p, nw, variant) for p in EIGH_PARAMS}
     params = {p: c for p, c in params.items() if len(c) > 1}
@@ -226,7 +235,7 @@ def apply_entry(entry, nw, precision):
     ids = {v: k for k, v in PARAM_NAMES.items()}
     for name, value in entry.items():
         p = ids[name]
-        set_value(p, nw, (mode & 3) if p in EIGH_PARAMS else rvariant, int(value))
+        set_value(p, nw, eigh_variant(mode) if p in EIGH_PARAMS else rvariant, int(value))
 
 
 def ensure(nw, precision, device='cuda', path=None, retune=False):

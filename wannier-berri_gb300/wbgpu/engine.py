@@ -401,6 +401,24 @@ def column_list(dev, quantities, with_H, lower):
     return dev._cache[key]
 
 
+def split_columns(dev, quantities, with_H, lower, first):
+    """column_list split into (columns of the fields of the quantities in `first`, the rest), for
+    a transform that computes two groups of fields in two precisions into one output array."""
+    key = ('cols_split', tuple(sorted(quantities)), with_H, bool(lower), tuple(sorted(first)))
+    if key not in dev._cache:
+        cols, lower_in = column_list(dev, quantities, with_H, lower)
+        _, index = field_plan(quantities, with_H, extra_keys_for(quantities))
+        nw2 = dev.nw * dev.nw
+        f = cols.cpu().numpy() // nw2
+        sel = np.zeros(len(lower_in), dtype=bool)
+        for q in first:
+            if q in index:
+                sel[index[q]:index[q] + QUANTITIES[q]['ncomp']] = True
+        c = cols.cpu().numpy()
+        dev._cache[key] = (torch.tensor(c[sel[f]], device=dev.device), torch.tensor(c[~sel[f]], device=dev.device))
+    return dev._cache[key]
+
+
 def extra_keys_for(quantities):
     keys = []
     if quantities & {'A', 'dA', 'O', 'Od', 'dO'}:
@@ -463,13 +481,36 @@ def r2k_geometry(dev, NKFFT):
                         maxPairLen=g.maxPairLen, maxSliceLen=g.maxSliceLen)
 
 
-PREC_FP32, PREC_FP64, PREC_DF64, PREC_FP32S = 0, 1, 2, 3
+PREC_FP32, PREC_FP64, PREC_DF64, PREC_FP32S, PREC_DF64C = 0, 1, 2, 3, 4
 # PREC_FP32S: FP32 transform whose k-independent R-space inputs carry a rounding residual
 # (hi + lo pair), so they enter with 48 bits; output, intermediates and phases as PREC_FP32.
-C64_PRECS = (PREC_FP32, PREC_FP32S)
+# PREC_DF64C: double-float transform (inputs, phases and intermediates as PREC_DF64) whose
+# output is rounded once to complex64.
+C64_PRECS = (PREC_FP32, PREC_FP32S, PREC_DF64C)
+DF64_PRECS = (PREC_DF64, PREC_DF64C)
+
+
+def _input_prec(prec):
+    """Precision of the R-space arrays and phase tables a transform of precision `prec` reads."""
+    return PREC_DF64 if prec == PREC_DF64C else prec
 EIGH_LOWER = 4  # wbg_eigh_batched mode bit: H given by its lower triangle
 EIGH_VALUES = 8  # wbg_eigh_batched mode bit: eigenvalues only
 EIGH_STAGE1, EIGH_STAGE2 = 16, 32  # wbg_eigh_batched mode bits: tridiagonalise / finish
+EIGH_PRECISE_VECTORS = 64  # wbg_eigh_batched mode bit: back-transform in the solve's precision
+EIGH_DF64_VECTORS = 128  # with EIGH_PRECISE_VECTORS: U kept in double-float complex
+# Above this num_wann the mixed path rotates in double-float (U, fields and products, Xbar rounded
+# to complex64): the FP32 rotation, fields and U errors grow with nw (AHC at nw = 96: 4.5e-6,
+# 6.4e-6, 9.5e-6 each against the oracle), the rotation is O(nw^3) and the tensor-core kernel
+# serves nw = 32 only.
+MIXED_FP32_ROTATION_MAX_NW = 32
+# Eigenvectors of the mixed path: back-transformed in double-float and rounded to complex64 once.
+# The FP32 back-transform loses ~sqrt(nw) ulps in U, which dominated the mixed path's error
+# against the oracle (AHC at nw = 32: 6.6e-7 of the 8.1e-7 total; nw = 96: 9.5e-6).
+MIXED_EIGH_BITS = EIGH_PRECISE_VECTORS
+# Transform precision of the mixed path's other k-space fields (lower triangles), and the
+# quantities whose fields are transformed in double-float (rounded to complex64) whatever it is.
+MIXED_FIELDS_PREC = 3  # PREC_FP32S
+MIXED_DF64_QUANTITIES = set()
 
 
 def _prec(p):
@@ -499,7 +540,7 @@ def _complex_tensor(shape, prec, device):
 def field_arrays(dev, quantities, with_H, prec):
     """R-space arrays XF[f][R][mn] of the requested k-space fields (wbg_r2k_fields), cached on
     the device system: the derivative / curl weights depend on the system only, not on dK."""
-    prec = _prec(prec)
+    prec = _input_prec(_prec(prec))
     keys = extra_keys_for(quantities)
     desc, index = field_plan(quantities, with_H, keys)
     ck = ('XF', tuple(sorted(quantities)), with_H, prec)
@@ -521,7 +562,7 @@ def field_arrays(dev, quantities, with_H, prec):
 
 
 def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, phases=None, block_start=0,
-        lower=False):
+        lower=False, cols=None):
     """Run the R->k stage for a batch of blocks; returns (fields, index, nF, keep-alive).
     prec: False/True (FP32/FP64) or PREC_DF64 (double-float, complex128-sized slots).
     phases: optional device tables from DeviceSystem.grid_phases (then block_start indexes them).
@@ -549,19 +590,21 @@ def r2k(dev, dKs, NKFFT, quantities, with_H, prec, out=None, workspace=None, pha
             ph += [sub, sub]
     else:
         for p in dev.geom.phases(dKs, NKFFT):  # page-locked staging so the upload does not stall the host
-            if prec == PREC_DF64:
+            if prec in DF64_PRECS:
                 host = torch.from_numpy(_df64_pairs(p)).pin_memory()
             else:
                 host = torch.from_numpy(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64)).pin_memory()
             ph.append(host.to(dev.device, non_blocking=True))
             ph.append(host)  # keep the staging buffer alive until the copy has run
     gt = dev.geom_tensors()
-    name = {PREC_FP32: 'r2k_fp32', PREC_FP32S: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64'}[prec]
+    name = {PREC_FP32: 'r2k_fp32', PREC_FP32S: 'r2k_fp32', PREC_FP64: 'r2k_fp64', PREC_DF64: 'r2k_df64',
+            PREC_DF64C: 'r2k_df64c'}[prec]
     common = (_ptr(gt['pair_start']), _ptr(gt['r2']), _ptr(gt['slice_start']), _ptr(gt['pair_r1']),
               _ptr(gt['slice_r0']), _ptr(ph[0]), _ptr(ph[2]), _ptr(ph[4]), nb, prec, _ptr(workspace),
               ctypes.c_size_t(workspace.numel()), _ptr(out), ctypes.byref(geo), _stream())
-    if lower:
-        cols, _ = column_list(dev, quantities, with_H, True)
+    if lower or cols is not None:
+        if cols is None:
+            cols, _ = column_list(dev, quantities, with_H, True)
         st = _timed(name, lib.wbg_r2k_columns, _ptr(XF), nF, _ptr(cols), cols.numel(), *common)
         _lib.check(st, "wbg_r2k_columns")
     else:
@@ -595,9 +638,11 @@ def eigh(Hfields, strideH, nw, nk, E=None, U=None, mode=1, work=None, flag=None)
 
 
 def rotate(U, fields, nFin, sel, herm, nw, nk, fp64, out=None):
+    """wbg_rotate: fp64 1 (complex128), 0 (complex64) or 2 (double-float U and fields stored in
+    complex128-sized slots, products in double-float, output complex64)."""
     lib = _lib.load()
     dev = U.device
-    cdt = torch.complex128 if fp64 else torch.complex64
+    cdt = torch.complex128 if fp64 == 1 else torch.complex64
     if out is None:
         out = torch.empty((nk, len(sel), nw, nw), dtype=cdt, device=dev)
     key = (tuple(sel), tuple(herm), str(dev))
@@ -628,12 +673,12 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
     nb = len(dKs)
     nkt = nb * nk
     keep = []
-    ph = (lambda p: None if phases is None else phases.get(p))
+    ph = (lambda p: None if phases is None else phases.get(_input_prec(p)))
     arena = ws if ws is not None else dev
     flag = arena.buffer('flag', (1,), torch.int32)
     flag.zero_()
 
-    def fields_for(q, with_H, prec, name, lower=False, wsname='r2k_ws'):
+    def fields_for(q, with_H, prec, name, lower=False, wsname='r2k_ws', cols=None):
         _, _, nF, _ = field_arrays(dev, q, with_H, prec)
         out = arena.buffer(name, (nkt, nF, nw, nw), torch.complex64 if prec in C64_PRECS else torch.complex128)
         geo = r2k_geometry(dev, NKFFT)
@@ -642,7 +687,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
                    "wbg_r2k_workspace_size")
         work = arena.buffer(wsname, (int(wsz.value),), torch.uint8)
         return r2k(dev, dKs, NKFFT, q, with_H, prec, out=out, workspace=work, phases=ph(prec),
-                   block_start=block_start, lower=lower)
+                   block_start=block_start, lower=lower, cols=cols)
 
     E = arena.buffer('E', (nkt, nw), torch.float64)
     ews = ctypes.c_size_t(0)
@@ -659,8 +704,13 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         lowerH = 'Ham' in dev.hermitian_bases()  # else the eigensolver symmetrises the full H(k)
         Hf, _, _, k0 = fields_for(set(), True, PREC_DF64, 'fields_H', lower=lowerH)
         keep.append(k0)
-        U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
-        mode = 3 | (EIGH_LOWER if lowerH else 0)
+        wide = nw > MIXED_FP32_ROTATION_MAX_NW and bool(quantities)
+        if wide:  # double-float vectors, fields and rotation; Xbar rounded to complex64 once
+            U = arena.buffer('Udf', (nkt, nw, nw), torch.complex128)
+            mode = 3 | (EIGH_LOWER if lowerH else 0) | EIGH_PRECISE_VECTORS | EIGH_DF64_VECTORS
+        else:
+            U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
+            mode = 3 | (EIGH_LOWER if lowerH else 0) | MIXED_EIGH_BITS
         if quantities:
             # the FP32 fields do not depend on the eigensolver: their transform runs on a side
             # stream next to the QL iteration (a few warps per SM, latency-bound), started once
@@ -669,20 +719,36 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
             # right away (after the main stream's upload of H, which they also read).
             main = torch.cuda.current_stream()
             side = arena.side_stream()
-            ck = ('XF', tuple(sorted(quantities)), False, PREC_FP32S)
-            if ck not in dev._cache:
+            fprec = PREC_DF64 if wide else MIXED_FIELDS_PREC
+            need = {_input_prec(fprec)}
+            if not wide and MIXED_DF64_QUANTITIES & set(quantities):
+                need.add(PREC_DF64)
+            if any(('XF', tuple(sorted(quantities)), False, p) not in dev._cache for p in need):
                 h_ready = torch.cuda.Event()
                 h_ready.record(main)
                 with torch.cuda.stream(side):
                     side.wait_event(h_ready)
-                    field_arrays(dev, quantities, False, PREC_FP32S)
+                    for p in need:
+                        field_arrays(dev, quantities, False, p)
             eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode | EIGH_STAGE1, work=ework, flag=flag)
             tridiag_done = torch.cuda.Event()
             tridiag_done.record(main)
             with torch.cuda.stream(side):
                 side.wait_event(tridiag_done)
-                fields, index, nF, k1 = fields_for(quantities, False, PREC_FP32S, 'fields', lower=True,
-                                                   wsname='r2k_ws_fields')
+                dfq = MIXED_DF64_QUANTITIES & set(quantities) if not wide else set()
+                if dfq and fprec != PREC_DF64C:
+                    # the fields of dfq in double-float (rounded to complex64), the rest in fprec,
+                    # into one array: two column lists over the same field layout
+                    cdf, crest = split_columns(dev, quantities, False, True, dfq)
+                    fields, index, nF, k1 = fields_for(quantities, False, PREC_DF64C, 'fields', cols=cdf,
+                                                       wsname='r2k_ws_fields')
+                    if crest.numel():
+                        _, _, _, k1b = fields_for(quantities, False, fprec, 'fields', cols=crest,
+                                                  wsname='r2k_ws_fields2')
+                        keep.append(k1b)
+                else:
+                    fields, index, nF, k1 = fields_for(quantities, False, fprec, 'fields', lower=True,
+                                                       wsname='r2k_ws_fields')
             E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode | EIGH_STAGE2, work=ework, flag=flag)
             main.wait_stream(side)
             keep.append(k1)
@@ -691,6 +757,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
             E, U, flag = eigh(Hf, nw * nw, nw, nkt, E=E, U=U, mode=mode, work=ework, flag=flag)
             fields, index, nF, lower_in = None, {}, 0, []
         fp64_fields = False
+        rot_prec = 2 if wide else 0
     else:
         raise ValueError(f"unknown precision mode {precision!r}")
     sel, herm, bindex = [], [], {}
@@ -706,7 +773,7 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
         herm = [(h or 1) | 4 if lower_in[f] else h for f, h in zip(sel, herm)]
     if sel:
         Xb = arena.buffer('Xbar', (nkt, len(sel), nw, nw), torch.complex128 if fp64_fields else torch.complex64)
-        Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nkt, fp64_fields, out=Xb)
+        Xbar, k2 = rotate(U, fields, nF, sel, herm, nw, nkt, 1 if fp64_fields else rot_prec, out=Xb)
         keep.append(k2)
     else:
         Xbar = None
@@ -731,11 +798,19 @@ class _GraphEntry:
         self.replays = 0
 
 
+def phase_precs(precision):
+    """Phase-table precisions band_data reads for `precision` (the grid tables a run precomputes)."""
+    if precision == 'fp64':
+        return [PREC_FP64]
+    return sorted({PREC_DF64, _input_prec(MIXED_FIELDS_PREC)})
+
+
 def _graph_precs(quantities, precision):
     """Phase-table precisions that band_data reads for `precision`."""
     if precision == 'fp64':
         return [PREC_FP64]
-    return [PREC_DF64, PREC_FP32S] if quantities else [PREC_DF64]
+    fp = _input_prec(MIXED_FIELDS_PREC)
+    return sorted({PREC_DF64, fp}) if quantities else [PREC_DF64]
 
 
 def _fill_phase_inputs(dev, tabs, dKs, NKFFT, phases, block_start):

@@ -180,7 +180,7 @@ def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, devi
     tetra = None
     if any(getattr(c, 'tetra', False) for c in calculators.values()):
         tetra = engine.TetraCorners(dev, grid, block_ids, precision)
-    precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
+    precs = engine.phase_precs(precision)
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
     flags = []
     for i0 in range(0, len(shifts), nb):

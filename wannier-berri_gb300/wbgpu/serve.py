@@ -227,7 +227,7 @@ class Server:
         req.ws = engine.Workspace(self.device)
         blocks = self._blocks_of(req)
         shifts = req.grid.block_shifts()
-        precs = [engine.PREC_FP64] if self.precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
+        precs = engine.phase_precs(self.precision)
         # cached, k-independent data (R-space fields, phase tables) are built on the preparation
         # stream; the request's stream waits for them once
         with torch.cuda.stream(self._prep_stream):
@@ -237,7 +237,7 @@ class Server:
             else:
                 engine.field_arrays(dev, set(), True, engine.PREC_DF64)
                 if quantities:  # energies-only requests (DOS-type) need no band-basis fields
-                    engine.field_arrays(dev, quantities, False, engine.PREC_FP32S)
+                    engine.field_arrays(dev, quantities, False, engine.MIXED_FIELDS_PREC)
             ready = torch.cuda.Event()
             ready.record(self._prep_stream)
         req.stream.wait_event(ready)

@@ -100,7 +100,7 @@ def tabulate(system, grid, quantities=('energy', 'berry_curvature'), ibands=None
     nk = grid.nk_per_block
     from .run import choose_batch
     nb = choose_batch(dev.nw, nk, len(shifts), _band_quantities(system, quantities), precision)
-    precs = [engine.PREC_FP64] if precision == 'fp64' else [engine.PREC_DF64, engine.PREC_FP32S]
+    precs = engine.phase_precs(precision)
     phases = {p: dev.grid_phases(shifts, grid.FFT, p) for p in precs}
     parts = {q: [] for q in quantities}
     for i0 in range(0, len(shifts), nb):
