@@ -202,7 +202,8 @@ int wbg_device_flags(unsigned int* flags, int clear);
  *   NLDrude_Fermider2 of calculators/static.py:545-556), 27, (a, b, c) at 9 a + 3 b + c.
  * WBG_FORMULA_SPIN_OMEGA (the static spin Hall conductivity) goes through wbg_berry_shc (below).
  * sea != 0: Fermi-sea weights (fder 0), sea == 0: Fermi-surface groups only (fder >= 1; the
- * caller takes the finite differences over the extended levels).  hist [nEF][ncomp] (double)
+ * caller takes the finite differences over the extended levels).  hist [nEF][ncomp] (fixed point, see
+ * "Histograms" below)
  * is accumulated; component (b, d) at 3 b + d.  Xbar may be NULL for WBG_FORMULA_IDENTITY. */
 #define WBG_FORMULA_IDENTITY 0
 #define WBG_FORMULA_INVMASS 1
@@ -211,7 +212,7 @@ int wbg_device_flags(unsigned int* flags, int clear);
 #define WBG_FORMULA_VELVELVEL 7
 #define WBG_FORMULA_SPIN_OMEGA 8
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
-                   int formula, int sea, double* hist, int fp64, void* stream);
+                   int formula, int sea, void* hist, int fp64, void* stream);
 
 /* ---- tetrahedron method (calculators/static.py:80-125 with tetra=True; grid/tetrahedron.py:
  * 15-281 TetraWeightsParal; corner energies data_K/data_K_R.py:121-141) ---------------------
@@ -269,7 +270,7 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
  * weight; der 1 from the product rule on the piecewise form, free of the cubic's cancellation). */
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
-                         int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64, double* hist,
+                         int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64, void* hist,
                          void* stream);
 
 /* ---- tabulation (calculators/tabulate.py:21-52 Tabulator with Energy, Velocity,
@@ -281,14 +282,23 @@ int wbg_berry_tabulate(const double* E, const void* Xbar, int nFbar, int iV, int
                        double degen_thresh, int internal_terms, int external_terms, double* tab, int fp64,
                        void* stream);
 
+/* ---- Histograms (every formula kernel, the tetrahedron accumulation, wbg_kubo / wbg_dynamic) ----
+ * A histogram of n entries is 2 n + 1 64-bit words, zeroed by the caller and accumulated (never
+ * cleared) by the kernels: entry i is the 128-bit two's-complement integer sum of floor(v 2^60)
+ * over its contributions v, low word at [2 i], high word at [2 i + 1]; word [2 n] counts
+ * contributions that were not finite (the readers then return NaN throughout).  Integer sums
+ * commute, so a histogram holds the same bits whatever the order of the atomic adds -- over
+ * threads, blocks, launches and concurrent requests.  Resolution 2^-60 absolute, range 2^67.
+ * Value of an entry: hi 2^4 + ((lo >> 32) 2^-28 + (lo mod 2^32) 2^-60) (wbg_scan_finalize). */
+
 /* ---- stage 4: Berry curvature traces + Fermi-level histogram ----------------------------
  * Xbar [nk][nFbar][nw][nw]: velocity dH/dk at iV..iV+2, A at iA..iA+2, rotA at iO..iO+2.
- * hist [scan.nEF][3] (double) is accumulated (not cleared).
+ * hist [scan.nEF][3] (fixed point, see "Histograms") is accumulated.
  * fp64: 1 complex128 Xbar; 0 complex64; 2 complex64 whose V and A are exactly Hermitian
  * (the mixed path's rotation output) -- then the (l, n) elements are taken as conj(X_nl) and
  * every load is a coalesced row segment (nw <= 32). */
 int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
-                    const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                    const wbg_scan* scan, int internal_terms, int external_terms, void* hist, int fp64,
                     void* stream);
 
 /* Orbital moment, Morb_Hpm = Morb_H + E_av Omega (formula/covariant.py:375-449), the non-additive
@@ -298,7 +308,7 @@ int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA
  * hist [scan.nEF][3] is accumulated.  The Morb calculator combines it with a wbg_berry_omega
  * histogram: M(E_F) = [cumsum(hist_Hpm) - 2 E_F cumsum(hist_Omega)] * factor / nk. */
 int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
-                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, void* hist, int fp64,
                    void* stream);
 
 /* Berry-curvature dipole, DerOmega (formula/covariant.py:212-259) with DerDcov
@@ -309,12 +319,13 @@ int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA,
  * hist [scan.nEF][3][3] ([c][d], before the calculator's swap of the last two axes). */
 int wbg_berry_deromega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
                        int idO, int nw, int nk, const wbg_scan* scan, int internal_terms, int external_terms,
-                       double* hist, int fp64, void* stream);
+                       void* hist, int fp64, void* stream);
 
 /* Kubo optical conductivity (calculators/dynamic.py:71-114,170-196).
  * Groups over all bands (degen_thresh); for every ordered pair of groups not pruned by
- * `nonzero`, f_w(E1,E2) f_E(E1,E2) M^{ab} is added to out[iEF][iw][a][b] (complex128,
- * accumulated, not normalised: the calculator multiplies by factor_opt / (nk * V)).
+ * `nonzero`, f_w(E1,E2) f_E(E1,E2) M^{ab} is added to out[iEF][iw][a][b] (complex: real and
+ * imaginary part each a fixed-point entry of "Histograms", 2 * nEF*nOmega*9 entries; accumulated,
+ * not normalised: the calculator multiplies by factor_opt / (nk * V)).
  * efermi [nEF] and omega [nOmega] are device arrays; gaussian != 0 selects the Gaussian
  * smearing of the imaginary part, else Lorentzian.  Xbar: V at iV, A at iA (3 fields each). */
 typedef struct {
@@ -324,13 +335,14 @@ typedef struct {
 int wbg_kubo_workspace_size(int nw, int nk, int nEF, size_t* bytes);
 int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
              const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
-             size_t workspace_bytes, double* out, int fp64, void* stream);
+             size_t workspace_bytes, void* out, int fp64, void* stream);
 
 /* ---- dynamic calculators (calculators/dynamic.py:26-360) -------------------------------------
  * The Kubo pair scan of wbg_kubo for every formula of DynamicCalculator: per k-point, groups
  * over all bands (degen_thresh), each ordered pair (G1, G2) kept by `nonzero` (dynamic.py:65-69;
  * JDOS: E1 < EFmax, E2 > EFmin, omega_min - 5 eta < E1 - E2 < omega_max + 5 eta, :158-162) adds
- * f_w(E1, E2) (FD(E2) - FD(E1)) M^c to out[iEF][iw][c] (complex128, accumulated, unnormalised).
+ * f_w(E1, E2) (FD(E2) - FD(E1)) M^c to out[iEF][iw][c] (complex, as wbg_kubo's: fixed-point real and
+ * imaginary parts, accumulated, unnormalised).
  * formula / M^c (n in G1, m in G2 summed; A = i D + Abar with Abar only when external_terms):
  *   WBG_DYN_OPTCOND    i A^a_nm A^b_mn, c = 3 a + b (OpticalConductivity, :170-196; = wbg_kubo)
  *   WBG_DYN_JDOS       1, one component (JDOS, :133-162)
@@ -364,7 +376,7 @@ int wbg_dynamic_ncomp(int formula);
 int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* bytes);
 int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spec, int nw, int nk,
                 const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
-                size_t workspace_bytes, double* out, int fp64, void* stream);
+                size_t workspace_bytes, void* out, int fp64, void* stream);
 
 /* Static spin Hall conductivity (calculators/static.py:647-660, formula SpinOmega of
  * formula/covariant.py:759-788): the Fermi-sea scan (as wbg_berry_scan with sea != 0) of the
@@ -373,10 +385,12 @@ int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_
  * spin->formula (WBG_DYN_SHC_SIMPLE / QIAO / RYOO) from the fields named in spin (see
  * wbg_dynamic_spec; Abar only with spin->external_terms).  hist [nEF][27] accumulated. */
 int wbg_berry_shc(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spin, int nw, int nk,
-                  const wbg_scan* scan, double* hist, int fp64, void* stream);
+                  const wbg_scan* scan, void* hist, int fp64, void* stream);
 
-/* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] */
-int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream);
+/* cumulative sum over levels times scale: out[i][c] = scale * sum_{j<=i} hist[j][c] (double),
+ * hist in the fixed-point layout of "Histograms"; NaN throughout when it counted a non-finite
+ * contribution */
+int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double* out, void* stream);
 
 /* ---- launch-shape table of the autotuner (no reference counterpart: the reference's numpy
  * calls have no launch shapes) ------------------------------------------------------------------

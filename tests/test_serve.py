@@ -1,8 +1,7 @@
 """Continuous batching on the GPU: every request's result is the same alone (run()) and in the
-mix of concurrent requests on other systems.  Tolerances: 1e-10 relative for the static
-calculators (only the order of the FP64 histogram atomics differs), 1e-6 for the Kubo
-conductivity, whose per-k pair records and per-frequency partial sums are FP32 in an order set by
-atomics (two identical runs differ at that level too)."""
+mix of concurrent requests on other systems -- bit for bit: every per-k-point computation is
+independent of how the blocks are batched, the Kubo pair records are stored in pair order, and
+every histogram and frequency sum is accumulated in order-independent fixed point."""
 import numpy as np
 import pytest
 
@@ -37,8 +36,7 @@ def _requests():
 def _close(a, b):
     for k in b:
         x, y = a[k].data, b[k].data
-        tol = 1e-6 if k == 'opt' else 1e-10
-        assert np.abs(x - y).max() <= tol * max(np.abs(y).max(), 1e-300), (k, np.abs(x - y).max())
+        assert np.array_equal(x, y), (k, np.abs(x - y).max())
 
 
 @pytest.mark.parametrize("precision", ['mixed', 'fp64'])

@@ -77,7 +77,7 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
 
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
-                   int formula, int sea, double* hist, int fp64, void* stream) {
+                   int formula, int sea, void* hist, int fp64, void* stream) {
   return wbg_berry_scan_run(E, Xbar, nFbar, iV, iW, nw, nk, scan, formula, sea, hist, fp64, (cudaStream_t)stream);
 }
 
@@ -103,14 +103,14 @@ int wbg_berry_tabulate(const double* E, const void* Xbar, int nFbar, int iV, int
 }
 
 int wbg_berry_omega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
-                    const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                    const wbg_scan* scan, int internal_terms, int external_terms, void* hist, int fp64,
                     void* stream) {
   return wbg_berry_omega_run(E, Xbar, nFbar, iV, iA, iO, nw, nk, scan, internal_terms, external_terms, hist, fp64,
                              (cudaStream_t)stream);
 }
 
 int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
-                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, double* hist, int fp64,
+                   int nk, const wbg_scan* scan, int internal_terms, int external_terms, void* hist, int fp64,
                    void* stream) {
   return wbg_berry_morb_run(E, Xbar, nFbar, iV, iA, iO, iB, iC, nw, nk, scan, internal_terms, external_terms, hist, fp64,
                             (cudaStream_t)stream);
@@ -118,7 +118,7 @@ int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA,
 
 int wbg_berry_deromega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
                        int idO, int nw, int nk, const wbg_scan* scan, int internal_terms, int external_terms,
-                       double* hist, int fp64, void* stream) {
+                       void* hist, int fp64, void* stream) {
   return wbg_berry_deromega_run(E, Xbar, nFbar, iV, iA, iO, iW, idA, idO, nw, nk, scan, internal_terms, external_terms,
                                 hist, fp64, (cudaStream_t)stream);
 }
@@ -131,13 +131,13 @@ int wbg_kubo_workspace_size(int nw, int nk, int nEF, size_t* bytes) {
 
 int wbg_kubo(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
              const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
-             size_t workspace_bytes, double* out, int fp64, void* stream) {
+             size_t workspace_bytes, void* out, int fp64, void* stream) {
   return wbg_kubo_run(E, Xbar, nFbar, iV, iA, nw, nk, external_terms, params, efermi, omega, workspace,
                       workspace_bytes, out, fp64, (cudaStream_t)stream);
 }
 
 int wbg_berry_shc(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spin, int nw, int nk,
-                  const wbg_scan* scan, double* hist, int fp64, void* stream) {
+                  const wbg_scan* scan, void* hist, int fp64, void* stream) {
   if (!spin) return WBG_STATUS_BAD_ARGUMENT;
   return wbg_berry_scan_run(E, Xbar, nFbar, spin->V, -1, nw, nk, scan, WBG_FORMULA_SPIN_OMEGA, 1, hist, fp64,
                             (cudaStream_t)stream, nullptr, nullptr, spin);
@@ -153,7 +153,7 @@ int wbg_dynamic_workspace_size(int formula, int nw, int nk, int nEF, size_t* byt
 
 int wbg_dynamic(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* spec, int nw, int nk,
                 const wbg_kubo_params* params, const double* efermi, const double* omega, void* workspace,
-                size_t workspace_bytes, double* out, int fp64, void* stream) {
+                size_t workspace_bytes, void* out, int fp64, void* stream) {
   return wbg_dynamic_run(E, Xbar, nFbar, spec, nw, nk, params, efermi, omega, workspace, workspace_bytes, out, fp64,
                          (cudaStream_t)stream);
 }
@@ -201,12 +201,12 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
                          int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64,
-                         double* hist, void* stream) {
+                         void* hist, void* stream) {
   return wbg_tetra_accumulate_run(E, Ecorner, corner_slot, blocks, nblocks, grid, nw, sel, P, ncomp, efermi, nEF, der,
                                   ascending, fp64, hist, (cudaStream_t)stream);
 }
 
-int wbg_scan_finalize(const double* hist, int nEF, int ncomp, double scale, double* out, void* stream) {
+int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double* out, void* stream) {
   return wbg_scan_finalize_run(hist, nEF, ncomp, scale, out, (cudaStream_t)stream);
 }
 

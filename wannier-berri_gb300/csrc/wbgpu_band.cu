@@ -11,6 +11,7 @@
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_df64.cuh"
+#include "wbgpu_fixed.cuh"
 #include "wbgpu_band.cuh"
 #include "wbgpu_tune.cuh"
 #include "wbgpu_spin.cuh"
@@ -445,16 +446,19 @@ WBG_D void emit_band_values(double* P, long long k, int nw, int nc, int lane, in
 template <typename T>
 __global__ void berry_omega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                    int iV, int iA, int iO, int nw, int nk, int L, int G, WbgScan sp, int internal_terms,
-                                   int external_terms, double* __restrict__ hist, double* __restrict__ tab,
+                                   int external_terms, wbg_u64* __restrict__ hist, int shist, double* __restrict__ tab,
                                    BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
-  double* sh = smb;                                   // [nEF][3]
-  double* Es = sh + 3 * sp.nEF;                       // [G][nw]
+  const int nh = 3 * sp.nEF;  // histogram entries [nEF][3]
+  // the block's histogram in shared memory (order-independent fixed point), or, when it does not
+  // fit, the global one directly
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);      // [G][nw]
   double* tv = Es + G * nw;                           // [G][nw][3]
   float* Ehl = reinterpret_cast<float*>(tv + 3 * G * nw);  // [G][2][nw]: double-float energies
   int* start = reinterpret_cast<int*>(Ehl + 2 * G * nw);   // [G][nw]
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  if (shist) fx_zero(sh, nh);
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
@@ -581,15 +585,13 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
         if (bin >= 0 && bin < sp.nEF)
-          for (int g = 0; g < 3; ++g) atomicAdd(&sh[bin * 3 + g], v[g]);
+          for (int g = 0; g < 3; ++g) fx_add_double(sh + 2 * (bin * 3 + g), v[g], sh + 2 * nh);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  if (hist)
-    for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
-      if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (hist && shist) fx_flush(sh, nh, hist);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -612,15 +614,16 @@ __global__ void berry_omega_kernel(const double* __restrict__ E, const typename 
 template <int C>
 __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __restrict__ Xbar, int nFbar, int iV,
                                  int iA, int iO, int nw, int nk, int G, WbgScan sp, int internal_terms,
-                                 int external_terms, double* __restrict__ hist) {
+                                 int external_terms, wbg_u64* __restrict__ hist, int shist) {
   constexpr int NWM = 32 * C;
   extern __shared__ double smb[];
-  double* sh = smb;                                         // [nEF][3]
-  double* Es = sh + 3 * sp.nEF;                             // [G][NWM]
+  const int nh = 3 * sp.nEF;  // histogram entries [nEF][3], fixed point (shared or global)
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);            // [G][NWM]
   double* tv = Es + G * NWM;                                // [G][NWM][3]
   float* Ehl = reinterpret_cast<float*>(tv + 3 * G * NWM);  // [G][2][NWM]
   int* start = reinterpret_cast<int*>(Ehl + 2 * G * NWM);   // [G][NWM]
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  if (shist) fx_zero(sh, nh);
   __syncthreads();
   const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* myE = Es + grp * NWM;
@@ -764,14 +767,13 @@ __global__ void berry_omega_cols(const double* __restrict__ E, const float2* __r
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
         if (bin >= 0 && bin < sp.nEF)
-          for (int g = 0; g < 3; ++g) atomicAdd(&sh[bin * 3 + g], v[g]);
+          for (int g = 0; g < 3; ++g) fx_add_double(sh + 2 * (bin * 3 + g), v[g], sh + 2 * nh);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
-    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (shist) fx_flush(sh, nh, hist);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -827,15 +829,16 @@ __device__ void spin_omega_terms(const KBand<T>& kb, int n, int gs, int ge, doub
 template <typename T, int NCM>
 __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                   int iV, int iW, int nw, int nk, int L, int G, WbgScan sp, int formula, int sea,
-                                  double* __restrict__ hist, BandSel bs, wbg_dynamic_spec fs) {
+                                  wbg_u64* __restrict__ hist, int shist, BandSel bs, wbg_dynamic_spec fs) {
   typedef typename C2<T>::t V;
   const int nc = scan_ncomp(formula);
   extern __shared__ double smb[];
-  double* sh = smb;                                   // [nEF][nc]
-  double* Es = sh + nc * sp.nEF;                      // [G][nw]
+  const int nh = nc * sp.nEF;  // histogram entries [nEF][nc], fixed point (shared or global)
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);      // [G][nw]
   double* tv = Es + G * nw;                           // [G][nw][NCM]
   int* start = reinterpret_cast<int*>(tv + NCM * G * nw);  // [G][nw]
-  for (int i = threadIdx.x; i < nc * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  if (shist) fx_zero(sh, nh);
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
@@ -963,14 +966,13 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
         if (bin >= 0 && bin < sp.nEF)
-          for (int c = 0; c < nc; ++c) atomicAdd(&sh[bin * nc + c], v[c]);
+          for (int c = 0; c < nc; ++c) fx_add_double(sh + 2 * (bin * nc + c), v[c], sh + 2 * nh);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nc * sp.nEF; i += blockDim.x)
-    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (hist && shist) fx_flush(sh, nh, hist);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -989,14 +991,16 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
 template <typename T>
 __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar, int nFbar,
                                   int iV, int iA, int iO, int iB, int iC, int nw, int nk, int L, int G, WbgScan sp,
-                                  int internal_terms, int external_terms, double* __restrict__ hist, BandSel bs) {
+                                  int internal_terms, int external_terms, wbg_u64* __restrict__ hist, int shist,
+                                  BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
-  double* sh = smb;                                      // [nEF][3]
-  double* Es = sh + 3 * sp.nEF;                          // [G][nw]
+  const int nh = 3 * sp.nEF;  // histogram entries [nEF][3], fixed point (shared or global)
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);         // [G][nw]
   double* Tn = Es + G * nw;                              // [G][nw+1][3]
   int* start = reinterpret_cast<int*>(Tn + 3 * G * (nw + 1));  // [G][nw]
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  if (shist) fx_zero(sh, nh);
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
@@ -1132,14 +1136,13 @@ __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
         if (bin >= 0 && bin < sp.nEF)
-          for (int g = 0; g < 3; ++g) atomicAdd(&sh[bin * 3 + g], myT[ge * 3 + g] - myT[gs * 3 + g]);
+          for (int g = 0; g < 3; ++g) fx_add_double(sh + 2 * (bin * 3 + g), myT[ge * 3 + g] - myT[gs * 3 + g], sh + 2 * nh);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 3 * sp.nEF; i += blockDim.x)
-    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (hist && shist) fx_flush(sh, nh, hist);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1162,15 +1165,16 @@ template <typename T>
 __global__ void berry_deromega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar,
                                       int nFbar, int iV, int iA, int iO, int iW, int idA, int idO, int nw, int nk,
                                       int L, int G, int table, WbgScan sp, int internal_terms, int external_terms,
-                                      double* __restrict__ hist, BandSel bs) {
+                                      wbg_u64* __restrict__ hist, int shist, BandSel bs) {
   typedef typename C2<T>::t V;
   extern __shared__ double smb[];
-  double* sh = smb;                                   // [nEF][9]
-  double* Es = sh + 9 * sp.nEF;                       // [G][nw]
+  const int nh = 9 * sp.nEF;  // histogram entries [nEF][9], fixed point (shared or global)
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);      // [G][nw]
   double* tv = Es + G * nw;                           // [G][nw][9]
   T* dinvS = reinterpret_cast<T*>(tv + 9 * G * nw);   // [G][nw][nw] when table != 0
   int* start = reinterpret_cast<int*>(dinvS + (table ? (size_t)G * nw * nw : 0));  // [G][nw]
-  for (int i = threadIdx.x; i < 9 * sp.nEF; i += blockDim.x) sh[i] = 0.0;
+  if (shist) fx_zero(sh, nh);
   __syncthreads();
   const int grp = threadIdx.x / L, lane = threadIdx.x % L;
   double* myE = Es + grp * nw;
@@ -1408,26 +1412,37 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
           else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
         }
         if (bin >= 0 && bin < sp.nEF)
-          for (int i = 0; i < 9; ++i) atomicAdd(&sh[bin * 9 + i], v[i]);
+          for (int i = 0; i < 9; ++i) fx_add_double(sh + 2 * (bin * 9 + i), v[i], sh + 2 * nh);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 9 * sp.nEF; i += blockDim.x)
-    if (sh[i] != 0.0) atomicAdd(&hist[i], sh[i]);
+  if (hist && shist) fx_flush(sh, nh, hist);
 }
 
-// cumulative sum over Fermi levels and normalisation: out[ie][c] = scale * sum_{j<=ie} hist[j][c]
-__global__ void scan_finalize_kernel(const double* __restrict__ hist, int nEF, int ncomp, double scale,
+// cumulative sum over Fermi levels and normalisation: out[ie][c] = scale * sum_{j<=ie} hist[j][c],
+// hist in the fixed-point layout of wbgpu_fixed.cuh; NaN throughout when a contribution was not finite
+__global__ void scan_finalize_kernel(const wbg_u64* __restrict__ hist, int nEF, int ncomp, double scale,
                                      double* __restrict__ out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncomp) return;
+  const bool bad = hist[2 * (size_t)nEF * ncomp] != 0ull;
   double s = 0.0;
   for (int ie = 0; ie < nEF; ++ie) {
-    s += hist[(long long)ie * ncomp + c];
-    out[(long long)ie * ncomp + c] = s * scale;
+    const size_t e = (size_t)ie * ncomp + c;
+    s += fx_value(hist[2 * e], hist[2 * e + 1]);
+    out[e] = bad ? nan("") : s * scale;
   }
+}
+
+// Shared memory of a formula kernel with an nh-entry histogram and `rest` bytes of other
+// per-block data: the fixed-point histogram sits in shared memory when both fit in one block
+// (shist = 1), else the kernel adds into the global histogram directly (shist = 0).
+size_t hist_smem(int nh, size_t rest, int& shist) {
+  const size_t h = fx_words((size_t)nh) * 8;
+  shist = h + rest <= 220 * 1024 ? 1 : 0;
+  return (shist ? h : 0) + rest;
 }
 
 int lanes_for(int n) {
@@ -1519,7 +1534,7 @@ int wbg_rotate_tune_candidates(int param, int nw, int variant, int* values, int 
 }
 
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
-                        const WbgScan* sp_in, int internal_terms, int external_terms, double* hist, int fp64,
+                        const WbgScan* sp_in, int internal_terms, int external_terms, void* hist, int fp64,
                         cudaStream_t stream, double* tab, const signed char* sel, double* P) {
   const BandSel bs{sel, P};
   if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
@@ -1533,24 +1548,26 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (fp64 == 2 && nw <= 128 && !tab && !sel) {  // FP32, exactly Hermitian V and A: column-per-lane kernel
     const int C = (nw + 31) / 32;
     const int G = 4;  // k-points (warps) per block
-    const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * 32 * C * (8 + 24 + 8 + 4);
+    int shist = 0;
+    const size_t sm = hist_smem(3 * sp->nEF, (size_t)G * 32 * C * (8 + 24 + 8 + 4), shist);
     if (sm > 220 * 1024) return WBG_ERR_SIZE;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     long long nblk = (nk + G - 1) / G;
     const long long cap = (long long)sms * 16;
     if (nblk > cap) nblk = cap;
-    void (*kern)(const double*, const float2*, int, int, int, int, int, int, int, WbgScan, int, int, double*) =
+    void (*kern)(const double*, const float2*, int, int, int, int, int, int, int, WbgScan, int, int, wbg_u64*, int) =
         C == 1 ? berry_omega_cols<1> : C == 2 ? berry_omega_cols<2> : C == 3 ? berry_omega_cols<3> : berry_omega_cols<4>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     kern<<<(int)nblk, 32 * G, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, G, *sp, internal_terms,
-                                           external_terms, hist);
+                                           external_terms, (wbg_u64*)hist, shist);
     return wbg_cuda_status(cudaGetLastError());
   }
   if (fp64 == 2) fp64 = 0;  // the general FP32 kernel does not need the symmetry
   const int L = lanes_for(nw);
   const int G = 128 / L;
-  const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * (8 + 24 + 8 + 4);
+  int shist = 0;
+  const size_t sm = hist_smem(3 * sp->nEF, (size_t)G * nw * (8 + 24 + 8 + 4), shist);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -1560,17 +1577,19 @@ int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, in
   if (fp64) {
     cudaFuncSetAttribute(berry_omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                 G, *sp, internal_terms, external_terms, hist, tab, bs);
+                                                                 G, *sp, internal_terms, external_terms, (wbg_u64*)hist, shist, tab,
+                                                                 bs);
   } else {
     cudaFuncSetAttribute(berry_omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_omega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, nw, nk, L,
-                                                                G, *sp, internal_terms, external_terms, hist, tab, bs);
+                                                                G, *sp, internal_terms, external_terms, (wbg_u64*)hist, shist, tab,
+                                                                 bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
 int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk,
-                       const WbgScan* sp_in, int formula, int sea, double* hist, int fp64, cudaStream_t stream,
+                       const WbgScan* sp_in, int formula, int sea, void* hist, int fp64, cudaStream_t stream,
                        const signed char* sel, double* P, const wbg_dynamic_spec* spin) {
   const BandSel bs{sel, P};
   if (nw < 1 || nk < 1 || !sp_in || !E || (!sel) != (!P)) return WBG_ERR_ARG;
@@ -1605,11 +1624,13 @@ int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int
   if (nblk > (long long)sms * 8) nblk = (long long)sms * 8;
 #define WBG_SCAN(TT, NCM)                                                                                          \
   do {                                                                                                             \
-    const size_t sm = (size_t)nc * sp->nEF * 8 + (size_t)G * nw * (8 + 8 * NCM + 4);                               \
+    int shist = 0;                                                                                                 \
+    const size_t sm = hist_smem(nc * sp->nEF, (size_t)G * nw * (8 + 8 * NCM + 4), shist);                         \
     if (sm > 220 * 1024) return WBG_ERR_SIZE;                                                                      \
     cudaFuncSetAttribute(berry_scan_kernel<TT, NCM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);     \
     berry_scan_kernel<TT, NCM><<<(int)nblk, G * L, sm, stream>>>(E, (const typename C2<TT>::t*)Xbar, nFbar, iV, iW, \
-                                                                 nw, nk, L, G, *sp, formula, sea, hist, bs, fs);   \
+                                                                 nw, nk, L, G, *sp, formula, sea, (wbg_u64*)hist,  \
+                                                                 shist, bs, fs);                                   \
   } while (0)
   if (nc == 27) {
     if (fp64) WBG_SCAN(double, 27);
@@ -1623,7 +1644,7 @@ int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int
 }
 
 int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
-                       int nk, const WbgScan* sp_in, int internal_terms, int external_terms, double* hist, int fp64,
+                       int nk, const WbgScan* sp_in, int internal_terms, int external_terms, void* hist, int fp64,
                        cudaStream_t stream, const signed char* sel, double* P) {
   const BandSel bs{sel, P};
   if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
@@ -1638,7 +1659,9 @@ int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int
   const int L = lanes_for(nw);
   if ((nw + L - 1) / L > WBG_BAND_MAXPER) return WBG_ERR_SIZE;
   const int G = 128 / L;
-  const size_t sm = 3 * (size_t)sp->nEF * 8 + (size_t)G * nw * 8 + (size_t)G * (nw + 1) * 24 + (size_t)G * nw * 4;
+  int shist = 0;
+  const size_t sm =
+      hist_smem(3 * sp->nEF, (size_t)G * nw * 8 + (size_t)G * (nw + 1) * 24 + (size_t)G * nw * 4, shist);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -1648,18 +1671,20 @@ int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int
   if (fp64) {
     cudaFuncSetAttribute(berry_morb_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_morb_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iB, iC,
-                                                                nw, nk, L, G, *sp, internal_terms, external_terms, hist, bs);
+                                                                nw, nk, L, G, *sp, internal_terms, external_terms,
+                                                                (wbg_u64*)hist, shist, bs);
   } else {
     cudaFuncSetAttribute(berry_morb_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_morb_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iB, iC, nw,
-                                                               nk, L, G, *sp, internal_terms, external_terms, hist, bs);
+                                                               nk, L, G, *sp, internal_terms, external_terms,
+                                                               (wbg_u64*)hist, shist, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
 int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
                            int idO, int nw, int nk, const WbgScan* sp_in, int internal_terms, int external_terms,
-                           double* hist, int fp64, cudaStream_t stream, const signed char* sel, double* P) {
+                           void* hist, int fp64, cudaStream_t stream, const signed char* sel, double* P) {
   const BandSel bs{sel, P};
   if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
   if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
@@ -1673,13 +1698,23 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
   const int L = lanes_for(nw);
   int G = 64 / L > 0 ? 64 / L : 1;
   const size_t tsz = fp64 ? 8 : 4;
-  auto smem = [&](int g, int table) {
-    return 9 * (size_t)sp->nEF * 8 + (size_t)g * nw * (8 + 72 + 4) + (table ? (size_t)g * nw * nw * tsz : 0);
+  // per-block data besides the histogram: energies, traces, group starts and the 1/dE table
+  auto rest = [&](int g, int table) {
+    return (size_t)g * nw * (8 + 72 + 4) + (table ? (size_t)g * nw * nw * tsz : 0);
   };
+  const size_t hbytes = fx_words((size_t)9 * sp->nEF) * 8;
+  auto smem = [&](int g, int table) { return hbytes + rest(g, table); };
   int table = 1;  // k-point groups per block shrink before the 1/dE table is dropped
   while (G > 1 && smem(G, 1) > 220 * 1024) G /= 2;
   if (smem(G, 1) > 220 * 1024) table = 0;
-  const size_t sm = smem(G, table);
+  int shist = 0;
+  if (smem(G, table) > 220 * 1024) {  // the histogram goes global before anything else gives way
+    G = 64 / L > 0 ? 64 / L : 1;
+    table = 1;
+    while (G > 1 && rest(G, 1) > 220 * 1024) G /= 2;
+    if (rest(G, 1) > 220 * 1024) table = 0;
+  }
+  const size_t sm = hist_smem(9 * sp->nEF, rest(G, table), shist);
   if (sm > 220 * 1024) return WBG_ERR_SIZE;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -1690,18 +1725,18 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
     cudaFuncSetAttribute(berry_deromega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iW,
                                                                     idA, idO, nw, nk, L, G, table, *sp, internal_terms,
-                                                                    external_terms, hist, bs);
+                                                                    external_terms, (wbg_u64*)hist, shist, bs);
   } else {
     cudaFuncSetAttribute(berry_deromega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA,
                                                                    idO, nw, nk, L, G, table, *sp, internal_terms,
-                                                                   external_terms, hist, bs);
+                                                                   external_terms, (wbg_u64*)hist, shist, bs);
   }
   return wbg_cuda_status(cudaGetLastError());
 }
 
-int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream) {
+int wbg_scan_finalize_run(const void* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream) {
   if (nEF < 1 || ncomp < 1 || !hist || !out) return WBG_ERR_ARG;
-  scan_finalize_kernel<<<(ncomp + 31) / 32, 32, 0, stream>>>(hist, nEF, ncomp, scale, out);
+  scan_finalize_kernel<<<(ncomp + 31) / 32, 32, 0, stream>>>((const wbg_u64*)hist, nEF, ncomp, scale, out);
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -15,20 +15,20 @@ int wbg_device_flags_run(unsigned int* flags, int clear);
 int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream);
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,
-                        const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
+                        const WbgScan* sp, int internal_terms, int external_terms, void* hist, int fp64,
                         cudaStream_t stream, double* tab = nullptr, const signed char* sel = nullptr,
                         double* P = nullptr);
 // sel / P (all formula kernels): per-band values for the tetrahedron method instead of the
 // histogram (wbg_band_values); sp then only supplies degen_thresh.
 int wbg_berry_morb_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iB, int iC, int nw,
-                       int nk, const WbgScan* sp, int internal_terms, int external_terms, double* hist, int fp64,
+                       int nk, const WbgScan* sp, int internal_terms, int external_terms, void* hist, int fp64,
                        cudaStream_t stream, const signed char* sel = nullptr, double* P = nullptr);
 int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
                            int idO, int nw, int nk, const WbgScan* sp, int internal_terms, int external_terms,
-                           double* hist, int fp64, cudaStream_t stream, const signed char* sel = nullptr,
+                           void* hist, int fp64, cudaStream_t stream, const signed char* sel = nullptr,
                            double* P = nullptr);
-int wbg_scan_finalize_run(const double* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);
+int wbg_scan_finalize_run(const void* hist, int nEF, int ncomp, double scale, double* out, cudaStream_t stream);
 int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const WbgScan* sp,
-                       int formula, int sea, double* hist, int fp64, cudaStream_t stream,
+                       int formula, int sea, void* hist, int fp64, cudaStream_t stream,
                        const signed char* sel = nullptr, double* P = nullptr,
                        const wbg_dynamic_spec* spin = nullptr);

@@ -25,6 +25,7 @@
 //              precision, FP64 atomics into the result.
 #include <float.h>
 #include "wbgpu_common.cuh"
+#include "wbgpu_fixed.cuh"
 #include "wbgpu_kubo.cuh"
 #include "wbgpu_spin.cuh"
 
@@ -218,23 +219,40 @@ __global__ void kubo_pairs(const double* __restrict__ E, const typename C2<T>::t
   band.nw2 = nw2;
   band.f = fs;
   const double eocc1max = kp.EFmin - 30.0 * kp.kBT, eocc0min = kp.EFmax + 30.0 * kp.kBT;
-  for (int pr = threadIdx.x; pr < ng * ng; pr += blockDim.x) {
-    const int g1 = pr / ng, g2 = pr % ng;
-    if (g1 == g2) continue;  // f_E(E, E) = 0
+  // Records are stored in pair order (slot = number of kept pairs before this one), so the
+  // accumulation over them runs in the same order on every run: a block-wide exclusive count of
+  // the kept pairs per round of blockDim.x pairs (warp ballots, warp totals in shared memory).
+  __shared__ int warp_kept[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
+  for (int base = 0; base < ng * ng; base += blockDim.x) {
+    const int pr = base + threadIdx.x;
+    const int g1 = pr < ng * ng ? pr / ng : 0, g2 = pr < ng * ng ? pr % ng : 0;
+    bool keep = pr < ng * ng && g1 != g2;  // f_E(E, E) = 0
     const double E1 = Eg[g1], E2 = Eg[g2];
-    if (F == WBG_DYN_JDOS) {
-      const double d = E1 - E2;
-      if (!(E1 < kp.EFmax && E2 > kp.EFmin && fs.omega_min - 5 * kp.eta < d && d < fs.omega_max + 5 * kp.eta))
-        continue;
-    } else if ((E1 < eocc1max && E2 < eocc1max) || (E1 > eocc0min && E2 > eocc0min)) {
-      continue;
+    if (keep) {
+      if (F == WBG_DYN_JDOS) {
+        const double d = E1 - E2;
+        keep = E1 < kp.EFmax && E2 > kp.EFmin && fs.omega_min - 5 * kp.eta < d && d < fs.omega_max + 5 * kp.eta;
+      } else {
+        keep = !((E1 < eocc1max && E2 < eocc1max) || (E1 > eocc0min && E2 > eocc0min));
+      }
     }
+    const unsigned ball = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_kept[wid] = __popc(ball);
+    __syncthreads();
+    int before = cnt;
+    for (int w = 0; w < wid; ++w) before += warp_kept[w];
+    const int slot = before + __popc(ball & ((1u << lane) - 1u));
+    int total = 0;
+    for (int w = 0; w < nwarps; ++w) total += warp_kept[w];
+    __syncthreads();
+    if (threadIdx.x == 0) cnt += total;  // read by the next round after its first barrier
+    if (!keep) continue;
     V M[NC];
 #pragma unroll
     for (int i = 0; i < NC; ++i) M[i] = czero<V>();
     for (int n = gstart[g1]; n < gstart[g1 + 1]; ++n)
       for (int m = gstart[g2]; m < gstart[g2 + 1]; ++m) add_element<T, F>(band, n, m, M);
-    const int slot = atomicAdd(&cnt, 1);
     const long long r = k * (long long)P + slot;
     rec_dE[r] = E2 - E1;
     for (int e = 0; e < kp.nEF; ++e)
@@ -278,13 +296,17 @@ __device__ typename C2<R>::t factor_omega(int formula, double dE, double om, R e
   return mkc<R>(v, R(0));
 }
 
-// grid: (ceil(nOmega / TPB), k chunks, level chunks); out [nEF][nOmega][NC] complex128 (accumulated)
+// grid: (ceil(nOmega / TPB), k chunks, level chunks); out: [nEF][nOmega][NC] complex entries, real
+// and imaginary part each a fixed-point entry of wbgpu_fixed.cuh (order-independent sums over the
+// blocks of k-points), then the count of non-finite contributions.  The block's sums of one
+// k-point's pair records are added to `out` after that k-point, so an FP32 accumulation chain
+// spans one k-point's records, not a chunk of k-points.
 // R: precision of the records and the accumulation (float: mixed path, double: FP64 path)
 template <int NC, typename R>
 __global__ void kubo_accum(const double* __restrict__ rec_dE, const R* __restrict__ rec_fE,
                            const typename C2<R>::t* __restrict__ rec_M, const int* __restrict__ count, int P, int nk,
                            int kchunk, const double* __restrict__ omega, WbgKubo kp, int formula, int efc,
-                           double2* __restrict__ out) {
+                           wbg_u64* __restrict__ out) {
   typedef typename C2<R>::t V;
   constexpr int nc = NC;
   extern __shared__ unsigned char smacc[];
@@ -299,6 +321,7 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const R* __restric
   const int fgroup = formula >= WBG_DYN_SHC_SIMPLE && formula <= WBG_DYN_SHC_RYOO ? kShcFactor : formula;
   const long long k0 = (long long)blockIdx.y * kchunk;
   const long long k1 = min((long long)nk, k0 + kchunk);
+  wbg_u64* bad = out + 4 * (long long)kp.nEF * kp.nOmega * nc;
   for (long long k = k0; k < k1; ++k) {
     const int nrec = count[k];
     for (int q = 0; q < nrec; ++q) {
@@ -319,15 +342,16 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const R* __restric
         }
       }
     }
+    if (nrec > 0 && active)
+      for (int e = 0; e < ne; ++e)
+        for (int i = 0; i < nc; ++i) {
+          V& a = acc[(e * nc + i) * blockDim.x + threadIdx.x];
+          wbg_u64* o = out + 4 * (((long long)(e0 + e) * kp.nOmega + w) * nc + i);
+          fx_add_double(o, (double)a.x, bad);
+          fx_add_double(o + 2, (double)a.y, bad);
+          a = czero<V>();
+        }
   }
-  if (!active) return;
-  for (int e = 0; e < ne; ++e)
-    for (int i = 0; i < nc; ++i) {
-      const V a = acc[(e * nc + i) * blockDim.x + threadIdx.x];
-      double2* o = out + ((long long)(e0 + e) * kp.nOmega + w) * nc + i;
-      atomicAdd(&o->x, (double)a.x);
-      atomicAdd(&o->y, (double)a.y);
-    }
 }
 
 template <typename T>
@@ -368,7 +392,7 @@ size_t wbg_dynamic_workspace_bytes(int formula, int nw, int nk, int nEF) {
 
 int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dynamic_spec* fs, int nw, int nk,
                     const WbgKubo* kp, const double* efermi, const double* omega, void* workspace,
-                    size_t workspace_bytes, double* out, int fp64, cudaStream_t stream) {
+                    size_t workspace_bytes, void* out, int fp64, cudaStream_t stream) {
   if (!E || !fs || !kp || !efermi || !omega || !workspace || !out || nw < 1 || nk < 1) return WBG_ERR_ARG;
   const int F = fs->formula;
   const int nc = wbg_dynamic_ncomp_impl(F);
@@ -430,7 +454,7 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
   do {                                                                                                         \
     cudaFuncSetAttribute(kubo_accum<NC, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);           \
     kubo_accum<NC, R><<<grid, tpb, sma, stream>>>(rec_dE, (const R*)rec_fE, (const typename C2<R>::t*)rec_M,   \
-                                                 count, P, nk, kchunk, omega, *kp, F, efc, (double2*)out);     \
+                                                 count, P, nk, kchunk, omega, *kp, F, efc, (wbg_u64*)out);     \
   } while (0)
   if (fp64) {
     if (nc == 1) WBG_ACCUM(1, double);
@@ -451,7 +475,7 @@ size_t wbg_kubo_workspace_bytes(int nw, int nk, int nEF) {
 
 int wbg_kubo_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int nw, int nk, int external_terms,
                  const WbgKubo* kp, const double* efermi, const double* omega, void* workspace,
-                 size_t workspace_bytes, double* out, int fp64, cudaStream_t stream) {
+                 size_t workspace_bytes, void* out, int fp64, cudaStream_t stream) {
   if (!kp || kp->nEF > 64) return WBG_ERR_ARG;
   wbg_dynamic_spec fs = {};
   fs.formula = WBG_DYN_OPTCOND;

@@ -14,6 +14,7 @@
 // block i - 1, index j, or for i = 0 corner block NKdiv - 1, index j - 1 (mod NKFFT: H(k) is
 // periodic in the reduced coordinates).
 #include "wbgpu_common.cuh"
+#include "wbgpu_fixed.cuh"
 #include "wbgpu_tetra.cuh"
 
 namespace {
@@ -319,17 +320,19 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
                                         const int* __restrict__ slot, const int* __restrict__ blocks,
                                         wbg_tetra_grid g, int nw, long long nkt, const signed char* __restrict__ sel,
                                         const double* __restrict__ P, int nc, const double* __restrict__ EF, int nEF,
-                                        int der, int ascending, int smem_hist, double* __restrict__ hist) {
+                                        int der, int ascending, int smem_hist, wbg_u64* __restrict__ hist) {
   extern __shared__ double sm[];
   const int G = blockDim.x / 32, w = threadIdx.x / 32, lane = threadIdx.x % 32;
-  double* acc = smem_hist ? sm : hist;
-  double* win = sm + (smem_hist ? (size_t)nEF * nc : 0) + (size_t)w * kWarpSmem;
+  const int nh = nEF * nc;  // fixed-point histogram entries (wbgpu_fixed.cuh)
+  wbg_u64* acc = smem_hist ? reinterpret_cast<wbg_u64*>(sm) : hist;
+  wbg_u64* bad = acc + 2 * nh;  // count of non-finite contributions
+  double* win = sm + (smem_hist ? fx_words(nh) : 0) + (size_t)w * kWarpSmem;
   float2* winf = reinterpret_cast<float2*>(win);            // F32: compensated window sums
   float2* xs = reinterpret_cast<float2*>(win + kWin * 32);  // F32: E_F - eb per level
   double* ek = win + 2 * kWin * 32;                         // [9][32]: corner s at s * 32 + lane
   float2* ekf = reinterpret_cast<float2*>(ek);              // F32: e - eb as (hi, lo)
   if (smem_hist) {
-    for (int i = threadIdx.x; i < nEF * nc; i += blockDim.x) sm[i] = 0.0;
+    fx_zero(acc, nh);
     __syncthreads();
   }
   const double wend = der == 0 ? 1.0 : 0.0;
@@ -341,8 +344,7 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
       if (s == 2) {  // Fermi sea: weight 1 at every level
         if (der == 0)
           for (int c = 0; c < nc; ++c) {
-            const double v = Pn[c];
-            if (v != 0.0) atomicAdd(&acc[c], v);
+            fx_add_double(acc + 2 * c, Pn[c], bad);
           }
         continue;
       }
@@ -412,17 +414,16 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
           const double d = wi - wprev;
           wprev = wi;
           if (d != 0.0)
-            for (int c = 0; c < nc; ++c) atomicAdd(&acc[(c0 + i) * nc + c], pv[c] * d);
+            for (int c = 0; c < nc; ++c) fx_add_double(acc + 2 * ((c0 + i) * nc + c), pv[c] * d, bad);
         }
       }
       if (i1 < nEF && wend != wprev)
-        for (int c = 0; c < nc; ++c) atomicAdd(&acc[i1 * nc + c], pv[c] * (wend - wprev));
+        for (int c = 0; c < nc; ++c) fx_add_double(acc + 2 * (i1 * nc + c), pv[c] * (wend - wprev), bad);
     }
   }
   if (smem_hist) {
     __syncthreads();
-    for (int i = threadIdx.x; i < nEF * nc; i += blockDim.x)
-      if (sm[i] != 0.0) atomicAdd(&hist[i], sm[i]);
+    fx_flush(acc, nh, hist);
   }
 }
 
@@ -458,7 +459,7 @@ int wbg_tetra_select_run(const double* E, const double* Ec, const int* slot, con
 
 int wbg_tetra_accumulate_run(const double* E, const double* Ec, const int* slot, const int* blocks, int nblocks,
                              const wbg_tetra_grid* g, int nw, const signed char* sel, const double* P, int ncomp,
-                             const double* EF, int nEF, int der, int ascending, int fp64, double* hist,
+                             const double* EF, int nEF, int der, int ascending, int fp64, void* hist,
                              cudaStream_t stream) {
   if (!E || !Ec || !slot || !blocks || !g || !sel || !P || !EF || !hist || nblocks < 1 || nw < 1 || nEF < 1 ||
       !grid_ok(g))
@@ -467,18 +468,18 @@ int wbg_tetra_accumulate_run(const double* E, const double* Ec, const int* slot,
   const long long nkt = (long long)nblocks * g->fft[0] * g->fft[1] * g->fft[2];
   const int G = 4;
   const size_t wsm = (size_t)G * kWarpSmem * 8;
-  const size_t hsm = (size_t)nEF * ncomp * 8;
+  const size_t hsm = fx_words((size_t)nEF * ncomp) * 8;
   const int smem_hist = wsm + hsm <= 200 * 1024;
   const size_t sm = wsm + (smem_hist ? hsm : 0);
   const int nblk = grid_cap(G, nkt, 4);
   if (fp64) {
     cudaFuncSetAttribute(tetra_accumulate_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     tetra_accumulate_kernel<false><<<nblk, 32 * G, sm, stream>>>(E, Ec, slot, blocks, *g, nw, nkt, sel, P, ncomp, EF,
-                                                                 nEF, der, ascending, smem_hist, hist);
+                                                                 nEF, der, ascending, smem_hist, (wbg_u64*)hist);
   } else {
     cudaFuncSetAttribute(tetra_accumulate_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     tetra_accumulate_kernel<true><<<nblk, 32 * G, sm, stream>>>(E, Ec, slot, blocks, *g, nw, nkt, sel, P, ncomp, EF,
-                                                                nEF, der, ascending, smem_hist, hist);
+                                                                nEF, der, ascending, smem_hist, (wbg_u64*)hist);
   }
   return wbg_cuda_status(cudaGetLastError());
 }

@@ -8,5 +8,5 @@ int wbg_tetra_select_run(const double* E, const double* Ec, const int* slot, con
                          signed char* sel, cudaStream_t stream);
 int wbg_tetra_accumulate_run(const double* E, const double* Ec, const int* slot, const int* blocks, int nblocks,
                              const wbg_tetra_grid* g, int nw, const signed char* sel, const double* P, int ncomp,
-                             const double* EF, int nEF, int der, int ascending, int fp64, double* hist,
+                             const double* EF, int nEF, int der, int ascending, int fp64, void* hist,
                              cudaStream_t stream);

@@ -34,6 +34,26 @@ WBG_FORMULA_VELVELVEL, WBG_FORMULA_SPIN_OMEGA = 7, 8
 from .result import EnergyResult
 
 
+def fixed_words(n):
+    """int64 words of an n-entry fixed-point histogram (the layout of csrc/wbgpu_fixed.cuh)."""
+    return 2 * n + 1
+
+
+def fixed_values(words, n):
+    """The n entries of a fixed-point histogram as doubles, rounded exactly as the device does
+    (hi 2^4 + ((lo >> 32) 2^-28 + (lo & 2^32-1) 2^-60)); NaN throughout when a contribution
+    was not finite."""
+    w = np.asarray(words)
+    lo = w[0:2 * n:2].view(np.uint64)
+    hi = w[1:2 * n:2].astype(np.float64)
+    a = (lo & np.uint64(0xffffffff)).astype(np.float64) * 2.0 ** -60
+    b = (lo >> np.uint64(32)).astype(np.float64) * 2.0 ** -28
+    v = hi * 16.0 + (b + a)
+    if w[2 * n] != 0:
+        v[:] = np.nan
+    return v
+
+
 class Calculator:
     def __init__(self, degen_thresh=1e-4, degen_Kramers=False, save_mode="bin+txt", print_comment=False):
         if degen_Kramers:
@@ -76,7 +96,9 @@ class StaticCalculator(Calculator):
         return self.external_terms and not system.force_internal_terms_only
 
     def reset(self, device):
-        self._hist = torch.zeros((self.nEF_extra, self.ncomp), dtype=torch.float64, device=device)
+        # [nEF][ncomp] order-independent fixed-point entries (two int64 words each) and the count
+        # of non-finite contributions: the kernels' sums are the same bits whatever the order
+        self._hist = torch.zeros(fixed_words(self.nEF_extra * self.ncomp), dtype=torch.int64, device=device)
         if self.tetra:
             self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
 
@@ -108,7 +130,7 @@ class StaticCalculator(Calculator):
         """Cumulative scan and normalisation (static.py:127-155) times the K-point factor."""
         cf = self.constant_factor if self.use_factor else np.sign(self.constant_factor)
         scale = cf / (cell_volume * nk) * factor
-        out = torch.empty_like(self._hist)
+        out = torch.empty((self.nEF_extra, self.ncomp), dtype=torch.float64, device=self._hist.device)
         _lib.check(_lib.load().wbg_scan_finalize(_ptr(self._hist), self.nEF_extra, self.ncomp, ctypes.c_double(scale),
                                                  _ptr(out), _stream()), "wbg_scan_finalize")
         return out.cpu().numpy()
@@ -397,8 +419,10 @@ class DynamicCalculator(Calculator):
         return 1 if self.formula == WBG_DYN_JDOS else 9 if self.formula == WBG_DYN_OPTCOND else 27
 
     def reset(self, device):
-        self._out = torch.zeros((len(self.Efermi), len(self.omega), self.ncomp), dtype=torch.complex128,
-                                device=device)
+        # [E_F][omega][ncomp] complex entries, real and imaginary parts each an order-independent
+        # fixed-point entry (csrc/wbgpu_fixed.cuh)
+        self._nout = len(self.Efermi) * len(self.omega) * self.ncomp
+        self._out = torch.zeros(fixed_words(2 * self._nout), dtype=torch.int64, device=device)
         self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
         self._om = torch.tensor(self.omega, dtype=torch.float64, device=device)
 
@@ -441,7 +465,8 @@ class DynamicCalculator(Calculator):
         return data.reshape((len(self.Efermi), len(self.omega)) + (3,) * self.ndim)
 
     def result(self, cell_volume, nk, factor=1.0):
-        data = self.select(self._out.cpu().numpy())
+        v = fixed_values(self._out.cpu().numpy(), 2 * self._nout)
+        data = self.select(v[0::2] + 1j * v[1::2])
         data = data * (self.constant_factor / (nk * cell_volume) * factor)
         return EnergyResult([self.Efermi, self.omega], data.real if self.real else data)
 
