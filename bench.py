@@ -386,7 +386,8 @@ def run_gpu(args):
     counts = timer.counts()
     # every timed step is one batch: kernels per batch of each stage (the mixed path calls the
     # eigensolver in two stages around the side-stream field transform, 3 kernels in all)
-    kernels_per_batch = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'eigh': 3, 'rotate': 1, 'berry_omega': 1}
+    kernels_per_batch = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'r2k_df64c': 3, 'eigh': 3, 'rotate': 1,
+                         'berry_omega': 1}
     gpu_launches = int(args.steps * sum(kernels_per_batch[k] for k in counts))
 
     # plain FP64 drop-in throughput on the same blocks, and the mixed-vs-FP64 error of one step
@@ -461,7 +462,9 @@ def run_gpu(args):
     except (OSError, KeyError, ValueError):
         peaks['hbm'] = 6800.0  # fallback figures of the profiling recipe
         peaks['tf32'] = 1.9e6 / 2.0
-    nF_fields = {'r2k_fp64': 10, 'r2k_df64': 1, 'r2k_fp32': 9}
+    # fields per stage of the AHC step: FP64 path H + 9; mixed path H (double-float), V (double-float
+    # transform rounded to complex64) and A, rotA (FP32)
+    nF_fields = {'r2k_fp64': 10, 'r2k_df64': 1, 'r2k_df64c': 3, 'r2k_fp32': 6}
     dominant = max(stage_ms, key=stage_ms.get)
     roof = stage_roofline(dominant, stage_ms[dominant], args.steps, B * nk, precision, peaks, nF_fields)
     # every stage against its own bound (stage times from CUDA events on the stage's stream; the

@@ -191,6 +191,16 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 #define WBG_DEVICE_FLAG_TC_TIMEOUT 1
 int wbg_device_flags(unsigned int* flags, int clear);
 
+/* Failure detection of the tensor-core kernels (no counterpart in the reference).  Every mbarrier
+ * wait of those kernels gives up after a bound (1 s by default), records
+ * WBG_DEVICE_FLAG_TC_TIMEOUT, waits (at most 1 s) for the products it has issued, frees its
+ * tensor memory and returns; the context stays usable.  wbg_tc_wait_limit sets the bound in ns
+ * (for tests: a small bound makes waits run out); wbg_tc_wait_probe runs one such wait on an
+ * mbarrier whose phase never completes and writes 0 to the device int *result when it ran out
+ * (1 if it completed). */
+int wbg_tc_wait_limit(unsigned long long ns);
+int wbg_tc_wait_probe(int* result, void* stream);
+
 /* ---- generic Fermi-level scan of additive group traces (calculators/static.py:60-169) ------
  * formula WBG_FORMULA_IDENTITY: group size (CumDOS / DOS, calculators/static.py:192-214), 1
  *   component; WBG_FORMULA_INVMASS: the inverse-mass tensor dV^b/dk_d (formula/elementary.py:28-34,

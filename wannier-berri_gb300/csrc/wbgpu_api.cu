@@ -76,6 +76,10 @@ int wbg_rotate(const void* U, long long strideU, const void* X, int nFin, const 
 
 int wbg_device_flags(unsigned int* flags, int clear) { return wbg_device_flags_run(flags, clear); }
 
+int wbg_tc_wait_limit(unsigned long long ns) { return wbg_tc_wait_limit_run(ns); }
+
+int wbg_tc_wait_probe(int* result, void* stream) { return wbg_tc_wait_probe_run(result, (cudaStream_t)stream); }
+
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
                    int formula, int sea, void* hist, int fp64, void* stream) {
   return wbg_berry_scan_run(E, Xbar, nFbar, iV, iW, nw, nk, scan, formula, sea, hist, fp64, (cudaStream_t)stream);

@@ -12,6 +12,8 @@ bool wbg_rotate_tc_supported(int nw, int fp64, int nFrot);
 int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                       int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream);
 int wbg_device_flags_run(unsigned int* flags, int clear);
+int wbg_tc_wait_limit_run(unsigned long long ns);
+int wbg_tc_wait_probe_run(int* result, cudaStream_t stream);
 int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
                    int nFrot, void* Xbar, int nw, int nk, int fp64, cudaStream_t stream);
 int wbg_berry_omega_run(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int nw, int nk,

@@ -95,6 +95,8 @@ template <> WBG_D bool cnonzero<cdf>(cdf a) { return a.x.hi != 0.0f || a.y.hi !=
 // ---------------------------------------------------------------------------------------
 // Lazy multiply-add chains (df_lazy_fma of wbgpu_df64.cuh for double-float; an ordinary fma
 // for double), renormalised once at the end of the chain by lz_done.
+WBG_D void lz_fma(float& acc, float a, float b) { acc = fmaf(a, b, acc); }
+WBG_D float lz_done(float acc) { return acc; }
 WBG_D void lz_fma(double& acc, double a, double b) { acc = fma(a, b, acc); }
 WBG_D double lz_done(double acc) { return acc; }
 WBG_D void lz_fma(df64& acc, df64 a, df64 b) { df_lazy_fma(acc, a, b); }
@@ -503,8 +505,19 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
       __syncwarp();
       if (act)
         for (int jj = lane; jj < cw; jj += L) {
-          VU sacc = czero<VU>();
-          for (int i = c + 1; i < n; ++i) cfmac(sacc, vsh[i], Us[i * CW + jj]);
+          // v^H u as two lazy chains (even and odd rows): in double-float a chain step costs one
+          // FP32 add on its critical path, the error terms are summed once at the end
+          VU sacc = czero<VU>(), sacc1 = czero<VU>();
+          int i = c + 1;
+          for (; i + 1 < n; i += 2) {
+            lz_cfmac(sacc, vsh[i], Us[i * CW + jj]);
+            lz_cfmac(sacc1, vsh[i + 1], Us[(i + 1) * CW + jj]);
+          }
+          if (i < n) lz_cfmac(sacc, vsh[i], Us[i * CW + jj]);
+          sacc = lz_cdone(sacc);
+          sacc1 = lz_cdone(sacc1);
+          sacc.x = sacc.x + sacc1.x;
+          sacc.y = sacc.y + sacc1.y;
           const VU ts = cmul(tau, sacc);
           for (int i = c + 1; i < n; ++i) {
             VU u = Us[i * CW + jj];

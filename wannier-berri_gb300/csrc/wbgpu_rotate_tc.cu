@@ -46,7 +46,12 @@ constexpr int NACC = NMAIN + 1;            // + one for the correction products
 static_assert((KD / 8) % NMAIN == 0, "K steps must split evenly over the main accumulators");
 constexpr uint32_t TMEM_COLS = NACC * ND <= 128 ? 128 : NACC * ND <= 256 ? 256 : 512;  // GEMM1 and GEMM2 share them
 constexpr int STAGE_LD = NW + 1;           // float2 row stride of the Hermitian-part staging
-constexpr unsigned long long WAIT_NS = 1000000000ull;  // 1 s bound on every mbarrier wait
+// Bound on every mbarrier wait of the kernel: 1 s, settable (wbg_tc_wait_limit) so that a test can
+// make a wait run out and exercise the abort path.  After an abort the kernel still waits, for at
+// most DRAIN_NS, for the products it has issued, so that no MMA is in flight when its tensor memory
+// is freed and the block exits.
+__device__ unsigned long long g_tc_wait_ns = 1000000000ull;
+constexpr unsigned long long DRAIN_NS = 1000000000ull;
 constexpr int TMAP_MAX = 256;              // tile slots (fields + padding) of one launch
 
 static_assert(FPT * NW * STAGE_LD * 8 <= A_BYTES, "staging must fit in the A operand buffer");
@@ -118,8 +123,8 @@ WBG_D unsigned long long global_ns() {
   return t;
 }
 
-// Wait for phase `parity` of the mbarrier to complete, for at most WAIT_NS.
-WBG_D bool mbar_wait(uint32_t mbar, uint32_t parity) {
+// Wait for phase `parity` of the mbarrier to complete, for at most limit_ns.
+WBG_D bool mbar_wait(uint32_t mbar, uint32_t parity, unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   while (true) {
     uint32_t ok;
@@ -130,7 +135,7 @@ WBG_D bool mbar_wait(uint32_t mbar, uint32_t parity) {
         : "r"(mbar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (global_ns() - t0 > WAIT_NS) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -183,8 +188,8 @@ WBG_D void issue_gemm(uint32_t d, const unsigned char* Ah, const unsigned char* 
 }
 
 // Every thread waits on the MMA barrier; a timeout anywhere aborts the whole CTA.
-WBG_D bool wait_all(uint32_t mbar, uint32_t parity, volatile int* abort_s) {
-  if (!mbar_wait(mbar, parity)) {
+WBG_D bool wait_all(uint32_t mbar, uint32_t parity, volatile int* abort_s, unsigned long long limit_ns) {
+  if (!mbar_wait(mbar, parity, limit_ns)) {
     *abort_s = 1;
     atomicOr(&g_wbg_device_flags, (unsigned)WBG_DEVICE_FLAG_TC_TIMEOUT);
   }
@@ -237,6 +242,7 @@ __global__ void __launch_bounds__(NTHR, 2)
   const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter (= field of the tile), column half
   const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;  // TMEM lanes of this warp
   uint32_t phase = 0;
+  const unsigned long long wait_ns = g_tc_wait_ns;
   const int ntiles = ntiles_s, nfull = nfull_s;
   float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
   for (long long k = blockIdx.x; k < nk && !abort_s; k += gridDim.x) {
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(NTHR, 2)
           }
         }
       }
-      if (!wait_all(mb, phase, &abort_s)) break;
+      if (!wait_all(mb, phase, &abort_s, wait_ns)) break;
       phase ^= 1;
       tc_fence_after();
       if (t >= nfull) {  // ---- diagonal-only fields: diag_n = Re sum_m conj(U_mn) T_mn
@@ -404,7 +410,7 @@ __global__ void __launch_bounds__(NTHR, 2)
         issue_gemm(D2, Ah, Al, Bh, Bl);
         mma_commit(mb);
       }
-      if (!wait_all(mb, phase, &abort_s)) break;
+      if (!wait_all(mb, phase, &abort_s, wait_ns)) break;
       phase ^= 1;
       tc_fence_after();
       {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][n] for n in its column half
@@ -437,12 +443,31 @@ __global__ void __launch_bounds__(NTHR, 2)
       __syncthreads();  // TMEM columns and the A buffers are reused by the next tile
     }
   }
+  if (abort_s) {  // a wait ran out: let the products already issued (phase `phase`) finish first
+    if (tid == 0) mbar_wait(mb, phase, DRAIN_NS);
+  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
   }
+}
+
+// A wait that runs out by construction: an mbarrier whose phase never completes, waited on with
+// the kernel's bound; records WBG_DEVICE_FLAG_TC_TIMEOUT exactly as the rotation does.
+__global__ void tc_wait_probe_kernel(int* result) {
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ int abort_s;
+  const uint32_t mb = smem_u32(&mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_s = 0;
+  }
+  __syncthreads();
+  const bool ok = wait_all(mb, 0, &abort_s, g_tc_wait_ns);  // nothing arrives: phase 0 never completes
+  if (threadIdx.x == 0) *result = ok ? 1 : 0;
 }
 
 }  // namespace
@@ -463,6 +488,16 @@ int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin,
   const long long grid = nk < 2ll * sms ? nk : 2ll * sms;
   rotate_tc_kernel<<<(unsigned)grid, NTHR, SMEM_BYTES, stream>>>((const float2*)U, strideU, (const float2*)X, nFin,
                                                                 fsel, herm, nFrot, (float2*)Xbar, nk);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_tc_wait_limit_run(unsigned long long ns) {
+  return wbg_cuda_status(cudaMemcpyToSymbol(g_tc_wait_ns, &ns, sizeof(ns)));
+}
+
+int wbg_tc_wait_probe_run(int* result, cudaStream_t stream) {
+  if (!result) return WBG_ERR_ARG;
+  tc_wait_probe_kernel<<<1, 32, 0, stream>>>(result);
   return wbg_cuda_status(cudaGetLastError());
 }
 

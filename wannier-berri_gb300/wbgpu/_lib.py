@@ -12,7 +12,7 @@ from . import build as _build
 
 EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
            'wbg_r2k_columns', 'wbg_ws_replicas',
-           'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_berry_tabulate', 'wbg_berry_scan',
+           'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_tc_wait_limit', 'wbg_tc_wait_probe', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
            'wbg_dynamic_ncomp', 'wbg_dynamic_workspace_size', 'wbg_dynamic', 'wbg_berry_shc',
            'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma',
@@ -74,6 +74,8 @@ _SIGS = {
     'wbg_eigh_batched_noalloc': (_I, [_P, _LL, _I, _I, _P, _P, _LL, _I, _P, _P]),
     'wbg_rotate': (_I, [_P, _LL, _P, _I, _P, _P, _I, _P, _I, _I, _I, _P]),
     'wbg_device_flags': (_I, [ctypes.POINTER(ctypes.c_uint), _I]),
+    'wbg_tc_wait_limit': (_I, [ctypes.c_ulonglong]),
+    'wbg_tc_wait_probe': (_I, [_P, _P]),
     'wbg_ws_replicas': (_I, [_P, _I, _P, _I, _P, _I, ctypes.POINTER(Lattice), ctypes.c_double, _I, _P, _P, _P]),
     'wbg_berry_tabulate': (_I, [_P, _P, _I, _I, _I, _I, _I, _I, ctypes.c_double, _I, _I, _P, _I, _P]),
     'wbg_berry_scan': (_I, [_P, _P, _I, _I, _I, _I, _I, ctypes.POINTER(Scan), _I, _I, _P, _I, _P]),

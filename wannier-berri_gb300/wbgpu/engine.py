@@ -508,9 +508,12 @@ MIXED_FP32_ROTATION_MAX_NW = 32
 # against the oracle (AHC at nw = 32: 6.6e-7 of the 8.1e-7 total; nw = 96: 9.5e-6).
 MIXED_EIGH_BITS = EIGH_PRECISE_VECTORS
 # Transform precision of the mixed path's other k-space fields (lower triangles), and the
-# quantities whose fields are transformed in double-float (rounded to complex64) whatever it is.
+# quantities whose fields are transformed in double-float (rounded to complex64) whatever it is:
+# the velocity, whose FP32 transform error enters D = V / dE (AHC at nw = 32 against the oracle:
+# 8.1e-7 with every field in FP32, 2.3e-7 with V in double-float and the precise eigenvectors; the
+# Berry-curvature dipole on two 12^3 blocks: 1.9e-6 and 4.8e-7).
 MIXED_FIELDS_PREC = 3  # PREC_FP32S
-MIXED_DF64_QUANTITIES = set()
+MIXED_DF64_QUANTITIES = {'V'}
 
 
 def _prec(p):
