@@ -351,13 +351,32 @@ class Server:
         self._free_streams.append(req.stream)
         self._finished.append(req.ticket)
 
+    def _fail(self, req, error):
+        """Retire a request whose issue or round end raised: its ticket gets the error, its work
+        already queued on its stream is waited for before its buffers and stream are reused, and
+        the other requests go on."""
+        if req in self._active:
+            self._active.remove(req)
+        try:
+            req.stream.synchronize()
+        finally:
+            req.ticket._finish(error=error)
+            req.ws.release()
+            self._used -= req.nbytes
+            self._free_streams.append(req.stream)
+            self._finished.append(req.ticket)
+
     def step(self):
         """One scheduler round: admit, issue one batch per active request, retire finished
-        requests.  Returns True while there is work left."""
+        requests.  A request whose work raises on the host (a calculator, a refinement round)
+        fails alone.  Returns True while there is work left."""
         self._admit()
         for req in list(self._active):
             if req.next_batch < len(req.batches):
-                self._issue(req)
+                try:
+                    self._issue(req)
+                except Exception as e:
+                    self._fail(req, e)
         for req in list(self._active):
             if req.next_batch == len(req.batches) and req.done_event.query():
                 if req.refine is not None:
@@ -365,12 +384,7 @@ class Server:
                         if not self._end_round(req):
                             continue  # next refinement round queued on the same stream
                     except Exception as e:
-                        req.ticket._finish(error=e)
-                        self._active.remove(req)
-                        req.ws.release()
-                        self._used -= req.nbytes
-                        self._free_streams.append(req.stream)
-                        self._finished.append(req.ticket)
+                        self._fail(req, e)
                         continue
                 self._active.remove(req)
                 self._finish(req)
