@@ -227,12 +227,13 @@ def probe_peak(torch, fp64):
 
 
 # DRAM bytes per k-point of the mixed path's eigensolver kernels (dram__bytes_read.sum +
-# dram__bytes_write.sum of eigh_tridiag<df64, cdf, float>, eigh_ql<df64> and
-# eigh_vectors<df64, float>) from one ncu --set full capture of the 16^3 case
+# dram__bytes_write.sum of eigh_tridiag<df64, cdf, df64>, eigh_ql<df64> and
+# eigh_vectors<df64, df64, float2>) from one ncu --set full capture of the 16^3 case
 # (python bench.py --nkfft 16 --blocks-per-step 1 --steps 1 --warmup 3 --no-cpu-baseline
-# --no-fp64-compare --no-serve --no-tetra; 4096 matrices per launch).  Each matrix's traffic is
-# its own (H read, reflectors and U written, d / e / tau), so it scales with the matrices of a launch.
-EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 1.1 + 2.1 + 0.0 + 28.8 + 63.5) * 1e6 / 4096
+# --no-fp64-compare --no-serve --no-tetra --no-configs --no-graphs-tune; 4096 matrices per launch).
+# Each matrix's traffic is its own (H read, reflectors and U written, d / e / tau), so it scales
+# with the matrices of a launch.
+EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 11.3 + 2.1 + 0.0 + 45.2 + 12.7) * 1e6 / 4096
 
 
 def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
