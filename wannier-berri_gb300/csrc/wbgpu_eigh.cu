@@ -368,10 +368,16 @@ WBG_D double hash_uniform(unsigned int a, unsigned int b) {
 // lam [n] (type R), then U[n][n] and the staged reflector [n], complex(TU).  The iterate of
 // lane j lives in column j of Z.  When complex(TU) and R have the same size (df64 solve,
 // float vectors) U overlays Z: element (i, j) is converted in place by the lane that owns
-// column j, so the group needs half the shared memory.
+// column j, so the group needs half the shared memory.  When complex(TU) is twice R (vectors
+// in the precision of the solve) U starts where Z starts and the conversion runs row by row.
 // ---------------------------------------------------------------------------------------
 template <typename R, typename TU>
 constexpr bool kUOverlaysZ = sizeof(typename C2<TU>::t) == sizeof(R);
+// complex(TU) twice the size of R (double-float or FP64 vectors from a solve of the same type): U
+// holds Z in the first half of its region, converted row by row from the last (row i of U covers
+// rows 2i and 2i+1 of Z, which are read by then), so the group needs U's region only
+template <typename R, typename TU>
+constexpr bool kUWideOverlay = sizeof(typename C2<TU>::t) == 2 * sizeof(R);
 
 template <typename R, typename TU, typename VO>
 __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const typename C2<TU>::t* __restrict__ tauIn,
@@ -387,13 +393,16 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
   const size_t zbytes = (((size_t)n * n + 3 * n) * sizeof(R) + 15) / 16 * 16;
   const size_t ubytes = kUOverlaysZ<R, TU> ? 0 : ((size_t)n * CW * sizeof(VU) + 15) / 16 * 16;
   const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
-  unsigned char* gbase = smv + (size_t)grp * (zbytes + ubytes + vbytes);
+  const bool wide = kUWideOverlay<R, TU> && CW == n;
+  const size_t regbytes = wide ? (zbytes > ubytes ? zbytes : ubytes) : zbytes + ubytes;
+  unsigned char* gbase = smv + (size_t)grp * (regbytes + vbytes);
   R* Zs = reinterpret_cast<R*>(gbase);  // Z(i,j) = Zs[i*n + j]
   R* ds = Zs + n * n;
   R* es = ds + n;
   R* lam = es + n;
-  VU* Us = kUOverlaysZ<R, TU> ? reinterpret_cast<VU*>(gbase) : reinterpret_cast<VU*>(gbase + zbytes);  // [i][j-c0]
-  VU* vsh = reinterpret_cast<VU*>(gbase + zbytes + ubytes);
+  VU* Us = (kUOverlaysZ<R, TU> || wide) ? reinterpret_cast<VU*>(gbase)
+                                         : reinterpret_cast<VU*>(gbase + zbytes);  // [i][j-c0]
+  VU* vsh = reinterpret_cast<VU*>(gbase + regbytes);
   for (int i = lane; i < n; i += L) { ds[i] = dIn[k * n + i]; es[i] = eIn[k * n + i]; lam[i] = A::from(E[k * n + i]); }
   __syncwarp();
   const R zero = A::from(0.0), one = A::from(1.0);
@@ -491,12 +500,31 @@ __global__ void eigh_vectors(const typename C2<TU>::t* __restrict__ Vh, const ty
   // column is independent; CW < n only when a full U does not fit in shared memory)
   for (int c0 = 0; c0 < n; c0 += CW) {
     const int cw = min(CW, n - c0);
-    for (int jj = lane; jj < cw; jj += L)
-      for (int i = 0; i < n; ++i) {
-        VU z = czero<VU>();
-        z.x = to_tu<TU>(Zs[i * n + c0 + jj]);
-        Us[i * CW + jj] = z;
+    if (wide) {  // U over Z: rows from the last, every lane's reads of a row before its writes
+      for (int i = n - 1; i >= 0; --i) {
+        constexpr int kQ = (WBG_EIGH_NMAX + 31) / 32;  // columns per lane (L >= min(n, 32))
+        R zr[kQ];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q)
+          if (lane + q * L < n) zr[q] = Zs[i * n + lane + q * L];
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kQ; ++q)
+          if (lane + q * L < n) {
+            VU z = czero<VU>();
+            z.x = to_tu<TU>(zr[q]);
+            Us[i * n + lane + q * L] = z;
+          }
+        __syncwarp();
       }
+    } else {
+      for (int jj = lane; jj < cw; jj += L)
+        for (int i = 0; i < n; ++i) {
+          VU z = czero<VU>();
+          z.x = to_tu<TU>(Zs[i * n + c0 + jj]);
+          Us[i * CW + jj] = z;
+        }
+    }
     for (int c = n - 2; c >= 0; --c) {
       // every lane passes the same __syncwarp calls: groups sharing a warp have different tau
       const VU tau = tauIn[k * n + c];
@@ -585,8 +613,12 @@ struct EighShape {
     const size_t vbytes = ((size_t)n * sizeof(VU) + 15) / 16 * 16;
     CW = n;  // back-transform chunk width: the whole U unless it does not fit next to Z
     auto ub = [&](int cw) { return kUOverlaysZ<R, TU> ? (size_t)0 : ((size_t)n * cw * sizeof(VU) + 15) / 16 * 16; };
-    if (!kUOverlaysZ<R, TU> && zbytes + ub(n) + vbytes > kMaxBlockSmem) CW = 32;
-    smV = zbytes + ub(CW) + vbytes;
+    if (kUWideOverlay<R, TU> && (zbytes > ub(n) ? zbytes : ub(n)) + vbytes <= kMaxBlockSmem) {
+      smV = (zbytes > ub(n) ? zbytes : ub(n)) + vbytes;  // U over Z (CW = n)
+    } else {
+      if (!kUOverlaysZ<R, TU> && zbytes + ub(n) + vbytes > kMaxBlockSmem) CW = 32;
+      smV = zbytes + ub(CW) + vbytes;
+    }
     gmaxV = 64 / L;
   }
   int tridiag_default() const { return pick_group(smT, LT, gmaxT); }
