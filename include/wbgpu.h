@@ -224,6 +224,43 @@ int wbg_tc_wait_probe(int* result, void* stream);
 int wbg_berry_scan(const double* E, const void* Xbar, int nFbar, int iV, int iW, int nw, int nk, const wbg_scan* scan,
                    int formula, int sea, void* hist, int fp64, void* stream);
 
+/* ---- in-group matrix products (formula/formula.py:121-151 FormulaProduct) -----------------
+ * Replaces the StaticCalculator trace (calculators/static.py:60-169) of the product formulas of
+ * formula/covariant.py:798-865: VelOmega (BerryDipole_FermiSurf / NLAHC_FermiSurf,
+ * calculators/static.py:449-469), MassVel (NLDrude_FermiSurf, :532-542), VelMassVel / MassMass
+ * (Hall_classic_FermiSurf / FermiSea, :407-446), VelSpin (GME_spin_FermiSurf, :340-350), VelHplus
+ * (GME_orb_FermiSurf, :266-281), OmegaS (AHC_Zeeman_spin, :605-615), OmegaOmega (:618-623),
+ * OmegaHplus (AHC_Zeeman_orb, :626-644), and of the single factor DerSpin (GME_spin_FermiSea,
+ * :322-337).  factor[0..nfactors) lists the factors in product order: WBG_FACTOR_VEL (V^a, 3
+ * components), WBG_FACTOR_SPIN (S^a, 3), WBG_FACTOR_OMEGA (the nn block of Omega^c,
+ * formula/covariant.py:161-203, 3), WBG_FACTOR_MASS (the nn block of the inverse mass M^{bd},
+ * formula/elementary.py:28-34, 9 at 3 b + d), WBG_FACTOR_DERSPIN (the generalised derivative of
+ * S, (a, d) at 3 a + d, formula/covariant.py:338-342) and WBG_FACTOR_HPLUS (Morb_Hpm with sign +1,
+ * formula/covariant.py:375-449, 3); internal_terms / external_terms select the terms of Omega and
+ * Morb_Hpm.  Per group G the trace Re sum_{n[, p[, q]] in G} F1_n(p) [F2_p(q) [F3_qn]] is binned as
+ * wbg_berry_scan (sea != 0: the Fermi-sea group), components of the factors one after another
+ * ((i d2 + j) d3 + m), at most 81.  Field indices into Xbar (full matrices, not lower triangles;
+ * -1 when unused): V (3); A (3) and O = rotA (3) for Omega or Morb_Hpm with external terms, and B,
+ * C (3 each) for Morb_Hpm; W = d^2H/dk_b dk_d (9) for a mass factor; S (3) for a spin factor and S
+ * with dS = dS^a/dk_d (9, 3 a + d) for DerSpin.  wbg_product_values writes the per-band values of
+ * the tetrahedron method instead (as wbg_band_values). */
+#define WBG_FACTOR_VEL 0
+#define WBG_FACTOR_SPIN 1
+#define WBG_FACTOR_OMEGA 2
+#define WBG_FACTOR_MASS 3
+#define WBG_FACTOR_DERSPIN 4
+#define WBG_FACTOR_HPLUS 5
+typedef struct {
+  int nfactors;   /* 1 to 3 */
+  int factor[3];  /* WBG_FACTOR_* in product order */
+  int internal_terms, external_terms;
+  int V, A, O, W, S, B, C, dS;
+} wbg_product_spec;
+int wbg_berry_product(const double* E, const void* Xbar, int nFbar, const wbg_product_spec* spec, int nw, int nk,
+                      const wbg_scan* scan, int sea, void* hist, int fp64, void* stream);
+int wbg_product_values(const double* E, const void* Xbar, int nFbar, const wbg_product_spec* spec, int nw, int nk,
+                       double degen_thresh, const signed char* sel, double* P, int fp64, void* stream);
+
 /* ---- tetrahedron method (calculators/static.py:80-125 with tetra=True; grid/tetrahedron.py:
  * 15-281 TetraWeightsParal; corner energies data_K/data_K_R.py:121-141) ---------------------
  * The parallelepiped k +- delta/2 (delta = 1/(NKdiv NKFFT) per axis) around each k-point is cut
@@ -268,16 +305,17 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
                     int formula, int internal_terms, int external_terms, double degen_thresh,
                     const signed char* sel, double* P, int fp64, void* stream);
 
-/* Weighted sum over the bands of every k-point: sum_n P[k][n][c] w_n(E_F) with the band weight
- * w_n = 1/12 sum over the 12 tetrahedra (k-point + 3 corners) of the linear-tetrahedron
- * occupation (der 0) or its E_F derivative (der 1) at efermi[0..nEF) -- weight 1 for sel 2
- * bands (der 0).  hist [nEF][ncomp] is accumulated in difference form (hist[i] += P (w(i) -
- * w(i-1))): wbg_scan_finalize turns it into the sum.  ascending != 0: efermi is sorted
- * ascending and only the levels between a band's smallest and largest corner energy are
- * evaluated.  fp64 = 1: the reference's FP64 arithmetic (der 1 from its expanded cubic);
- * fp64 = 0 (mixed precision): energies relative to each band's lowest one as double-float
- * pairs, then FP32 relative to each tetrahedron's lowest corner (~1e-7 relative error per
- * weight; der 1 from the product rule on the piecewise form, free of the cubic's cancellation). */
+/* Weighted sum over the bands of every k-point (ncomp = 1..81 components per band):
+ * sum_n P[k][n][c] w_n(E_F) with the band weight w_n = 1/12 sum over the 12 tetrahedra
+ * (k-point + 3 corners) of the linear-tetrahedron occupation (der 0) or its E_F derivative
+ * (der 1) at efermi[0..nEF) -- weight 1 for sel 2 bands (der 0).  hist [nEF][ncomp] is
+ * accumulated in difference form (hist[i] += P (w(i) - w(i-1))): wbg_scan_finalize turns it
+ * into the sum.  ascending != 0: efermi is sorted ascending and only the levels between a
+ * band's smallest and largest corner energy are evaluated.  fp64 = 1: the reference's FP64
+ * arithmetic (der 1 from its expanded cubic); fp64 = 0 (mixed precision): energies relative
+ * to each band's lowest one as double-float pairs, then FP32 relative to each tetrahedron's
+ * lowest corner (~1e-7 relative error per weight; der 1 from the product rule on the
+ * piecewise form, free of the cubic's cancellation). */
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
                          int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64, void* hist,
@@ -412,7 +450,9 @@ int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double
  *   WBG_TUNE_EIGH_VECTORS_GROUP  matrices per block of the inverse iteration and
  *                                back-transform                                variant: eigh mode & 3
  *   WBG_TUNE_ROTATE_KPOINTS      k-points per block of the CUDA-core tiled U^dagger X U  variant: fp64
- *   WBG_TUNE_ROTATE_ENGINE       1 tensor cores, 2 CUDA cores (where both serve the case) variant: fp64
+ *   WBG_TUNE_ROTATE_ENGINE       1 tensor cores, warp-specialised (two tiles in flight), 2 CUDA
+ *                                cores, 3 tensor cores one tile at a time (the built-in choice;
+ *                                where they serve the case)                    variant: fp64
  * wbg_tune_candidates lists the values that fit the launch limits of (parameter, nw, variant);
  * wbg_tune_set accepts 0 or one of them (else WBG_STATUS_BAD_ARGUMENT), so every launch shape
  * the table can select is one the kernels accept.  Results do not depend on the eigensolver and

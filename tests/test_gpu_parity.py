@@ -154,12 +154,23 @@ def test_rotate_lower_triangle_input(fp64, nw):
     assert torch.equal(a[:, 2, d, d].real, b[:, 2, d, d].real)
 
 
+@pytest.mark.parametrize("engine_id", [1, 3])
 @pytest.mark.parametrize("nF", [1, 4, 9])
 @pytest.mark.parametrize("lower", [False, True])
-def test_rotate_tensor_core_vs_fp64(nF, lower):
+def test_rotate_tensor_core_vs_fp64(nF, lower, engine_id):
     """FP32 rotation at nw = 32 (tcgen05, 3xTF32 products, FP32 accumulation) against the FP64
     CUDA-core rotation: every output mode, field counts that leave partial 128-row tiles, a
-    batch that is not a multiple of the persistent grid.  Relative error < 2e-6 of max |Xbar|."""
+    batch that is not a multiple of the persistent grid; the warp-specialised kernel (engine 1)
+    and the one-tile-at-a-time kernel (engine 3, the default).  Relative error < 2e-6 of max |Xbar|."""
+    from wbgpu import autotune
+    autotune.set_value(autotune.ROTATE_ENGINE, 32, 0, engine_id)
+    try:
+        _rotate_tc_case(nF, lower)
+    finally:
+        autotune.set_value(autotune.ROTATE_ENGINE, 32, 0, 0)
+
+
+def _rotate_tc_case(nF, lower):
     nw, nk = 32, 1000
     rng = np.random.default_rng(31 + nF)
     X = rng.standard_normal((nk, nF, nw, nw)) + 1j * rng.standard_normal((nk, nF, nw, nw))

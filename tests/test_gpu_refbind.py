@@ -67,18 +67,22 @@ def test_reference_goldens_through_drop_in(random_ref):
 
 @pytest.mark.parametrize("precision,tol", [('fp64', 1e-9), ('mixed', 1e-6)])
 def test_drop_in_equals_reference_cpu_run(c2small_ref, precision, tol):
-    """AHC, Morb, BerryDipole_FermiSea and OpticalConductivity of the reference's run() on the MDRS
-    model: Data_K_GPU against the reference's own Data_K_R, block by block summed by the driver."""
+    """AHC, Morb, BerryDipole_FermiSea / FermiSurf, Hall_classic_FermiSea, GME_orb_FermiSurf and
+    OpticalConductivity of the reference's run() on the MDRS model: Data_K_GPU against the
+    reference's own Data_K_R, block by block summed by the driver."""
     system = c2small_ref
     EF = np.linspace(-2, 2, 101)
     mk = lambda: {'ahc': RC.static.AHC(Efermi=EF), 'morb': RC.static.Morb(Efermi=EF),
                   'bcd': RC.static.BerryDipole_FermiSea(Efermi=EF),
+                  'bcd_fsurf': RC.static.BerryDipole_FermiSurf(Efermi=EF),
+                  'hall_fsea': RC.static.Hall_classic_FermiSea(Efermi=EF),
+                  'gme_orb': RC.static.GME_orb_FermiSurf(Efermi=EF),
                   'opt': RC.dynamic.OpticalConductivity(Efermi=np.linspace(-1, 1, 5), omega=np.linspace(0, 3, 20),
                                                         smr_fixed_width=0.1)}
     cpu = RU.ref_run(wb, system, (2, 1, 2), (3, 4, 3), mk())
     gpu = RU.ref_run(wb, system, (2, 1, 2), (3, 4, 3), mk(), data_k_class=Data_K_GPU,
                      parameters_K={'precision': precision})
-    for key in ('ahc', 'morb', 'bcd', 'opt'):
+    for key in ('ahc', 'morb', 'bcd', 'bcd_fsurf', 'hall_fsea', 'gme_orb', 'opt'):
         a, b = gpu.results[key], cpu.results[key]
         assert a.data.shape == b.data.shape, key
         assert maxrel(a.data, b.data) < tol, (key, maxrel(a.data, b.data))
@@ -98,5 +102,5 @@ def test_drop_in_refinement_and_unsupported(c2small_ref):
                      data_k_class=Data_K_GPU)
     assert maxrel(gpu.results['ahc'].data, cpu.results['ahc'].data) < 1e-9
     with pytest.raises(NotImplementedError):
-        RU.ref_run(wb, system, (1, 1, 1), (3, 3, 3), {'g': RC.static.GME_orb_FermiSurf(Efermi=EF)},
+        RU.ref_run(wb, system, (1, 1, 1), (3, 3, 3), {'d': RC.static.NLDrude_FermiSea(Efermi=EF)},
                    data_k_class=Data_K_GPU)

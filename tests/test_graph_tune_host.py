@@ -32,7 +32,7 @@ def test_candidates_cover_every_nw():
             kp = autotune.candidates(autotune.ROTATE_KPOINTS, nw, fp64)
             assert bool(kp) == (nw % 4 == 0 and 8 <= nw <= 64), (nw, fp64, kp)
             eng = autotune.candidates(autotune.ROTATE_ENGINE, nw, fp64)
-            assert eng == ([1, 2] if (nw == 32 and fp64 == 0) else [])
+            assert eng == ([1, 2, 3] if (nw == 32 and fp64 == 0) else [])
 
 
 def test_set_get_reject():

@@ -202,6 +202,24 @@ int wbg_band_values(const double* E, const void* Xbar, int nFbar, const wbg_fiel
   }
 }
 
+int wbg_berry_product(const double* E, const void* Xbar, int nFbar, const wbg_product_spec* spec, int nw, int nk,
+                      const wbg_scan* scan, int sea, void* hist, int fp64, void* stream) {
+  return wbg_berry_product_run(E, Xbar, nFbar, spec, nw, nk, scan, sea, hist, fp64, (cudaStream_t)stream);
+}
+
+int wbg_product_values(const double* E, const void* Xbar, int nFbar, const wbg_product_spec* spec, int nw, int nk,
+                       double degen_thresh, const signed char* sel, double* P, int fp64, void* stream) {
+  if (!sel || !P) return WBG_STATUS_BAD_ARGUMENT;
+  WbgScan sp;
+  sp.EFmin = 0.0;  // groups come from sel; no histogram
+  sp.EFmax = 0.0;
+  sp.dEF = 1.0;
+  sp.degen_thresh = degen_thresh;
+  sp.nEF = 0;
+  sp.reserved = 0;
+  return wbg_berry_product_run(E, Xbar, nFbar, spec, nw, nk, &sp, 0, nullptr, fp64, (cudaStream_t)stream, sel, P);
+}
+
 int wbg_tetra_accumulate(const double* E, const double* Ecorner, const int* corner_slot, const int* blocks,
                          int nblocks, const wbg_tetra_grid* grid, int nw, const signed char* sel, const double* P,
                          int ncomp, const double* efermi, int nEF, int der, int ascending, int fp64,

@@ -976,6 +976,270 @@ __global__ void berry_scan_kernel(const double* __restrict__ E, const typename C
 }
 
 // ---------------------------------------------------------------------------------------
+// In-group matrix products (formula/formula.py:121-151, FormulaProduct) of one to three
+// factors with the factor lists of formula/covariant.py:798-865 (VelOmega, MassVel, MassMass,
+// VelMassVel, VelSpin, OmegaS, OmegaOmega, VelHplus, OmegaHplus) and the single-factor DerSpin
+// (formula/covariant.py:338-342).  The factors are the velocity V^a and the spin S^a (the group
+// blocks of the fields), the Berry curvature Omega^c (its nn block, formula/covariant.py:161-203),
+// Morb_Hpm^c with sign +1 (Morb_H + (E_p + E_q)/2 Omega, formula/covariant.py:375-449), the inverse
+// mass M^{bd} (the generalised derivative of V, formula/formula.py:108-112 with
+// formula/elementary.py:28-34) and the spin derivative dS^{ad} (the generalised derivative of S).
+// For band n of a group G the diagonal element of the product is
+//   t_n = Re F1_nn                                 (one factor)
+//   t_n = Re sum_{p in G} F1_np F2_pn              (two factors)
+//   t_n = Re sum_{p, q in G} F1_np F2_pq F3_qn     (three factors)
+// with component (i, j[, m]) at (i d2 + j) d3 + m: the Cartesian indices of the factors one
+// after another.  The group trace sum_{n in G} t_n is binned like wbg_berry_scan (with sea != 0
+// the bands below the window form one group [0, bandmax)).  A factor element (p, q) with an
+// l-sum runs over the bands l outside the group:
+//   Omega^c_pq = s_pq + conj(s_qp),
+//   s_pq = sum_l [-i D^a_pl D^b_lq - D^a_pl A^b_lq + D^b_pl A^a_lq] + O^c_pq / 2
+//          - i sum_{p' in G} A^a_pp' A^b_p'q,                     (a, b) = (c + 1, c + 2) mod 3
+//   M^{bd}_pq = W^{bd}_pq - sum_l D^d_pl V^b_lq + sum_l V^b_pl D^d_lq,
+// D_xy = -V_xy / (E_x - E_y) (0 below 1e-7).  A lane accumulates its bands' rows t_n in
+// shared memory (up to 81 components); groups of L lanes take one k-point at a time.
+// ---------------------------------------------------------------------------------------
+template <typename T, typename VS>
+struct ProductTerms {
+  typedef typename C2<T>::t V;
+  const VS* X;
+  const double* E;
+  const float* Eh;
+  const float* El;
+  int nw;
+  long long nw2;
+  wbg_product_spec s;
+  WBG_D V x(int fld, int p, int q) const {
+    const VS v = X[fld * nw2 + (long long)p * nw + q];
+    V r;
+    r.x = (T)v.x;
+    r.y = (T)v.y;
+    return r;
+  }
+  WBG_D V D(int a, int p, int q) const { return cscale(x(s.V + a, p, q), -inv_gap<T>(E, Eh, El, p, q)); }
+  // Omega^c_pq (orb = false) or Morb_H^c_pq (orb = true): s_pq + conj(s_qp) with
+  //   s_pq = sum_l w_l [-i D^a_pl D^b_lq] + sum_l [-D^a_pl Y^b_lq + D^b_pl Y^a_lq] + Z^c_pq / 2
+  //          - i sum_{r in G} A^a_pr w_r A^b_rq,
+  // w = 1, Y = A, Z = rotA for Omega; w = E, Y = B, Z = C for Morb_H (formula/covariant.py:161-203, 375-416)
+  WBG_D void curv(bool orb, int p, int q, int gs, int ge, V* out) const {
+    const int fY = orb ? s.B : s.A, fZ = orb ? s.C : s.O;
+    V s1[3], s2[3];  // s_pq and s_qp
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s1[c] = s2[c] = czero<V>();
+    for (int l = 0; l < nw; ++l) {
+      if (l >= gs && l < ge) continue;
+      const T w = orb ? (T)E[l] : T(1);
+      V Dpl[3], Dlq[3], Dql[3], Dlp[3], Ylq[3], Ylp[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Dpl[a] = D(a, p, l);
+        Dlq[a] = D(a, l, q);
+        Dql[a] = D(a, q, l);
+        Dlp[a] = D(a, l, p);
+        Ylq[a] = s.external_terms ? x(fY + a, l, q) : czero<V>();
+        Ylp[a] = s.external_terms ? x(fY + a, l, p) : czero<V>();
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int al = (c + 1) % 3, be = (c + 2) % 3;
+        if (s.internal_terms) {
+          s1[c] = csub(s1[c], cmuli(cscale(cmul(Dpl[al], Dlq[be]), w)));
+          s2[c] = csub(s2[c], cmuli(cscale(cmul(Dql[al], Dlp[be]), w)));
+        }
+        if (s.external_terms) {
+          s1[c] = cadd(s1[c], csub(cmul(Dpl[be], Ylq[al]), cmul(Dpl[al], Ylq[be])));
+          s2[c] = cadd(s2[c], csub(cmul(Dql[be], Ylp[al]), cmul(Dql[al], Ylp[be])));
+        }
+      }
+    }
+    if (s.external_terms) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int al = (c + 1) % 3, be = (c + 2) % 3;
+        s1[c] = cadd(s1[c], cscale(x(fZ + c, p, q), T(0.5)));
+        s2[c] = cadd(s2[c], cscale(x(fZ + c, q, p), T(0.5)));
+        V a1 = czero<V>(), a2 = czero<V>();
+        for (int r = gs; r < ge; ++r) {
+          const T w = orb ? (T)E[r] : T(1);
+          cfma(a1, cscale(x(s.A + al, p, r), w), x(s.A + be, r, q));
+          cfma(a2, cscale(x(s.A + al, q, r), w), x(s.A + be, r, p));
+        }
+        s1[c] = csub(s1[c], cmuli(a1));
+        s2[c] = csub(s2[c], cmuli(a2));
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[c] = cadd(s1[c], cconj(s2[c]));
+  }
+  // generalised derivative of the 3-component field fX with its derivative fdX (9, (a, d) at
+  // 3 a + d): dX^{ad}_pq - sum_l D^d_pl X^a_lq + sum_l X^a_pl D^d_lq (formula/formula.py:108-112)
+  WBG_D void gender(int fX, int fdX, int p, int q, int gs, int ge, V* out) const {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) out[i] = x(fdX + i, p, q);
+    for (int l = 0; l < nw; ++l) {
+      if (l >= gs && l < ge) continue;
+      V Xlq[3], Xpl[3], Dpl[3], Dlq[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        Xlq[a] = x(fX + a, l, q);
+        Xpl[a] = x(fX + a, p, l);
+        Dpl[a] = D(a, p, l);
+        Dlq[a] = D(a, l, q);
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) out[3 * a + d] = cadd(out[3 * a + d], csub(cmul(Xpl[a], Dlq[d]), cmul(Dpl[d], Xlq[a])));
+    }
+  }
+  // element (p, q) of factor `kind`; returns its number of components
+  WBG_D int elem(int kind, int p, int q, int gs, int ge, V* out) const {
+    if (kind == WBG_FACTOR_OMEGA) { curv(false, p, q, gs, ge, out); return 3; }
+    if (kind == WBG_FACTOR_MASS) { gender(s.V, s.W, p, q, gs, ge, out); return 9; }
+    if (kind == WBG_FACTOR_DERSPIN) { gender(s.S, s.dS, p, q, gs, ge, out); return 9; }
+    if (kind == WBG_FACTOR_HPLUS) {  // Morb_Hpm, sign +1 (formula/covariant.py:419-449)
+      V om[3];
+      curv(true, p, q, gs, ge, out);
+      curv(false, p, q, gs, ge, om);
+      const T eav = (T)(0.5 * (E[p] + E[q]));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) out[c] = cadd(out[c], cscale(om[c], eav));
+      return 3;
+    }
+    const int f = kind == WBG_FACTOR_SPIN ? s.S : s.V;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) out[a] = x(f + a, p, q);
+    return 3;
+  }
+};
+
+// T: arithmetic (FP64 in both paths: the blocks' l-sums cancel against W and the products of up
+// to three blocks amplify FP32 rounding), VS: storage of Xbar (complex64 in the mixed path)
+template <typename T, typename VS>
+__global__ void berry_product_kernel(const double* __restrict__ E, const VS* __restrict__ Xbar,
+                                     int nFbar, wbg_product_spec ps, int nc, int nw, int nk, int L, int G, WbgScan sp,
+                                     int sea, wbg_u64* __restrict__ hist, int shist, BandSel bs) {
+  typedef typename C2<T>::t V;
+  extern __shared__ double smb[];
+  const int nh = nc * sp.nEF;
+  wbg_u64* sh = shist ? reinterpret_cast<wbg_u64*>(smb) : hist;
+  double* Es = smb + (shist ? fx_words(nh) : 0);                  // [G][nw]
+  double* tv = Es + G * nw;                                       // [G][nw][nc]
+  float* Ehl = reinterpret_cast<float*>(tv + (size_t)G * nw * nc);  // [G][2][nw]
+  int* start = reinterpret_cast<int*>(Ehl + 2 * G * nw);          // [G][nw]
+  if (shist) fx_zero(sh, nh);
+  __syncthreads();
+  const int grp = threadIdx.x / L, lane = threadIdx.x % L;
+  double* myE = Es + grp * nw;
+  double* myT = tv + (size_t)nc * grp * nw;
+  float* myEh = Ehl + 2 * grp * nw;
+  float* myEl = myEh + nw;
+  int* myS = start + grp * nw;
+  const long long nw2 = (long long)nw * nw;
+  for (long long base = (long long)blockIdx.x * G; base < nk; base += (long long)gridDim.x * G) {
+    const long long k = base + grp;
+    const bool valid = k < nk;
+    const long long kk = valid ? k : nk - 1;
+    for (int i = lane; i < nw; i += L) {
+      const double e = E[kk * nw + i];
+      const float eh = (float)e;
+      myE[i] = e;
+      myEh[i] = eh;
+      myEl[i] = (float)(e - (double)eh);
+    }
+    __syncwarp();
+    for (int i = lane; i < nw; i += L) myS[i] = (i == 0) || (myE[i] - myE[i - 1] > sp.degen_thresh);
+    __syncwarp();
+    int bandmax = 0;
+    if (bs.sel) {
+      bandmax = sel_bandmax(bs.sel + kk * nw, nw, lane, L);
+    } else if (sea) {
+      int below = 0, f0 = nw;
+      for (int n = lane; n < nw; n += L) {
+        below += myE[n] < sp.EFmin;
+        if (myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) f0 = min(f0, n);
+        }
+      }
+      below = group_sum_i(below, L);
+      f0 = group_min_i(f0, L);
+      bandmax = min(below, f0);
+    }
+    ProductTerms<T, VS> pt{Xbar + kk * nFbar * nw2, myE, myEh, myEl, nw, nw2, ps};
+    for (int n = lane; n < nw; n += L) {
+      int gs = n, ge = n + 1;
+      while (!myS[gs]) --gs;
+      while (ge < nw && !myS[ge]) ++ge;
+      bool need;
+      if (n < bandmax) { gs = 0; ge = bandmax; need = true; }
+      else need = bs.sel ? bs.sel[kk * nw + n] == 1 : (myE[ge - 1] >= sp.EFmin && myE[gs] <= sp.EFmax);
+      double* t = myT + (size_t)n * nc;
+      for (int c = 0; c < nc; ++c) t[c] = 0.0;
+      if (!need) continue;
+      V F1[9], F2[9], F3[9];
+      if (ps.nfactors == 1) {
+        const int d1 = pt.elem(ps.factor[0], n, n, gs, ge, F1);
+        for (int i = 0; i < d1; ++i) t[i] += (double)F1[i].x;
+      }
+      for (int p = gs; p < ge && ps.nfactors > 1; ++p) {
+        const int d1 = pt.elem(ps.factor[0], n, p, gs, ge, F1);
+        if (ps.nfactors == 2) {
+          const int d2 = pt.elem(ps.factor[1], p, n, gs, ge, F2);
+          for (int i = 0; i < d1; ++i)
+            for (int j = 0; j < d2; ++j) t[i * d2 + j] += (double)cmul(F1[i], F2[j]).x;
+        } else {
+          for (int q = gs; q < ge; ++q) {
+            const int d2 = pt.elem(ps.factor[1], p, q, gs, ge, F2);
+            const int d3 = pt.elem(ps.factor[2], q, n, gs, ge, F3);
+            for (int i = 0; i < d1; ++i)
+              for (int j = 0; j < d2; ++j) {
+                const V ab = cmul(F1[i], F2[j]);
+                for (int m = 0; m < d3; ++m) t[(i * d2 + j) * d3 + m] += (double)cmul(ab, F3[m]).x;
+              }
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (valid && bs.P) {
+      emit_band_values(bs.P, k, nw, nc, lane, L, bandmax, bs.sel + k * nw, myS, myT, nc);
+    } else if (valid) {
+      for (int n = lane; n < nw; n += L) {
+        int gs = -1, ge = -1;
+        bool seag = false;
+        if (n == 0 && bandmax > 0) { gs = 0; ge = bandmax; seag = true; }
+        else if (n >= bandmax && myS[n]) {
+          int g1 = n + 1;
+          while (g1 < nw && !myS[g1]) ++g1;
+          if (myE[g1 - 1] >= sp.EFmin && myE[n] <= sp.EFmax) { gs = n; ge = g1; }
+        }
+        if (gs < 0) continue;
+        double esum = 0.0;
+        for (int q = gs; q < ge; ++q) esum += myE[q];
+        int bin = -1;
+        if (seag) bin = 0;
+        else {
+          const double Em = esum / (double)(ge - gs);
+          if (Em < sp.EFmin) bin = 0;
+          else if (Em <= sp.EFmax) bin = (int)ceil((Em - sp.EFmin) / sp.dEF);
+        }
+        if (bin >= 0 && bin < sp.nEF)
+          for (int c = 0; c < nc; ++c) {
+            double v = 0.0;
+            for (int q = gs; q < ge; ++q) v += myT[(size_t)q * nc + c];
+            fx_add_double(sh + 2 * (bin * nc + c), v, sh + 2 * nh);
+          }
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (hist && shist) fx_flush(sh, nh, hist);
+}
+
+// ---------------------------------------------------------------------------------------
 // Orbital moment, Morb_Hpm (formula/covariant.py:375-449): non-additive, so the trace over
 // inn = [0, n), out = [n, nw) is needed at every group border n (calculators/static.py:109-117).
 // The trace splits into pair functions of bands (m in inn, l in out / n' in inn):
@@ -1504,9 +1768,9 @@ int wbg_rotate_run(const void* U, long long strideU, const void* X, int nFin, co
   if (nw < 1 || nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
   // tensor cores (3xTF32) for the FP32 path at nw = 32 (unless the tuner chose the CUDA cores);
   // the kernel reads X in 16-byte pieces
-  if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0 &&
-      wbg_tuned(WBG_TUNE_ROTATE_ENGINE, fp64 ? 1 : 0, nw) != 2)
-    return wbg_rotate_tc_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
+  const int engine = wbg_tuned(WBG_TUNE_ROTATE_ENGINE, fp64 ? 1 : 0, nw);
+  if (wbg_rotate_tc_supported(nw, fp64, nFrot) && (reinterpret_cast<uintptr_t>(X) & 15) == 0 && engine != 2)
+    return wbg_rotate_tc_run(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream, engine != 1);
   if (fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
   if (fp64 == 2)  // double-float U and X, products in double-float, Xbar rounded to complex64
     return launch_rotate<df64, float2>(U, strideU, X, nFin, fsel, herm, nFrot, Xbar, nw, nk, stream);
@@ -1518,7 +1782,7 @@ int wbg_rotate_tune_candidates(int param, int nw, int variant, int* values, int 
   int count = 0;
   if (param == WBG_TUNE_ROTATE_ENGINE) {
     if (wbg_rotate_tc_supported(nw, variant, 1))
-      for (int v = 1; v <= 2 && count < capacity; ++v) values[count++] = v;
+      for (int v = 1; v <= 3 && count < capacity; ++v) values[count++] = v;
     return count;
   }
   if (param != WBG_TUNE_ROTATE_KPOINTS || nw % 4 != 0 || nw < 8 || nw > 64) return 0;
@@ -1640,6 +1904,67 @@ int wbg_berry_scan_run(const double* E, const void* Xbar, int nFbar, int iV, int
     else WBG_SCAN(float, 9);
   }
 #undef WBG_SCAN
+  return wbg_cuda_status(cudaGetLastError());
+}
+
+int wbg_berry_product_run(const double* E, const void* Xbar, int nFbar, const wbg_product_spec* spec, int nw, int nk,
+                          const WbgScan* sp_in, int sea, void* hist, int fp64, cudaStream_t stream,
+                          const signed char* sel, double* P) {
+  const BandSel bs{sel, P};
+  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || !spec || (!sel) != (!P) || (fp64 != 0 && fp64 != 1))
+    return WBG_ERR_ARG;
+  if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
+  const wbg_product_spec ps = *spec;
+  if (ps.nfactors < 1 || ps.nfactors > 3) return WBG_ERR_ARG;
+  auto ok = [&](int first, int n) { return first >= 0 && first + n <= nFbar; };
+  int nc = 1;
+  for (int i = 0; i < ps.nfactors; ++i) {
+    const int f = ps.factor[i];
+    if (f == WBG_FACTOR_VEL) {
+      if (!ok(ps.V, 3)) return WBG_ERR_ARG;
+    } else if (f == WBG_FACTOR_SPIN) {
+      if (!ok(ps.S, 3)) return WBG_ERR_ARG;
+    } else if (f == WBG_FACTOR_OMEGA) {
+      if (!ok(ps.V, 3) || (ps.external_terms && !(ok(ps.A, 3) && ok(ps.O, 3)))) return WBG_ERR_ARG;
+    } else if (f == WBG_FACTOR_MASS) {
+      if (!ok(ps.V, 3) || !ok(ps.W, 9)) return WBG_ERR_ARG;
+    } else if (f == WBG_FACTOR_DERSPIN) {
+      if (!ok(ps.V, 3) || !ok(ps.S, 3) || !ok(ps.dS, 9)) return WBG_ERR_ARG;
+    } else if (f == WBG_FACTOR_HPLUS) {
+      if (!ok(ps.V, 3) || (ps.external_terms && !(ok(ps.A, 3) && ok(ps.O, 3) && ok(ps.B, 3) && ok(ps.C, 3))))
+        return WBG_ERR_ARG;
+    } else {
+      return WBG_ERR_ARG;
+    }
+    if ((f == WBG_FACTOR_OMEGA || f == WBG_FACTOR_HPLUS) &&
+        ((ps.internal_terms != 0 && ps.internal_terms != 1) || (ps.external_terms != 0 && ps.external_terms != 1)))
+      return WBG_ERR_ARG;
+    nc *= (f == WBG_FACTOR_MASS || f == WBG_FACTOR_DERSPIN) ? 9 : 3;
+  }
+  WbgScan spv = *sp_in;
+  if (sel) { spv.nEF = 0; hist = nullptr; }
+  const int L = lanes_for(nw);
+  const size_t per_group = (size_t)nw * (8 + 8 * (size_t)nc + 8 + 4);
+  int G = 128 / L;
+  while (G > 1 && (size_t)G * per_group > 96 * 1024) G /= 2;
+  int shist = 0;
+  const size_t sm = hist_smem(nc * spv.nEF, (size_t)G * per_group, shist);
+  if (sm > 220 * 1024) return WBG_ERR_SIZE;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  long long nblk = (nk + G - 1) / G;
+  if (nblk > (long long)sms * 8) nblk = (long long)sms * 8;
+  if (fp64) {
+    auto kern = berry_product_kernel<double, double2>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    kern<<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, ps, nc, nw, nk, L, G, spv, sea,
+                                           (wbg_u64*)hist, shist, bs);
+  } else {
+    auto kern = berry_product_kernel<double, float2>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    kern<<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, ps, nc, nw, nk, L, G, spv, sea,
+                                           (wbg_u64*)hist, shist, bs);
+  }
   return wbg_cuda_status(cudaGetLastError());
 }
 

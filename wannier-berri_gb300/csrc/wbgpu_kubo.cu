@@ -22,7 +22,9 @@
 //              FP64 path).
 // kubo_accum:  one thread per frequency, a chunk of levels per block (grid z), a chunk of
 //              k-points per block (grid y): accumulation in shared memory in the records'
-//              precision, FP64 atomics into the result.
+//              precision, fixed-point sums into the result (FP64 path, and JDOS).
+// kubo_gemm:   the mixed path's 9- and 27-component sums as a register-tiled complex GEMM
+//              (frequencies x (level, component) per k-point, records as the contraction).
 #include <float.h>
 #include "wbgpu_common.cuh"
 #include "wbgpu_fixed.cuh"
@@ -354,6 +356,121 @@ __global__ void kubo_accum(const double* __restrict__ rec_dE, const R* __restric
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Mixed path, NC = 9 or 27: the same sums as a register-tiled complex GEMM per k-point,
+//   out[w][(e, c)] += sum_r F[w][r] G[r][(e, c)],   F = f_w(dE_r), G = f_E[r][e] M[r][c]
+// (calculators/dynamic.py:97-98: restot += factor_omega @ (factor_Efermi x M)).  A block takes
+// a tile of KG_TW frequencies x KG_TC columns (e, c) and a chunk of k-points; per chunk of
+// KG_RC records F and G are staged in shared memory (F from the FP64 difference dE - w, then
+// FP32) and every thread accumulates a 4 x 8 tile of outputs in FP32 registers.  Sums run in
+// three levels: a record chunk in FP32, the chunks of one k-point in FP32, the k-points of the
+// block in FP64 (shared memory), so that no FP32 chain is longer than one k-point's chunks;
+// the block's FP64 sums go to `out` once, as fixed-point entries.
+// ---------------------------------------------------------------------------------------
+constexpr int KG_TW = 64, KG_TC = 128, KG_RC = 32, KG_THR = 256;
+constexpr size_t KG_SMEM = (size_t)32 * KG_THR * sizeof(double2) + (size_t)KG_RC * (KG_TW + KG_TC) * sizeof(float2);
+
+template <int NC>
+__global__ void __launch_bounds__(KG_THR, 1)
+    kubo_gemm(const double* __restrict__ rec_dE, const float* __restrict__ rec_fE, const float2* __restrict__ rec_M,
+              const int* __restrict__ count, int P, int nk, int kchunk, const double* __restrict__ omega, WbgKubo kp,
+              int formula, wbg_u64* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smg[];
+  double2* accd = reinterpret_cast<double2*>(smg);  // [32][KG_THR]: thread tid's output q at q * KG_THR + tid
+  float2* Fs = reinterpret_cast<float2*>(accd + 32 * KG_THR);  // [KG_RC][KG_TW]
+  float2* Gs = Fs + KG_RC * KG_TW;                             // [KG_RC][KG_TC]
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int w0 = blockIdx.x * KG_TW, col0 = blockIdx.z * KG_TC;
+  const int ncol = kp.nEF * NC;
+  const float eta = (float)kp.eta;
+  const int fgroup = formula >= WBG_DYN_SHC_SIMPLE && formula <= WBG_DYN_SHC_RYOO ? kShcFactor : formula;
+  for (int q = 0; q < 32; ++q) accd[q * KG_THR + tid] = make_double2(0.0, 0.0);
+  const long long k0 = (long long)blockIdx.y * kchunk;
+  const long long k1 = min((long long)nk, k0 + kchunk);
+  for (long long k = k0; k < k1; ++k) {
+    const int nrec = count[k];
+    if (nrec == 0) continue;
+    const long long rbase = k * (long long)P;
+    float2 acck[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acck[i][j] = make_float2(0.f, 0.f);
+    for (int r0 = 0; r0 < nrec; r0 += KG_RC) {
+      const int rn = min(KG_RC, nrec - r0);
+      __syncthreads();  // the previous chunk's tiles are read
+      for (int idx = tid; idx < KG_RC * KG_TW; idx += KG_THR) {
+        const int r = idx / KG_TW, w = idx % KG_TW;
+        float2 v = make_float2(0.f, 0.f);
+        if (r < rn && w0 + w < kp.nOmega)
+          v = factor_omega<float>(fgroup, __ldg(rec_dE + rbase + r0 + r), __ldg(omega + w0 + w), eta, kp.gaussian);
+        Fs[idx] = v;
+      }
+      for (int idx = tid; idx < KG_RC * KG_TC; idx += KG_THR) {
+        const int r = idx / KG_TC, col = col0 + idx % KG_TC;
+        float2 v = make_float2(0.f, 0.f);
+        if (r < rn && col < ncol) {
+          const int e = col / NC, c = col - e * NC;
+          const long long rr = rbase + r0 + r;
+          const float fe = __ldg(rec_fE + rr * kp.nEF + e);
+          const float2 m = __ldg(rec_M + rr * NC + c);
+          v = make_float2(fe * m.x, fe * m.y);
+        }
+        Gs[idx] = v;
+      }
+      __syncthreads();
+      float2 acc[4][8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = make_float2(0.f, 0.f);
+#pragma unroll 2
+      for (int r = 0; r < KG_RC; ++r) {
+        float2 f[4], g[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) f[i] = Fs[r * KG_TW + ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) g[j] = Gs[r * KG_TC + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            acc[i][j].x = fmaf(f[i].x, g[j].x, fmaf(-f[i].y, g[j].y, acc[i][j].x));
+            acc[i][j].y = fmaf(f[i].x, g[j].y, fmaf(f[i].y, g[j].x, acc[i][j].y));
+          }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          acck[i][j].x += acc[i][j].x;
+          acck[i][j].y += acc[i][j].y;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        double2& a = accd[(i * 8 + j) * KG_THR + tid];
+        a.x += (double)acck[i][j].x;
+        a.y += (double)acck[i][j].y;
+      }
+  }
+  wbg_u64* bad = out + 4 * (long long)kp.nEF * kp.nOmega * NC;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int w = w0 + ty + 16 * i, col = col0 + tx + 16 * j;
+      if (w >= kp.nOmega || col >= ncol) continue;
+      const int e = col / NC, c = col - e * NC;
+      const double2 a = accd[(i * 8 + j) * KG_THR + tid];
+      wbg_u64* o = out + 4 * (((long long)e * kp.nOmega + w) * NC + c);
+      fx_add_double(o, a.x, bad);
+      fx_add_double(o + 2, a.y, bad);
+    }
+}
+
 template <typename T>
 void launch_pairs(int formula, int nk, size_t smp, cudaStream_t stream, const double* E, const void* Xbar, int nFbar,
                   const wbg_dynamic_spec& fs, int nw, const WbgKubo& kp, const double* efermi, double* rec_dE,
@@ -460,10 +577,24 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
     if (nc == 1) WBG_ACCUM(1, double);
     else if (nc == 9) WBG_ACCUM(9, double);
     else WBG_ACCUM(27, double);
-  } else {
-    if (nc == 1) WBG_ACCUM(1, float);
-    else if (nc == 9) WBG_ACCUM(9, float);
-    else WBG_ACCUM(27, float);
+  } else if (nc == 1) {
+    WBG_ACCUM(1, float);
+  } else {  // the register-tiled GEMM: one block per SM, frequency x column tiles x k chunks
+    const int gw = (kp->nOmega + KG_TW - 1) / KG_TW, gc = (kp->nEF * nc + KG_TC - 1) / KG_TC;
+    int gk = (sms + gw * gc - 1) / (gw * gc);
+    if (gk > nk) gk = nk;
+    const int kc = (nk + gk - 1) / gk;
+    gk = (nk + kc - 1) / kc;
+    const dim3 gg(gw, gk, gc);
+    if (nc == 9) {
+      cudaFuncSetAttribute(kubo_gemm<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KG_SMEM);
+      kubo_gemm<9><<<gg, KG_THR, KG_SMEM, stream>>>(rec_dE, (const float*)rec_fE, (const float2*)rec_M, count, P, nk,
+                                                    kc, omega, *kp, F, (wbg_u64*)out);
+    } else {
+      cudaFuncSetAttribute(kubo_gemm<27>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KG_SMEM);
+      kubo_gemm<27><<<gg, KG_THR, KG_SMEM, stream>>>(rec_dE, (const float*)rec_fE, (const float2*)rec_M, count, P, nk,
+                                                     kc, omega, *kp, F, (wbg_u64*)out);
+    }
   }
 #undef WBG_ACCUM
   return wbg_cuda_status(cudaGetLastError());

@@ -454,6 +454,344 @@ __global__ void __launch_bounds__(NTHR, 2)
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Warp-specialised form of the same rotation (one CTA per SM, two tiles in flight):
+//   warps 8-11  loaders: the embedded U of the next k-point into B[k % 2] and the X rows of
+//               the next tile into A[t % 2], split into TF32 hi / lo;
+//   warp 12     one thread issues GEMM1 (T = X U into TMEM D[t % 2]) and, once the epilogue
+//               has staged T^H, GEMM2 (Y^H = T^H U into the same columns);
+//   warps 0-7   epilogue: TMEM -> T^H (into A[t % 2], whose X rows GEMM1 has consumed), then
+//               TMEM -> Xbar (diagonal-only tiles: diag(U^dagger T) by a row reduction).
+// Buffers hand over through mbarriers (one phase per tile and buffer, so the parity of use u
+// of a buffer is u & 1); every wait is bounded in time (the abort path of rotate_tc_kernel: a
+// collective decision inside each role, the tensor memory freed only after the issued products
+// have completed).  While the epilogue turns tile t around, the loaders fill tile t + 1 and
+// GEMM1 of tile t + 1 runs after GEMM2 of tile t.
+// ---------------------------------------------------------------------------------------
+constexpr int PIPE_EPI = 256;                      // warps 0-7
+constexpr int PIPE_LD0 = 256, PIPE_LDN = 128;      // warps 8-11
+constexpr int PIPE_MMA_WARP = 12;
+constexpr int PIPE_THR = 13 * 32;
+constexpr int PIPE_SMEM = 2 * (2 * B_BYTES) + 2 * (2 * A_BYTES);  // B[2] and A[2], hi and lo each
+constexpr uint32_t PIPE_TMEM_COLS = 512;           // D[0] at column 0, D[1] at column 256
+static_assert(NACC * ND <= 256, "one tile's accumulators must fit 256 TMEM columns");
+
+WBG_D void mbar_init(uint32_t mb) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory"); }
+WBG_D void mbar_arrive(uint32_t mb) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mb) : "memory");
+}
+WBG_D bool mbar_test(uint32_t mb, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mb), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait that also gives up as soon as another role has aborted
+WBG_D bool pipe_wait(uint32_t mb, uint32_t parity, volatile int* abort_s, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_test(mb, parity)) {
+    if (*abort_s) return false;
+    if (global_ns() - t0 > limit_ns) {
+      *abort_s = 1;
+      atomicOr(&g_wbg_device_flags, (unsigned)WBG_DEVICE_FLAG_TC_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+WBG_D void named_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+// named barrier with an OR over the participants' predicates: one decision for the whole role
+WBG_D bool named_any(int id, int count, bool pred) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.s32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((int)pred), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(PIPE_THR, 1)
+    rotate_tc_pipe(const float2* __restrict__ U, long long strideU, const float2* __restrict__ X, int nFin,
+                   const int* __restrict__ fsel, const int* __restrict__ herm, int nFrot, float2* __restrict__ Xbar,
+                   int nk) {
+  extern __shared__ __align__(128) unsigned char smp[];
+  unsigned char* Bbuf = smp;                     // [2][hi | lo] embedded U
+  unsigned char* Abuf = smp + 4 * B_BYTES;       // [2][hi | lo] tile operand (X rows, then T^H)
+  __shared__ __align__(8) uint64_t bar_s[14];    // full_b[2] free_b[2] full_a1[2] mma1[2] full_a2[2] mma2[2] free[2]
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
+  __shared__ short tmap_s[TMAP_MAX];
+  __shared__ int nfull_s, ntiles_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  auto bar = [&](int which, int b) { return smem_u32(&bar_s[2 * which + b]); };
+  enum { FULL_B = 0, FREE_B = 1, FULL_A1 = 2, MMA1 = 3, FULL_A2 = 4, MMA2 = 5, FREE_T = 6 };
+  if (tid == 0) {
+    for (int i = 0; i < 14; ++i) mbar_init(smem_u32(&bar_s[i]));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_s = 0;
+    int nf = 0;
+    for (int f = 0; f < nFrot; ++f) nf += (herm[f] & 3) != 2;
+    const int nt = (nFrot + FPT - 1) / FPT;
+    for (int i = 0; i < nt * FPT; ++i) tmap_s[i] = -1;
+    int a = 0, b = nf;
+    for (int f = 0; f < nFrot; ++f) tmap_s[(herm[f] & 3) == 2 ? b++ : a++] = (short)f;
+    nfull_s = (nf + FPT - 1) / FPT;
+    ntiles_s = nt;
+  }
+  if (warp == PIPE_MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(PIPE_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = tmem_base_s;
+  const unsigned long long wait_ns = g_tc_wait_ns;
+  const int ntiles = ntiles_s, nfull = nfull_s;
+  const long long nkc = blockIdx.x < nk ? (nk - 1 - blockIdx.x) / gridDim.x + 1 : 0;  // k-points of this CTA
+  const long long ntt = nkc * ntiles;                                               // its tiles
+  if (warp >= 8 && warp < 12) {
+    // ================= loaders =================
+    const int lt = tid - PIPE_LD0;
+    long long tt = 0;
+    for (long long i = 0; i < nkc; ++i) {
+      const long long k = blockIdx.x + i * gridDim.x;
+      const int kb = (int)(i & 1);
+      bool ok = i < 2 || pipe_wait(bar(FREE_B, kb), (uint32_t)(((i >> 1) - 1) & 1), &abort_s, wait_ns);
+      if (named_any(1, PIPE_LDN, !ok || abort_s)) break;
+      unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
+      unsigned char* Bl = Bh + B_BYTES;
+      {
+        constexpr int PER = NW * NW / PIPE_LDN;
+        const float2* Uk = U + k * strideU;
+        float2 uv[PER];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) uv[q] = Uk[q * PIPE_LDN + lt];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+          const int e = q * PIPE_LDN + lt, j = e / NW, n = e % NW;
+          put_split(Bh, Bl, op_off(n, j), uv[q].x);
+          put_split(Bh, Bl, op_off(n, NW + j), -uv[q].y);
+          put_split(Bh, Bl, op_off(NW + n, j), uv[q].y);
+          put_split(Bh, Bl, op_off(NW + n, NW + j), uv[q].x);
+        }
+      }
+      fence_async_smem();
+      named_sync(1, PIPE_LDN);
+      if (lt == 0) mbar_arrive(bar(FULL_B, kb));
+      bool stop = false;
+      for (int t = 0; t < ntiles; ++t, ++tt) {
+        const int b = (int)(tt & 1);
+        const long long u = tt >> 1;
+        ok = u < 1 || pipe_wait(bar(FREE_T, b), (uint32_t)((u - 1) & 1), &abort_s, wait_ns);
+        if (named_any(1, PIPE_LDN, !ok || abort_s)) { stop = true; break; }
+        unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+        unsigned char* Al = Ah + A_BYTES;
+        constexpr int CPR = NW / 4;
+        constexpr int PER = FPT * NW * CPR / PIPE_LDN;
+        float2 xv[PER][4];
+        int code[FPT];
+#pragma unroll
+        for (int fl = 0; fl < FPT; ++fl) {
+          const int f = tmap_s[t * FPT + fl];
+          if (f < 0) {
+            code[fl] = -1;
+          } else {
+            const int fs = fsel[f];
+            code[fl] = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+          const int e = q * PIPE_LDN + lt, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
+          const int c = code[fl];
+          const bool lower = c >= 0 && (c >> 30);
+          const float2* Xf = X + (k * nFin + (c >= 0 ? (c & 0x3fffffff) : 0)) * (long long)(NW * NW);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) xv[q][r] = make_float2(0.f, 0.f);
+          if (c == -2) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) xv[q][r] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+          } else if (c >= 0) {
+            if (!lower || m >= n0 + 3) {
+              const float4* src = reinterpret_cast<const float4*>(Xf + m * NW + n0);
+              const float4 a = src[0], bb = src[1];
+              xv[q][0] = make_float2(a.x, a.y);
+              xv[q][1] = make_float2(a.z, a.w);
+              xv[q][2] = make_float2(bb.x, bb.y);
+              xv[q][3] = make_float2(bb.z, bb.w);
+            } else {
+#pragma unroll
+              for (int r = 0; r < 4; ++r) {
+                const int n = n0 + r;
+                if (m >= n) {
+                  xv[q][r] = Xf[m * NW + n];
+                } else {
+                  const float2 w = Xf[n * NW + m];
+                  xv[q][r] = make_float2(w.x, -w.y);
+                }
+              }
+            }
+            if (lower && m >= n0 && m < n0 + 4) {
+#pragma unroll
+              for (int r = 0; r < 4; ++r)
+                if (n0 + r == m) xv[q][r].y = 0.f;
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+          const int e = q * PIPE_LDN + lt, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
+          const int r = fl * NW + m;
+          put_split4(Ah, Al, op_off(r, n0), xv[q][0].x, xv[q][1].x, xv[q][2].x, xv[q][3].x);
+          put_split4(Ah, Al, op_off(r, NW + n0), xv[q][0].y, xv[q][1].y, xv[q][2].y, xv[q][3].y);
+        }
+        fence_async_smem();
+        named_sync(1, PIPE_LDN);
+        if (lt == 0) mbar_arrive(bar(FULL_A1, b));
+      }
+      if (stop) break;
+    }
+  } else if (warp == PIPE_MMA_WARP) {
+    // ================= MMA issue (one thread) =================
+    if (lane == 0) {
+      uint32_t last_bar = 0, last_par = 0;
+      for (long long tt = 0; tt < ntt; ++tt) {
+        const long long i = tt / ntiles;
+        const int t = (int)(tt % ntiles), kb = (int)(i & 1), b = (int)(tt & 1);
+        const long long u = tt >> 1;
+        const bool diag = t >= nfull;
+        if (t == 0 && !pipe_wait(bar(FULL_B, kb), (uint32_t)((i >> 1) & 1), &abort_s, wait_ns)) break;
+        if (u >= 1 && !pipe_wait(bar(FREE_T, b), (uint32_t)((u - 1) & 1), &abort_s, wait_ns)) break;
+        if (!pipe_wait(bar(FULL_A1, b), (uint32_t)(u & 1), &abort_s, wait_ns)) break;
+        tc_fence_after();
+        const unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+        const unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
+        const uint32_t D = tbase + (uint32_t)b * 256;
+        issue_gemm(D, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
+        mma_commit(bar(MMA1, b));
+        last_bar = bar(MMA1, b);
+        last_par = (uint32_t)(u & 1);
+        if (!pipe_wait(bar(FULL_A2, b), (uint32_t)(u & 1), &abort_s, wait_ns)) break;
+        tc_fence_after();
+        if (!diag) issue_gemm(D, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
+        mma_commit(bar(MMA2, b));
+        last_bar = bar(MMA2, b);
+        if (t == ntiles - 1) mma_commit(bar(FREE_B, kb));
+      }
+      if (abort_s && last_bar) mbar_wait(last_bar, last_par, DRAIN_NS);  // no product in flight at exit
+    }
+  } else if (warp < 8) {
+    // ================= epilogue =================
+    const int quarter = warp & 3, half = warp >> 2;
+    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
+    long long tt = 0;
+    bool stop = false;
+    for (long long i = 0; i < nkc && !stop; ++i) {
+      const long long k = blockIdx.x + i * gridDim.x;
+      for (int t = 0; t < ntiles; ++t, ++tt) {
+        const int b = (int)(tt & 1);
+        const long long u = tt >> 1;
+        const bool diag = t >= nfull;
+        unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+        unsigned char* Al = Ah + A_BYTES;
+        const uint32_t D = tbase + (uint32_t)b * 256;
+        bool ok = pipe_wait(bar(MMA1, b), (uint32_t)(u & 1), &abort_s, wait_ns);
+        if (named_any(2, PIPE_EPI, !ok || abort_s)) { stop = true; break; }
+        tc_fence_after();
+        const int f = tmap_s[t * FPT + quarter];
+        if (diag) {  // diag_n = Re sum_m conj(U_mn) T_mn
+          float re[16], im[16];
+          tmem_cols16(D + lane_base, 16 * half, re);
+          tmem_cols16(D + lane_base, NW + 16 * half, im);
+          if (f >= 0) {
+            const float2* Um = U + k * strideU + lane * NW + 16 * half;
+            float sum[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const float2 uu = Um[q];
+              sum[q] = uu.x * re[q] + uu.y * im[q];
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+              for (int q = 0; q < 16; ++q) sum[q] += __shfl_xor_sync(0xffffffffu, sum[q], off);
+            float v = 0.f;
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              if (q == lane) v = sum[q];
+            if (lane < 16) {
+              const int n = 16 * half + lane;
+              Xbar[(k * nFrot + f) * (long long)(NW * NW) + n * NW + n] = make_float2(v, 0.f);
+            }
+          }
+        } else {  // T -> A2 = T^H (rows of field q, K blocks Re | -Im)
+          const int row0 = quarter * NW;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            float v[16];
+            tmem_cols16(D + lane_base, NW * half + 16 * c, v);
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              put_split(Ah, Al, op_off(row0 + 16 * c + q, NW * half + lane), half ? -v[q] : v[q]);
+          }
+        }
+        tc_fence_before();
+        fence_async_smem();
+        named_sync(2, PIPE_EPI);
+        if (tid == 0) mbar_arrive(bar(FULL_A2, b));
+        ok = pipe_wait(bar(MMA2, b), (uint32_t)(u & 1), &abort_s, wait_ns);
+        if (named_any(2, PIPE_EPI, !ok || abort_s)) { stop = true; break; }
+        tc_fence_after();
+        if (!diag) {  // Y^H -> Xbar (Hermitian part staged in the tile's A buffer: GEMM2 has read it)
+          const int hm = f >= 0 ? (herm[f] & 3) : 0;
+          float2* dst = Xbar + (k * nFrot + (f >= 0 ? f : 0)) * (long long)(NW * NW);
+          float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
+          float re[16], im[16];
+          tmem_cols16(D + lane_base, 16 * half, re);
+          tmem_cols16(D + lane_base, NW + 16 * half, im);
+          if (f >= 0) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int n = 16 * half + q;
+              if (hm == 0) dst[n * NW + lane] = make_float2(re[q], -im[q]);
+              else if (hm == 2) { if (n == lane) dst[n * NW + n] = make_float2(re[q], 0.f); }
+              else stage[lane * STAGE_LD + n] = make_float2(re[q], im[q]);
+            }
+          }
+          named_sync(2, PIPE_EPI);
+          if (f >= 0 && hm == 1) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int n = 16 * half + q;
+              const float2 a = stage[lane * STAGE_LD + n], bb = stage[n * STAGE_LD + lane];
+              dst[n * NW + lane] = make_float2(0.5f * (a.x + bb.x), -0.5f * (a.y - bb.y));
+            }
+          }
+        }
+        tc_fence_before();
+        named_sync(2, PIPE_EPI);
+        if (tid == 0) mbar_arrive(bar(FREE_T, b));
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == PIPE_MMA_WARP) {
+    __syncwarp();  // lane 0 ran the issue loop alone: reconverge before the warp-wide dealloc
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(PIPE_TMEM_COLS) : "memory");
+  }
+}
+
 // A wait that runs out by construction: an mbarrier whose phase never completes, waited on with
 // the kernel's bound; records WBG_DEVICE_FLAG_TC_TIMEOUT exactly as the rotation does.
 __global__ void tc_wait_probe_kernel(int* result) {
@@ -477,12 +815,20 @@ bool wbg_rotate_tc_supported(int nw, int fp64, int nFrot) {
 }
 
 int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin, const int* fsel, const int* herm,
-                      int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream) {
+                      int nFrot, void* Xbar, int nw, int nk, cudaStream_t stream, bool serial) {
   if (nw != NW || nFrot > TMAP_MAX - 2 * FPT) return WBG_ERR_SIZE;
   if (nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return WBG_ERR_CUDA;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return WBG_ERR_CUDA;
+  if (!serial) {  // one CTA per SM (its shared memory and tensor memory take the whole SM)
+    if (cudaFuncSetAttribute(rotate_tc_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM) != cudaSuccess)
+      return WBG_ERR_CUDA;
+    const long long grid = nk < sms ? nk : sms;
+    rotate_tc_pipe<<<(unsigned)grid, PIPE_THR, PIPE_SMEM, stream>>>((const float2*)U, strideU, (const float2*)X, nFin,
+                                                                    fsel, herm, nFrot, (float2*)Xbar, nk);
+    return wbg_cuda_status(cudaGetLastError());
+  }
   if (cudaFuncSetAttribute(rotate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
     return WBG_ERR_CUDA;
   const long long grid = nk < 2ll * sms ? nk : 2ll * sms;

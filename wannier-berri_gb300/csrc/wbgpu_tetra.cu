@@ -348,8 +348,8 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
           }
         continue;
       }
-      double pv[9];
-      for (int c = 0; c < nc; ++c) pv[c] = Pn[c];
+      double pv[9];  // the band's values in registers; more than 9 components are read from P
+      for (int c = 0; c < nc && c < 9; ++c) pv[c] = Pn[c];
       const double e0 = E[kk * nw + n];
       double lo = e0, hi = e0;
       double ev[8];
@@ -414,11 +414,13 @@ __global__ void tetra_accumulate_kernel(const double* __restrict__ E, const doub
           const double d = wi - wprev;
           wprev = wi;
           if (d != 0.0)
-            for (int c = 0; c < nc; ++c) fx_add_double(acc + 2 * ((c0 + i) * nc + c), pv[c] * d, bad);
+            for (int c = 0; c < nc; ++c)
+              fx_add_double(acc + 2 * ((c0 + i) * nc + c), (nc <= 9 ? pv[c] : Pn[c]) * d, bad);
         }
       }
       if (i1 < nEF && wend != wprev)
-        for (int c = 0; c < nc; ++c) fx_add_double(acc + 2 * (i1 * nc + c), pv[c] * (wend - wprev), bad);
+        for (int c = 0; c < nc; ++c)
+          fx_add_double(acc + 2 * (i1 * nc + c), (nc <= 9 ? pv[c] : Pn[c]) * (wend - wprev), bad);
     }
   }
   if (smem_hist) {
@@ -464,7 +466,7 @@ int wbg_tetra_accumulate_run(const double* E, const double* Ec, const int* slot,
   if (!E || !Ec || !slot || !blocks || !g || !sel || !P || !EF || !hist || nblocks < 1 || nw < 1 || nEF < 1 ||
       !grid_ok(g))
     return WBG_ERR_ARG;
-  if (ncomp < 1 || ncomp > 9 || der < 0 || der > 1 || fp64 < 0 || fp64 > 1) return WBG_ERR_ARG;
+  if (ncomp < 1 || ncomp > 81 || der < 0 || der > 1 || fp64 < 0 || fp64 > 1) return WBG_ERR_ARG;
   const long long nkt = (long long)nblocks * g->fft[0] * g->fft[1] * g->fft[2];
   const int G = 4;
   const size_t wsm = (size_t)G * kWarpSmem * 8;

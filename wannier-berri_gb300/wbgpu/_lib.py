@@ -15,6 +15,7 @@ EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_wo
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_tc_wait_limit', 'wbg_tc_wait_probe', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
            'wbg_dynamic_ncomp', 'wbg_dynamic_workspace_size', 'wbg_dynamic', 'wbg_berry_shc',
+           'wbg_berry_product', 'wbg_product_values',
            'wbg_scan_finalize', 'wbg_tetra_select', 'wbg_band_values', 'wbg_tetra_accumulate', 'wbg_probe_fma',
            'wbg_tune_candidates', 'wbg_tune_set', 'wbg_tune_get']
 
@@ -56,6 +57,12 @@ class FieldIndex(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ['V', 'A', 'O', 'W', 'dA', 'dO', 'B', 'C']]
 
 
+class ProductSpec(ctypes.Structure):
+    _fields_ = ([('nfactors', ctypes.c_int), ('factor', ctypes.c_int * 3), ('internal_terms', ctypes.c_int),
+                 ('external_terms', ctypes.c_int)] +
+                [(n, ctypes.c_int) for n in ['V', 'A', 'O', 'W', 'S', 'B', 'C', 'dS']])
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _LL = ctypes.c_longlong
@@ -90,6 +97,9 @@ _SIGS = {
     'wbg_dynamic': (_I, [_P, _P, _I, ctypes.POINTER(DynamicSpec), _I, _I, ctypes.POINTER(KuboParams), _P, _P, _P, _SZ,
                          _P, _I, _P]),
     'wbg_berry_shc': (_I, [_P, _P, _I, ctypes.POINTER(DynamicSpec), _I, _I, ctypes.POINTER(Scan), _P, _I, _P]),
+    'wbg_berry_product': (_I, [_P, _P, _I, ctypes.POINTER(ProductSpec), _I, _I, ctypes.POINTER(Scan), _I, _P, _I,
+                               _P]),
+    'wbg_product_values': (_I, [_P, _P, _I, ctypes.POINTER(ProductSpec), _I, _I, ctypes.c_double, _P, _P, _I, _P]),
     'wbg_scan_finalize': (_I, [_P, _I, _I, ctypes.c_double, _P, _P]),
     'wbg_tetra_select': (_I, [_P, _P, _P, _P, _I, ctypes.POINTER(TetraGrid), _I, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, _I, _P, _P]),

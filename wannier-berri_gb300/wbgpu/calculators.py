@@ -24,7 +24,8 @@ from .engine import _ptr, _stream
 import types
 
 from .factors import (factor_ahc, factor_morb, factor_ohmic, factor_opt, factor_shc, factor_shift_current,
-                      factor_injection_current, factor_nlahc, factor_nldrude)
+                      factor_injection_current, factor_nlahc, factor_nldrude, factor_hall_classic, fac_spin_Z,
+                      fac_orb_Z, factor_gme_spin, factor_gme_orb)
 
 WBG_FORMULA_IDENTITY, WBG_FORMULA_INVMASS, WBG_FORMULA_VELVEL = 0, 1, 2  # include/wbgpu.h
 WBG_FORMULA_OMEGA, WBG_FORMULA_DEROMEGA, WBG_FORMULA_MORB, WBG_FORMULA_DIAG = 3, 4, 5, 6
@@ -102,23 +103,30 @@ class StaticCalculator(Calculator):
         if self.tetra:
             self._ef = torch.tensor(self.Efermi, dtype=torch.float64, device=device)
 
-    def tetra_accumulate(self, bd, formula, hist, ncomp, fields, ext=False):
+    def tetra_accumulate(self, bd, formula, hist, ncomp, fields, ext=False, product=None):
         """Tetrahedron method for one batch (static.py:80-85,119-125): bands selected by their
-        corner energies (sea for fder 0), per-band values of `formula`, weighted sum into the
-        histogram in difference form (wbg_scan_finalize then yields the result)."""
+        corner energies (sea for fder 0), per-band values of `formula` (or of the in-group
+        product `product`, a wbg_product_spec), weighted sum into the histogram in difference
+        form (wbg_scan_finalize then yields the result)."""
         tc = bd.tetra
         if tc is None:
             raise RuntimeError("tetra=True needs the corner energies of run() over a regular Grid")
         lib = _lib.load()
         sel = tc.selection(bd, self.Efermi[0], self.Efermi[-1], self.degen_thresh, int(self.fder == 0))
         P = torch.empty((bd.nk_total, bd.nw, ncomp), dtype=torch.float64, device=bd.E.device)
-        fi = _lib.FieldIndex(**{k: int(bd.index.get(q, 0)) for k, q in fields.items()})
         xbar = _ptr(bd.Xbar) if bd.Xbar is not None else None
         nF = bd.Xbar.shape[1] if bd.Xbar is not None else 0
-        st = engine._timed('band_values', lib.wbg_band_values, _ptr(bd.E), xbar, nF, ctypes.byref(fi), bd.nw,
-                           bd.nk_total, formula, int(self.internal_terms), int(ext),
-                           ctypes.c_double(self.degen_thresh), _ptr(sel), _ptr(P), int(bd.fp64_fields), _stream())
-        _lib.check(st, "wbg_band_values")
+        if product is not None:
+            st = engine._timed('band_values', lib.wbg_product_values, _ptr(bd.E), xbar, nF, ctypes.byref(product),
+                               bd.nw, bd.nk_total, ctypes.c_double(self.degen_thresh), _ptr(sel), _ptr(P),
+                               int(bd.fp64_fields), _stream())
+            _lib.check(st, "wbg_product_values")
+        else:
+            fi = _lib.FieldIndex(**{k: int(bd.index.get(q, 0)) for k, q in fields.items()})
+            st = engine._timed('band_values', lib.wbg_band_values, _ptr(bd.E), xbar, nF, ctypes.byref(fi), bd.nw,
+                               bd.nk_total, formula, int(self.internal_terms), int(ext),
+                               ctypes.c_double(self.degen_thresh), _ptr(sel), _ptr(P), int(bd.fp64_fields), _stream())
+            _lib.check(st, "wbg_band_values")
         ascending = int(len(self.Efermi) < 2 or np.all(np.diff(self.Efermi) > 0))
         st = engine._timed('tetra_accumulate', lib.wbg_tetra_accumulate, _ptr(bd.E), _ptr(tc.Ec), _ptr(tc.slot),
                            _ptr(bd.tetra_blocks), bd.nblocks, ctypes.byref(tc.grid), bd.nw, _ptr(sel), _ptr(P), ncomp,
@@ -555,6 +563,211 @@ class InjectionCurrent(DynamicCalculator):
         self.constant_factor = factor_injection_current
 
 
+# include/wbgpu.h
+WBG_FACTOR_VEL, WBG_FACTOR_SPIN, WBG_FACTOR_OMEGA, WBG_FACTOR_MASS, WBG_FACTOR_DERSPIN, WBG_FACTOR_HPLUS = range(6)
+_FACTOR_DIM = {WBG_FACTOR_VEL: 3, WBG_FACTOR_SPIN: 3, WBG_FACTOR_OMEGA: 3, WBG_FACTOR_MASS: 9,
+               WBG_FACTOR_DERSPIN: 9, WBG_FACTOR_HPLUS: 3}
+
+
+class _ProductCalculator(StaticCalculator):
+    """Static calculators whose formula is an in-group matrix product (formula/formula.py:121-151,
+    FormulaProduct; factor lists of formula/covariant.py:798-858) through wbg_berry_product:
+    ``factors`` in product order, Fermi surface (fder 1, central difference over the extended
+    levels) or Fermi sea (fder 0, the sea group)."""
+    factors = ()
+
+    def __init__(self, **kwargs):
+        self.ncomp = int(np.prod([_FACTOR_DIM[f] for f in self.factors]))
+        super().__init__(**kwargs)
+
+    def quantities(self, system):
+        q = set()
+        ext = self.external(system)
+        for f in self.factors:
+            if f == WBG_FACTOR_SPIN:
+                q.add('S')
+            elif f == WBG_FACTOR_MASS:
+                q |= {'V', 'W'}
+            elif f == WBG_FACTOR_DERSPIN:
+                q |= {'V', 'S', 'dS'}
+            else:
+                q.add('V')
+                if f == WBG_FACTOR_OMEGA and ext:
+                    q |= {'A', 'O'}
+                if f == WBG_FACTOR_HPLUS and ext:
+                    q |= {'A', 'O', 'B', 'C'}
+        return q
+
+    def spec(self, bd, system):
+        g = lambda q: int(bd.index[q]) if q in bd.index else -1
+        fac = list(self.factors) + [0] * (3 - len(self.factors))
+        return _lib.ProductSpec(nfactors=len(self.factors), factor=(ctypes.c_int * 3)(*fac),
+                                internal_terms=int(self.internal_terms), external_terms=int(self.external(system)),
+                                V=g('V'), A=g('A'), O=g('O'), W=g('W'), S=g('S'), B=g('B'), C=g('C'), dS=g('dS'))
+
+    def accumulate(self, bd, system):
+        ps = self.spec(bd, system)
+        if self.tetra:
+            return self.tetra_accumulate(bd, None, self._hist, self.ncomp, None, product=ps)
+        sc = self.scan_struct()
+        st = engine._timed('berry_product', _lib.load().wbg_berry_product, _ptr(bd.E), _ptr(bd.Xbar),
+                           bd.Xbar.shape[1], ctypes.byref(ps), bd.nw, bd.nk_total, ctypes.byref(sc),
+                           int(self.fder == 0), _ptr(self._hist), int(bd.fp64_fields), _stream())
+        _lib.check(st, "wbg_berry_product")
+
+    def _data(self, cell_volume, nk, factor):
+        data = self.finalize(cell_volume, nk, factor)
+        if self.fder == 1 and not self.tetra:  # calculators/static.py:137-140
+            data = (data[2:] - data[:-2]) / (2 * self.dEF)
+        return data.reshape((-1,) + (3,) * sum(1 + (_FACTOR_DIM[f] == 9) for f in self.factors))
+
+    def result(self, cell_volume, nk, factor=1.0):
+        return EnergyResult(self.Efermi, self._data(cell_volume, nk, factor))
+
+
+class BerryDipole_FermiSurf(_ProductCalculator):
+    r"""Berry curvature dipole (dimensionless) from the Fermi surface (calculators/static.py:449-458):
+    D_bd = -\int [dk] v_b Omega_d f' (formula VelOmega, formula/covariant.py:798-801)."""
+    factors, fder = (WBG_FACTOR_VEL, WBG_FACTOR_OMEGA), 1
+
+
+class NLAHC_FermiSurf(BerryDipole_FermiSurf):
+    r"""Nonlinear anomalous Hall conductivity (S^2/A) from the Fermi surface (calculators/static.py:461-469):
+    the Fermi-surface Berry-curvature dipole times e^3/hbar^2 tau."""
+
+    def __init__(self, constant_factor=factor_nlahc, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class NLDrude_FermiSurf(_ProductCalculator):
+    r"""Drude conductivity (S^2/A) from the Fermi surface (calculators/static.py:532-542):
+    e^3/hbar^2 tau^2 \int [dk] d_b v_a v_c f' (formula MassVel, formula/covariant.py:830-833)."""
+    factors, fder = (WBG_FACTOR_MASS, WBG_FACTOR_VEL), 1
+
+    def __init__(self, constant_factor=factor_nldrude, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class GME_spin_FermiSurf(_ProductCalculator):
+    r"""Spin gyrotropic magnetoelectric tensor from the Fermi surface (calculators/static.py:340-350):
+    \int [dk] v_a s_m f' (formula VelSpin)."""
+    factors, fder = (WBG_FACTOR_VEL, WBG_FACTOR_SPIN), 1
+
+    def __init__(self, constant_factor=factor_gme_spin, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class OmegaOmega(_ProductCalculator):
+    r"""\int [dk] Omega_a Omega_b f' (calculators/static.py:618-623, formula OmegaOmega,
+    formula/covariant.py:855-858)."""
+    factors, fder = (WBG_FACTOR_OMEGA, WBG_FACTOR_OMEGA), 1
+
+
+class AHC_Zeeman_spin(_ProductCalculator):
+    r"""Spin Zeeman correction of the AHC (S/m/T) from the Fermi surface (calculators/static.py:605-615):
+    e^2/hbar \int [dk] Omega_d s_m f' (formula OmegaS, formula/covariant.py:849-852)."""
+    factors, fder = (WBG_FACTOR_OMEGA, WBG_FACTOR_SPIN), 1
+
+    def __init__(self, constant_factor=fac_spin_Z * factor_ahc, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+def _hall_curl(T):
+    """The two antisymmetrisations of the classical Hall tensor (calculators/static.py:418-420,
+    440-442): T[e, p, q, r, s] -> X[e, p, q, g] = T[.., b(g), a(g)] - T[.., a(g), b(g)], then
+    out[e, h, g] = (X[e, a(h), b(h), g] - X[e, b(h), a(h), g]) / 2, (a, b)(g) = (g+1, g+2) mod 3."""
+    a, b = [1, 2, 0], [2, 0, 1]
+    X = T[:, :, :, b, a] - T[:, :, :, a, b]
+    return 0.5 * (X[:, a, b, :] - X[:, b, a, :])
+
+
+class Hall_classic_FermiSurf(_ProductCalculator):
+    r"""Classical Hall conductivity (S/m/T) from the Fermi surface (calculators/static.py:407-424):
+    e^3/hbar^2 tau^2 eps_{g m r} \int [dk] v_a d_r v_b v_g f' (formula VelMassVel,
+    formula/covariant.py:842-846), antisymmetrised to [E_F, 3, 3]."""
+    factors, fder = (WBG_FACTOR_VEL, WBG_FACTOR_MASS, WBG_FACTOR_VEL), 1
+
+    def __init__(self, constant_factor=factor_hall_classic, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+    def result(self, cell_volume, nk, factor=1.0):
+        return EnergyResult(self.Efermi, _hall_curl(self._data(cell_volume, nk, factor)))
+
+
+class Hall_classic_FermiSea(_ProductCalculator):
+    r"""Classical Hall conductivity (S/m/T) from the Fermi sea (calculators/static.py:427-446):
+    -e^3/hbar^2 tau^2 eps_{g m r} \int [dk] d_g v_a d_r v_b f (formula MassMass,
+    formula/covariant.py:836-839); the second mass tensor's derivative index goes first
+    (static.py:438), then the antisymmetrisations of Hall_classic_FermiSurf."""
+    factors, fder = (WBG_FACTOR_MASS, WBG_FACTOR_MASS), 0
+
+    def __init__(self, constant_factor=factor_hall_classic, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+    def result(self, cell_volume, nk, factor=1.0):
+        data = self._data(cell_volume, nk, factor).transpose(0, 4, 1, 2, 3)
+        return EnergyResult(self.Efermi, _hall_curl(data))
+
+
+class GME_spin_FermiSea(_ProductCalculator):
+    r"""Spin gyrotropic magnetoelectric tensor from the Fermi sea (calculators/static.py:322-337):
+    -\int [dk] d_a s_m f (formula DerSpin, the generalised derivative of S, formula/covariant.py:338-342),
+    returned with the derivative index first (static.py:334-336)."""
+    factors, fder = (WBG_FACTOR_DERSPIN,), 0
+
+    def __init__(self, constant_factor=factor_gme_spin, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+    def result(self, cell_volume, nk, factor=1.0):
+        return EnergyResult(self.Efermi, self._data(cell_volume, nk, factor).swapaxes(1, 2))
+
+
+class _MinusTwoEfOmega(_ProductCalculator):
+    """A product with Morb_Hpm (sign +1) minus 2 E_F times the same product with Omega in its place
+    (calculators/static.py:276-281, 639-644): H + G - 2 E_F Omega as the orbital moment."""
+    omega_twin = None
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self._omega = self.omega_twin(**kwargs)
+
+    def quantities(self, system):
+        return super().quantities(system) | self._omega.quantities(system)
+
+    def reset(self, device):
+        super().reset(device)
+        self._omega.reset(device)
+
+    def accumulate(self, bd, system):
+        super().accumulate(bd, system)
+        self._omega.accumulate(bd, system)
+
+    def result(self, cell_volume, nk, factor=1.0):
+        h = self._data(cell_volume, nk, factor)
+        om = self._omega._data(cell_volume, nk, factor)
+        return EnergyResult(self.Efermi, h - 2.0 * om * self.Efermi.reshape((-1,) + (1,) * (om.ndim - 1)))
+
+
+class GME_orb_FermiSurf(_MinusTwoEfOmega):
+    r"""Orbital gyrotropic magnetoelectric tensor from the Fermi surface (calculators/static.py:266-281):
+    \int [dk] v_a m_m f' with m = H + G - 2 E_F Omega (formula VelHplus, formula/covariant.py:804-808,
+    minus 2 E_F times BerryDipole_FermiSurf)."""
+    factors, fder, omega_twin = (WBG_FACTOR_VEL, WBG_FACTOR_HPLUS), 1, BerryDipole_FermiSurf
+
+    def __init__(self, constant_factor=factor_gme_orb, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
+class AHC_Zeeman_orb(_MinusTwoEfOmega):
+    r"""Orbital Zeeman correction of the AHC (S/m/T) from the Fermi surface (calculators/static.py:626-644):
+    e^2/hbar \int [dk] Omega_d m_m f' with m = H + G - 2 E_F Omega (formula OmegaHplus,
+    formula/covariant.py:861-865, minus 2 E_F times OmegaOmega)."""
+    factors, fder, omega_twin = (WBG_FACTOR_OMEGA, WBG_FACTOR_HPLUS), 1, OmegaOmega
+
+    def __init__(self, constant_factor=fac_orb_Z * factor_ahc, **kwargs):
+        super().__init__(constant_factor=constant_factor, **kwargs)
+
+
 # the reference's calculator modules (calculators/static.py, calculators/dynamic.py): both define an SHC
 def _no_kernel(name, ref):
     """A calculator of the reference (calculators/static.py) without a GPU kernel here: same name,
@@ -565,23 +778,21 @@ def _no_kernel(name, ref):
 
 
 _NO_KERNEL = {
-    'BerryDipole_FermiSurf': 'calculators/static.py:449-458', 'NLAHC_FermiSurf': 'calculators/static.py:461-469',
-    'NLDrude_FermiSea': 'calculators/static.py:519-529', 'NLDrude_FermiSurf': 'calculators/static.py:532-542',
-    'Hall_classic_FermiSurf': 'calculators/static.py:407-424', 'Hall_classic_FermiSea': 'calculators/static.py:427-446',
-    'GME_orb_FermiSurf': 'calculators/static.py:266-281', 'GME_orb_FermiSea': 'calculators/static.py:284-300',
-    'GME_spin_FermiSea': 'calculators/static.py:322-337', 'GME_spin_FermiSurf': 'calculators/static.py:340-350',
+    'NLDrude_FermiSea': 'calculators/static.py:519-529', 'GME_orb_FermiSea': 'calculators/static.py:284-300',
     'eMChA_FermiSurf': 'calculators/static.py:560-565', 'NLDrude_Zeeman_spin': 'calculators/static.py:568-573',
     'NLDrude_Zeeman_orb_Omega': 'calculators/static.py:576-581', 'NLDrude_Zeeman_orb': 'calculators/static.py:584-600',
-    'AHC_Zeeman_spin': 'calculators/static.py:605-615', 'OmegaOmega': 'calculators/static.py:618-623',
-    'AHC_Zeeman_orb': 'calculators/static.py:626-644', 'QuantumMetric_FermiSea': 'calculators/static.py:663-670',
-    'QuantumMetric_Vel_DQ': 'calculators/static.py:673-680'}
+    'QuantumMetric_FermiSea': 'calculators/static.py:663-670', 'QuantumMetric_Vel_DQ': 'calculators/static.py:673-680'}
 _no_kernel_classes = {n: _no_kernel(n, r) for n, r in _NO_KERNEL.items()}
 globals().update(_no_kernel_classes)
 
 static = types.SimpleNamespace(**_no_kernel_classes, **dict(
     StaticCalculator=StaticCalculator, AHC=AHC, Morb=Morb, BerryDipole_FermiSea=BerryDipole_FermiSea,
     NLAHC_FermiSea=NLAHC_FermiSea, DOS=DOS, CumDOS=CumDOS, Ohmic_FermiSea=Ohmic_FermiSea,
-    Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static))
+    Ohmic_FermiSurf=Ohmic_FermiSurf, Spin=Spin, NLDrude_Fermider2=NLDrude_Fermider2, SHC=SHC_static,
+    BerryDipole_FermiSurf=BerryDipole_FermiSurf, NLAHC_FermiSurf=NLAHC_FermiSurf, NLDrude_FermiSurf=NLDrude_FermiSurf,
+    GME_spin_FermiSurf=GME_spin_FermiSurf, OmegaOmega=OmegaOmega, AHC_Zeeman_spin=AHC_Zeeman_spin,
+    Hall_classic_FermiSurf=Hall_classic_FermiSurf, Hall_classic_FermiSea=Hall_classic_FermiSea,
+    GME_spin_FermiSea=GME_spin_FermiSea, GME_orb_FermiSurf=GME_orb_FermiSurf, AHC_Zeeman_orb=AHC_Zeeman_orb))
 def _elsewhere(name, ref, hint):
     """A calculator class of the reference served differently here (or not at all): constructing it
     raises NotImplementedError that says where the equivalent lives."""

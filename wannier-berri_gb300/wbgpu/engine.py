@@ -37,8 +37,10 @@ QUANTITIES = {
     'SHA': dict(order=0, herm=0, ncomp=9),
     'SR': dict(order=0, herm=0, ncomp=9),
     'SHR': dict(order=0, herm=0, ncomp=9),
+    # dS = Xbar('SS', 1): the derivative of the spin matrices, (spin a, direction d) at 3 a + d
+    'dS': dict(order=1, herm=1, ncomp=9),
 }
-QUANTITY_ORDER = ['V', 'A', 'O', 'Od', 'W', 'dA', 'dO', 'B', 'C', 'S', 'SH', 'SA', 'SHA', 'SR', 'SHR']
+QUANTITY_ORDER = ['V', 'A', 'O', 'Od', 'W', 'dA', 'dO', 'B', 'C', 'S', 'SH', 'SA', 'SHA', 'SR', 'SHR', 'dS']
 # R-space key of each plain (moment-0) quantity and the components of every extra key
 MOM0_KEY = {'B': 'BB', 'C': 'CC', 'S': 'SS', 'SH': 'SH', 'SA': 'SA', 'SHA': 'SHA', 'SR': 'SR', 'SHR': 'SHR'}
 KEY_NCOMP = {'AA': 3, 'BB': 3, 'CC': 3, 'SS': 3, 'SH': 3, 'SA': 9, 'SHA': 9, 'SR': 9, 'SHR': 9}
@@ -363,6 +365,8 @@ def field_plan(quantities, with_H, extra_keys):
             desc += [(ROT, base_of['AA'], g, 0) for g in range(3)]
         elif q == 'dO':
             desc += [(DROT, base_of['AA'], g, d) for g in range(3) for d in range(3)]
+        elif q == 'dS':
+            desc += [(DER1, base_of['SS'] + a, d, 0) for a in range(3) for d in range(3)]
         elif q in MOM0_KEY:
             desc += [(MOM0, base_of[MOM0_KEY[q]] + a, 0, 0) for a in range(QUANTITIES[q]['ncomp'])]
     return desc, index
@@ -426,6 +430,8 @@ def extra_keys_for(quantities):
     for q in QUANTITY_ORDER:
         if q in quantities and q in MOM0_KEY:
             keys.append(MOM0_KEY[q])
+    if 'dS' in quantities and 'SS' not in keys:
+        keys.append('SS')
     return keys
 
 

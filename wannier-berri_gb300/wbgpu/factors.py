@@ -1,5 +1,5 @@
 """Physical prefactors (same definitions as the reference factors.py:1-36, from scipy.constants)."""
-from scipy.constants import elementary_charge, hbar, physical_constants, angstrom, pi
+from scipy.constants import elementary_charge, hbar, physical_constants, angstrom, pi, electron_mass
 
 bohr = physical_constants['Bohr radius'][0] / angstrom
 eV_au = physical_constants['electron volt-hartree relationship'][0]
@@ -14,3 +14,10 @@ factor_shift_current = hbar / elementary_charge * pi * elementary_charge ** 3 / 
 factor_injection_current = - pi * elementary_charge ** 3 / (hbar ** 2) * TAU_UNIT
 factor_nlahc = elementary_charge ** 3 / hbar ** 2 * TAU_UNIT  # factors.py:28
 factor_nldrude = -(elementary_charge ** 3 / hbar ** 2 * TAU_UNIT ** 2 * elementary_charge / hbar)  # factors.py:31-32
+factor_hall_classic = -(elementary_charge ** 3 / hbar ** 2 * angstrom * TAU_UNIT ** 2 *
+                        elementary_charge ** 2 / hbar ** 2)  # factors.py:29-30, with tau^2 E^1 B^1
+bohr_magneton = elementary_charge * hbar / (2 * electron_mass)  # factors.py:6
+fac_orb_Z = elementary_charge / 2 / hbar * angstrom ** 2  # factors.py:16: m_orb B in eV
+fac_spin_Z = hbar / (2 * electron_mass)  # factors.py:17: m_spin B in eV
+factor_gme_spin = -bohr_magneton / angstrom ** 2  # factors.py:22
+factor_gme_orb = -(elementary_charge * angstrom ** 2) * elementary_charge / (2 * hbar) / angstrom ** 2  # factors.py:12,20

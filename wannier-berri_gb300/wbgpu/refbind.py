@@ -47,6 +47,11 @@ STATIC_TWINS = {
     'AHC': 'AHC', 'Morb': 'Morb', 'BerryDipole_FermiSea': 'BerryDipole_FermiSea', 'NLAHC_FermiSea': 'NLAHC_FermiSea',
     'DOS': 'DOS', 'CumDOS': 'CumDOS', 'Ohmic_FermiSea': 'Ohmic_FermiSea', 'Ohmic_FermiSurf': 'Ohmic_FermiSurf',
     'Spin': 'Spin', 'NLDrude_Fermider2': 'NLDrude_Fermider2', 'SHC': 'SHC_static',
+    'BerryDipole_FermiSurf': 'BerryDipole_FermiSurf', 'NLAHC_FermiSurf': 'NLAHC_FermiSurf',
+    'NLDrude_FermiSurf': 'NLDrude_FermiSurf', 'GME_spin_FermiSurf': 'GME_spin_FermiSurf', 'OmegaOmega': 'OmegaOmega',
+    'AHC_Zeeman_spin': 'AHC_Zeeman_spin', 'Hall_classic_FermiSurf': 'Hall_classic_FermiSurf',
+    'Hall_classic_FermiSea': 'Hall_classic_FermiSea', 'GME_spin_FermiSea': 'GME_spin_FermiSea',
+    'GME_orb_FermiSurf': 'GME_orb_FermiSurf', 'AHC_Zeeman_orb': 'AHC_Zeeman_orb',
 }
 DYNAMIC_TWINS = {
     'OpticalConductivity': 'OpticalConductivity', 'JDOS': 'JDOS', 'SHC': 'SHC', 'ShiftCurrent': 'ShiftCurrent',
@@ -190,6 +195,17 @@ _TR_INV = {
     (ref_static, 'Spin'): ('transform_odd', 'transform_ident'),
     (ref_static, 'NLDrude_Fermider2'): ('transform_odd', 'transform_odd'),
     (ref_static, 'SHC'): ('transform_ident', 'transform_ident'),
+    (ref_static, 'BerryDipole_FermiSurf'): ('transform_ident', 'transform_odd'),
+    (ref_static, 'NLAHC_FermiSurf'): ('transform_ident', 'transform_odd'),
+    (ref_static, 'NLDrude_FermiSurf'): ('transform_odd', 'transform_odd'),
+    (ref_static, 'GME_spin_FermiSurf'): ('transform_ident', 'transform_odd'),
+    (ref_static, 'OmegaOmega'): ('transform_ident', 'transform_ident'),
+    (ref_static, 'AHC_Zeeman_spin'): ('transform_ident', 'transform_ident'),
+    (ref_static, 'Hall_classic_FermiSurf'): ('transform_ident', 'transform_ident'),
+    (ref_static, 'Hall_classic_FermiSea'): ('transform_ident', 'transform_ident'),
+    (ref_static, 'GME_spin_FermiSea'): ('transform_ident', 'transform_odd'),
+    (ref_static, 'GME_orb_FermiSurf'): ('transform_ident', 'transform_odd'),
+    (ref_static, 'AHC_Zeeman_orb'): ('transform_ident', 'transform_ident'),
     (ref_dynamic, 'OpticalConductivity'): ('transform_trans', 'transform_ident'),
     (ref_dynamic, 'JDOS'): ('transform_ident', 'transform_ident'),
     (ref_dynamic, 'SHC'): ('transform_ident', 'transform_ident'),
