@@ -595,6 +595,48 @@ def _oracle_rate(s, nkfft, calcs):
     return int(np.prod(nkfft)) / (time.perf_counter() - t0)
 
 
+def bench_rotation_engines(nk, reps):
+    """CUDA-event time of U^dagger X U at nw = 32 on `nk` synthetic k-points with the mixed AHC
+    path's fields (V and A from lower triangles, V plain, A Hermitian part, rotA diagonal only) for
+    each engine of the rotation (wbg_tune ROTATE_ENGINE): 1 tensor cores warp-specialised, 3
+    tensor cores one tile at a time, 2 CUDA cores; and the largest difference between the engines."""
+    import torch
+    from wbgpu import autotune, engine
+    nw = 32
+    g = torch.Generator(device='cuda').manual_seed(1)
+    U = (torch.randn(nk, nw, nw, dtype=torch.complex64, device='cuda', generator=g) / nw ** 0.5).contiguous()
+    X = torch.randn(nk, 9, nw, nw, dtype=torch.complex64, device='cuda', generator=g)
+    sel, herm = list(range(9)), [0 | 4] * 3 + [1 | 4] * 3 + [2 | 4] * 3
+    out = {}
+    ref = None
+    for e in (3, 1, 2):
+        autotune.set_value(autotune.ROTATE_ENGINE, nw, 0, e)
+        Y = torch.empty((nk, 9, nw, nw), dtype=torch.complex64, device='cuda')
+        for _ in range(2):
+            engine.rotate(U, X, 9, sel, herm, nw, nk, 0, out=Y)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(max(1, reps)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            engine.rotate(U, X, 9, sel, herm, nw, nk, 0, out=Y)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        d = torch.arange(nw, device='cuda')
+        if ref is None:
+            ref = Y.clone()
+            diff = 0.0
+        else:
+            diff = max(float((Y[:, :6] - ref[:, :6]).abs().max()), float((Y[:, 6:, d, d] - ref[:, 6:, d, d]).abs().max()))
+        out[{1: "tensor_warp_specialised", 2: "cuda_cores", 3: "tensor_one_tile"}[e]] = {
+            "ms_median": float(np.median(ts)), "max_abs_diff_vs_one_tile": diff}
+    autotune.set_value(autotune.ROTATE_ENGINE, nw, 0, 0)
+    out["nk"] = nk
+    out["device_flags"] = engine.device_flags()
+    return out
+
+
 def bench_configs():
     """run() throughput of the cubic nw = 8 model (AHC at 501 E_F, the whole 48^3 grid in 8^3
     blocks) and of the spinor nw = 96 model with SOC (R in [-5,5]^3; OpticalConductivity at 11
@@ -688,45 +730,54 @@ def bench_batched(nsys=32):
             "max_rel_err_vs_fp64": err, "nw": [s.num_wann for s in systems]}
 
 
-def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
-    """Poisson arrivals (mean `rate` per s) of AHC requests over `nsys` resident systems
-    (num_wann 8-128), grids 8^3-32^3, each with 0-3 rounds of adaptive refinement (the
-    reference's policy: the largest K-point divided into 2^3 blocks per round): p50 / p99 latency
-    from submit to result and throughput, against the plain FP64 run() of the first `nbase`
-    requests (same refinement) one after the other."""
+def bench_served(nsys=16, nreq=120, load=0.7, nbase=24):
+    """Poisson arrivals of AHC requests over `nsys` resident systems (num_wann log-uniform
+    8-128), grids 16^3-32^3, each with 0-3 rounds of refinement around the largest Berry
+    curvatures (8^3 sub-grids around the top 1% of k-points by |Omega| per round).  The offered
+    rate is `load` times the server's capacity, measured first by serving the same requests all at
+    once; p50 / p99 latency from submit to result at that rate, and throughput, against the plain
+    FP64 path of the first `nbase` requests (same refinement) one after the other."""
     import numpy as np
     import torch
     import wbgpu
     from wbgpu import engine
     from wbgpu.calculators import AHC
-    from wbgpu.run import run_adaptive
+    from wbgpu.run import run_refine_omega
     ef = np.linspace(-1, 1, 201)
     systems = tb_pool(nsys, 5000, 8, 128)
     rng = np.random.default_rng(5001)
     reqs = []
     for i in range(nreq):
         s = int(rng.integers(nsys))
-        nkfft, nkdiv = int(rng.choice([8, 16])), int(rng.choice([1, 2]))
-        reqs.append((s, nkdiv, nkfft, int(rng.integers(0, 4))))
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        reqs.append((s, int(rng.choice([1, 2])), 16, int(rng.integers(0, 4))))
     grids = {}
     grid_of = lambda r: grids.setdefault(r[:3], wbgpu.Grid(systems[r[0]], NKdiv=r[1], NKFFT=r[2]))
     srv = wbgpu.Server(precision='mixed', max_active=8)
     for i, s in enumerate(systems):
         srv.add_system(i, s)
+    submit = lambda r: srv.submit(r[0], grid_of(r), {'ahc': AHC(Efermi=ef)}, refine_omega=r[3])
     for r in set(q[:3] for q in reqs):  # warm the per-(system, grid) caches: R-space fields, phase tables
         srv.submit(r[0], grid_of(r), {'ahc': AHC(Efermi=ef)})
     srv.run_until_idle()
     torch.cuda.synchronize()
+    # capacity: every request at once
+    srv._finished.clear()
+    t0 = time.perf_counter()
+    cal = [submit(r) for r in reqs]
+    srv.run_until_idle()
+    torch.cuda.synchronize()
+    capacity = nreq / (time.perf_counter() - t0)
+    rate = load * capacity
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     srv._finished.clear()
     tickets = []
     with srv:
         t0 = time.perf_counter()
-        for (s, nkdiv, nkfft, nit), ta in zip(reqs, arrivals):
+        for r, ta in zip(reqs, arrivals):
             dt = t0 + ta - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            tickets.append(srv.submit(s, grid_of((s, nkdiv, nkfft)), {'ahc': AHC(Efermi=ef)}, adpt_num_iter=nit))
+            tickets.append(submit(r))
         for t in tickets:
             t.wait(600)
     st = srv.stats(tickets)
@@ -736,18 +787,23 @@ def bench_served(nsys=16, nreq=200, rate=200.0, nbase=40):
     for s, nkdiv, nkfft, nit in reqs[:nbase]:
         g = grid_of((s, nkdiv, nkfft))
         dev = devs.setdefault(s, engine.DeviceSystem(systems[s]))
-        if nit:
-            K = run_adaptive(systems[s], g, {'ahc': AHC(Efermi=ef)}, 'fp64', dev, nit)[1]
-            nkb += g.nk_per_block * len(K)
+        if nit:  # k-points as the server counts them: the grid, then per round 1% of it x (8^3 + 1)
+            run_refine_omega(systems[s], g, {'ahc': AHC(Efermi=ef)}, 'fp64', rounds=nit, dev_system=dev)
+            n = g.nk_per_block * g.nblocks
+            nkb += n + nit * max(1, int(round(0.01 * n))) * (8 ** 3 + 1)
         else:
             wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision='fp64', dev_system=dev)
             nkb += g.nk_per_block * g.nblocks
     torch.cuda.synchronize()
-    st.update({"workload": f"{nreq} AHC requests, Poisson arrivals at {rate:g}/s over {nsys} resident systems "
-                           "(num_wann log-uniform 8-128, seeded), grids 8^3-32^3, 0-3 refinement rounds each "
-                           "(reference policy), 201 E_F, mixed precision",
-               "offered_rate_per_s": rate, "plain_fp64_serial_kpoints_per_s": nkb / (time.perf_counter() - t0),
-               "plain_fp64_serial_sample": f"first {nbase} requests run one after the other"})
+    err = max(float(np.max(np.abs(a.wait()['ahc'].data - b.wait()['ahc'].data)) /
+                    np.max(np.abs(b.wait()['ahc'].data))) for a, b in zip(tickets[:4], cal[:4]))
+    st.update({"workload": f"{nreq} AHC requests over {nsys} resident systems (num_wann log-uniform 8-128, "
+                           "seeded), grids 16^3-32^3, 0-3 rounds of refinement around the top 1% |Omega| "
+                           "k-points (8^3 sub-grids), 201 E_F, mixed precision",
+               "capacity_requests_per_s": capacity, "offered_rate_per_s": rate, "offered_load": load,
+               "plain_fp64_serial_kpoints_per_s": nkb / (time.perf_counter() - t0),
+               "plain_fp64_serial_sample": f"first {nbase} requests run one after the other",
+               "same_request_repeat_max_rel_diff": err})
     return st
 
 
@@ -825,9 +881,15 @@ def main():
     ap.add_argument('--tetra-nkdiv', type=int, default=NKDIV, help='NKdiv of --tetra-only')
     ap.add_argument('--no-graphs-tune', action='store_true', help='skip the CUDA-graph and autotuner measurements')
     ap.add_argument('--graphs-tune-only', action='store_true', help='run only the CUDA-graph and autotuner measurements')
+    ap.add_argument('--rotation-engines', type=int, default=0, metavar='NK',
+                    help='only time the nw = 32 rotation engines (tensor cores: warp-specialised and one tile at '
+                         'a time; CUDA cores) on NK synthetic k-points of the AHC field set')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.rotation_engines:
+        print(json.dumps({"rotation_engines": bench_rotation_engines(args.rotation_engines, args.steps)}), flush=True)
+        return 0
     if args.graphs_tune_only:
         import torch
         from wbgpu import _lib

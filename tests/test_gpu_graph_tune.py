@@ -167,13 +167,15 @@ def test_rotate_engine_choice():
     ref = engine.rotate(torch.from_numpy(Q).cuda(), torch.from_numpy(Xh).cuda(), nf, sel, herm, nw, nk,
                         True)[0].cpu().numpy()
     U32, X32 = torch.from_numpy(Q).cuda().to(torch.complex64), torch.from_numpy(Xh).cuda().to(torch.complex64)
-    assert autotune.candidates(autotune.ROTATE_ENGINE, nw, 0) == [1, 2]
+    assert autotune.candidates(autotune.ROTATE_ENGINE, nw, 0) == [1, 2, 3]
     outs = []
-    for v in (1, 2):
+    for v in (1, 2, 3):
         autotune.set_value(autotune.ROTATE_ENGINE, nw, 0, v)
         outs.append(engine.rotate(U32, X32, nf, sel, herm, nw, nk, False)[0].cpu().numpy())
         assert _rel(outs[-1], ref) < 2e-6, v
-    assert not np.array_equal(outs[0], outs[1])  # two engines really ran
+    autotune.set_value(autotune.ROTATE_ENGINE, nw, 0, 0)
+    assert not np.array_equal(outs[0], outs[1])  # tensor and CUDA cores really ran
+    assert np.array_equal(outs[0], outs[2])  # the two tensor-core kernels do the same arithmetic
 
 
 def test_autotune_ensure_and_run(systems, tmp_path, monkeypatch):

@@ -398,26 +398,36 @@ __global__ void __launch_bounds__(KG_THR, 1)
       for (int j = 0; j < 8; ++j) acck[i][j] = make_float2(0.f, 0.f);
     for (int r0 = 0; r0 < nrec; r0 += KG_RC) {
       const int rn = min(KG_RC, nrec - r0);
+      // the chunk's loads all issued before any is used (one memory latency per chunk)
+      constexpr int PF = KG_RC * KG_TW / KG_THR, PG = KG_RC * KG_TC / KG_THR;
+      double dEv[PF], omv[PF];
+      float fev[PG];
+      float2 mv[PG];
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int idx = q * KG_THR + tid, r = idx / KG_TW, w = idx % KG_TW;
+        const bool ok = r < rn && w0 + w < kp.nOmega;
+        dEv[q] = ok ? __ldg(rec_dE + rbase + r0 + r) : 0.0;
+        omv[q] = ok ? __ldg(omega + w0 + w) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < PG; ++q) {
+        const int idx = q * KG_THR + tid, r = idx / KG_TC, col = col0 + idx % KG_TC;
+        const bool ok = r < rn && col < ncol;
+        const int e = col / NC, c = col - e * NC;
+        const long long rr = rbase + r0 + r;
+        fev[q] = ok ? __ldg(rec_fE + rr * kp.nEF + e) : 0.f;
+        mv[q] = ok ? __ldg(rec_M + rr * NC + c) : make_float2(0.f, 0.f);
+      }
       __syncthreads();  // the previous chunk's tiles are read
-      for (int idx = tid; idx < KG_RC * KG_TW; idx += KG_THR) {
-        const int r = idx / KG_TW, w = idx % KG_TW;
-        float2 v = make_float2(0.f, 0.f);
-        if (r < rn && w0 + w < kp.nOmega)
-          v = factor_omega<float>(fgroup, __ldg(rec_dE + rbase + r0 + r), __ldg(omega + w0 + w), eta, kp.gaussian);
-        Fs[idx] = v;
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int idx = q * KG_THR + tid, r = idx / KG_TW, w = idx % KG_TW;
+        Fs[idx] = (r < rn && w0 + w < kp.nOmega) ? factor_omega<float>(fgroup, dEv[q], omv[q], eta, kp.gaussian)
+                                                 : make_float2(0.f, 0.f);
       }
-      for (int idx = tid; idx < KG_RC * KG_TC; idx += KG_THR) {
-        const int r = idx / KG_TC, col = col0 + idx % KG_TC;
-        float2 v = make_float2(0.f, 0.f);
-        if (r < rn && col < ncol) {
-          const int e = col / NC, c = col - e * NC;
-          const long long rr = rbase + r0 + r;
-          const float fe = __ldg(rec_fE + rr * kp.nEF + e);
-          const float2 m = __ldg(rec_M + rr * NC + c);
-          v = make_float2(fe * m.x, fe * m.y);
-        }
-        Gs[idx] = v;
-      }
+#pragma unroll
+      for (int q = 0; q < PG; ++q) Gs[q * KG_THR + tid] = make_float2(fev[q] * mv[q].x, fev[q] * mv[q].y);
       __syncthreads();
       float2 acc[4][8];
 #pragma unroll
@@ -581,7 +591,8 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
     WBG_ACCUM(1, float);
   } else {  // the register-tiled GEMM: one block per SM, frequency x column tiles x k chunks
     const int gw = (kp->nOmega + KG_TW - 1) / KG_TW, gc = (kp->nEF * nc + KG_TC - 1) / KG_TC;
-    int gk = (sms + gw * gc - 1) / (gw * gc);
+    int gk = sms / (gw * gc);  // one wave of one block per SM
+    if (gk < 1) gk = 1;
     if (gk > nk) gk = nk;
     const int kc = (nk + gk - 1) / gk;
     gk = (nk + kc - 1) / kc;

@@ -117,24 +117,97 @@ WBG_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::
 // hint: bring the 128-byte line holding p into L2 (no register result, no fault semantics)
 WBG_D void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+// Asynchronous 16-byte global -> shared copies (no registers held, no waits between them)
+WBG_D void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+WBG_D void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+// The X rows of one tile (FPT fields of NW x NW complex) copied as they are into `raw`
+// ([field slot][m][n] float2, FPT * NW * NW * 8 bytes): every copy of the tile is in flight at
+// once; slots of padding or of an invalid selection are not copied (the reader fills them).
+// Thread `i` of `nthr` takes every nthr-th 16-byte piece.
+WBG_D void stage_tile_raw(float2* raw, const float2* X, long long k, int nFin, const int* code, int i, int nthr) {
+  constexpr int PIECES = NW * NW / 2;  // 16-byte pieces per field
+  for (int c = i; c < FPT * PIECES; c += nthr) {
+    const int fl = c / PIECES, pc = c % PIECES;
+    const int cd = code[fl];
+    if (cd < 0) continue;
+    const float2* Xf = X + (k * nFin + (cd & 0x3fffffff)) * (long long)(NW * NW);
+    cp_async16(raw + fl * NW * NW + 2 * pc, Xf + 2 * pc);
+  }
+}
+
+// Elements n0..n0+3 of row m of slot fl from the raw copy: a field given by its lower triangle is
+// read as the Hermitian matrix it stands for (X[m][n] = conj(X[n][m]) above the diagonal, real
+// diagonal); padding reads 0, an invalid selection NaN.
+WBG_D void tile_chunk(const float2* raw, int code, int fl, int m, int n0, float2 (&v)[4]) {
+  if (code < 0) {
+    const float f = code == -2 ? __int_as_float(0x7fc00000) : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = make_float2(f, f);
+    return;
+  }
+  const bool lower = (code >> 30) != 0;
+  const float2* Xf = raw + fl * NW * NW;
+  const float4 a = *reinterpret_cast<const float4*>(Xf + m * NW + n0);
+  const float4 b = *reinterpret_cast<const float4*>(Xf + m * NW + n0 + 2);
+  v[0] = make_float2(a.x, a.y);
+  v[1] = make_float2(a.z, a.w);
+  v[2] = make_float2(b.x, b.y);
+  v[3] = make_float2(b.z, b.w);
+  if (lower && m <= n0 + 3) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int n = n0 + q;
+      if (m < n) {
+        const float2 w = Xf[n * NW + m];
+        v[q] = make_float2(w.x, -w.y);
+      } else if (m == n) {
+        v[q].y = 0.f;
+      }
+    }
+  }
+}
+
 WBG_D unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
+// Phase test of an mbarrier: the potentially blocking try_wait, or (WBG_TC_SPIN) the
+// non-blocking test_wait polled in a loop.
+#ifndef WBG_TC_SPIN
+#define WBG_TC_SPIN 0
+#endif
+WBG_D bool mbar_poll(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+#if WBG_TC_SPIN
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+#else
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+#endif
+  return ok != 0;
+}
+
 // Wait for phase `parity` of the mbarrier to complete, for at most limit_ns.
 WBG_D bool mbar_wait(uint32_t mbar, uint32_t parity, unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   while (true) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (ok) return true;
+    if (mbar_poll(mbar, parity)) return true;
     if (global_ns() - t0 > limit_ns) return false;
   }
 }
@@ -212,6 +285,8 @@ __global__ void __launch_bounds__(NTHR, 2)
   // tile map: full fields first, then the diagonal-only fields (herm 2); a tile holding only
   // diagonal-only fields stops after T = X U (diag(U^dagger T) by a reduction over the rows)
   __shared__ short tmap_s[TMAP_MAX];
+  __shared__ int code_s[TMAP_MAX];
+  __shared__ signed char hm_s[TMAP_MAX];
   __shared__ int nfull_s, ntiles_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mb = smem_u32(&mbar);
@@ -225,6 +300,18 @@ __global__ void __launch_bounds__(NTHR, 2)
     for (int i = 0; i < nt * FPT; ++i) tmap_s[i] = -1;
     int a = 0, b = nf;
     for (int f = 0; f < nFrot; ++f) tmap_s[(herm[f] & 3) == 2 ? b++ : a++] = (short)f;
+    // per slot: -1 padding, -2 invalid selection, else source field | lower-triangle input << 30;
+    // the output mode herm & 3 (the selection lives in device memory: validated here, once)
+    for (int i = 0; i < nt * FPT; ++i) {
+      const int f = tmap_s[i];
+      int c = -1;
+      if (f >= 0) {
+        const int fs = fsel[f];
+        c = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
+      }
+      code_s[i] = c;
+      hm_s[i] = (signed char)(f >= 0 ? (herm[f] & 3) : 0);
+    }
     nfull_s = (nf + FPT - 1) / FPT;  // tiles from here on hold diagonal-only fields and padding
     ntiles_s = nt;
   }
@@ -265,62 +352,25 @@ __global__ void __launch_bounds__(NTHR, 2)
     for (int t = 0; t < ntiles; ++t) {
       // ---- A1: rows (fl, m) of the tile's fields, K = [Re X[m][:] | Im X[m][:]].
       // A task is 4 consecutive elements n0..n0+3 of one row: a 16-byte store per operand half.
-      // A field given by its lower triangle is read as the Hermitian matrix it stands for
-      // (X[m][n] = conj(X[n][m]) above the diagonal, real diagonal).  Every load of the tile
-      // is issued before the first store.
+      // The tile's rows arrive as a raw copy in the lo half of the operand buffer (all copies in
+      // flight at once), every thread takes its chunks from there, then writes hi / lo.
       {
         constexpr int CPR = NW / 4;              // tasks per row
         constexpr int PER = FPT * NW * CPR / NTHR;
-        float2 xv[PER][4];
+        float2* raw = reinterpret_cast<float2*>(Al);
         int code[FPT];  // per field: -1 padding, -2 invalid selection, else source field | lower << 30
 #pragma unroll
-        for (int fl = 0; fl < FPT; ++fl) {
-          const int f = tmap_s[t * FPT + fl];
-          if (f < 0) {
-            code[fl] = -1;
-          } else {
-            const int fs = fsel[f];  // selection lives in device memory: validate here
-            code[fl] = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
-          }
-        }
+        for (int fl = 0; fl < FPT; ++fl) code[fl] = code_s[t * FPT + fl];
+        stage_tile_raw(raw, X, k, nFin, code, tid, NTHR);
+        cp_async_wait_all();
+        __syncthreads();
+        float2 xv[PER][4];
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
           const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
-          const int c = code[fl];
-          const bool lower = c >= 0 && (c >> 30);
-          const float2* Xf = X + (k * nFin + (c >= 0 ? (c & 0x3fffffff) : 0)) * (long long)(NW * NW);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) xv[i][q] = make_float2(0.f, 0.f);
-          if (c == -2) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) xv[i][q] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-          } else if (c >= 0) {
-            if (!lower || m >= n0 + 3) {  // the whole chunk is stored: two 16-byte loads
-              const float4* src = reinterpret_cast<const float4*>(Xf + m * NW + n0);
-              const float4 a = src[0], b = src[1];
-              xv[i][0] = make_float2(a.x, a.y);
-              xv[i][1] = make_float2(a.z, a.w);
-              xv[i][2] = make_float2(b.x, b.y);
-              xv[i][3] = make_float2(b.z, b.w);
-            } else {
-#pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                const int n = n0 + q;
-                if (m >= n) {
-                  xv[i][q] = Xf[m * NW + n];
-                } else {
-                  const float2 u = Xf[n * NW + m];
-                  xv[i][q] = make_float2(u.x, -u.y);
-                }
-              }
-            }
-            if (lower && m >= n0 && m < n0 + 4) {  // real diagonal
-#pragma unroll
-              for (int q = 0; q < 4; ++q)
-                if (n0 + q == m) xv[i][q].y = 0.f;
-            }
-          }
+          tile_chunk(raw, code[fl], fl, m, n0, xv[i]);
         }
+        __syncthreads();  // the raw copy is read: its space takes the lo operand
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
           const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
@@ -349,11 +399,9 @@ __global__ void __launch_bounds__(NTHR, 2)
           for (int i = 0; i < PER; ++i) {
             const int e = i * NTHR + tid, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
             if ((n0 & 15) != 0) continue;  // one prefetch per 128-byte line (16 complex floats)
-            const int f = tmap_s[tn * FPT + fl];
-            if (f < 0) continue;
-            const int fs = fsel[f];
-            if (fs < 0 || fs >= nFin) continue;
-            prefetch_l2(X + (kn * nFin + fs) * (long long)(NW * NW) + m * NW + n0);
+            const int c = code_s[tn * FPT + fl];
+            if (c < 0) continue;
+            prefetch_l2(X + (kn * nFin + (c & 0x3fffffff)) * (long long)(NW * NW) + m * NW + n0);
           }
         }
       }
@@ -415,7 +463,7 @@ __global__ void __launch_bounds__(NTHR, 2)
       tc_fence_after();
       {  // ---- D2 -> Xbar: thread (field q, row m) holds Y^H[m][n] for n in its column half
         const int f = tmap_s[t * FPT + quarter];
-        const int hm = f >= 0 ? (herm[f] & 3) : 0;
+        const int hm = hm_s[t * FPT + quarter];
         float2* dst = Xbar + (k * nFrot + (f >= 0 ? f : 0)) * (long long)(NW * NW);
         float re[16], im[16];
         tmem_cols16(D2 + lane_base, 16 * half, re);
@@ -457,19 +505,44 @@ __global__ void __launch_bounds__(NTHR, 2)
 // ---------------------------------------------------------------------------------------
 // Warp-specialised form of the same rotation (one CTA per SM, two tiles in flight):
 //   warps 8-11  loaders: the embedded U of the next k-point into B[k % 2] and the X rows of
-//               the next tile into A[t % 2], split into TF32 hi / lo;
-//   warp 12     one thread issues GEMM1 (T = X U into TMEM D[t % 2]) and, once the epilogue
-//               has staged T^H, GEMM2 (Y^H = T^H U into the same columns);
+//               the next tile into A[t % 2] (a raw asynchronous copy, then split into TF32 hi / lo);
+//   warp 12     one thread issues, whichever is ready first, GEMM1 (T = X U into TMEM D[t % 2])
+//               of the next tile or GEMM2 (Y^H = T^H U into the same columns) of a tile whose
+//               T^H is staged;
 //   warps 0-7   epilogue: TMEM -> T^H (into A[t % 2], whose X rows GEMM1 has consumed), then
 //               TMEM -> Xbar (diagonal-only tiles: diag(U^dagger T) by a row reduction).
 // Buffers hand over through mbarriers (one phase per tile and buffer, so the parity of use u
 // of a buffer is u & 1); every wait is bounded in time (the abort path of rotate_tc_kernel: a
 // collective decision inside each role, the tensor memory freed only after the issued products
-// have completed).  While the epilogue turns tile t around, the loaders fill tile t + 1 and
-// GEMM1 of tile t + 1 runs after GEMM2 of tile t.
+// have completed).  While the epilogue turns tile t around, the loaders fill tile t + 1.
+// Measured on GB300 (nw = 32, 9 fields, 55 296 k-points): 4.5 ms against 3.9 ms for the
+// one-tile-at-a-time kernel with two CTAs per SM; an event trace shows each GEMM of 24
+// tcgen05.mma (M = 128, N = 64, K = 8) taking 1.3-1.8 us from issue to completion, so the MMA
+// stream of one CTA sets the pace and two CTAs' streams interleave better than one CTA's roles.
 // ---------------------------------------------------------------------------------------
-constexpr int PIPE_EPI = 256;                      // warps 0-7
-constexpr int PIPE_LD0 = 256, PIPE_LDN = 128;      // warps 8-11
+#ifndef WBG_TC_TRACE
+#define WBG_TC_TRACE 0
+#endif
+#if WBG_TC_TRACE
+// event timeline of CTA 0 (profiling builds only): tag << 56 | tile << 32 | ns since the first event
+__device__ unsigned long long g_tc_trace[8192];
+__device__ unsigned int g_tc_trace_n;
+__device__ unsigned long long g_tc_trace_t0;
+WBG_D void tc_trace(int tag, long long tile) {
+  if (blockIdx.x != 0 || tile >= 64) return;
+  const unsigned int i = atomicAdd(&g_tc_trace_n, 1u);
+  if (i < 8192) {
+    atomicCAS(&g_tc_trace_t0, 0ull, global_ns());
+    g_tc_trace[i] = ((unsigned long long)tag << 56) | ((unsigned long long)tile << 32) |
+                    ((global_ns() - g_tc_trace_t0) & 0xffffffffull);
+  }
+}
+#define TC_TRACE(tag, tile) tc_trace(tag, tile)
+#else
+#define TC_TRACE(tag, tile)
+#endif
+constexpr int PIPE_EPI = 256;                      // epilogue: warps 0-7
+constexpr int PIPE_LD0 = 256, PIPE_LDN = 128;      // loaders: warps 8-11
 constexpr int PIPE_MMA_WARP = 12;
 constexpr int PIPE_THR = 13 * 32;
 constexpr int PIPE_SMEM = 2 * (2 * B_BYTES) + 2 * (2 * A_BYTES);  // B[2] and A[2], hi and lo each
@@ -480,10 +553,12 @@ WBG_D void mbar_init(uint32_t mb) { asm volatile("mbarrier.init.shared::cta.b64 
 WBG_D void mbar_arrive(uint32_t mb) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mb) : "memory");
 }
-WBG_D bool mbar_test(uint32_t mb, uint32_t parity) {
+WBG_D bool mbar_test(uint32_t mb, uint32_t parity) { return mbar_poll(mb, parity); }
+// non-blocking phase test (the issue thread polls several barriers in turn)
+WBG_D bool mbar_test_nb(uint32_t mb, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
       : "r"(mb), "r"(parity)
@@ -527,6 +602,8 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
   __shared__ short tmap_s[TMAP_MAX];
+  __shared__ int code_s[TMAP_MAX];
+  __shared__ signed char hm_s[TMAP_MAX];
   __shared__ int nfull_s, ntiles_s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   auto bar = [&](int which, int b) { return smem_u32(&bar_s[2 * which + b]); };
@@ -541,6 +618,18 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
     for (int i = 0; i < nt * FPT; ++i) tmap_s[i] = -1;
     int a = 0, b = nf;
     for (int f = 0; f < nFrot; ++f) tmap_s[(herm[f] & 3) == 2 ? b++ : a++] = (short)f;
+    // per slot: -1 padding, -2 invalid selection, else source field | lower-triangle input << 30;
+    // the output mode herm & 3 (the selection lives in device memory: validated here, once)
+    for (int i = 0; i < nt * FPT; ++i) {
+      const int f = tmap_s[i];
+      int c = -1;
+      if (f >= 0) {
+        const int fs = fsel[f];
+        c = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
+      }
+      code_s[i] = c;
+      hm_s[i] = (signed char)(f >= 0 ? (herm[f] & 3) : 0);
+    }
     nfull_s = (nf + FPT - 1) / FPT;
     ntiles_s = nt;
   }
@@ -565,8 +654,6 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
     for (long long i = 0; i < nkc; ++i) {
       const long long k = blockIdx.x + i * gridDim.x;
       const int kb = (int)(i & 1);
-      bool ok = i < 2 || pipe_wait(bar(FREE_B, kb), (uint32_t)(((i >> 1) - 1) & 1), &abort_s, wait_ns);
-      if (named_any(1, PIPE_LDN, !ok || abort_s)) break;
       unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
       unsigned char* Bl = Bh + B_BYTES;
       {
@@ -575,6 +662,9 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
         float2 uv[PER];
 #pragma unroll
         for (int q = 0; q < PER; ++q) uv[q] = Uk[q * PIPE_LDN + lt];
+        // U_k's loads are in flight: now wait for its buffer (k-point i - 2 done)
+        const bool ok = i < 2 || pipe_wait(bar(FREE_B, kb), (uint32_t)(((i >> 1) - 1) & 1), &abort_s, wait_ns);
+        if (named_any(1, PIPE_LDN, !ok || abort_s)) break;
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
           const int e = q * PIPE_LDN + lt, j = e / NW, n = e % NW;
@@ -591,62 +681,29 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
       for (int t = 0; t < ntiles; ++t, ++tt) {
         const int b = (int)(tt & 1);
         const long long u = tt >> 1;
-        ok = u < 1 || pipe_wait(bar(FREE_T, b), (uint32_t)((u - 1) & 1), &abort_s, wait_ns);
-        if (named_any(1, PIPE_LDN, !ok || abort_s)) { stop = true; break; }
         unsigned char* Ah = Abuf + b * 2 * A_BYTES;
         unsigned char* Al = Ah + A_BYTES;
         constexpr int CPR = NW / 4;
         constexpr int PER = FPT * NW * CPR / PIPE_LDN;
-        float2 xv[PER][4];
         int code[FPT];
 #pragma unroll
-        for (int fl = 0; fl < FPT; ++fl) {
-          const int f = tmap_s[t * FPT + fl];
-          if (f < 0) {
-            code[fl] = -1;
-          } else {
-            const int fs = fsel[f];
-            code[fl] = (fs >= 0 && fs < nFin) ? (fs | ((herm[f] & 4) ? (1 << 30) : 0)) : -2;
-          }
-        }
+        for (int fl = 0; fl < FPT; ++fl) code[fl] = code_s[t * FPT + fl];
+        const bool ok = u < 1 || pipe_wait(bar(FREE_T, b), (uint32_t)((u - 1) & 1), &abort_s, wait_ns);
+        if (named_any(1, PIPE_LDN, !ok || abort_s)) { stop = true; break; }
+        if (lt == 0) TC_TRACE(2, tt);
+        // the tile's rows as a raw copy in the lo half of its buffer, all copies in flight at once
+        float2* raw = reinterpret_cast<float2*>(Al);
+        stage_tile_raw(raw, X, k, nFin, code, lt, PIPE_LDN);
+        cp_async_wait_all();
+        named_sync(1, PIPE_LDN);
+        if (lt == 0) TC_TRACE(1, tt);
+        float2 xv[PER][4];
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
           const int e = q * PIPE_LDN + lt, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
-          const int c = code[fl];
-          const bool lower = c >= 0 && (c >> 30);
-          const float2* Xf = X + (k * nFin + (c >= 0 ? (c & 0x3fffffff) : 0)) * (long long)(NW * NW);
-#pragma unroll
-          for (int r = 0; r < 4; ++r) xv[q][r] = make_float2(0.f, 0.f);
-          if (c == -2) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) xv[q][r] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-          } else if (c >= 0) {
-            if (!lower || m >= n0 + 3) {
-              const float4* src = reinterpret_cast<const float4*>(Xf + m * NW + n0);
-              const float4 a = src[0], bb = src[1];
-              xv[q][0] = make_float2(a.x, a.y);
-              xv[q][1] = make_float2(a.z, a.w);
-              xv[q][2] = make_float2(bb.x, bb.y);
-              xv[q][3] = make_float2(bb.z, bb.w);
-            } else {
-#pragma unroll
-              for (int r = 0; r < 4; ++r) {
-                const int n = n0 + r;
-                if (m >= n) {
-                  xv[q][r] = Xf[m * NW + n];
-                } else {
-                  const float2 w = Xf[n * NW + m];
-                  xv[q][r] = make_float2(w.x, -w.y);
-                }
-              }
-            }
-            if (lower && m >= n0 && m < n0 + 4) {
-#pragma unroll
-              for (int r = 0; r < 4; ++r)
-                if (n0 + r == m) xv[q][r].y = 0.f;
-            }
-          }
+          tile_chunk(raw, code[fl], fl, m, n0, xv[q]);
         }
+        named_sync(1, PIPE_LDN);  // the raw copy is read: its space takes the lo operand
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
           const int e = q * PIPE_LDN + lt, fl = e / (NW * CPR), m = (e / CPR) % NW, n0 = (e % CPR) * 4;
@@ -656,130 +713,162 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
         }
         fence_async_smem();
         named_sync(1, PIPE_LDN);
-        if (lt == 0) mbar_arrive(bar(FULL_A1, b));
+        if (lt == 0) {
+          TC_TRACE(3, tt);
+          mbar_arrive(bar(FULL_A1, b));
+        }
       }
       if (stop) break;
     }
   } else if (warp == PIPE_MMA_WARP) {
     // ================= MMA issue (one thread) =================
     if (lane == 0) {
+      volatile int* ab = &abort_s;
       uint32_t last_bar = 0, last_par = 0;
-      for (long long tt = 0; tt < ntt; ++tt) {
-        const long long i = tt / ntiles;
-        const int t = (int)(tt % ntiles), kb = (int)(i & 1), b = (int)(tt & 1);
-        const long long u = tt >> 1;
-        const bool diag = t >= nfull;
-        if (t == 0 && !pipe_wait(bar(FULL_B, kb), (uint32_t)((i >> 1) & 1), &abort_s, wait_ns)) break;
-        if (u >= 1 && !pipe_wait(bar(FREE_T, b), (uint32_t)((u - 1) & 1), &abort_s, wait_ns)) break;
-        if (!pipe_wait(bar(FULL_A1, b), (uint32_t)(u & 1), &abort_s, wait_ns)) break;
-        tc_fence_after();
-        const unsigned char* Ah = Abuf + b * 2 * A_BYTES;
-        const unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
-        const uint32_t D = tbase + (uint32_t)b * 256;
-        issue_gemm(D, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
-        mma_commit(bar(MMA1, b));
-        last_bar = bar(MMA1, b);
-        last_par = (uint32_t)(u & 1);
-        if (!pipe_wait(bar(FULL_A2, b), (uint32_t)(u & 1), &abort_s, wait_ns)) break;
-        tc_fence_after();
-        if (!diag) issue_gemm(D, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
-        mma_commit(bar(MMA2, b));
-        last_bar = bar(MMA2, b);
-        if (t == ntiles - 1) mma_commit(bar(FREE_B, kb));
+      long long g1 = 0, g2 = 0;  // next tile for GEMM1, for GEMM2
+      unsigned long long t0 = global_ns();
+      while (g2 < ntt && !*ab) {
+        bool progress = false;
+        if (g1 < ntt) {
+          const long long i = g1 / ntiles, u = g1 >> 1;
+          const int t = (int)(g1 % ntiles), kb = (int)(i & 1), b = (int)(g1 & 1);
+          const bool ready = (t != 0 || mbar_test_nb(bar(FULL_B, kb), (uint32_t)((i >> 1) & 1))) &&
+                             (u < 1 || mbar_test_nb(bar(FREE_T, b), (uint32_t)((u - 1) & 1))) &&
+                             mbar_test_nb(bar(FULL_A1, b), (uint32_t)(u & 1));
+          if (ready) {
+            tc_fence_after();
+            TC_TRACE(4, g1);
+            const unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+            const unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
+            issue_gemm(tbase + (uint32_t)b * 256, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
+            mma_commit(bar(MMA1, b));
+            last_bar = bar(MMA1, b);
+            last_par = (uint32_t)(u & 1);
+            ++g1;
+            progress = true;
+          }
+        }
+        if (g2 < g1) {
+          const long long i = g2 / ntiles, u = g2 >> 1;
+          const int t = (int)(g2 % ntiles), kb = (int)(i & 1), b = (int)(g2 & 1);
+          if (mbar_test_nb(bar(FULL_A2, b), (uint32_t)(u & 1))) {
+            tc_fence_after();
+            TC_TRACE(5, g2);
+            const unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+            const unsigned char* Bh = Bbuf + kb * 2 * B_BYTES;
+            if (t < nfull) issue_gemm(tbase + (uint32_t)b * 256, Ah, Ah + A_BYTES, Bh, Bh + B_BYTES);
+            mma_commit(bar(MMA2, b));
+            last_bar = bar(MMA2, b);
+            last_par = (uint32_t)(u & 1);
+            if (t == ntiles - 1) mma_commit(bar(FREE_B, kb));
+            ++g2;
+            progress = true;
+          }
+        }
+        if (progress) {
+          t0 = global_ns();
+        } else if (global_ns() - t0 > wait_ns) {
+          *ab = 1;
+          atomicOr(&g_wbg_device_flags, (unsigned)WBG_DEVICE_FLAG_TC_TIMEOUT);
+        }
       }
-      if (abort_s && last_bar) mbar_wait(last_bar, last_par, DRAIN_NS);  // no product in flight at exit
+      if (*ab && last_bar) mbar_wait(last_bar, last_par, DRAIN_NS);  // no product in flight at exit
     }
   } else if (warp < 8) {
     // ================= epilogue =================
-    const int quarter = warp & 3, half = warp >> 2;
+    const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter (= field of the tile), column half
     const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
-    long long tt = 0;
-    bool stop = false;
-    for (long long i = 0; i < nkc && !stop; ++i) {
+    for (long long tt = 0; tt < ntt; ++tt) {
+      const long long i = tt / ntiles, u = tt >> 1;
+      const int t = (int)(tt % ntiles), b = (int)(tt & 1);
       const long long k = blockIdx.x + i * gridDim.x;
-      for (int t = 0; t < ntiles; ++t, ++tt) {
-        const int b = (int)(tt & 1);
-        const long long u = tt >> 1;
-        const bool diag = t >= nfull;
-        unsigned char* Ah = Abuf + b * 2 * A_BYTES;
-        unsigned char* Al = Ah + A_BYTES;
-        const uint32_t D = tbase + (uint32_t)b * 256;
-        bool ok = pipe_wait(bar(MMA1, b), (uint32_t)(u & 1), &abort_s, wait_ns);
-        if (named_any(2, PIPE_EPI, !ok || abort_s)) { stop = true; break; }
-        tc_fence_after();
-        const int f = tmap_s[t * FPT + quarter];
-        if (diag) {  // diag_n = Re sum_m conj(U_mn) T_mn
-          float re[16], im[16];
-          tmem_cols16(D + lane_base, 16 * half, re);
-          tmem_cols16(D + lane_base, NW + 16 * half, im);
-          if (f >= 0) {
-            const float2* Um = U + k * strideU + lane * NW + 16 * half;
-            float sum[16];
+      const bool diag = t >= nfull;
+      unsigned char* Ah = Abuf + b * 2 * A_BYTES;
+      unsigned char* Al = Ah + A_BYTES;
+      const uint32_t D = tbase + (uint32_t)b * 256;
+      bool ok = pipe_wait(bar(MMA1, b), (uint32_t)(u & 1), &abort_s, wait_ns);
+      if (named_any(2, PIPE_EPI, !ok || abort_s)) break;
+      if (tid == 0) TC_TRACE(6, tt);
+      tc_fence_after();
+      const int f = tmap_s[t * FPT + quarter];
+      if (diag) {  // diag_n = Re sum_m conj(U_mn) T_mn
+        float re[16], im[16];
+        tmem_cols16(D + lane_base, 16 * half, re);
+        tmem_cols16(D + lane_base, NW + 16 * half, im);
+        if (f >= 0) {
+          const float2* Um = U + k * strideU + lane * NW + 16 * half;
+          float sum[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const float2 uu = Um[q];
-              sum[q] = uu.x * re[q] + uu.y * im[q];
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-              for (int q = 0; q < 16; ++q) sum[q] += __shfl_xor_sync(0xffffffffu, sum[q], off);
-            float v = 0.f;
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-              if (q == lane) v = sum[q];
-            if (lane < 16) {
-              const int n = 16 * half + lane;
-              Xbar[(k * nFrot + f) * (long long)(NW * NW) + n * NW + n] = make_float2(v, 0.f);
-            }
+          for (int q = 0; q < 16; ++q) {
+            const float2 uu = Um[q];
+            sum[q] = uu.x * re[q] + uu.y * im[q];
           }
-        } else {  // T -> A2 = T^H (rows of field q, K blocks Re | -Im)
-          const int row0 = quarter * NW;
 #pragma unroll
-          for (int c = 0; c < 2; ++c) {
-            float v[16];
-            tmem_cols16(D + lane_base, NW * half + 16 * c, v);
+          for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-            for (int q = 0; q < 16; ++q)
-              put_split(Ah, Al, op_off(row0 + 16 * c + q, NW * half + lane), half ? -v[q] : v[q]);
+            for (int q = 0; q < 16; ++q) sum[q] += __shfl_xor_sync(0xffffffffu, sum[q], off);
+          float v = 0.f;
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            if (q == lane) v = sum[q];
+          if (lane < 16) {
+            const int n = 16 * half + lane;
+            Xbar[(k * nFrot + f) * (long long)(NW * NW) + n * NW + n] = make_float2(v, 0.f);
           }
         }
-        tc_fence_before();
-        fence_async_smem();
-        named_sync(2, PIPE_EPI);
-        if (tid == 0) mbar_arrive(bar(FULL_A2, b));
-        ok = pipe_wait(bar(MMA2, b), (uint32_t)(u & 1), &abort_s, wait_ns);
-        if (named_any(2, PIPE_EPI, !ok || abort_s)) { stop = true; break; }
-        tc_fence_after();
-        if (!diag) {  // Y^H -> Xbar (Hermitian part staged in the tile's A buffer: GEMM2 has read it)
-          const int hm = f >= 0 ? (herm[f] & 3) : 0;
-          float2* dst = Xbar + (k * nFrot + (f >= 0 ? f : 0)) * (long long)(NW * NW);
-          float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
-          float re[16], im[16];
-          tmem_cols16(D + lane_base, 16 * half, re);
-          tmem_cols16(D + lane_base, NW + 16 * half, im);
-          if (f >= 0) {
+      } else {  // T -> A2 = T^H (rows of field q, K blocks Re | -Im)
+        const int row0 = quarter * NW;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int n = 16 * half + q;
-              if (hm == 0) dst[n * NW + lane] = make_float2(re[q], -im[q]);
-              else if (hm == 2) { if (n == lane) dst[n * NW + n] = make_float2(re[q], 0.f); }
-              else stage[lane * STAGE_LD + n] = make_float2(re[q], im[q]);
-            }
-          }
-          named_sync(2, PIPE_EPI);
-          if (f >= 0 && hm == 1) {
+        for (int c = 0; c < 2; ++c) {
+          float v[16];
+          tmem_cols16(D + lane_base, NW * half + 16 * c, v);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int n = 16 * half + q;
-              const float2 a = stage[lane * STAGE_LD + n], bb = stage[n * STAGE_LD + lane];
-              dst[n * NW + lane] = make_float2(0.5f * (a.x + bb.x), -0.5f * (a.y - bb.y));
-            }
+          for (int q = 0; q < 16; ++q)
+            put_split(Ah, Al, op_off(row0 + 16 * c + q, NW * half + lane), half ? -v[q] : v[q]);
+        }
+      }
+      tc_fence_before();
+      fence_async_smem();
+      named_sync(2, PIPE_EPI);
+      if (tid == 0) {
+        TC_TRACE(7, tt);
+        mbar_arrive(bar(FULL_A2, b));
+      }
+      ok = pipe_wait(bar(MMA2, b), (uint32_t)(u & 1), &abort_s, wait_ns);
+      if (named_any(2, PIPE_EPI, !ok || abort_s)) break;
+      if (tid == 0) TC_TRACE(8, tt);
+      tc_fence_after();
+      if (!diag) {  // Y^H -> Xbar (Hermitian part staged in the tile's A buffer: GEMM2 has read it)
+        const int hm = hm_s[t * FPT + quarter];
+        float2* dst = Xbar + (k * nFrot + (f >= 0 ? f : 0)) * (long long)(NW * NW);
+        float2* stage = reinterpret_cast<float2*>(Ah) + quarter * NW * STAGE_LD;
+        float re[16], im[16];
+        tmem_cols16(D + lane_base, 16 * half, re);
+        tmem_cols16(D + lane_base, NW + 16 * half, im);
+        if (f >= 0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int n = 16 * half + q;
+            if (hm == 0) dst[n * NW + lane] = make_float2(re[q], -im[q]);
+            else if (hm == 2) { if (n == lane) dst[n * NW + n] = make_float2(re[q], 0.f); }
+            else stage[lane * STAGE_LD + n] = make_float2(re[q], im[q]);
           }
         }
-        tc_fence_before();
-        named_sync(2, PIPE_EPI);
-        if (tid == 0) mbar_arrive(bar(FREE_T, b));
+        named_sync(2, PIPE_EPI);  // both column halves of every field are staged
+        if (f >= 0 && hm == 1) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int n = 16 * half + q;
+            const float2 a = stage[lane * STAGE_LD + n], bb = stage[n * STAGE_LD + lane];
+            dst[n * NW + lane] = make_float2(0.5f * (a.x + bb.x), -0.5f * (a.y - bb.y));
+          }
+        }
+      }
+      tc_fence_before();
+      named_sync(2, PIPE_EPI);
+      if (tid == 0) {
+        TC_TRACE(9, tt);
+        mbar_arrive(bar(FREE_T, b));
       }
     }
   }
@@ -836,6 +925,22 @@ int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin,
                                                                 fsel, herm, nFrot, (float2*)Xbar, nk);
   return wbg_cuda_status(cudaGetLastError());
 }
+
+#if WBG_TC_TRACE
+extern "C" int wbg_tc_trace_read(unsigned long long* out, unsigned int* n, int clear) {
+  if (cudaDeviceSynchronize() != cudaSuccess) return WBG_ERR_CUDA;
+  if (cudaMemcpyFromSymbol(n, g_tc_trace_n, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+  const unsigned int m = *n < 8192 ? *n : 8192;
+  if (m && cudaMemcpyFromSymbol(out, g_tc_trace, m * sizeof(unsigned long long)) != cudaSuccess) return WBG_ERR_CUDA;
+  if (clear) {
+    const unsigned int z = 0;
+    const unsigned long long z64 = 0;
+    cudaMemcpyToSymbol(g_tc_trace_n, &z, sizeof(z));
+    cudaMemcpyToSymbol(g_tc_trace_t0, &z64, sizeof(z64));
+  }
+  return WBG_OK;
+}
+#endif
 
 int wbg_tc_wait_limit_run(unsigned long long ns) {
   return wbg_cuda_status(cudaMemcpyToSymbol(g_tc_wait_ns, &ns, sizeof(ns)));

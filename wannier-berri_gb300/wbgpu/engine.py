@@ -123,14 +123,16 @@ class RGeometry:
         self.maxPairLen = int(np.diff(self.pair_start).max())
         self.maxSliceLen = int(np.diff(self.slice_start).max())
 
-    def phases(self, dKs, NKFFT):
-        """Per-axis tables exp(2 pi i R_d (j/N_d + dK_d)) for every block: list of 3 arrays
-        (nblocks, N_d, nr_d) complex128 (rvectors.py:467-468 with the FFT kernel of fft.py:179)."""
+    def phases(self, dKs, NKFFT, step=None):
+        """Per-axis tables exp(2 pi i R_d (j s_d + dK_d)) for every block, s_d = 1/N_d (the FFT
+        grid of fft.py:179, rvectors.py:467-468) or the per-axis `step` of a sub-grid (a block of
+        N_d points spaced by step_d): list of 3 arrays (nblocks, N_d, nr_d) complex128."""
         dKs = np.atleast_2d(dKs)
         out = []
         for d in range(3):
             Rd = self.rmin[d] + np.arange(self.nr[d])
-            k = np.arange(NKFFT[d])[None, :] / NKFFT[d] + dKs[:, d][:, None]     # (nb, N)
+            sd = 1.0 / NKFFT[d] if step is None else float(step[d])
+            k = np.arange(NKFFT[d])[None, :] * sd + dKs[:, d][:, None]     # (nb, N)
             out.append(np.exp(2j * np.pi * k[:, :, None] * Rd[None, None, :]))
         return out
 
@@ -295,39 +297,49 @@ class DeviceSystem:
     def side_stream(self):
         return self.workspace().side_stream()
 
-    def grid_phases(self, shifts, NKFFT, prec):
+    def grid_phases(self, shifts, NKFFT, prec, step=None, cache=True):
         """Device-resident per-axis phase tables for every block of a grid (built once per grid):
-        the three tables of one precision go up in one copy (from page-locked memory when large)."""
+        the three tables of one precision go up in one copy (from page-locked memory when large).
+        `step`: per-axis spacing of sub-grid blocks (RGeometry.phases).  cache=False: tables of
+        blocks used once (refinement sub-grids), not kept by the system: returns (tables, staging
+        buffer), the staging buffer to be kept alive until the copy has run."""
         shifts = np.ascontiguousarray(shifts, dtype=np.float64)
-        skey = (tuple(int(n) for n in NKFFT), hash(shifts.tobytes()), shifts.shape)
+        skey = (tuple(int(n) for n in NKFFT), hash(shifts.tobytes()), shifts.shape,
+                None if step is None else tuple(float(x) for x in step))
         key = ('phases',) + skey + (int(prec),)
+        if not cache:
+            return self._upload_phases(self.geom.phases(shifts, NKFFT, step), prec)
         if key not in self._cache:
             hkey = ('phases_host',) + skey
             if hkey not in self._cache:
-                self._cache[hkey] = self.geom.phases(shifts, NKFFT)
-            parts = []
-            for p in self._cache[hkey]:
-                if prec == PREC_DF64:
-                    parts.append(_df64_pairs(p))
-                else:
-                    parts.append(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64))
-            # one flat buffer of the tables' real words (float64 for FP64, float32 otherwise); every
-            # table starts on a multiple of its element size
-            words = [a.reshape(-1).view(np.float64 if a.dtype == np.complex128 else np.float32) for a in parts]
-            host = torch.from_numpy(np.concatenate(words))
-            if torch.cuda.is_available() and host.numel() * host.element_size() > (4 << 20):
-                host = host.pin_memory()  # large tables: asynchronous copy from page-locked memory
-            dev_flat = host.to(self.device, non_blocking=host.is_pinned())
-            tabs, off = [], 0
-            for a, w in zip(parts, words):
-                t = dev_flat[off:off + w.size]
-                off += w.size
-                if np.iscomplexobj(a):
-                    t = torch.view_as_complex(t.view(-1, 2))
-                tabs.append(t.view(a.shape))
+                self._cache[hkey] = self.geom.phases(shifts, NKFFT, step)
+            tabs, host = self._upload_phases(self._cache[hkey], prec)
             self._cache[key] = tabs
             self._cache[key + ('staging',)] = host  # page-locked source of the in-flight copy
         return self._cache[key]
+
+    def _upload_phases(self, tables, prec):
+        parts = []
+        for p in tables:
+            if prec == PREC_DF64:
+                parts.append(_df64_pairs(p))
+            else:
+                parts.append(p.astype(np.complex128 if prec == PREC_FP64 else np.complex64))
+        # one flat buffer of the tables' real words (float64 for FP64, float32 otherwise); every
+        # table starts on a multiple of its element size
+        words = [a.reshape(-1).view(np.float64 if a.dtype == np.complex128 else np.float32) for a in parts]
+        host = torch.from_numpy(np.concatenate(words))
+        if torch.cuda.is_available() and host.numel() * host.element_size() > (4 << 20):
+            host = host.pin_memory()  # large tables: asynchronous copy from page-locked memory
+        dev_flat = host.to(self.device, non_blocking=host.is_pinned())
+        tabs, off = [], 0
+        for a, w in zip(parts, words):
+            t = dev_flat[off:off + w.size]
+            off += w.size
+            if np.iscomplexobj(a):
+                t = torch.view_as_complex(t.view(-1, 2))
+            tabs.append(t.view(a.shape))
+        return tabs, host
 
     def wcc_tensor(self, fp64):
         k = ('wcc', fp64)

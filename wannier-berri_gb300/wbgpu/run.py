@@ -144,6 +144,171 @@ def run_adaptive(system, grid, calculators, precision, dev, adpt_num_iter, adpt_
     return ref.total(), np.array(ref.K), np.array(ref.dK), np.array(ref.fac)
 
 
+# ---------------------------------------------------------------------------------------
+# Refinement around the largest Berry curvatures: the top fraction of the k-points by
+# max_n |Omega_n(k)| get a mesh^3 sub-grid of their cell, round after round.
+# ---------------------------------------------------------------------------------------
+def subgrid_shifts(points, cell, mesh):
+    """Block shifts of mesh^3 sub-grids centred on `points` (n, 3) whose cells have edges `cell`
+    (3,): the sub-grid of k has the points k + (j - (mesh - 1) / 2) cell / mesh, j = 0..mesh-1 per
+    axis (the midpoints of the mesh^3 sub-cells), i.e. shift k - (mesh - 1) / 2 step and per-axis
+    step = cell / mesh.  Returns (shifts, step)."""
+    step = np.asarray(cell, dtype=float) / mesh
+    return np.asarray(points, dtype=float) - 0.5 * (mesh - 1) * step[None, :], step
+
+
+def block_points(shifts, NKFFT, step, index):
+    """Coordinates of the k-points `index` (flat: block-major, C order of the block's NKFFT points)
+    of blocks with `shifts` and per-axis `step`."""
+    nk = int(np.prod(NKFFT))
+    index = np.asarray(index, dtype=np.int64)
+    b, j = index // nk, index % nk
+    ijk = np.stack(np.unravel_index(j, tuple(int(n) for n in NKFFT)), axis=-1)
+    return np.asarray(shifts, dtype=float)[b] + ijk * np.asarray(step, dtype=float)[None, :]
+
+
+def _omega_scores(bd, degen_thresh):
+    """max over bands of |Omega_n(k)| (group-averaged Berry curvature, the tabulation kernel of
+    wbg_berry_tabulate) for every k-point of a batch."""
+    import ctypes
+    from . import _lib
+    from .engine import _ptr, _stream
+    tab = torch.empty((bd.nk_total, bd.nw, 7), dtype=torch.float64, device=bd.E.device)
+    ext = 1 if 'A' in bd.index else 0
+    st = _lib.load().wbg_berry_tabulate(_ptr(bd.E), _ptr(bd.Xbar), bd.Xbar.shape[1], bd.index['V'],
+                                        bd.index.get('A', 0), bd.index.get('Od', 0), bd.nw, bd.nk_total,
+                                        ctypes.c_double(degen_thresh), 1, ext, _ptr(tab), int(bd.fp64_fields),
+                                        _stream())
+    _lib.check(st, "wbg_berry_tabulate")
+    return tab[:, :, 4:7].norm(dim=2).amax(dim=1)
+
+
+def _evaluate_blocks(dev, system, shifts, NKFFT, step, calculators, quantities, precision, scores,
+                     degen_thresh=1e-4, cached_phases=True):
+    """Stages 1-3 and every calculator over blocks of NKFFT points (spacing `step`, None: 1/NKFFT)
+    at `shifts`; with `scores` the per-k Berry-curvature scores of the blocks in order (device)."""
+    nk = int(np.prod(NKFFT))
+    nb = choose_batch(dev.nw, nk, len(shifts), quantities, precision)
+    keep, phases = [], {}
+    for p in engine.phase_precs(precision):
+        if cached_phases:
+            phases[p] = dev.grid_phases(shifts, NKFFT, p, step=step)
+        else:
+            phases[p], host = dev.grid_phases(shifts, NKFFT, p, step=step, cache=False)
+            keep.append(host)
+    out, flags = [], []
+    for i0 in range(0, len(shifts), nb):
+        bd = engine.band_data(dev, shifts[i0:i0 + nb], NKFFT, quantities, precision, phases=phases, block_start=i0)
+        for c in calculators.values():
+            c.accumulate(bd, system)
+        if scores:
+            out.append(_omega_scores(bd, degen_thresh))
+        flags.append(bd._flag.clone())
+        del bd
+    engine.check_flags(flags)
+    return torch.cat(out) if scores else None
+
+
+class _Job:
+    """Blocks of one kind within a refinement round: NKFFT points spaced by `step` (None: the
+    FFT grid) at `shifts`, accumulated by `calcs`; their results enter with weight `factor` per
+    block of `nk` points and `sign`."""
+
+    def __init__(self, shifts, fft, step, calcs, scores, nk, factor, sign):
+        self.shifts, self.fft, self.step, self.calcs = np.asarray(shifts, dtype=float), tuple(fft), step, calcs
+        self.scores, self.nk, self.factor, self.sign = scores, nk, factor, sign
+
+
+class OmegaRefinement:
+    """Refinement around the largest Berry curvatures, round by round.  Round 0 is the grid; after
+    each round, top x (k-points of the grid) of its scored k-points (the grid's, then the previous
+    round's sub-grid points) with the largest max_n |Omega_n(k)| are each replaced by a mesh^3
+    sub-grid of their cell (subgrid_shifts): every round refines as many points as the first.  The result is the grid's sum with each refined point's value
+    replaced by the mean of its sub-grid: per refined point k of weight w (1/N for a point of the
+    grid of N k-points, w / mesh^3 one round further), w (mean over the sub-grid - value at k).
+    Refining every point (top = 1) gives the grid with mesh times more points per axis, shifted by
+    half a sub-cell.  jobs() lists the current round's blocks; end_round(scores) takes the
+    round's per-k scores (of the scored job, in block order) and plans the next round."""
+
+    def __init__(self, system, grid, calculators, device, rounds=1, top=0.01, mesh=8):
+        if any(getattr(c, 'tetra', False) for c in calculators.values()):
+            raise NotImplementedError("refinement around the largest Berry curvatures does not take tetra=True")
+        if not top > 0.0 or mesh < 1 or rounds < 0:
+            raise ValueError("top must be > 0 (refined points per round / points of the grid), mesh >= 1, "
+                             "rounds >= 0")
+        self.system, self.templates, self.device = system, calculators, device
+        self.rounds, self.top, self.mesh = int(rounds), float(top), int(mesh)
+        self.quantities = set()
+        for c in calculators.values():
+            self.quantities |= c.quantities(system)
+        ext = system.has_R_mat('AA') and not system.force_internal_terms_only
+        self.quantities |= {'V', 'A', 'Od'} if ext else {'V'}
+        fft = np.array(grid.FFT, dtype=int)
+        npts = fft * np.array(grid.div, dtype=int)
+        self.cell, self.weight = 1.0 / npts, 1.0 / float(np.prod(npts))
+        self.round = 0
+        self.total = {}
+        self._jobs = [_Job(grid.block_shifts(), fft, None, self._fresh(), self.rounds > 0, int(np.prod(fft)),
+                           1.0 / grid.nblocks, 1.0)]
+        self.kpoints = self.n_grid = grid.nblocks * int(np.prod(fft))
+
+    def _fresh(self):
+        cs = {k: copy.deepcopy(c) for k, c in self.templates.items()}
+        for c in cs.values():
+            c.reset(self.device)
+        return cs
+
+    def jobs(self):
+        return self._jobs
+
+    def end_round(self, scores):
+        """Add the round's results; plan the next round from `scores` (device tensor of the
+        scored job's k-points).  Returns True while a round is left."""
+        V = self.system.cell_volume
+        for job in self._jobs:
+            for k, c in job.calcs.items():
+                r = c.result(V, job.nk, job.factor) * job.sign
+                self.total[k] = r if k not in self.total else self.total[k] + r
+        if self.round >= self.rounds:
+            return False
+        scored = [j for j in self._jobs if j.scores][0]
+        n_top = min(scores.numel(), max(1, int(round(self.top * self.n_grid))))
+        sel = np.sort(torch.topk(scores, n_top).indices.cpu().numpy())
+        pts = block_points(scored.shifts, scored.fft, 1.0 / np.array(scored.fft) if scored.step is None
+                           else scored.step, sel)
+        sub_shifts, step = subgrid_shifts(pts, self.cell, self.mesh)
+        self.round += 1
+        m3 = (self.mesh,) * 3
+        self._jobs = [_Job(sub_shifts, m3, step, self._fresh(), self.round < self.rounds, self.mesh ** 3,
+                           self.weight, 1.0),
+                      _Job(pts, (1, 1, 1), None, self._fresh(), False, 1, self.weight, -1.0)]
+        self.kpoints += len(sub_shifts) * self.mesh ** 3 + len(pts)
+        self.cell, self.weight = step, self.weight / self.mesh ** 3
+        return True
+
+    def result(self):
+        return ResultDict(self.total)
+
+
+def run_refine_omega(system, grid, calculators, precision='mixed', rounds=1, top=0.01, mesh=8, dev_system=None,
+                     degen_thresh=1e-4):
+    """run() refined around the largest Berry curvatures (OmegaRefinement): `rounds` rounds, each
+    refining top x (points of the grid) of the previous round's k-points by mesh^3 sub-grids."""
+    engine.require_cuda()
+    dev = dev_system or engine.DeviceSystem(system)
+    ref = OmegaRefinement(system, grid, calculators, dev.device, rounds, top, mesh)
+    while True:
+        scores = None
+        for job in ref.jobs():
+            sc = _evaluate_blocks(dev, system, job.shifts, job.fft, job.step, job.calcs, ref.quantities, precision,
+                                  job.scores, degen_thresh, cached_phases=ref.round == 0)
+            if job.scores:
+                scores = sc
+        if not ref.end_round(scores):
+            break
+    return ref.result()
+
+
 def run(system, grid, calculators, precision='fp64', blocks_per_batch=None, device='cuda', dev_system=None,
         blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1, cuda_graph=False, autotune=False, **_ignored):
     """Integrate ``calculators`` over ``grid``.  precision: 'fp64' (plain) or 'mixed'

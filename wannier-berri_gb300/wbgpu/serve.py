@@ -18,6 +18,9 @@ one GPU and runs many integration requests at once:
 * A request with ``adpt_num_iter`` > 0 runs in rounds of adaptive refinement (run.Refinement,
   the reference's policy): each round's blocks get per-block results; when the round's event
   fires, the host selects and divides K-points and queues the next round on the same stream.
+* A request with ``refine_omega`` > 0 runs in rounds of refinement around the largest Berry
+  curvatures (run.OmegaRefinement): every batch also writes its k-points' max_n |Omega_n(k)|;
+  when a round's event fires, the host takes the top fraction and queues their sub-grids.
 
 No counterpart in the reference; the numerical path is exactly ``run()``'s.
 """
@@ -31,7 +34,7 @@ import torch
 
 from . import engine
 from .result import ResultDict
-from .run import Refinement, choose_batch
+from .run import OmegaRefinement, Refinement, _omega_scores, choose_batch
 
 
 def admit(pending_bytes, used_bytes, budget_bytes, free_slots):
@@ -97,11 +100,15 @@ class Ticket:
 
 
 class _Request:
-    def __init__(self, ticket, key, grid, calculators, blocks, adapt=None):
+    def __init__(self, ticket, key, grid, calculators, blocks, adapt=None, omega=None):
         self.ticket, self.key, self.grid, self.calculators = ticket, key, grid, calculators
         self.blocks = blocks
         self.adapt = adapt  # (adpt_num_iter, adpt_mesh, adpt_fac) or None
         self.refine = None  # run.Refinement of an adaptive request
+        self.omega = omega  # (rounds, top, mesh) of a refinement around the largest |Omega|, or None
+        self.oref = None  # its run.OmegaRefinement
+        self.ophases = None  # phase tables of the round's jobs (and their staging buffers)
+        self.score_parts = []
         self.shifts = None  # block shifts of the current round (adaptive requests)
         self.cells = None  # and their dense-grid cells
         self.round_calcs = []
@@ -164,21 +171,28 @@ class Server:
         self._systems[key] = (system, dev)
         return dev
 
-    def submit(self, key, grid, calculators, blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1):
+    def submit(self, key, grid, calculators, blocks=None, adpt_num_iter=0, adpt_mesh=2, adpt_fac=1, refine_omega=0,
+               refine_top=0.01, refine_mesh=8):
         """Queue an integration of `calculators` over `grid` (optionally a subset `blocks` of its
-        division-grid K-points, or with `adpt_num_iter` rounds of adaptive refinement) for the
-        system registered as `key`; returns a Ticket."""
+        division-grid K-points, with `adpt_num_iter` rounds of adaptive refinement, or with
+        `refine_omega` rounds of refinement around the largest Berry curvatures: the `refine_top`
+        fraction of the k-points by |Omega| refined by refine_mesh^3 sub-grids) for the system
+        registered as `key`; returns a Ticket."""
         if key not in self._systems:
             raise ValueError(f"unknown system {key!r}: add_system() first")
-        adapt = None
+        adapt = omega = None
         if adpt_num_iter:
             if blocks is not None:
                 raise ValueError("adaptive refinement runs over the whole grid (blocks must be None)")
             adapt = (adpt_num_iter, adpt_mesh, adpt_fac)
+        if refine_omega:
+            if blocks is not None or adapt is not None:
+                raise ValueError("refinement around |Omega| runs over the whole grid, without adpt_num_iter")
+            omega = (int(refine_omega), float(refine_top), int(refine_mesh))
         with self._lock:
             self._rid += 1
             t = Ticket(self._rid, key)
-            self._pending.append(_Request(t, key, grid, dict(calculators), blocks, adapt))
+            self._pending.append(_Request(t, key, grid, dict(calculators), blocks, adapt, omega))
         self._wake.set()
         return t
 
@@ -246,6 +260,12 @@ class Server:
         if req.adapt is not None:
             req.refine = Refinement(system, req.grid, req.calculators, *req.adapt)
             self._plan_round(req)
+        elif req.omega is not None:
+            with torch.cuda.stream(req.stream):  # its calculators' buffers belong to the request's stream
+                req.oref = OmegaRefinement(system, req.grid, req.calculators, self.device, *req.omega)
+            req.quantities = req.oref.quantities
+            req.ticket.nkpoints = 0
+            self._plan_oround(req)
         else:
             req.batches = [blocks[i:i + nb] for i in range(0, len(blocks), nb)]
             req.ticket.nkpoints = len(blocks) * req.grid.nk_per_block
@@ -270,6 +290,40 @@ class Server:
         req.next_batch = 0
         req.done_event = None
         req.ticket.nkpoints += n * req.grid.nk_per_block
+
+    def _plan_oround(self, req):
+        """Batches of the current round's jobs of a refinement around |Omega|: (job, blocks)."""
+        system, dev = self._systems[req.key]
+        req.batches, req.ophases = [], []
+        for j, job in enumerate(req.oref.jobs()):
+            n = len(job.shifts)
+            nb = choose_batch(dev.nw, job.nk, n, req.quantities, self.precision, max_kpoints=self.max_kpoints)
+            req.batches += [(j, np.arange(i, min(i + nb, n))) for i in range(0, n, nb)]
+            with torch.cuda.stream(req.stream):
+                if req.oref.round == 0:  # the grid itself: the system's cached tables
+                    req.ophases.append(req.phases)
+                else:
+                    tabs = {}
+                    for p in engine.phase_precs(self.precision):
+                        tabs[p], host = dev.grid_phases(job.shifts, job.fft, p, step=job.step, cache=False)
+                        tabs[(p, 'staging')] = host
+                    req.ophases.append(tabs)
+        req.ticket.nkpoints = req.oref.kpoints
+        req.next_batch = 0
+        req.done_event = None
+        req.score_parts = []
+
+    def _issue_omega(self, req, system, dev):
+        j, idx = req.batches[req.next_batch - 1]
+        job = req.oref.jobs()[j]
+        ph = {p: t for p, t in req.ophases[j].items() if not isinstance(p, tuple)}
+        bd = engine.band_data(dev, job.shifts[idx], job.fft, req.quantities, self.precision, phases=ph,
+                              block_start=int(idx[0]), ws=req.ws)
+        for c in job.calcs.values():
+            c.accumulate(bd, system)
+        if job.scores:
+            req.score_parts.append(_omega_scores(bd, 1e-4).clone())
+        return bd
 
     def _issue_adaptive(self, req, idx, system, dev):
         corners = None
@@ -302,11 +356,29 @@ class Server:
             return False
         return True
 
+    def _end_oround(self, req):
+        """A round of a refinement around |Omega| is done: add its results, plan the next."""
+        with torch.cuda.stream(req.stream):
+            scores = torch.cat(req.score_parts) if req.score_parts else None
+            more = req.oref.end_round(scores)
+        if more:
+            self._plan_oround(req)
+            return False
+        return True
+
     def _issue(self, req):
         system, dev = self._systems[req.key]
         idx = req.batches[req.next_batch]
         req.next_batch += 1
         shifts = req.grid.block_shifts()
+        if req.oref is not None:
+            with torch.cuda.stream(req.stream):
+                bd = self._issue_omega(req, system, dev)
+                req.flags.append(bd._flag.clone())
+                if req.next_batch == len(req.batches):
+                    req.done_event = torch.cuda.Event()
+                    req.done_event.record(req.stream)
+            return
         with torch.cuda.stream(req.stream):
             contiguous = np.all(np.diff(idx) == 1)
             stages = engine.band_data
@@ -340,6 +412,8 @@ class Server:
                 factor = 1.0 / req.grid.nblocks
                 if req.refine is not None:
                     res = req.refine.total()
+                elif req.oref is not None:
+                    res = req.oref.result()
                 else:
                     res = ResultDict({k: c.result(system.cell_volume, nk, factor)
                                       for k, c in req.calculators.items()})
@@ -379,9 +453,9 @@ class Server:
                     self._fail(req, e)
         for req in list(self._active):
             if req.next_batch == len(req.batches) and req.done_event.query():
-                if req.refine is not None:
+                if req.refine is not None or req.oref is not None:
                     try:
-                        if not self._end_round(req):
+                        if not (self._end_round(req) if req.refine is not None else self._end_oround(req)):
                             continue  # next refinement round queued on the same stream
                     except Exception as e:
                         self._fail(req, e)
