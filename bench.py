@@ -163,8 +163,9 @@ def config_dict(args):
 def dtype_of(precision):
     if precision == 'fp64':
         return "f64 / c128 throughout"
-    return ("f64 energies, gaps, scan; double-float (48-bit) H(k) and eigensolver; fp32 fields and "
-            "back-transform; 3xTF32 tensor-core rotation, fp32 accumulation")
+    return ("f64 energies, gaps, scan; double-float (48-bit) H(k), eigensolver and eigenvector back-transform "
+            "(U rounded to c64); double-float velocity transform (rounded to c64), other fields fp32 with "
+            "R-space hi+lo residuals; 3xTF32 tensor-core rotation, fp32 accumulation")
 
 
 # ---------------------------------------------------------------------------------------
@@ -595,6 +596,33 @@ def _oracle_rate(s, nkfft, calcs):
     return int(np.prod(nkfft)) / (time.perf_counter() - t0)
 
 
+def bench_kubo_block(nkfft):
+    """One NKFFT^3 block of the spinor nw = 96 model through run() (OpticalConductivity at 11 E_F x
+    400 frequencies, Lorentzian 0.05 eV, + AHC), mixed precision, after one warm-up block: wall
+    time and CUDA-event stage times."""
+    import torch
+    import wbgpu
+    from wbgpu import engine, models, System_R
+    from wbgpu.calculators import AHC, OpticalConductivity
+    ef3, om = np.linspace(-1, 1, 11), np.linspace(0, 4, 400)
+    s3 = System_R.from_dict(models.config_system(3))
+    g3 = wbgpu.Grid(s3, NKdiv=6, NKFFT=nkfft)
+    d3 = engine.DeviceSystem(s3)
+    mk3 = lambda: {'opt': OpticalConductivity(Efermi=ef3, omega=om, smr_fixed_width=0.05), 'ahc': AHC(Efermi=ef3)}
+    wbgpu.run(s3, g3, mk3(), precision='mixed', dev_system=d3, blocks=[5])
+    torch.cuda.synchronize()
+    timer = engine.StageTimer()
+    engine.set_timer(timer)
+    t0 = time.perf_counter()
+    wbgpu.run(s3, g3, mk3(), precision='mixed', dev_system=d3, blocks=[0])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    engine.set_timer(None)
+    stages = {k: sum(a.elapsed_time(b) for a, b in evs) for k, evs in timer.events.items()}
+    return {"nkfft": nkfft, "kpoints": nkfft ** 3, "ms": dt * 1e3, "kpoints_per_s": nkfft ** 3 / dt,
+            "stage_ms": stages}
+
+
 def bench_rotation_engines(nk, reps):
     """CUDA-event time of U^dagger X U at nw = 32 on `nk` synthetic k-points with the mixed AHC
     path's fields (V and A from lower triangles, V plain, A Hermitian part, rotA diagonal only) for
@@ -881,12 +909,18 @@ def main():
     ap.add_argument('--tetra-nkdiv', type=int, default=NKDIV, help='NKdiv of --tetra-only')
     ap.add_argument('--no-graphs-tune', action='store_true', help='skip the CUDA-graph and autotuner measurements')
     ap.add_argument('--graphs-tune-only', action='store_true', help='run only the CUDA-graph and autotuner measurements')
+    ap.add_argument('--kubo-only', type=int, default=0, metavar='NKFFT',
+                    help='only run the nw = 96 spinor model (OpticalConductivity at 11 E_F x 400 omega + AHC) over '
+                         'one NKFFT^3 block, mixed precision, with per-stage times (profiling captures)')
     ap.add_argument('--rotation-engines', type=int, default=0, metavar='NK',
                     help='only time the nw = 32 rotation engines (tensor cores: warp-specialised and one tile at '
                          'a time; CUDA cores) on NK synthetic k-points of the AHC field set')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.kubo_only:
+        print(json.dumps({"kubo_c3": bench_kubo_block(args.kubo_only)}), flush=True)
+        return 0
     if args.rotation_engines:
         print(json.dumps({"rotation_engines": bench_rotation_engines(args.rotation_engines, args.steps)}), flush=True)
         return 0
