@@ -810,27 +810,37 @@ def bench_served(nsys=16, nreq=120, load=0.7, nbase=24):
             t.wait(600)
     st = srv.stats(tickets)
     devs = {}
-    t0 = time.perf_counter()
-    nkb = 0
-    for s, nkdiv, nkfft, nit in reqs[:nbase]:
-        g = grid_of((s, nkdiv, nkfft))
-        dev = devs.setdefault(s, engine.DeviceSystem(systems[s]))
-        if nit:  # k-points as the server counts them: the grid, then per round 1% of it x (8^3 + 1)
-            run_refine_omega(systems[s], g, {'ahc': AHC(Efermi=ef)}, 'fp64', rounds=nit, dev_system=dev)
-            n = g.nk_per_block * g.nblocks
-            nkb += n + nit * max(1, int(round(0.01 * n))) * (8 ** 3 + 1)
-        else:
-            wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision='fp64', dev_system=dev)
-            nkb += g.nk_per_block * g.nblocks
-    torch.cuda.synchronize()
+    sample = [reqs[i] for i in sorted(rng.choice(nreq, size=min(nbase, nreq), replace=False))]
+
+    def serial(precision):
+        """The sample's requests one after the other through run() / run_refine_omega."""
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nkb = 0
+        for s, nkdiv, nkfft, nit in sample:
+            g = grid_of((s, nkdiv, nkfft))
+            dev = devs.setdefault(s, engine.DeviceSystem(systems[s]))
+            if nit:  # k-points as the server counts them: the grid, then per round 1% of it x (8^3 + 1)
+                run_refine_omega(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision, rounds=nit, dev_system=dev)
+                n = g.nk_per_block * g.nblocks
+                nkb += n + nit * max(1, int(round(0.01 * n))) * (8 ** 3 + 1)
+            else:
+                wbgpu.run(systems[s], g, {'ahc': AHC(Efermi=ef)}, precision=precision, dev_system=dev)
+                nkb += g.nk_per_block * g.nblocks
+        torch.cuda.synchronize()
+        return nkb / (time.perf_counter() - t0)
+
+    serial_mixed = serial('mixed')
+    serial_fp64 = serial('fp64')
     err = max(float(np.max(np.abs(a.wait()['ahc'].data - b.wait()['ahc'].data)) /
                     np.max(np.abs(b.wait()['ahc'].data))) for a, b in zip(tickets[:4], cal[:4]))
     st.update({"workload": f"{nreq} AHC requests over {nsys} resident systems (num_wann log-uniform 8-128, "
                            "seeded), grids 16^3-32^3, 0-3 rounds of refinement around the top 1% |Omega| "
                            "k-points (8^3 sub-grids), 201 E_F, mixed precision",
                "capacity_requests_per_s": capacity, "offered_rate_per_s": rate, "offered_load": load,
-               "plain_fp64_serial_kpoints_per_s": nkb / (time.perf_counter() - t0),
-               "plain_fp64_serial_sample": f"first {nbase} requests run one after the other",
+               "plain_fp64_serial_kpoints_per_s": serial_fp64, "mixed_serial_kpoints_per_s": serial_mixed,
+               "mixed_vs_fp64_serial": serial_mixed / serial_fp64,
+               "serial_sample": f"{len(sample)} random requests of the stream, one after the other",
                "same_request_repeat_max_rel_diff": err})
     return st
 

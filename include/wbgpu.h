@@ -61,6 +61,9 @@ typedef struct {
 
 int wbg_abi_version(void);
 const char* wbg_status_string(int status);
+/* The CUDA runtime's message for the error behind the most recent WBG_STATUS_CUDA_ERROR that any
+ * entry point returned in this process ("none" if there was none); no reference counterpart. */
+const char* wbg_last_cuda_error_string(void);
 
 /* ---- stage 1: R -> k --------------------------------------------------------------------
  * wbg_r2k_fields (once per system and field set): R-space arrays of the k-space fields,
@@ -137,14 +140,26 @@ int wbg_r2k_columns(const void* XF, int nfields, const int* cols, int ncols, con
  *         FP32 back-transform loses ~sqrt(nw) ulps.
  * mode | 64 | 128 (WBG_EIGH_DF64_VECTORS), modes 2, 3: as 64 with U kept in double-float complex
  *         (re.hi, re.lo, im.hi, im.lo floats per element, 16 bytes) for a double-float rotation.
+ * mode | 256 (WBG_EIGH_REFINE), modes 2, 3 with nw <= 32, eigenvectors: the whole solve in FP32
+ *         (H rounded to FP32), then one Ogita-Aishima refinement step against the double-float
+ *         (mode 3) or FP64 (mode 2) H, with a Rayleigh-Ritz step inside clusters of close
+ *         eigenvalues; U complex64.  Eigenvalues to ~1e-13 |H|, eigenvectors as accurate as
+ *         complex64 holds them.  Not with 8, 64 or 128.  With the two-stage split, the STAGE2
+ *         call reads H as well (the refinement), so H must still hold the matrices.
  * E [nk][nw] ascending (float64); U: matrix k at U + k*strideU, column n = eigenvector n.
- * errflag: device int, OR-ed with 1 when the QL iteration did not converge. */
+ * errflag: device int, OR-ed with 1 when the QL iteration did not converge, and (WBG_EIGH_REFINE)
+ *          with 4 when more than 8 eigenvalues of one matrix lay within 2^-8 max|lambda| of each
+ *          other in a run (re-diagonalised 8 at a time: exact where the run is exactly degenerate,
+ *          otherwise its eigenvalues keep the FP32 solve's accuracy), or when a matrix still needed
+ *          a correction above 2^-12 in its second refinement step (a matrix needing one above 2^-12
+ *          in the first step takes a second). */
 #define WBG_EIGH_LOWER 4
 #define WBG_EIGH_VALUES 8
 #define WBG_EIGH_STAGE1 16
 #define WBG_EIGH_STAGE2 32
 #define WBG_EIGH_PRECISE_VECTORS 64
 #define WBG_EIGH_DF64_VECTORS 128
+#define WBG_EIGH_REFINE 256
 int wbg_eigh_workspace_size(int nw, int nk, size_t* bytes);
 int wbg_eigh_batched(const void* H, long long strideH, int nw, int nk, double* E, void* U, long long strideU,
                      int mode, void* workspace, size_t workspace_bytes, int* errflag, void* stream);
@@ -445,7 +460,8 @@ int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double
  * A host-side table, per (parameter, variant, nw), of launch shapes that a tuner measured to be
  * fastest; 0 (the initial value) selects the built-in occupancy heuristic.  Parameters:
  *   WBG_TUNE_EIGH_TRIDIAG_GROUP  matrices per block of the tridiagonalisation   variant: eigh mode & 3,
- *                                4 for modes 2 / 3 with WBG_EIGH_PRECISE_VECTORS
+ *                                4 for modes 2 / 3 with WBG_EIGH_PRECISE_VECTORS,
+ *                                5 for modes 2 / 3 with WBG_EIGH_REFINE
  *   WBG_TUNE_EIGH_QL_BLOCK       matrices (threads) per block of the QL sweep   variant: eigh mode & 3
  *   WBG_TUNE_EIGH_VECTORS_GROUP  matrices per block of the inverse iteration and
  *                                back-transform                                variant: eigh mode & 3
@@ -453,6 +469,9 @@ int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double
  *   WBG_TUNE_ROTATE_ENGINE       1 tensor cores, warp-specialised (two tiles in flight), 2 CUDA
  *                                cores, 3 tensor cores one tile at a time (the built-in choice;
  *                                where they serve the case)                    variant: fp64
+ *   WBG_TUNE_KUBO_ENGINE         the mixed path's 9- and 27-component Kubo band sums: 1 tensor
+ *                                cores (the built-in choice), 2 CUDA-core register-tiled GEMM
+ *                                                                               variant 0, nw 1
  * wbg_tune_candidates lists the values that fit the launch limits of (parameter, nw, variant);
  * wbg_tune_set accepts 0 or one of them (else WBG_STATUS_BAD_ARGUMENT), so every launch shape
  * the table can select is one the kernels accept.  Results do not depend on the eigensolver and
@@ -464,7 +483,8 @@ int wbg_scan_finalize(const void* hist, int nEF, int ncomp, double scale, double
 #define WBG_TUNE_EIGH_VECTORS_GROUP 2
 #define WBG_TUNE_ROTATE_KPOINTS 3
 #define WBG_TUNE_ROTATE_ENGINE 4
-#define WBG_TUNE_NPARAM 5
+#define WBG_TUNE_KUBO_ENGINE 5
+#define WBG_TUNE_NPARAM 6
 int wbg_tune_candidates(int param, int nw, int variant, int* values, int capacity, int* count);
 int wbg_tune_set(int param, int nw, int variant, int value);
 int wbg_tune_get(int param, int nw, int variant, int* value);

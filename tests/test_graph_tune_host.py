@@ -51,12 +51,25 @@ def test_set_get_reject():
         assert autotune.get_value(p, nw, variant) == 0
     with pytest.raises(ValueError):
         autotune.set_value(autotune.ROTATE_ENGINE, 16, 0, 1)  # no tensor-core rotation at nw = 16
-    for args in [(-1, 8, 1, 0), (5, 8, 1, 0), (0, 0, 1, 0), (0, 129, 1, 0), (0, 8, 5, 0), (0, 8, 1, -1)]:
+    for args in [(-1, 8, 1, 0), (6, 8, 1, 0), (0, 0, 1, 0), (0, 129, 1, 0), (0, 8, 6, 0), (0, 8, 1, -1)]:
         with pytest.raises(ValueError):
             autotune.set_value(*args)
     autotune.set_value(autotune.EIGH_QL_BLOCK, 8, 1, 64)
     autotune.reset([8])
     assert autotune.get_value(autotune.EIGH_QL_BLOCK, 8, 1) == 0
+
+
+def test_kubo_engine_entry():
+    """The Kubo engine is one process-wide entry (variant 0, nw 1): 1 tensor cores, 2 CUDA cores."""
+    assert autotune.candidates(autotune.KUBO_ENGINE, 1, 0) == [1, 2]
+    assert autotune.candidates(autotune.KUBO_ENGINE, 2, 0) == []
+    for bad in [(1, 0, 3), (2, 0, 1), (1, 1, 1)]:
+        with pytest.raises(ValueError):
+            autotune.set_value(autotune.KUBO_ENGINE, *bad)
+    autotune.set_value(autotune.KUBO_ENGINE, 1, 0, 2)
+    assert autotune.get_value(autotune.KUBO_ENGINE, 1, 0) == 2
+    autotune.reset([1])
+    assert autotune.get_value(autotune.KUBO_ENGINE, 1, 0) == 0
 
 
 def test_exports_declared():

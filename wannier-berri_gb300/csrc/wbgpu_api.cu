@@ -7,9 +7,25 @@
 #include "wbgpu_kubo.cuh"
 #include "wbgpu_tetra.cuh"
 
+#include <atomic>
+
+namespace {
+std::atomic<int> g_last_cuda_error{0};
+}
+
+int wbg_note_cuda_error(cudaError_t e) {
+  g_last_cuda_error.store((int)e, std::memory_order_relaxed);
+  return WBG_ERR_CUDA;
+}
+
 extern "C" {
 
 int wbg_abi_version(void) { return WBG_ABI_VERSION; }
+
+const char* wbg_last_cuda_error_string(void) {
+  const int e = g_last_cuda_error.load(std::memory_order_relaxed);
+  return e == 0 ? "none" : cudaGetErrorString((cudaError_t)e);
+}
 
 const char* wbg_status_string(int status) {
   switch (status) {

@@ -17,6 +17,7 @@
 // Device-side error flags (bitmask) written by kernels into a caller-provided int.
 #define WBG_FLAG_QL_NOCONV 1
 #define WBG_FLAG_BOUNDS 2
+#define WBG_FLAG_REFINE_WIDE 4  // refined eigensolver: a cluster wider than its Rayleigh-Ritz block
 
 template <typename T> struct C2;
 template <> struct C2<double> { typedef double2 t; };
@@ -57,4 +58,6 @@ WBG_HD double2 to_c64(double2 a) { return a; }
 
 template <typename V> WBG_HD V czero() { V r; r.x = 0; r.y = 0; return r; }
 
-static inline int wbg_cuda_status(cudaError_t e) { return e == cudaSuccess ? WBG_OK : WBG_ERR_CUDA; }
+// Records e as the library's last CUDA error (wbg_last_cuda_error_string) and returns WBG_ERR_CUDA.
+int wbg_note_cuda_error(cudaError_t e);
+static inline int wbg_cuda_status(cudaError_t e) { return e == cudaSuccess ? WBG_OK : wbg_note_cuda_error(e); }

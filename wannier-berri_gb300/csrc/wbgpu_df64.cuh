@@ -144,6 +144,14 @@ template <> struct Arith<double> {
   // relative floor for inverse-iteration pivots: growth per tiny pivot stays within range
   static __device__ __forceinline__ double pivot_floor() { return 2.220446049250313e-16; }
 };
+template <> struct Arith<float> {
+  static __device__ __forceinline__ float from(double x) { return (float)x; }
+  static __device__ __forceinline__ double to(float x) { return (double)x; }
+  static __device__ __forceinline__ float eps() { return 5.9604644775390625e-08f; }  // 2^-24
+  static __device__ __forceinline__ float tiny_norm() { return 1e-30f; }
+  // FP32 exponent range: three consecutive pivots at the floor stay below 1e20
+  static __device__ __forceinline__ float pivot_floor() { return 1e-6f; }
+};
 template <> struct Arith<df64> {
   static __device__ __forceinline__ df64 from(double x) { return df_from(x); }
   static __device__ __forceinline__ double to(df64 x) { return df_to_double(x); }
@@ -165,6 +173,7 @@ template <> WBG_HD cdf czero<cdf>() {
 }
 
 // warp shuffles of the real types
+__device__ __forceinline__ float shfl_xor(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ double shfl_xor(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ df64 shfl_xor(df64 v, int off) {
   v.hi = __shfl_xor_sync(0xffffffffu, v.hi, off);

@@ -49,6 +49,12 @@ WBG_D typename C2<R>::t herm_avg(cdf a, cdf b) {
   r.y = (a.y - b.y) * half;
   return r;
 }
+template <>
+WBG_D float2 herm_avg<float>(cdf a, cdf b) {  // the FP32 solve of the refined mode
+  const df64 half = df_from_f(0.5f);
+  const df64 x = (a.x + b.x) * half, y = (a.y - b.y) * half;
+  return make_float2(x.hi + x.lo, y.hi + y.lo);
+}
 
 // Element (i, j <= i) of a matrix given by its lower triangle; the diagonal is taken real.
 template <typename R>
@@ -59,6 +65,10 @@ template <typename R>
 WBG_D typename C2<R>::t lower_elem(cdf a, bool diag) {
   if (diag) a.y = Arith<R>::from(0.0);
   return a;
+}
+template <>
+WBG_D float2 lower_elem<float>(cdf a, bool diag) {
+  return make_float2(a.x.hi + a.x.lo, diag ? 0.0f : a.y.hi + a.y.lo);
 }
 
 // Rounding of a solver real into the back-transform precision.  df64 -> float adds the two
@@ -572,6 +582,438 @@ int lanes_for(int n) {
   return L < 4 ? 4 : L;
 }
 
+// ---------------------------------------------------------------------------------------
+// 4. Refinement of an FP32 eigendecomposition against the double-float H (WBG_EIGH_REFINE):
+//    one step of the Ogita-Aishima iteration (T. Ogita, K. Aishima, "Iterative refinement for
+//    symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35, 2018), with a
+//    Rayleigh-Ritz step inside clusters of close eigenvalues.
+// One warp per matrix, n <= 32; lane j owns eigenvector x_j of the FP32 solve (U, E):
+//   r_j = H x_j - lambda_j x_j           H x_j in double-float, r rounded to FP32
+//   C_ij = x_i^H r_j                      FP32 (|r| ~ 1e-6 |H|: the sum's rounding is far below
+//                                         what the step needs)
+//   lambda'_j = lambda_j + C_jj / |x_j|^2 + sum_{i unclustered} |C_ij|^2 / (lambda_j - lambda_i)
+//          (the Rayleigh quotient of x_j and its second-order error, which the step removes
+//          from the vector: ~ (u |H|)^2 / gap otherwise)
+//   x'_j = x_j + sum_i x_i E_ij,  E_ij = C_ij / (lambda_j - lambda_i) when the two are more than
+//          delta apart, -x_i^H x_j / 2 inside a cluster, E_jj = (1 - |x_j|^2) / 2
+// (C_ij = x_i^H H x_j - lambda_j x_i^H x_j holds both the paper's S_ij and lambda_j R_ij.)
+// A cluster is a run of eigenvalues whose consecutive gaps are at most delta (2^-8 of the
+// largest |lambda|): its refined columns X_c are re-diagonalised by Rayleigh-Ritz,
+// P = X_c^H H X_c (H X_c in double-float, the sums in FP64), X_c orthonormalised by
+// Gc = X_c^H X_c = L L^H (Cholesky in FP64 from the FP32 columns), L^-1 P L^-H = V diag(mu) V^H
+// by cyclic Jacobi in FP64, X_c <- X_c L^-H V, lambda_c <- mu.  A cluster of more than RF_MAXC is
+// re-diagonalised in consecutive runs of RF_MAXC (exact where its eigenvalues are exactly
+// degenerate) and flagged (WBG_FLAG_REFINE_WIDE).  From an FP32 solve the step gives eigenvalues
+// to ~1e-13 |H| and eigenvectors to the complex64 rounding.
+// ---------------------------------------------------------------------------------------
+constexpr int RF_MAXC = 8;  // largest cluster re-diagonalised by Rayleigh-Ritz
+
+WBG_D void lz_fma_mixed(df64& acc, df64 a, float b) {  // acc += a b (a double-float, b FP32), lazily
+  const float p = a.hi * b;
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  const float s = acc.hi + p;
+  const float v = s - acc.hi;
+  const float t = (acc.hi - (s - v)) + (p - v);
+  acc.hi = s;
+  acc.lo = acc.lo + (t + e);
+}
+
+// H(k) into shared memory as the packed lower triangle (row i from i (i + 1) / 2) of double-float
+// complex: from the lower triangle of the input, or 1/2 (H + H^dagger) of the full matrix; the
+// diagonal real.  One warp, n <= 32.
+WBG_D cdf to_cdf(cdf a) { return a; }
+WBG_D cdf to_cdf(double2 a) {
+  cdf r;
+  r.x = df_from(a.x);
+  r.y = df_from(a.y);
+  return r;
+}
+template <typename HIn>
+WBG_D void stage_h(const HIn* Hk, int n, int lowerIn, cdf* Hs, int lane) {
+  const df64 half = df_from_f(0.5f);
+  for (int i = 0; i < n; ++i)
+    if (lane <= i) {
+      cdf a = to_cdf(Hk[i * n + lane]);
+      if (!lowerIn) {
+        const cdf b = to_cdf(Hk[lane * n + i]);
+        a.x = (a.x + b.x) * half;
+        a.y = (a.y - b.y) * half;
+      }
+      if (lane == i) a.y = df_from_f(0.0f);
+      Hs[tri(i) + lane] = a;
+    }
+}
+WBG_D cdf hs_elem(const cdf* Hs, int i, int m) {  // element (i, m) of the staged H
+  if (m <= i) return Hs[tri(i) + m];
+  cdf a = Hs[tri(m) + i];
+  a.y = -a.y;
+  return a;
+}
+
+// acc += h v (complex, h double-float, v FP32)
+WBG_D void lz_cfma_mixed(df64& ar, df64& ai, const cdf& h, float2 v) {
+  lz_fma_mixed(ar, h.x, v.x);
+  lz_fma_mixed(ar, -h.y, v.y);
+  lz_fma_mixed(ai, h.x, v.y);
+  lz_fma_mixed(ai, h.y, v.x);
+}
+// acc += conj(h) v
+WBG_D void lz_cfmac_mixed(df64& ar, df64& ai, const cdf& h, float2 v) {
+  lz_fma_mixed(ar, h.x, v.x);
+  lz_fma_mixed(ar, h.y, v.y);
+  lz_fma_mixed(ai, h.x, v.y);
+  lz_fma_mixed(ai, -h.y, v.x);
+}
+
+// m x m Hermitian A (row-major, FP64) -> diagonal (ascending), V <- its eigenvectors
+// (columns): cyclic Jacobi, each rotation W = diag(1, e^{-i phi}) J on the pair (p, q) with
+// a_pq = r e^{i phi} and J the real rotation that zeroes r (tangent t = sgn(th) /
+// (|th| + sqrt(th^2 + 1)), th = (a_qq - a_pp) / 2r)
+WBG_D void jacobi_herm(double2* A, double2* V, int m) {
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) V[i * m + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double off = 0.0, nrm = 0.0;
+    for (int p = 0; p < m; ++p) {
+      nrm += A[p * m + p].x * A[p * m + p].x;
+      for (int q = p + 1; q < m; ++q) off += A[p * m + q].x * A[p * m + q].x + A[p * m + q].y * A[p * m + q].y;
+    }
+    if (off <= 1e-32 * nrm || off == 0.0) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double2 b = A[p * m + q];
+        const double r = sqrt(b.x * b.x + b.y * b.y);
+        if (r == 0.0) continue;
+        const double2 ph = make_double2(b.x / r, -b.y / r);  // e^{-i phi}
+        const double th = (A[q * m + q].x - A[p * m + p].x) / (2.0 * r);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        const double2 w00 = make_double2(c, 0.0), w01 = make_double2(s, 0.0);
+        const double2 w10 = make_double2(-s * ph.x, -s * ph.y), w11 = make_double2(c * ph.x, c * ph.y);
+        for (int u = 0; u < m; ++u) {  // A <- A W, V <- V W
+          const double2 ap = A[u * m + p], aq = A[u * m + q];
+          A[u * m + p] = cadd(cmul(ap, w00), cmul(aq, w10));
+          A[u * m + q] = cadd(cmul(ap, w01), cmul(aq, w11));
+          const double2 vp = V[u * m + p], vq = V[u * m + q];
+          V[u * m + p] = cadd(cmul(vp, w00), cmul(vq, w10));
+          V[u * m + q] = cadd(cmul(vp, w01), cmul(vq, w11));
+        }
+        for (int u = 0; u < m; ++u) {  // A <- W^H A
+          const double2 ap = A[p * m + u], aq = A[q * m + u];
+          A[p * m + u] = cadd(cmulc(w00, ap), cmulc(w10, aq));
+          A[q * m + u] = cadd(cmulc(w01, ap), cmulc(w11, aq));
+        }
+        A[p * m + q] = make_double2(0.0, 0.0);
+        A[q * m + p] = make_double2(0.0, 0.0);
+        A[p * m + p].y = 0.0;
+        A[q * m + q].y = 0.0;
+      }
+  }
+  for (int i = 0; i < m; ++i) {  // ascending
+    int b = i;
+    for (int j = i + 1; j < m; ++j)
+      if (A[j * m + j].x < A[b * m + b].x) b = j;
+    if (b != i) {
+      const double2 t = A[i * m + i];
+      A[i * m + i] = A[b * m + b];
+      A[b * m + b] = t;
+      for (int r = 0; r < m; ++r) {
+        const double2 v = V[r * m + i];
+        V[r * m + i] = V[r * m + b];
+        V[r * m + b] = v;
+      }
+    }
+  }
+}
+
+WBG_D double warp_sum(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// shared memory of one matrix: X [32][32] complex64 (column j at stride 32: the FP32 solve,
+// then the refined columns), H (packed lower triangle, double-float complex), lamd [32], the
+// cluster's P (then W), Gc (then S), A and V [RF_MAXC^2] complex128, lamf [32], cluster starts [32]
+constexpr size_t RF_X_BYTES = 32 * 32 * 8, RF_H_BYTES = 32 * 33 / 2 * 16, RF_PC_BYTES = RF_MAXC * RF_MAXC * 16;
+constexpr size_t RF_GROUP_BYTES = RF_X_BYTES + RF_H_BYTES + 32 * 8 + 4 * RF_PC_BYTES + 32 * 4 + 32 * 4;
+
+template <typename HIn>
+__global__ void __launch_bounds__(64, 1) eigh_refine(const HIn* __restrict__ H, long long strideH, int n, int nk,
+                                                  int lowerIn, float2* __restrict__ U, long long strideU,
+                                                  double* __restrict__ E, int G, int* __restrict__ errflag,
+                                                  const int* __restrict__ list, int* __restrict__ relist) {
+  extern __shared__ __align__(16) unsigned char smr[];
+  const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // first step: matrix blockIdx.x G + grp; second step (list): the listed matrices
+  long long k = (long long)blockIdx.x * G + grp;
+  const long long cnt = list ? list[0] : nk;
+  const bool valid = k < cnt;
+  if (list && !valid) return;  // past the listed matrices: the warp leaves (no block-wide barrier here)
+  if (!valid) k = nk - 1;       // a tail warp repeats the last matrix and writes nothing
+  if (list) k = list[1 + k];
+  unsigned char* base = smr + (size_t)grp * RF_GROUP_BYTES;
+  float2* X = reinterpret_cast<float2*>(base);
+  cdf* Hs = reinterpret_cast<cdf*>(base + RF_X_BYTES);
+  double* lamd = reinterpret_cast<double*>(base + RF_X_BYTES + RF_H_BYTES);
+  double2* Pc = reinterpret_cast<double2*>(lamd + 32);
+  double2* Gc = Pc + RF_MAXC * RF_MAXC;
+  double2* Ab = Gc + RF_MAXC * RF_MAXC;
+  double2* Vb = Ab + RF_MAXC * RF_MAXC;
+  float* lamf = reinterpret_cast<float*>(Vb + RF_MAXC * RF_MAXC);
+  int* cstart = reinterpret_cast<int*>(lamf + 32);
+  stage_h<HIn>(H + k * strideH, n, lowerIn, Hs, lane);
+  for (int idx = lane; idx < n * n; idx += 32) X[(idx / n) * 32 + idx % n] = U[k * strideU + idx];
+  for (int i = lane; i < n; i += 32) lamf[i] = (float)E[k * n + i];  // FP32 eigenvalues, exact
+  __syncwarp();
+  const int j = lane < n ? lane : n - 1;  // lanes past n repeat the last column (nothing written)
+  float amax = 0.0f;
+  for (int i = 0; i < n; ++i) amax = fmaxf(amax, fabsf(lamf[i]));
+  const float delta = amax * 0x1p-8f;
+  const float lj = lamf[j];
+  const df64 mlj = df_from_f(-lj);
+  float2 r[32];  // residual of column j
+#pragma unroll
+  for (int i0 = 0; i0 < 32; i0 += 4) {
+    if (i0 < n) {
+      df64 ar[4], ai[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) ar[t] = ai[t] = df_from_f(0.0f);
+      // rows i0 .. i0 + 3 (past n: row n - 1, discarded): columns m <= i0 from the rows of the
+      // triangle, m > i0 + 3 from its columns (conjugated), the three between element by element
+      for (int m = 0; m <= i0; ++m) {
+        const float2 v = X[m * 32 + j];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int i = i0 + t < n ? i0 + t : n - 1;
+          lz_cfma_mixed(ar[t], ai[t], Hs[tri(i) + m], v);
+        }
+      }
+      for (int m = i0 + 1; m < n && m <= i0 + 3; ++m) {
+        const float2 v = X[m * 32 + j];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int i = i0 + t < n ? i0 + t : n - 1;
+          lz_cfma_mixed(ar[t], ai[t], hs_elem(Hs, i, m), v);
+        }
+      }
+      for (int m = i0 + 4; m < n; ++m) {
+        const float2 v = X[m * 32 + j];
+        const cdf* hm = Hs + tri(m) + i0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) lz_cfmac_mixed(ar[t], ai[t], hm[t], v);
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int i = i0 + t < n ? i0 + t : n - 1;
+        const float2 xi = X[i * 32 + j];
+        lz_fma_mixed(ar[t], mlj, xi.x);
+        lz_fma_mixed(ai[t], mlj, xi.y);
+        const df64 a = df_lazy_done(ar[t]), b = df_lazy_done(ai[t]);
+        r[i0 + t] = i0 + t < n ? make_float2(a.hi + a.lo, b.hi + b.lo) : make_float2(0.0f, 0.0f);
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) r[i0 + t] = make_float2(0.0f, 0.0f);
+    }
+  }
+  // cluster starts by the FP32 eigenvalues; lane j's column is in a cluster (of two or more)
+  if (lane < n) cstart[lane] = lane == 0 || lamf[lane] - lamf[lane - 1] > delta;
+  __syncwarp();
+  const bool inc = lane < n && (!cstart[lane] || (lane + 1 < n && !cstart[lane + 1]));
+  float2 xp[32];  // the correction x'_j - x_j (kept apart from x_j: one rounding at the end)
+  float gj = 0.0f;  // |x_j|^2 (FP32: enters lambda' through C_jj / gj, C_jj ~ 1e-6 |H|)
+#pragma unroll
+  for (int m = 0; m < 32; ++m) {
+    xp[m] = make_float2(0.0f, 0.0f);
+    const float2 v = m < n ? X[m * 32 + j] : make_float2(0.0f, 0.0f);
+    gj = fmaf(v.x, v.x, fmaf(v.y, v.y, gj));
+  }
+  double lnew = lj;
+  float l2 = 0.0f;  // second-order part: the Rayleigh quotient of x_j errs by sum_i |C_ij|^2 / (lambda_i - lambda_j)
+  float emax = 0.0f;  // largest correction of the column
+  for (int i = 0; i < n; ++i) {
+    float2 c0 = make_float2(0.0f, 0.0f), c1 = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int m = 0; m < 32; m += 2) {
+      if (m < n) cfmac(c0, X[m * 32 + i], r[m]);
+      if (m + 1 < n) cfmac(c1, X[(m + 1) * 32 + i], r[m + 1]);
+    }
+    const float2 c = make_float2(c0.x + c1.x, c0.y + c1.y);
+    const float d = lj - lamf[i];
+    const bool near = i != j && fabsf(d) <= delta;
+    float2 g = make_float2(0.0f, 0.0f);
+    if (__any_sync(0xffffffffu, near))  // same cluster: first-order orthogonalisation, E_ij = -G_ij / 2
+      for (int m = 0; m < n; ++m) cfmac(g, X[m * 32 + i], X[m * 32 + j]);
+    float2 e;
+    if (i == j) {
+      lnew = (double)lj + (double)(c.x / gj);
+      e = make_float2(0.5f * (1.0f - gj), 0.0f);
+    } else if (near) {
+      e = make_float2(-0.5f * g.x, -0.5f * g.y);
+    } else {
+      const float rd = 1.0f / d;
+      e = make_float2(c.x * rd, c.y * rd);
+      l2 = fmaf(c.x * c.x + c.y * c.y, rd, l2);
+    }
+    emax = fmaxf(emax, fabsf(e.x) + fabsf(e.y));
+#pragma unroll
+    for (int m = 0; m < 32; ++m)
+      if (m < n) cfma(xp[m], X[m * 32 + i], e);
+  }
+  __syncwarp();  // every lane is done reading the FP32 solve
+  // One step leaves the square of the FP32 solve's error: a matrix whose correction exceeds
+  // 2^-12 somewhere (an unusually poor FP32 eigenvector) is listed for a second step, which the
+  // launcher runs on the listed matrices from this step's output; one that still needs it then
+  // is flagged (WBG_FLAG_REFINE_WIDE).
+  if (__any_sync(0xffffffffu, lane < n && emax > 0x1p-12f) && lane == 0 && valid) {
+    if (relist) relist[1 + atomicAdd(relist, 1)] = (int)k;
+    else atomicOr(errflag, WBG_FLAG_REFINE_WIDE);
+  }
+  if (inc) {     // a cluster's columns take x'_j (rounded) for the Rayleigh-Ritz step
+#pragma unroll
+    for (int m = 0; m < 32; ++m)
+      if (m < n) {
+        const float2 v = X[m * 32 + lane];
+        X[m * 32 + lane] = make_float2(v.x + xp[m].x, v.y + xp[m].y);
+      }
+  }
+  if (lane < n) lamd[lane] = lnew + (double)l2;
+  __syncwarp();
+  // column j = x + c (c: the correction, zero for a cluster's columns), normalised: |x + c|^2 with
+  // |x|^2 in double-float and the small terms in FP32, s = 1 / |x + c| - 1, and each element
+  // x + (c + (x + c) s) rounded once.  Columns outside clusters are written before the
+  // Rayleigh-Ritz steps (their corrections need no registers past this point), the others after.
+  auto write_column = [&](const bool with_corr) {
+    df64 nr = df_from_f(0.0f);
+    float small = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 32; ++q)
+      if (q < n) {
+        const float2 v = X[q * 32 + j], cq = with_corr ? xp[q] : make_float2(0.0f, 0.0f);
+        lz_fma_mixed(nr, df_from_f(v.x), v.x);
+        lz_fma_mixed(nr, df_from_f(v.y), v.y);
+        small = fmaf(2.0f * v.x + cq.x, cq.x, fmaf(2.0f * v.y + cq.y, cq.y, small));
+      }
+    const float sc = (float)(1.0 / sqrt(df_to_double(df_lazy_done(nr)) + (double)small) - 1.0);
+    if (valid && lane < n) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q)
+        if (q < n) {
+          const float2 v = X[q * 32 + lane], cq = with_corr ? xp[q] : make_float2(0.0f, 0.0f);
+          const float tx = cq.x + (v.x + cq.x) * sc, ty = cq.y + (v.y + cq.y) * sc;
+          U[k * strideU + q * n + lane] = make_float2(v.x + tx, v.y + ty);
+        }
+      E[k * n + lane] = lamd[lane];
+    }
+  };
+  if (!inc) write_column(true);
+  // Rayleigh-Ritz in each cluster: lane q holds row q of H X_c; sums over rows by shuffles
+  for (int c0 = 0; c0 < n;) {
+    int cend = c0 + 1;  // end of the cluster
+    while (cend < n && !cstart[cend]) ++cend;
+    const int c1 = min(cend, c0 + RF_MAXC);  // a wider cluster in runs of RF_MAXC
+    if (cend - c0 > RF_MAXC && lane == 0 && valid) atomicOr(errflag, WBG_FLAG_REFINE_WIDE);
+    const int m = c1 - c0;
+    if (m > 1) {
+      const int q = lane < n ? lane : n - 1;
+      const bool row = lane < n;
+      for (int t = 0; t < m; ++t) {
+        df64 yr = df_from_f(0.0f), yi = df_from_f(0.0f);  // (H x'_t)_q
+        for (int s = 0; s < n; ++s) lz_cfma_mixed(yr, yi, hs_elem(Hs, q, s), X[s * 32 + c0 + t]);
+        const double2 y = make_double2(df_to_double(df_lazy_done(yr)), df_to_double(df_lazy_done(yi)));
+        const float2 xt = X[q * 32 + c0 + t];
+        for (int p = 0; p < m; ++p) {
+          const float2 xf = X[q * 32 + c0 + p];
+          const double2 xpq = make_double2(xf.x, xf.y);
+          double2 pv = cmulc(xpq, y), gv = cmulc(xpq, make_double2(xt.x, xt.y));
+          if (!row) pv = gv = make_double2(0.0, 0.0);
+          pv.x = warp_sum(pv.x);
+          pv.y = warp_sum(pv.y);
+          gv.x = warp_sum(gv.x);
+          gv.y = warp_sum(gv.y);
+          if (lane == 0) {
+            Pc[p * RF_MAXC + t] = pv;
+            Gc[p * RF_MAXC + t] = gv;
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {  // Gc = L L^H, S = L^-H (over Gc); A = S^H P S = V mu V^H; W = S V (over P)
+        double2 *S = Gc, *L = Ab, *Li = Vb;
+        for (int j = 0; j < m; ++j) {  // Cholesky (the FP32 vectors of a cluster can be far from orthonormal)
+          double dj = Gc[j * RF_MAXC + j].x;
+          for (int t = 0; t < j; ++t) dj -= L[j * m + t].x * L[j * m + t].x + L[j * m + t].y * L[j * m + t].y;
+          dj = sqrt(fmax(dj, 1e-30));
+          L[j * m + j] = make_double2(dj, 0.0);
+          for (int i = j + 1; i < m; ++i) {
+            double2 t2 = Gc[i * RF_MAXC + j];
+            for (int t = 0; t < j; ++t) t2 = csub(t2, cmul(L[i * m + t], cconj(L[j * m + t])));
+            L[i * m + j] = make_double2(t2.x / dj, t2.y / dj);
+          }
+        }
+        for (int j = 0; j < m; ++j) {  // L^-1, lower triangular
+          for (int i = 0; i < j; ++i) Li[i * m + j] = make_double2(0.0, 0.0);
+          Li[j * m + j] = make_double2(1.0 / L[j * m + j].x, 0.0);
+          for (int i = j + 1; i < m; ++i) {
+            double2 t2 = make_double2(0.0, 0.0);
+            for (int t = j; t < i; ++t) t2 = cadd(t2, cmul(L[i * m + t], Li[t * m + j]));
+            Li[i * m + j] = make_double2(-t2.x / L[i * m + i].x, -t2.y / L[i * m + i].x);
+          }
+        }
+        for (int a = 0; a < m; ++a)
+          for (int b = 0; b < m; ++b) S[a * RF_MAXC + b] = cconj(Li[b * m + a]);
+        for (int a = 0; a < m; ++a)  // V <- P S
+          for (int b = 0; b < m; ++b) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int s = 0; s < m; ++s) t = cadd(t, cmul(Pc[a * RF_MAXC + s], S[s * RF_MAXC + b]));
+            Vb[a * m + b] = t;
+          }
+        for (int a = 0; a < m; ++a)  // A <- S^H (P S)
+          for (int b = 0; b < m; ++b) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int s = 0; s < m; ++s) t = cadd(t, cmulc(S[s * RF_MAXC + a], Vb[s * m + b]));
+            Ab[a * m + b] = t;
+          }
+        for (int a = 0; a < m; ++a)  // Hermitian part
+          for (int b = a; b < m; ++b) {
+            const double2 u = Ab[a * m + b], v = Ab[b * m + a];
+            Ab[a * m + b] = make_double2(0.5 * (u.x + v.x), 0.5 * (u.y - v.y));
+            Ab[b * m + a] = cconj(Ab[a * m + b]);
+          }
+        jacobi_herm(Ab, Vb, m);
+        for (int a = 0; a < m; ++a) {
+          lamd[c0 + a] = Ab[a * m + a].x;
+          for (int b = 0; b < m; ++b) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int s = 0; s < m; ++s) t = cadd(t, cmul(S[a * RF_MAXC + s], Vb[s * m + b]));
+            Pc[a * RF_MAXC + b] = t;
+          }
+        }
+      }
+      __syncwarp();
+      if (row) {  // row q of X_c <- X_c W, in FP64 from the FP32 values
+        double2 xr[RF_MAXC];
+#pragma unroll
+        for (int b = 0; b < RF_MAXC; ++b) {
+          xr[b] = make_double2(0.0, 0.0);
+          if (b < m)
+            for (int t = 0; t < m; ++t) {
+              const float2 v = X[q * 32 + c0 + t];
+              xr[b] = cadd(xr[b], cmul(make_double2(v.x, v.y), Pc[t * RF_MAXC + b]));
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < RF_MAXC; ++b)
+          if (b < m) X[q * 32 + c0 + b] = make_float2((float)xr[b].x, (float)xr[b].y);
+      }
+      __syncwarp();
+    }
+    c0 = c1;
+  }
+  if (inc) write_column(false);
+}
+
 // Shared memory of one SM (228 KB, 1 KB of it reserved per resident block) and the largest
 // dynamic allocation this file asks of one block.
 constexpr size_t kSmemPerSM = 228 * 1024, kSmemPerBlockReserved = 1024, kMaxBlockSmem = 220 * 1024;
@@ -693,6 +1135,29 @@ int launch_eigh(const void* H, long long strideH, int n, int nk, void* E, void* 
   return wbg_cuda_status(cudaGetLastError());
 }
 
+// FP32 solve (tridiagonalisation, QL, inverse iteration, back-transform all in FP32) and one
+// refinement step against the double-float or FP64 H (section 4)
+template <typename HIn>
+int launch_eigh_refined(const void* H, long long strideH, int n, int nk, void* E, void* U, long long strideU,
+                        int lowerIn, int stage, void* workspace, int* errflag, cudaStream_t stream) {
+  const int st = launch_eigh<float, float, HIn, float2>(H, strideH, n, nk, E, U, strideU, lowerIn, 0, stage, 5,
+                                                       workspace, errflag, stream);
+  if (st != WBG_OK || stage == 1) return st;
+  const int G = 2;
+  const size_t sm = G * RF_GROUP_BYTES;
+  // list of the matrices that take a second step: [count, k ...] over the reflectors' workspace
+  // (free once the back-transform has run)
+  int* list = (int*)workspace;
+  cudaMemsetAsync(list, 0, sizeof(int), stream);
+  cudaFuncSetAttribute(eigh_refine<HIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const unsigned grid = (unsigned)((nk + G - 1) / G);
+  eigh_refine<HIn><<<grid, 32 * G, sm, stream>>>((const HIn*)H, strideH, n, nk, lowerIn, (float2*)U, strideU,
+                                                (double*)E, G, errflag, nullptr, list);
+  eigh_refine<HIn><<<grid, 32 * G, sm, stream>>>((const HIn*)H, strideH, n, nk, lowerIn, (float2*)U, strideU,
+                                                (double*)E, G, errflag, list, nullptr);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
 }  // namespace
 
 size_t wbg_eigh_workspace_bytes(int n, int nk) {
@@ -708,8 +1173,18 @@ int wbg_eigh_run(const void* H, long long strideH, int n, int nk, void* E, void*
   if (!H && stage != 2) return WBG_ERR_ARG;
   if (mode < 0 ||
       mode > (3 | WBG_EIGH_LOWER | WBG_EIGH_VALUES | WBG_EIGH_STAGE1 | WBG_EIGH_STAGE2 | WBG_EIGH_PRECISE_VECTORS |
-              WBG_EIGH_DF64_VECTORS))
+              WBG_EIGH_DF64_VECTORS | WBG_EIGH_REFINE))
     return WBG_ERR_ARG;
+  if (mode & WBG_EIGH_REFINE) {  // FP32 solve + refinement: modes 2 / 3, eigenvectors, n <= 32
+    if ((mode & 3) < 2 || n > 32 || vo || (mode & (WBG_EIGH_PRECISE_VECTORS | WBG_EIGH_DF64_VECTORS)) || !H ||
+        ((mode & WBG_EIGH_STAGE1) && (mode & WBG_EIGH_STAGE2)))
+      return WBG_ERR_ARG;
+    if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
+    const int lo = (mode & WBG_EIGH_LOWER) ? 1 : 0;
+    if ((mode & 3) == 2)
+      return launch_eigh_refined<double2>(H, strideH, n, nk, E, U, strideU, lo, stage, workspace, errflag, stream);
+    return launch_eigh_refined<cdf>(H, strideH, n, nk, E, U, strideU, lo, stage, workspace, errflag, stream);
+  }
   if ((mode & WBG_EIGH_DF64_VECTORS) && (!(mode & WBG_EIGH_PRECISE_VECTORS) || (mode & 3) < 2)) return WBG_ERR_ARG;
   if ((mode & WBG_EIGH_STAGE1) && (mode & WBG_EIGH_STAGE2)) return WBG_ERR_ARG;
   if (workspace_bytes < wbg_eigh_workspace_bytes(n, nk)) return WBG_ERR_WORKSPACE;
@@ -757,6 +1232,7 @@ int wbg_eigh_tune_candidates(int param, int n, int variant, int* values, int cap
     case 1: return EighShape<double, double>(n).candidates(param, values, capacity);
     case 0: return EighShape<double, float>(n).candidates(param, values, capacity);
     case 4: return EighShape<df64, df64>(n).candidates(param, values, capacity);
+    case 5: return EighShape<float, float>(n).candidates(param, values, capacity);
     default: return EighShape<df64, float>(n).candidates(param, values, capacity);
   }
 }

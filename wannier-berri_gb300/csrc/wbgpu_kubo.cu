@@ -30,6 +30,7 @@
 #include "wbgpu_fixed.cuh"
 #include "wbgpu_kubo.cuh"
 #include "wbgpu_spin.cuh"
+#include "wbgpu_tune.cuh"
 
 namespace {
 
@@ -589,6 +590,10 @@ int wbg_dynamic_run(const double* E, const void* Xbar, int nFbar, const wbg_dyna
     else WBG_ACCUM(27, double);
   } else if (nc == 1) {
     WBG_ACCUM(1, float);
+  } else if (wbg_tuned(WBG_TUNE_KUBO_ENGINE, 0, 1) != 2) {  // tensor cores (the built-in choice)
+    const int st = wbg_kubo_tc_run(rec_dE, rec_fE, rec_M, count, P, nk, omega, kp->nOmega, kp->nEF, nc, kp->eta,
+                                   kp->gaussian, F, out, stream);
+    if (st != WBG_OK) return st;
   } else {  // the register-tiled GEMM: one block per SM, frequency x column tiles x k chunks
     const int gw = (kp->nOmega + KG_TW - 1) / KG_TW, gc = (kp->nEF * nc + KG_TC - 1) / KG_TC;
     int gk = sms / (gw * gc);  // one wave of one block per SM

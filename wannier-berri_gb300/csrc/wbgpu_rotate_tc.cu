@@ -22,6 +22,8 @@
 // library's device error word, releases its tensor memory and returns.
 #include "wbgpu_common.cuh"
 #include "wbgpu_band.cuh"
+#include "wbgpu_fixed.cuh"
+#include "wbgpu_kubo.cuh"
 
 __device__ unsigned int g_wbg_device_flags;
 
@@ -881,6 +883,345 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Kubo band sums on the tensor cores (mixed path; calculators/dynamic.py:97-98,
+//   restot += factor_omega @ (factor_Efermi x M)):
+//   out[w][j] += sum_r F[w][r] G[r][j] per k-point,  F = f_w(dE_r), G[r][(e, c)] = f_E[r][e] M[r][c]
+// over the pair records of wbgpu_kubo.cu (dE FP64, f_E and M FP32).  Real embedding with two K
+// entries per record (Re F, Im F):
+//   A[w][2r + p]      = p ? Im F : Re F                                  M = 128 frequencies
+//   B[2j + q][2r + p] = [[Re G, -Im G], [Im G, Re G]][q][p]              N = 2 x (<= 104 columns j)
+//   D[w][2j + q]      = q ? Im (F G)[w][j] : Re (F G)[w][j]
+// F is formed in FP32 from dE - w taken as (dE_hi - w_hi) + (dE_lo - w_lo) (double-float halves:
+// the difference to FP32 accuracy without the FP64 pipe).  Operands are split into TF32 hi + lo
+// (3xTF32) as in the rotation.  The records of one k-point run in chunks of KT_RC = 8 (K = 16, two
+// MMA K-steps, three products each): a chunk's products go to a fresh TMEM accumulator, so no
+// accumulator takes more than six truncating steps, and the two accumulators alternate, so that
+// the tensor cores fill one while the epilogue drains the other.  The epilogue adds each chunk
+// with round-to-nearest into per-k-point FP32 sums held in registers, and adds those to the
+// fixed-point output once per k-point (order-independent: the same bits in any grid shape).
+// Roles (384 threads, one CTA per SM): warps 0-7 epilogue (TMEM lane quarter = warp & 3, column
+// half = warp >> 2), warps 8-11 operand producers (four operand stages), the first of which
+// also issues the chunk's MMAs once the producers are done with it.  (A thirteenth warp for the
+// issue would put four warps on one SM sub-partition, whose 16K registers then hold at most 128
+// per thread.)  Every mbarrier wait is bounded by the kernel's wait limit, as in the rotation.
+// ---------------------------------------------------------------------------------------
+constexpr int KT_M = 128, KT_CT = 104, KT_NMAX = 2 * KT_CT, KT_RC = 8, KT_K = 2 * KT_RC, KT_NST = 4;
+constexpr int KT_LBO = 128;                          // K-adjacent core matrices contiguous
+constexpr int KT_SBO = (KT_K / 4) * KT_LBO + 16;     // 8-row groups, 16 bytes apart in banks
+constexpr int KT_A_BYTES = (KT_M / 8) * KT_SBO;      // one copy (hi or lo) of F
+constexpr int KT_B_BYTES = (KT_NMAX / 8) * KT_SBO;   // one copy of the embedded G
+constexpr int KT_STAGE = 2 * KT_A_BYTES + 2 * KT_B_BYTES;
+// a chunk's records, copied one chunk ahead: dE, f_E of the tile's levels (<= KT_EMAX), M (<= 27)
+constexpr int KT_EMAX = 16, KT_NCMAX = 27;
+constexpr int KT_REC_BYTES = KT_RC * 8 + KT_RC * KT_EMAX * 4 + KT_RC * KT_NCMAX * 8;
+constexpr int KT_SMEM = KT_NST * KT_STAGE + 2 * KT_REC_BYTES;
+constexpr int KT_EPI = 256, KT_PROD0 = 256, KT_PRODN = 128, KT_THR = 12 * 32;
+constexpr uint32_t KT_TMEM_COLS = 512;               // accumulator of chunk t at column 256 (t & 1)
+static_assert(KT_SMEM <= 220 * 1024, "two operand stages must fit one CTA's shared memory");
+
+WBG_D uint64_t kt_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(KT_LBO >> 4) << 16) | ((uint64_t)(KT_SBO >> 4) << 32) |
+         (1ull << 46);
+}
+WBG_D uint32_t kt_off(int r, int k) {  // byte offset of element (row r, K index k % 4 == 0) of an operand
+  return (uint32_t)((r >> 3) * KT_SBO + (k >> 2) * KT_LBO + (r & 7) * 16);
+}
+WBG_D void kt_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+WBG_D void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+WBG_D void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+WBG_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+WBG_D void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }  // all but the newest group
+
+// Records r0 .. r0 + rn - 1 of k-point k into a record buffer: dE, f_E of levels e0 .. e0 + ne - 1,
+// the NC components of M; thread i of nthr takes every nthr-th 4- or 8-byte piece.
+WBG_D void kt_stage_records(unsigned char* rb, const double* rec_dE, const float* rec_fE, const float2* rec_M,
+                            long long rbase, int rn, int nEF, int e0, int ne, int NC, int i, int nthr) {
+  double* de = reinterpret_cast<double*>(rb);
+  float* fe = reinterpret_cast<float*>(rb + KT_RC * 8);
+  float2* mm = reinterpret_cast<float2*>(rb + KT_RC * 8 + KT_RC * KT_EMAX * 4);
+  for (int p = i; p < rn; p += nthr) cp_async8(de + p, rec_dE + rbase + p);
+  for (int p = i; p < rn * ne; p += nthr) {
+    const int r = p / ne, e = p - r * ne;
+    cp_async4(fe + r * KT_EMAX + e, rec_fE + (rbase + r) * nEF + e0 + e);
+  }
+  for (int p = i; p < rn * NC; p += nthr) {
+    const int r = p / NC, c = p - r * NC;
+    cp_async8(mm + r * KT_NCMAX + c, rec_M + (rbase + r) * NC + c);
+  }
+}
+
+WBG_D void tmem_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+WBG_D void tmem_ld_wait8(uint32_t* r) {
+  asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+               "+r"(r[7])::"memory");
+}
+
+// f_w of one record for frequency w: dE - w and -dE - w from the double-float halves; formula
+// WBG_DYN_OPTCOND dE / (dE - w - i eta), WBG_DYN_SHC_SIMPLE (every spin Hall kind)
+// 1 / (-dE - w - i eta) / 2, WBG_DYN_SHIFT smear(-dE - w) + smear(dE - w), otherwise
+// smear(-dE - w); Lorentzian or Gaussian (the frequency factors of wbgpu_kubo.cu in FP32)
+WBG_D float2 kt_factor(int formula, float deh, float del, float wh, float wl, float eta, int gaussian) {
+  const float dp = (deh - wh) + (del - wl), dm = (-deh - wh) + (-del - wl);
+  if (formula == WBG_DYN_OPTCOND || formula == WBG_DYN_SHC_SIMPLE) {
+    const bool opt = formula == WBG_DYN_OPTCOND;
+    const float d = opt ? dp : dm;
+    const float den = __fdividef(1.0f, fmaf(d, d, eta * eta));
+    float cre = d * den, cim = eta * den;
+    if (gaussian) {
+      const float x = d / eta;
+      cim = fabsf(d) < eta * 14.142135623730951f ? 1.7724538509055160f / eta * __expf(-x * x) : 0.0f;
+    }
+    const float s = opt ? deh + del : 0.5f;
+    return make_float2(s * cre, s * cim);
+  }
+  auto sm = [&](float x) {
+    if (gaussian) {
+      const float y = x / eta;
+      return fabsf(x) < eta * 14.142135623730951f ? 0.5641895835477563f / eta * __expf(-y * y) : 0.0f;
+    }
+    return 0.3183098861837907f * eta * __fdividef(1.0f, fmaf(x, x, eta * eta));
+  };
+  float v = sm(dm);
+  if (formula == WBG_DYN_SHIFT) v += sm(dp);
+  return make_float2(v, 0.0f);
+}
+
+__global__ void __launch_bounds__(KT_THR, 1)
+    kubo_tc(const double* __restrict__ rec_dE, const float* __restrict__ rec_fE, const float2* __restrict__ rec_M,
+            const int* __restrict__ count, int P, int nk, int kchunk, const double* __restrict__ omega, int nOmega,
+            int nEF, int NC, int ctile, float eta, int gaussian, int fgroup, wbg_u64* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char smk[];
+  __shared__ __align__(8) uint64_t bar_s[KT_NST + 4];  // empty[KT_NST] accfull[2] accfree[2]
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
+  __shared__ float2 de_s[KT_NST][KT_RC];      // (hi, lo) of the chunk's dE, per stage
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int w0 = blockIdx.x * KT_M, col0 = blockIdx.z * ctile;
+  const int ncol = nEF * NC, nct = min(ctile, ncol - col0);  // ctile <= KT_CT
+  const int N = (2 * nct + 15) / 16 * 16;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(KT_M >> 4) << 24);
+  const long long k0 = (long long)blockIdx.y * kchunk, k1 = min((long long)nk, k0 + kchunk);
+  auto bar = [&](int i) { return smem_u32(&bar_s[i]); };
+  enum { EMPTY = 0, ACCFULL = KT_NST, ACCFREE = KT_NST + 2 };
+  if (tid == 0) {
+    for (int i = 0; i < KT_NST + 2; ++i) mbar_init(bar(i));  // one arrival: the MMA commit
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(ACCFREE + i)), "r"(KT_EPI) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_s = 0;
+  }
+  for (int i = tid; i < KT_SMEM / 16; i += KT_THR)  // padding rows and columns stay zero
+    reinterpret_cast<uint4*>(smk)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (warp == KT_PROD0 / 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(KT_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = tmem_base_s;
+  const unsigned long long wait_ns = g_tc_wait_ns;
+  volatile int* ab = &abort_s;
+  if (warp >= 8 && warp < 12) {
+    // ================= operand producers =================
+    const int pt = tid - KT_PROD0;
+    const int w = w0 + pt;  // this thread's row of F
+    const double om = w < nOmega ? omega[w] : 0.0;
+    const float wh = (float)om, wl = (float)(om - (double)wh);
+    uint32_t last_bar = 0, last_par = 0;  // the issuing thread's last commit
+    // the chunk sequence: (k-point, first record) over the CTA's k-points with records
+    const int e0 = col0 / NC, ne = (col0 + nct - 1) / NC - e0 + 1;  // the tile's levels (<= KT_EMAX)
+    auto skip_empty = [&](long long& kk, int& rr) {
+      while (kk < k1 && rr >= count[kk]) {
+        ++kk;
+        rr = 0;
+      }
+    };
+    auto rbuf = [&](int tt) { return smk + KT_NST * KT_STAGE + (int)(tt & 1) * KT_REC_BYTES; };
+    long long kc = k0, kn;
+    int rc = 0, rnx;
+    skip_empty(kc, rc);
+    if (kc < k1)
+      kt_stage_records(rbuf(0), rec_dE, rec_fE, rec_M, kc * (long long)P + rc, min(KT_RC, count[kc] - rc), nEF, e0, ne,
+                       NC, pt, KT_PRODN);
+    cp_async_commit();
+    kn = kc;
+    rnx = rc + KT_RC;
+    skip_empty(kn, rnx);
+    for (int t = 0; kc < k1; ++t) {
+      const int s = (int)(t % KT_NST), rn = min(KT_RC, count[kc] - rc);
+      bool ok = true;
+      if (lane == 0 && t >= KT_NST)
+        ok = pipe_wait(bar(EMPTY + s), (uint32_t)((t / KT_NST - 1) & 1), ab, wait_ns);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (named_any(1, KT_PRODN, !ok || *ab)) break;  // one decision for all producers
+      unsigned char* Ah = smk + s * KT_STAGE;
+      unsigned char* Al = Ah + KT_A_BYTES;
+      unsigned char* Bh = Al + KT_A_BYTES;
+      unsigned char* Bl = Bh + KT_B_BYTES;
+      if (kn < k1)  // the next chunk's records, in flight while this one is formed
+        kt_stage_records(rbuf(t + 1), rec_dE, rec_fE, rec_M, kn * (long long)P + rnx, min(KT_RC, count[kn] - rnx), nEF,
+                         e0, ne, NC, pt, KT_PRODN);
+      cp_async_commit();
+      cp_async_wait_prev();  // this chunk's records
+      named_sync(1, KT_PRODN);
+      const unsigned char* rb = rbuf(t);
+      const double* rde = reinterpret_cast<const double*>(rb);
+      const float* rfe = reinterpret_cast<const float*>(rb + KT_RC * 8);
+      const float2* rm = reinterpret_cast<const float2*>(rb + KT_RC * 8 + KT_RC * KT_EMAX * 4);
+      if (pt < KT_RC) {
+        const double de = pt < rn ? rde[pt] : 0.0;
+        const float h = (float)de;
+        de_s[s][pt] = make_float2(h, (float)(de - (double)h));
+      }
+      named_sync(1, KT_PRODN);
+      // A: row pt, records (2q, 2q + 1) -> K entries 4q .. 4q + 3
+#pragma unroll 1
+      for (int q = 0; q < KT_RC / 2; ++q) {
+        float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
+        if (w < nOmega) {
+          const float2 a = de_s[s][2 * q], b = de_s[s][2 * q + 1];
+          if (2 * q < rn) f0 = kt_factor(fgroup, a.x, a.y, wh, wl, eta, gaussian);
+          if (2 * q + 1 < rn) f1 = kt_factor(fgroup, b.x, b.y, wh, wl, eta, gaussian);
+        }
+        put_split4(Ah, Al, kt_off(pt, 4 * q), f0.x, f0.y, f1.x, f1.y);
+      }
+      // B: rows 2j, 2j + 1 for column j of the tile, records (2q, 2q + 1)
+      for (int idx = pt; idx < nct * (KT_RC / 2); idx += KT_PRODN) {
+        const int j = idx % nct, q = idx / nct;
+        const int col = col0 + j, e = col / NC, c = col - e * NC;
+        float2 g[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = 2 * q + h;
+          g[h] = make_float2(0.f, 0.f);
+          if (r < rn) {
+            const float fe = rfe[r * KT_EMAX + e - e0];
+            const float2 m = rm[r * KT_NCMAX + c];
+            g[h] = make_float2(fe * m.x, fe * m.y);
+          }
+        }
+        put_split4(Bh, Bl, kt_off(2 * j, 4 * q), g[0].x, -g[0].y, g[1].x, -g[1].y);
+        put_split4(Bh, Bl, kt_off(2 * j + 1, 4 * q), g[0].y, g[0].x, g[1].y, g[1].x);
+      }
+      fence_async_smem();
+      named_sync(1, KT_PRODN);
+      // ---- MMA issue (one thread): the chunk's operands are complete; the accumulators are
+      // free once the epilogue has drained the previous chunk
+      const int b = (int)(t & 1);  // accumulator buffer: the epilogue drains the other meanwhile
+      if (pt == 0 && (t < 2 || pipe_wait(bar(ACCFREE + b), (uint32_t)((t / 2 - 1) & 1), ab, wait_ns))) {
+        tc_fence_after();
+        const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
+        const uint32_t D = tbase + (uint32_t)(256 * b);
+#pragma unroll
+        for (int ks = 0; ks < KT_K / 8; ++ks) {
+          const uint32_t so = (uint32_t)ks * 2 * KT_LBO;
+          kt_mma(D, kt_desc(ah + so), kt_desc(bh + so), idesc, ks > 0);
+          kt_mma(D, kt_desc(al + so), kt_desc(bh + so), idesc, 1);
+          kt_mma(D, kt_desc(ah + so), kt_desc(bl + so), idesc, 1);
+        }
+        mma_commit(bar(EMPTY + s));
+        mma_commit(bar(ACCFULL + b));
+        last_bar = bar(ACCFULL + b);
+        last_par = (uint32_t)((t / 2) & 1);
+      }
+      kc = kn;
+      rc = rnx;
+      if (kn < k1) {
+        rnx += KT_RC;
+        skip_empty(kn, rnx);
+      }
+    }
+    cp_async_wait_all();  // no copy in flight at exit
+    if (pt == 0 && *ab && last_bar) mbar_wait(last_bar, last_par, DRAIN_NS);  // no product in flight at exit
+  } else {
+    // ================= epilogue =================
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = 32 * quarter + lane, w = w0 + row;
+    const int nh = N / 2, n8 = nh / 8;  // this warp's columns [half nh, (half + 1) nh), in pieces of 8
+    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
+    const uint32_t D0 = tbase + lane_base + (uint32_t)(half * nh);
+    wbg_u64* bad = out + 4 * (long long)nEF * nOmega * NC;
+    float acc[KT_CT];
+#pragma unroll
+    for (int i = 0; i < KT_CT; ++i) acc[i] = 0.f;
+    int t = 0;
+    for (long long k = k0; k < k1; ++k) {
+      const int nrec = count[k];
+      bool stop = false;
+      for (int r0 = 0; r0 < nrec; r0 += KT_RC, ++t) {
+        bool ok = true;
+        const int b = (int)(t & 1);
+        if (lane == 0) ok = pipe_wait(bar(ACCFULL + b), (uint32_t)((t / 2) & 1), ab, wait_ns);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (named_any(2, KT_EPI, !ok || *ab)) {
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t D = D0 + (uint32_t)(256 * b);
+#pragma unroll
+        for (int p = 0; p < KT_CT / 8; p += 2) {  // two pieces of 8 columns per wait
+          if (p < n8) {
+            uint32_t v[2][8];
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+              if (p + u < n8) tmem_ld8(D + 8 * (p + u), v[u]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+              if (p + u < n8) {
+                tmem_ld_wait8(v[u]);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) acc[8 * (p + u) + i] += __uint_as_float(v[u][i]);
+              }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(bar(ACCFREE + b));
+      }
+      if (stop) break;
+      if (nrec > 0) {  // the k-point's sums into the fixed-point output
+#pragma unroll
+        for (int i = 0; i < KT_CT; i += 2) {
+          const int j = (half * nh + i) / 2;  // complex column of the tile
+          if (i < nh && j < nct && w < nOmega) {
+            const int col = col0 + j, e = col / NC, c = col - e * NC;
+            wbg_u64* o = out + 4 * (((long long)e * nOmega + w) * NC + c);
+            fx_add_double(o, (double)acc[i], bad);
+            fx_add_double(o + 2, (double)acc[i + 1], bad);
+          }
+          acc[i] = acc[i + 1] = 0.f;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == KT_PROD0 / 32) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(KT_TMEM_COLS) : "memory");
+  }
+}
+
 // A wait that runs out by construction: an mbarrier whose phase never completes, waited on with
 // the kernel's bound; records WBG_DEVICE_FLAG_TC_TIMEOUT exactly as the rotation does.
 __global__ void tc_wait_probe_kernel(int* result) {
@@ -908,28 +1249,59 @@ int wbg_rotate_tc_run(const void* U, long long strideU, const void* X, int nFin,
   if (nw != NW || nFrot > TMAP_MAX - 2 * FPT) return WBG_ERR_SIZE;
   if (nk < 1 || nFrot < 1 || !U || !X || !Xbar || !fsel || !herm) return WBG_ERR_ARG;
   int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return WBG_ERR_CUDA;
+  if (const cudaError_t e_ = cudaGetDevice(&dev)) return wbg_cuda_status(e_);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return WBG_ERR_CUDA;
   if (!serial) {  // one CTA per SM (its shared memory and tensor memory take the whole SM)
-    if (cudaFuncSetAttribute(rotate_tc_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM) != cudaSuccess)
-      return WBG_ERR_CUDA;
+    if (const cudaError_t e_ = cudaFuncSetAttribute(rotate_tc_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM))
+      return wbg_cuda_status(e_);
     const long long grid = nk < sms ? nk : sms;
     rotate_tc_pipe<<<(unsigned)grid, PIPE_THR, PIPE_SMEM, stream>>>((const float2*)U, strideU, (const float2*)X, nFin,
                                                                     fsel, herm, nFrot, (float2*)Xbar, nk);
     return wbg_cuda_status(cudaGetLastError());
   }
-  if (cudaFuncSetAttribute(rotate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
-    return WBG_ERR_CUDA;
+  if (const cudaError_t e_ = cudaFuncSetAttribute(rotate_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES))
+    return wbg_cuda_status(e_);
   const long long grid = nk < 2ll * sms ? nk : 2ll * sms;
   rotate_tc_kernel<<<(unsigned)grid, NTHR, SMEM_BYTES, stream>>>((const float2*)U, strideU, (const float2*)X, nFin,
                                                                 fsel, herm, nFrot, (float2*)Xbar, nk);
   return wbg_cuda_status(cudaGetLastError());
 }
 
+int wbg_kubo_tc_run(const double* rec_dE, const void* rec_fE, const void* rec_M, const int* count, int P, int nk,
+                    const double* omega, int nOmega, int nEF, int NC, double eta, int gaussian, int formula, void* out,
+                    cudaStream_t stream) {
+  if (!rec_dE || !rec_fE || !rec_M || !count || !omega || !out || nk < 1 || nOmega < 1 || nEF < 1 || NC < 1 ||
+      !(eta > 0.0))
+    return WBG_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (const cudaError_t e_ = cudaGetDevice(&dev)) return wbg_cuda_status(e_);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return WBG_ERR_CUDA;
+  const int f = formula == WBG_DYN_OPTCOND || formula == WBG_DYN_SHIFT ? formula
+                : (formula >= WBG_DYN_SHC_SIMPLE && formula <= WBG_DYN_SHC_RYOO) ? WBG_DYN_SHC_SIMPLE
+                                                                                  : WBG_DYN_INJECTION;
+  if (NC > KT_NCMAX) return WBG_ERR_ARG;
+  const int ncol = nEF * NC;
+  // column tiles of <= KT_CT columns spanning <= KT_EMAX levels, balanced
+  const int cmax = KT_CT < (KT_EMAX - 1) * NC ? KT_CT : (KT_EMAX - 1) * NC;
+  const int gw = (nOmega + KT_M - 1) / KT_M, gc = (ncol + cmax - 1) / cmax;
+  const int ctile = (ncol + gc - 1) / gc;
+  int gk = sms / (gw * gc);                // one wave of one CTA per SM
+  if (gk < 1) gk = 1;
+  if (gk > nk) gk = nk;
+  const int kc = (nk + gk - 1) / gk;
+  gk = (nk + kc - 1) / kc;
+  if (const cudaError_t e_ = cudaFuncSetAttribute(kubo_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, KT_SMEM))
+    return wbg_cuda_status(e_);
+  kubo_tc<<<dim3(gw, gk, gc), KT_THR, KT_SMEM, stream>>>(rec_dE, (const float*)rec_fE, (const float2*)rec_M, count, P,
+                                                        nk, kc, omega, nOmega, nEF, NC, ctile, (float)eta, gaussian, f,
+                                                        (wbg_u64*)out);
+  return wbg_cuda_status(cudaGetLastError());
+}
+
 #if WBG_TC_TRACE
 extern "C" int wbg_tc_trace_read(unsigned long long* out, unsigned int* n, int clear) {
-  if (cudaDeviceSynchronize() != cudaSuccess) return WBG_ERR_CUDA;
-  if (cudaMemcpyFromSymbol(n, g_tc_trace_n, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+  if (const cudaError_t e_ = cudaDeviceSynchronize()) return wbg_cuda_status(e_);
+  if (const cudaError_t e_ = cudaMemcpyFromSymbol(n, g_tc_trace_n, sizeof(unsigned int))) return wbg_cuda_status(e_);
   const unsigned int m = *n < 8192 ? *n : 8192;
   if (m && cudaMemcpyFromSymbol(out, g_tc_trace, m * sizeof(unsigned long long)) != cudaSuccess) return WBG_ERR_CUDA;
   if (clear) {
@@ -954,11 +1326,11 @@ int wbg_tc_wait_probe_run(int* result, cudaStream_t stream) {
 
 int wbg_device_flags_run(unsigned int* flags, int clear) {
   if (!flags) return WBG_ERR_ARG;
-  if (cudaDeviceSynchronize() != cudaSuccess) return WBG_ERR_CUDA;
-  if (cudaMemcpyFromSymbol(flags, g_wbg_device_flags, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+  if (const cudaError_t e_ = cudaDeviceSynchronize()) return wbg_cuda_status(e_);
+  if (const cudaError_t e_ = cudaMemcpyFromSymbol(flags, g_wbg_device_flags, sizeof(unsigned int))) return wbg_cuda_status(e_);
   if (clear) {
     const unsigned int zero = 0;
-    if (cudaMemcpyToSymbol(g_wbg_device_flags, &zero, sizeof(unsigned int)) != cudaSuccess) return WBG_ERR_CUDA;
+    if (const cudaError_t e_ = cudaMemcpyToSymbol(g_wbg_device_flags, &zero, sizeof(unsigned int))) return wbg_cuda_status(e_);
   }
   return WBG_OK;
 }

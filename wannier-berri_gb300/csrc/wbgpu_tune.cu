@@ -7,7 +7,7 @@
 #include "wbgpu_tune.cuh"
 
 namespace {
-constexpr int kVariants = 5;
+constexpr int kVariants = 6;
 int g_tune[WBG_TUNE_NPARAM][kVariants][WBG_EIGH_NMAX + 1];  // zero-initialised: heuristics
 
 bool valid_key(int param, int nw, int variant) {
@@ -16,6 +16,12 @@ bool valid_key(int param, int nw, int variant) {
 }
 
 int candidates(int param, int nw, int variant, int* values, int capacity) {
+  if (param == WBG_TUNE_KUBO_ENGINE) {  // one setting for every case: variant 0, nw 1
+    if (variant != 0 || nw != 1) return 0;
+    int count = 0;
+    for (int v = 1; v <= 2 && count < capacity; ++v) values[count++] = v;
+    return count;
+  }
   if (param <= WBG_TUNE_EIGH_VECTORS_GROUP) return wbg_eigh_tune_candidates(param, nw, variant, values, capacity);
   return wbg_rotate_tune_candidates(param, nw, variant, values, capacity);
 }

@@ -10,7 +10,7 @@ import os
 
 from . import build as _build
 
-EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
+EXPORTS = ['wbg_abi_version', 'wbg_status_string', 'wbg_last_cuda_error_string', 'wbg_r2k_fields', 'wbg_r2k_workspace_size', 'wbg_r2k',
            'wbg_r2k_columns', 'wbg_ws_replicas',
            'wbg_eigh_workspace_size', 'wbg_eigh_batched', 'wbg_eigh_batched_noalloc', 'wbg_rotate', 'wbg_device_flags', 'wbg_tc_wait_limit', 'wbg_tc_wait_probe', 'wbg_berry_tabulate', 'wbg_berry_scan',
            'wbg_berry_omega', 'wbg_berry_morb', 'wbg_berry_deromega', 'wbg_kubo_workspace_size', 'wbg_kubo',
@@ -71,6 +71,7 @@ _SZ = ctypes.c_size_t
 _SIGS = {
     'wbg_abi_version': (_I, []),
     'wbg_status_string': (ctypes.c_char_p, [_I]),
+    'wbg_last_cuda_error_string': (ctypes.c_char_p, []),
     'wbg_r2k_fields': (_I, [_P, _I, _P, _I, _I, _P, _I, _P, ctypes.POINTER(Lattice), _I, _P, _P]),
     'wbg_r2k_workspace_size': (_I, [ctypes.POINTER(R2KGeom), _I, _I, _I, ctypes.POINTER(_SZ)]),
     'wbg_r2k': (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _P, _SZ, _P, ctypes.POINTER(R2KGeom), _P]),
@@ -143,6 +144,8 @@ def check(status, what):
     if status == STATUS_OK:
         return
     msg = load().wbg_status_string(status).decode()
+    if status == 3:
+        msg += ": " + load().wbg_last_cuda_error_string().decode()
     if status in (1, 2, 5):
         raise ValueError(f"{what}: {msg} (status {status})")
     raise RuntimeError(f"{what}: {msg} (status {status})")

@@ -24,10 +24,10 @@ import numpy as np
 
 from . import _lib
 
-EIGH_TRIDIAG_GROUP, EIGH_QL_BLOCK, EIGH_VECTORS_GROUP, ROTATE_KPOINTS, ROTATE_ENGINE = range(5)
+EIGH_TRIDIAG_GROUP, EIGH_QL_BLOCK, EIGH_VECTORS_GROUP, ROTATE_KPOINTS, ROTATE_ENGINE, KUBO_ENGINE = range(6)
 PARAM_NAMES = {EIGH_TRIDIAG_GROUP: 'eigh_tridiag_group', EIGH_QL_BLOCK: 'eigh_ql_block',
                EIGH_VECTORS_GROUP: 'eigh_vectors_group', ROTATE_KPOINTS: 'rotate_kpoints',
-               ROTATE_ENGINE: 'rotate_engine'}
+               ROTATE_ENGINE: 'rotate_engine', KUBO_ENGINE: 'kubo_engine'}
 EIGH_PARAMS = (EIGH_TRIDIAG_GROUP, EIGH_QL_BLOCK, EIGH_VECTORS_GROUP)
 ROTATE_PARAMS = (ROTATE_KPOINTS, ROTATE_ENGINE)
 # eigh mode and rotation variant (fp64 flag) of each precision of run()
@@ -68,11 +68,12 @@ def reset(nws=range(1, 129)):
     """Every entry of the given num_wann back to the built-in heuristics."""
     for nw in nws:
         for p in EIGH_PARAMS:
-            for v in range(5):
+            for v in range(6):
                 set_value(p, nw, v, 0)
         for p in ROTATE_PARAMS:
             for v in (0, 1):
                 set_value(p, nw, v, 0)
+    set_value(KUBO_ENGINE, 1, 0, 0)
 
 
 def coordinate_descent(params, time_fn, apply_fn, rounds=1):
