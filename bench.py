@@ -163,8 +163,9 @@ def config_dict(args):
 def dtype_of(precision):
     if precision == 'fp64':
         return "f64 / c128 throughout"
-    return ("f64 energies, gaps, scan; double-float (48-bit) H(k), eigensolver and eigenvector back-transform "
-            "(U rounded to c64); double-float velocity transform (rounded to c64), other fields fp32 with "
+    return ("f64 energies, gaps, scan; double-float (48-bit) H(k); fp32 eigensolver refined by one "
+            "Ogita-Aishima step against the double-float H (double-float residuals; energies to ~1e-13 |H|, "
+            "U c64 rounded once); double-float velocity transform (rounded to c64), other fields fp32 with "
             "R-space hi+lo residuals; 3xTF32 tensor-core rotation, fp32 accumulation")
 
 
@@ -227,14 +228,15 @@ def probe_peak(torch, fp64):
     return best / 1e9  # GFLOP/s
 
 
-# DRAM bytes per k-point of the mixed path's eigensolver kernels (dram__bytes_read.sum +
-# dram__bytes_write.sum of eigh_tridiag<df64, cdf, df64>, eigh_ql<df64> and
-# eigh_vectors<df64, df64, float2>) from one ncu --set full capture of the 16^3 case
-# (python bench.py --nkfft 16 --blocks-per-step 1 --steps 1 --warmup 3 --no-cpu-baseline
-# --no-fp64-compare --no-serve --no-tetra --no-configs --no-graphs-tune; 4096 matrices per launch).
-# Each matrix's traffic is its own (H read, reflectors and U written, d / e / tau), so it scales
-# with the matrices of a launch.
-EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 11.3 + 2.1 + 0.0 + 45.2 + 12.7) * 1e6 / 4096
+# DRAM bytes per k-point of the mixed path's eigensolver kernels at nw = 32 (dram__bytes_read.sum +
+# dram__bytes_write.sum of eigh_tridiag<float, cdf, float>, eigh_ql<float>,
+# eigh_vectors<float, float, float2> and the two eigh_refine<cdf> launches) from one ncu capture of
+# the 16^3 case (python bench.py --nkfft 16 --blocks-per-step 1 --steps 1 --warmup 3 --no-cpu-baseline
+# --no-fp64-compare --no-serve --no-tetra --no-configs --no-graphs-tune, ncu --metrics
+# dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum -k regex:eigh_ -s 15 -c 5; 4096
+# matrices per launch).  Each matrix's traffic is its own (H read by the solve and the refinement,
+# reflectors, d / e / tau, U written and re-read), so it scales with the matrices of a launch.
+EIGH_MIXED_DRAM_BYTES_PER_K = (42.0 + 1.1 + 1.1 + 0.0 + 27.3 + 13.6 + 77.1 + 0.4) * 1e6 / 4096
 
 
 def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fields):
@@ -257,9 +259,8 @@ def stage_roofline(stage, ms_total, n_calls, k_per_call, precision, peaks, nF_fi
         work = 20.0 * n ** 3 * k_per_call
         if precision == 'fp64':
             bound, unit, peak, src = 'fp64', 'GFLOP/s', peaks['fp64'], 'wbg_probe_fma FP64 FMA rate measured in this run'
-        else:
-            bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run'
-            pipe_factor = 8.5  # FP32 flops per double-float flop (FMA = 3 FMA + 1 MUL + 10 ADD)
+        else:  # FP32 solve (tridiagonalisation, QL, inverse iteration, back-transform) + refinement
+            bound, unit, peak, src = 'fp32', 'GFLOP/s', peaks['fp32'], 'wbg_probe_fma FP32 FMA rate measured in this run' 
     elif stage == 'rotate':
         work = 16.0 * n ** 3 * 9 * k_per_call      # two complex GEMMs per field, 9 fields
         if precision == 'fp64':
@@ -291,7 +292,7 @@ def _traffic(stage, precision, k_per_call):
     captured case by the k-points of a launch), else None."""
     if stage == 'eigh' and precision == 'mixed':
         return {"traffic": EIGH_MIXED_DRAM_BYTES_PER_K * k_per_call,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three eigh kernels, "
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five eigh launches, "
                                   "16^3 case (4096 matrices) scaled to the k-points of a launch"}
     return {"traffic": None}
 
@@ -388,7 +389,9 @@ def run_gpu(args):
     counts = timer.counts()
     # every timed step is one batch: kernels per batch of each stage (the mixed path calls the
     # eigensolver in two stages around the side-stream field transform, 3 kernels in all)
-    kernels_per_batch = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'r2k_df64c': 3, 'eigh': 3, 'rotate': 1,
+    # eigh: tridiagonalisation, QL, inverse iteration, and the refinement's two launches (mixed, 16 < nw <= 32)
+    kernels_per_batch = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'r2k_df64c': 3,
+                         'eigh': 5 if (precision == 'mixed' and 16 < NW <= 32) else 3, 'rotate': 1,
                          'berry_omega': 1}
     gpu_launches = int(args.steps * sum(kernels_per_batch[k] for k in counts))
 

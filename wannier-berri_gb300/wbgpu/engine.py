@@ -527,10 +527,14 @@ MIXED_FP32_ROTATION_MAX_NW = 32
 # The FP32 back-transform loses ~sqrt(nw) ulps in U, which dominated the mixed path's error
 # against the oracle (AHC at nw = 32: 6.6e-7 of the 8.1e-7 total; nw = 96: 9.5e-6).
 MIXED_EIGH_BITS = EIGH_PRECISE_VECTORS
-# nw <= 32: the FP32 solve refined against the double-float H (EIGH_REFINE) instead: eigenvectors
-# as accurate as the double-float back-transform gives them (|U^H U - I| 3.6e-8 against 3.7e-8 on
-# random nw = 32 matrices), energies to ~1e-13 |H|, in 8.5 instead of 14.0 ms per 55 296 matrices.
+# MIXED_EIGH_REFINE_NW[0] < nw <= [1]: the FP32 solve refined against the double-float H
+# (EIGH_REFINE) instead: eigenvectors as accurate as the double-float back-transform gives them
+# (|U^H U - I| 3.6e-8 against 3.7e-8 on random nw = 32 matrices), energies to ~1e-13 |H|, in 8.5
+# instead of 14.0 ms per 55 296 matrices at nw = 32.  The refinement takes a warp per matrix; at
+# nw <= 16 the double-float solve packs several matrices per warp and stays faster (the nw = 8
+# configuration: 21.8 M k-points/s against 18.1 M refined).
 MIXED_EIGH_REFINE = True
+MIXED_EIGH_REFINE_NW = (16, 32)
 # Transform precision of the mixed path's other k-space fields (lower triangles), and the
 # quantities whose fields are transformed in double-float (rounded to complex64) whatever it is:
 # the velocity, whose FP32 transform error enters D = V / dE (AHC at nw = 32 against the oracle:
@@ -737,7 +741,8 @@ def band_data(dev, dKs, NKFFT, quantities, precision='fp64', phases=None, block_
             mode = 3 | (EIGH_LOWER if lowerH else 0) | EIGH_PRECISE_VECTORS | EIGH_DF64_VECTORS
         else:
             U = arena.buffer('U32', (nkt, nw, nw), torch.complex64)
-            bits = EIGH_REFINE if (MIXED_EIGH_REFINE and nw <= 32) else MIXED_EIGH_BITS
+            refine = MIXED_EIGH_REFINE and MIXED_EIGH_REFINE_NW[0] < nw <= MIXED_EIGH_REFINE_NW[1]
+            bits = EIGH_REFINE if refine else MIXED_EIGH_BITS
             mode = 3 | (EIGH_LOWER if lowerH else 0) | bits
         if quantities:
             # the FP32 fields do not depend on the eigensolver: their transform runs on a side
