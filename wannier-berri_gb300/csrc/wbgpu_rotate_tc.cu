@@ -898,27 +898,34 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
 // MMA K-steps, three products each): a chunk's products go to a fresh TMEM accumulator, so no
 // accumulator takes more than six truncating steps, and the two accumulators alternate, so that
 // the tensor cores fill one while the epilogue drains the other.  The epilogue adds each chunk
-// with round-to-nearest into per-k-point FP32 sums held in registers, and adds those to the
-// fixed-point output once per k-point (order-independent: the same bits in any grid shape).
-// Roles (384 threads, one CTA per SM): warps 0-7 epilogue (TMEM lane quarter = warp & 3, column
-// half = warp >> 2), warps 8-11 operand producers (four operand stages), the first of which
-// also issues the chunk's MMAs once the producers are done with it.  (A thirteenth warp for the
-// issue would put four warps on one SM sub-partition, whose 16K registers then hold at most 128
-// per thread.)  Every mbarrier wait is bounded by the kernel's wait limit, as in the rotation.
+// with round-to-nearest into per-k-point FP32 sums, and adds those to the fixed-point output once
+// per k-point (order-independent: the same bits in any grid shape).
+// Roles (512 threads x 128 registers, one CTA per SM): warps 0-7 epilogue (TMEM lane quarter =
+// warp & 3, column half = warp >> 2: a chunk's loads in two batches), adding each drained chunk
+// into per-k-point FP32 sums in shared memory; warps 8-15 operand producers (two operand stages,
+// records copied three chunks ahead; each thread forms four factors of one frequency row), the
+// first of which also issues the chunk's MMAs once the producers are done with it.  Every mbarrier wait is bounded by the kernel's wait
+// limit, as in the rotation.
 // ---------------------------------------------------------------------------------------
-constexpr int KT_M = 128, KT_CT = 104, KT_NMAX = 2 * KT_CT, KT_RC = 8, KT_K = 2 * KT_RC, KT_NST = 4;
+constexpr int KT_M = 128, KT_CT = 104, KT_NMAX = 2 * KT_CT, KT_RC = 8, KT_K = 2 * KT_RC, KT_NST = 2;
 constexpr int KT_LBO = 128;                          // K-adjacent core matrices contiguous
 constexpr int KT_SBO = (KT_K / 4) * KT_LBO + 16;     // 8-row groups, 16 bytes apart in banks
 constexpr int KT_A_BYTES = (KT_M / 8) * KT_SBO;      // one copy (hi or lo) of F
 constexpr int KT_B_BYTES = (KT_NMAX / 8) * KT_SBO;   // one copy of the embedded G
 constexpr int KT_STAGE = 2 * KT_A_BYTES + 2 * KT_B_BYTES;
-// a chunk's records, copied one chunk ahead: dE, f_E of the tile's levels (<= KT_EMAX), M (<= 27)
+// a chunk's records, copied ahead: dE, f_E of the tile's levels (<= KT_EMAX), M (<= KT_NCMAX)
 constexpr int KT_EMAX = 16, KT_NCMAX = 27;
 constexpr int KT_REC_BYTES = KT_RC * 8 + KT_RC * KT_EMAX * 4 + KT_RC * KT_NCMAX * 8;
-constexpr int KT_SMEM = KT_NST * KT_STAGE + 2 * KT_REC_BYTES;
-constexpr int KT_EPI = 256, KT_PROD0 = 256, KT_PRODN = 128, KT_THR = 12 * 32;
+constexpr int KT_NREC = 4;  // record buffers: copies run KT_NREC - 1 chunks ahead (cp_async_wait_ahead)
+// per-k-point FP32 sums, row = frequency (TMEM lane), KT_ACC_LD floats apart: rows 848 bytes apart
+// fall on eight distinct 16-byte bank groups, so a warp's 16-byte accesses are conflict-free
+constexpr int KT_ACC_LD = KT_NMAX + 4;
+constexpr int KT_ACC_BYTES = KT_M * KT_ACC_LD * 4;
+constexpr int KT_SMEM = KT_NST * KT_STAGE + KT_NREC * KT_REC_BYTES + KT_ACC_BYTES;
+constexpr int KT_EPI = 256, KT_PROD0 = 256, KT_PRODN = 256, KT_THR = 16 * 32;
 constexpr uint32_t KT_TMEM_COLS = 512;               // accumulator of chunk t at column 256 (t & 1)
-static_assert(KT_SMEM <= 220 * 1024, "two operand stages must fit one CTA's shared memory");
+static_assert(KT_SMEM <= 220 * 1024, "operand stages, records and the sums must fit one CTA's shared memory");
+static_assert(KT_ACC_LD % 4 == 0, "16-byte rows of the sums");
 
 WBG_D uint64_t kt_desc(uint32_t saddr) {
   return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(KT_LBO >> 4) << 16) | ((uint64_t)(KT_SBO >> 4) << 32) |
@@ -940,7 +947,8 @@ WBG_D void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 WBG_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-WBG_D void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }  // all but the newest group
+// every group but the newest KT_NREC - 1 complete (KT_NREC = 4)
+WBG_D void cp_async_wait_ahead() { asm volatile("cp.async.wait_group 3;" ::: "memory"); }
 
 // Records r0 .. r0 + rn - 1 of k-point k into a record buffer: dE, f_E of levels e0 .. e0 + ne - 1,
 // the NC components of M; thread i of nthr takes every nthr-th 4- or 8-byte piece.
@@ -958,6 +966,47 @@ WBG_D void kt_stage_records(unsigned char* rb, const double* rec_dE, const float
     const int r = p / NC, c = p - r * NC;
     cp_async8(mm + r * KT_NCMAX + c, rec_M + (rbase + r) * NC + c);
   }
+}
+
+// Bounded wait of the Kubo kernel: mbarrier.try_wait with a suspend-time hint, so that a waiting
+// thread sleeps in the barrier unit (up to 20 us per try) instead of spinning; gives up on an abort
+// by another role or after limit_ns, recording the timeout like pipe_wait.
+WBG_D bool kt_wait(uint32_t mb, uint32_t parity, volatile int* abort_s, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(mb), "r"(parity), "r"(20000u)
+        : "memory");
+    if (ok) return true;
+    if (*abort_s) return false;
+    if (global_ns() - t0 > limit_ns) {
+      *abort_s = 1;
+      atomicOr(&g_wbg_device_flags, (unsigned)WBG_DEVICE_FLAG_TC_TIMEOUT);
+      return false;
+    }
+  }
+}
+
+// x rounded to TF32 (10-bit mantissa, to nearest, ties away from zero: the result of cvt.rna.tf32.f32
+// for finite x) with two integer operations on the full-rate integer pipe
+WBG_D uint32_t tf32_rna_int(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
+// four K-consecutive values split as hi + lo (both TF32) into the two operand copies, as put_split4
+WBG_D void kt_split4(unsigned char* hi, unsigned char* lo, uint32_t off, float a, float b, float c, float d) {
+  uint4 h, l;
+  h.x = tf32_rna_int(a);
+  h.y = tf32_rna_int(b);
+  h.z = tf32_rna_int(c);
+  h.w = tf32_rna_int(d);
+  l.x = tf32_rna_int(a - __uint_as_float(h.x));
+  l.y = tf32_rna_int(b - __uint_as_float(h.y));
+  l.z = tf32_rna_int(c - __uint_as_float(h.z));
+  l.w = tf32_rna_int(d - __uint_as_float(h.w));
+  *reinterpret_cast<uint4*>(hi + off) = h;
+  *reinterpret_cast<uint4*>(lo + off) = l;
 }
 
 WBG_D void tmem_ld8(uint32_t taddr, uint32_t* r) {
@@ -1020,7 +1069,7 @@ __global__ void __launch_bounds__(KT_THR, 1)
   if (tid == 0) {
     for (int i = 0; i < KT_NST + 2; ++i) mbar_init(bar(i));  // one arrival: the MMA commit
     for (int i = 0; i < 2; ++i)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(ACCFREE + i)), "r"(KT_EPI) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(ACCFREE + i)), "r"(KT_EPI / 32) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_s = 0;
   }
@@ -1039,10 +1088,11 @@ __global__ void __launch_bounds__(KT_THR, 1)
   const uint32_t tbase = tmem_base_s;
   const unsigned long long wait_ns = g_tc_wait_ns;
   volatile int* ab = &abort_s;
-  if (warp >= 8 && warp < 12) {
+  if (warp >= KT_PROD0 / 32) {
     // ================= operand producers =================
     const int pt = tid - KT_PROD0;
-    const int w = w0 + pt;  // this thread's row of F
+    const int prow = pt & (KT_M - 1), phalf = pt / KT_M;  // row of F; records 4 phalf .. 4 phalf + 3
+    const int w = w0 + prow;
     const double om = w < nOmega ? omega[w] : 0.0;
     const float wh = (float)om, wl = (float)(om - (double)wh);
     uint32_t last_bar = 0, last_par = 0;  // the issuing thread's last commit
@@ -1054,33 +1104,35 @@ __global__ void __launch_bounds__(KT_THR, 1)
         rr = 0;
       }
     };
-    auto rbuf = [&](int tt) { return smk + KT_NST * KT_STAGE + (int)(tt & 1) * KT_REC_BYTES; };
-    long long kc = k0, kn;
-    int rc = 0, rnx;
+    auto rbuf = [&](int tt) { return smk + KT_NST * KT_STAGE + (tt % KT_NREC) * KT_REC_BYTES; };
+    long long kc = k0, kf;  // the chunk being formed, and the next one to copy
+    int rc = 0, rf;
     skip_empty(kc, rc);
-    if (kc < k1)
-      kt_stage_records(rbuf(0), rec_dE, rec_fE, rec_M, kc * (long long)P + rc, min(KT_RC, count[kc] - rc), nEF, e0, ne,
-                       NC, pt, KT_PRODN);
-    cp_async_commit();
-    kn = kc;
-    rnx = rc + KT_RC;
-    skip_empty(kn, rnx);
+    kf = kc;
+    rf = rc;
+    auto prefetch = [&](int tt) {  // the records of chunk kf / rf into buffer tt, then advance kf / rf
+      if (kf < k1) {
+        kt_stage_records(rbuf(tt), rec_dE, rec_fE, rec_M, kf * (long long)P + rf, min(KT_RC, count[kf] - rf), nEF,
+                         e0, ne, NC, pt, KT_PRODN);
+        rf += KT_RC;
+        skip_empty(kf, rf);
+      }
+      cp_async_commit();  // one group per chunk, empty past the last
+    };
+    for (int tt = 0; tt < KT_NREC - 1; ++tt) prefetch(tt);
     for (int t = 0; kc < k1; ++t) {
       const int s = (int)(t % KT_NST), rn = min(KT_RC, count[kc] - rc);
       bool ok = true;
       if (lane == 0 && t >= KT_NST)
-        ok = pipe_wait(bar(EMPTY + s), (uint32_t)((t / KT_NST - 1) & 1), ab, wait_ns);
+        ok = kt_wait(bar(EMPTY + s), (uint32_t)((t / KT_NST - 1) & 1), ab, wait_ns);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (named_any(1, KT_PRODN, !ok || *ab)) break;  // one decision for all producers
       unsigned char* Ah = smk + s * KT_STAGE;
       unsigned char* Al = Ah + KT_A_BYTES;
       unsigned char* Bh = Al + KT_A_BYTES;
       unsigned char* Bl = Bh + KT_B_BYTES;
-      if (kn < k1)  // the next chunk's records, in flight while this one is formed
-        kt_stage_records(rbuf(t + 1), rec_dE, rec_fE, rec_M, kn * (long long)P + rnx, min(KT_RC, count[kn] - rnx), nEF,
-                         e0, ne, NC, pt, KT_PRODN);
-      cp_async_commit();
-      cp_async_wait_prev();  // this chunk's records
+      prefetch(t + KT_NREC - 1);  // KT_NREC - 1 chunks ahead (its buffer held chunk t - 1, now read)
+      cp_async_wait_ahead();      // this chunk's records
       named_sync(1, KT_PRODN);
       const unsigned char* rb = rbuf(t);
       const double* rde = reinterpret_cast<const double*>(rb);
@@ -1092,18 +1144,20 @@ __global__ void __launch_bounds__(KT_THR, 1)
         de_s[s][pt] = make_float2(h, (float)(de - (double)h));
       }
       named_sync(1, KT_PRODN);
-      // A: row pt, records (2q, 2q + 1) -> K entries 4q .. 4q + 3
-#pragma unroll 1
-      for (int q = 0; q < KT_RC / 2; ++q) {
+      // A: row prow, records (2q, 2q + 1) -> K entries 4q .. 4q + 3, q = 2 phalf, 2 phalf + 1
+#pragma unroll
+      for (int qq = 0; qq < 2; ++qq) {
+        const int q = 2 * phalf + qq;
         float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
         if (w < nOmega) {
           const float2 a = de_s[s][2 * q], b = de_s[s][2 * q + 1];
           if (2 * q < rn) f0 = kt_factor(fgroup, a.x, a.y, wh, wl, eta, gaussian);
           if (2 * q + 1 < rn) f1 = kt_factor(fgroup, b.x, b.y, wh, wl, eta, gaussian);
         }
-        put_split4(Ah, Al, kt_off(pt, 4 * q), f0.x, f0.y, f1.x, f1.y);
+        kt_split4(Ah, Al, kt_off(prow, 4 * q), f0.x, f0.y, f1.x, f1.y);
       }
       // B: rows 2j, 2j + 1 for column j of the tile, records (2q, 2q + 1)
+#pragma unroll 2
       for (int idx = pt; idx < nct * (KT_RC / 2); idx += KT_PRODN) {
         const int j = idx % nct, q = idx / nct;
         const int col = col0 + j, e = col / NC, c = col - e * NC;
@@ -1118,15 +1172,15 @@ __global__ void __launch_bounds__(KT_THR, 1)
             g[h] = make_float2(fe * m.x, fe * m.y);
           }
         }
-        put_split4(Bh, Bl, kt_off(2 * j, 4 * q), g[0].x, -g[0].y, g[1].x, -g[1].y);
-        put_split4(Bh, Bl, kt_off(2 * j + 1, 4 * q), g[0].y, g[0].x, g[1].y, g[1].x);
+        kt_split4(Bh, Bl, kt_off(2 * j, 4 * q), g[0].x, -g[0].y, g[1].x, -g[1].y);
+        kt_split4(Bh, Bl, kt_off(2 * j + 1, 4 * q), g[0].y, g[0].x, g[1].y, g[1].x);
       }
       fence_async_smem();
       named_sync(1, KT_PRODN);
       // ---- MMA issue (one thread): the chunk's operands are complete; the accumulators are
       // free once the epilogue has drained the previous chunk
       const int b = (int)(t & 1);  // accumulator buffer: the epilogue drains the other meanwhile
-      if (pt == 0 && (t < 2 || pipe_wait(bar(ACCFREE + b), (uint32_t)((t / 2 - 1) & 1), ab, wait_ns))) {
+      if (pt == 0 && (t < 2 || kt_wait(bar(ACCFREE + b), (uint32_t)((t / 2 - 1) & 1), ab, wait_ns))) {
         tc_fence_after();
         const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
         const uint32_t D = tbase + (uint32_t)(256 * b);
@@ -1142,73 +1196,77 @@ __global__ void __launch_bounds__(KT_THR, 1)
         last_bar = bar(ACCFULL + b);
         last_par = (uint32_t)((t / 2) & 1);
       }
-      kc = kn;
-      rc = rnx;
-      if (kn < k1) {
-        rnx += KT_RC;
-        skip_empty(kn, rnx);
-      }
+      rc += KT_RC;
+      skip_empty(kc, rc);
     }
     cp_async_wait_all();  // no copy in flight at exit
     if (pt == 0 && *ab && last_bar) mbar_wait(last_bar, last_par, DRAIN_NS);  // no product in flight at exit
   } else {
     // ================= epilogue =================
-    const int quarter = warp & 3, half = warp >> 2;
-    const int row = 32 * quarter + lane, w = w0 + row;
-    const int nh = N / 2, n8 = nh / 8;  // this warp's columns [half nh, (half + 1) nh), in pieces of 8
-    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
-    const uint32_t D0 = tbase + lane_base + (uint32_t)(half * nh);
+    const int quarter = warp & 3, half = warp >> 2, row = 32 * quarter + lane, w = w0 + row;
+    const int nh = N / 2, n8 = nh / 8;  // this warp's columns [half nh, (half + 1) nh), pieces of 8
+    const uint32_t D0 = tbase + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(half * nh);
+    float* accs = reinterpret_cast<float*>(smk + KT_NST * KT_STAGE + KT_NREC * KT_REC_BYTES) + row * KT_ACC_LD +
+                  half * nh;
     wbg_u64* bad = out + 4 * (long long)nEF * nOmega * NC;
-    float acc[KT_CT];
-#pragma unroll
-    for (int i = 0; i < KT_CT; ++i) acc[i] = 0.f;
     int t = 0;
-    for (long long k = k0; k < k1; ++k) {
+    bool stop = false;
+    for (long long k = k0; k < k1 && !stop; ++k) {
       const int nrec = count[k];
-      bool stop = false;
       for (int r0 = 0; r0 < nrec; r0 += KT_RC, ++t) {
+        const int b = t & 1;
         bool ok = true;
-        const int b = (int)(t & 1);
-        if (lane == 0) ok = pipe_wait(bar(ACCFULL + b), (uint32_t)((t / 2) & 1), ab, wait_ns);
+        if (lane == 0) ok = kt_wait(bar(ACCFULL + b), (uint32_t)((t / 2) & 1), ab, wait_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (named_any(2, KT_EPI, !ok || *ab)) {
+        if (!ok) {  // a warp-wide decision: the epilogue warps share no barrier after this point
           stop = true;
           break;
         }
         tc_fence_after();
         const uint32_t D = D0 + (uint32_t)(256 * b);
+        constexpr int PH = (KT_CT / 8 + 1) / 2;  // pieces per batch of loads
 #pragma unroll
-        for (int p = 0; p < KT_CT / 8; p += 2) {  // two pieces of 8 columns per wait
-          if (p < n8) {
-            uint32_t v[2][8];
+        for (int h2 = 0; h2 < 2; ++h2) {
+          uint32_t v[PH][8];
 #pragma unroll
-            for (int u = 0; u < 2; ++u)
-              if (p + u < n8) tmem_ld8(D + 8 * (p + u), v[u]);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int u = 0; u < 2; ++u)
-              if (p + u < n8) {
-                tmem_ld_wait8(v[u]);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) acc[8 * (p + u) + i] += __uint_as_float(v[u][i]);
-              }
+          for (int p = 0; p < PH; ++p)
+            if (h2 * PH + p < n8) tmem_ld8(D + 8 * (h2 * PH + p), v[p]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (h2 == 1) {
+            tc_fence_before();
+            __syncwarp();  // every lane's loads are complete: one arrival per warp frees the accumulator
+            if (lane == 0) mbar_arrive(bar(ACCFREE + b));
           }
-        }
-        tc_fence_before();
-        mbar_arrive(bar(ACCFREE + b));
-      }
-      if (stop) break;
-      if (nrec > 0) {  // the k-point's sums into the fixed-point output
 #pragma unroll
-        for (int i = 0; i < KT_CT; i += 2) {
-          const int j = (half * nh + i) / 2;  // complex column of the tile
-          if (i < nh && j < nct && w < nOmega) {
+          for (int p = 0; p < PH; ++p)
+            if (h2 * PH + p < n8) {
+              tmem_ld_wait8(v[p]);
+              float4* a4 = reinterpret_cast<float4*>(accs + 8 * (h2 * PH + p));
+              float4 x = a4[0], y = a4[1];
+              x.x += __uint_as_float(v[p][0]);
+              x.y += __uint_as_float(v[p][1]);
+              x.z += __uint_as_float(v[p][2]);
+              x.w += __uint_as_float(v[p][3]);
+              y.x += __uint_as_float(v[p][4]);
+              y.y += __uint_as_float(v[p][5]);
+              y.z += __uint_as_float(v[p][6]);
+              y.w += __uint_as_float(v[p][7]);
+              a4[0] = x;
+              a4[1] = y;
+            }
+        }
+      }
+      if (!stop && nrec > 0) {  // the k-point's sums into the fixed-point output
+        for (int jj = 0; 2 * jj < nh; ++jj) {
+          const int j = (half * nh) / 2 + jj;  // complex column of the tile
+          const float2 a = reinterpret_cast<const float2*>(accs)[jj];
+          reinterpret_cast<float2*>(accs)[jj] = make_float2(0.f, 0.f);
+          if (j < nct && w < nOmega) {
             const int col = col0 + j, e = col / NC, c = col - e * NC;
             wbg_u64* o = out + 4 * (((long long)e * nOmega + w) * NC + c);
-            fx_add_double(o, (double)acc[i], bad);
-            fx_add_double(o + 2, (double)acc[i + 1], bad);
+            fx_add_double(o, (double)a.x, bad);
+            fx_add_double(o + 2, (double)a.y, bad);
           }
-          acc[i] = acc[i + 1] = 0.f;
         }
       }
     }
