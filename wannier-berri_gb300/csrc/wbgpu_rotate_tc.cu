@@ -895,11 +895,12 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
 // F is formed in FP32 from dE - w taken as (dE_hi - w_hi) + (dE_lo - w_lo) (double-float halves:
 // the difference to FP32 accuracy without the FP64 pipe).  Operands are split into TF32 hi + lo
 // (3xTF32) as in the rotation.  The records of one k-point run in chunks of KT_RC = 8 (K = 16, two
-// MMA K-steps, three products each): a chunk's products go to a fresh TMEM accumulator, so no
-// accumulator takes more than six truncating steps, and the two accumulators alternate, so that
-// the tensor cores fill one while the epilogue drains the other.  The epilogue adds each chunk
-// with round-to-nearest into per-k-point FP32 sums, and adds those to the fixed-point output once
-// per k-point (order-independent: the same bits in any grid shape).
+// MMA K-steps, three products each); KT_FILL = 2 consecutive chunks of a k-point go to a fresh TMEM
+// accumulator, so no accumulator takes more than twelve truncating steps (at most ~3e-7 relative
+// drift toward zero), and the two accumulators alternate, so that the tensor cores fill one while
+// the epilogue drains the other.  The epilogue adds each fill with round-to-nearest into
+// per-k-point FP32 sums, and adds those to the fixed-point output once per k-point
+// (order-independent: the same bits in any grid shape).
 // Roles (512 threads x 128 registers, one CTA per SM): warps 0-7 epilogue (TMEM lane quarter =
 // warp & 3, column half = warp >> 2: a chunk's loads in two batches), adding each drained chunk
 // into per-k-point FP32 sums in shared memory; warps 8-15 operand producers (two operand stages,
@@ -908,6 +909,7 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
 // limit, as in the rotation.
 // ---------------------------------------------------------------------------------------
 constexpr int KT_M = 128, KT_CT = 104, KT_NMAX = 2 * KT_CT, KT_RC = 8, KT_K = 2 * KT_RC, KT_NST = 2;
+constexpr int KT_FILL = 2;  // chunks per accumulator fill: <= 12 truncating steps before a drain
 constexpr int KT_LBO = 128;                          // K-adjacent core matrices contiguous
 constexpr int KT_SBO = (KT_K / 4) * KT_LBO + 16;     // 8-row groups, 16 bytes apart in banks
 constexpr int KT_A_BYTES = (KT_M / 8) * KT_SBO;      // one copy (hi or lo) of F
@@ -1120,6 +1122,7 @@ __global__ void __launch_bounds__(KT_THR, 1)
       cp_async_commit();  // one group per chunk, empty past the last
     };
     for (int tt = 0; tt < KT_NREC - 1; ++tt) prefetch(tt);
+    int f = -1;  // fill sequence number
     for (int t = 0; kc < k1; ++t) {
       const int s = (int)(t % KT_NST), rn = min(KT_RC, count[kc] - rc);
       bool ok = true;
@@ -1179,22 +1182,26 @@ __global__ void __launch_bounds__(KT_THR, 1)
       named_sync(1, KT_PRODN);
       // ---- MMA issue (one thread): the chunk's operands are complete; the accumulators are
       // free once the epilogue has drained the previous chunk
-      const int b = (int)(t & 1);  // accumulator buffer: the epilogue drains the other meanwhile
-      if (pt == 0 && (t < 2 || kt_wait(bar(ACCFREE + b), (uint32_t)((t / 2 - 1) & 1), ab, wait_ns))) {
+      // fills of up to KT_FILL chunks of one k-point per accumulator; the two accumulators alternate
+      const int cik = rc / KT_RC;  // chunk of the k-point
+      const bool first = cik % KT_FILL == 0, lastc = cik % KT_FILL == KT_FILL - 1 || rc + KT_RC >= count[kc];
+      if (first) ++f;
+      const int b = f & 1;
+      if (pt == 0 && (!first || f < 2 || kt_wait(bar(ACCFREE + b), (uint32_t)((f / 2 - 1) & 1), ab, wait_ns))) {
         tc_fence_after();
         const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
         const uint32_t D = tbase + (uint32_t)(256 * b);
 #pragma unroll
         for (int ks = 0; ks < KT_K / 8; ++ks) {
           const uint32_t so = (uint32_t)ks * 2 * KT_LBO;
-          kt_mma(D, kt_desc(ah + so), kt_desc(bh + so), idesc, ks > 0);
+          kt_mma(D, kt_desc(ah + so), kt_desc(bh + so), idesc, ks > 0 || !first);
           kt_mma(D, kt_desc(al + so), kt_desc(bh + so), idesc, 1);
           kt_mma(D, kt_desc(ah + so), kt_desc(bl + so), idesc, 1);
         }
         mma_commit(bar(EMPTY + s));
-        mma_commit(bar(ACCFULL + b));
-        last_bar = bar(ACCFULL + b);
-        last_par = (uint32_t)((t / 2) & 1);
+        last_bar = bar(EMPTY + s);  // completes once every product issued so far has
+        last_par = (uint32_t)((t / KT_NST) & 1);
+        if (lastc) mma_commit(bar(ACCFULL + b));
       }
       rc += KT_RC;
       skip_empty(kc, rc);
@@ -1209,11 +1216,11 @@ __global__ void __launch_bounds__(KT_THR, 1)
     float* accs = reinterpret_cast<float*>(smk + KT_NST * KT_STAGE + KT_NREC * KT_REC_BYTES) + row * KT_ACC_LD +
                   half * nh;
     wbg_u64* bad = out + 4 * (long long)nEF * nOmega * NC;
-    int t = 0;
+    int t = 0;  // fill sequence number
     bool stop = false;
     for (long long k = k0; k < k1 && !stop; ++k) {
       const int nrec = count[k];
-      for (int r0 = 0; r0 < nrec; r0 += KT_RC, ++t) {
+      for (int r0 = 0; r0 < nrec; r0 += KT_FILL * KT_RC, ++t) {
         const int b = t & 1;
         bool ok = true;
         if (lane == 0) ok = kt_wait(bar(ACCFULL + b), (uint32_t)((t / 2) & 1), ab, wait_ns);
