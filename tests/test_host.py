@@ -44,6 +44,31 @@ def test_workspace_queries_without_gpu():
         _lib.check(1, "x")
     with pytest.raises(RuntimeError):
         _lib.check(3, "x")
+    assert lib.wbg_last_cuda_error_string().decode()  # "none", or the runtime's message
+
+
+def test_eigh_flag_words():
+    """The eigensolver's error word: bit 0 (QL did not converge) raises, bit 2 (refined solve: a
+    cluster wider than the Rayleigh-Ritz block, or a matrix that did not settle) warns."""
+    import warnings
+    torch = pytest.importorskip("torch")
+    engine.check_flags([torch.zeros(1, dtype=torch.int32)])
+    with pytest.raises(RuntimeError):
+        engine.check_flags([torch.zeros(1, dtype=torch.int32), torch.tensor([1], dtype=torch.int32)])
+    with pytest.raises(RuntimeError):
+        engine.check_flags([torch.tensor([5], dtype=torch.int32)])
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        engine.check_flags([torch.tensor([4], dtype=torch.int32), torch.zeros(1, dtype=torch.int32)])
+    assert any(issubclass(x.category, RuntimeWarning) for x in w)
+
+
+def test_mixed_eigensolver_plan():
+    """The mixed path refines an FP32 solve at 16 < nw <= 32 and keeps the double-float solve with
+    precise eigenvectors elsewhere (the mode bits of wbg_eigh_batched)."""
+    assert engine.EIGH_REFINE == 256 and engine.EIGH_PRECISE_VECTORS == 64
+    lo, hi = engine.MIXED_EIGH_REFINE_NW
+    assert (lo, hi) == (16, 32) and engine.MIXED_EIGH_REFINE
 
 
 def test_rgeometry_structure():
