@@ -5,6 +5,7 @@ and the next call on the same context is correct.
 * wbg_tc_wait_probe waits on an mbarrier phase that never completes, with a 1 ms bound.
 * the rotation itself with a 0 ns bound: a block whose products are not done when it first looks
   gives up; afterwards, with the normal bound, the rotation is correct and unflagged.
+* the tensor-core Kubo sums with a 0 ns bound, then the same run again with the normal bound.
 """
 import ctypes
 
@@ -70,3 +71,32 @@ def test_rotation_timeout_then_recovery():
     assert _flags() == 0
     err = float((got.to(torch.complex128) - ref).abs().max() / ref.abs().max())
     assert err < 2e-6, err
+
+
+def test_kubo_timeout_then_recovery():
+    """The tensor-core Kubo sums (kubo_tc) with a 0 ns bound on every wait: blocks that find a
+    barrier not yet complete give up (producers, issuing thread and epilogue alike), drain their
+    products and free their tensor memory; afterwards, with the normal bound, the same run gives
+    the same bits as before the timeout and no flag."""
+    import wbgpu
+    from wbgpu import models, system as wsys
+    lib = _lib.load()
+    s = wsys.System_R.from_dict(models.config_system(2, small=True))
+    s.do_ws_dist(3)
+    mk = lambda: {'opt': wbgpu.calculators.OpticalConductivity(Efermi=np.linspace(-0.6, 0.6, 5),
+                                                               omega=np.linspace(0.0, 3.0, 200),
+                                                               smr_fixed_width=0.1)}
+    grid = wbgpu.Grid(s, NKdiv=1, NKFFT=(4, 4, 4))
+    before = wbgpu.run(s, grid, mk(), precision='mixed')['opt'].data
+    _flags()
+    try:
+        _lib.check(lib.wbg_tc_wait_limit(ctypes.c_ulonglong(0)), "wbg_tc_wait_limit")
+        wbgpu.run(s, grid, mk(), precision='mixed')
+        torch.cuda.synchronize()
+        _flags()  # whether a block gave up depends on timing; the recovery below must hold either way
+    finally:
+        _lib.check(lib.wbg_tc_wait_limit(ctypes.c_ulonglong(DEFAULT_NS)), "wbg_tc_wait_limit")
+    after = wbgpu.run(s, grid, mk(), precision='mixed')['opt'].data
+    torch.cuda.synchronize()
+    assert _flags() == 0
+    assert np.array_equal(before, after)

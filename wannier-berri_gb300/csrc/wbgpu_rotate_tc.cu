@@ -902,11 +902,11 @@ __global__ void __launch_bounds__(PIPE_THR, 1)
 // per-k-point FP32 sums, and adds those to the fixed-point output once per k-point
 // (order-independent: the same bits in any grid shape).
 // Roles (512 threads x 128 registers, one CTA per SM): warps 0-7 epilogue (TMEM lane quarter =
-// warp & 3, column half = warp >> 2: a chunk's loads in two batches), adding each drained chunk
-// into per-k-point FP32 sums in shared memory; warps 8-15 operand producers (two operand stages,
+// warp & 3, column half = warp >> 2: a fill's loads in two batches), adding each drained fill into
+// per-k-point FP32 sums in shared memory; warps 8-15 operand producers (two operand stages,
 // records copied three chunks ahead; each thread forms four factors of one frequency row), the
-// first of which also issues the chunk's MMAs once the producers are done with it.  Every mbarrier wait is bounded by the kernel's wait
-// limit, as in the rotation.
+// first of which also issues the chunk's MMAs once the producers are done with it.  Every mbarrier
+// wait is bounded by the kernel's wait limit, as in the rotation.
 // ---------------------------------------------------------------------------------------
 constexpr int KT_M = 128, KT_CT = 104, KT_NMAX = 2 * KT_CT, KT_RC = 8, KT_K = 2 * KT_RC, KT_NST = 2;
 constexpr int KT_FILL = 2;  // chunks per accumulator fill: <= 12 truncating steps before a drain
