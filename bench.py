@@ -389,9 +389,9 @@ def run_gpu(args):
     counts = timer.counts()
     # every timed step is one batch: kernels per batch of each stage (the mixed path calls the
     # eigensolver in two stages around the side-stream field transform, 3 kernels in all)
-    # eigh: tridiagonalisation, QL, inverse iteration, and the refinement's two launches (mixed, 16 < nw <= 32)
+    # eigh: tridiagonalisation, QL, inverse iteration, and the refinement's two launches (mixed, 24 < nw <= 32)
     kernels_per_batch = {'r2k_fp64': 3, 'r2k_fp32': 3, 'r2k_df64': 3, 'r2k_df64c': 3,
-                         'eigh': 5 if (precision == 'mixed' and 16 < NW <= 32) else 3, 'rotate': 1,
+                         'eigh': 5 if (precision == 'mixed' and 24 < NW <= 32) else 3, 'rotate': 1,
                          'berry_omega': 1}
     gpu_launches = int(args.steps * sum(kernels_per_batch[k] for k in counts))
 

@@ -379,7 +379,9 @@ int wbg_berry_morb(const double* E, const void* Xbar, int nFbar, int iV, int iA,
  * (formula/formula.py:95-118); BerryDipole_FermiSea (calculators/static.py:472-487).
  * Xbar: V at iV (3), A at iA (3), rotA at iO (3), d_a d_b H at iW (9, [a][b]),
  * d_d A_b at idA (9, [b][d]), d_d rotA_c at idO (9, [c][d]).
- * hist [scan.nEF][3][3] ([c][d], before the calculator's swap of the last two axes). */
+ * hist [scan.nEF][3][3] ([c][d], before the calculator's swap of the last two axes).
+ * fp64: 1 complex128 Xbar and FP64 arithmetic; 0 complex64 Xbar, FP32 arithmetic; 2 complex64
+ * Xbar, double-float arithmetic (the mixed path). */
 int wbg_berry_deromega(const double* E, const void* Xbar, int nFbar, int iV, int iA, int iO, int iW, int idA,
                        int idO, int nw, int nk, const wbg_scan* scan, int internal_terms, int external_terms,
                        void* hist, int fp64, void* stream);

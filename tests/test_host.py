@@ -64,11 +64,13 @@ def test_eigh_flag_words():
 
 
 def test_mixed_eigensolver_plan():
-    """The mixed path refines an FP32 solve at 16 < nw <= 32 and keeps the double-float solve with
-    precise eigenvectors elsewhere (the mode bits of wbg_eigh_batched)."""
+    """The mixed path refines an FP32 solve at 24 < nw <= 32 and keeps the double-float solve with
+    precise eigenvectors elsewhere (the mode bits of wbg_eigh_batched); its Berry-curvature dipole
+    runs in double-float arithmetic on the complex64 fields."""
     assert engine.EIGH_REFINE == 256 and engine.EIGH_PRECISE_VECTORS == 64
     lo, hi = engine.MIXED_EIGH_REFINE_NW
-    assert (lo, hi) == (16, 32) and engine.MIXED_EIGH_REFINE
+    assert (lo, hi) == (24, 32) and engine.MIXED_EIGH_REFINE
+    assert engine.MIXED_DEROMEGA_ARITH == 2
 
 
 def test_rgeometry_structure():

@@ -228,6 +228,20 @@ template <typename T> WBG_D T recip_gap(double dE);
 template <> WBG_D double recip_gap<double>(double dE) { return 1.0 / dE; }
 // FP64 difference (no cancellation loss), FP32 reciprocal
 template <> WBG_D float recip_gap<float>(double dE) { return 1.0f / (float)dE; }
+// FP64 difference, double-float reciprocal
+template <> WBG_D df64 recip_gap<df64>(double dE) { return df_from_f(1.0f) / df_from(dE); }
+
+// a stored complex element in the arithmetic's complex type (FP32 storage, double-float arithmetic)
+template <typename V, typename S> WBG_D V ld_c(S a) { return a; }
+template <> WBG_D cdf ld_c<cdf, float2>(float2 a) {
+  cdf r;
+  r.x = df_from_f(a.x);
+  r.y = df_from_f(a.y);
+  return r;
+}
+WBG_D double to_dbl(float x) { return (double)x; }
+WBG_D double to_dbl(double x) { return x; }
+WBG_D double to_dbl(df64 x) { return df_to_double(x); }
 
 // 1/(E_n - E_l), 0 below 1e-7 (degenerate pairs).  FP64 path: native doubles.  FP32 path: the
 // energies are held as double-float pairs (Eh + El = E to 48 bits); Eh_n - Eh_l is exact when
@@ -1425,8 +1439,8 @@ __global__ void berry_morb_kernel(const double* __restrict__ E, const typename C
 // over (s,a,b) in {(+1, alpha_c, beta_c), (-1, beta_c, alpha_c)}; the group value is
 // sum_{m in G} 2 Re S^{cd}.  hist is [nEF][3][3] (c, d) -- the calculator swaps c and d.
 // ---------------------------------------------------------------------------------------
-template <typename T>
-__global__ void berry_deromega_kernel(const double* __restrict__ E, const typename C2<T>::t* __restrict__ Xbar,
+template <typename T, typename VS = typename C2<T>::t>
+__global__ void berry_deromega_kernel(const double* __restrict__ E, const VS* __restrict__ Xbar,
                                       int nFbar, int iV, int iA, int iO, int iW, int idA, int idO, int nw, int nk,
                                       int L, int G, int table, WbgScan sp, int internal_terms, int external_terms,
                                       wbg_u64* __restrict__ hist, int shist, BandSel bs) {
@@ -1457,7 +1471,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
       for (int idx = lane; idx < nw * nw; idx += L) {  // dinv(x, y) = 1/(E_x - E_y), 0 below 1e-7
         const int x = idx / nw, y = idx % nw;
         const double dE = myE[x] - myE[y];
-        myDinv[idx] = fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+        myDinv[idx] = fabs(dE) < 1e-7 ? Arith<T>::from(0.0) : recip_gap<T>(dE);
       }
     __syncwarp();
     int bandmax;
@@ -1477,18 +1491,18 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
       f0 = group_min_i(f0, L);
       bandmax = min(below, f0);
     }
-    const V* Xk = Xbar + kk * nFbar * nw2;
-#define XV(a, x, y) Xk[(iV + (a)) * nw2 + (x) * nw + (y)]
-#define XA(a, x, y) Xk[(iA + (a)) * nw2 + (x) * nw + (y)]
-#define XO(a, x, y) Xk[(iO + (a)) * nw2 + (x) * nw + (y)]
-#define XW(a, b, x, y) Xk[(iW + 3 * (a) + (b)) * nw2 + (x) * nw + (y)]
-#define XdA(b, d, x, y) Xk[(idA + 3 * (b) + (d)) * nw2 + (x) * nw + (y)]
-#define XdO(c, d, x, y) Xk[(idO + 3 * (c) + (d)) * nw2 + (x) * nw + (y)]
+    const VS* Xk = Xbar + kk * nFbar * nw2;
+#define XV(a, x, y) ld_c<V>(Xk[(iV + (a)) * nw2 + (x) * nw + (y)])
+#define XA(a, x, y) ld_c<V>(Xk[(iA + (a)) * nw2 + (x) * nw + (y)])
+#define XO(a, x, y) ld_c<V>(Xk[(iO + (a)) * nw2 + (x) * nw + (y)])
+#define XW(a, b, x, y) ld_c<V>(Xk[(iW + 3 * (a) + (b)) * nw2 + (x) * nw + (y)])
+#define XdA(b, d, x, y) ld_c<V>(Xk[(idA + 3 * (b) + (d)) * nw2 + (x) * nw + (y)])
+#define XdO(c, d, x, y) ld_c<V>(Xk[(idO + 3 * (c) + (d)) * nw2 + (x) * nw + (y)])
     // 1/(E_x - E_y) from the table, or recomputed when the table does not fit in shared memory
     auto dinv = [&](int x, int y) -> T {
       if (table) return myDinv[x * nw + y];
       const double dE = myE[x] - myE[y];
-      return fabs(dE) < 1e-7 ? T(0) : recip_gap<T>(dE);
+      return fabs(dE) < 1e-7 ? Arith<T>::from(0.0) : recip_gap<T>(dE);
     };
 #define DV(a, x, y) cscale(XV(a, x, y), -dinv((x), (y)))
     for (int m = lane; m < nw; m += L) {
@@ -1582,15 +1596,15 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
               for (int t = 0; t < 2; ++t) {
                 const double sg = t == 0 ? 1.0 : -1.0;
                 const int a = t == 0 ? al : be, b = t == 0 ? be : al;
-                if (internal_terms) acc += sg * (double)cmul(Dml[a], dDlm[3 * b + d]).y;  // Re(-i s x) = s Im x
+                if (internal_terms) acc += sg * to_dbl(cmul(Dml[a], dDlm[3 * b + d]).y);  // Re(-i s x) = s Im x
                 if (external_terms) {
-                  acc -= sg * (double)cmul(Dml[a], dAlm[3 * b + d]).x;
-                  acc -= sg * (double)cmul(dDml[3 * a + d], XA(b, l, m)).x;
+                  acc -= sg * to_dbl(cmul(Dml[a], dAlm[3 * b + d]).x);
+                  acc -= sg * to_dbl(cmul(dDml[3 * a + d], XA(b, l, m)).x);
                 }
               }
               if (external_terms) {  // 1/2 dO_mm: - D^d_ml O^c_lm + O^c_ml D^d_lm
                 const V Dlm_d = DV(d, l, m);
-                acc += 0.5 * ((double)cmul(Dml[d], XO(c, l, m)).x * -1.0 + (double)cmul(XO(c, m, l), Dlm_d).x);
+                acc += 0.5 * (to_dbl(cmul(Dml[d], XO(c, l, m)).x) * -1.0 + to_dbl(cmul(XO(c, m, l), Dlm_d).x));
               }
               val[3 * c + d] += 2.0 * acc;
             }
@@ -1600,7 +1614,7 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
 #pragma unroll
           for (int c = 0; c < 3; ++c)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) val[3 * c + d] += (double)XdO(c, d, m, m).x;  // 2 Re(1/2 dOc_mm)
+            for (int d = 0; d < 3; ++d) val[3 * c + d] += to_dbl(XdO(c, d, m, m).x);  // 2 Re(1/2 dOc_mm)
           // -i s sum_{n' in G} A^a_mn' dA^{bd}_n'm
           for (int np = gs; np < ge; ++np) {
             V dAn[9];
@@ -1631,8 +1645,8 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const typena
               const int al = (c + 1) % 3, be = (c + 2) % 3;
 #pragma unroll
               for (int d = 0; d < 3; ++d) {
-                const double x1 = (double)cmul(XA(al, m, np), dAn[3 * be + d]).y;
-                const double x2 = (double)cmul(XA(be, m, np), dAn[3 * al + d]).y;
+                const double x1 = to_dbl(cmul(XA(al, m, np), dAn[3 * be + d]).y);
+                const double x2 = to_dbl(cmul(XA(be, m, np), dAn[3 * al + d]).y);
                 val[3 * c + d] += 2.0 * (x1 - x2);  // 2 Re(-i s A dA) = 2 s Im(A dA)
               }
             }
@@ -2011,7 +2025,7 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
                            int idO, int nw, int nk, const WbgScan* sp_in, int internal_terms, int external_terms,
                            void* hist, int fp64, cudaStream_t stream, const signed char* sel, double* P) {
   const BandSel bs{sel, P};
-  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P)) return WBG_ERR_ARG;
+  if (nw < 1 || nk < 1 || !sp_in || !E || !Xbar || (!sel) != (!P) || fp64 < 0 || fp64 > 2) return WBG_ERR_ARG;
   if (!sel && (sp_in->nEF < 1 || !hist || !(sp_in->dEF > 0.0))) return WBG_ERR_ARG;
   WbgScan spv = *sp_in;
   if (sel) { spv.nEF = 0; hist = nullptr; }
@@ -2046,11 +2060,17 @@ int wbg_berry_deromega_run(const double* E, const void* Xbar, int nFbar, int iV,
   long long nblk = (nk + G - 1) / G;
   const long long cap = (long long)sms * 8;
   if (nblk > cap) nblk = cap;
-  if (fp64) {
+  if (fp64 == 1) {
     cudaFuncSetAttribute(berry_deromega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<double><<<(int)nblk, G * L, sm, stream>>>(E, (const double2*)Xbar, nFbar, iV, iA, iO, iW,
                                                                     idA, idO, nw, nk, L, G, table, *sp, internal_terms,
                                                                     external_terms, (wbg_u64*)hist, shist, bs);
+  } else if (fp64 == 2) {  // complex64 Xbar, double-float arithmetic
+    cudaFuncSetAttribute(berry_deromega_kernel<df64, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         220 * 1024);
+    berry_deromega_kernel<df64, float2><<<(int)nblk, G * L, sm, stream>>>(
+        E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA, idO, nw, nk, L, G, table, *sp, internal_terms,
+        external_terms, (wbg_u64*)hist, shist, bs);
   } else {
     cudaFuncSetAttribute(berry_deromega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     berry_deromega_kernel<float><<<(int)nblk, G * L, sm, stream>>>(E, (const float2*)Xbar, nFbar, iV, iA, iO, iW, idA,

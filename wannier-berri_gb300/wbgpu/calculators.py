@@ -228,7 +228,7 @@ class BerryDipole_FermiSea(StaticCalculator):
         st = engine._timed('berry_deromega', _lib.load().wbg_berry_deromega, _ptr(bd.E), _ptr(bd.Xbar),
                            bd.Xbar.shape[1], g('V'), g('A'), g('O'), g('W'), g('dA'), g('dO'), bd.nw, bd.nk_total,
                            ctypes.byref(sc), int(self.internal_terms), int(ext), _ptr(self._hist),
-                           int(bd.fp64_fields), _stream())
+                           1 if bd.fp64_fields else engine.MIXED_DEROMEGA_ARITH, _stream())
         _lib.check(st, "wbg_berry_deromega")
 
     def result(self, cell_volume, nk, factor=1.0):

@@ -532,9 +532,11 @@ MIXED_EIGH_BITS = EIGH_PRECISE_VECTORS
 # (|U^H U - I| 3.6e-8 against 3.7e-8 on random nw = 32 matrices), energies to ~1e-13 |H|, in 8.5
 # instead of 14.0 ms per 55 296 matrices at nw = 32.  The refinement takes a warp per matrix; at
 # nw <= 16 the double-float solve packs several matrices per warp and stays faster (the nw = 8
-# configuration: 21.8 M k-points/s against 18.1 M refined).
+# configuration: 21.8 M k-points/s against 18.1 M refined), and at num_wann 18 and 21 of the
+# batched benchmark's systems the refined solve put the Berry-curvature dipole 1.1-1.3e-6 from the
+# FP64 path (0.5-0.8e-6 with the double-float solve): the refinement serves 24 < nw <= 32.
 MIXED_EIGH_REFINE = True
-MIXED_EIGH_REFINE_NW = (16, 32)
+MIXED_EIGH_REFINE_NW = (24, 32)
 # Transform precision of the mixed path's other k-space fields (lower triangles), and the
 # quantities whose fields are transformed in double-float (rounded to complex64) whatever it is:
 # the velocity, whose FP32 transform error enters D = V / dE (AHC at nw = 32 against the oracle:
@@ -542,6 +544,11 @@ MIXED_EIGH_REFINE_NW = (16, 32)
 # Berry-curvature dipole on two 12^3 blocks: 1.9e-6 and 4.8e-7).
 MIXED_FIELDS_PREC = 3  # PREC_FP32S
 MIXED_DF64_QUANTITIES = {'V'}
+# Arithmetic of the mixed path's Berry-curvature dipole (wbg_berry_deromega fp64 argument): 2 =
+# double-float on the complex64 band-basis fields.  Its sums over intermediate bands of V D terms
+# cancel strongly near degeneracies; in FP32 they put the BCD of a num_wann = 82 system 3.9e-6 from
+# the FP64 path (the complex64 rounding of the fields alone: 6e-8).
+MIXED_DEROMEGA_ARITH = 2
 
 
 def _prec(p):
