@@ -220,3 +220,17 @@ def test_tabulate_and_sdct_names_point_elsewhere():
                 getattr(ns, n)()
     with pytest.raises(NotImplementedError, match=r"wbgpu\.tabulate\(system, grid"):
         C.TabulatorAll({})
+
+
+def test_deromega_rejects_unknown_arithmetic():
+    """wbg_berry_deromega takes fp64 = 0 (FP32), 1 (FP64) or 2 (complex64 fields, double-float
+    arithmetic); anything else is a bad argument, refused before any device work."""
+    import ctypes
+    lib = _lib.load()
+    sc = _lib.Scan(EFmin=-1.0, EFmax=1.0, dEF=0.1, degen_thresh=1e-4, nEF=21)
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the argument checks come first
+    for bad in (3, -1):
+        st = lib.wbg_berry_deromega(dummy, dummy, 21, 0, 3, 6, 9, 12, 3, 8, 10, ctypes.byref(sc), 1, 1, dummy,
+                                    bad, None)
+        assert st == 1, (bad, st)
+
