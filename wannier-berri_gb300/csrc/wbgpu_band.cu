@@ -239,6 +239,28 @@ template <> WBG_D cdf ld_c<cdf, float2>(float2 a) {
   r.y = df_from_f(a.y);
   return r;
 }
+// acc += a b and acc -= a b of the complex accumulators: plain FMAs for float / double; for
+// double-float lazily (df_lazy_fma: the error terms gathered in lo, renormalised once by cdone)
+template <typename V> WBG_D void cmac(V& acc, const V& a, const V& b) { cfma(acc, a, b); }
+template <typename V> WBG_D void cmsub(V& acc, const V& a, const V& b) { acc = csub(acc, cmul(a, b)); }
+template <typename V> WBG_D V cdone(V a) { return a; }
+template <> WBG_D void cmac<cdf>(cdf& acc, const cdf& a, const cdf& b) {
+  df_lazy_fma(acc.x, a.x, b.x);
+  df_lazy_fma(acc.x, -a.y, b.y);
+  df_lazy_fma(acc.y, a.x, b.y);
+  df_lazy_fma(acc.y, a.y, b.x);
+}
+template <> WBG_D void cmsub<cdf>(cdf& acc, const cdf& a, const cdf& b) {
+  df_lazy_fma(acc.x, -a.x, b.x);
+  df_lazy_fma(acc.x, a.y, b.y);
+  df_lazy_fma(acc.y, -a.x, b.y);
+  df_lazy_fma(acc.y, -a.y, b.x);
+}
+template <> WBG_D cdf cdone<cdf>(cdf a) {
+  a.x = df_lazy_done(a.x);
+  a.y = df_lazy_done(a.y);
+  return a;
+}
 WBG_D double to_dbl(float x) { return (double)x; }
 WBG_D double to_dbl(double x) { return x; }
 WBG_D double to_dbl(df64 x) { return df_to_double(x); }
@@ -1539,9 +1561,9 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const VS* __
               for (int b = 0; b < 3; ++b)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                  cfma(dDlm[3 * b + d], Vlp[b], Dpm[d]);
-                  dDml[3 * b + d] = csub(dDml[3 * b + d], cmul(Dmp[b], Vpl[d]));
-                  cfma(dAlm[3 * b + d], Alp[b], Dpm[d]);
+                  cmac(dDlm[3 * b + d], Vlp[b], Dpm[d]);
+                  cmsub(dDml[3 * b + d], Dmp[b], Vpl[d]);
+                  cmac(dAlm[3 * b + d], Alp[b], Dpm[d]);
                 }
             } else {
               // dD_lm: - D^b_lp V^d_pm ; dD_ml: + V^a_mp D^d_pl ; dA_lm: - D^d_lp A^b_pm
@@ -1557,11 +1579,17 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const VS* __
               for (int b = 0; b < 3; ++b)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                  dDlm[3 * b + d] = csub(dDlm[3 * b + d], cmul(Dlp[b], Vpm[d]));
-                  cfma(dDml[3 * b + d], Vmp[b], Dpl[d]);
-                  dAlm[3 * b + d] = csub(dAlm[3 * b + d], cmul(Dlp[d], Apm[b]));
+                  cmsub(dDlm[3 * b + d], Dlp[b], Vpm[d]);
+                  cmac(dDml[3 * b + d], Vmp[b], Dpl[d]);
+                  cmsub(dAlm[3 * b + d], Dlp[d], Apm[b]);
                 }
             }
+          }
+#pragma unroll
+          for (int i = 0; i < 9; ++i) {
+            dDlm[i] = cdone(dDlm[i]);
+            dDml[i] = cdone(dDml[i]);
+            dAlm[i] = cdone(dAlm[i]);
           }
           const T dml = dinv(m, l);  // 1/(E_m - E_l)
           // symmetrise in (b, d) (the bracket is symmetric, W = d_b d_d H too) and scale
@@ -1636,10 +1664,12 @@ __global__ void berry_deromega_kernel(const double* __restrict__ E, const VS* __
               for (int b = 0; b < 3; ++b)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                  dAn[3 * b + d] = csub(dAn[3 * b + d], cmul(Dnl[d], Alm[b]));
-                  cfma(dAn[3 * b + d], Anl[b], Dlm[d]);
+                  cmsub(dAn[3 * b + d], Dnl[d], Alm[b]);
+                  cmac(dAn[3 * b + d], Anl[b], Dlm[d]);
                 }
             }
+#pragma unroll
+            for (int i = 0; i < 9; ++i) dAn[i] = cdone(dAn[i]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const int al = (c + 1) % 3, be = (c + 2) % 3;
